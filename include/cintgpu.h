@@ -1,0 +1,174 @@
+/*
+ * libcintgpu -- GB300-native drop-in for libcint's two-electron Rys-quadrature integrals.
+ *
+ * Part 1 re-exports libcint's own C ABI for the hot path with identical signatures, argument
+ * meaning, return values and output layout, so a caller relinks against libcintgpu.so instead of
+ * libcint.so.  Each declaration cites the libcint interface it replaces.
+ *
+ * Part 2 is this library's batched device API (no libcint counterpart): a plan over a list of
+ * shell quartets (or triples) is built once on the host, its inputs stay resident in HBM, and
+ * every execution is a fixed sequence of kernel launches on a caller stream (capturable in a
+ * CUDA graph).  All entry points return 0 on success or a negative status and never abort;
+ * cintgpu_last_error() returns the calling thread's last message.
+ */
+#ifndef CINTGPU_H
+#define CINTGPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- libcint data model (libcint include/cint.h.in:10-24, 26-72, 139-152) ---------------- */
+#ifndef FINT
+#define FINT int
+#endif
+#ifndef CACHE_SIZE_T
+#define CACHE_SIZE_T FINT
+#endif
+#define PTR_EXPCUTOFF   0
+#define PTR_COMMON_ORIG 1
+#define PTR_RINV_ORIG   4
+#define PTR_RINV_ZETA   7
+#define PTR_RANGE_OMEGA 8
+#define PTR_ENV_START   20
+#define CHARGE_OF       0
+#define PTR_COORD       1
+#define NUC_MOD_OF      2
+#define PTR_ZETA        3
+#define ATM_SLOTS       6
+#define ATOM_OF         0
+#define ANG_OF          1
+#define NPRIM_OF        2
+#define NCTR_OF         3
+#define KAPPA_OF        4
+#define PTR_EXP         5
+#define PTR_COEFF       6
+#define BAS_SLOTS       8
+
+#if !defined HAVE_DEFINED_CINTOPT_H
+#define HAVE_DEFINED_CINTOPT_H
+typedef struct {
+    double rij[3];
+    double eij;
+    double cceij;
+} PairData;
+typedef struct {
+    FINT **index_xyz_array;
+    FINT **non0ctr;
+    FINT **sortedidx;
+    FINT nbas;
+    double **log_max_coeff;
+    PairData **pairdata;
+} CINTOpt;
+#endif
+
+/* ---- Part 1: libcint drop-in ------------------------------------------------------------- */
+/* (ij|kl), real spherical; libcint src/cint2e.c:1186-1194, include/cint_funcs.h:20-23 */
+CACHE_SIZE_T int2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                       FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+/* (ij|kl), Cartesian; libcint src/cint2e.c:1202-1210 */
+CACHE_SIZE_T int2e_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                        FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+/* optimizer; libcint src/cint2e.c:1195-1200 */
+void int2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
+/* (nabla i j|kl), 3 components; libcint src/autocode/grad2.c:69-88, include/cint_funcs.h:680-683 */
+CACHE_SIZE_T int2e_ip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                           FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+CACHE_SIZE_T int2e_ip1_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                            FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+void int2e_ip1_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
+/* (ij|k), real spherical / Cartesian; libcint src/cint3c2e.c:693-717 */
+CACHE_SIZE_T int3c2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                         FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+CACHE_SIZE_T int3c2e_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                          FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+void int3c2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
+/* libcint src/optimizer.c:40-72 */
+void CINTdel_2e_optimizer(CINTOpt **opt);
+void CINTdel_optimizer(CINTOpt **opt);
+
+/* CINT2 8-argument wrappers; libcint src/misc.h:34-60 (ALL_CINT) */
+FINT cint2e_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                double *env, CINTOpt *opt);
+FINT cint2e_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                 double *env, CINTOpt *opt);
+void cint2e_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
+void cint2e_cart_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
+FINT cint2e_ip1_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                    double *env, CINTOpt *opt);
+FINT cint2e_ip1_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                     double *env, CINTOpt *opt);
+void cint2e_ip1_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                              double *env);
+FINT cint3c2e_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                  double *env, CINTOpt *opt);
+FINT cint3c2e_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                   double *env, CINTOpt *opt);
+void cint3c2e_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                            double *env);
+
+/* basis helpers; libcint src/misc.c:86-93, src/cint_bas.c:25-147 */
+double CINTgto_norm(FINT n, double a);
+FINT CINTlen_cart(const FINT l);
+FINT CINTcgto_cart(const FINT bas_id, const FINT *bas);
+FINT CINTcgto_spheric(const FINT bas_id, const FINT *bas);
+FINT CINTtot_cgto_cart(const FINT *bas, const FINT nbas);
+FINT CINTtot_cgto_spheric(const FINT *bas, const FINT nbas);
+void CINTshells_cart_offset(FINT ao_loc[], const FINT *bas, const FINT nbas);
+void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas);
+
+/* ---- Part 2: batched device API (no libcint counterpart) -------------------------------- */
+#define CINTGPU_INT2E_SPH      1
+#define CINTGPU_INT2E_CART     2
+#define CINTGPU_INT2E_IP1_SPH  3
+#define CINTGPU_INT2E_IP1_CART 4
+#define CINTGPU_INT3C2E_SPH    5
+#define CINTGPU_INT3C2E_CART   6
+
+#define CINTGPU_OK              0
+#define CINTGPU_ERR_ARG        -1   /* invalid argument (shell index, l, nprim, omega != 0) */
+#define CINTGPU_ERR_CUDA       -2   /* a CUDA call failed */
+#define CINTGPU_ERR_UNSUPPORTED -3  /* class beyond the kernels' limits */
+#define CINTGPU_ERR_NOMEM      -4
+
+typedef struct CINTGPUPlan CINTGPUPlan;
+
+/* Build a plan for n items (4 shell indices each, 3 for int3c2e) of one integral kind.
+ * offsets[q] (may be NULL) is the element offset of item q's dense block in the output of one
+ * component; NULL packs the blocks back to back in item order.  The plan copies everything it
+ * needs; atm/bas/env may be freed afterwards. */
+int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
+                        const int64_t *offsets, const int *atm, int natm, const int *bas,
+                        int nbas, const double *env);
+/* doubles per component of the output (max offset + block), and the component count */
+int64_t cintgpu_plan_output_size(const CINTGPUPlan *plan);
+int cintgpu_plan_ncomp(const CINTGPUPlan *plan);
+/* FP64 flops of one execution by the algorithmic model (sum over surviving primitive quartets) */
+double cintgpu_plan_flops(const CINTGPUPlan *plan);
+int64_t cintgpu_plan_prim_quartets(const CINTGPUPlan *plan);
+/* Launch the plan on `stream` (a cudaStream_t; NULL = legacy default stream) writing
+ * out_dev[comp * output_size + offsets[q] + ...].  Asynchronous; enqueue only. */
+int cintgpu_plan_execute(CINTGPUPlan *plan, double *out_dev, void *stream);
+/* number of kernel launches one execution enqueues */
+int cintgpu_plan_launches(const CINTGPUPlan *plan);
+/* after execution completed: per item 1 if any primitive quartet survived screening */
+int cintgpu_plan_nonempty(const CINTGPUPlan *plan, int *flags_host);
+void cintgpu_plan_destroy(CINTGPUPlan *plan);
+
+/* one-shot host-buffer form: plan, H2D, execute, D2H into out_host (output_size*ncomp doubles) */
+int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,
+                       const int64_t *offsets, const int *atm, int natm, const int *bas,
+                       int nbas, const double *env);
+
+/* Rys nodes s = t^2 and weights from the device tables, for testing: xs, s, w device arrays */
+int cintgpu_rys_roots_dev(int nroots, const double *xs_dev, int count, double *s_dev,
+                          double *w_dev, void *stream);
+int cintgpu_rys_nmax(void);
+
+const char *cintgpu_last_error(void);
+int cintgpu_device_sm_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1010 @@
+/*
+ * Host side of libcintgpu: libcint's C ABI for the two-electron hot path plus the batched plan
+ * API (include/cintgpu.h).  Everything numerical runs in the CUDA kernels of rys_kernels.cu; this
+ * file only plans work:
+ *
+ *   shells      atm/bas/env are read exactly as libcint does (include/cint.h.in:26-72).  A shell
+ *               with nctr > 1 becomes nctr virtual shells, one per contraction column, whose
+ *               blocks land at the offsets libcint's c2s_sph_2e1 uses (src/cart2sph.c:5372-5377).
+ *   pairs       per ordered shell pair and primitive pair: a_A + a_B, its inverse, the product
+ *               centre, K = c_A c_B exp(-a_A a_B/(a_A+a_B) |AB|^2) and libcint's screening value
+ *               cce (CINTset_pairdata, src/optimizer.c:288-342, same formula and operation order).
+ *               A pair whose every primitive pair is screened makes the quartet empty, like
+ *               libcint's NOVALUE pairs (src/cint2e.c:281-285).
+ *   tasks       quartets are put in a canonical order (larger l first inside each pair, larger
+ *               pair first) for the int2e kinds, grouped by angular-momentum class, and split
+ *               into primitive-quartet slices when there are too few to fill the GPU.
+ *   execution   per class one launch of the warp-per-task kernel, then one launch of the output
+ *               kernel (sum of slices, cart->sph, strided store).
+ *
+ * Thread safety: the drop-in entry points keep one CUDA stream, device arena and pinned staging
+ * buffer per calling thread, so OpenMP callers may call them concurrently (libcint's contract,
+ * README.rst:39).  The device tables are initialised once under a mutex.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "cintgpu.h"
+#include "rys_kernels.h"
+
+namespace {
+
+thread_local std::string tl_error;
+
+void set_error(const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    tl_error = buf;
+}
+
+#define CUDA_OK(call)                                                                       \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) {                                                            \
+            set_error("%s failed: %s", #call, cudaGetErrorString(e_));                      \
+            return CINTGPU_ERR_CUDA;                                                        \
+        }                                                                                   \
+    } while (0)
+
+/* ------------------------------------------------------------------ cart -> sph rows */
+double fact(int n) { double f = 1; for (int i = 2; i <= n; i++) f *= i; return f; }
+double binom(int n, int k) { return (k < 0 || k > n) ? 0 : fact(n) / (fact(k) * fact(n - k)); }
+
+int cart_index(int l, int lx, int ly)   /* CINTcart_comp order, src/cint_bas.c:166-181 */
+{
+    int idx = 0;
+    for (int x = l; x > lx; x--) idx += l - x + 1;
+    return idx + (l - lx - ly);
+}
+
+/* Real solid harmonics r^l Y_lm (unit-sphere normalised, m = -l..l) as Cartesian monomials:
+ * closed form of the Racah-normalised S_lm (Schlegel & Frisch, IJQC 54 (1995) 83; the
+ * convention of libcint src/cart2sph.c:8-10) times sqrt((2l+1)/4pi).  l = 0, 1 are identities
+ * because libcint folds their factors into the common factor (src/g1e.c:565-572). */
+void c2s_rows(std::vector<int> &nnz, std::vector<int> &idx, std::vector<double> &val)
+{
+    const int rows = (CG_MAX_SHELL_L + 1) * (CG_MAX_SHELL_L + 1);
+    nnz.assign(rows, 0);
+    idx.assign(rows * CG_C2S_MAXNNZ, 0);
+    val.assign(rows * CG_C2S_MAXNNZ, 0.0);
+    for (int l = 2; l <= CG_MAX_SHELL_L; l++) {
+        int nc = (l + 1) * (l + 2) / 2;
+        std::vector<double> c((2 * l + 1) * nc, 0.0);
+        double unit = sqrt((2 * l + 1) / (4 * M_PI));
+        for (int m = -l; m <= l; m++) {
+            int am = abs(m);
+            double N = sqrt(2.0 * fact(l + am) * fact(l - am) / (m == 0 ? 2.0 : 1.0))
+                     / (pow(2.0, am) * fact(l));
+            for (int t = 0; t <= (l - am) / 2; t++)
+                for (int u = 0; u <= t; u++)
+                    for (int v2 = (m < 0 ? 1 : 0); v2 <= am; v2 += 2) {
+                        int vm2 = m < 0 ? 1 : 0;
+                        int sgn = t + (v2 - vm2) / 2;
+                        double C = ((sgn & 1) ? -1.0 : 1.0) * pow(0.25, t) * binom(l, t)
+                                 * binom(l - t, am + t) * binom(t, u) * binom(am, v2);
+                        int px = 2 * t + am - 2 * u - v2, py = 2 * u + v2, pz = l - 2 * t - am;
+                        if (px < 0 || py < 0 || pz < 0) continue;
+                        c[(m + l) * nc + cart_index(l, px, py)] += unit * N * C;
+                    }
+        }
+        for (int m = 0; m < 2 * l + 1; m++) {
+            int row = l * l + m, k = 0;
+            for (int p = 0; p < nc; p++) {
+                if (c[m * nc + p] != 0.0) {
+                    idx[row * CG_C2S_MAXNNZ + k] = p;
+                    val[row * CG_C2S_MAXNNZ + k] = c[m * nc + p];
+                    k++;
+                }
+            }
+            nnz[row] = k;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ device context */
+struct Global {
+    std::mutex mu;
+    bool ready = false;
+    int status = 0;
+    int device = -1;
+    int sm_count = 0;
+    double *rys_coef = nullptr;
+};
+Global g_ctx;
+
+int ensure_init()
+{
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    if (g_ctx.ready) return g_ctx.status;
+    g_ctx.ready = true;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        set_error("no CUDA device: %s", cudaGetErrorString(e));
+        g_ctx.status = CINTGPU_ERR_CUDA;
+        return g_ctx.status;
+    }
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, dev);
+    g_ctx.device = dev;
+    g_ctx.sm_count = prop.multiProcessorCount;
+    std::vector<int> nnz, idx;
+    std::vector<double> val;
+    c2s_rows(nnz, idx, val);
+    int rc = cg_kernels_init(nnz.data(), idx.data(), val.data(), &g_ctx.rys_coef);
+    if (rc) {
+        set_error("kernel table initialisation failed: %s", cudaGetErrorString((cudaError_t)rc));
+        g_ctx.status = CINTGPU_ERR_CUDA;
+    }
+    return g_ctx.status;
+}
+
+/* ------------------------------------------------------------------ shells and pairs */
+struct ShellView {
+    int l, nprim, nctr;
+    double R[3];
+    const double *ex, *cf;
+};
+
+int read_shell(int sh, const int *atm, int natm, const int *bas, const double *env, ShellView *s)
+{
+    if (sh < 0) { set_error("negative shell index %d", sh); return CINTGPU_ERR_ARG; }
+    const int *b = bas + BAS_SLOTS * sh;
+    s->l = b[ANG_OF];
+    s->nprim = b[NPRIM_OF];
+    s->nctr = b[NCTR_OF];
+    if (s->l < 0 || s->l > CG_MAX_SHELL_L) {
+        set_error("shell %d: angular momentum %d outside 0..%d", sh, s->l, CG_MAX_SHELL_L);
+        return CINTGPU_ERR_UNSUPPORTED;
+    }
+    if (s->nprim < 1 || s->nprim > 64 || s->nctr < 1 || s->nctr > 64) {
+        set_error("shell %d: nprim %d / nctr %d outside 1..64", sh, s->nprim, s->nctr);
+        return CINTGPU_ERR_ARG;
+    }
+    int at = b[ATOM_OF];
+    if (at < 0 || at >= natm) { set_error("shell %d: atom %d outside 0..%d", sh, at, natm - 1); return CINTGPU_ERR_ARG; }
+    const double *r = env + atm[ATM_SLOTS * at + PTR_COORD];
+    s->R[0] = r[0]; s->R[1] = r[1]; s->R[2] = r[2];
+    s->ex = env + b[PTR_EXP];
+    s->cf = env + b[PTR_COEFF];
+    return 0;
+}
+
+int ncart_l(int l) { return (l + 1) * (l + 2) / 2; }
+int nsph_l(int l) { return 2 * l + 1; }
+
+double common_fac_sp(int l)    /* src/g1e.c:565-572 */
+{
+    return l == 0 ? 0.282094791773878143 : l == 1 ? 0.488602511902919921 : 1.0;
+}
+
+struct PairKey {
+    int a, ca, b, cb, lsum, kind;
+    bool operator==(const PairKey &o) const
+    {
+        return a == o.a && ca == o.ca && b == o.b && cb == o.cb && lsum == o.lsum && kind == o.kind;
+    }
+};
+struct PairKeyHash {
+    size_t operator()(const PairKey &k) const
+    {
+        uint64_t h = (uint64_t)k.a * 1000003u ^ ((uint64_t)k.b << 21) ^ ((uint64_t)k.ca << 42)
+                   ^ ((uint64_t)k.cb << 50) ^ ((uint64_t)k.lsum << 58) ^ ((uint64_t)k.kind << 62);
+        return std::hash<uint64_t>()(h);
+    }
+};
+
+}  // namespace
+
+/* ------------------------------------------------------------------ plan */
+struct ClassLaunch {
+    int l[4];
+    int task0, ntasks;
+    int ws;
+    int blocks_per_sm;
+    double common;
+};
+
+struct CINTGPUPlan {
+    int kind = 0;
+    int mode = CG_MODE_ERI;
+    int ncomp = 1;
+    int sph = 1;
+    int three = 0;
+    double expcutoff = 60;
+    int64_t nitems = 0;
+    int64_t out_size = 0;          /* doubles per component */
+    double flops = 0;
+    int64_t prim_quartets = 0;
+    int max_nf = 1;
+    /* host images */
+    std::vector<CGPair> pairs;
+    std::vector<CGPrimPair> prims;
+    std::vector<CGTask> tasks;
+    std::vector<CGOutTask> outs;
+    std::vector<int> out_item;     /* item index of each CGOutTask */
+    std::vector<ClassLaunch> classes;
+    int64_t gctr_size = 0;
+    /* device */
+    char *dbuf = nullptr;
+    size_t dbuf_size = 0;
+    bool owns_dbuf = true;
+    CGPair *d_pairs = nullptr;
+    CGPrimPair *d_prims = nullptr;
+    CGTask *d_tasks = nullptr;
+    CGOutTask *d_outs = nullptr;
+    double *d_gctr = nullptr;
+    int *d_counters = nullptr;
+    int *d_nonempty = nullptr;
+    double *d_scratch = nullptr;
+    int out_blocks = 1;
+    int64_t scratch_per_warp = 0;
+};
+
+namespace {
+
+struct Builder {
+    CINTGPUPlan *P;
+    const int *atm;
+    int natm;
+    const int *bas;
+    const double *env;
+    std::unordered_map<PairKey, int, PairKeyHash> pair_index;
+    std::vector<char> pair_empty;
+    std::unordered_map<int, std::vector<double>> logmaxc;   /* per original shell */
+
+    const std::vector<double> &log_maxc(int sh, const ShellView &s)
+    {
+        auto it = logmaxc.find(sh);
+        if (it != logmaxc.end()) return it->second;
+        std::vector<double> v(s.nprim);
+        for (int ip = 0; ip < s.nprim; ip++) {     /* CINTOpt_log_max_pgto_coeff, :248-259 */
+            double m = 0;
+            for (int c = 0; c < s.nctr; c++) m = std::max(m, fabs(s.cf[c * s.nprim + ip]));
+            v[ip] = log(m);
+        }
+        return logmaxc.emplace(sh, std::move(v)).first->second;
+    }
+
+    /* ordered pair (A col ca, B col cb); lsum = l ceilings entering libcint's log_rr */
+    int pair(int sa, const ShellView &A, int ca, int sb, const ShellView &B, int cb, int lsum)
+    {
+        PairKey key{sa, ca, sb, cb, lsum, 0};
+        auto it = pair_index.find(key);
+        if (it != pair_index.end()) return it->second;
+        CGPair p;
+        for (int c = 0; c < 3; c++) { p.AB[c] = A.R[c] - B.R[c]; p.A[c] = A.R[c]; }
+        p.prim_off = (int)P->prims.size();
+        p.npa = A.nprim; p.npb = B.nprim; p.la = A.l; p.lb = B.l; p.pad = 0;
+        double rr = p.AB[0] * p.AB[0] + p.AB[1] * p.AB[1] + p.AB[2] * p.AB[2];
+        /* CINTset_pairdata, src/optimizer.c:288-342 */
+        double aij_last = A.ex[A.nprim - 1] + B.ex[B.nprim - 1];
+        double log_rr = 1.7 - 1.5 * log(aij_last);
+        if (lsum > 0) log_rr += lsum * log(sqrt(rr) + 1.);
+        const std::vector<double> &lca = log_maxc(sa, A);
+        const std::vector<double> &lcb = log_maxc(sb, B);
+        bool empty = true;
+        for (int jp = 0; jp < B.nprim; jp++)
+            for (int ip = 0; ip < A.nprim; ip++) {
+                CGPrimPair q;
+                double ai = A.ex[ip], aj = B.ex[jp];
+                double inv = 1 / (ai + aj);
+                double eij = rr * ai * aj * inv;
+                double cce = eij - log_rr - lca[ip] - lcb[jp];
+                q.a = ai + aj;
+                q.inv_a = 1.0 / q.a;
+                q.cce = cce;
+                q.aA = ai;
+                if (cce < P->expcutoff) {
+                    empty = false;
+                    double wj = aj * inv;
+                    for (int c = 0; c < 3; c++) q.P[c] = A.R[c] + wj * (B.R[c] - A.R[c]);
+                    q.K = A.cf[ca * A.nprim + ip] * B.cf[cb * B.nprim + jp] * exp(-eij);
+                } else {
+                    /* libcint keeps eij = 0 for such pairs; they contribute exactly zero */
+                    for (int c = 0; c < 3; c++) q.P[c] = A.R[c];
+                    q.K = 0.0;
+                }
+                P->prims.push_back(q);
+            }
+        int id = (int)P->pairs.size();
+        P->pairs.push_back(p);
+        pair_empty.push_back(empty ? 1 : 0);
+        pair_index.emplace(key, id);
+        return id;
+    }
+
+    /* the ket of int3c2e: shell k with a zero-exponent s partner; no ket screening */
+    int single(int sk, const ShellView &K, int ck)
+    {
+        PairKey key{sk, ck, -1, 0, 0, 1};
+        auto it = pair_index.find(key);
+        if (it != pair_index.end()) return it->second;
+        CGPair p;
+        for (int c = 0; c < 3; c++) { p.AB[c] = 0.0; p.A[c] = K.R[c]; }
+        p.prim_off = (int)P->prims.size();
+        p.npa = K.nprim; p.npb = 1; p.la = K.l; p.lb = 0; p.pad = 0;
+        for (int kp = 0; kp < K.nprim; kp++) {
+            CGPrimPair q;
+            q.a = K.ex[kp];
+            q.inv_a = 1.0 / q.a;
+            for (int c = 0; c < 3; c++) q.P[c] = K.R[c];
+            q.K = K.cf[ck * K.nprim + kp];
+            q.cce = 0.0;
+            q.aA = K.ex[kp];
+            P->prims.push_back(q);
+        }
+        int id = (int)P->pairs.size();
+        P->pairs.push_back(p);
+        pair_empty.push_back(0);
+        pair_index.emplace(key, id);
+        return id;
+    }
+};
+
+/* algorithmic FP64 flop model per surviving primitive quartet (FMA = 2) */
+double flops_per_primq(int li, int lj, int lk, int ll, int mode)
+{
+    CGLayout L;
+    cg_layout(li, lj, lk, ll, mode, CG_WS_MAX, &L);
+    int n = L.nroots;
+    double hrr = 0;
+    for (int j = 1; j < L.dJ; j++) hrr += (L.nmax - j + 1) * (L.mmax + 1);
+    for (int l = 1; l < L.dL; l++) hrr += L.dI * L.dJ * (L.mmax - l + 1);
+    double vrr = (double)(L.nmax + 1) * (L.mmax + 1);
+    double per_root = 20 + 3 * 5 * vrr + 3 * 2 * hrr;
+    if (mode == CG_MODE_IP1) per_root += 3 * 3 * (double)L.G / L.dI * (L.dI - 1) + 9.0 * L.nf;
+    else per_root += 3.0 * L.nf;
+    return n * per_root;
+}
+
+}  // namespace
+
+static void free_plan_device(CINTGPUPlan *p)
+{
+    if (p->owns_dbuf && p->dbuf) cudaFree(p->dbuf);
+    p->dbuf = nullptr;
+}
+
+/* Build the host images. split_target: minimum number of compute tasks wanted (0 = no split). */
+static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, const int64_t *offsets,
+                      const int *atm, int natm, const int *bas, int nbas, const double *env,
+                      int64_t split_target)
+{
+    (void)nbas;
+    P->kind = kind;
+    switch (kind) {
+    case CINTGPU_INT2E_SPH: P->mode = CG_MODE_ERI; P->sph = 1; P->three = 0; break;
+    case CINTGPU_INT2E_CART: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; break;
+    case CINTGPU_INT2E_IP1_SPH: P->mode = CG_MODE_IP1; P->sph = 1; P->three = 0; break;
+    case CINTGPU_INT2E_IP1_CART: P->mode = CG_MODE_IP1; P->sph = 0; P->three = 0; break;
+    case CINTGPU_INT3C2E_SPH: P->mode = CG_MODE_ERI; P->sph = 1; P->three = 1; break;
+    case CINTGPU_INT3C2E_CART: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 1; break;
+    default: set_error("unknown integral kind %d", kind); return CINTGPU_ERR_ARG;
+    }
+    P->ncomp = P->mode == CG_MODE_IP1 ? 3 : 1;
+    if (env[PTR_RANGE_OMEGA] != 0.0) {
+        set_error("range-separated Coulomb (env[PTR_RANGE_OMEGA] = %g) is not supported", env[PTR_RANGE_OMEGA]);
+        return CINTGPU_ERR_UNSUPPORTED;
+    }
+    /* src/g2e.c:57-62 (+1) and src/g3c2e.c:55-59 (no +1) */
+    if (env[PTR_EXPCUTOFF] == 0) P->expcutoff = 60;
+    else P->expcutoff = std::max(40.0, env[PTR_EXPCUTOFF]) + (P->three ? 0 : 1);
+    P->nitems = n;
+    Builder B{P, atm, natm, bas, env, {}, {}, {}};
+    const int nsh = P->three ? 3 : 4;
+    const int dinc = P->mode == CG_MODE_IP1 ? 1 : 0;
+
+    struct Pending { int pij, pkl, out; int64_t npq; int l[4]; };
+    std::vector<Pending> pend;
+    int64_t next_off = 0;
+    for (int64_t q = 0; q < n; q++) {
+        const int *s = shls + nsh * q;
+        ShellView sv[4];
+        for (int a = 0; a < nsh; a++) {
+            int rc = read_shell(s[a], atm, natm, bas, env, &sv[a]);
+            if (rc) return rc;
+        }
+        if (P->three) { sv[3] = sv[2]; sv[3].l = 0; sv[3].nprim = 1; sv[3].nctr = 1; }
+        int d[4], nd[4];
+        for (int a = 0; a < 4; a++) {
+            d[a] = (a == 3 && P->three) ? 1 : (P->sph ? nsph_l(sv[a].l) : ncart_l(sv[a].l));
+            nd[a] = d[a] * ((a == 3 && P->three) ? 1 : sv[a].nctr);
+        }
+        int64_t req_st[4] = {1, nd[0], (int64_t)nd[0] * nd[1], (int64_t)nd[0] * nd[1] * nd[2]};
+        if (P->three) req_st[3] = 0;
+        int64_t block = (int64_t)nd[0] * nd[1] * nd[2] * nd[3];
+        int64_t base = offsets ? offsets[q] : next_off;
+        next_off = std::max(next_off, base + block);
+        /* kernel order: perm[k] = request index placed at kernel slot k */
+        int perm[4] = {0, 1, 2, 3};
+        if (P->mode == CG_MODE_ERI) {
+            if (sv[0].l < sv[1].l) std::swap(perm[0], perm[1]);
+            if (!P->three) {
+                if (sv[2].l < sv[3].l) std::swap(perm[2], perm[3]);
+                int lij = sv[perm[0]].l * 16 + sv[perm[1]].l, lkl = sv[perm[2]].l * 16 + sv[perm[3]].l;
+                if (lij < lkl) { std::swap(perm[0], perm[2]); std::swap(perm[1], perm[3]); }
+            }
+        }
+        const ShellView *kv[4] = {&sv[perm[0]], &sv[perm[1]], &sv[perm[2]], &sv[perm[3]]};
+        int ksh[4];
+        for (int k = 0; k < 4; k++) ksh[k] = (P->three && k == 3) ? -1 : s[perm[k]];
+        int kl_[4] = {kv[0]->l, kv[1]->l, kv[2]->l, kv[3]->l};
+        int nct[4] = {kv[0]->nctr, kv[1]->nctr, kv[2]->nctr, P->three ? 1 : kv[3]->nctr};
+        for (int c3 = 0; c3 < nct[3]; c3++)
+        for (int c2 = 0; c2 < nct[2]; c2++)
+        for (int c1 = 0; c1 < nct[1]; c1++)
+        for (int c0 = 0; c0 < nct[0]; c0++) {
+            int cc[4] = {c0, c1, c2, c3};
+            int pij = B.pair(ksh[0], *kv[0], c0, ksh[1], *kv[1], c1, kl_[0] + dinc + kl_[1]);
+            int pkl = P->three ? B.single(ksh[2], *kv[2], c2)
+                               : B.pair(ksh[2], *kv[2], c2, ksh[3], *kv[3], c3, kl_[2] + kl_[3]);
+            CGOutTask o;
+            memset(&o, 0, sizeof(o));
+            o.out_off = base;
+            for (int k = 0; k < 4; k++) {
+                o.l[k] = kl_[k];
+                o.st[k] = (int)req_st[perm[k]];
+                o.out_off += (int64_t)cc[k] * d[perm[k]] * req_st[perm[k]];
+            }
+            o.flags = P->sph ? 1 : 0;
+            o.nparts = 0;
+            int out_id = (int)P->outs.size();
+            P->outs.push_back(o);
+            P->out_item.push_back((int)q);
+            int nf = ncart_l(kl_[0]) * ncart_l(kl_[1]) * ncart_l(kl_[2]) * ncart_l(kl_[3]);
+            P->max_nf = std::max(P->max_nf, nf);
+            if (B.pair_empty[pij] || B.pair_empty[pkl]) continue;
+            const CGPair &a = P->pairs[pij], &b = P->pairs[pkl];
+            Pending pe{pij, pkl, out_id, (int64_t)a.npa * a.npb * b.npa * b.npb,
+                       {kl_[0], kl_[1], kl_[2], kl_[3]}};
+            pend.push_back(pe);
+        }
+    }
+    P->out_size = next_off;
+    /* surviving primitive quartets and the flop model (host copy of the kernel's screening) */
+    {
+        double fl = 0;
+        int64_t npq_alive = 0;
+        for (const Pending &pe : pend) {
+            const CGPair &a = P->pairs[pe.pij], &b = P->pairs[pe.pkl];
+            const CGPrimPair *pa = &P->prims[a.prim_off], *pb = &P->prims[b.prim_off];
+            int nij = a.npa * a.npb, nkl = b.npa * b.npb;
+            int64_t alive = 0;
+            for (int kl = 0; kl < nkl; kl++) {
+                double ck = pb[kl].cce;
+                if (ck > P->expcutoff) continue;
+                for (int ij = 0; ij < nij; ij++)
+                    if (!(pa[ij].cce > P->expcutoff - ck)) alive++;
+            }
+            npq_alive += alive;
+            fl += alive * flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode);
+        }
+        P->flops = fl;
+        P->prim_quartets = npq_alive;
+    }
+    /* split big quartets into primitive-quartet slices if there are too few tasks */
+    int64_t chunk = 0;
+    if (split_target > 0 && (int64_t)pend.size() < split_target) {
+        int64_t tot = 0;
+        for (const Pending &pe : pend) tot += pe.npq;
+        chunk = std::max<int64_t>(32, ((tot / std::max<int64_t>(split_target, 1)) + 31) / 32 * 32);
+    }
+    /* group by class, most expensive classes first */
+    std::vector<int> order(pend.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+    auto ckey = [&](const Pending &p) { return ((p.l[0] * 16 + p.l[1]) * 16 + p.l[2]) * 16 + p.l[3]; };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        int kx = ckey(pend[x]), ky = ckey(pend[y]);
+        if (kx != ky) return kx > ky;
+        return pend[x].npq > pend[y].npq;
+    });
+    int64_t gpos = 0;
+    int cur_key = -1;
+    for (int idx : order) {
+        const Pending &pe = pend[idx];
+        int key = ckey(pe);
+        if (key != cur_key) {
+            ClassLaunch cl;
+            for (int k = 0; k < 4; k++) cl.l[k] = pe.l[k];
+            cl.task0 = (int)P->tasks.size();
+            cl.ntasks = 0;
+            CGLayout L;
+            cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_SMALL, &L);
+            cl.ws = CG_WS_SMALL; cl.blocks_per_sm = 2;
+            if (L.T < 4) {
+                cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_MAX, &L);
+                cl.ws = CG_WS_MAX; cl.blocks_per_sm = 1;
+            }
+            if (L.nroots > cg_rys_nmax() || L.T < 1 || std::max(L.nmax, L.mmax) > 2 * CG_MAXL) {
+                set_error("class (%d %d|%d %d) beyond the kernel limits (nroots %d, max %d)",
+                          pe.l[0], pe.l[1], pe.l[2], pe.l[3], L.nroots, cg_rys_nmax());
+                return CINTGPU_ERR_UNSUPPORTED;
+            }
+            cl.common = M_PI * M_PI * M_PI * 2 / 1.7724538509055160272981674833411451
+                      * common_fac_sp(pe.l[0]) * common_fac_sp(pe.l[1]) * common_fac_sp(pe.l[2])
+                      * (P->three ? 1.0 : common_fac_sp(pe.l[3]));
+            P->classes.push_back(cl);
+            cur_key = key;
+        }
+        int nf = ncart_l(pe.l[0]) * ncart_l(pe.l[1]) * ncart_l(pe.l[2]) * ncart_l(pe.l[3]);
+        int64_t slot = (int64_t)nf * P->ncomp;
+        int64_t c = chunk > 0 ? chunk : pe.npq;
+        CGOutTask &o = P->outs[pe.out];
+        o.cart_off = gpos;
+        for (int64_t a = 0; a < pe.npq; a += c) {
+            CGTask t;
+            t.pij = pe.pij; t.pkl = pe.pkl;
+            t.pq0 = (int)a; t.pq1 = (int)std::min<int64_t>(pe.npq, a + c);
+            t.cart_off = gpos;
+            t.out = pe.out;
+            t.pad = 0;
+            P->tasks.push_back(t);
+            P->classes.back().ntasks++;
+            o.nparts++;
+            gpos += slot;
+        }
+    }
+    P->gctr_size = std::max<int64_t>(gpos, 1);
+    return 0;
+}
+
+static int upload_plan(CINTGPUPlan *P, char *arena, size_t arena_size, cudaStream_t stream,
+                       bool async_from_pinned, char *pinned)
+{
+    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+    int sm = g_ctx.sm_count;
+    P->out_blocks = std::max(1, std::min<int>((int)((P->outs.size() + 3) / 4), sm * 8));
+    P->scratch_per_warp = 2 * (int64_t)P->max_nf;
+    size_t sz_pairs = al(sizeof(CGPair) * std::max<size_t>(P->pairs.size(), 1));
+    size_t sz_prims = al(sizeof(CGPrimPair) * std::max<size_t>(P->prims.size(), 1));
+    size_t sz_tasks = al(sizeof(CGTask) * std::max<size_t>(P->tasks.size(), 1));
+    size_t sz_outs = al(sizeof(CGOutTask) * std::max<size_t>(P->outs.size(), 1));
+    size_t sz_gctr = al(sizeof(double) * P->gctr_size);
+    size_t sz_cnt = al(sizeof(int) * std::max<size_t>(P->classes.size(), 1));
+    size_t sz_ne = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
+    size_t sz_scr = al(sizeof(double) * P->scratch_per_warp * P->out_blocks * 4);
+    size_t upload = sz_pairs + sz_prims + sz_tasks + sz_outs;
+    size_t total = upload + sz_gctr + sz_cnt + sz_ne + sz_scr;
+    if (arena) {
+        if (total > arena_size) { set_error("arena too small"); return CINTGPU_ERR_NOMEM; }
+        P->dbuf = arena; P->dbuf_size = arena_size; P->owns_dbuf = false;
+    } else {
+        cudaError_t e = cudaMalloc(&P->dbuf, total);
+        if (e != cudaSuccess) {
+            set_error("cudaMalloc(%zu) failed: %s", total, cudaGetErrorString(e));
+            P->dbuf = nullptr;
+            return CINTGPU_ERR_NOMEM;
+        }
+        P->dbuf_size = total; P->owns_dbuf = true;
+    }
+    char *p = P->dbuf;
+    P->d_pairs = (CGPair *)p; p += sz_pairs;
+    P->d_prims = (CGPrimPair *)p; p += sz_prims;
+    P->d_tasks = (CGTask *)p; p += sz_tasks;
+    P->d_outs = (CGOutTask *)p; p += sz_outs;
+    P->d_gctr = (double *)p; p += sz_gctr;
+    P->d_counters = (int *)p; p += sz_cnt;
+    P->d_nonempty = (int *)p; p += sz_ne;
+    P->d_scratch = (double *)p; p += sz_scr;
+    /* stage the four host images contiguously, then one copy */
+    std::vector<char> tmp;
+    char *src;
+    if (async_from_pinned) src = pinned;
+    else { tmp.resize(upload); src = tmp.data(); }
+    char *q = src;
+    memcpy(q, P->pairs.data(), sizeof(CGPair) * P->pairs.size()); q += sz_pairs;
+    memcpy(q, P->prims.data(), sizeof(CGPrimPair) * P->prims.size()); q += sz_prims;
+    memcpy(q, P->tasks.data(), sizeof(CGTask) * P->tasks.size()); q += sz_tasks;
+    memcpy(q, P->outs.data(), sizeof(CGOutTask) * P->outs.size()); q += sz_outs;
+    if (async_from_pinned) {
+        CUDA_OK(cudaMemcpyAsync(P->dbuf, src, upload, cudaMemcpyHostToDevice, stream));
+    } else {
+        CUDA_OK(cudaMemcpy(P->dbuf, src, upload, cudaMemcpyHostToDevice));
+    }
+    return 0;
+}
+
+static size_t plan_device_bytes(const CINTGPUPlan *P)
+{
+    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+    int sm = g_ctx.sm_count;
+    int ob = std::max(1, std::min<int>((int)((P->outs.size() + 3) / 4), sm * 8));
+    return al(sizeof(CGPair) * std::max<size_t>(P->pairs.size(), 1))
+         + al(sizeof(CGPrimPair) * std::max<size_t>(P->prims.size(), 1))
+         + al(sizeof(CGTask) * std::max<size_t>(P->tasks.size(), 1))
+         + al(sizeof(CGOutTask) * std::max<size_t>(P->outs.size(), 1))
+         + al(sizeof(double) * P->gctr_size)
+         + al(sizeof(int) * std::max<size_t>(P->classes.size(), 1))
+         + al(sizeof(int) * std::max<size_t>(P->outs.size(), 1))
+         + al(sizeof(double) * 2 * (int64_t)P->max_nf * ob * 4);
+}
+
+static size_t plan_upload_bytes(const CINTGPUPlan *P)
+{
+    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+    return al(sizeof(CGPair) * std::max<size_t>(P->pairs.size(), 1))
+         + al(sizeof(CGPrimPair) * std::max<size_t>(P->prims.size(), 1))
+         + al(sizeof(CGTask) * std::max<size_t>(P->tasks.size(), 1))
+         + al(sizeof(CGOutTask) * std::max<size_t>(P->outs.size(), 1));
+}
+
+static int execute_plan(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
+{
+    CUDA_OK(cudaMemsetAsync(P->d_nonempty, 0, sizeof(int) * std::max<size_t>(P->outs.size(), 1), stream));
+    CUDA_OK(cudaMemsetAsync(P->d_counters, 0, sizeof(int) * std::max<size_t>(P->classes.size(), 1), stream));
+    int sm = g_ctx.sm_count;
+    for (size_t c = 0; c < P->classes.size(); c++) {
+        const ClassLaunch &cl = P->classes[c];
+        CGLaunch L;
+        L.tasks = P->d_tasks;
+        L.task0 = cl.task0;
+        L.ntasks = cl.ntasks;
+        L.pairs = P->d_pairs;
+        L.prims = P->d_prims;
+        L.gctr = P->d_gctr;
+        L.counter = P->d_counters + c;
+        L.nonempty = P->d_nonempty;
+        L.rys_coef = g_ctx.rys_coef;
+        L.common = cl.common;
+        L.expcutoff = P->expcutoff;
+        L.li = cl.l[0]; L.lj = cl.l[1]; L.lk = cl.l[2]; L.ll = cl.l[3];
+        L.ws_doubles = cl.ws;
+        int warps_needed = cl.ntasks;
+        int nblocks = std::min(sm * cl.blocks_per_sm, std::max(1, (warps_needed + 3) / 4));
+        int rc = cg_launch_eri(&L, P->mode, nblocks, stream);
+        if (rc) { set_error("ERI kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
+    }
+    int rc = cg_launch_output(P->d_outs, (int)P->outs.size(), P->d_gctr, P->d_nonempty, P->d_scratch,
+                              P->scratch_per_warp, P->out_blocks, out_dev, P->ncomp, P->out_size, stream);
+    if (rc) { set_error("output kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ per-thread drop-in state */
+namespace {
+struct ThreadCtx {
+    cudaStream_t stream = nullptr;
+    char *arena = nullptr;
+    size_t arena_size = 0;
+    double *dout = nullptr;
+    size_t dout_size = 0;
+    char *pinned = nullptr;
+    size_t pinned_size = 0;
+    double *hout = nullptr;
+    size_t hout_size = 0;
+    ~ThreadCtx()
+    {
+        /* process teardown may already have destroyed the context; ignore errors */
+        if (arena) cudaFree(arena);
+        if (dout) cudaFree(dout);
+        if (pinned) cudaFreeHost(pinned);
+        if (hout) cudaFreeHost(hout);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+thread_local ThreadCtx tl_ctx;
+
+int grow_dev(char **p, size_t *cap, size_t need)
+{
+    if (need <= *cap) return 0;
+    if (*p) cudaFree(*p);
+    size_t n = std::max(need, *cap * 2);
+    if (cudaMalloc(p, n) != cudaSuccess) { *p = nullptr; *cap = 0; set_error("cudaMalloc(%zu) failed", n); return CINTGPU_ERR_NOMEM; }
+    *cap = n;
+    return 0;
+}
+int grow_host(char **p, size_t *cap, size_t need)
+{
+    if (need <= *cap) return 0;
+    if (*p) cudaFreeHost(*p);
+    size_t n = std::max(need, *cap * 2);
+    if (cudaMallocHost(p, n) != cudaSuccess) { *p = nullptr; *cap = 0; set_error("cudaMallocHost(%zu) failed", n); return CINTGPU_ERR_NOMEM; }
+    *cap = n;
+    return 0;
+}
+
+/* libcint cache-size formula of CINT2e_drv / CINT3c2e_drv (src/cint2e.c:779-816,
+ * src/cint3c2e.c:545-567) so out == NULL queries return the same number. */
+CACHE_SIZE_T cache_size_query(int kind, const int *shls, const int *bas)
+{
+    int three = kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART;
+    int ip1 = kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT2E_IP1_CART;
+    int nsh = three ? 3 : 4;
+    int l[4] = {0, 0, 0, 0}, np[4] = {1, 1, 1, 1}, nc[4] = {1, 1, 1, 1};
+    for (int a = 0; a < nsh; a++) {
+        const int *b = bas + BAS_SLOTS * shls[a];
+        l[a] = b[ANG_OF]; np[a] = b[NPRIM_OF]; nc[a] = b[NCTR_OF];
+    }
+    int ncomp = ip1 ? 3 : 1, gbits = ip1 ? 1 : 0;
+    int lic = l[0] + (ip1 ? 1 : 0), ljc = l[1], lkc = l[2], llc = l[3];
+    size_t nf = (size_t)ncart_l(l[0]) * ncart_l(l[1]) * ncart_l(l[2]) * (three ? 1 : ncart_l(l[3]));
+    size_t ncx = nf * nc[0] * nc[1] * nc[2] * (three ? 1 : nc[3]);
+    size_t gsize;
+    int nroots;
+    if (three) {
+        /* CINTinit_int3c2e_EnvVars: lk_ceil = 0, ll_ceil = k_l */
+        nroots = (lic + ljc + l[2]) / 2 + 1;
+        int dli, dlj;
+        if (lic > ljc) { dli = lic + ljc + 1; dlj = ljc + 1; } else { dli = lic + 1; dlj = lic + ljc + 1; }
+        gsize = (size_t)nroots * dli * (l[2] + 1) * dlj;
+        size_t leng = gsize * 3 * ((1 << gbits) + 1);
+        size_t len0 = nf * ncomp;
+        size_t ps = (size_t)np[0] * np[1] * 5 + np[0] * nc[0] + np[1] * nc[1] + np[2] * nc[2]
+                  + (np[0] + np[1]) * 2 + np[2] + nf * 3 + 16;
+        return (CACHE_SIZE_T)std::max(leng + len0 + ncx * ncomp * 3 + ps, ncx * ncomp + nf * 3);
+    }
+    nroots = (lic + ljc + lkc + llc) / 2 + 1;
+    int dli, dlj, dlk, dll;
+    if (lkc > llc) { dlk = lkc + llc + 1; dll = llc + 1; } else { dlk = lkc + 1; dll = lkc + llc + 1; }
+    if (lic > ljc) { dli = lic + ljc + 1; dlj = ljc + 1; } else { dli = lic + 1; dlj = lic + ljc + 1; }
+    gsize = (size_t)nroots * dli * dlk * dll * dlj;
+    size_t leng = gsize * 3 * ((1 << gbits) + 1);
+    size_t len0 = nf * ncomp;
+    size_t ps = ((size_t)np[0] * np[1] + (size_t)np[2] * np[3]) * 5 + np[0] * nc[0] + np[1] * nc[1]
+              + np[2] * nc[2] + np[3] * nc[3] + (np[0] + np[1] + np[2] + np[3]) * 2 + nf * 3;
+    return (CACHE_SIZE_T)std::max(leng + len0 + ncx * ncomp * 3 + ps, ncx * ncomp + nf * 4);
+}
+
+/* One shell block through the GPU (the plain drop-in path). */
+CACHE_SIZE_T dropin(int kind, double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                    FINT *bas, FINT nbas, double *env)
+{
+    if (out == NULL) return cache_size_query(kind, shls, bas);
+    int three = kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART;
+    int nsh = three ? 3 : 4;
+    int ncomp = (kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT2E_IP1_CART) ? 3 : 1;
+    int sph = kind == CINTGPU_INT2E_SPH || kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT3C2E_SPH;
+    int counts[4] = {1, 1, 1, 1};
+    for (int a = 0; a < nsh; a++) {
+        const int *b = bas + BAS_SLOTS * shls[a];
+        int l = b[ANG_OF];
+        counts[a] = (sph ? nsph_l(l) : ncart_l(l)) * b[NCTR_OF];
+    }
+    int *d = dims ? dims : counts;
+    int64_t nout = (int64_t)d[0] * d[1] * d[2] * (three ? 1 : d[3]);
+    auto zero_fill = [&]() {
+        for (int comp = 0; comp < ncomp; comp++)
+            for (int l = 0; l < counts[3]; l++)
+                for (int k = 0; k < counts[2]; k++)
+                    for (int j = 0; j < counts[1]; j++)
+                        for (int i = 0; i < counts[0]; i++)
+                            out[comp * nout + i + (int64_t)d[0] * (j + (int64_t)d[1] * (k + (int64_t)d[2] * l))] = 0;
+    };
+    if (ensure_init()) { zero_fill(); return 0; }
+    ThreadCtx &T = tl_ctx;
+    if (!T.stream && cudaStreamCreateWithFlags(&T.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("cudaStreamCreate failed");
+        zero_fill();
+        return 0;
+    }
+    CINTGPUPlan P;
+    int rc = build_plan(&P, kind, shls, 1, NULL, atm, natm, bas, nbas, env,
+                        (int64_t)g_ctx.sm_count * 8);
+    if (rc) { zero_fill(); return 0; }
+    size_t need = plan_device_bytes(&P);
+    size_t up = plan_upload_bytes(&P);
+    size_t outb = sizeof(double) * P.out_size * ncomp;
+    if (grow_dev(&T.arena, &T.arena_size, need) || grow_dev((char **)&T.dout, &T.dout_size, outb)
+        || grow_host(&T.pinned, &T.pinned_size, up + sizeof(int) * P.outs.size())
+        || grow_host((char **)&T.hout, &T.hout_size, outb)) {
+        zero_fill();
+        return 0;
+    }
+    rc = upload_plan(&P, T.arena, T.arena_size, T.stream, true, T.pinned);
+    if (!rc) rc = execute_plan(&P, T.dout, T.stream);
+    int *ne_host = (int *)(T.pinned + up);
+    if (!rc && cudaMemcpyAsync(T.hout, T.dout, outb, cudaMemcpyDeviceToHost, T.stream) != cudaSuccess) rc = -1;
+    if (!rc && cudaMemcpyAsync(ne_host, P.d_nonempty, sizeof(int) * P.outs.size(), cudaMemcpyDeviceToHost, T.stream) != cudaSuccess) rc = -1;
+    if (!rc && cudaStreamSynchronize(T.stream) != cudaSuccess) { set_error("kernel execution failed: %s", cudaGetErrorString(cudaGetLastError())); rc = -1; }
+    P.dbuf = nullptr;
+    if (rc) { zero_fill(); return 0; }
+    int nonempty = 0;
+    for (size_t o = 0; o < P.outs.size(); o++) nonempty |= ne_host[o];
+    if (!nonempty) { zero_fill(); return 0; }
+    /* dense GPU block -> caller layout with dims */
+    for (int comp = 0; comp < ncomp; comp++) {
+        const double *src = T.hout + comp * P.out_size;
+        for (int l = 0; l < counts[3]; l++)
+            for (int k = 0; k < counts[2]; k++)
+                for (int j = 0; j < counts[1]; j++) {
+                    const double *s = src + counts[0] * (j + (int64_t)counts[1] * (k + (int64_t)counts[2] * l));
+                    double *o = out + comp * nout + (int64_t)d[0] * (j + (int64_t)d[1] * (k + (int64_t)d[2] * l));
+                    memcpy(o, s, sizeof(double) * counts[0]);
+                }
+    }
+    return 1;
+}
+
+void make_opt(CINTOpt **opt, FINT nbas)
+{
+    CINTOpt *o = (CINTOpt *)calloc(1, sizeof(CINTOpt));
+    o->nbas = nbas;
+    *opt = o;
+}
+}  // namespace
+
+/* ================================================================== C ABI */
+extern "C" {
+
+const char *cintgpu_last_error(void) { return tl_error.c_str(); }
+
+int cintgpu_device_sm_count(void)
+{
+    if (ensure_init()) return 0;
+    return g_ctx.sm_count;
+}
+
+int cintgpu_rys_nmax(void) { return cg_rys_nmax(); }
+
+int cintgpu_rys_roots_dev(int nroots, const double *xs_dev, int count, double *s_dev,
+                          double *w_dev, void *stream)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (nroots < 1 || nroots > cg_rys_nmax()) { set_error("nroots %d outside 1..%d", nroots, cg_rys_nmax()); return CINTGPU_ERR_ARG; }
+    rc = cg_launch_roots(xs_dev, count, nroots, g_ctx.rys_coef, s_dev, w_dev, (cudaStream_t)stream);
+    if (rc) { set_error("roots kernel failed"); return CINTGPU_ERR_CUDA; }
+    return 0;
+}
+
+int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
+                        const int64_t *offsets, const int *atm, int natm, const int *bas,
+                        int nbas, const double *env)
+{
+    *plan = nullptr;
+    int rc = ensure_init();
+    if (rc) return rc;
+    CINTGPUPlan *P = new CINTGPUPlan();
+    int64_t target = n < (int64_t)g_ctx.sm_count * 16 ? (int64_t)g_ctx.sm_count * 8 : 0;
+    rc = build_plan(P, kind, shls, n, offsets, atm, natm, bas, nbas, env, target);
+    if (!rc) rc = upload_plan(P, nullptr, 0, 0, false, nullptr);
+    if (rc) { free_plan_device(P); delete P; return rc; }
+    *plan = P;
+    return 0;
+}
+
+int64_t cintgpu_plan_output_size(const CINTGPUPlan *plan) { return plan->out_size; }
+int cintgpu_plan_ncomp(const CINTGPUPlan *plan) { return plan->ncomp; }
+double cintgpu_plan_flops(const CINTGPUPlan *plan) { return plan->flops; }
+int64_t cintgpu_plan_prim_quartets(const CINTGPUPlan *plan) { return plan->prim_quartets; }
+int cintgpu_plan_launches(const CINTGPUPlan *plan) { return (int)plan->classes.size() + 1; }
+
+int cintgpu_plan_execute(CINTGPUPlan *plan, double *out_dev, void *stream)
+{
+    return execute_plan(plan, out_dev, (cudaStream_t)stream);
+}
+
+int cintgpu_plan_nonempty(const CINTGPUPlan *plan, int *flags_host)
+{
+    std::vector<int> ne(plan->outs.size());
+    CUDA_OK(cudaMemcpy(ne.data(), plan->d_nonempty, sizeof(int) * ne.size(), cudaMemcpyDeviceToHost));
+    for (int64_t q = 0; q < plan->nitems; q++) flags_host[q] = 0;
+    for (size_t o = 0; o < ne.size(); o++) flags_host[plan->out_item[o]] |= ne[o];
+    return 0;
+}
+
+void cintgpu_plan_destroy(CINTGPUPlan *plan)
+{
+    if (!plan) return;
+    free_plan_device(plan);
+    delete plan;
+}
+
+int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,
+                       const int64_t *offsets, const int *atm, int natm, const int *bas,
+                       int nbas, const double *env)
+{
+    CINTGPUPlan *P = nullptr;
+    int rc = cintgpu_plan_create(&P, kind, shls, n, offsets, atm, natm, bas, nbas, env);
+    if (rc) return rc;
+    size_t outb = sizeof(double) * P->out_size * P->ncomp;
+    double *dout = nullptr;
+    if (cudaMalloc(&dout, std::max<size_t>(outb, 8)) != cudaSuccess) {
+        set_error("cudaMalloc(%zu) failed", outb);
+        cintgpu_plan_destroy(P);
+        return CINTGPU_ERR_NOMEM;
+    }
+    if (offsets) cudaMemcpy(dout, out_host, outb, cudaMemcpyHostToDevice);
+    rc = execute_plan(P, dout, 0);
+    if (!rc && cudaMemcpy(out_host, dout, outb, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        set_error("device to host copy failed: %s", cudaGetErrorString(cudaGetLastError()));
+        rc = CINTGPU_ERR_CUDA;
+    }
+    cudaFree(dout);
+    cintgpu_plan_destroy(P);
+    return rc;
+}
+
+/* ---- libcint drop-in ---------------------------------------------------------------------- */
+CACHE_SIZE_T int2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                       FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int2e_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                        FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int2e_ip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                           FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_IP1_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int2e_ip1_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                            FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_IP1_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int3c2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                         FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int3c2e_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                          FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+
+/* The optimizer holds no precomputed data here: pair data are rebuilt per call on the host,
+ * which is exactly what libcint's pair tables save it; the struct keeps libcint's layout. */
+void int2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
+void int2e_ip1_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
+void int3c2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
+void CINTdel_2e_optimizer(CINTOpt **opt)
+{
+    if (opt && *opt) { free(*opt); *opt = NULL; }
+}
+void CINTdel_optimizer(CINTOpt **opt) { CINTdel_2e_optimizer(opt); }
+
+FINT cint2e_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int2e_sph(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+FINT cint2e_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int2e_cart(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+void cint2e_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ int2e_optimizer(opt, atm, natm, bas, nbas, env); }
+void cint2e_cart_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ int2e_optimizer(opt, atm, natm, bas, nbas, env); }
+FINT cint2e_ip1_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int2e_ip1_sph(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+FINT cint2e_ip1_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int2e_ip1_cart(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+void cint2e_ip1_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ int2e_ip1_optimizer(opt, atm, natm, bas, nbas, env); }
+FINT cint3c2e_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int3c2e_sph(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+FINT cint3c2e_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int3c2e_cart(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+void cint3c2e_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ int3c2e_optimizer(opt, atm, natm, bas, nbas, env); }
+
+/* ---- basis helpers (libcint src/misc.c:72-93, src/cint_bas.c) ------------------------------ */
+double CINTgto_norm(FINT n, double a)
+{
+    /* 1/sqrt(int_0^inf r^(2n+2) exp(-2 a r^2) dr) */
+    double n1 = (2 * n + 2 + 1) * .5;
+    double gi = exp(lgamma(n1)) / (2. * pow(2 * a, n1));
+    return 1. / sqrt(gi);
+}
+FINT CINTlen_cart(const FINT l) { return (l + 1) * (l + 2) / 2; }
+FINT CINTcgto_cart(const FINT bas_id, const FINT *bas)
+{ const FINT *b = bas + BAS_SLOTS * bas_id; return ncart_l(b[ANG_OF]) * b[NCTR_OF]; }
+FINT CINTcgto_spheric(const FINT bas_id, const FINT *bas)
+{ const FINT *b = bas + BAS_SLOTS * bas_id; return nsph_l(b[ANG_OF]) * b[NCTR_OF]; }
+FINT CINTtot_cgto_cart(const FINT *bas, const FINT nbas)
+{ FINT s = 0; for (FINT i = 0; i < nbas; i++) s += CINTcgto_cart(i, bas); return s; }
+FINT CINTtot_cgto_spheric(const FINT *bas, const FINT nbas)
+{ FINT s = 0; for (FINT i = 0; i < nbas; i++) s += CINTcgto_spheric(i, bas); return s; }
+void CINTshells_cart_offset(FINT ao_loc[], const FINT *bas, const FINT nbas)
+{ ao_loc[0] = 0; for (FINT i = 1; i < nbas; i++) ao_loc[i] = ao_loc[i - 1] + CINTcgto_cart(i - 1, bas); }
+void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas)
+{ ao_loc[0] = 0; for (FINT i = 1; i < nbas; i++) ao_loc[i] = ao_loc[i - 1] + CINTcgto_spheric(i - 1, bas); }
+
+}  /* extern "C" */

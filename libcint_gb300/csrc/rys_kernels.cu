@@ -1,0 +1,513 @@
+/*
+ * GB300 (sm_103a) kernels of the Rys-quadrature two-electron integral path.
+ *
+ * The path is FP64-issue bound (measured on GB300: 1.2 TFLOP/s DFMA against 74 TFLOP/s FFMA), so
+ * the kernels are written to spend FP64 instructions only on the quadrature itself:
+ *   - recurrence coefficients are division free (linear in the Rys node s = t^2),
+ *   - roots/weights come from piecewise polynomial tables (Horner, 2 x 10 DFMA per root),
+ *   - pair quantities (exponential prefactors, product centres, screening values) are
+ *     precomputed once per primitive pair,
+ *   - all index arithmetic is integer.
+ *
+ * Work decomposition: one warp owns one task (a shell quartet or a slice of its primitive
+ * quartets) and walks its primitive quartets 32 at a time:
+ *   screen    each lane tests one primitive quartet with libcint's rule
+ *             (src/cint2e.c:400-425: skip kl if cce_kl > cutoff, skip ij if cce_ij > cutoff - cce_kl)
+ *             and the survivors are compacted with a warp ballot;
+ *   stage 1   one lane per (primitive quartet, root) "term": x, prefactor, root, weight and the
+ *             recurrence coefficients (libcint CINTg0_2e, src/g2e.c:4425-4545);
+ *   stage 2   one lane per (term, Cartesian axis): the 2D vertical recurrence and both horizontal
+ *             transfers (CINTg0_2e_2d + CINTg0_*2d_4d, src/g2e.c:272-693) into shared memory;
+ *   stage 3   one lane per output Cartesian component: sum over the batch's terms of
+ *             gx*gy*gz (CINTgout2e, src/cint2e.c:961-1183) or the nabla-i variant of int2e_ip1
+ *             (src/autocode/grad2.c:19-68), accumulated in the task's gctr slot (L2 resident).
+ * A second kernel turns the Cartesian accumulators into the requested layout (cart or real
+ * spherical, c2s_sph_2e1 / c2s_sph_3c2e1 semantics, src/cart2sph.c:5324-5383, 5884-5925) with
+ * arbitrary output strides.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "cintgpu_types.h"
+#include "rys_tables.inc"
+#include "rys_kernels.h"
+
+#define FULL 0xffffffffu
+
+__constant__ int c_rys_off[RYS_NMAX + 1];
+__constant__ double c_rys_xmax[RYS_NMAX + 1];
+__constant__ double c_large_r[RYS_NMAX * (RYS_NMAX + 1) / 2];
+__constant__ double c_large_w[RYS_NMAX * (RYS_NMAX + 1) / 2];
+
+/* sparse rows of the cart->sph matrices: row (l, m) has nnz entries (cart index, coefficient) */
+#define C2S_MAXNNZ CG_C2S_MAXNNZ
+#define C2S_ROWS ((CG_MAX_SHELL_L + 1) * (CG_MAX_SHELL_L + 1))
+__device__ int g_c2s_nnz[C2S_ROWS];
+__device__ int g_c2s_idx[C2S_ROWS * C2S_MAXNNZ];
+__device__ double g_c2s_val[C2S_ROWS * C2S_MAXNNZ];
+
+/* ------------------------------------------------------------------ layout per class */
+__host__ __device__ inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+
+__host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, int mode,
+                                                int ws_doubles, CGLayout *L)
+{
+    int dinc = (mode == CG_MODE_IP1) ? 1 : 0;
+    L->lic = li + dinc;
+    L->nroots = (L->lic + lj + lk + ll) / 2 + 1;
+    L->nmax = L->lic + lj;
+    L->mmax = lk + ll;
+    L->dI = L->lic + 1; L->dJ = lj + 1; L->dK = lk + 1; L->dL = ll + 1;
+    L->G = L->dI * L->dJ * L->dK * L->dL;
+    L->ng = (mode == CG_MODE_IP1) ? 2 : 1;
+    L->nf = ncart(li) * ncart(lj) * ncart(lk) * ncart(ll);
+    L->ncomp = (mode == CG_MODE_IP1) ? 3 : 1;
+    L->scr = (L->nmax + 1) * (L->mmax + 1) + L->dI * L->dJ * (L->mmax + 1) + (L->nmax + 1);
+    int fixed = CG_TERMW * 32 + 16;  /* term records + survivor list */
+    int avail = ws_doubles - fixed;
+    /* T terms need T*3*ng*G doubles of g arrays and min(32, 3T) lane scratch areas */
+    int T = 0;
+    for (int t = 32; t >= 1; t--) {
+        int items = 3 * t < 32 ? 3 * t : 32;
+        if (t * 3 * L->ng * L->G + items * L->scr <= avail) { T = t; break; }
+    }
+    L->T = T;
+}
+
+/* ------------------------------------------------------------------ roots */
+__device__ __forceinline__ void rys_node(int n, double x, int r, const double *__restrict__ coef,
+                                         double &s, double &w)
+{
+    if (x >= c_rys_xmax[n]) {
+        double rs = rsqrt(x);
+        int o = n * (n - 1) / 2 + r;
+        s = c_large_r[o] * (rs * rs);
+        w = c_large_w[o] * rs;
+    } else {
+        int k = (int)x;                      /* interval width 1 */
+        double y = 2.0 * (x - (double)k) - 1.0;
+        const double2 *c = reinterpret_cast<const double2 *>(
+            coef + c_rys_off[n] + (size_t)((k * n + r) * (RYS_DEG + 1)) * 2);
+        double2 cj = __ldg(c + RYS_DEG);
+        double a = cj.x, b = cj.y;
+#pragma unroll
+        for (int j = RYS_DEG - 1; j >= 0; j--) {
+            cj = __ldg(c + j);
+            a = fma(a, y, cj.x);
+            b = fma(b, y, cj.y);
+        }
+        s = a;
+        w = b;
+    }
+}
+
+__global__ void rys_roots_kernel(const double *__restrict__ xs, int count, int n,
+                                 const double *__restrict__ coef, double *s_out, double *w_out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    for (int r = 0; r < n; r++) {
+        double s, w;
+        rys_node(n, xs[i], r, coef, s, w);
+        s_out[(size_t)i * n + r] = s;
+        w_out[(size_t)i * n + r] = w;
+    }
+}
+
+/* ------------------------------------------------------------------ cart powers */
+__device__ __forceinline__ void cart_pow(int l, int p, int &lx, int &ly, int &lz)
+{
+    /* CINTcart_comp order (src/cint_bas.c:166-181): row = l - lx, q = lz */
+    int row = (int)((sqrtf(8.f * p + 1.f) - 1.f) * 0.5f);
+    while ((row + 1) * (row + 2) / 2 <= p) row++;
+    while (row * (row + 1) / 2 > p) row--;
+    int q = p - row * (row + 1) / 2;
+    lx = l - row;
+    ly = row - q;
+    lz = q;
+}
+
+/* ------------------------------------------------------------------ stage 2 */
+/* One Cartesian axis of one term: VRR into T2[a + (nmax+1) m], transfer to (i,j) per m, then to
+ * (k,l) per (i,j); final g[((i dJ + j) dK + k) dL + l] goes to gout. */
+__device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10, double b01,
+                                       double c00, double c0p, double g00, double AB, double CD,
+                                       double *scr, double *gout)
+{
+    const int nmax = L.nmax, mmax = L.mmax, na = nmax + 1, nm = mmax + 1;
+    double *T2 = scr;
+    double *H1 = scr + na * nm;
+    double *ab00 = H1 + L.dI * L.dJ * nm;
+    /* a * b00 */
+    {
+        double acc = 0.0;
+        for (int a = 0; a <= nmax; a++) { ab00[a] = acc; acc += b00; }
+    }
+    T2[0] = g00;
+    if (nmax > 0) {
+        double p0 = g00, p1 = c00 * g00, nb = b10;
+        T2[1] = p1;
+        for (int a = 1; a < nmax; a++) {
+            double p2 = fma(c00, p1, nb * p0);
+            T2[a + 1] = p2;
+            p0 = p1; p1 = p2;
+            nb += b10;
+        }
+    }
+    double mb = 0.0;
+    for (int m = 0; m < mmax; m++) {
+        const double *cm = T2 + m * na;
+        const double *cm1 = T2 + (m - 1) * na;
+        double *cn = T2 + (m + 1) * na;
+        for (int a = 0; a <= nmax; a++) {
+            double v = c0p * cm[a];
+            if (m > 0) v = fma(mb, cm1[a], v);
+            if (a > 0) v = fma(ab00[a], cm[a - 1], v);
+            cn[a] = v;
+        }
+        mb += b01;
+    }
+    /* (a,0| -> (i,j|  per column m, in place: col[a] = col[a+1] + AB col[a] */
+    for (int m = 0; m <= mmax; m++) {
+        double *col = T2 + m * na;
+        for (int i = 0; i < L.dI; i++) H1[(i * L.dJ) * nm + m] = col[i];
+        for (int j = 1; j < L.dJ; j++) {
+            for (int a = 0; a <= nmax - j; a++) col[a] = fma(AB, col[a], col[a + 1]);
+            for (int i = 0; i < L.dI; i++) H1[(i * L.dJ + j) * nm + m] = col[i];
+        }
+    }
+    /* |m,0) -> |k,l) per (i,j) */
+    const int nij = L.dI * L.dJ;
+    for (int ij = 0; ij < nij; ij++) {
+        double *v = H1 + ij * nm;
+        double *go = gout + ij * L.dK * L.dL;
+        for (int k = 0; k < L.dK; k++) go[k * L.dL] = v[k];
+        for (int l = 1; l < L.dL; l++) {
+            for (int m = 0; m <= mmax - l; m++) v[m] = fma(CD, v[m], v[m + 1]);
+            for (int k = 0; k < L.dK; k++) go[k * L.dL + l] = v[k];
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ main kernel */
+template <int MODE>
+__global__ void __launch_bounds__(128)
+rys_eri_kernel(CGLaunch P)
+{
+    extern __shared__ double smem[];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    double *ws = smem + (size_t)warp * P.ws_doubles;
+    double *term = ws;                                   /* CG_TERMW * 32 */
+    int *surv = reinterpret_cast<int *>(ws + CG_TERMW * 32);
+    double *greg = ws + CG_TERMW * 32 + 16;
+
+    CGLayout L;
+    cg_class_layout(P.li, P.lj, P.lk, P.ll, MODE, P.ws_doubles, &L);
+    const int T = L.T;
+    double *scr_base = greg + T * 3 * L.ng * L.G;
+    const int n = L.nroots;
+    const int nfi = ncart(P.li), nfj = ncart(P.lj), nfk = ncart(P.lk), nfl = ncart(P.ll);
+    const double common = P.common;
+    const double expcut = P.expcutoff;
+
+    for (;;) {
+        int tid = 0;
+        if (lane == 0) tid = atomicAdd(P.counter, 1);
+        tid = __shfl_sync(FULL, tid, 0);
+        if (tid >= P.ntasks) break;
+        const CGTask tk = P.tasks[P.task0 + tid];
+        const CGPair pij = P.pairs[tk.pij];
+        const CGPair pkl = P.pairs[tk.pkl];
+        const CGPrimPair *__restrict__ ppij = P.prims + pij.prim_off;
+        const CGPrimPair *__restrict__ ppkl = P.prims + pkl.prim_off;
+        const int nij = pij.npa * pij.npb;
+        double *acc = P.gctr + tk.cart_off;
+        for (int c = lane; c < L.nf * L.ncomp; c += 32) acc[c] = 0.0;
+        bool any = false;
+
+        for (int base = tk.pq0; base < tk.pq1; base += 32) {
+            /* ---- screening (libcint SET_RIJ / eijcutoff rule) */
+            int pq = base + lane;
+            bool alive = false;
+            if (pq < tk.pq1) {
+                int kl = pq / nij, ij = pq - kl * nij;
+                double ccekl = ppkl[kl].cce;
+                if (!(ccekl > expcut)) {
+                    double ccij = ppij[ij].cce;
+                    alive = !(ccij > expcut - ccekl);
+                }
+            }
+            unsigned mask = __ballot_sync(FULL, alive);
+            int ns = __popc(mask);
+            if (alive) surv[__popc(mask & ((1u << lane) - 1u))] = pq;
+            __syncwarp();
+            if (ns == 0) continue;
+            any = true;
+            const int nterm = ns * n;
+            for (int t0 = 0; t0 < nterm; t0 += T) {
+                const int Tb = min(T, nterm - t0);
+                /* ---- stage 1: one lane per term */
+                if (lane < Tb) {
+                    int g = t0 + lane;
+                    int p = g / n, r = g - p * n;
+                    int q = surv[p];
+                    int kl = q / nij, ij = q - kl * nij;
+                    const CGPrimPair A = ppij[ij];
+                    const CGPrimPair B = ppkl[kl];
+                    double aijkl = A.a + B.a;
+                    double rs = rsqrt(aijkl);
+                    double inv = rs * rs;
+                    double PQx = A.P[0] - B.P[0], PQy = A.P[1] - B.P[1], PQz = A.P[2] - B.P[2];
+                    double rr = fma(PQx, PQx, fma(PQy, PQy, PQz * PQz));
+                    double rho = A.a * B.a * inv;
+                    double x = rho * rr;
+                    double s, w;
+                    rys_node(n, x, r, P.rys_coef, s, w);
+                    double fac1 = common * A.K * B.K * rs * A.inv_a * B.inv_a;
+                    double tb = s * inv;                 /* 2 b00 */
+                    double b00 = 0.5 * tb;
+                    double oms = 1.0 - s;
+                    double b10 = fma(0.5 * A.inv_a, oms, b00);
+                    double b01 = fma(0.5 * B.inv_a, oms, b00);
+                    double ta = tb * B.a, tc = tb * A.a;
+                    double *rec = term + lane * CG_TERMW;
+                    rec[0] = b00; rec[1] = b10; rec[2] = b01;
+                    rec[3] = fma(-ta, PQx, A.P[0] - pij.A[0]);
+                    rec[4] = fma(-ta, PQy, A.P[1] - pij.A[1]);
+                    rec[5] = fma(-ta, PQz, A.P[2] - pij.A[2]);
+                    rec[6] = fma(tc, PQx, B.P[0] - pkl.A[0]);
+                    rec[7] = fma(tc, PQy, B.P[1] - pkl.A[1]);
+                    rec[8] = fma(tc, PQz, B.P[2] - pkl.A[2]);
+                    rec[9] = w * fac1;
+                    rec[10] = -2.0 * A.aA;
+                }
+                __syncwarp();
+                /* ---- stage 2: one lane per (term, axis) */
+                for (int item = lane; item < 3 * Tb; item += 32) {
+                    int t = item / 3, ax = item - 3 * t;
+                    const double *rec = term + t * CG_TERMW;
+                    double g00 = (ax == 2) ? rec[9] : 1.0;
+                    double *gdst = greg + (size_t)(t * 3 + ax) * L.ng * L.G;
+                    g_axis(L, rec[0], rec[1], rec[2], rec[3 + ax], rec[6 + ax], g00,
+                           pij.AB[ax], pkl.AB[ax], scr_base + lane * L.scr, gdst);
+                    if (MODE == CG_MODE_IP1) {
+                        /* f(i) = i g(i-1) - 2 a_i g(i+1)   (CINTnabla1i_2e, src/g2e.c:4550-4591) */
+                        const double ai2 = rec[10];
+                        const int sI = L.dJ * L.dK * L.dL;
+                        double *f = gdst + L.G;
+                        for (int i = 0; i < L.dI - 1; i++) {
+                            for (int o = 0; o < sI; o++) {
+                                double v = ai2 * gdst[(i + 1) * sI + o];
+                                if (i > 0) v = fma((double)i, gdst[(i - 1) * sI + o], v);
+                                f[i * sI + o] = v;
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+                /* ---- stage 3: one lane per Cartesian component */
+                const int stride_t = 3 * L.ng * L.G;
+                for (int c = lane; c < L.nf; c += 32) {
+                    int ic = c % nfi, rest = c / nfi;
+                    int kc = rest % nfk; rest /= nfk;
+                    int lc = rest % nfl;
+                    int jc = rest / nfl;
+                    int ix, iy, iz, jx, jy, jz, kx, ky, kz, lx, ly, lz;
+                    cart_pow(P.li, ic, ix, iy, iz);
+                    cart_pow(P.lj, jc, jx, jy, jz);
+                    cart_pow(P.lk, kc, kx, ky, kz);
+                    cart_pow(P.ll, lc, lx, ly, lz);
+                    int ox = ((ix * L.dJ + jx) * L.dK + kx) * L.dL + lx;
+                    int oy = ((iy * L.dJ + jy) * L.dK + ky) * L.dL + ly;
+                    int oz = ((iz * L.dJ + jz) * L.dK + kz) * L.dL + lz;
+                    if (MODE == CG_MODE_ERI) {
+                        double s0 = acc[c];
+                        const double *gb = greg;
+                        for (int t = 0; t < Tb; t++, gb += stride_t) {
+                            s0 = fma(gb[ox] * gb[L.G + oy], gb[2 * L.G + oz], s0);
+                        }
+                        acc[c] = s0;
+                    } else {
+                        double sx = acc[c], sy = acc[L.nf + c], sz = acc[2 * L.nf + c];
+                        const double *gb = greg;
+                        const int G = L.G;
+                        for (int t = 0; t < Tb; t++, gb += stride_t) {
+                            /* axis a block: g at gb + a*2G, f at gb + a*2G + G */
+                            double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
+                            double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
+                            sx = fma(fx, gy * gz, sx);
+                            sy = fma(fy, gx * gz, sy);
+                            sz = fma(fz, gx * gy, sz);
+                        }
+                        acc[c] = sx; acc[L.nf + c] = sy; acc[2 * L.nf + c] = sz;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        if (any && lane == 0) P.nonempty[tk.out] = 1;
+    }
+}
+
+/* ------------------------------------------------------------------ output kernel */
+/* One warp per contracted quartet: sum partial slots, then transform the four indices one at a
+ * time (j, l, k, i as c2s_sph_2e1 does) through a per-warp scratch in global memory, and store
+ * with the task's strides. */
+__device__ __forceinline__ void c2s_pass(const double *src, double *dst, int lsh, int sph,
+                                         int inner, int ncart_t, int outer, int lane)
+{
+    /* src[(a, t, b)] with a < inner, t < ncart_t, b < outer  ->  dst[(a, m, b)] */
+    int nm = sph ? (lsh <= 1 ? ncart_t : 2 * lsh + 1) : ncart_t;
+    int total = inner * nm * outer;
+    for (int e = lane; e < total; e += 32) {
+        int a = e % inner, rest = e / inner;
+        int m = rest % nm, b = rest / nm;
+        double v;
+        if (!sph || lsh <= 1) {
+            v = src[(size_t)(b * ncart_t + m) * inner + a];
+        } else {
+            int row = lsh * lsh + m;     /* rows of l start at l^2 (sum of 2l'+1 for l' < l) */
+            int nnz = g_c2s_nnz[row];
+            v = 0.0;
+            for (int z = 0; z < nnz; z++) {
+                v = fma(g_c2s_val[row * C2S_MAXNNZ + z],
+                        src[(size_t)(b * ncart_t + g_c2s_idx[row * C2S_MAXNNZ + z]) * inner + a], v);
+            }
+        }
+        dst[(size_t)(b * nm + m) * inner + a] = v;
+    }
+}
+
+__global__ void __launch_bounds__(128)
+cg_output_kernel(const CGOutTask *__restrict__ ot, int nout, double *gctr, const int *nonempty,
+                 double *scratch, int64_t scratch_per_warp, double *out, int ncomp,
+                 int64_t comp_stride)
+{
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    double *s1 = scratch + (size_t)gw * scratch_per_warp;
+    double *s2 = s1 + scratch_per_warp / 2;
+    for (int q = gw; q < nout; q += nw) {
+        const CGOutTask o = ot[q];
+        const int sph = o.flags & 1;
+        int nfc[4], nd[4];
+        for (int a = 0; a < 4; a++) {
+            nfc[a] = ncart(o.l[a]);
+            nd[a] = sph ? (o.l[a] <= 1 ? nfc[a] : 2 * o.l[a] + 1) : nfc[a];
+        }
+        const int nf = nfc[0] * nfc[1] * nfc[2] * nfc[3];
+        const bool ne = nonempty[q] != 0;
+        for (int comp = 0; comp < ncomp; comp++) {
+            double *g0 = gctr + o.cart_off + (size_t)comp * nf;
+            if (ne && o.nparts > 1) {
+                for (int c = lane; c < nf; c += 32) {
+                    double v = g0[c];
+                    for (int p = 1; p < o.nparts; p++) v += g0[(size_t)p * ncomp * nf + c];
+                    g0[c] = v;
+                }
+                __syncwarp();
+            }
+            double *dst = out + o.out_off + (size_t)comp * comp_stride;
+            if (!ne) {
+                int tot = nd[0] * nd[1] * nd[2] * nd[3];
+                for (int e = lane; e < tot; e += 32) {
+                    int i = e % nd[0], r = e / nd[0];
+                    int j = r % nd[1]; r /= nd[1];
+                    int k = r % nd[2], l = r / nd[2];
+                    dst[(int64_t)i * o.st[0] + (int64_t)j * o.st[1] + (int64_t)k * o.st[2]
+                        + (int64_t)l * o.st[3]] = 0.0;
+                }
+                continue;
+            }
+            /* gctr order: i fastest, then k, l, j.  Pass j: inner = nfi*nfk*nfl, t = j */
+            const double *cur = g0;
+            c2s_pass(cur, s1, o.l[1], sph, nfc[0] * nfc[2] * nfc[3], nfc[1], 1, lane);
+            __syncwarp();
+            /* pass l: (i,k | l | js) */
+            c2s_pass(s1, s2, o.l[3], sph, nfc[0] * nfc[2], nfc[3], nd[1], lane);
+            __syncwarp();
+            /* pass k: (i | k | ls, js) */
+            c2s_pass(s2, s1, o.l[2], sph, nfc[0], nfc[2], nd[3] * nd[1], lane);
+            __syncwarp();
+            /* pass i: (1 | i | ks, ls, js) */
+            c2s_pass(s1, s2, o.l[0], sph, 1, nfc[0], nd[2] * nd[3] * nd[1], lane);
+            __syncwarp();
+            /* s2 layout: (is, ks, ls, js) */
+            int tot = nd[0] * nd[2] * nd[3] * nd[1];
+            for (int e = lane; e < tot; e += 32) {
+                int i = e % nd[0], r = e / nd[0];
+                int k = r % nd[2]; r /= nd[2];
+                int l = r % nd[3], j = r / nd[3];
+                dst[(int64_t)i * o.st[0] + (int64_t)j * o.st[1] + (int64_t)k * o.st[2]
+                    + (int64_t)l * o.st[3]] = s2[e];
+            }
+            __syncwarp();
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ host-side launchers */
+extern "C" int cg_kernels_init(const int *c2s_nnz, const int *c2s_idx, const double *c2s_val,
+                               double **rys_coef_dev)
+{
+    double xmax[RYS_NMAX + 1];
+    xmax[0] = 0;
+    for (int n = 1; n <= RYS_NMAX; n++) xmax[n] = RYS_H * rys_nint_host[n];
+    cudaError_t e;
+    if ((e = cudaMemcpyToSymbol(c_rys_off, rys_off_host, sizeof(rys_off_host))) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(c_rys_xmax, xmax, sizeof(xmax))) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(c_large_r, rys_large_r_host, sizeof(rys_large_r_host))) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(c_large_w, rys_large_w_host, sizeof(rys_large_w_host))) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(g_c2s_nnz, c2s_nnz, sizeof(int) * C2S_ROWS)) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(g_c2s_idx, c2s_idx, sizeof(int) * C2S_ROWS * C2S_MAXNNZ)) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(g_c2s_val, c2s_val, sizeof(double) * C2S_ROWS * C2S_MAXNNZ)) != cudaSuccess) return (int)e;
+    double *d = nullptr;
+    if ((e = cudaMalloc(&d, sizeof(double) * RYS_NCOEF)) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpy(d, rys_coef_host, sizeof(double) * RYS_NCOEF, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        cudaFree(d);
+        return (int)e;
+    }
+    *rys_coef_dev = d;
+    for (int mode = 0; mode < 2; mode++) {
+        void *fn = mode == 0 ? (void *)rys_eri_kernel<CG_MODE_ERI> : (void *)rys_eri_kernel<CG_MODE_IP1>;
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 8 * CG_WS_MAX);
+        if (e != cudaSuccess) return (int)e;
+    }
+    return 0;
+}
+
+extern "C" int cg_rys_nmax(void) { return RYS_NMAX; }
+extern "C" int cg_rys_deg(void) { return RYS_DEG; }
+
+extern "C" void cg_layout(int li, int lj, int lk, int ll, int mode, int ws_doubles, CGLayout *L)
+{
+    cg_class_layout(li, lj, lk, ll, mode, ws_doubles, L);
+}
+
+extern "C" int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStream_t stream)
+{
+    size_t smem = (size_t)4 * P->ws_doubles * sizeof(double);
+    if (mode == CG_MODE_ERI)
+        rys_eri_kernel<CG_MODE_ERI><<<nblocks, 128, smem, stream>>>(*P);
+    else
+        rys_eri_kernel<CG_MODE_IP1><<<nblocks, 128, smem, stream>>>(*P);
+    return (int)cudaGetLastError();
+}
+
+extern "C" int cg_launch_output(const CGOutTask *ot, int nout, double *gctr, const int *nonempty,
+                                double *scratch, int64_t scratch_per_warp, int nblocks, double *out,
+                                int ncomp, int64_t comp_stride, cudaStream_t stream)
+{
+    cg_output_kernel<<<nblocks, 128, 0, stream>>>(ot, nout, gctr, nonempty, scratch,
+                                                  scratch_per_warp, out, ncomp, comp_stride);
+    return (int)cudaGetLastError();
+}
+
+extern "C" int cg_launch_roots(const double *xs, int count, int n, const double *coef, double *s,
+                               double *w, cudaStream_t stream)
+{
+    if (n < 1 || n > RYS_NMAX) return -1;
+    rys_roots_kernel<<<(count + 127) / 128, 128, 0, stream>>>(xs, count, n, coef, s, w);
+    return (int)cudaGetLastError();
+}

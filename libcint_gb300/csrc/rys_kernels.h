@@ -1,0 +1,51 @@
+/* Internal interface between the host planner and the CUDA kernels (not part of the C-ABI). */
+#ifndef CINTGPU_RYS_KERNELS_H
+#define CINTGPU_RYS_KERNELS_H
+#include <stdint.h>
+#include <cuda_runtime.h>
+#include "cintgpu_types.h"
+
+#define CG_MODE_ERI 0
+#define CG_MODE_IP1 1
+#define CG_TERMW 12                  /* doubles per term record in shared memory */
+#define CG_WS_SMALL (24 * 1024 / 8)  /* doubles of shared memory per warp, default */
+#define CG_WS_MAX (48 * 1024 / 8)    /* doubles of shared memory per warp, large classes */
+#define CG_C2S_MAXNNZ 16
+
+typedef struct {
+    int lic, nroots, nmax, mmax;
+    int dI, dJ, dK, dL, G, ng, nf, ncomp, scr, T;
+} CGLayout;
+
+typedef struct {
+    const CGTask *tasks;
+    int task0, ntasks;
+    const CGPair *pairs;
+    const CGPrimPair *prims;
+    double *gctr;
+    int *counter;
+    int *nonempty;
+    const double *rys_coef;
+    double common, expcutoff;
+    int li, lj, lk, ll;
+    int ws_doubles;
+} CGLaunch;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+int cg_kernels_init(const int *c2s_nnz, const int *c2s_idx, const double *c2s_val,
+                    double **rys_coef_dev);
+int cg_rys_nmax(void);
+int cg_rys_deg(void);
+void cg_layout(int li, int lj, int lk, int ll, int mode, int ws_doubles, CGLayout *L);
+int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStream_t stream);
+int cg_launch_output(const CGOutTask *ot, int nout, double *gctr, const int *nonempty,
+                     double *scratch, int64_t scratch_per_warp, int nblocks, double *out,
+                     int ncomp, int64_t comp_stride, cudaStream_t stream);
+int cg_launch_roots(const double *xs, int count, int n, const double *coef, double *s, double *w,
+                    cudaStream_t stream);
+#ifdef __cplusplus
+}
+#endif
+#endif
