@@ -1,0 +1,282 @@
+"""Benchmark of the batched Rys int2e_sph path on the c1 workload (see libcint_gb300/molecules.py).
+
+Workload (one "step"): one execution of a batched int2e_sph plan over a seeded sample of the
+Schwarz-surviving unique shell quartets of c1 (120 atoms, 14 A cube, 3s3p2d1f per atom, 1-8
+primitives; keep Q_ij * Q_kl >= 1e-12 with Q_ij = sqrt(max|(ij|ij)|)).  The sample (100k
+quartets, tests/golden/c1_quartets.npz) was drawn uniformly from the unique quartets
+(i>=j, k>=l, ij>=kl) by rejection on libcint's own Schwarz bounds; the full list (~3e10 quartets)
+does not fit a bench step.  GPU and CPU legs evaluate the same list.  Metric: spherical integrals per second
+(sum of di*dj*dk*dl over the step's quartets / time).
+
+  value      device-resident inputs, one plan execution per step, CUDA events on the launching
+             stream, L2 flushed (256 MiB memset) before every step outside the events.
+  e2e        the one-shot host-buffer C-ABI call cintgpu_batch_host (host planning, H2D, kernels,
+             D2H of every integral) per step, wall clock.
+  roofline   the Rys kernels are FP64-issue bound: achieved = algorithmic FP64 flops of the step
+             (model of cintgpu_plan_flops) / step time, against the measured DFMA peak.
+  cpu_baseline  the C restatement (oracle/, "port") with OpenMP on all host cores over a bounded
+             sample of the same quartet list.
+
+--impl reference times the CPU implementation of the path on the host cores (the port; libcint
+itself cannot be rebuilt where its sources are absent) and prints the same metric.
+Multi-GPU (torchrun): every rank evaluates the committed list (weak scaling: fixed work per GPU),
+no collectives on the data path; the time is the max over ranks.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import struct
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FP64_PEAK_TFLOPS = 1.196      # measured DFMA peak of this GB300 pool, profiles/fp64_peak_gb300.md
+SCHWARZ = 1e-12
+L2_FLUSH_BYTES = 256 << 20
+
+
+def load_quartets(n=None):
+    """The committed c1 sample (tests/golden/c1_quartets.npz, made by make_c1_sample.py with
+    libcint's own Schwarz bounds): unique quartets with Q_ij Q_kl >= 1e-12, uniform."""
+    qs = np.load(os.path.join(ROOT, 'tests', 'golden', 'c1_quartets.npz'))['quartets']
+    return np.ascontiguousarray(qs[:n] if n else qs, dtype=np.int32)
+
+
+def integrals_of(mol, qs):
+    d = np.array([mol.nsph(s) for s in range(mol.nbas)], dtype=np.int64)
+    return int((d[qs[:, 0]] * d[qs[:, 1]] * d[qs[:, 2]] * d[qs[:, 3]]).sum())
+
+
+def write_bench_input(path, mol, qs):
+    with open(path, 'wb') as f:
+        f.write(struct.pack('4i', mol.natm, mol.nbas, mol.env.size, len(qs)))
+        f.write(mol.atm.astype(np.int32).tobytes())
+        f.write(mol.bas.astype(np.int32).tobytes())
+        f.write(mol.env.astype(np.float64).tobytes())
+        f.write(np.ascontiguousarray(qs, dtype=np.int32).tobytes())
+
+
+def cpu_port_rate(mol, qs, threads, target_s=12.0):
+    """Time the C restatement (oracle port) with OpenMP over a bounded prefix of qs."""
+    subprocess.run(['make', '-s', '-C', os.path.join(ROOT, 'oracle'), 'oracle'], check=True)
+    exe = os.path.join(ROOT, 'oracle', '_build', 'oracle_bench')
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, 'in.bin')
+        n = min(len(qs), 2000)
+        while True:
+            write_bench_input(path, mol, qs[:n])
+            r = subprocess.run([exe, path, str(threads)], capture_output=True, text=True, check=True)
+            res = json.loads(r.stdout)
+            if res['seconds'] >= 0.3 * target_s or n >= len(qs):
+                break
+            n = min(len(qs), int(n * max(2.0, target_s / max(res['seconds'], 1e-3))))
+    return res
+
+
+class ClockSampler:
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+        try:
+            self.f = open(self.path, 'w')
+            self.proc = subprocess.Popen(['nvidia-smi', '--query-gpu=' + q, '--format=csv',
+                                          '-lms', '200'], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self, device_index):
+        try:
+            rows = [l.strip().split(', ') for l in open(self.path).read().strip().splitlines()[1:]]
+        except OSError:
+            return None
+        rows = [r for r in rows if len(r) >= 9 and r[0] == str(device_index)]
+        if not rows:
+            return None
+        mhz = [float(r[1].split()[0]) for r in rows]
+        mx = float(rows[0][2].split()[0])
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip() == 'Active'})
+        return {'sm_mhz': statistics.median(mhz), 'sm_max_mhz': mx, 'reasons': reasons,
+                'samples': len(rows)}
+
+
+def run_reference(args, rank, world):
+    from libcint_gb300 import molecules as M
+    if rank != 0:
+        return
+    mol = M.config1(seed=0)
+    qs = load_quartets(args.quartets)
+    threads = os.cpu_count()
+    rates = []
+    for step in range(args.warmup + args.steps):
+        res = cpu_port_rate(mol, qs, threads, target_s=args.cpu_seconds)
+        if step >= args.warmup:
+            rates.append(res['integrals'] / res['seconds'])
+    v = float(np.median(rates))
+    line = {
+        'impl': 'reference', 'metric': 'int2e_sph integrals/s (c1 Schwarz-screened quartets)',
+        'value': v, 'unit': 'integrals/s', 'n_gpus': args.gpus, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': 1e3 * res['seconds'], 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+        'config': {'workload': 'c1: 120 atoms, 14 A cube, 3s3p2d1f, 1-8 prims, Schwarz 1e-12',
+                   'quartets_per_step': res['quartets']},
+        'cpu_baseline': {'value': v, 'unit': 'integrals/s', 'cores': res['threads'], 'kind': 'port',
+                         'sample': '%d Schwarz-surviving c1 quartets, OpenMP dynamic' % res['quartets']},
+        'e2e': {'value': v, 'unit': 'integrals/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        'note': 'libcint itself is not buildable on the GPU host (its sources are not shipped); '
+                'the timed CPU implementation is the C restatement in oracle/ (same checksum as '
+                'libcint on a shared sample).',
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world):
+    import torch
+    import libcint_gb300 as cg
+    from libcint_gb300 import molecules as M
+    dev = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(dev)
+    cg.build_library()
+    mol = M.config1(seed=0)
+    qs = load_quartets(args.quartets)
+    nint = integrals_of(mol, qs)
+    plan = cg.Plan(cg.INT2E_SPH, mol, qs)
+    out = torch.empty(plan.output_size, dtype=torch.float64, device='cuda')
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device='cuda')
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        plan.execute(out, stream)
+    torch.cuda.synchronize()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    clk = ClockSampler(os.path.join(ROOT, 'gpurun_out', 'clocks_rank%d.csv' % rank)
+                       if os.path.isdir(os.path.join(ROOT, 'gpurun_out')) else
+                       os.path.join(tempfile.gettempdir(), 'cintgpu_clocks.csv'))
+    evs = []
+    with clk:
+        time.sleep(0.3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.execute(out, stream)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    tot_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([tot_s], device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_s = float(t.item())
+    # end-to-end through the one-shot host-buffer C-ABI call
+    host_out = np.zeros(plan.output_size)
+    e2e_times = []
+    for it in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
+        t1 = time.perf_counter()
+        rc = cg.lib().cintgpu_batch_host(cg.INT2E_SPH, host_out.ctypes.data_as(ctypes.c_void_p),
+                                         qs.ctypes.data_as(ctypes.c_void_p), len(qs), None,
+                                         mol.atm.ctypes.data_as(ctypes.c_void_p), mol.natm,
+                                         mol.bas.ctypes.data_as(ctypes.c_void_p), mol.nbas,
+                                         mol.env.ctypes.data_as(ctypes.c_void_p))
+        if rc:
+            raise RuntimeError(cg.last_error())
+        if it > 0:
+            e2e_times.append(time.perf_counter() - t1)
+    h2d = int(cg.lib().cintgpu_plan_upload_bytes(plan._h)) + qs.nbytes
+    d2h = plan.output_size * 8
+    if rank != 0:
+        return
+    value = nint * world * args.steps / tot_s
+    achieved = plan.flops * args.steps / tot_s / 1e12
+    clocks = clk.summary(dev)
+    line = {
+        'metric': 'int2e_sph integrals/s (c1 Schwarz-screened quartets, batched plan)',
+        'value': value, 'unit': 'integrals/s', 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': 1e3 * tot_s / args.steps, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+        'config': {'workload': 'c1: 120 atoms, 14 A cube, 3s3p2d1f, 1-8 prims, Schwarz 1e-12',
+                   'quartets_per_step': int(len(qs)), 'integrals_per_step': nint,
+                   'prim_quartets_per_step': int(plan.prim_quartets),
+                   'l2': 'flushed before every step (256 MiB memset), outside the step events',
+                   'wall_s_timed_region': wall},
+        'quartets_per_s': len(qs) * world * args.steps / tot_s,
+        'gpu_launches': plan.launches * args.steps,
+        'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': FP64_PEAK_TFLOPS,
+                     'unit': 'TFLOP/s', 'frac': achieved / FP64_PEAK_TFLOPS,
+                     'traffic': None,
+                     'peak_source': 'measured DFMA peak (profiles/fp64_peak_gb300.md); '
+                                    'MEASURED_PEAKS.json carries no FP64 figure'},
+        'e2e': {'value': nint / statistics.median(e2e_times) if e2e_times else None,
+                'unit': 'integrals/s',
+                'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
+                'path': 'cintgpu_batch_host (plan + H2D + kernels + D2H), wall clock'},
+        'clocks': clocks,
+    }
+    if not args.no_cpu:
+        res = cpu_port_rate(mol, qs, os.cpu_count(), target_s=args.cpu_seconds)
+        line['cpu_baseline'] = {'value': res['integrals'] / res['seconds'], 'unit': 'integrals/s',
+                                'cores': res['threads'], 'kind': 'port',
+                                'sample': 'first %d quartets of the step list (%.1f s)'
+                                          % (res['quartets'], res['seconds'])}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gpu', choices=['gpu', 'reference'])
+    ap.add_argument('--quartets', type=int, default=0, help='0 = the whole committed sample')
+    ap.add_argument('--e2e-steps', type=int, default=3)
+    ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    ap.add_argument('--no-cpu', action='store_true')
+    args = ap.parse_args()
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    if world > 1:
+        import torch.distributed as dist
+        backend = 'gloo' if args.impl == 'reference' else 'nccl'
+        if backend == 'nccl':
+            import torch
+            torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
+        dist.init_process_group(backend)
+    if args.impl == 'reference':
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -149,6 +149,8 @@ int64_t cintgpu_plan_prim_quartets(const CINTGPUPlan *plan);
 /* Launch the plan on `stream` (a cudaStream_t; NULL = legacy default stream) writing
  * out_dev[comp * output_size + offsets[q] + ...].  Asynchronous; enqueue only. */
 int cintgpu_plan_execute(CINTGPUPlan *plan, double *out_dev, void *stream);
+/* bytes the plan keeps resident in HBM (pair tables, task lists) and uploaded at creation */
+int64_t cintgpu_plan_upload_bytes(const CINTGPUPlan *plan);
 /* number of kernel launches one execution enqueues */
 int cintgpu_plan_launches(const CINTGPUPlan *plan);
 /* after execution completed: per item 1 if any primitive quartet survived screening */

@@ -61,6 +61,8 @@ def lib():
     L.cintgpu_plan_flops.restype = dbl
     L.cintgpu_plan_prim_quartets.argtypes = [vp]
     L.cintgpu_plan_prim_quartets.restype = i64
+    L.cintgpu_plan_upload_bytes.argtypes = [vp]
+    L.cintgpu_plan_upload_bytes.restype = i64
     L.cintgpu_plan_launches.argtypes = [vp]
     L.cintgpu_plan_launches.restype = i32
     L.cintgpu_plan_execute.argtypes = [vp, vp, vp]

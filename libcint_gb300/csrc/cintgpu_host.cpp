@@ -211,12 +211,10 @@ struct PairKeyHash {
 }  // namespace
 
 /* ------------------------------------------------------------------ plan */
-struct ClassLaunch {
-    int l[4];
-    int task0, ntasks;
-    int ws;
-    int blocks_per_sm;
-    double common;
+struct TaskGroup {              /* one kernel launch: tasks [task0, task0 + ntasks) */
+    int task0 = 0, ntasks = 0;
+    int ws = CG_WS_SMALL;       /* shared-memory doubles per warp */
+    int blocks_per_sm = 2;
 };
 
 struct CINTGPUPlan {
@@ -236,8 +234,9 @@ struct CINTGPUPlan {
     std::vector<CGPrimPair> prims;
     std::vector<CGTask> tasks;
     std::vector<CGOutTask> outs;
+    std::vector<int> pqlist;       /* surviving primitive quartets, per task slice */
     std::vector<int> out_item;     /* item index of each CGOutTask */
-    std::vector<ClassLaunch> classes;
+    TaskGroup groups[2];           /* [0] regular classes, [1] classes needing 48 KB per warp */
     int64_t gctr_size = 0;
     /* device */
     char *dbuf = nullptr;
@@ -247,12 +246,15 @@ struct CINTGPUPlan {
     CGPrimPair *d_prims = nullptr;
     CGTask *d_tasks = nullptr;
     CGOutTask *d_outs = nullptr;
+    int *d_pqlist = nullptr;
     double *d_gctr = nullptr;
-    int *d_counters = nullptr;
+    int *d_counters = nullptr;     /* [0], [1]: task counters of the groups; [2]: status */
     int *d_nonempty = nullptr;
     double *d_scratch = nullptr;
     int out_blocks = 1;
     int64_t scratch_per_warp = 0;
+    cudaStream_t side = nullptr;   /* second stream for the large-class group */
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace {
@@ -378,6 +380,11 @@ static void free_plan_device(CINTGPUPlan *p)
 {
     if (p->owns_dbuf && p->dbuf) cudaFree(p->dbuf);
     p->dbuf = nullptr;
+    if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+    if (p->ev_join) cudaEventDestroy(p->ev_join);
+    if (p->side) cudaStreamDestroy(p->side);
+    p->ev_fork = p->ev_join = nullptr;
+    p->side = nullptr;
 }
 
 /* Build the host images. split_target: minimum number of compute tasks wanted (0 = no split). */
@@ -476,198 +483,215 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         }
     }
     P->out_size = next_off;
-    /* surviving primitive quartets and the flop model (host copy of the kernel's screening) */
-    {
-        double fl = 0;
-        int64_t npq_alive = 0;
-        for (const Pending &pe : pend) {
-            const CGPair &a = P->pairs[pe.pij], &b = P->pairs[pe.pkl];
-            const CGPrimPair *pa = &P->prims[a.prim_off], *pb = &P->prims[b.prim_off];
-            int nij = a.npa * a.npb, nkl = b.npa * b.npb;
-            int64_t alive = 0;
-            for (int kl = 0; kl < nkl; kl++) {
-                double ck = pb[kl].cce;
-                if (ck > P->expcutoff) continue;
-                for (int ij = 0; ij < nij; ij++)
-                    if (!(pa[ij].cce > P->expcutoff - ck)) alive++;
-            }
-            npq_alive += alive;
-            fl += alive * flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode);
+    /* Screening on the host with libcint's rule and loop order (src/cint2e.c:400-425: kl outer,
+     * ij inner; skip kl if cce_kl > cutoff, skip ij if cce_ij > cutoff - cce_kl): the kernels get
+     * the surviving primitive quartets as a list, so work can be sliced evenly. */
+    struct Work { int pe; int64_t off, n; double cost_pq; };
+    std::vector<Work> work;
+    work.reserve(pend.size());
+    double fl = 0;
+    for (size_t w = 0; w < pend.size(); w++) {
+        const Pending &pe = pend[w];
+        const CGPair &a = P->pairs[pe.pij], &b = P->pairs[pe.pkl];
+        const CGPrimPair *pa = &P->prims[a.prim_off], *pb = &P->prims[b.prim_off];
+        int nij = a.npa * a.npb, nkl = b.npa * b.npb;
+        int64_t off = (int64_t)P->pqlist.size();
+        for (int kl = 0; kl < nkl; kl++) {
+            double ck = pb[kl].cce;
+            if (ck > P->expcutoff) continue;
+            for (int ij = 0; ij < nij; ij++)
+                if (!(pa[ij].cce > P->expcutoff - ck)) P->pqlist.push_back(kl * nij + ij);
         }
-        P->flops = fl;
-        P->prim_quartets = npq_alive;
+        int64_t n = (int64_t)P->pqlist.size() - off;
+        double cpq = flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode);
+        fl += n * cpq;
+        if (n > 0) work.push_back({(int)w, off, n, cpq});
     }
-    /* split big quartets into primitive-quartet slices if there are too few tasks */
-    int64_t chunk = 0;
-    if (split_target > 0 && (int64_t)pend.size() < split_target) {
-        int64_t tot = 0;
-        for (const Pending &pe : pend) tot += pe.npq;
-        chunk = std::max<int64_t>(32, ((tot / std::max<int64_t>(split_target, 1)) + 31) / 32 * 32);
-    }
-    /* group by class, most expensive classes first */
-    std::vector<int> order(pend.size());
-    for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
-    auto ckey = [&](const Pending &p) { return ((p.l[0] * 16 + p.l[1]) * 16 + p.l[2]) * 16 + p.l[3]; };
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-        int kx = ckey(pend[x]), ky = ckey(pend[y]);
-        if (kx != ky) return kx > ky;
-        return pend[x].npq > pend[y].npq;
-    });
+    if (P->pqlist.size() > (size_t)INT32_MAX) { set_error("too many primitive quartets in one plan"); return CINTGPU_ERR_ARG; }
+    P->flops = fl;
+    P->prim_quartets = (int64_t)P->pqlist.size();
+    /* slices: no task above ~1/32 of a warp's fair share (or 32 primitive quartets) */
+    const double warps = (double)std::max(1, g_ctx.sm_count) * 8.0;
+    double target = std::max(fl / (warps * 32.0), 2.0e5);
+    if (split_target > 0) target = std::min(target, fl / (double)split_target);
+    struct TaskCost { CGTask t; double cost; int group; };
+    std::vector<TaskCost> tc;
     int64_t gpos = 0;
-    int cur_key = -1;
-    for (int idx : order) {
-        const Pending &pe = pend[idx];
-        int key = ckey(pe);
-        if (key != cur_key) {
-            ClassLaunch cl;
-            for (int k = 0; k < 4; k++) cl.l[k] = pe.l[k];
-            cl.task0 = (int)P->tasks.size();
-            cl.ntasks = 0;
-            CGLayout L;
-            cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_SMALL, &L);
-            cl.ws = CG_WS_SMALL; cl.blocks_per_sm = 2;
-            if (L.T < 4) {
-                cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_MAX, &L);
-                cl.ws = CG_WS_MAX; cl.blocks_per_sm = 1;
-            }
-            if (L.nroots > cg_rys_nmax() || L.T < 1 || std::max(L.nmax, L.mmax) > 2 * CG_MAXL) {
-                set_error("class (%d %d|%d %d) beyond the kernel limits (nroots %d, max %d)",
-                          pe.l[0], pe.l[1], pe.l[2], pe.l[3], L.nroots, cg_rys_nmax());
-                return CINTGPU_ERR_UNSUPPORTED;
-            }
-            cl.common = M_PI * M_PI * M_PI * 2 / 1.7724538509055160272981674833411451
-                      * common_fac_sp(pe.l[0]) * common_fac_sp(pe.l[1]) * common_fac_sp(pe.l[2])
-                      * (P->three ? 1.0 : common_fac_sp(pe.l[3]));
-            P->classes.push_back(cl);
-            cur_key = key;
+    for (const Work &w : work) {
+        const Pending &pe = pend[w.pe];
+        CGLayout L;
+        cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_SMALL, &L);
+        int group = 0;
+        if (L.T < 2) {
+            cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_MAX, &L);
+            group = 1;
         }
+        if (L.nroots > cg_rys_nmax() || L.T < 1 || L.G >= 1024) {
+            set_error("class (%d %d|%d %d) beyond the kernel limits (nroots %d, max %d)",
+                      pe.l[0], pe.l[1], pe.l[2], pe.l[3], L.nroots, cg_rys_nmax());
+            return CINTGPU_ERR_UNSUPPORTED;
+        }
+        int64_t slice = std::max<int64_t>(32, (int64_t)(target / w.cost_pq));
         int nf = ncart_l(pe.l[0]) * ncart_l(pe.l[1]) * ncart_l(pe.l[2]) * ncart_l(pe.l[3]);
         int64_t slot = (int64_t)nf * P->ncomp;
-        int64_t c = chunk > 0 ? chunk : pe.npq;
         CGOutTask &o = P->outs[pe.out];
         o.cart_off = gpos;
-        for (int64_t a = 0; a < pe.npq; a += c) {
-            CGTask t;
-            t.pij = pe.pij; t.pkl = pe.pkl;
-            t.pq0 = (int)a; t.pq1 = (int)std::min<int64_t>(pe.npq, a + c);
-            t.cart_off = gpos;
-            t.out = pe.out;
-            t.pad = 0;
-            P->tasks.push_back(t);
-            P->classes.back().ntasks++;
+        for (int64_t a0 = 0; a0 < w.n; a0 += slice) {
+            TaskCost x;
+            x.t.pij = pe.pij; x.t.pkl = pe.pkl;
+            x.t.pq_off = (int)(w.off + a0);
+            x.t.npq = (int)std::min<int64_t>(slice, w.n - a0);
+            x.t.cart_off = gpos;
+            x.t.out = pe.out;
+            x.t.pad = 0;
+            x.cost = x.t.npq * w.cost_pq;
+            x.group = group;
+            tc.push_back(x);
             o.nparts++;
             gpos += slot;
         }
+    }
+    /* longest tasks first within each launch (LPT order for the dynamic work counter) */
+    std::stable_sort(tc.begin(), tc.end(), [](const TaskCost &x, const TaskCost &y) {
+        if (x.group != y.group) return x.group < y.group;
+        return x.cost > y.cost;
+    });
+    P->tasks.reserve(tc.size());
+    for (int g = 0; g < 2; g++) {
+        P->groups[g].task0 = (int)P->tasks.size();
+        for (const TaskCost &x : tc)
+            if (x.group == g) P->tasks.push_back(x.t);
+        P->groups[g].ntasks = (int)P->tasks.size() - P->groups[g].task0;
+        P->groups[g].ws = g == 0 ? CG_WS_SMALL : CG_WS_MAX;
+        P->groups[g].blocks_per_sm = g == 0 ? 2 : 1;
     }
     P->gctr_size = std::max<int64_t>(gpos, 1);
     return 0;
 }
 
+struct DevLayout {
+    size_t pairs, prims, tasks, outs, pq, gctr, cnt, ne, scr;
+    size_t upload, total;
+    int out_blocks;
+    int64_t spw;
+};
+
+static DevLayout dev_layout(const CINTGPUPlan *P)
+{
+    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+    DevLayout D;
+    D.out_blocks = std::max(1, std::min<int>((int)((P->outs.size() + 3) / 4), g_ctx.sm_count * 8));
+    D.spw = 2 * (int64_t)P->max_nf;
+    D.pairs = al(sizeof(CGPair) * std::max<size_t>(P->pairs.size(), 1));
+    D.prims = al(sizeof(CGPrimPair) * std::max<size_t>(P->prims.size(), 1));
+    D.tasks = al(sizeof(CGTask) * std::max<size_t>(P->tasks.size(), 1));
+    D.outs = al(sizeof(CGOutTask) * std::max<size_t>(P->outs.size(), 1));
+    D.pq = al(sizeof(int) * std::max<size_t>(P->pqlist.size(), 1));
+    D.gctr = al(sizeof(double) * P->gctr_size);
+    D.cnt = al(sizeof(int) * 4);
+    D.ne = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
+    D.scr = al(sizeof(double) * D.spw * D.out_blocks * 4);
+    D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq;
+    D.total = D.upload + D.gctr + D.cnt + D.ne + D.scr;
+    return D;
+}
+
+static size_t plan_device_bytes(const CINTGPUPlan *P) { return dev_layout(P).total; }
+static size_t plan_upload_bytes(const CINTGPUPlan *P) { return dev_layout(P).upload; }
+
+/* Place the plan in device memory (a caller arena or its own allocation) and copy the host
+ * images: pinned + async on `stream` for the drop-in, synchronous otherwise. */
 static int upload_plan(CINTGPUPlan *P, char *arena, size_t arena_size, cudaStream_t stream,
                        bool async_from_pinned, char *pinned)
 {
-    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
-    int sm = g_ctx.sm_count;
-    P->out_blocks = std::max(1, std::min<int>((int)((P->outs.size() + 3) / 4), sm * 8));
-    P->scratch_per_warp = 2 * (int64_t)P->max_nf;
-    size_t sz_pairs = al(sizeof(CGPair) * std::max<size_t>(P->pairs.size(), 1));
-    size_t sz_prims = al(sizeof(CGPrimPair) * std::max<size_t>(P->prims.size(), 1));
-    size_t sz_tasks = al(sizeof(CGTask) * std::max<size_t>(P->tasks.size(), 1));
-    size_t sz_outs = al(sizeof(CGOutTask) * std::max<size_t>(P->outs.size(), 1));
-    size_t sz_gctr = al(sizeof(double) * P->gctr_size);
-    size_t sz_cnt = al(sizeof(int) * std::max<size_t>(P->classes.size(), 1));
-    size_t sz_ne = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
-    size_t sz_scr = al(sizeof(double) * P->scratch_per_warp * P->out_blocks * 4);
-    size_t upload = sz_pairs + sz_prims + sz_tasks + sz_outs;
-    size_t total = upload + sz_gctr + sz_cnt + sz_ne + sz_scr;
+    DevLayout D = dev_layout(P);
+    P->out_blocks = D.out_blocks;
+    P->scratch_per_warp = D.spw;
     if (arena) {
-        if (total > arena_size) { set_error("arena too small"); return CINTGPU_ERR_NOMEM; }
+        if (D.total > arena_size) { set_error("arena too small"); return CINTGPU_ERR_NOMEM; }
         P->dbuf = arena; P->dbuf_size = arena_size; P->owns_dbuf = false;
     } else {
-        cudaError_t e = cudaMalloc(&P->dbuf, total);
+        cudaError_t e = cudaMalloc(&P->dbuf, D.total);
         if (e != cudaSuccess) {
-            set_error("cudaMalloc(%zu) failed: %s", total, cudaGetErrorString(e));
+            set_error("cudaMalloc(%zu) failed: %s", D.total, cudaGetErrorString(e));
             P->dbuf = nullptr;
             return CINTGPU_ERR_NOMEM;
         }
-        P->dbuf_size = total; P->owns_dbuf = true;
+        P->dbuf_size = D.total; P->owns_dbuf = true;
     }
     char *p = P->dbuf;
-    P->d_pairs = (CGPair *)p; p += sz_pairs;
-    P->d_prims = (CGPrimPair *)p; p += sz_prims;
-    P->d_tasks = (CGTask *)p; p += sz_tasks;
-    P->d_outs = (CGOutTask *)p; p += sz_outs;
-    P->d_gctr = (double *)p; p += sz_gctr;
-    P->d_counters = (int *)p; p += sz_cnt;
-    P->d_nonempty = (int *)p; p += sz_ne;
-    P->d_scratch = (double *)p; p += sz_scr;
-    /* stage the four host images contiguously, then one copy */
+    P->d_pairs = (CGPair *)p; p += D.pairs;
+    P->d_prims = (CGPrimPair *)p; p += D.prims;
+    P->d_tasks = (CGTask *)p; p += D.tasks;
+    P->d_outs = (CGOutTask *)p; p += D.outs;
+    P->d_pqlist = (int *)p; p += D.pq;
+    P->d_gctr = (double *)p; p += D.gctr;
+    P->d_counters = (int *)p; p += D.cnt;
+    P->d_nonempty = (int *)p; p += D.ne;
+    P->d_scratch = (double *)p; p += D.scr;
     std::vector<char> tmp;
     char *src;
     if (async_from_pinned) src = pinned;
-    else { tmp.resize(upload); src = tmp.data(); }
+    else { tmp.resize(D.upload); src = tmp.data(); }
     char *q = src;
-    memcpy(q, P->pairs.data(), sizeof(CGPair) * P->pairs.size()); q += sz_pairs;
-    memcpy(q, P->prims.data(), sizeof(CGPrimPair) * P->prims.size()); q += sz_prims;
-    memcpy(q, P->tasks.data(), sizeof(CGTask) * P->tasks.size()); q += sz_tasks;
-    memcpy(q, P->outs.data(), sizeof(CGOutTask) * P->outs.size()); q += sz_outs;
+    memcpy(q, P->pairs.data(), sizeof(CGPair) * P->pairs.size()); q += D.pairs;
+    memcpy(q, P->prims.data(), sizeof(CGPrimPair) * P->prims.size()); q += D.prims;
+    memcpy(q, P->tasks.data(), sizeof(CGTask) * P->tasks.size()); q += D.tasks;
+    memcpy(q, P->outs.data(), sizeof(CGOutTask) * P->outs.size()); q += D.outs;
+    memcpy(q, P->pqlist.data(), sizeof(int) * P->pqlist.size()); q += D.pq;
     if (async_from_pinned) {
-        CUDA_OK(cudaMemcpyAsync(P->dbuf, src, upload, cudaMemcpyHostToDevice, stream));
+        CUDA_OK(cudaMemcpyAsync(P->dbuf, src, D.upload, cudaMemcpyHostToDevice, stream));
     } else {
-        CUDA_OK(cudaMemcpy(P->dbuf, src, upload, cudaMemcpyHostToDevice));
+        CUDA_OK(cudaMemcpy(P->dbuf, src, D.upload, cudaMemcpyHostToDevice));
     }
     return 0;
 }
 
-static size_t plan_device_bytes(const CINTGPUPlan *P)
+static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
 {
-    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
-    int sm = g_ctx.sm_count;
-    int ob = std::max(1, std::min<int>((int)((P->outs.size() + 3) / 4), sm * 8));
-    return al(sizeof(CGPair) * std::max<size_t>(P->pairs.size(), 1))
-         + al(sizeof(CGPrimPair) * std::max<size_t>(P->prims.size(), 1))
-         + al(sizeof(CGTask) * std::max<size_t>(P->tasks.size(), 1))
-         + al(sizeof(CGOutTask) * std::max<size_t>(P->outs.size(), 1))
-         + al(sizeof(double) * P->gctr_size)
-         + al(sizeof(int) * std::max<size_t>(P->classes.size(), 1))
-         + al(sizeof(int) * std::max<size_t>(P->outs.size(), 1))
-         + al(sizeof(double) * 2 * (int64_t)P->max_nf * ob * 4);
+    const TaskGroup &G = P->groups[g];
+    if (G.ntasks == 0) return 0;
+    CGLaunch L;
+    L.tasks = P->d_tasks;
+    L.task0 = G.task0;
+    L.ntasks = G.ntasks;
+    L.pairs = P->d_pairs;
+    L.prims = P->d_prims;
+    L.pqlist = P->d_pqlist;
+    L.gctr = P->d_gctr;
+    L.counter = P->d_counters + g;
+    L.nonempty = P->d_nonempty;
+    L.status = P->d_counters + 2;
+    L.rys_coef = g_ctx.rys_coef;
+    L.common_base = M_PI * M_PI * M_PI * 2 / 1.7724538509055160272981674833411451;
+    L.three = P->three;
+    L.ws_doubles = G.ws;
+    int nblocks = std::min(g_ctx.sm_count * G.blocks_per_sm, std::max(1, (G.ntasks + 3) / 4));
+    int rc = cg_launch_eri(&L, P->mode, nblocks, stream);
+    if (rc) { set_error("ERI kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
+    return 0;
 }
 
-static size_t plan_upload_bytes(const CINTGPUPlan *P)
-{
-    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
-    return al(sizeof(CGPair) * std::max<size_t>(P->pairs.size(), 1))
-         + al(sizeof(CGPrimPair) * std::max<size_t>(P->prims.size(), 1))
-         + al(sizeof(CGTask) * std::max<size_t>(P->tasks.size(), 1))
-         + al(sizeof(CGOutTask) * std::max<size_t>(P->outs.size(), 1));
-}
-
+/* memsets, the two task groups (concurrently when the plan owns a side stream), the output
+ * kernel.  Everything is enqueued on `stream`; nothing synchronises with the host. */
 static int execute_plan(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
 {
     CUDA_OK(cudaMemsetAsync(P->d_nonempty, 0, sizeof(int) * std::max<size_t>(P->outs.size(), 1), stream));
-    CUDA_OK(cudaMemsetAsync(P->d_counters, 0, sizeof(int) * std::max<size_t>(P->classes.size(), 1), stream));
-    int sm = g_ctx.sm_count;
-    for (size_t c = 0; c < P->classes.size(); c++) {
-        const ClassLaunch &cl = P->classes[c];
-        CGLaunch L;
-        L.tasks = P->d_tasks;
-        L.task0 = cl.task0;
-        L.ntasks = cl.ntasks;
-        L.pairs = P->d_pairs;
-        L.prims = P->d_prims;
-        L.gctr = P->d_gctr;
-        L.counter = P->d_counters + c;
-        L.nonempty = P->d_nonempty;
-        L.rys_coef = g_ctx.rys_coef;
-        L.common = cl.common;
-        L.expcutoff = P->expcutoff;
-        L.li = cl.l[0]; L.lj = cl.l[1]; L.lk = cl.l[2]; L.ll = cl.l[3];
-        L.ws_doubles = cl.ws;
-        int warps_needed = cl.ntasks;
-        int nblocks = std::min(sm * cl.blocks_per_sm, std::max(1, (warps_needed + 3) / 4));
-        int rc = cg_launch_eri(&L, P->mode, nblocks, stream);
-        if (rc) { set_error("ERI kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
+    CUDA_OK(cudaMemsetAsync(P->d_counters, 0, sizeof(int) * 4, stream));
+    bool fork = P->side && P->groups[1].ntasks > 0 && P->groups[0].ntasks > 0;
+    if (fork) {
+        CUDA_OK(cudaEventRecord(P->ev_fork, stream));
+        CUDA_OK(cudaStreamWaitEvent(P->side, P->ev_fork, 0));
+        int rc = launch_group(P, 1, P->side);
+        if (rc) return rc;
+        CUDA_OK(cudaEventRecord(P->ev_join, P->side));
+        rc = launch_group(P, 0, stream);
+        if (rc) return rc;
+        CUDA_OK(cudaStreamWaitEvent(stream, P->ev_join, 0));
+    } else {
+        int rc = launch_group(P, 1, stream);
+        if (!rc) rc = launch_group(P, 0, stream);
+        if (rc) return rc;
     }
     int rc = cg_launch_output(P->d_outs, (int)P->outs.size(), P->d_gctr, P->d_nonempty, P->d_scratch,
                               P->scratch_per_warp, P->out_blocks, out_dev, P->ncomp, P->out_size, stream);
@@ -873,6 +897,12 @@ int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n
     int64_t target = n < (int64_t)g_ctx.sm_count * 16 ? (int64_t)g_ctx.sm_count * 8 : 0;
     rc = build_plan(P, kind, shls, n, offsets, atm, natm, bas, nbas, env, target);
     if (!rc) rc = upload_plan(P, nullptr, 0, 0, false, nullptr);
+    if (!rc && (cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking) != cudaSuccess
+                || cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming) != cudaSuccess
+                || cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming) != cudaSuccess)) {
+        set_error("stream/event creation failed");
+        rc = CINTGPU_ERR_CUDA;
+    }
     if (rc) { free_plan_device(P); delete P; return rc; }
     *plan = P;
     return 0;
@@ -882,7 +912,11 @@ int64_t cintgpu_plan_output_size(const CINTGPUPlan *plan) { return plan->out_siz
 int cintgpu_plan_ncomp(const CINTGPUPlan *plan) { return plan->ncomp; }
 double cintgpu_plan_flops(const CINTGPUPlan *plan) { return plan->flops; }
 int64_t cintgpu_plan_prim_quartets(const CINTGPUPlan *plan) { return plan->prim_quartets; }
-int cintgpu_plan_launches(const CINTGPUPlan *plan) { return (int)plan->classes.size() + 1; }
+int cintgpu_plan_launches(const CINTGPUPlan *plan)
+{
+    return (plan->groups[0].ntasks > 0) + (plan->groups[1].ntasks > 0) + 1;
+}
+int64_t cintgpu_plan_upload_bytes(const CINTGPUPlan *plan) { return (int64_t)plan_upload_bytes(plan); }
 
 int cintgpu_plan_execute(CINTGPUPlan *plan, double *out_dev, void *stream)
 {

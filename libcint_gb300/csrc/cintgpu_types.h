@@ -36,7 +36,8 @@ typedef struct {
 
 typedef struct {
     int pij, pkl;        /* bra / ket pair indices */
-    int pq0, pq1;        /* primitive-quartet range [pq0, pq1), pq = kl * nij + ij */
+    int pq_off, npq;     /* surviving primitive quartets pqlist[pq_off .. pq_off+npq),
+                            each encoded kl * nij + ij */
     int64_t cart_off;    /* accumulator slot in gctr */
     int out;             /* CGOutTask index (for the non-empty flag) */
     int pad;

@@ -62,7 +62,7 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     L->nf = ncart(li) * ncart(lj) * ncart(lk) * ncart(ll);
     L->ncomp = (mode == CG_MODE_IP1) ? 3 : 1;
     L->scr = (L->nmax + 1) * (L->mmax + 1) + L->dI * L->dJ * (L->mmax + 1) + (L->nmax + 1);
-    int fixed = CG_TERMW * 32 + 16;  /* term records + survivor list */
+    int fixed = CG_TERMW * 32;       /* term records */
     int avail = ws_doubles - fixed;
     /* T terms need T*3*ng*G doubles of g arrays and min(32, 3T) lane scratch areas */
     int T = 0;
@@ -189,6 +189,192 @@ __device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10
 }
 
 /* ------------------------------------------------------------------ main kernel */
+__device__ __forceinline__ double common_fac_sp(int l)   /* libcint src/g1e.c:565-572 */
+{
+    return l == 0 ? 0.282094791773878143 : (l == 1 ? 0.488602511902919921 : 1.0);
+}
+
+/* One task: a slice of the surviving primitive quartets of one contracted quartet.
+ * NS > 0: lane-private register accumulators for components c = lane + 32 s, s < NS
+ * NS = 0: accumulators in the task's gctr slot (large classes). */
+template <int MODE, int NS>
+__device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, const CGLayout &L,
+                                         double *term, double *greg, int lane)
+{
+    const CGPair pij = P.pairs[tk.pij];
+    const CGPair pkl = P.pairs[tk.pkl];
+    const CGPrimPair *__restrict__ ppij = P.prims + pij.prim_off;
+    const CGPrimPair *__restrict__ ppkl = P.prims + pkl.prim_off;
+    const int *__restrict__ pql = P.pqlist + tk.pq_off;
+    const int nij = pij.npa * pij.npb;
+    const int li = pij.la, lj = pij.lb, lk = pkl.la, ll = pkl.lb;
+    const int nfi = ncart(li), nfj = ncart(lj), nfk = ncart(lk), nfl = ncart(ll);
+    const int n = L.nroots;
+    const int T = L.T;
+    const double common = P.common_base * common_fac_sp(li) * common_fac_sp(lj)
+                        * common_fac_sp(lk) * (P.three ? 1.0 : common_fac_sp(ll));
+    double *scr_base = greg + T * 3 * L.ng * L.G;
+    double *acc = P.gctr + tk.cart_off;
+
+    /* per-lane component offsets into the g arrays, packed 10 bits per axis */
+    int offs[NS > 0 ? NS : 1];
+    double ra[NS > 0 ? NS : 1][MODE == CG_MODE_IP1 ? 3 : 1];
+    auto comp_offsets = [&](int c) -> int {
+        int ic = c % nfi, rest = c / nfi;
+        int kc = rest % nfk; rest /= nfk;
+        int lc = rest % nfl;
+        int jc = rest / nfl;
+        int ix, iy, iz, jx, jy, jz, kx, ky, kz, lx, ly, lz;
+        cart_pow(li, ic, ix, iy, iz);
+        cart_pow(lj, jc, jx, jy, jz);
+        cart_pow(lk, kc, kx, ky, kz);
+        cart_pow(ll, lc, lx, ly, lz);
+        int ox = ((ix * L.dJ + jx) * L.dK + kx) * L.dL + lx;
+        int oy = ((iy * L.dJ + jy) * L.dK + ky) * L.dL + ly;
+        int oz = ((iz * L.dJ + jz) * L.dK + kz) * L.dL + lz;
+        return ox | (oy << 10) | (oz << 20);
+    };
+    if (NS > 0) {
+#pragma unroll
+        for (int s = 0; s < (NS > 0 ? NS : 1); s++) {
+            int c = lane + 32 * s;
+            offs[s] = c < L.nf ? comp_offsets(c) : 0;
+#pragma unroll
+            for (int q = 0; q < (MODE == CG_MODE_IP1 ? 3 : 1); q++) ra[s][q] = 0.0;
+        }
+    } else {
+        for (int c = lane; c < L.nf * L.ncomp; c += 32) acc[c] = 0.0;
+    }
+
+    const int nterm = tk.npq * n;
+    for (int t0 = 0; t0 < nterm; t0 += T) {
+        const int Tb = min(T, nterm - t0);
+        /* ---- stage 1: one lane per term */
+        if (lane < Tb) {
+            int g = t0 + lane;
+            int p = g / n, r = g - p * n;
+            int q = __ldg(pql + p);
+            int kl = q / nij, ij = q - kl * nij;
+            const CGPrimPair A = ppij[ij];
+            const CGPrimPair B = ppkl[kl];
+            double aijkl = A.a + B.a;
+            double rs = rsqrt(aijkl);
+            double inv = rs * rs;
+            double PQx = A.P[0] - B.P[0], PQy = A.P[1] - B.P[1], PQz = A.P[2] - B.P[2];
+            double rr = fma(PQx, PQx, fma(PQy, PQy, PQz * PQz));
+            double rho = A.a * B.a * inv;
+            double x = rho * rr;
+            double s, w;
+            rys_node(n, x, r, P.rys_coef, s, w);
+            double fac1 = common * A.K * B.K * rs * A.inv_a * B.inv_a;
+            double tb = s * inv;                 /* 2 b00 */
+            double b00 = 0.5 * tb;
+            double oms = 1.0 - s;
+            double b10 = fma(0.5 * A.inv_a, oms, b00);
+            double b01 = fma(0.5 * B.inv_a, oms, b00);
+            double ta = tb * B.a, tc = tb * A.a;
+            double *rec = term + lane * CG_TERMW;
+            rec[0] = b00; rec[1] = b10; rec[2] = b01;
+            rec[3] = fma(-ta, PQx, A.P[0] - pij.A[0]);
+            rec[4] = fma(-ta, PQy, A.P[1] - pij.A[1]);
+            rec[5] = fma(-ta, PQz, A.P[2] - pij.A[2]);
+            rec[6] = fma(tc, PQx, B.P[0] - pkl.A[0]);
+            rec[7] = fma(tc, PQy, B.P[1] - pkl.A[1]);
+            rec[8] = fma(tc, PQz, B.P[2] - pkl.A[2]);
+            rec[9] = w * fac1;
+            rec[10] = -2.0 * A.aA;
+        }
+        __syncwarp();
+        /* ---- stage 2: one lane per (term, axis) */
+        for (int item = lane; item < 3 * Tb; item += 32) {
+            int t = item / 3, ax = item - 3 * t;
+            const double *rec = term + t * CG_TERMW;
+            double g00 = (ax == 2) ? rec[9] : 1.0;
+            double *gdst = greg + (size_t)(t * 3 + ax) * L.ng * L.G;
+            g_axis(L, rec[0], rec[1], rec[2], rec[3 + ax], rec[6 + ax], g00,
+                   pij.AB[ax], pkl.AB[ax], scr_base + lane * L.scr, gdst);
+            if (MODE == CG_MODE_IP1) {
+                /* f(i) = i g(i-1) - 2 a_i g(i+1)   (CINTnabla1i_2e, src/g2e.c:4550-4591) */
+                const double ai2 = rec[10];
+                const int sI = L.dJ * L.dK * L.dL;
+                double *f = gdst + L.G;
+                for (int i = 0; i < L.dI - 1; i++) {
+                    for (int o = 0; o < sI; o++) {
+                        double v = ai2 * gdst[(i + 1) * sI + o];
+                        if (i > 0) v = fma((double)i, gdst[(i - 1) * sI + o], v);
+                        f[i * sI + o] = v;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        /* ---- stage 3: one lane per Cartesian component */
+        const int stride_t = 3 * L.ng * L.G;
+        const int G = L.G;
+        if (NS > 0) {
+#pragma unroll
+            for (int s = 0; s < (NS > 0 ? NS : 1); s++) {
+                if (lane + 32 * s >= L.nf) continue;
+                const int ox = offs[s] & 1023, oy = (offs[s] >> 10) & 1023, oz = offs[s] >> 20;
+                const double *gb = greg;
+                if (MODE == CG_MODE_ERI) {
+                    double s0 = ra[s][0];
+                    for (int t = 0; t < Tb; t++, gb += stride_t)
+                        s0 = fma(gb[ox] * gb[G + oy], gb[2 * G + oz], s0);
+                    ra[s][0] = s0;
+                } else {
+                    double sx = ra[s][0], sy = ra[s][MODE == CG_MODE_IP1 ? 1 : 0],
+                           sz = ra[s][MODE == CG_MODE_IP1 ? 2 : 0];
+                    for (int t = 0; t < Tb; t++, gb += stride_t) {
+                        double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
+                        double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
+                        sx = fma(fx, gy * gz, sx);
+                        sy = fma(fy, gx * gz, sy);
+                        sz = fma(fz, gx * gy, sz);
+                    }
+                    ra[s][0] = sx;
+                    ra[s][MODE == CG_MODE_IP1 ? 1 : 0] = sy;
+                    ra[s][MODE == CG_MODE_IP1 ? 2 : 0] = sz;
+                }
+            }
+        } else {
+            for (int c = lane; c < L.nf; c += 32) {
+                const int o3 = comp_offsets(c);
+                const int ox = o3 & 1023, oy = (o3 >> 10) & 1023, oz = o3 >> 20;
+                const double *gb = greg;
+                if (MODE == CG_MODE_ERI) {
+                    double s0 = acc[c];
+                    for (int t = 0; t < Tb; t++, gb += stride_t)
+                        s0 = fma(gb[ox] * gb[G + oy], gb[2 * G + oz], s0);
+                    acc[c] = s0;
+                } else {
+                    double sx = acc[c], sy = acc[L.nf + c], sz = acc[2 * L.nf + c];
+                    for (int t = 0; t < Tb; t++, gb += stride_t) {
+                        double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
+                        double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
+                        sx = fma(fx, gy * gz, sx);
+                        sy = fma(fy, gx * gz, sy);
+                        sz = fma(fz, gx * gy, sz);
+                    }
+                    acc[c] = sx; acc[L.nf + c] = sy; acc[2 * L.nf + c] = sz;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (NS > 0) {
+#pragma unroll
+        for (int s = 0; s < (NS > 0 ? NS : 1); s++) {
+            int c = lane + 32 * s;
+            if (c < L.nf) {
+#pragma unroll
+                for (int q = 0; q < (MODE == CG_MODE_IP1 ? 3 : 1); q++) acc[q * L.nf + c] = ra[s][q];
+            }
+        }
+    }
+    if (lane == 0) P.nonempty[tk.out] = 1;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(128)
 rys_eri_kernel(CGLaunch P)
@@ -198,17 +384,7 @@ rys_eri_kernel(CGLaunch P)
     const int warp = threadIdx.x >> 5;
     double *ws = smem + (size_t)warp * P.ws_doubles;
     double *term = ws;                                   /* CG_TERMW * 32 */
-    int *surv = reinterpret_cast<int *>(ws + CG_TERMW * 32);
-    double *greg = ws + CG_TERMW * 32 + 16;
-
-    CGLayout L;
-    cg_class_layout(P.li, P.lj, P.lk, P.ll, MODE, P.ws_doubles, &L);
-    const int T = L.T;
-    double *scr_base = greg + T * 3 * L.ng * L.G;
-    const int n = L.nroots;
-    const int nfi = ncart(P.li), nfj = ncart(P.lj), nfk = ncart(P.lk), nfl = ncart(P.ll);
-    const double common = P.common;
-    const double expcut = P.expcutoff;
+    double *greg = ws + CG_TERMW * 32;
 
     for (;;) {
         int tid = 0;
@@ -216,136 +392,21 @@ rys_eri_kernel(CGLaunch P)
         tid = __shfl_sync(FULL, tid, 0);
         if (tid >= P.ntasks) break;
         const CGTask tk = P.tasks[P.task0 + tid];
-        const CGPair pij = P.pairs[tk.pij];
-        const CGPair pkl = P.pairs[tk.pkl];
-        const CGPrimPair *__restrict__ ppij = P.prims + pij.prim_off;
-        const CGPrimPair *__restrict__ ppkl = P.prims + pkl.prim_off;
-        const int nij = pij.npa * pij.npb;
-        double *acc = P.gctr + tk.cart_off;
-        for (int c = lane; c < L.nf * L.ncomp; c += 32) acc[c] = 0.0;
-        bool any = false;
-
-        for (int base = tk.pq0; base < tk.pq1; base += 32) {
-            /* ---- screening (libcint SET_RIJ / eijcutoff rule) */
-            int pq = base + lane;
-            bool alive = false;
-            if (pq < tk.pq1) {
-                int kl = pq / nij, ij = pq - kl * nij;
-                double ccekl = ppkl[kl].cce;
-                if (!(ccekl > expcut)) {
-                    double ccij = ppij[ij].cce;
-                    alive = !(ccij > expcut - ccekl);
-                }
-            }
-            unsigned mask = __ballot_sync(FULL, alive);
-            int ns = __popc(mask);
-            if (alive) surv[__popc(mask & ((1u << lane) - 1u))] = pq;
-            __syncwarp();
-            if (ns == 0) continue;
-            any = true;
-            const int nterm = ns * n;
-            for (int t0 = 0; t0 < nterm; t0 += T) {
-                const int Tb = min(T, nterm - t0);
-                /* ---- stage 1: one lane per term */
-                if (lane < Tb) {
-                    int g = t0 + lane;
-                    int p = g / n, r = g - p * n;
-                    int q = surv[p];
-                    int kl = q / nij, ij = q - kl * nij;
-                    const CGPrimPair A = ppij[ij];
-                    const CGPrimPair B = ppkl[kl];
-                    double aijkl = A.a + B.a;
-                    double rs = rsqrt(aijkl);
-                    double inv = rs * rs;
-                    double PQx = A.P[0] - B.P[0], PQy = A.P[1] - B.P[1], PQz = A.P[2] - B.P[2];
-                    double rr = fma(PQx, PQx, fma(PQy, PQy, PQz * PQz));
-                    double rho = A.a * B.a * inv;
-                    double x = rho * rr;
-                    double s, w;
-                    rys_node(n, x, r, P.rys_coef, s, w);
-                    double fac1 = common * A.K * B.K * rs * A.inv_a * B.inv_a;
-                    double tb = s * inv;                 /* 2 b00 */
-                    double b00 = 0.5 * tb;
-                    double oms = 1.0 - s;
-                    double b10 = fma(0.5 * A.inv_a, oms, b00);
-                    double b01 = fma(0.5 * B.inv_a, oms, b00);
-                    double ta = tb * B.a, tc = tb * A.a;
-                    double *rec = term + lane * CG_TERMW;
-                    rec[0] = b00; rec[1] = b10; rec[2] = b01;
-                    rec[3] = fma(-ta, PQx, A.P[0] - pij.A[0]);
-                    rec[4] = fma(-ta, PQy, A.P[1] - pij.A[1]);
-                    rec[5] = fma(-ta, PQz, A.P[2] - pij.A[2]);
-                    rec[6] = fma(tc, PQx, B.P[0] - pkl.A[0]);
-                    rec[7] = fma(tc, PQy, B.P[1] - pkl.A[1]);
-                    rec[8] = fma(tc, PQz, B.P[2] - pkl.A[2]);
-                    rec[9] = w * fac1;
-                    rec[10] = -2.0 * A.aA;
-                }
-                __syncwarp();
-                /* ---- stage 2: one lane per (term, axis) */
-                for (int item = lane; item < 3 * Tb; item += 32) {
-                    int t = item / 3, ax = item - 3 * t;
-                    const double *rec = term + t * CG_TERMW;
-                    double g00 = (ax == 2) ? rec[9] : 1.0;
-                    double *gdst = greg + (size_t)(t * 3 + ax) * L.ng * L.G;
-                    g_axis(L, rec[0], rec[1], rec[2], rec[3 + ax], rec[6 + ax], g00,
-                           pij.AB[ax], pkl.AB[ax], scr_base + lane * L.scr, gdst);
-                    if (MODE == CG_MODE_IP1) {
-                        /* f(i) = i g(i-1) - 2 a_i g(i+1)   (CINTnabla1i_2e, src/g2e.c:4550-4591) */
-                        const double ai2 = rec[10];
-                        const int sI = L.dJ * L.dK * L.dL;
-                        double *f = gdst + L.G;
-                        for (int i = 0; i < L.dI - 1; i++) {
-                            for (int o = 0; o < sI; o++) {
-                                double v = ai2 * gdst[(i + 1) * sI + o];
-                                if (i > 0) v = fma((double)i, gdst[(i - 1) * sI + o], v);
-                                f[i * sI + o] = v;
-                            }
-                        }
-                    }
-                }
-                __syncwarp();
-                /* ---- stage 3: one lane per Cartesian component */
-                const int stride_t = 3 * L.ng * L.G;
-                for (int c = lane; c < L.nf; c += 32) {
-                    int ic = c % nfi, rest = c / nfi;
-                    int kc = rest % nfk; rest /= nfk;
-                    int lc = rest % nfl;
-                    int jc = rest / nfl;
-                    int ix, iy, iz, jx, jy, jz, kx, ky, kz, lx, ly, lz;
-                    cart_pow(P.li, ic, ix, iy, iz);
-                    cart_pow(P.lj, jc, jx, jy, jz);
-                    cart_pow(P.lk, kc, kx, ky, kz);
-                    cart_pow(P.ll, lc, lx, ly, lz);
-                    int ox = ((ix * L.dJ + jx) * L.dK + kx) * L.dL + lx;
-                    int oy = ((iy * L.dJ + jy) * L.dK + ky) * L.dL + ly;
-                    int oz = ((iz * L.dJ + jz) * L.dK + kz) * L.dL + lz;
-                    if (MODE == CG_MODE_ERI) {
-                        double s0 = acc[c];
-                        const double *gb = greg;
-                        for (int t = 0; t < Tb; t++, gb += stride_t) {
-                            s0 = fma(gb[ox] * gb[L.G + oy], gb[2 * L.G + oz], s0);
-                        }
-                        acc[c] = s0;
-                    } else {
-                        double sx = acc[c], sy = acc[L.nf + c], sz = acc[2 * L.nf + c];
-                        const double *gb = greg;
-                        const int G = L.G;
-                        for (int t = 0; t < Tb; t++, gb += stride_t) {
-                            /* axis a block: g at gb + a*2G, f at gb + a*2G + G */
-                            double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
-                            double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
-                            sx = fma(fx, gy * gz, sx);
-                            sy = fma(fy, gx * gz, sy);
-                            sz = fma(fz, gx * gy, sz);
-                        }
-                        acc[c] = sx; acc[L.nf + c] = sy; acc[2 * L.nf + c] = sz;
-                    }
-                }
-                __syncwarp();
-            }
+        const int la = P.pairs[tk.pij].la, lb = P.pairs[tk.pij].lb;
+        const int lc = P.pairs[tk.pkl].la, ld = P.pairs[tk.pkl].lb;
+        CGLayout L;
+        cg_class_layout(la, lb, lc, ld, MODE, P.ws_doubles, &L);
+        const int ns = (L.nf + 31) >> 5;
+        if (L.T < 1) {
+            if (lane == 0) atomicOr(P.status, 1);
+            continue;
         }
-        if (any && lane == 0) P.nonempty[tk.out] = 1;
+        if (ns <= 1) run_task<MODE, 1>(P, tk, L, term, greg, lane);
+        else if (ns <= 2) run_task<MODE, 2>(P, tk, L, term, greg, lane);
+        else if (ns <= 4) run_task<MODE, 4>(P, tk, L, term, greg, lane);
+        else if (ns <= 8) run_task<MODE, 8>(P, tk, L, term, greg, lane);
+        else if (ns <= 16 && MODE == CG_MODE_ERI) run_task<MODE, 16>(P, tk, L, term, greg, lane);
+        else run_task<MODE, 0>(P, tk, L, term, greg, lane);
     }
 }
 

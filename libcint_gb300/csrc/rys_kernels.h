@@ -22,12 +22,14 @@ typedef struct {
     int task0, ntasks;
     const CGPair *pairs;
     const CGPrimPair *prims;
+    const int *pqlist;
     double *gctr;
     int *counter;
     int *nonempty;
+    int *status;
     const double *rys_coef;
-    double common, expcutoff;
-    int li, lj, lk, ll;
+    double common_base;       /* 2 pi^3 / sqrt(pi); times the s/p factors per task */
+    int three;                /* int3c2e: the fourth shell is the unit s partner */
     int ws_doubles;
 } CGLaunch;
 
