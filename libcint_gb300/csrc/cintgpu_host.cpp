@@ -514,13 +514,19 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     const double warps = (double)std::max(1, g_ctx.sm_count) * 8.0;
     double target = std::max(fl / (warps * 32.0), 2.0e5);
     if (split_target > 0) target = std::min(target, fl / (double)split_target);
+    /* shared memory per warp of the regular group: 24 KB unless CINTGPU_WS_KB overrides (tuning) */
+    int ws_small = CG_WS_SMALL;
+    if (const char *e = getenv("CINTGPU_WS_KB")) {
+        int kb = atoi(e);
+        if (kb >= 8 && kb <= 48) ws_small = kb * 1024 / 8;
+    }
     struct TaskCost { CGTask t; double cost; int group; };
     std::vector<TaskCost> tc;
     int64_t gpos = 0;
     for (const Work &w : work) {
         const Pending &pe = pend[w.pe];
         CGLayout L;
-        cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_SMALL, &L);
+        cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, ws_small, &L);
         int group = 0;
         if (L.T < 2) {
             cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_MAX, &L);
@@ -531,7 +537,9 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
                       pe.l[0], pe.l[1], pe.l[2], pe.l[3], L.nroots, cg_rys_nmax());
             return CINTGPU_ERR_UNSUPPORTED;
         }
-        int64_t slice = std::max<int64_t>(32, (int64_t)(target / w.cost_pq));
+        /* at least one batch of terms per slice, at least 4 primitive quartets */
+        int64_t slice = std::max<int64_t>(std::max<int64_t>(4, (L.T + L.nroots - 1) / L.nroots),
+                                          (int64_t)(target / w.cost_pq));
         int nf = ncart_l(pe.l[0]) * ncart_l(pe.l[1]) * ncart_l(pe.l[2]) * ncart_l(pe.l[3]);
         int64_t slot = (int64_t)nf * P->ncomp;
         CGOutTask &o = P->outs[pe.out];
@@ -562,8 +570,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         for (const TaskCost &x : tc)
             if (x.group == g) P->tasks.push_back(x.t);
         P->groups[g].ntasks = (int)P->tasks.size() - P->groups[g].task0;
-        P->groups[g].ws = g == 0 ? CG_WS_SMALL : CG_WS_MAX;
-        P->groups[g].blocks_per_sm = g == 0 ? 2 : 1;
+        P->groups[g].ws = g == 0 ? ws_small : CG_WS_MAX;
+        P->groups[g].blocks_per_sm = cg_blocks_per_sm(P->mode, P->groups[g].ws);
     }
     P->gctr_size = std::max<int64_t>(gpos, 1);
     return 0;

@@ -1,0 +1,71 @@
+// FP64 (DFMA) and FP32 (FFMA) issue-rate microbenchmark: the denominator of the roofline that
+// bench.py reports for the Rys kernels (they are FP64-issue bound).  8 independent FMA chains per
+// thread, grids of 1-2 blocks per SM, CUDA events around one launch after a warm-up launch.
+// Build and run:  nvcc -gencode arch=compute_103a,code=sm_103a -O3 -o fp64_peak fp64_peak.cu
+#include <cstdio>
+#include <cuda_runtime.h>
+template<int NCHAIN>
+__global__ void dfma_kernel(double *out, int iters, double a, double b) {
+    double acc[NCHAIN];
+#pragma unroll
+    for (int c = 0; c < NCHAIN; c++) acc[c] = threadIdx.x * 1e-3 + c;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int c = 0; c < NCHAIN; c++) acc[c] = fma(acc[c], a, b);
+    }
+    double s = 0;
+#pragma unroll
+    for (int c = 0; c < NCHAIN; c++) s += acc[c];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+template<int NCHAIN>
+__global__ void ffma_kernel(float *out, int iters, float a, float b) {
+    float acc[NCHAIN];
+#pragma unroll
+    for (int c = 0; c < NCHAIN; c++) acc[c] = threadIdx.x * 1e-3f + c;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int c = 0; c < NCHAIN; c++) acc[c] = fmaf(acc[c], a, b);
+    }
+    float s = 0;
+#pragma unroll
+    for (int c = 0; c < NCHAIN; c++) s += acc[c];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+int main() {
+    int dev = 0; cudaDeviceProp p; cudaGetDeviceProperties(&p, dev);
+    printf("name=%s sms=%d cc=%d.%d smem/block optin=%zu regs/sm=%d l2=%d\n", p.name, p.multiProcessorCount,
+           p.major, p.minor, p.sharedMemPerBlockOptin, p.regsPerMultiprocessor, p.l2CacheSize);
+    int sms = p.multiProcessorCount;
+    double *dout; cudaMalloc(&dout, sizeof(double) * sms * 16 * 1024);
+    cudaEvent_t e0, e1; cudaEventCreate(&e0); cudaEventCreate(&e1);
+    int cfgs[][2] = {{128, 1}, {256, 1}, {256, 2}, {512, 2}, {1024, 2}, {32, 1}, {64,1}};
+    for (auto &c : cfgs) {
+        int threads = c[0], bps = c[1];
+        int blocks = sms * bps;
+        int iters = 20000;
+        dfma_kernel<8><<<blocks, threads>>>(dout, 100, 0.999, 1e-3);
+        cudaEventRecord(e0);
+        dfma_kernel<8><<<blocks, threads>>>(dout, iters, 0.999, 1e-3);
+        cudaEventRecord(e1); cudaEventSynchronize(e1);
+        float ms; cudaEventElapsedTime(&ms, e0, e1);
+        double flops = 2.0 * 8 * iters * (double)blocks * threads;
+        printf("DFMA threads=%d blocks/sm=%d : %.3f ms  %.3f TFLOP/s\n", threads, bps, ms, flops / ms / 1e9);
+    }
+    float *fout = (float*)dout;
+    for (auto &c : cfgs) {
+        int threads = c[0], bps = c[1];
+        int blocks = sms * bps;
+        int iters = 20000;
+        ffma_kernel<8><<<blocks, threads>>>(fout, 100, 0.999f, 1e-3f);
+        cudaEventRecord(e0);
+        ffma_kernel<8><<<blocks, threads>>>(fout, iters, 0.999f, 1e-3f);
+        cudaEventRecord(e1); cudaEventSynchronize(e1);
+        float ms; cudaEventElapsedTime(&ms, e0, e1);
+        double flops = 2.0 * 8 * iters * (double)blocks * threads;
+        printf("FFMA threads=%d blocks/sm=%d : %.3f ms  %.3f TFLOP/s\n", threads, bps, ms, flops / ms / 1e9);
+    }
+    cudaError_t err = cudaGetLastError();
+    printf("err=%s\n", cudaGetErrorString(err));
+    return err != cudaSuccess;
+}

@@ -61,7 +61,7 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     L->ng = (mode == CG_MODE_IP1) ? 2 : 1;
     L->nf = ncart(li) * ncart(lj) * ncart(lk) * ncart(ll);
     L->ncomp = (mode == CG_MODE_IP1) ? 3 : 1;
-    L->scr = (L->nmax + 1) * (L->mmax + 1) + L->dI * L->dJ * (L->mmax + 1) + (L->nmax + 1);
+    L->scr = (L->nmax + 1) * (L->mmax + 1) + (L->nmax + 1) + (L->mmax + 1);
     int fixed = CG_TERMW * 32;       /* term records */
     int avail = ws_doubles - fixed;
     /* T terms need T*3*ng*G doubles of g arrays and min(32, 3T) lane scratch areas */
@@ -127,16 +127,16 @@ __device__ __forceinline__ void cart_pow(int l, int p, int &lx, int &ly, int &lz
 }
 
 /* ------------------------------------------------------------------ stage 2 */
-/* One Cartesian axis of one term: VRR into T2[a + (nmax+1) m], transfer to (i,j) per m, then to
- * (k,l) per (i,j); final g[((i dJ + j) dK + k) dL + l] goes to gout. */
+/* One Cartesian axis of one term: VRR into T2[a + (nmax+1) m], then the two horizontal
+ * transfers; final g[((i dJ + j) dK + k) dL + l] goes to gout.  Lane scratch: T2, a*b00, and a
+ * vector of length mmax+1. */
 __device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10, double b01,
                                        double c00, double c0p, double g00, double AB, double CD,
                                        double *scr, double *gout)
 {
     const int nmax = L.nmax, mmax = L.mmax, na = nmax + 1, nm = mmax + 1;
     double *T2 = scr;
-    double *H1 = scr + na * nm;
-    double *ab00 = H1 + L.dI * L.dJ * nm;
+    double *ab00 = scr + na * nm;
     /* a * b00 */
     {
         double acc = 0.0;
@@ -166,24 +166,29 @@ __device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10
         }
         mb += b01;
     }
-    /* (a,0| -> (i,j|  per column m, in place: col[a] = col[a+1] + AB col[a] */
-    for (int m = 0; m <= mmax; m++) {
-        double *col = T2 + m * na;
-        for (int i = 0; i < L.dI; i++) H1[(i * L.dJ) * nm + m] = col[i];
-        for (int j = 1; j < L.dJ; j++) {
-            for (int a = 0; a <= nmax - j; a++) col[a] = fma(AB, col[a], col[a + 1]);
-            for (int i = 0; i < L.dI; i++) H1[(i * L.dJ + j) * nm + m] = col[i];
+    /* (a,0| -> (i,j| one j level at a time, in place on every column m:
+     * col[a] = col[a+1] + AB col[a]; after level j, row i of all columns is g(i,j,m) and goes
+     * through |m,0) -> |k,l) in a short vector, so no (i,j,m) intermediate is stored. */
+    double *tmp = ab00 + na;
+    for (int j = 0; j < L.dJ; j++) {
+        if (j > 0) {
+            for (int m = 0; m <= mmax; m++) {
+                double *col = T2 + m * na;
+                for (int a = 0; a <= nmax - j; a++) col[a] = fma(AB, col[a], col[a + 1]);
+            }
         }
-    }
-    /* |m,0) -> |k,l) per (i,j) */
-    const int nij = L.dI * L.dJ;
-    for (int ij = 0; ij < nij; ij++) {
-        double *v = H1 + ij * nm;
-        double *go = gout + ij * L.dK * L.dL;
-        for (int k = 0; k < L.dK; k++) go[k * L.dL] = v[k];
-        for (int l = 1; l < L.dL; l++) {
-            for (int m = 0; m <= mmax - l; m++) v[m] = fma(CD, v[m], v[m + 1]);
-            for (int k = 0; k < L.dK; k++) go[k * L.dL + l] = v[k];
+        for (int i = 0; i < L.dI; i++) {
+            double *go = gout + (i * L.dJ + j) * L.dK * L.dL;
+            if (L.dL == 1) {
+                for (int k = 0; k < L.dK; k++) go[k] = T2[i + na * k];
+                continue;
+            }
+            for (int m = 0; m <= mmax; m++) tmp[m] = T2[i + na * m];
+            for (int k = 0; k < L.dK; k++) go[k * L.dL] = tmp[k];
+            for (int l = 1; l < L.dL; l++) {
+                for (int m = 0; m <= mmax - l; m++) tmp[m] = fma(CD, tmp[m], tmp[m + 1]);
+                for (int k = 0; k < L.dK; k++) go[k * L.dL + l] = tmp[k];
+            }
         }
     }
 }
@@ -402,9 +407,7 @@ rys_eri_kernel(CGLaunch P)
             continue;
         }
         if (ns <= 1) run_task<MODE, 1>(P, tk, L, term, greg, lane);
-        else if (ns <= 2) run_task<MODE, 2>(P, tk, L, term, greg, lane);
         else if (ns <= 4) run_task<MODE, 4>(P, tk, L, term, greg, lane);
-        else if (ns <= 8) run_task<MODE, 8>(P, tk, L, term, greg, lane);
         else if (ns <= 16 && MODE == CG_MODE_ERI) run_task<MODE, 16>(P, tk, L, term, greg, lane);
         else run_task<MODE, 0>(P, tk, L, term, greg, lane);
     }
@@ -536,6 +539,15 @@ extern "C" int cg_kernels_init(const int *c2s_nnz, const int *c2s_idx, const dou
         if (e != cudaSuccess) return (int)e;
     }
     return 0;
+}
+
+extern "C" int cg_blocks_per_sm(int mode, int ws_doubles)
+{
+    int nb = 0;
+    size_t smem = (size_t)4 * ws_doubles * sizeof(double);
+    void *fn = mode == CG_MODE_ERI ? (void *)rys_eri_kernel<CG_MODE_ERI> : (void *)rys_eri_kernel<CG_MODE_IP1>;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem) != cudaSuccess) return 1;
+    return nb > 0 ? nb : 1;
 }
 
 extern "C" int cg_rys_nmax(void) { return RYS_NMAX; }

@@ -39,6 +39,7 @@ extern "C" {
 int cg_kernels_init(const int *c2s_nnz, const int *c2s_idx, const double *c2s_val,
                     double **rys_coef_dev);
 int cg_rys_nmax(void);
+int cg_blocks_per_sm(int mode, int ws_doubles);
 int cg_rys_deg(void);
 void cg_layout(int li, int lj, int lk, int ll, int mode, int ws_doubles, CGLayout *L);
 int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStream_t stream);
