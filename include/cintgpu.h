@@ -131,6 +131,14 @@ void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas);
 #define CINTGPU_ERR_UNSUPPORTED -3  /* class beyond the kernels' limits */
 #define CINTGPU_ERR_NOMEM      -4
 
+/* Coulomb-like contraction and its adjoint over a list of unique shell quartets
+ * (i >= j, k >= l, ij >= kl; each counted with its permutation multiplicity).  Densities and J
+ * live in the plan's Cartesian AO basis (cintgpu_plan_nao_cart functions, shell order, each
+ * contraction column contiguous); cintgpu_cart2sph gives the per-l transformation. */
+#define CINTGPU_J_BUILD        7   /* J[ij] += sum_kl (ij|kl) D[kl] over the list */
+#define CINTGPU_J_GRAD         8   /* adjoint: dL/dR for L = 1/2 sum D (ij|kl) D */
+#define CINTGPU_J_GRAD_EXP     9   /* adjoint: dL/dR and dL/d(primitive exponent) */
+
 typedef struct CINTGPUPlan CINTGPUPlan;
 
 /* Build a plan for n items (4 shell indices each, 3 for int3c2e) of one integral kind.
@@ -153,6 +161,19 @@ int cintgpu_plan_execute(CINTGPUPlan *plan, double *out_dev, void *stream);
 int64_t cintgpu_plan_upload_bytes(const CINTGPUPlan *plan);
 /* number of kernel launches one execution enqueues */
 int cintgpu_plan_launches(const CINTGPUPlan *plan);
+/* Cartesian AO count of the plan's basis (J/adjoint kinds) */
+int cintgpu_plan_nao_cart(const CINTGPUPlan *plan);
+/* J kinds: vj_dev (nao_cart^2, row major) += the contraction of the listed quartets with
+ * dm_dev (Cartesian, symmetric).  Only the (I >= J) shell blocks of the pair order the plan uses
+ * are written; symmetrise with J = X + X^T - diag-blocks(X) (done by the Python layer). */
+int cintgpu_plan_execute_j(CINTGPUPlan *plan, const double *dm_dev, double *vj_dev, void *stream);
+/* adjoint kinds: grad_dev (natm x 3) += dL/dR; galpha_dev (sum of nprim over shells, shell
+ * order; J_GRAD_EXP only, may be NULL otherwise) += dL/d(exponent) at fixed env coefficients */
+int cintgpu_plan_execute_grad(CINTGPUPlan *plan, const double *dm_dev, double *grad_dev,
+                              double *galpha_dev, void *stream);
+/* cart -> real spherical coefficients of angular momentum l: (2l+1) x ncart row major (identity
+ * for l <= 1, whose factors libcint folds into the common factor); returns the row count */
+int cintgpu_cart2sph(int l, double *c);
 /* after execution completed: per item 1 if any primitive quartet survived screening */
 int cintgpu_plan_nonempty(const CINTGPUPlan *plan, int *flags_host);
 void cintgpu_plan_destroy(CINTGPUPlan *plan);

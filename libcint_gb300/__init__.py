@@ -76,6 +76,14 @@ def lib():
     L.cintgpu_rys_roots_dev.argtypes = [i32, vp, i32, vp, vp, vp]
     L.cintgpu_rys_roots_dev.restype = i32
     L.cintgpu_rys_nmax.restype = i32
+    L.cintgpu_plan_nao_cart.argtypes = [vp]
+    L.cintgpu_plan_nao_cart.restype = i32
+    L.cintgpu_plan_execute_j.argtypes = [vp, vp, vp, vp]
+    L.cintgpu_plan_execute_j.restype = i32
+    L.cintgpu_plan_execute_grad.argtypes = [vp, vp, vp, vp, vp]
+    L.cintgpu_plan_execute_grad.restype = i32
+    L.cintgpu_cart2sph.argtypes = [i32, vp]
+    L.cintgpu_cart2sph.restype = i32
     L.cintgpu_last_error.restype = ctypes.c_char_p
     L.cintgpu_device_sm_count.restype = i32
     _lib = L

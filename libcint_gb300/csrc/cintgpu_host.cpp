@@ -155,7 +155,7 @@ int ensure_init()
 
 /* ------------------------------------------------------------------ shells and pairs */
 struct ShellView {
-    int l, nprim, nctr;
+    int l, nprim, nctr, atom;
     double R[3];
     const double *ex, *cf;
 };
@@ -177,6 +177,7 @@ int read_shell(int sh, const int *atm, int natm, const int *bas, const double *e
     }
     int at = b[ATOM_OF];
     if (at < 0 || at >= natm) { set_error("shell %d: atom %d outside 0..%d", sh, at, natm - 1); return CINTGPU_ERR_ARG; }
+    s->atom = at;
     const double *r = env + atm[ATM_SLOTS * at + PTR_COORD];
     s->R[0] = r[0]; s->R[1] = r[1]; s->R[2] = r[2];
     s->ex = env + b[PTR_EXP];
@@ -223,6 +224,10 @@ struct CINTGPUPlan {
     int ncomp = 1;
     int sph = 1;
     int three = 0;
+    int jmode = 0;                 /* J contraction instead of stored integrals */
+    int nao_cart = 0;
+    int natm = 0;
+    int64_t nprim_tot = 0;
     double expcutoff = 60;
     int64_t nitems = 0;
     int64_t out_size = 0;          /* doubles per component */
@@ -253,6 +258,12 @@ struct CINTGPUPlan {
     double *d_scratch = nullptr;
     int out_blocks = 1;
     int64_t scratch_per_warp = 0;
+    double *d_wscratch = nullptr;  /* per-warp accumulators of the J contraction */
+    const double *cur_dm = nullptr;  /* density / J / gradient of the execution being enqueued */
+    double *cur_vj = nullptr;
+    double *cur_grad = nullptr, *cur_galpha = nullptr;
+    int64_t wscratch_stride = 0;
+    int wscratch_warps = 0;
     cudaStream_t side = nullptr;   /* second stream for the large-class group */
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
@@ -268,6 +279,22 @@ struct Builder {
     std::unordered_map<PairKey, int, PairKeyHash> pair_index;
     std::vector<char> pair_empty;
     std::unordered_map<int, std::vector<double>> logmaxc;   /* per original shell */
+    const std::vector<int> *ao_loc = nullptr;     /* Cartesian AO offset per shell (J/adjoint) */
+    const std::vector<int> *prim_loc = nullptr;   /* first primitive per shell (J/adjoint) */
+
+    void locate(CGPair &p, int sa, const ShellView &A, int ca, int sb, const ShellView &B, int cb)
+    {
+        p.atom_a = A.atom; p.atom_b = B.atom;
+        p.ao_a = p.ao_b = p.gp_a = p.gp_b = 0;
+        if (ao_loc && sa >= 0 && sa < (int)ao_loc->size()) {
+            p.ao_a = (*ao_loc)[sa] + ca * ncart_l(A.l);
+            p.gp_a = (*prim_loc)[sa];
+        }
+        if (ao_loc && sb >= 0 && sb < (int)ao_loc->size()) {
+            p.ao_b = (*ao_loc)[sb] + cb * ncart_l(B.l);
+            p.gp_b = (*prim_loc)[sb];
+        }
+    }
 
     const std::vector<double> &log_maxc(int sh, const ShellView &s)
     {
@@ -292,6 +319,7 @@ struct Builder {
         for (int c = 0; c < 3; c++) { p.AB[c] = A.R[c] - B.R[c]; p.A[c] = A.R[c]; }
         p.prim_off = (int)P->prims.size();
         p.npa = A.nprim; p.npb = B.nprim; p.la = A.l; p.lb = B.l; p.pad = 0;
+        locate(p, sa, A, ca, sb, B, cb);
         double rr = p.AB[0] * p.AB[0] + p.AB[1] * p.AB[1] + p.AB[2] * p.AB[2];
         /* CINTset_pairdata, src/optimizer.c:288-342 */
         double aij_last = A.ex[A.nprim - 1] + B.ex[B.nprim - 1];
@@ -340,6 +368,7 @@ struct Builder {
         for (int c = 0; c < 3; c++) { p.AB[c] = 0.0; p.A[c] = K.R[c]; }
         p.prim_off = (int)P->prims.size();
         p.npa = K.nprim; p.npb = 1; p.la = K.l; p.lb = 0; p.pad = 0;
+        locate(p, sk, K, ck, -1, K, 0);
         for (int kp = 0; kp < K.nprim; kp++) {
             CGPrimPair q;
             q.a = K.ex[kp];
@@ -370,7 +399,10 @@ double flops_per_primq(int li, int lj, int lk, int ll, int mode)
     double vrr = (double)(L.nmax + 1) * (L.mmax + 1);
     double per_root = 20 + 3 * 5 * vrr + 3 * 2 * hrr;
     if (mode == CG_MODE_IP1) per_root += 3 * 3 * (double)L.G / L.dI * (L.dI - 1) + 9.0 * L.nf;
-    else per_root += 3.0 * L.nf;
+    else if (mode == CG_MODE_GRAD || mode == CG_MODE_GRADA) {
+        double nT = (double)(li + 1) * (lj + 1) * (lk + 1) * (ll + 1);
+        per_root += 9.0 * L.nf + 3 * nT * (mode == CG_MODE_GRADA ? 20 : 12);
+    } else per_root += 3.0 * L.nf;
     return n * per_root;
 }
 
@@ -401,6 +433,9 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     case CINTGPU_INT2E_IP1_CART: P->mode = CG_MODE_IP1; P->sph = 0; P->three = 0; break;
     case CINTGPU_INT3C2E_SPH: P->mode = CG_MODE_ERI; P->sph = 1; P->three = 1; break;
     case CINTGPU_INT3C2E_CART: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 1; break;
+    case CINTGPU_J_BUILD: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; P->jmode = 1; break;
+    case CINTGPU_J_GRAD: P->mode = CG_MODE_GRAD; P->sph = 0; P->three = 0; break;
+    case CINTGPU_J_GRAD_EXP: P->mode = CG_MODE_GRADA; P->sph = 0; P->three = 0; break;
     default: set_error("unknown integral kind %d", kind); return CINTGPU_ERR_ARG;
     }
     P->ncomp = P->mode == CG_MODE_IP1 ? 3 : 1;
@@ -412,11 +447,28 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     if (env[PTR_EXPCUTOFF] == 0) P->expcutoff = 60;
     else P->expcutoff = std::max(40.0, env[PTR_EXPCUTOFF]) + (P->three ? 0 : 1);
     P->nitems = n;
+    P->natm = natm;
     Builder B{P, atm, natm, bas, env, {}, {}, {}};
+    const bool contracting = P->jmode || P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA;
+    std::vector<int> ao_loc, prim_loc;
+    if (contracting) {
+        ao_loc.resize(nbas + 1);
+        prim_loc.resize(nbas + 1);
+        ao_loc[0] = prim_loc[0] = 0;
+        for (int i = 0; i < nbas; i++) {
+            const int *b = bas + BAS_SLOTS * i;
+            ao_loc[i + 1] = ao_loc[i] + ncart_l(b[ANG_OF]) * b[NCTR_OF];
+            prim_loc[i + 1] = prim_loc[i] + b[NPRIM_OF];
+        }
+        P->nao_cart = ao_loc[nbas];
+        P->nprim_tot = prim_loc[nbas];
+        B.ao_loc = &ao_loc;
+        B.prim_loc = &prim_loc;
+    }
     const int nsh = P->three ? 3 : 4;
     const int dinc = P->mode == CG_MODE_IP1 ? 1 : 0;
 
-    struct Pending { int pij, pkl, out; int64_t npq; int l[4]; };
+    struct Pending { int pij, pkl, out; int64_t npq; int l[4]; int sym; };
     std::vector<Pending> pend;
     int64_t next_off = 0;
     for (int64_t q = 0; q < n; q++) {
@@ -425,6 +477,19 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         for (int a = 0; a < nsh; a++) {
             int rc = read_shell(s[a], atm, natm, bas, env, &sv[a]);
             if (rc) return rc;
+            if (contracting && s[a] >= nbas) { set_error("shell %d outside nbas %d", s[a], nbas); return CINTGPU_ERR_ARG; }
+            if (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) {
+                if (sv[a].l > 4) { set_error("adjoint supports l <= 4 (shell %d has %d)", s[a], sv[a].l); return CINTGPU_ERR_UNSUPPORTED; }
+                if (P->mode == CG_MODE_GRADA && sv[a].nprim > CG_GRAD_MAXPRIM) {
+                    set_error("exponent adjoint supports nprim <= %d", CG_GRAD_MAXPRIM);
+                    return CINTGPU_ERR_UNSUPPORTED;
+                }
+            }
+        }
+        int qsym = 0;
+        if (!P->three) {
+            qsym = (s[0] != s[1] ? 1 : 0) | (s[2] != s[3] ? 2 : 0)
+                 | ((s[0] != s[2] || s[1] != s[3]) ? 4 : 0);
         }
         if (P->three) { sv[3] = sv[2]; sv[3].l = 0; sv[3].nprim = 1; sv[3].nctr = 1; }
         int d[4], nd[4];
@@ -439,7 +504,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         next_off = std::max(next_off, base + block);
         /* kernel order: perm[k] = request index placed at kernel slot k */
         int perm[4] = {0, 1, 2, 3};
-        if (P->mode == CG_MODE_ERI) {
+        if (P->mode != CG_MODE_IP1) {
             if (sv[0].l < sv[1].l) std::swap(perm[0], perm[1]);
             if (!P->three) {
                 if (sv[2].l < sv[3].l) std::swap(perm[2], perm[3]);
@@ -478,7 +543,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             if (B.pair_empty[pij] || B.pair_empty[pkl]) continue;
             const CGPair &a = P->pairs[pij], &b = P->pairs[pkl];
             Pending pe{pij, pkl, out_id, (int64_t)a.npa * a.npb * b.npa * b.npb,
-                       {kl_[0], kl_[1], kl_[2], kl_[3]}};
+                       {kl_[0], kl_[1], kl_[2], kl_[3]}, qsym};
             pend.push_back(pe);
         }
     }
@@ -515,7 +580,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     double target = std::max(fl / (warps * 32.0), 2.0e5);
     if (split_target > 0) target = std::min(target, fl / (double)split_target);
     /* shared memory per warp of the regular group: 24 KB unless CINTGPU_WS_KB overrides (tuning) */
-    int ws_small = CG_WS_SMALL;
+    int ws_small = (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) ? CG_WS_MAX : CG_WS_SMALL;
     if (const char *e = getenv("CINTGPU_WS_KB")) {
         int kb = atoi(e);
         if (kb >= 8 && kb <= 48) ws_small = kb * 1024 / 8;
@@ -551,7 +616,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             x.t.npq = (int)std::min<int64_t>(slice, w.n - a0);
             x.t.cart_off = gpos;
             x.t.out = pe.out;
-            x.t.pad = 0;
+            x.t.sym = pe.sym;
             x.cost = x.t.npq * w.cost_pq;
             x.group = group;
             tc.push_back(x);
@@ -571,14 +636,17 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             if (x.group == g) P->tasks.push_back(x.t);
         P->groups[g].ntasks = (int)P->tasks.size() - P->groups[g].task0;
         P->groups[g].ws = g == 0 ? ws_small : CG_WS_MAX;
-        P->groups[g].blocks_per_sm = cg_blocks_per_sm(P->mode, P->groups[g].ws);
+        P->groups[g].blocks_per_sm = (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA)
+                                         ? cg_grad_blocks_per_sm(P->mode, P->groups[g].ws)
+                                         : cg_blocks_per_sm(P->mode, P->groups[g].ws);
     }
     P->gctr_size = std::max<int64_t>(gpos, 1);
     return 0;
 }
 
 struct DevLayout {
-    size_t pairs, prims, tasks, outs, pq, gctr, cnt, ne, scr;
+    size_t pairs, prims, tasks, outs, pq, gctr, cnt, ne, scr, wscr;
+    int wwarps;
     size_t upload, total;
     int out_blocks;
     int64_t spw;
@@ -599,8 +667,15 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     D.cnt = al(sizeof(int) * 4);
     D.ne = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
     D.scr = al(sizeof(double) * D.spw * D.out_blocks * 4);
+    D.wwarps = 0;
+    D.wscr = 0;
+    if (P->jmode) {
+        D.wwarps = g_ctx.sm_count * 4 * (P->groups[0].blocks_per_sm + P->groups[1].blocks_per_sm);
+        D.wscr = al(sizeof(double) * (size_t)D.wwarps * P->max_nf);
+        D.gctr = al(sizeof(double));   /* J plans keep no per-task accumulators */
+    }
     D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq;
-    D.total = D.upload + D.gctr + D.cnt + D.ne + D.scr;
+    D.total = D.upload + D.gctr + D.cnt + D.ne + D.scr + D.wscr;
     return D;
 }
 
@@ -637,6 +712,9 @@ static int upload_plan(CINTGPUPlan *P, char *arena, size_t arena_size, cudaStrea
     P->d_counters = (int *)p; p += D.cnt;
     P->d_nonempty = (int *)p; p += D.ne;
     P->d_scratch = (double *)p; p += D.scr;
+    P->d_wscratch = (double *)p; p += D.wscr;
+    P->wscratch_stride = P->max_nf;
+    P->wscratch_warps = D.wwarps;
     std::vector<char> tmp;
     char *src;
     if (async_from_pinned) src = pinned;
@@ -655,8 +733,34 @@ static int upload_plan(CINTGPUPlan *P, char *arena, size_t arena_size, cudaStrea
     return 0;
 }
 
+static int launch_grad_group(CINTGPUPlan *P, int g, cudaStream_t stream)
+{
+    const TaskGroup &G = P->groups[g];
+    if (G.ntasks == 0) return 0;
+    CGGradLaunch L;
+    L.tasks = P->d_tasks + G.task0;
+    L.ntasks = G.ntasks;
+    L.pairs = P->d_pairs;
+    L.prims = P->d_prims;
+    L.pqlist = P->d_pqlist;
+    L.counter = P->d_counters + g;
+    L.status = P->d_counters + 2;
+    L.rys_coef = g_ctx.rys_coef;
+    L.common_base = M_PI * M_PI * M_PI * 2 / 1.7724538509055160272981674833411451;
+    L.ws_doubles = G.ws;
+    L.dm = P->cur_dm;
+    L.nao = P->nao_cart;
+    L.grad = P->cur_grad;
+    L.galpha = P->cur_galpha;
+    int nblocks = std::min(g_ctx.sm_count * G.blocks_per_sm, std::max(1, (G.ntasks + 3) / 4));
+    int rc = cg_launch_grad(&L, P->mode, nblocks, stream);
+    if (rc) { set_error("adjoint kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
+    return 0;
+}
+
 static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
 {
+    if (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) return launch_grad_group(P, g, stream);
     const TaskGroup &G = P->groups[g];
     if (G.ntasks == 0) return 0;
     CGLaunch L;
@@ -674,6 +778,14 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.common_base = M_PI * M_PI * M_PI * 2 / 1.7724538509055160272981674833411451;
     L.three = P->three;
     L.ws_doubles = G.ws;
+    L.jmode = P->jmode;
+    L.wscratch = P->d_wscratch;
+    if (P->jmode && g == 1)   /* the groups run concurrently: separate warp slots */
+        L.wscratch += (size_t)g_ctx.sm_count * 4 * P->groups[0].blocks_per_sm * P->max_nf;
+    L.wscratch_stride = P->wscratch_stride;
+    L.dm = P->cur_dm;
+    L.vj = P->cur_vj;
+    L.nao = P->nao_cart;
     int nblocks = std::min(g_ctx.sm_count * G.blocks_per_sm, std::max(1, (G.ntasks + 3) / 4));
     int rc = cg_launch_eri(&L, P->mode, nblocks, stream);
     if (rc) { set_error("ERI kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
@@ -701,6 +813,7 @@ static int execute_plan(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
         if (!rc) rc = launch_group(P, 0, stream);
         if (rc) return rc;
     }
+    if (P->jmode || P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) return 0;
     int rc = cg_launch_output(P->d_outs, (int)P->outs.size(), P->d_gctr, P->d_nonempty, P->d_scratch,
                               P->scratch_per_warp, P->out_blocks, out_dev, P->ncomp, P->out_size, stream);
     if (rc) { set_error("output kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
@@ -929,6 +1042,50 @@ int64_t cintgpu_plan_upload_bytes(const CINTGPUPlan *plan) { return (int64_t)pla
 int cintgpu_plan_execute(CINTGPUPlan *plan, double *out_dev, void *stream)
 {
     return execute_plan(plan, out_dev, (cudaStream_t)stream);
+}
+
+int cintgpu_plan_nao_cart(const CINTGPUPlan *plan) { return plan->nao_cart; }
+
+int cintgpu_plan_execute_j(CINTGPUPlan *plan, const double *dm_dev, double *vj_dev, void *stream)
+{
+    if (!plan->jmode) { set_error("plan is not a J_BUILD plan"); return CINTGPU_ERR_ARG; }
+    plan->cur_dm = dm_dev;
+    plan->cur_vj = vj_dev;
+    return execute_plan(plan, nullptr, (cudaStream_t)stream);
+}
+
+int cintgpu_plan_execute_grad(CINTGPUPlan *plan, const double *dm_dev, double *grad_dev,
+                              double *galpha_dev, void *stream)
+{
+    if (plan->mode != CG_MODE_GRAD && plan->mode != CG_MODE_GRADA) {
+        set_error("plan is not an adjoint plan");
+        return CINTGPU_ERR_ARG;
+    }
+    if (plan->mode == CG_MODE_GRADA && !galpha_dev) { set_error("J_GRAD_EXP needs galpha"); return CINTGPU_ERR_ARG; }
+    plan->cur_dm = dm_dev;
+    plan->cur_grad = grad_dev;
+    plan->cur_galpha = galpha_dev;
+    return execute_plan(plan, nullptr, (cudaStream_t)stream);
+}
+
+int cintgpu_cart2sph(int l, double *c)
+{
+    int nc = ncart_l(l);
+    if (l < 0 || l > CG_MAX_SHELL_L) return 0;
+    if (l <= 1) {
+        for (int i = 0; i < nc * nc; i++) c[i] = 0;
+        for (int i = 0; i < nc; i++) c[i * nc + i] = 1;
+        return nc;
+    }
+    std::vector<int> nnz, idx;
+    std::vector<double> val;
+    c2s_rows(nnz, idx, val);
+    for (int i = 0; i < (2 * l + 1) * nc; i++) c[i] = 0;
+    for (int m = 0; m < 2 * l + 1; m++) {
+        int row = l * l + m;
+        for (int z = 0; z < nnz[row]; z++) c[m * nc + idx[row * CG_C2S_MAXNNZ + z]] = val[row * CG_C2S_MAXNNZ + z];
+    }
+    return 2 * l + 1;
 }
 
 int cintgpu_plan_nonempty(const CINTGPUPlan *plan, int *flags_host)

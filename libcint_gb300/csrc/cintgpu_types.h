@@ -5,7 +5,8 @@
  *   CGPair[npair]        one ordered shell pair (A, B); A is the recurrence base centre
  *   CGPrimPair[nprim]    its primitive pairs, ip fastest (jp * npa + ip), libcint's loop order
  *                        (src/cint2e.c:400-425); contraction coefficients are folded into K
- *   CGTask[ntask]        one unit of kernel work: (bra pair, ket pair, primitive-quartet range)
+ *   CGTask[ntask]        one unit of kernel work: bra pair, ket pair and a slice of the surviving
+ *                        primitive quartets (pqlist)
  *   CGOutTask[nout]      one contracted shell quartet to transform (cart -> sph) and store
  *   gctr                 Cartesian accumulators, CGTask::cart_off, layout [comp][nf]
  */
@@ -22,6 +23,9 @@ typedef struct {
     int prim_off;        /* first CGPrimPair */
     int npa, npb;        /* primitive counts of A and B */
     int la, lb;          /* angular momenta */
+    int ao_a, ao_b;      /* Cartesian AO offsets of A and B (J contraction, adjoint) */
+    int atom_a, atom_b;  /* atoms of A and B (adjoint) */
+    int gp_a, gp_b;      /* first global primitive index of A and B (exponent adjoint) */
     int pad;
 } CGPair;
 
@@ -40,7 +44,7 @@ typedef struct {
                             each encoded kl * nij + ij */
     int64_t cart_off;    /* accumulator slot in gctr */
     int out;             /* CGOutTask index (for the non-empty flag) */
-    int pad;
+    int sym;             /* unique-quartet flags: bit0 I != J, bit1 K != L, bit2 IJ != KL */
 } CGTask;
 
 typedef struct {

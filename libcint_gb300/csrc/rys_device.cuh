@@ -1,0 +1,242 @@
+/*
+ * Device-side building blocks shared by the CUDA translation units of the Rys path
+ * (rys_kernels.cu: integrals, J contraction; rys_grad.cu: the adjoint).  Each translation unit
+ * that includes this header owns its copy of the small constant tables and fills them through
+ * cg_tu_tables_init().
+ *
+ * Contents: class layout of the per-warp shared memory, Rys node/weight evaluation from the
+ * piecewise polynomial tables, Cartesian component powers, and the per-axis vertical recurrence
+ * plus both horizontal transfers (libcint CINTg0_2e_2d, src/g2e.c:272-421, and
+ * CINTg0_*2d_4d, src/g2e.c:428-693, restated with the i and k centres as bases).
+ */
+#ifndef CINTGPU_RYS_DEVICE_CUH
+#define CINTGPU_RYS_DEVICE_CUH
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "cintgpu_types.h"
+#include "rys_tables.inc"
+#include "rys_kernels.h"
+
+#define FULL 0xffffffffu
+
+static __constant__ int c_rys_off[RYS_NMAX + 1];
+static __constant__ double c_rys_xmax[RYS_NMAX + 1];
+static __constant__ double c_large_r[RYS_NMAX * (RYS_NMAX + 1) / 2];
+static __constant__ double c_large_w[RYS_NMAX * (RYS_NMAX + 1) / 2];
+
+/* sparse rows of the cart->sph matrices: row (l, m) has nnz entries (cart index, coefficient) */
+#define C2S_MAXNNZ CG_C2S_MAXNNZ
+#define C2S_ROWS ((CG_MAX_SHELL_L + 1) * (CG_MAX_SHELL_L + 1))
+static __device__ int g_c2s_nnz[C2S_ROWS];
+static __device__ int g_c2s_idx[C2S_ROWS * C2S_MAXNNZ];
+static __device__ double g_c2s_val[C2S_ROWS * C2S_MAXNNZ];
+
+/* ------------------------------------------------------------------ layout per class */
+__host__ __device__ inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+
+/* Per-mode increments of the four g-array axes: derivatives raise the angular momentum the
+ * recurrences must reach (ip1: i+1, libcint grad2.c ng = {1,0,0,0,...}; coordinate adjoint:
+ * i+1, j+1, k+1; exponent adjoint: +2 on all four). */
+__host__ __device__ inline void cg_mode_incs(int mode, int inc[4])
+{
+    inc[0] = inc[1] = inc[2] = inc[3] = 0;
+    if (mode == CG_MODE_IP1) inc[0] = 1;
+    else if (mode == CG_MODE_GRAD) { inc[0] = 1; inc[1] = 1; inc[2] = 1; }
+    else if (mode == CG_MODE_GRADA) { inc[0] = 2; inc[1] = 2; inc[2] = 2; inc[3] = 2; }
+}
+
+__host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, int mode,
+                                                int ws_doubles, CGLayout *L)
+{
+    int inc[4];
+    cg_mode_incs(mode, inc);
+    L->lic = li + inc[0];
+    const int ljc = lj + inc[1], lkc = lk + inc[2], llc = ll + inc[3];
+    L->nroots = (L->lic + ljc + lkc + llc) / 2 + 1;
+    L->nmax = L->lic + ljc;
+    L->mmax = lkc + llc;
+    L->dI = L->lic + 1; L->dJ = ljc + 1; L->dK = lkc + 1; L->dL = llc + 1;
+    L->G = L->dI * L->dJ * L->dK * L->dL;
+    L->ng = (mode == CG_MODE_IP1) ? 2 : 1;
+    L->nf = ncart(li) * ncart(lj) * ncart(lk) * ncart(ll);
+    L->ncomp = (mode == CG_MODE_IP1) ? 3 : 1;
+    L->scr = (L->nmax + 1) * (L->mmax + 1) + (L->nmax + 1) + (L->mmax + 1);
+    int termw = (mode == CG_MODE_GRAD || mode == CG_MODE_GRADA) ? CG_TERMW_GRAD : CG_TERMW;
+    int fixed = termw * 32;
+    if (mode == CG_MODE_GRAD || mode == CG_MODE_GRADA)
+        fixed += 2 * 225 + 4 * CG_GRAD_MAXPRIM + 512;  /* density blocks, exponent sums, chunk table */
+    int avail = ws_doubles - fixed;
+    /* T terms need T*3*ng*G doubles of g arrays and min(32, 3T) lane scratch areas */
+    int T = 0;
+    for (int t = 32; t >= 1; t--) {
+        int items = 3 * t < 32 ? 3 * t : 32;
+        if (t * 3 * L->ng * L->G + items * L->scr <= avail) { T = t; break; }
+    }
+    L->T = T;
+}
+
+/* ------------------------------------------------------------------ roots */
+__device__ __forceinline__ void rys_node(int n, double x, int r, const double *__restrict__ coef,
+                                         double &s, double &w)
+{
+    if (x >= c_rys_xmax[n]) {
+        double rs = rsqrt(x);
+        int o = n * (n - 1) / 2 + r;
+        s = c_large_r[o] * (rs * rs);
+        w = c_large_w[o] * rs;
+    } else {
+        int k = (int)x;                      /* interval width 1 */
+        double y = 2.0 * (x - (double)k) - 1.0;
+        const double2 *c = reinterpret_cast<const double2 *>(
+            coef + c_rys_off[n] + (size_t)((k * n + r) * (RYS_DEG + 1)) * 2);
+        double2 cj = __ldg(c + RYS_DEG);
+        double a = cj.x, b = cj.y;
+#pragma unroll
+        for (int j = RYS_DEG - 1; j >= 0; j--) {
+            cj = __ldg(c + j);
+            a = fma(a, y, cj.x);
+            b = fma(b, y, cj.y);
+        }
+        s = a;
+        w = b;
+    }
+}
+
+/* ------------------------------------------------------------------ cart powers */
+__device__ __forceinline__ void cart_pow(int l, int p, int &lx, int &ly, int &lz)
+{
+    /* CINTcart_comp order (src/cint_bas.c:166-181): row = l - lx, q = lz */
+    int row = (int)((sqrtf(8.f * p + 1.f) - 1.f) * 0.5f);
+    while ((row + 1) * (row + 2) / 2 <= p) row++;
+    while (row * (row + 1) / 2 > p) row--;
+    int q = p - row * (row + 1) / 2;
+    lx = l - row;
+    ly = row - q;
+    lz = q;
+}
+
+/* ------------------------------------------------------------------ stage 2 */
+/* One Cartesian axis of one term: VRR into T2[a + (nmax+1) m], then the two horizontal
+ * transfers; final g[((i dJ + j) dK + k) dL + l] goes to gout.  Lane scratch: T2, a*b00, and a
+ * vector of length mmax+1. */
+__device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10, double b01,
+                                       double c00, double c0p, double g00, double AB, double CD,
+                                       double *scr, double *gout)
+{
+    const int nmax = L.nmax, mmax = L.mmax, na = nmax + 1, nm = mmax + 1;
+    double *T2 = scr;
+    double *ab00 = scr + na * nm;
+    /* a * b00 */
+    {
+        double acc = 0.0;
+        for (int a = 0; a <= nmax; a++) { ab00[a] = acc; acc += b00; }
+    }
+    T2[0] = g00;
+    if (nmax > 0) {
+        double p0 = g00, p1 = c00 * g00, nb = b10;
+        T2[1] = p1;
+        for (int a = 1; a < nmax; a++) {
+            double p2 = fma(c00, p1, nb * p0);
+            T2[a + 1] = p2;
+            p0 = p1; p1 = p2;
+            nb += b10;
+        }
+    }
+    double mb = 0.0;
+    for (int m = 0; m < mmax; m++) {
+        const double *cm = T2 + m * na;
+        const double *cm1 = T2 + (m - 1) * na;
+        double *cn = T2 + (m + 1) * na;
+        for (int a = 0; a <= nmax; a++) {
+            double v = c0p * cm[a];
+            if (m > 0) v = fma(mb, cm1[a], v);
+            if (a > 0) v = fma(ab00[a], cm[a - 1], v);
+            cn[a] = v;
+        }
+        mb += b01;
+    }
+    /* (a,0| -> (i,j| one j level at a time, in place on every column m:
+     * col[a] = col[a+1] + AB col[a]; after level j, row i of all columns is g(i,j,m) and goes
+     * through |m,0) -> |k,l) in a short vector, so no (i,j,m) intermediate is stored. */
+    double *tmp = ab00 + na;
+    for (int j = 0; j < L.dJ; j++) {
+        if (j > 0) {
+            for (int m = 0; m <= mmax; m++) {
+                double *col = T2 + m * na;
+                for (int a = 0; a <= nmax - j; a++) col[a] = fma(AB, col[a], col[a + 1]);
+            }
+        }
+        for (int i = 0; i < L.dI; i++) {
+            double *go = gout + (i * L.dJ + j) * L.dK * L.dL;
+            if (L.dL == 1) {
+                for (int k = 0; k < L.dK; k++) go[k] = T2[i + na * k];
+                continue;
+            }
+            for (int m = 0; m <= mmax; m++) tmp[m] = T2[i + na * m];
+            for (int k = 0; k < L.dK; k++) go[k * L.dL] = tmp[k];
+            for (int l = 1; l < L.dL; l++) {
+                for (int m = 0; m <= mmax - l; m++) tmp[m] = fma(CD, tmp[m], tmp[m + 1]);
+                for (int k = 0; k < L.dK; k++) go[k * L.dL + l] = tmp[k];
+            }
+        }
+    }
+}
+
+
+/* fill this translation unit's copies of the tables */
+static int cg_tu_tables_init(const int *c2s_nnz, const int *c2s_idx, const double *c2s_val)
+{
+    double xmax[RYS_NMAX + 1];
+    xmax[0] = 0;
+    for (int n = 1; n <= RYS_NMAX; n++) xmax[n] = RYS_H * rys_nint_host[n];
+    cudaError_t e;
+    if ((e = cudaMemcpyToSymbol(c_rys_off, rys_off_host, sizeof(rys_off_host))) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(c_rys_xmax, xmax, sizeof(xmax))) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(c_large_r, rys_large_r_host, sizeof(rys_large_r_host))) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(c_large_w, rys_large_w_host, sizeof(rys_large_w_host))) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(g_c2s_nnz, c2s_nnz, sizeof(int) * C2S_ROWS)) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(g_c2s_idx, c2s_idx, sizeof(int) * C2S_ROWS * C2S_MAXNNZ)) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyToSymbol(g_c2s_val, c2s_val, sizeof(double) * C2S_ROWS * C2S_MAXNNZ)) != cudaSuccess) return (int)e;
+    return 0;
+}
+
+__device__ __forceinline__ double common_fac_sp(int l)   /* libcint src/g1e.c:565-572 */
+{
+    return l == 0 ? 0.282094791773878143 : (l == 1 ? 0.488602511902919921 : 1.0);
+}
+
+/* Stage 1 for one term (primitive quartet q = kl * nij + ij, root r): x, prefactor, Rys node and
+ * weight, and the division-free recurrence coefficients (libcint CINTg0_2e, src/g2e.c:4425-4545,
+ * rewritten in s = t^2: b00 = s / 2(aij+akl), b10 = b00 + (1-s)/2aij, b01 = b00 + (1-s)/2akl,
+ * c00 = PA - s akl/(aij+akl) PQ, c0p = QC + s aij/(aij+akl) PQ).  rec[9] = weight * prefactor. */
+__device__ __forceinline__ void cg_term(const CGPrimPair &A, const CGPrimPair &B, const CGPair &pij,
+                                        const CGPair &pkl, int n, int r, double common,
+                                        const double *__restrict__ coef, double *rec)
+{
+    double aijkl = A.a + B.a;
+    double rs = rsqrt(aijkl);
+    double inv = rs * rs;
+    double PQx = A.P[0] - B.P[0], PQy = A.P[1] - B.P[1], PQz = A.P[2] - B.P[2];
+    double rr = fma(PQx, PQx, fma(PQy, PQy, PQz * PQz));
+    double rho = A.a * B.a * inv;
+    double x = rho * rr;
+    double s, w;
+    rys_node(n, x, r, coef, s, w);
+    double fac1 = common * A.K * B.K * rs * A.inv_a * B.inv_a;
+    double tb = s * inv;                 /* 2 b00 */
+    double b00 = 0.5 * tb;
+    double oms = 1.0 - s;
+    double b10 = fma(0.5 * A.inv_a, oms, b00);
+    double b01 = fma(0.5 * B.inv_a, oms, b00);
+    double ta = tb * B.a, tc = tb * A.a;
+    rec[0] = b00; rec[1] = b10; rec[2] = b01;
+    rec[3] = fma(-ta, PQx, A.P[0] - pij.A[0]);
+    rec[4] = fma(-ta, PQy, A.P[1] - pij.A[1]);
+    rec[5] = fma(-ta, PQz, A.P[2] - pij.A[2]);
+    rec[6] = fma(tc, PQx, B.P[0] - pkl.A[0]);
+    rec[7] = fma(tc, PQy, B.P[1] - pkl.A[1]);
+    rec[8] = fma(tc, PQz, B.P[2] - pkl.A[2]);
+    rec[9] = w * fac1;
+}
+
+#endif

@@ -25,80 +25,7 @@
  * spherical, c2s_sph_2e1 / c2s_sph_3c2e1 semantics, src/cart2sph.c:5324-5383, 5884-5925) with
  * arbitrary output strides.
  */
-#include <cuda_runtime.h>
-#include <stdint.h>
-#include "cintgpu_types.h"
-#include "rys_tables.inc"
-#include "rys_kernels.h"
-
-#define FULL 0xffffffffu
-
-__constant__ int c_rys_off[RYS_NMAX + 1];
-__constant__ double c_rys_xmax[RYS_NMAX + 1];
-__constant__ double c_large_r[RYS_NMAX * (RYS_NMAX + 1) / 2];
-__constant__ double c_large_w[RYS_NMAX * (RYS_NMAX + 1) / 2];
-
-/* sparse rows of the cart->sph matrices: row (l, m) has nnz entries (cart index, coefficient) */
-#define C2S_MAXNNZ CG_C2S_MAXNNZ
-#define C2S_ROWS ((CG_MAX_SHELL_L + 1) * (CG_MAX_SHELL_L + 1))
-__device__ int g_c2s_nnz[C2S_ROWS];
-__device__ int g_c2s_idx[C2S_ROWS * C2S_MAXNNZ];
-__device__ double g_c2s_val[C2S_ROWS * C2S_MAXNNZ];
-
-/* ------------------------------------------------------------------ layout per class */
-__host__ __device__ inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
-
-__host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, int mode,
-                                                int ws_doubles, CGLayout *L)
-{
-    int dinc = (mode == CG_MODE_IP1) ? 1 : 0;
-    L->lic = li + dinc;
-    L->nroots = (L->lic + lj + lk + ll) / 2 + 1;
-    L->nmax = L->lic + lj;
-    L->mmax = lk + ll;
-    L->dI = L->lic + 1; L->dJ = lj + 1; L->dK = lk + 1; L->dL = ll + 1;
-    L->G = L->dI * L->dJ * L->dK * L->dL;
-    L->ng = (mode == CG_MODE_IP1) ? 2 : 1;
-    L->nf = ncart(li) * ncart(lj) * ncart(lk) * ncart(ll);
-    L->ncomp = (mode == CG_MODE_IP1) ? 3 : 1;
-    L->scr = (L->nmax + 1) * (L->mmax + 1) + (L->nmax + 1) + (L->mmax + 1);
-    int fixed = CG_TERMW * 32;       /* term records */
-    int avail = ws_doubles - fixed;
-    /* T terms need T*3*ng*G doubles of g arrays and min(32, 3T) lane scratch areas */
-    int T = 0;
-    for (int t = 32; t >= 1; t--) {
-        int items = 3 * t < 32 ? 3 * t : 32;
-        if (t * 3 * L->ng * L->G + items * L->scr <= avail) { T = t; break; }
-    }
-    L->T = T;
-}
-
-/* ------------------------------------------------------------------ roots */
-__device__ __forceinline__ void rys_node(int n, double x, int r, const double *__restrict__ coef,
-                                         double &s, double &w)
-{
-    if (x >= c_rys_xmax[n]) {
-        double rs = rsqrt(x);
-        int o = n * (n - 1) / 2 + r;
-        s = c_large_r[o] * (rs * rs);
-        w = c_large_w[o] * rs;
-    } else {
-        int k = (int)x;                      /* interval width 1 */
-        double y = 2.0 * (x - (double)k) - 1.0;
-        const double2 *c = reinterpret_cast<const double2 *>(
-            coef + c_rys_off[n] + (size_t)((k * n + r) * (RYS_DEG + 1)) * 2);
-        double2 cj = __ldg(c + RYS_DEG);
-        double a = cj.x, b = cj.y;
-#pragma unroll
-        for (int j = RYS_DEG - 1; j >= 0; j--) {
-            cj = __ldg(c + j);
-            a = fma(a, y, cj.x);
-            b = fma(b, y, cj.y);
-        }
-        s = a;
-        w = b;
-    }
-}
+#include "rys_device.cuh"
 
 __global__ void rys_roots_kernel(const double *__restrict__ xs, int count, int n,
                                  const double *__restrict__ coef, double *s_out, double *w_out)
@@ -113,91 +40,8 @@ __global__ void rys_roots_kernel(const double *__restrict__ xs, int count, int n
     }
 }
 
-/* ------------------------------------------------------------------ cart powers */
-__device__ __forceinline__ void cart_pow(int l, int p, int &lx, int &ly, int &lz)
-{
-    /* CINTcart_comp order (src/cint_bas.c:166-181): row = l - lx, q = lz */
-    int row = (int)((sqrtf(8.f * p + 1.f) - 1.f) * 0.5f);
-    while ((row + 1) * (row + 2) / 2 <= p) row++;
-    while (row * (row + 1) / 2 > p) row--;
-    int q = p - row * (row + 1) / 2;
-    lx = l - row;
-    ly = row - q;
-    lz = q;
-}
-
-/* ------------------------------------------------------------------ stage 2 */
-/* One Cartesian axis of one term: VRR into T2[a + (nmax+1) m], then the two horizontal
- * transfers; final g[((i dJ + j) dK + k) dL + l] goes to gout.  Lane scratch: T2, a*b00, and a
- * vector of length mmax+1. */
-__device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10, double b01,
-                                       double c00, double c0p, double g00, double AB, double CD,
-                                       double *scr, double *gout)
-{
-    const int nmax = L.nmax, mmax = L.mmax, na = nmax + 1, nm = mmax + 1;
-    double *T2 = scr;
-    double *ab00 = scr + na * nm;
-    /* a * b00 */
-    {
-        double acc = 0.0;
-        for (int a = 0; a <= nmax; a++) { ab00[a] = acc; acc += b00; }
-    }
-    T2[0] = g00;
-    if (nmax > 0) {
-        double p0 = g00, p1 = c00 * g00, nb = b10;
-        T2[1] = p1;
-        for (int a = 1; a < nmax; a++) {
-            double p2 = fma(c00, p1, nb * p0);
-            T2[a + 1] = p2;
-            p0 = p1; p1 = p2;
-            nb += b10;
-        }
-    }
-    double mb = 0.0;
-    for (int m = 0; m < mmax; m++) {
-        const double *cm = T2 + m * na;
-        const double *cm1 = T2 + (m - 1) * na;
-        double *cn = T2 + (m + 1) * na;
-        for (int a = 0; a <= nmax; a++) {
-            double v = c0p * cm[a];
-            if (m > 0) v = fma(mb, cm1[a], v);
-            if (a > 0) v = fma(ab00[a], cm[a - 1], v);
-            cn[a] = v;
-        }
-        mb += b01;
-    }
-    /* (a,0| -> (i,j| one j level at a time, in place on every column m:
-     * col[a] = col[a+1] + AB col[a]; after level j, row i of all columns is g(i,j,m) and goes
-     * through |m,0) -> |k,l) in a short vector, so no (i,j,m) intermediate is stored. */
-    double *tmp = ab00 + na;
-    for (int j = 0; j < L.dJ; j++) {
-        if (j > 0) {
-            for (int m = 0; m <= mmax; m++) {
-                double *col = T2 + m * na;
-                for (int a = 0; a <= nmax - j; a++) col[a] = fma(AB, col[a], col[a + 1]);
-            }
-        }
-        for (int i = 0; i < L.dI; i++) {
-            double *go = gout + (i * L.dJ + j) * L.dK * L.dL;
-            if (L.dL == 1) {
-                for (int k = 0; k < L.dK; k++) go[k] = T2[i + na * k];
-                continue;
-            }
-            for (int m = 0; m <= mmax; m++) tmp[m] = T2[i + na * m];
-            for (int k = 0; k < L.dK; k++) go[k * L.dL] = tmp[k];
-            for (int l = 1; l < L.dL; l++) {
-                for (int m = 0; m <= mmax - l; m++) tmp[m] = fma(CD, tmp[m], tmp[m + 1]);
-                for (int k = 0; k < L.dK; k++) go[k * L.dL + l] = tmp[k];
-            }
-        }
-    }
-}
 
 /* ------------------------------------------------------------------ main kernel */
-__device__ __forceinline__ double common_fac_sp(int l)   /* libcint src/g1e.c:565-572 */
-{
-    return l == 0 ? 0.282094791773878143 : (l == 1 ? 0.488602511902919921 : 1.0);
-}
 
 /* One task: a slice of the surviving primitive quartets of one contracted quartet.
  * NS > 0: lane-private register accumulators for components c = lane + 32 s, s < NS
@@ -219,7 +63,8 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
     const double common = P.common_base * common_fac_sp(li) * common_fac_sp(lj)
                         * common_fac_sp(lk) * (P.three ? 1.0 : common_fac_sp(ll));
     double *scr_base = greg + T * 3 * L.ng * L.G;
-    double *acc = P.gctr + tk.cart_off;
+    double *acc = P.jmode ? P.wscratch + (size_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * P.wscratch_stride
+                          : P.gctr + tk.cart_off;
 
     /* per-lane component offsets into the g arrays, packed 10 bits per axis */
     int offs[NS > 0 ? NS : 1];
@@ -262,31 +107,8 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             int kl = q / nij, ij = q - kl * nij;
             const CGPrimPair A = ppij[ij];
             const CGPrimPair B = ppkl[kl];
-            double aijkl = A.a + B.a;
-            double rs = rsqrt(aijkl);
-            double inv = rs * rs;
-            double PQx = A.P[0] - B.P[0], PQy = A.P[1] - B.P[1], PQz = A.P[2] - B.P[2];
-            double rr = fma(PQx, PQx, fma(PQy, PQy, PQz * PQz));
-            double rho = A.a * B.a * inv;
-            double x = rho * rr;
-            double s, w;
-            rys_node(n, x, r, P.rys_coef, s, w);
-            double fac1 = common * A.K * B.K * rs * A.inv_a * B.inv_a;
-            double tb = s * inv;                 /* 2 b00 */
-            double b00 = 0.5 * tb;
-            double oms = 1.0 - s;
-            double b10 = fma(0.5 * A.inv_a, oms, b00);
-            double b01 = fma(0.5 * B.inv_a, oms, b00);
-            double ta = tb * B.a, tc = tb * A.a;
             double *rec = term + lane * CG_TERMW;
-            rec[0] = b00; rec[1] = b10; rec[2] = b01;
-            rec[3] = fma(-ta, PQx, A.P[0] - pij.A[0]);
-            rec[4] = fma(-ta, PQy, A.P[1] - pij.A[1]);
-            rec[5] = fma(-ta, PQz, A.P[2] - pij.A[2]);
-            rec[6] = fma(tc, PQx, B.P[0] - pkl.A[0]);
-            rec[7] = fma(tc, PQy, B.P[1] - pkl.A[1]);
-            rec[8] = fma(tc, PQz, B.P[2] - pkl.A[2]);
-            rec[9] = w * fac1;
+            cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec);
             rec[10] = -2.0 * A.aA;
         }
         __syncwarp();
@@ -377,7 +199,36 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             }
         }
     }
-    if (lane == 0) P.nonempty[tk.out] = 1;
+    if (MODE == CG_MODE_ERI && P.jmode) {
+        /* J contraction of this slice (linear, so slices contract independently):
+         * X[i,j] += s_kl sum_kl (ij|kl) D[k,l];  X[k,l] += s_ij sum_ij (ij|kl) D[i,j] if IJ != KL,
+         * s = 2 for an off-diagonal shell pair of the unique list (D and (ij|kl) symmetric). */
+        __syncwarp();
+        const int nao = P.nao;
+        const double skl = (tk.sym & 2) ? 2.0 : 1.0, sij = (tk.sym & 1) ? 2.0 : 1.0;
+        const double *Dkl = P.dm + (size_t)pkl.ao_a * nao + pkl.ao_b;
+        for (int e = lane; e < nfi * nfj; e += 32) {
+            int i = e % nfi, j = e / nfi;
+            double v = 0.0;
+            for (int l = 0; l < nfl; l++)
+                for (int k = 0; k < nfk; k++)
+                    v = fma(acc[i + nfi * (k + nfk * (l + nfl * j))], __ldg(Dkl + (size_t)k * nao + l), v);
+            atomicAdd(P.vj + (size_t)(pij.ao_a + i) * nao + pij.ao_b + j, skl * v);
+        }
+        if (tk.sym & 4) {
+            const double *Dij = P.dm + (size_t)pij.ao_a * nao + pij.ao_b;
+            for (int e = lane; e < nfk * nfl; e += 32) {
+                int k = e % nfk, l = e / nfk;
+                double v = 0.0;
+                for (int j = 0; j < nfj; j++)
+                    for (int i = 0; i < nfi; i++)
+                        v = fma(acc[i + nfi * (k + nfk * (l + nfl * j))], __ldg(Dij + (size_t)i * nao + j), v);
+                atomicAdd(P.vj + (size_t)(pkl.ao_a + k) * nao + pkl.ao_b + l, sij * v);
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0 && !P.jmode) P.nonempty[tk.out] = 1;
 }
 
 template <int MODE>
@@ -515,17 +366,11 @@ cg_output_kernel(const CGOutTask *__restrict__ ot, int nout, double *gctr, const
 extern "C" int cg_kernels_init(const int *c2s_nnz, const int *c2s_idx, const double *c2s_val,
                                double **rys_coef_dev)
 {
-    double xmax[RYS_NMAX + 1];
-    xmax[0] = 0;
-    for (int n = 1; n <= RYS_NMAX; n++) xmax[n] = RYS_H * rys_nint_host[n];
+    int rc = cg_tu_tables_init(c2s_nnz, c2s_idx, c2s_val);
+    if (rc) return rc;
+    rc = cg_grad_tu_init(c2s_nnz, c2s_idx, c2s_val);
+    if (rc) return rc;
     cudaError_t e;
-    if ((e = cudaMemcpyToSymbol(c_rys_off, rys_off_host, sizeof(rys_off_host))) != cudaSuccess) return (int)e;
-    if ((e = cudaMemcpyToSymbol(c_rys_xmax, xmax, sizeof(xmax))) != cudaSuccess) return (int)e;
-    if ((e = cudaMemcpyToSymbol(c_large_r, rys_large_r_host, sizeof(rys_large_r_host))) != cudaSuccess) return (int)e;
-    if ((e = cudaMemcpyToSymbol(c_large_w, rys_large_w_host, sizeof(rys_large_w_host))) != cudaSuccess) return (int)e;
-    if ((e = cudaMemcpyToSymbol(g_c2s_nnz, c2s_nnz, sizeof(int) * C2S_ROWS)) != cudaSuccess) return (int)e;
-    if ((e = cudaMemcpyToSymbol(g_c2s_idx, c2s_idx, sizeof(int) * C2S_ROWS * C2S_MAXNNZ)) != cudaSuccess) return (int)e;
-    if ((e = cudaMemcpyToSymbol(g_c2s_val, c2s_val, sizeof(double) * C2S_ROWS * C2S_MAXNNZ)) != cudaSuccess) return (int)e;
     double *d = nullptr;
     if ((e = cudaMalloc(&d, sizeof(double) * RYS_NCOEF)) != cudaSuccess) return (int)e;
     if ((e = cudaMemcpy(d, rys_coef_host, sizeof(double) * RYS_NCOEF, cudaMemcpyHostToDevice)) != cudaSuccess) {

@@ -7,7 +7,11 @@
 
 #define CG_MODE_ERI 0
 #define CG_MODE_IP1 1
+#define CG_MODE_GRAD 2               /* adjoint, nuclear-coordinate gradient */
+#define CG_MODE_GRADA 3              /* adjoint, coordinates and primitive exponents */
 #define CG_TERMW 12                  /* doubles per term record in shared memory */
+#define CG_TERMW_GRAD 20             /* term record of the adjoint kernel */
+#define CG_GRAD_MAXPRIM 16           /* primitives per shell supported by the exponent adjoint */
 #define CG_WS_SMALL (24 * 1024 / 8)  /* doubles of shared memory per warp, default */
 #define CG_WS_MAX (48 * 1024 / 8)    /* doubles of shared memory per warp, large classes */
 #define CG_C2S_MAXNNZ 16
@@ -31,7 +35,31 @@ typedef struct {
     double common_base;       /* 2 pi^3 / sqrt(pi); times the s/p factors per task */
     int three;                /* int3c2e: the fourth shell is the unit s partner */
     int ws_doubles;
+    /* J contraction (ERI mode only): accumulators in a per-warp slot, contracted at task end */
+    int jmode;
+    double *wscratch;         /* per-warp accumulator slots */
+    int64_t wscratch_stride;
+    const double *dm;         /* Cartesian density, nao x nao, row major */
+    double *vj;               /* J accumulator (one triangle of shell blocks, see the host) */
+    int nao;
 } CGLaunch;
+
+typedef struct {
+    const CGTask *tasks;
+    int ntasks;
+    const CGPair *pairs;
+    const CGPrimPair *prims;
+    const int *pqlist;
+    int *counter;
+    int *status;
+    const double *rys_coef;
+    double common_base;
+    int ws_doubles;
+    const double *dm;         /* Cartesian density, nao x nao */
+    int nao;
+    double *grad;             /* natm x 3 */
+    double *galpha;           /* per global primitive (GRADA only) */
+} CGGradLaunch;
 
 #ifdef __cplusplus
 extern "C" {
@@ -46,6 +74,9 @@ int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStream_t stream)
 int cg_launch_output(const CGOutTask *ot, int nout, double *gctr, const int *nonempty,
                      double *scratch, int64_t scratch_per_warp, int nblocks, double *out,
                      int ncomp, int64_t comp_stride, cudaStream_t stream);
+int cg_grad_tu_init(const int *c2s_nnz, const int *c2s_idx, const double *c2s_val);
+int cg_launch_grad(const CGGradLaunch *P, int mode, int nblocks, cudaStream_t stream);
+int cg_grad_blocks_per_sm(int mode, int ws_doubles);
 int cg_launch_roots(const double *xs, int count, int n, const double *coef, double *s, double *w,
                     cudaStream_t stream);
 #ifdef __cplusplus
