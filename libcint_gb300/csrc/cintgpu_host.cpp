@@ -486,11 +486,6 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
                 }
             }
         }
-        int qsym = 0;
-        if (!P->three) {
-            qsym = (s[0] != s[1] ? 1 : 0) | (s[2] != s[3] ? 2 : 0)
-                 | ((s[0] != s[2] || s[1] != s[3]) ? 4 : 0);
-        }
         if (P->three) { sv[3] = sv[2]; sv[3].l = 0; sv[3].nprim = 1; sv[3].nctr = 1; }
         int d[4], nd[4];
         for (int a = 0; a < 4; a++) {
@@ -515,6 +510,15 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         const ShellView *kv[4] = {&sv[perm[0]], &sv[perm[1]], &sv[perm[2]], &sv[perm[3]]};
         int ksh[4];
         for (int k = 0; k < 4; k++) ksh[k] = (P->three && k == 3) ? -1 : s[perm[k]];
+        /* permutation flags of the unique quartet, in kernel order (the J epilogue weights the
+         * kernel's bra and ket blocks with them) */
+        int qsym = 0;
+        if (!P->three) {
+            int b0 = std::min(ksh[0], ksh[1]), b1 = std::max(ksh[0], ksh[1]);
+            int k0 = std::min(ksh[2], ksh[3]), k1 = std::max(ksh[2], ksh[3]);
+            qsym = (ksh[0] != ksh[1] ? 1 : 0) | (ksh[2] != ksh[3] ? 2 : 0)
+                 | ((b0 != k0 || b1 != k1) ? 4 : 0);
+        }
         int kl_[4] = {kv[0]->l, kv[1]->l, kv[2]->l, kv[3]->l};
         int nct[4] = {kv[0]->nctr, kv[1]->nctr, kv[2]->nctr, P->three ? 1 : kv[3]->nctr};
         for (int c3 = 0; c3 < nct[3]; c3++)
