@@ -27,6 +27,9 @@
  */
 #include "rys_device.cuh"
 
+/* piecewise polynomial Rys tables (rys_tables.inc), copied in at initialisation */
+static __device__ double g_rys_coef[RYS_NCOEF];
+
 __global__ void rys_roots_kernel(const double *__restrict__ xs, int count, int n,
                                  const double *__restrict__ coef, double *s_out, double *w_out)
 {
@@ -371,12 +374,10 @@ extern "C" int cg_kernels_init(const int *c2s_nnz, const int *c2s_idx, const dou
     rc = cg_grad_tu_init(c2s_nnz, c2s_idx, c2s_val);
     if (rc) return rc;
     cudaError_t e;
+    /* the root table lives in the module image; no device allocation at initialisation */
+    if ((e = cudaMemcpyToSymbol(g_rys_coef, rys_coef_host, sizeof(double) * RYS_NCOEF)) != cudaSuccess) return (int)e;
     double *d = nullptr;
-    if ((e = cudaMalloc(&d, sizeof(double) * RYS_NCOEF)) != cudaSuccess) return (int)e;
-    if ((e = cudaMemcpy(d, rys_coef_host, sizeof(double) * RYS_NCOEF, cudaMemcpyHostToDevice)) != cudaSuccess) {
-        cudaFree(d);
-        return (int)e;
-    }
+    if ((e = cudaGetSymbolAddress((void **)&d, g_rys_coef)) != cudaSuccess) return (int)e;
     *rys_coef_dev = d;
     for (int mode = 0; mode < 2; mode++) {
         void *fn = mode == 0 ? (void *)rys_eri_kernel<CG_MODE_ERI> : (void *)rys_eri_kernel<CG_MODE_IP1>;
