@@ -183,6 +183,19 @@ int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,
                        const int64_t *offsets, const int *atm, int natm, const int *bas,
                        int nbas, const double *env);
 
+/* Allocation-free batched int2e_sph (no libcint counterpart).  For callers that cannot allocate
+ * device memory during a call (work enqueued inside a CUDA stream capture, or frameworks that own
+ * the device memory budget).  Same result as a CINTGPU_INT2E_SPH plan with offsets = NULL: out_dev
+ * receives the dense blocks of the n quartets back to back (sum of di*dj*dk*dl doubles).  All
+ * device scratch lives in one static device array of CINTGPU_NOALLOC_BYTES (32 MiB, held by every
+ * GPU that loads the library until exit); a batch needing more returns CINTGPU_ERR_NOMEM with a
+ * message.  The first call on a device sets up the array's address (make it before any stream
+ * capture).  Calls share the array: calls that overlap on the GPU race, so serialise them.
+ * Asynchronous on `stream` (a cudaStream_t); calls no cudaMalloc/cudaFree. */
+#define CINTGPU_NOALLOC_BYTES (32 << 20)
+int cintgpu_int2e_sph_noalloc(double *out_dev, const int *shls, int64_t n, const int *atm,
+                              int natm, const int *bas, int nbas, const double *env, void *stream);
+
 /* Rys nodes s = t^2 and weights from the device tables, for testing: xs, s, w device arrays */
 int cintgpu_rys_roots_dev(int nroots, const double *xs_dev, int count, double *s_dev,
                           double *w_dev, void *stream);

@@ -1211,3 +1211,58 @@ void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas)
 { ao_loc[0] = 0; for (FINT i = 1; i < nbas; i++) ao_loc[i] = ao_loc[i - 1] + CINTcgto_spheric(i - 1, bas); }
 
 }  /* extern "C" */
+
+/* ================================================================== internal hooks */
+#include "cintgpu_internal.h"
+
+int cg_init(void) { return ensure_init(); }
+int cg_sm_count(void) { return g_ctx.sm_count; }
+void cg_set_error_msg(const char *msg) { set_error("%s", msg); }
+CINTGPUPlan *cg_plan_new(void) { return new CINTGPUPlan(); }
+void cg_plan_free_host(CINTGPUPlan *P) { P->dbuf = nullptr; delete P; }
+
+int cg_plan_build(CINTGPUPlan *P, int kind, const int *shls, int64_t n, const int64_t *offsets,
+                  const int *atm, int natm, const int *bas, int nbas, const double *env,
+                  int64_t split_target)
+{
+    return build_plan(P, kind, shls, n, offsets, atm, natm, bas, nbas, env, split_target);
+}
+
+size_t cg_plan_bytes(const CINTGPUPlan *P) { return plan_device_bytes(P); }
+
+int cg_plan_place(CINTGPUPlan *P, char *region, size_t region_bytes, cudaStream_t stream)
+{
+    DevLayout D = dev_layout(P);
+    if (D.total > region_bytes) { set_error("plan needs %zu bytes, region has %zu", D.total, region_bytes); return CINTGPU_ERR_NOMEM; }
+    P->out_blocks = D.out_blocks;
+    P->scratch_per_warp = D.spw;
+    P->dbuf = region; P->dbuf_size = region_bytes; P->owns_dbuf = false;
+    char *p = region;
+    P->d_pairs = (CGPair *)p; p += D.pairs;
+    P->d_prims = (CGPrimPair *)p; p += D.prims;
+    P->d_tasks = (CGTask *)p; p += D.tasks;
+    P->d_outs = (CGOutTask *)p; p += D.outs;
+    P->d_pqlist = (int *)p; p += D.pq;
+    P->d_gctr = (double *)p; p += D.gctr;
+    P->d_counters = (int *)p; p += D.cnt;
+    P->d_nonempty = (int *)p; p += D.ne;
+    P->d_scratch = (double *)p; p += D.scr;
+    P->d_wscratch = (double *)p; p += D.wscr;
+    P->wscratch_stride = P->max_nf;
+    P->wscratch_warps = D.wwarps;
+    std::vector<char> img(D.upload);
+    char *q = img.data();
+    memcpy(q, P->pairs.data(), sizeof(CGPair) * P->pairs.size()); q += D.pairs;
+    memcpy(q, P->prims.data(), sizeof(CGPrimPair) * P->prims.size()); q += D.prims;
+    memcpy(q, P->tasks.data(), sizeof(CGTask) * P->tasks.size()); q += D.tasks;
+    memcpy(q, P->outs.data(), sizeof(CGOutTask) * P->outs.size()); q += D.outs;
+    memcpy(q, P->pqlist.data(), sizeof(int) * P->pqlist.size());
+    /* pageable source: returns once the data is staged, so img may be released afterwards */
+    CUDA_OK(cudaMemcpyAsync(region, img.data(), D.upload, cudaMemcpyHostToDevice, stream));
+    return 0;
+}
+
+int cg_plan_run(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
+{
+    return execute_plan(P, out_dev, stream);
+}
