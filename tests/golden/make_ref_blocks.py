@@ -1,0 +1,82 @@
+"""Generate tests/golden/ref_blocks.npz: libcint's own output blocks for a fixed set of shell
+quartets/triples, so the checker and the CUDA path can be compared with the reference itself on
+machines where libcint's sources (and so oracle/_ref/libcint.so) are absent.
+
+Run where libcint's sources exist:  make -C oracle ref && python tests/golden/make_ref_blocks.py
+
+Contents (all through libcint 6.1.1 built by oracle/Makefile, opt = NULL, cache = NULL):
+  kat_int2e_sph / kat_int2e_ip1_sph  90 quartets (every 5th with <= 450 elements) of libcint
+                                     testsuite/test_cint.py's loop over its self-contained basis
+                                     (nbas = 4 passed, 8 shells)
+  c0_int2e_sph / c0_int2e_cart / c0_int2e_ip1_sph   60 unique quartets of molecules.config0(3)
+  c2_int3c2e_sph                     60 (ij|P) triples of molecules.config2(1, natm=6, box=5)
+  cache_sizes                        the out == NULL cache-size answers for a few quartets
+Each block is stored flattened in libcint's (Fortran) order with its item list.
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from libcint_gb300 import molecules as M  # noqa: E402
+from tests import _oracle  # noqa: E402
+
+
+def main():
+    o = _oracle.load()
+    assert o.ref is not None, 'build libcint first: make -C oracle ref'
+    out = {}
+    mol, nbas = M.kat_basis()
+    items = []
+    for l in range(8):
+        for k in range(l + 1):
+            for j in range(8):
+                for i in range(j + 1):
+                    items.append((i, j, k, l))
+    size = lambda q: int(np.prod([mol.nsph(s) for s in q]))
+    items = np.array([q for q in items[::5] if size(q) <= 450][:90], dtype=np.int32)
+    for name in ('int2e_sph', 'int2e_ip1_sph'):
+        blocks = [o.ref.call(name, mol, q, nbas=nbas)[1].ravel(order='F') for q in items]
+        out['kat_' + name + '_items'] = items
+        out['kat_' + name] = np.concatenate(blocks)
+    mol0 = M.config0(seed=3)
+    rng = np.random.RandomState(9)
+    qs = M.unique_quartets(mol0.nbas)
+    qs = qs[rng.choice(len(qs), 60, replace=False)].astype(np.int32)
+    for name in ('int2e_sph', 'int2e_cart', 'int2e_ip1_sph'):
+        blocks = [o.ref.call(name, mol0, q)[1].ravel(order='F') for q in qs]
+        out['c0_' + name + '_items'] = qs
+        out['c0_' + name] = np.concatenate(blocks)
+    mol2, norb = M.config2(seed=1, natm=6, box=5.0)
+    tr = []
+    for _ in range(60):
+        i, j = sorted(rng.randint(0, norb, 2))[::-1]
+        tr.append((i, j, rng.randint(norb, mol2.nbas)))
+    tr = np.array(tr, dtype=np.int32)
+    out['c2_int3c2e_sph_items'] = tr
+    out['c2_int3c2e_sph'] = np.concatenate([o.ref.call('int3c2e_sph', mol2, t)[1].ravel(order='F')
+                                            for t in tr])
+    # cache-size answers (out == NULL)
+    f = o.ref.lib
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    cs = []
+    for name, q in (('int2e_sph', (1, 3, 5, 7)), ('int2e_ip1_sph', (3, 1, 2, 0)),
+                    ('int2e_cart', (1, 1, 0, 0)), ('int3c2e_sph', (2, 1, 3, 0))):
+        shls = np.array(q, dtype=np.int32)
+        r = getattr(f, name)(None, None, P(shls), P(mol.atm), mol.natm, P(mol.bas), nbas,
+                             P(mol.env), None, None)
+        cs.append((name, q, r))
+    out['cache_names'] = np.array([c[0] for c in cs])
+    out['cache_shls'] = np.array([c[1] for c in cs], dtype=np.int32)
+    out['cache_sizes'] = np.array([c[2] for c in cs], dtype=np.int64)
+    np.savez_compressed(os.path.join(HERE, 'ref_blocks.npz'), **out)
+    print({k: v.shape for k, v in out.items()})
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,87 @@
+"""The C-ABI library: loads without a GPU, exports every function include/cintgpu.h declares, its
+host-only parts agree with libcint (cart->sph rows, basis helpers, cache-size answers), and the
+compute entry points fail loudly when no GPU is usable (no CPU fallback).  CPU only."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from libcint_gb300 import molecules as M
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_functions():
+    src = open(os.path.join(ROOT, 'include', 'cintgpu.h')).read()
+    src = re.sub(r'/\*.*?\*/', ' ', src, flags=re.S)
+    src = '\n'.join(l for l in src.splitlines() if not l.strip().startswith('#'))
+    names = []
+    for chunk in ' '.join(src.split()).split(';'):
+        chunk = chunk.strip()
+        if not chunk or chunk.startswith('typedef') or '{' in chunk or '}' in chunk:
+            continue
+        m = re.search(r'(\w+)\s*\(', chunk)
+        if m:
+            names.append(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_function(gpulib):
+    L = gpulib.lib()
+    names = _declared_functions()
+    assert len(names) > 40
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_cart2sph_rows_match_checker(gpulib, oracle):
+    L = gpulib.lib()
+    ol = oracle.port.lib
+    for l in range(0, 7):
+        nc = (l + 1) * (l + 2) // 2
+        ns = 2 * l + 1 if l > 1 else nc
+        a = np.zeros(ns * nc)
+        b = np.zeros(ns * nc)
+        assert L.cintgpu_cart2sph(l, a.ctypes.data_as(ctypes.c_void_p)) == ns
+        ol.oracle_cart2sph_coeff(l, b.ctypes.data_as(ctypes.c_void_p))
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-15)
+
+
+def test_basis_helpers(gpulib):
+    L = gpulib.lib()
+    for l in range(6):
+        for a in (0.05, 1.0, 37.5):
+            assert abs(L.CINTgto_norm(l, a) - M.gto_norm(l, a)) <= 1e-14 * M.gto_norm(l, a)
+    mol = M.config0(seed=1)
+    L.CINTtot_cgto_spheric.restype = ctypes.c_int
+    assert L.CINTtot_cgto_spheric(mol.bas.ctypes.data_as(ctypes.c_void_p), mol.nbas) == 104
+    loc = np.zeros(mol.nbas, dtype=np.int32)
+    L.CINTshells_spheric_offset(loc.ctypes.data_as(ctypes.c_void_p),
+                                mol.bas.ctypes.data_as(ctypes.c_void_p), mol.nbas)
+    np.testing.assert_array_equal(loc, mol.ao_loc()[:-1])
+
+
+def test_cache_size_query_matches_libcint(gpulib):
+    """out == NULL returns libcint's cache size (src/cint2e.c:801-816); pure host path."""
+    fx = np.load(os.path.join(ROOT, 'tests', 'golden', 'ref_blocks.npz'))
+    mol, nbas = M.kat_basis()
+    L = gpulib.lib()
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    for name, shls, want in zip(fx['cache_names'], fx['cache_shls'], fx['cache_sizes']):
+        s = np.ascontiguousarray(shls, dtype=np.int32)
+        got = getattr(L, str(name))(None, None, P(s), P(mol.atm), mol.natm, P(mol.bas), nbas,
+                                    P(mol.env), None, None)
+        assert got == want, (name, got, want)
+
+
+def test_no_gpu_fails_loudly(gpulib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip('a GPU is present')
+    mol = M.config0(seed=0)
+    with pytest.raises(gpulib.CintGpuError, match='CUDA'):
+        gpulib.Plan(gpulib.INT2E_SPH, mol, M.unique_quartets(mol.nbas)[:4])
+    flag, blk = gpulib.dropin('int2e_sph', mol, (1, 0, 0, 0))
+    assert flag == 0 and not blk.any() and gpulib.last_error()

@@ -3,7 +3,7 @@
 Tolerances: the reference's own accuracy statement is ~1e-12 relative (libcint README.rst:217)
 and its root fits deviate from 60-digit values by up to ~4e-12 (n = 7), so element-wise gates are
 ABS_TOL = 1e-12 absolute everywhere and REL_TOL = 1e-10 relative where |ref| > 1e-10 and
-|ref| > 1e-4 * max|Cartesian block| (elements produced by cancellation in the cart -> sph transform
+|ref| > 1e-3 * max|Cartesian block| (elements produced by cancellation in the cart -> sph transform
 carry the block's absolute error, not their own relative one; see assert_block_close).  Golden sums use libcint's own
 criterion round(|v - ref| / sqrt(count), place) == 0 (testsuite/test_cint.py:148-149).
 """
@@ -24,16 +24,18 @@ def close_kat(v, ref, count, place):
 
 def assert_block_close(a, b, what='', scale=None):
     """abs <= ABS_TOL everywhere; rel <= REL_TOL where |b| > 1e-10 and the element is not
-    dominated by cancellation, i.e. |b| > 1e-4 * scale (scale: the block's Cartesian maximum
+    dominated by cancellation, i.e. |b| > 1e-3 * scale (scale: the block's Cartesian maximum
     when given, else max|b|).  Cart -> sph of high-l shells cancels up to 5 decades (an (ss|g)
     block has Cartesian elements 1e5 x its spherical ones), so relative agreement of the
-    cancelled elements is bounded by the conditioning, for libcint itself as well."""
+    cancelled elements is bounded by the conditioning, for libcint itself as well: elements below
+    1e-3 of the block's largest Cartesian element carry ~1e-14 of that maximum as rounding, i.e.
+    up to ~1e-10 of themselves (libcint vs the checker: 2.1e-10 at 1.1e-4 of the maximum)."""
     a = np.asarray(a).ravel()
     b = np.asarray(b).ravel()
     d = np.abs(a - b)
     assert d.max(initial=0) <= ABS_TOL, '%s max abs diff %.3e' % (what, d.max(initial=0))
     sc = np.abs(b).max(initial=0) if scale is None else scale
-    big = (np.abs(b) > 1e-10) & (np.abs(b) > 1e-4 * sc)
+    big = (np.abs(b) > 1e-10) & (np.abs(b) > 1e-3 * sc)
     if big.any():
         rel = (d[big] / np.abs(b[big])).max()
         assert rel <= REL_TOL, '%s max rel diff %.3e' % (what, rel)
@@ -176,3 +178,29 @@ def test_batched_3c2e(gpulib, oracle):
         assert_block_close(res[off:off + nb], oblk.ravel(order='F'), '3c2e %s' % (it,),
                            cart_scale(oracle, 'int3c2e_sph', mol, it))
         off += nb
+
+
+@pytest.mark.parametrize('key', ['kat_int2e_sph', 'kat_int2e_ip1_sph', 'c0_int2e_sph',
+                                 'c0_int2e_cart', 'c0_int2e_ip1_sph', 'c2_int3c2e_sph'])
+def test_gpu_matches_libcint_blocks(gpulib, oracle, key):
+    """Directly against libcint's own output (tests/golden/ref_blocks.npz, generated by
+    make_ref_blocks.py from libcint built from its sources)."""
+    import os
+    fx = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'ref_blocks.npz'))
+    items, ref = fx[key + '_items'], fx[key]
+    name = key.split('_', 1)[1]
+    nbas = None
+    if key.startswith('kat'):
+        mol, nbas = M.kat_basis()
+    elif key.startswith('c0'):
+        mol = M.config0(seed=3)
+    else:
+        mol, _ = M.config2(seed=1, natm=6, box=5.0)
+    off = 0
+    for it in items:
+        _, blk = gpulib.dropin(name, mol, it, nbas=nbas)
+        b = blk.ravel(order='F')
+        assert_block_close(b, ref[off:off + b.size], '%s %s' % (key, it),
+                           cart_scale(oracle, name, mol, it, nbas))
+        off += b.size
+    assert off == ref.size

@@ -1,0 +1,116 @@
+"""The checker pinned before it is trusted: the C restatement (oracle/) against libcint's golden
+values, against libcint's own output blocks (fixture made by tests/golden/make_ref_blocks.py) and,
+where libcint was built from its sources here, against libcint live.  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+from libcint_gb300 import molecules as M
+
+GOLD = os.path.join(os.path.dirname(__file__), 'golden')
+
+
+def close_kat(v, ref, count, place):
+    """libcint testsuite/test_cint.py:148-149"""
+    return round(abs(v - ref) / count ** .5, place) == 0
+
+
+def _kat_items():
+    out = []
+    for l in range(8):
+        for k in range(l + 1):
+            for j in range(8):
+                for i in range(j + 1):
+                    out.append((i, j, k, l))
+    return out
+
+
+@pytest.mark.parametrize('name,golden', [('int2e_sph', 56243.88080655417),
+                                         ('int2e_ip1_sph', 115489.8647398112)])
+def test_oracle_reproduces_libcint_golden_sums(oracle, name, golden):
+    """testsuite/test_cint.py:479-480"""
+    mol, nbas = M.kat_basis()
+    v, cnt = 0.0, 0
+    for q in _kat_items():
+        _, blk = oracle.port.call(name, mol, q, nbas=nbas)
+        v += np.abs(blk).sum()
+        cnt += blk.size
+    assert close_kat(v, golden, cnt, 8), v
+
+
+def test_oracle_reproduces_3c2e_golden_sum(oracle):
+    """testsuite/test_3c2e.py:303 and the 3c2e == 4c2e(zero-exponent fit shell) identity"""
+    mol, nbas = M.kat_basis_3c2e()
+    v, cnt = 0.0, 0
+    for k in range(nbas):
+        mol.bas[8, M.ATOM_OF] = mol.bas[k, M.ATOM_OF]
+        for j in range(nbas):
+            for i in range(nbas):
+                _, b3 = oracle.port.call('int3c2e_sph', mol, (i, j, k), nbas=nbas)
+                _, b4 = oracle.port.call('int2e_sph', mol, (i, j, k, 8), nbas=nbas)
+                np.testing.assert_allclose(b3.ravel(), b4.ravel(), rtol=1e-10, atol=1e-12)
+                v += np.abs(b3).sum()
+                cnt += b3.size
+    assert close_kat(v, 1586.350797347553, cnt, 10), v
+
+
+def _compare(got, ref, scale):
+    d = np.abs(got - ref)
+    assert d.max() <= 1e-12, d.max()
+    big = (np.abs(ref) > 1e-10) & (np.abs(ref) > 1e-3 * scale)
+    if big.any():
+        assert (d[big] / np.abs(ref[big])).max() <= 1e-10
+
+
+@pytest.mark.parametrize('key,molname', [('kat_int2e_sph', 'kat'), ('kat_int2e_ip1_sph', 'kat'),
+                                         ('c0_int2e_sph', 'c0'), ('c0_int2e_cart', 'c0'),
+                                         ('c0_int2e_ip1_sph', 'c0'), ('c2_int3c2e_sph', 'c2')])
+def test_oracle_matches_libcint_blocks(oracle, key, molname):
+    fx = np.load(os.path.join(GOLD, 'ref_blocks.npz'))
+    items, ref = fx[key + '_items'], fx[key]
+    name = key.split('_', 1)[1]
+    nbas = None
+    if molname == 'kat':
+        mol, nbas = M.kat_basis()
+    elif molname == 'c0':
+        mol = M.config0(seed=3)
+    else:
+        mol, _ = M.config2(seed=1, natm=6, box=5.0)
+    off = 0
+    for it in items:
+        _, blk = oracle.port.call(name, mol, it, nbas=nbas)
+        b = blk.ravel(order='F')
+        scale = np.abs(b).max(initial=0)
+        if name.endswith('_sph'):
+            _, c = oracle.port.call(name[:-4] + '_cart', mol, it, nbas=nbas)
+            scale = np.abs(c).max(initial=0)
+        _compare(b, ref[off:off + b.size], scale)
+        off += b.size
+    assert off == ref.size
+
+
+def test_oracle_matches_libcint_live_c1(oracle):
+    if oracle.ref is None:
+        pytest.skip('libcint not built from sources on this machine')
+    mol = M.config1(seed=0)
+    qs = np.load(os.path.join(GOLD, 'c1_quartets.npz'))['quartets'][:150]
+    for q in qs:
+        _, a = oracle.port.call('int2e_sph', mol, q)
+        _, b = oracle.ref.call('int2e_sph', mol, q)
+        assert np.abs(a - b).max() <= 1e-12
+
+
+def test_oracle_roots_against_mpmath(oracle):
+    pytest.importorskip('mpmath')
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(__file__)), 'libcint_gb300', 'csrc'))
+    import rys_exact as R
+    rng = np.random.RandomState(3)
+    for n in (1, 2, 5, 7, 9, 12):
+        for x in list(rng.uniform(0, 60 + 5 * n, 6)) + [0.0, 1e-9, 300.0]:
+            s, w = R.rys_exact(n, x)
+            so, wo = oracle.roots(n, x)
+            f0 = float(sum(w))
+            assert max(abs(float(a) - b) for a, b in zip(s, so)) < 1e-14
+            assert max(abs(float(a) - b) for a, b in zip(w, wo)) < 1e-14 * f0
