@@ -150,6 +150,127 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _timed(fn, reps=3):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return best
+
+
+def extra_dropin(cg, mol, qs, batched_value, n=2000):
+    """The plain drop-in: one libcint-signature int2e_sph call per quartet (host buffers)."""
+    sub = qs[:n]
+    nint = integrals_of(mol, sub)
+    buf = np.zeros(int(max(np.prod([mol.nsph(s) for s in q]) for q in sub)))
+    f = cg.lib().int2e_sph
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    f(P(buf), None, P(np.ascontiguousarray(sub[0])), P(mol.atm), mol.natm, P(mol.bas), mol.nbas,
+      P(mol.env), None, None)
+    t0 = time.perf_counter()
+    for q in sub:
+        f(P(buf), None, P(np.ascontiguousarray(q)), P(mol.atm), mol.natm, P(mol.bas), mol.nbas,
+          P(mol.env), None, None)
+    dt = time.perf_counter() - t0
+    v = nint / dt
+    return {'workload': 'first %d quartets of the c1 list, one int2e_sph call each' % n,
+            'integrals_per_s': v, 'quartets_per_s': n / dt, 'batched_over_dropin': batched_value / v}
+
+
+def extra_int3c2e(cg, seed=0, npairs=40):
+    """c2: (ij|P) for screened orbital pairs against every auxiliary shell, batched."""
+    import torch
+    from libcint_gb300 import molecules as M
+    mol, norb = M.config2(seed=seed)
+    # unit zero-exponent s shell for (P|P) = (P fit|P fit) (libcint testsuite/test_3c2e.py:134-146)
+    env = list(mol.env)
+    pe = len(env)
+    env += [0.0, 2.0 * np.sqrt(np.pi)]
+    bas = np.vstack([mol.bas, [[0, 0, 1, 1, 0, pe, pe + 1, 0]]]).astype(np.int32)
+    molf = M.Mol(mol.atm, bas, np.array(env), mol.name)
+    fit = bas.shape[0] - 1
+    aux = np.arange(norb, mol.nbas, dtype=np.int32)
+
+    def diag_max(items):
+        p = cg.Plan(cg.INT2E_SPH, molf, items)
+        out = torch.zeros(p.output_size, dtype=torch.float64, device='cuda')
+        p.execute(out)
+        torch.cuda.synchronize()
+        v = np.abs(out.cpu().numpy())
+        d = np.array([molf.nsph(int(a)) * molf.nsph(int(b)) for a, b, _, _ in items]) ** 2
+        return np.maximum.reduceat(v, np.concatenate([[0], np.cumsum(d)[:-1]]))
+    qp = np.sqrt(diag_max(np.stack([aux, np.full_like(aux, fit), aux, np.full_like(aux, fit)], 1)))
+    rng = np.random.RandomState(seed)
+    ii = rng.randint(0, norb, 4 * npairs)
+    jj = rng.randint(0, norb, 4 * npairs)
+    pr = np.unique(np.stack([np.maximum(ii, jj), np.minimum(ii, jj)], 1), axis=0)[:npairs * 2]
+    qij = np.sqrt(diag_max(np.concatenate([pr, pr], 1).astype(np.int32)))
+    keep = qij * qp.max() >= 1e-12
+    pr = pr[keep][:npairs]
+    qij = qij[keep][:npairs]
+    tri = np.array([(i, j, P) for (i, j), q in zip(pr, qij) for P, qq in zip(aux, qp)
+                    if q * qq >= 1e-12], dtype=np.int32)
+    p = cg.Plan(cg.INT3C2E_SPH, mol, tri)
+    out = torch.empty(p.output_size, dtype=torch.float64, device='cuda')
+    dt = _timed(lambda: p.execute(out))
+    nint = sum(mol.nsph(int(a)) * mol.nsph(int(b)) * mol.nsph(int(c)) for a, b, c in tri)
+    return {'workload': 'c2: 200 atoms, 18 A; %d screened orbital pairs x all 2000 aux shells '
+                        '(Q_ij Q_P >= 1e-12)' % len(pr),
+            'triples': int(len(tri)), 'integrals_per_s': nint / dt, 'ms': 1e3 * dt,
+            'fp64_frac': p.flops / dt / 1e12 / FP64_PEAK_TFLOPS}
+
+
+def extra_adjoint(cg, seed=0):
+    """c3: 24 atoms, full unique quartet list; adjoint gradient vs int2e_ip1 formed and contracted
+    on the same GPU; agreement between the two."""
+    import torch
+    from libcint_gb300 import molecules as M
+    from libcint_gb300.coulomb import CoulombPlans, grad_via_ip1
+    mol = M.config3(seed=seed)
+    nao = sum(mol.nsph(i) for i in range(mol.nbas))
+    rng = np.random.RandomState(seed)
+    d = rng.normal(0, 0.1, (nao, nao))
+    dm = torch.as_tensor(0.5 * (d + d.T), device='cuda')
+    plans = CoulombPlans(mol)
+    t_fwd = _timed(lambda: plans.energy(dm))
+    g_adj = [None]
+
+    def adj():
+        g_adj[0] = plans.grad(dm)[0]
+    t_adj = _timed(adj)
+    g_ip1 = [None]
+
+    def ip1():
+        g_ip1[0] = grad_via_ip1(mol, dm)
+    t_ip1 = _timed(ip1, reps=1)
+    diff = float((g_adj[0] - g_ip1[0]).abs().max() / g_ip1[0].abs().max())
+    plans_a = CoulombPlans(mol, with_exponents=True)
+    t_adj_a = _timed(lambda: plans_a.grad(dm))
+    return {'workload': 'c3: 24 atoms, 8 A, s,p,d x 3-5 prims, all %d unique quartets'
+                        % len(M.unique_quartets(mol.nbas)),
+            'forward_J_ms': 1e3 * t_fwd, 'adjoint_grad_ms': 1e3 * t_adj,
+            'adjoint_grad_with_exponents_ms': 1e3 * t_adj_a, 'ip1_route_grad_ms': 1e3 * t_ip1,
+            'adjoint_speedup_over_ip1': t_ip1 / t_adj, 'max_rel_diff_vs_ip1': diff}
+
+
+def run_extras(cg, mol, qs, value, args):
+    out = {}
+    for name, fn in (('dropin', lambda: extra_dropin(cg, mol, qs, value)),
+                     ('int3c2e', lambda: extra_int3c2e(cg)),
+                     ('adjoint', lambda: extra_adjoint(cg))):
+        try:
+            out[name] = fn()
+        except Exception as e:  # an extra must not hide the headline line
+            out[name] = {'error': repr(e)[:300]}
+    return out
+
+
 def run_gpu(args, rank, world):
     import torch
     import libcint_gb300 as cg
@@ -239,6 +360,8 @@ def run_gpu(args, rank, world):
                 'path': 'cintgpu_batch_host (plan + H2D + kernels + D2H), wall clock'},
         'clocks': clocks,
     }
+    if not args.no_extras:
+        line['extras'] = run_extras(cg, mol, qs, value, args)
     if not args.no_cpu:
         res = cpu_port_rate(mol, qs, os.cpu_count(), target_s=args.cpu_seconds)
         line['cpu_baseline'] = {'value': res['integrals'] / res['seconds'], 'unit': 'integrals/s',
@@ -258,6 +381,7 @@ def main():
     ap.add_argument('--e2e-steps', type=int, default=3)
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-extras', action='store_true', help='skip the drop-in, int3c2e and adjoint lines')
     args = ap.parse_args()
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))

@@ -240,6 +240,9 @@ struct CINTGPUPlan {
     std::vector<CGTask> tasks;
     std::vector<CGOutTask> outs;
     std::vector<int> pqlist;       /* surviving primitive quartets, per task slice */
+    std::vector<CGGradClass> gclass;   /* adjoint iteration tables per class */
+    std::vector<CGGradChunk> gchunk;
+    std::vector<CGGradEnt> gent;
     std::vector<int> out_item;     /* item index of each CGOutTask */
     TaskGroup groups[2];           /* [0] regular classes, [1] classes needing 48 KB per warp */
     int64_t gctr_size = 0;
@@ -252,6 +255,9 @@ struct CINTGPUPlan {
     CGTask *d_tasks = nullptr;
     CGOutTask *d_outs = nullptr;
     int *d_pqlist = nullptr;
+    CGGradClass *d_gclass = nullptr;
+    CGGradChunk *d_gchunk = nullptr;
+    CGGradEnt *d_gent = nullptr;
     double *d_gctr = nullptr;
     int *d_counters = nullptr;     /* [0], [1]: task counters of the groups; [2]: status */
     int *d_nonempty = nullptr;
@@ -407,6 +413,62 @@ double flops_per_primq(int li, int lj, int lk, int ll, int mode)
 }
 
 }  // namespace
+
+/* Adjoint iteration tables of one class (kernel order li, lj, lk, ll): for every axis a and a-axis
+ * power tuple u, the Cartesian components sharing u, as (partner g offsets, component index),
+ * in chunks of <= 16 sorted longest first.  See rys_grad.cu. */
+static int build_grad_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
+{
+    CGLayout L;
+    cg_layout(li, lj, lk, ll, P->mode, CG_WS_MAX, &L);
+    const int l[4] = {li, lj, lk, ll};
+    const int nfc[4] = {ncart_l(li), ncart_l(lj), ncart_l(lk), ncart_l(ll)};
+    auto cidx = [](int lq, int lx, int ly) { int r = lq - lx; return r * (r + 1) / 2 + (r - ly); };
+    struct Ch { int axis_u, ent, len; };
+    std::vector<Ch> list;
+    for (int a = 0; a < 3; a++) {
+        const int b = a == 2 ? 0 : a + 1, c = 3 - a - b;
+        int u = 0;
+        for (int p3 = 0; p3 <= l[3]; p3++)
+        for (int p2 = 0; p2 <= l[2]; p2++)
+        for (int p1 = 0; p1 <= l[1]; p1++)
+        for (int p0 = 0; p0 <= l[0]; p0++) {
+            u = ((p3 * (l[2] + 1) + p2) * (l[1] + 1) + p1) * (l[0] + 1) + p0;
+            const int p[4] = {p0, p1, p2, p3};
+            int start = (int)P->gent.size();
+            for (int b3 = 0; b3 <= l[3] - p[3]; b3++)
+            for (int b2 = 0; b2 <= l[2] - p[2]; b2++)
+            for (int b1 = 0; b1 <= l[1] - p[1]; b1++)
+            for (int b0 = 0; b0 <= l[0] - p[0]; b0++) {
+                const int bb[4] = {b0, b1, b2, b3};
+                int cc[4], pw[3][4];
+                for (int q = 0; q < 4; q++) {
+                    cc[q] = l[q] - p[q] - bb[q];
+                    pw[a][q] = p[q]; pw[b][q] = bb[q]; pw[c][q] = cc[q];
+                }
+                int ob = ((bb[0] * L.dJ + bb[1]) * L.dK + bb[2]) * L.dL + bb[3];
+                int oc = ((cc[0] * L.dJ + cc[1]) * L.dK + cc[2]) * L.dL + cc[3];
+                int ci[4];
+                for (int q = 0; q < 4; q++) ci[q] = cidx(l[q], pw[0][q], pw[1][q]);
+                CGGradEnt e;
+                e.ob_oc = ob | (oc << 16);
+                e.c = ((ci[0] * nfc[1] + ci[1]) * nfc[2] + ci[2]) * nfc[3] + ci[3];
+                P->gent.push_back(e);
+            }
+            int total = (int)P->gent.size() - start;
+            for (int o = 0; o < total; o += 16)
+                list.push_back({a | (u << 2), start + o, std::min(16, total - o)});
+        }
+    }
+    std::stable_sort(list.begin(), list.end(), [](const Ch &x, const Ch &y) { return x.len > y.len; });
+    CGGradClass gc;
+    gc.chunk_off = (int)P->gchunk.size();
+    gc.nchunk = (int)list.size();
+    gc.pad0 = gc.pad1 = 0;
+    for (const Ch &x : list) P->gchunk.push_back({x.axis_u, x.ent, x.len, 0});
+    P->gclass.push_back(gc);
+    return (int)P->gclass.size() - 1;
+}
 
 static void free_plan_device(CINTGPUPlan *p)
 {
@@ -584,13 +646,14 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     double target = std::max(fl / (warps * 32.0), 2.0e5);
     if (split_target > 0) target = std::min(target, fl / (double)split_target);
     /* shared memory per warp of the regular group: 24 KB unless CINTGPU_WS_KB overrides (tuning) */
-    int ws_small = (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) ? CG_WS_MAX : CG_WS_SMALL;
+    int ws_small = CG_WS_SMALL;
     if (const char *e = getenv("CINTGPU_WS_KB")) {
         int kb = atoi(e);
         if (kb >= 8 && kb <= 48) ws_small = kb * 1024 / 8;
     }
     struct TaskCost { CGTask t; double cost; int group; };
     std::vector<TaskCost> tc;
+    std::unordered_map<int, int> grad_cls;
     int64_t gpos = 0;
     for (const Work &w : work) {
         const Pending &pe = pend[w.pe];
@@ -613,6 +676,13 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         int64_t slot = (int64_t)nf * P->ncomp;
         CGOutTask &o = P->outs[pe.out];
         o.cart_off = gpos;
+        int cls = 0;
+        if (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) {
+            int key = ((pe.l[0] * 16 + pe.l[1]) * 16 + pe.l[2]) * 16 + pe.l[3];
+            auto it = grad_cls.find(key);
+            cls = it != grad_cls.end() ? it->second
+                                       : (grad_cls[key] = build_grad_class(P, pe.l[0], pe.l[1], pe.l[2], pe.l[3]));
+        }
         for (int64_t a0 = 0; a0 < w.n; a0 += slice) {
             TaskCost x;
             x.t.pij = pe.pij; x.t.pkl = pe.pkl;
@@ -621,6 +691,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             x.t.cart_off = gpos;
             x.t.out = pe.out;
             x.t.sym = pe.sym;
+            x.t.cls = cls;
+            x.t.pad = 0;
             x.cost = x.t.npq * w.cost_pq;
             x.group = group;
             tc.push_back(x);
@@ -649,7 +721,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
 }
 
 struct DevLayout {
-    size_t pairs, prims, tasks, outs, pq, gctr, cnt, ne, scr, wscr;
+    size_t pairs, prims, tasks, outs, pq, gcl, gch, gen, gctr, cnt, ne, scr, wscr;
     int wwarps;
     size_t upload, total;
     int out_blocks;
@@ -667,18 +739,22 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     D.tasks = al(sizeof(CGTask) * std::max<size_t>(P->tasks.size(), 1));
     D.outs = al(sizeof(CGOutTask) * std::max<size_t>(P->outs.size(), 1));
     D.pq = al(sizeof(int) * std::max<size_t>(P->pqlist.size(), 1));
+    D.gcl = al(sizeof(CGGradClass) * std::max<size_t>(P->gclass.size(), 1));
+    D.gch = al(sizeof(CGGradChunk) * std::max<size_t>(P->gchunk.size(), 1));
+    D.gen = al(sizeof(CGGradEnt) * std::max<size_t>(P->gent.size(), 1));
     D.gctr = al(sizeof(double) * P->gctr_size);
     D.cnt = al(sizeof(int) * 4);
     D.ne = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
     D.scr = al(sizeof(double) * D.spw * D.out_blocks * 4);
     D.wwarps = 0;
     D.wscr = 0;
-    if (P->jmode) {
+    const bool grad = P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA;
+    if (P->jmode || (grad && P->max_nf > CG_W_SMEM)) {
         D.wwarps = g_ctx.sm_count * 4 * (P->groups[0].blocks_per_sm + P->groups[1].blocks_per_sm);
         D.wscr = al(sizeof(double) * (size_t)D.wwarps * P->max_nf);
-        D.gctr = al(sizeof(double));   /* J plans keep no per-task accumulators */
     }
-    D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq;
+    if (P->jmode || grad) D.gctr = al(sizeof(double));   /* no per-task accumulators */
+    D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq + D.gcl + D.gch + D.gen;
     D.total = D.upload + D.gctr + D.cnt + D.ne + D.scr + D.wscr;
     return D;
 }
@@ -712,6 +788,12 @@ static int upload_plan(CINTGPUPlan *P, char *arena, size_t arena_size, cudaStrea
     P->d_tasks = (CGTask *)p; p += D.tasks;
     P->d_outs = (CGOutTask *)p; p += D.outs;
     P->d_pqlist = (int *)p; p += D.pq;
+    P->d_gclass = (CGGradClass *)p; p += D.gcl;
+    P->d_gchunk = (CGGradChunk *)p; p += D.gch;
+    P->d_gent = (CGGradEnt *)p; p += D.gen;
+    P->d_gclass = (CGGradClass *)p; p += D.gcl;
+    P->d_gchunk = (CGGradChunk *)p; p += D.gch;
+    P->d_gent = (CGGradEnt *)p; p += D.gen;
     P->d_gctr = (double *)p; p += D.gctr;
     P->d_counters = (int *)p; p += D.cnt;
     P->d_nonempty = (int *)p; p += D.ne;
@@ -729,6 +811,9 @@ static int upload_plan(CINTGPUPlan *P, char *arena, size_t arena_size, cudaStrea
     memcpy(q, P->tasks.data(), sizeof(CGTask) * P->tasks.size()); q += D.tasks;
     memcpy(q, P->outs.data(), sizeof(CGOutTask) * P->outs.size()); q += D.outs;
     memcpy(q, P->pqlist.data(), sizeof(int) * P->pqlist.size()); q += D.pq;
+    memcpy(q, P->gclass.data(), sizeof(CGGradClass) * P->gclass.size()); q += D.gcl;
+    memcpy(q, P->gchunk.data(), sizeof(CGGradChunk) * P->gchunk.size()); q += D.gch;
+    memcpy(q, P->gent.data(), sizeof(CGGradEnt) * P->gent.size()); q += D.gen;
     if (async_from_pinned) {
         CUDA_OK(cudaMemcpyAsync(P->dbuf, src, D.upload, cudaMemcpyHostToDevice, stream));
     } else {
@@ -756,6 +841,13 @@ static int launch_grad_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.nao = P->nao_cart;
     L.grad = P->cur_grad;
     L.galpha = P->cur_galpha;
+    L.gclass = P->d_gclass;
+    L.gchunk = P->d_gchunk;
+    L.gent = P->d_gent;
+    L.wglobal = P->d_wscratch;
+    if (g == 1 && P->d_wscratch)
+        L.wglobal += (size_t)g_ctx.sm_count * 4 * P->groups[0].blocks_per_sm * P->max_nf;
+    L.wstride = P->max_nf;
     int nblocks = std::min(g_ctx.sm_count * G.blocks_per_sm, std::max(1, (G.ntasks + 3) / 4));
     int rc = cg_launch_grad(&L, P->mode, nblocks, stream);
     if (rc) { set_error("adjoint kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
@@ -1243,6 +1335,12 @@ int cg_plan_place(CINTGPUPlan *P, char *region, size_t region_bytes, cudaStream_
     P->d_tasks = (CGTask *)p; p += D.tasks;
     P->d_outs = (CGOutTask *)p; p += D.outs;
     P->d_pqlist = (int *)p; p += D.pq;
+    P->d_gclass = (CGGradClass *)p; p += D.gcl;
+    P->d_gchunk = (CGGradChunk *)p; p += D.gch;
+    P->d_gent = (CGGradEnt *)p; p += D.gen;
+    P->d_gclass = (CGGradClass *)p; p += D.gcl;
+    P->d_gchunk = (CGGradChunk *)p; p += D.gch;
+    P->d_gent = (CGGradEnt *)p; p += D.gen;
     P->d_gctr = (double *)p; p += D.gctr;
     P->d_counters = (int *)p; p += D.cnt;
     P->d_nonempty = (int *)p; p += D.ne;
@@ -1256,7 +1354,10 @@ int cg_plan_place(CINTGPUPlan *P, char *region, size_t region_bytes, cudaStream_
     memcpy(q, P->prims.data(), sizeof(CGPrimPair) * P->prims.size()); q += D.prims;
     memcpy(q, P->tasks.data(), sizeof(CGTask) * P->tasks.size()); q += D.tasks;
     memcpy(q, P->outs.data(), sizeof(CGOutTask) * P->outs.size()); q += D.outs;
-    memcpy(q, P->pqlist.data(), sizeof(int) * P->pqlist.size());
+    memcpy(q, P->pqlist.data(), sizeof(int) * P->pqlist.size()); q += D.pq;
+    memcpy(q, P->gclass.data(), sizeof(CGGradClass) * P->gclass.size()); q += D.gcl;
+    memcpy(q, P->gchunk.data(), sizeof(CGGradChunk) * P->gchunk.size()); q += D.gch;
+    memcpy(q, P->gent.data(), sizeof(CGGradEnt) * P->gent.size());
     /* pageable source: returns once the data is staged, so img may be released afterwards */
     CUDA_OK(cudaMemcpyAsync(region, img.data(), D.upload, cudaMemcpyHostToDevice, stream));
     return 0;

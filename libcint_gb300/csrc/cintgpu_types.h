@@ -45,7 +45,17 @@ typedef struct {
     int64_t cart_off;    /* accumulator slot in gctr */
     int out;             /* CGOutTask index (for the non-empty flag) */
     int sym;             /* unique-quartet flags: bit0 I != J, bit1 K != L, bit2 IJ != KL */
+    int cls;             /* adjoint only: index of the class's iteration tables (CGGradClass) */
+    int pad;
 } CGTask;
+
+/* Adjoint iteration tables, one set per angular-momentum class, built on the host.
+ * For axis a and a-axis power tuple u, the components sharing u are the entries
+ * ent[chunk.ent .. chunk.ent + chunk.len): offsets of the partner axes' g values and the
+ * component index into the cotangent W.  Chunks hold <= 16 entries, sorted longest first. */
+typedef struct { int chunk_off, nchunk, pad0, pad1; } CGGradClass;
+typedef struct { int axis_u; int ent; int len; int pad; } CGGradChunk;  /* axis | u << 2 */
+typedef struct { int ob_oc; int c; } CGGradEnt;                          /* ob | oc << 16 */
 
 typedef struct {
     int64_t cart_off;    /* first accumulator slot; nparts slots follow, each ncomp*nf long */

@@ -64,7 +64,7 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     int termw = (mode == CG_MODE_GRAD || mode == CG_MODE_GRADA) ? CG_TERMW_GRAD : CG_TERMW;
     int fixed = termw * 32;
     if (mode == CG_MODE_GRAD || mode == CG_MODE_GRADA)
-        fixed += 2 * 225 + 4 * CG_GRAD_MAXPRIM + 512;  /* density blocks, exponent sums, chunk table */
+        fixed += 2 * 225 + 4 * CG_GRAD_MAXPRIM + (L->nf <= CG_W_SMEM ? L->nf : 0);  /* D blocks, exponent sums, W */
     int avail = ws_doubles - fixed;
     /* T terms need T*3*ng*G doubles of g arrays and min(32, 3T) lane scratch areas */
     int T = 0;

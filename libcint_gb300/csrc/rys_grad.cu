@@ -15,39 +15,13 @@
  *
  * so each Cartesian component costs 3 FP64 operations per axis and root, independent of how many
  * derivatives are taken.  The fourth centre follows from translational invariance.
- * Work items are (term, axis, a-axis tuple, chunk of at most K partner tuples); every quantity
- * downstream of H is linear in H, so chunks contribute independently and the lanes stay balanced.
+ * Work items are (term, chunk): a chunk is <= 16 components sharing one a-axis tuple, listed in
+ * host-built per-class tables (CGGradChunk/CGGradEnt: g offsets of the partner axes and the
+ * component index) sorted longest first, so a round of lanes runs chunks of similar length.  Every
+ * quantity downstream of H is linear in H, so chunks of one tuple contribute independently.
+ * W (the cotangent per component) is formed once per task, in shared memory up to (dd|dd).
  */
 #include "rys_device.cuh"
-
-#define GRAD_CHUNK_TABLE 1024
-
-/* chunk size K for a class: at most GRAD_CHUNK_TABLE (tuple, chunk) entries */
-__host__ __device__ inline int grad_chunk(int li, int lj, int lk, int ll, int *nchunks)
-{
-    int l[4] = {li, lj, lk, ll};
-    for (int K = 16;; K *= 2) {
-        int tot = 0;
-        for (int p0 = 0; p0 <= l[0]; p0++)
-            for (int p1 = 0; p1 <= l[1]; p1++)
-                for (int p2 = 0; p2 <= l[2]; p2++)
-                    for (int p3 = 0; p3 <= l[3]; p3++) {
-                        int nv = (l[0] - p0 + 1) * (l[1] - p1 + 1) * (l[2] - p2 + 1) * (l[3] - p3 + 1);
-                        tot += (nv + K - 1) / K;
-                    }
-        if (tot <= GRAD_CHUNK_TABLE || K >= 4096) {
-            if (nchunks) *nchunks = tot;
-            return K;
-        }
-    }
-}
-
-__device__ __forceinline__ int cart_idx(int l, int lx, int ly)
-{
-    /* CINTcart_comp order: rows of decreasing lx, inside a row decreasing ly */
-    int r = l - lx;
-    return r * (r + 1) / 2 + (r - ly);
-}
 
 template <int MODE>
 __global__ void __launch_bounds__(128)
@@ -61,8 +35,8 @@ rys_grad_kernel(CGGradLaunch P)
     double *Dij = term + CG_TERMW_GRAD * 32;            /* 225 */
     double *Dkl = Dij + 225;                            /* 225 */
     double *aacc = Dkl + 225;                           /* 4 * CG_GRAD_MAXPRIM */
-    int *ctab = reinterpret_cast<int *>(aacc + 4 * CG_GRAD_MAXPRIM);   /* GRAD_CHUNK_TABLE ints */
-    double *greg = aacc + 4 * CG_GRAD_MAXPRIM + GRAD_CHUNK_TABLE / 2;
+    double *wsm = aacc + 4 * CG_GRAD_MAXPRIM;           /* cotangent W (nf <= CG_W_SMEM) */
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 
     for (;;) {
         int tid = 0;
@@ -100,32 +74,18 @@ rys_grad_kernel(CGGradLaunch P)
         }
         if (MODE == CG_MODE_GRADA)
             for (int e = lane; e < 4 * CG_GRAD_MAXPRIM; e += 32) aacc[e] = 0.0;
-        /* (tuple, chunk) table: tuples u = (p0,p1,p2,p3), p0 fastest */
-        int nchunk = 0;
-        const int K = grad_chunk(li, lj, lk, ll, &nchunk);
-        const int nT = (li + 1) * (lj + 1) * (lk + 1) * (ll + 1);
-        {
-            int base = 0;
-            for (int u0 = 0; u0 < nT; u0 += 32) {
-                int u = u0 + lane, cnt = 0, p[4];
-                if (u < nT) {
-                    int r = u;
-                    p[0] = r % (li + 1); r /= (li + 1);
-                    p[1] = r % (lj + 1); r /= (lj + 1);
-                    p[2] = r % (lk + 1); p[3] = r / (lk + 1);
-                    int nv = (li - p[0] + 1) * (lj - p[1] + 1) * (lk - p[2] + 1) * (ll - p[3] + 1);
-                    cnt = (nv + K - 1) / K;
-                }
-                int incl = cnt;
-                for (int o = 1; o < 32; o <<= 1) {
-                    int v = __shfl_up_sync(FULL, incl, o);
-                    if (lane >= o) incl += v;
-                }
-                int start = base + incl - cnt;
-                for (int q = 0; q < cnt; q++) ctab[start + q] = u | (q << 16);
-                base += __shfl_sync(FULL, incl, 31);
-            }
+        __syncwarp();
+        /* cotangent of every Cartesian component, c = ((i nfj + j) nfk + k) nfl + l */
+        double *W = L.nf <= CG_W_SMEM ? wsm : P.wglobal + (size_t)gw * P.wstride;
+        for (int c = lane; c < L.nf; c += 32) {
+            int l = c % nfl, r = c / nfl;
+            int k = r % nfk; r /= nfk;
+            W[c] = Dij[r] * Dkl[k * nfl + l];
         }
+        const CGGradClass cl = P.gclass[tk.cls];
+        const CGGradChunk *__restrict__ chunks = P.gchunk + cl.chunk_off;
+        const CGGradEnt *__restrict__ ents = P.gent;
+        double *greg = L.nf <= CG_W_SMEM ? wsm + L.nf : wsm;
         __syncwarp();
         double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
         const int sI = L.dJ * L.dK * L.dL, sJ = L.dK * L.dL, sK = L.dL;
@@ -160,44 +120,29 @@ rys_grad_kernel(CGGradLaunch P)
                        pkl.AB[ax], greg + T * 3 * G + lane * L.scr, greg + (size_t)(t * 3 + ax) * G);
             }
             __syncwarp();
-            const int items = Tb * 3 * nchunk;
+            /* items: (term, chunk); chunks are longest first so a round of lanes runs chunks of
+             * similar length */
+            const int items = Tb * cl.nchunk;
             for (int it = lane; it < items; it += 32) {
-                int t = it / (3 * nchunk);
-                int rem = it - t * 3 * nchunk;
-                int a = rem / nchunk;
-                int e = ctab[rem - a * nchunk];
-                int u = e & 0xffff, q = e >> 16;
+                int t = it / cl.nchunk;
+                const CGGradChunk ch = chunks[it - t * cl.nchunk];
+                const int a = ch.axis_u & 3, u = ch.axis_u >> 2;
+                const int b = a == 2 ? 0 : a + 1, c = 3 - a - b;
+                const double *ga = greg + (size_t)(t * 3 + a) * G;
+                const double *gb = greg + (size_t)(t * 3 + b) * G;
+                const double *gc = greg + (size_t)(t * 3 + c) * G;
+                double H = 0.0;
+                for (int e = 0; e < ch.len; e++) {
+                    const int2 en2 = __ldg(reinterpret_cast<const int2 *>(ents) + ch.ent + e);
+                    const CGGradEnt en = {en2.x, en2.y};
+                    H = fma(W[en.c] * gb[en.ob_oc & 0xffff], gc[en.ob_oc >> 16], H);
+                }
                 int p0, p1, p2, p3;
                 {
                     int r = u;
                     p0 = r % (li + 1); r /= (li + 1);
                     p1 = r % (lj + 1); r /= (lj + 1);
                     p2 = r % (lk + 1); p3 = r / (lk + 1);
-                }
-                const int b = a == 2 ? 0 : a + 1, c = 3 - a - b;
-                const double *ga = greg + (size_t)(t * 3 + a) * G;
-                const double *gb = greg + (size_t)(t * 3 + b) * G;
-                const double *gc = greg + (size_t)(t * 3 + c) * G;
-                const int r0 = li - p0 + 1, r1 = lj - p1 + 1, r2 = lk - p2 + 1, r3 = ll - p3 + 1;
-                const int nv = r0 * r1 * r2 * r3;
-                const int v1 = min(nv, (q + 1) * K);
-                double H = 0.0;
-                for (int v = q * K; v < v1; v++) {
-                    int r = v;
-                    int b0 = r % r0; r /= r0;
-                    int b1 = r % r1; r /= r1;
-                    int b2 = r % r2; int b3 = r / r2;
-                    int c0 = li - p0 - b0, c1 = lj - p1 - b1, c2 = lk - p2 - b2, c3 = ll - p3 - b3;
-                    int ob = ((b0 * L.dJ + b1) * L.dK + b2) * L.dL + b3;
-                    int oc = ((c0 * L.dJ + c1) * L.dK + c2) * L.dL + c3;
-                    /* x and y powers per shell for the component index */
-                    int xI = a == 0 ? p0 : (b == 0 ? b0 : c0), yI = a == 1 ? p0 : (b == 1 ? b0 : c0);
-                    int xJ = a == 0 ? p1 : (b == 0 ? b1 : c1), yJ = a == 1 ? p1 : (b == 1 ? b1 : c1);
-                    int xK = a == 0 ? p2 : (b == 0 ? b2 : c2), yK = a == 1 ? p2 : (b == 1 ? b2 : c2);
-                    int xL = a == 0 ? p3 : (b == 0 ? b3 : c3), yL = a == 1 ? p3 : (b == 1 ? b3 : c3);
-                    double W = Dij[cart_idx(li, xI, yI) * nfj + cart_idx(lj, xJ, yJ)]
-                             * Dkl[cart_idx(lk, xK, yK) * nfl + cart_idx(ll, xL, yL)];
-                    H = fma(W * gb[ob], gc[oc], H);
                 }
                 const double *rec = term + t * CG_TERMW_GRAD;
                 const int ou = ((p0 * L.dJ + p1) * L.dK + p2) * L.dL + p3;
@@ -243,8 +188,8 @@ rys_grad_kernel(CGGradLaunch P)
                 int s = e / CG_GRAD_MAXPRIM, p = e - s * CG_GRAD_MAXPRIM;
                 if (p < np[s] && aacc[e] != 0.0) atomicAdd(P.galpha + gp[s] + p, aacc[e]);
             }
-            __syncwarp();
         }
+        __syncwarp();
     }
 }
 

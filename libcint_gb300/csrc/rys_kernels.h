@@ -59,7 +59,14 @@ typedef struct {
     int nao;
     double *grad;             /* natm x 3 */
     double *galpha;           /* per global primitive (GRADA only) */
+    const CGGradClass *gclass;
+    const CGGradChunk *gchunk;
+    const CGGradEnt *gent;
+    double *wglobal;          /* per-warp cotangent slots for classes with nf > CG_W_SMEM */
+    int64_t wstride;
 } CGGradLaunch;
+
+#define CG_W_SMEM 1296        /* cotangent blocks up to (dd|dd) stay in shared memory */
 
 #ifdef __cplusplus
 extern "C" {
