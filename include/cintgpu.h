@@ -161,6 +161,9 @@ int cintgpu_plan_execute(CINTGPUPlan *plan, double *out_dev, void *stream);
 int64_t cintgpu_plan_upload_bytes(const CINTGPUPlan *plan);
 /* number of kernel launches one execution enqueues */
 int cintgpu_plan_launches(const CINTGPUPlan *plan);
+/* device-side error flags of the last execution (synchronises): 0 = fine, bit0 = a task's class
+ * did not fit the kernel's shared-memory layout (its contribution is missing) */
+int cintgpu_plan_status(const CINTGPUPlan *plan);
 /* Cartesian AO count of the plan's basis (J/adjoint kinds) */
 int cintgpu_plan_nao_cart(const CINTGPUPlan *plan);
 /* J kinds: vj_dev (nao_cart^2, row major) += the contraction of the listed quartets with

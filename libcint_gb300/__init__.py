@@ -76,6 +76,8 @@ def lib():
     L.cintgpu_rys_roots_dev.argtypes = [i32, vp, i32, vp, vp, vp]
     L.cintgpu_rys_roots_dev.restype = i32
     L.cintgpu_rys_nmax.restype = i32
+    L.cintgpu_plan_status.argtypes = [vp]
+    L.cintgpu_plan_status.restype = i32
     L.cintgpu_plan_nao_cart.argtypes = [vp]
     L.cintgpu_plan_nao_cart.restype = i32
     L.cintgpu_plan_execute_j.argtypes = [vp, vp, vp, vp]

@@ -424,7 +424,7 @@ static int build_grad_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
     const int l[4] = {li, lj, lk, ll};
     const int nfc[4] = {ncart_l(li), ncart_l(lj), ncart_l(lk), ncart_l(ll)};
     auto cidx = [](int lq, int lx, int ly) { int r = lq - lx; return r * (r + 1) / 2 + (r - ly); };
-    struct Ch { int axis_u, ent, len; };
+    struct Ch { int axis_u, ent, len, ou, p0, p1, p2; };
     std::vector<Ch> list;
     for (int a = 0; a < 3; a++) {
         const int b = a == 2 ? 0 : a + 1, c = 3 - a - b;
@@ -456,8 +456,9 @@ static int build_grad_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
                 P->gent.push_back(e);
             }
             int total = (int)P->gent.size() - start;
+            int ou = ((p0 * L.dJ + p1) * L.dK + p2) * L.dL + p3;
             for (int o = 0; o < total; o += 16)
-                list.push_back({a | (u << 2), start + o, std::min(16, total - o)});
+                list.push_back({a | (u << 2), start + o, std::min(16, total - o), ou, p0, p1, p2});
         }
     }
     std::stable_sort(list.begin(), list.end(), [](const Ch &x, const Ch &y) { return x.len > y.len; });
@@ -465,7 +466,15 @@ static int build_grad_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
     gc.chunk_off = (int)P->gchunk.size();
     gc.nchunk = (int)list.size();
     gc.pad0 = gc.pad1 = 0;
-    for (const Ch &x : list) P->gchunk.push_back({x.axis_u, x.ent, x.len, 0});
+    for (const Ch &x : list) {
+        CGGradChunk g;
+        g.axis_u = x.axis_u; g.ent = x.ent; g.len = x.len; g.ou = x.ou; g.pad = 0;
+        g.om[0] = x.p0 ? x.ou - L.dJ * L.dK * L.dL : x.ou;
+        g.om[1] = x.p1 ? x.ou - L.dK * L.dL : x.ou;
+        g.om[2] = x.p2 ? x.ou - L.dL : x.ou;
+        g.p[0] = x.p0; g.p[1] = x.p1; g.p[2] = x.p2;
+        P->gchunk.push_back(g);
+    }
     P->gclass.push_back(gc);
     return (int)P->gclass.size() - 1;
 }
@@ -788,9 +797,6 @@ static int upload_plan(CINTGPUPlan *P, char *arena, size_t arena_size, cudaStrea
     P->d_tasks = (CGTask *)p; p += D.tasks;
     P->d_outs = (CGOutTask *)p; p += D.outs;
     P->d_pqlist = (int *)p; p += D.pq;
-    P->d_gclass = (CGGradClass *)p; p += D.gcl;
-    P->d_gchunk = (CGGradChunk *)p; p += D.gch;
-    P->d_gent = (CGGradEnt *)p; p += D.gen;
     P->d_gclass = (CGGradClass *)p; p += D.gcl;
     P->d_gchunk = (CGGradChunk *)p; p += D.gch;
     P->d_gent = (CGGradEnt *)p; p += D.gen;
@@ -1142,6 +1148,29 @@ int cintgpu_plan_execute(CINTGPUPlan *plan, double *out_dev, void *stream)
 
 int cintgpu_plan_nao_cart(const CINTGPUPlan *plan) { return plan->nao_cart; }
 
+int cintgpu_plan_status(const CINTGPUPlan *plan)
+{
+    int st = 0;
+    CUDA_OK(cudaDeviceSynchronize());
+    CUDA_OK(cudaMemcpy(&st, plan->d_counters + 2, sizeof(int), cudaMemcpyDeviceToHost));
+    return st;
+}
+
+int cintgpu_plan_debug(const CINTGPUPlan *plan, int64_t *info)
+{
+    info[0] = (int64_t)plan->tasks.size();
+    info[1] = plan->groups[0].ntasks;
+    info[2] = plan->groups[1].ntasks;
+    info[3] = (int64_t)plan->gclass.size();
+    info[4] = (int64_t)plan->gchunk.size();
+    info[5] = (int64_t)plan->gent.size();
+    info[6] = plan->groups[0].ws;
+    info[7] = plan->groups[0].blocks_per_sm;
+    info[8] = plan->groups[1].blocks_per_sm;
+    info[9] = plan->mode;
+    return 0;
+}
+
 int cintgpu_plan_execute_j(CINTGPUPlan *plan, const double *dm_dev, double *vj_dev, void *stream)
 {
     if (!plan->jmode) { set_error("plan is not a J_BUILD plan"); return CINTGPU_ERR_ARG; }
@@ -1335,9 +1364,6 @@ int cg_plan_place(CINTGPUPlan *P, char *region, size_t region_bytes, cudaStream_
     P->d_tasks = (CGTask *)p; p += D.tasks;
     P->d_outs = (CGOutTask *)p; p += D.outs;
     P->d_pqlist = (int *)p; p += D.pq;
-    P->d_gclass = (CGGradClass *)p; p += D.gcl;
-    P->d_gchunk = (CGGradChunk *)p; p += D.gch;
-    P->d_gent = (CGGradEnt *)p; p += D.gen;
     P->d_gclass = (CGGradClass *)p; p += D.gcl;
     P->d_gchunk = (CGGradChunk *)p; p += D.gch;
     P->d_gent = (CGGradEnt *)p; p += D.gen;

@@ -54,7 +54,14 @@ typedef struct {
  * ent[chunk.ent .. chunk.ent + chunk.len): offsets of the partner axes' g values and the
  * component index into the cotangent W.  Chunks hold <= 16 entries, sorted longest first. */
 typedef struct { int chunk_off, nchunk, pad0, pad1; } CGGradClass;
-typedef struct { int axis_u; int ent; int len; int pad; } CGGradChunk;  /* axis | u << 2 */
+typedef struct {
+    int axis_u;          /* axis | u << 2 */
+    int ent, len;        /* entries [ent, ent + len) */
+    int ou;              /* offset of tuple u in the axis's g array */
+    int om[3];           /* offset of u lowered on shell I, J, K (= ou where that power is 0) */
+    int pad;
+    double p[3];         /* powers of u on shells I, J, K (as doubles: no conversion in the kernel) */
+} CGGradChunk;
 typedef struct { int ob_oc; int c; } CGGradEnt;                          /* ob | oc << 16 */
 
 typedef struct {

@@ -52,7 +52,13 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     cg_mode_incs(mode, inc);
     L->lic = li + inc[0];
     const int ljc = lj + inc[1], lkc = lk + inc[2], llc = ll + inc[3];
-    L->nroots = (L->lic + ljc + lkc + llc) / 2 + 1;
+    /* every product the adjoint forms raises ONE center (by 1 for a coordinate, by 2 for an
+     * exponent), so the quadrature needs only that much above li+lj+lk+ll even though the g
+     * arrays reach the increment on every center */
+    const int lsum = li + lj + lk + ll;
+    if (mode == CG_MODE_GRAD) L->nroots = (lsum + 1) / 2 + 1;
+    else if (mode == CG_MODE_GRADA) L->nroots = (lsum + 2) / 2 + 1;
+    else L->nroots = (L->lic + ljc + lkc + llc) / 2 + 1;
     L->nmax = L->lic + ljc;
     L->mmax = lkc + llc;
     L->dI = L->lic + 1; L->dJ = ljc + 1; L->dK = lkc + 1; L->dL = llc + 1;
@@ -61,16 +67,37 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     L->nf = ncart(li) * ncart(lj) * ncart(lk) * ncart(ll);
     L->ncomp = (mode == CG_MODE_IP1) ? 3 : 1;
     L->scr = (L->nmax + 1) * (L->mmax + 1) + (L->nmax + 1) + (L->mmax + 1);
-    int termw = (mode == CG_MODE_GRAD || mode == CG_MODE_GRADA) ? CG_TERMW_GRAD : CG_TERMW;
-    int fixed = termw * 32;
-    if (mode == CG_MODE_GRAD || mode == CG_MODE_GRADA)
-        fixed += 2 * 225 + 4 * CG_GRAD_MAXPRIM + (L->nf <= CG_W_SMEM ? L->nf : 0);  /* D blocks, exponent sums, W */
-    int avail = ws_doubles - fixed;
-    /* T terms need T*3*ng*G doubles of g arrays and min(32, 3T) lane scratch areas */
+    const bool grad = mode == CG_MODE_GRAD || mode == CG_MODE_GRADA;
     int T = 0;
-    for (int t = 32; t >= 1; t--) {
-        int items = 3 * t < 32 ? 3 * t : 32;
-        if (t * 3 * L->ng * L->G + items * L->scr <= avail) { T = t; break; }
+    if (!grad) {
+        int avail = ws_doubles - CG_TERMW * 32;     /* term records */
+        /* T terms need T*3*ng*G doubles of g arrays and min(32, 3T) lane scratch areas */
+        for (int t = 32; t >= 1; t--) {
+            int items = 3 * t < 32 ? 3 * t : 32;
+            if (t * 3 * L->ng * L->G + items * L->scr <= avail) { T = t; break; }
+        }
+        L->off_dij = L->off_dkl = L->off_aacc = L->off_w = L->off_g = L->off_scr = 0;
+        L->gstride = 3 * L->ng * L->G;
+    } else {
+        /* adjoint: term records scale with T; density blocks, exponent sums (GRADA) and the
+         * cotangent (nf <= CG_W_SMEM) are per task */
+        int d1 = (ncart(li) * ncart(lj) + 1) & ~1, d2 = (ncart(lk) * ncart(ll) + 1) & ~1;
+        int aa = mode == CG_MODE_GRADA ? 4 * CG_GRAD_MAXPRIM : 0;
+        int wsm = L->nf <= CG_W_SMEM ? ((L->nf + 1) & ~1) : 0;
+        int fixed = d1 + d2 + aa + wsm;
+        /* odd per-term stride of the g arrays: lanes reading the same offset of different terms
+         * hit distinct shared-memory banks */
+        L->gstride = 3 * L->G + ((3 * L->G) % 2 == 0 ? 1 : 0);
+        for (int t = 32; t >= 1; t--) {
+            int items = 3 * t < 32 ? 3 * t : 32;
+            if (t * (CG_TERMW_GRAD + L->gstride) + items * L->scr + fixed <= ws_doubles) { T = t; break; }
+        }
+        L->off_dij = T * CG_TERMW_GRAD;
+        L->off_dkl = L->off_dij + d1;
+        L->off_aacc = L->off_dkl + d2;
+        L->off_w = L->off_aacc + aa;
+        L->off_g = L->off_w + wsm;
+        L->off_scr = L->off_g + T * L->gstride;
     }
     L->T = T;
 }

@@ -31,11 +31,7 @@ rys_grad_kernel(CGGradLaunch P)
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     double *ws = smem + (size_t)warp * P.ws_doubles;
-    double *term = ws;                                  /* CG_TERMW_GRAD * 32 */
-    double *Dij = term + CG_TERMW_GRAD * 32;            /* 225 */
-    double *Dkl = Dij + 225;                            /* 225 */
-    double *aacc = Dkl + 225;                           /* 4 * CG_GRAD_MAXPRIM */
-    double *wsm = aacc + 4 * CG_GRAD_MAXPRIM;           /* cotangent W (nf <= CG_W_SMEM) */
+    double *term = ws;                                  /* T * CG_TERMW_GRAD */
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 
     for (;;) {
@@ -54,6 +50,7 @@ rys_grad_kernel(CGGradLaunch P)
             continue;
         }
         const int T = L.T, n = L.nroots, G = L.G;
+        double *Dij = ws + L.off_dij, *Dkl = ws + L.off_dkl, *aacc = ws + L.off_aacc;
         const int nfi = ncart(li), nfj = ncart(lj), nfk = ncart(lk), nfl = ncart(ll);
         const int nao = P.nao;
         const CGPrimPair *__restrict__ ppij = P.prims + pij.prim_off;
@@ -76,7 +73,7 @@ rys_grad_kernel(CGGradLaunch P)
             for (int e = lane; e < 4 * CG_GRAD_MAXPRIM; e += 32) aacc[e] = 0.0;
         __syncwarp();
         /* cotangent of every Cartesian component, c = ((i nfj + j) nfk + k) nfl + l */
-        double *W = L.nf <= CG_W_SMEM ? wsm : P.wglobal + (size_t)gw * P.wstride;
+        double *W = L.nf <= CG_W_SMEM ? ws + L.off_w : P.wglobal + (size_t)gw * P.wstride;
         for (int c = lane; c < L.nf; c += 32) {
             int l = c % nfl, r = c / nfl;
             int k = r % nfk; r /= nfk;
@@ -85,7 +82,7 @@ rys_grad_kernel(CGGradLaunch P)
         const CGGradClass cl = P.gclass[tk.cls];
         const CGGradChunk *__restrict__ chunks = P.gchunk + cl.chunk_off;
         const CGGradEnt *__restrict__ ents = P.gent;
-        double *greg = L.nf <= CG_W_SMEM ? wsm + L.nf : wsm;
+        double *greg = ws + L.off_g;
         __syncwarp();
         double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
         const int sI = L.dJ * L.dK * L.dL, sJ = L.dK * L.dL, sK = L.dL;
@@ -106,10 +103,13 @@ rys_grad_kernel(CGGradLaunch P)
                 rec[11] = 2.0 * (A.a - A.aA);
                 rec[12] = 2.0 * B.aA;
                 rec[13] = 2.0 * (B.a - B.aA);
-                rec[14] = (double)(ij % pij.npa);
-                rec[15] = (double)(ij / pij.npa);
-                rec[16] = (double)(kl % pkl.npa);
-                rec[17] = (double)(kl / pkl.npa);
+                if (MODE == CG_MODE_GRADA) {
+                    int *ri = reinterpret_cast<int *>(rec + 14);
+                    ri[0] = ij % pij.npa;
+                    ri[1] = ij / pij.npa;
+                    ri[2] = kl % pkl.npa;
+                    ri[3] = kl / pkl.npa;
+                }
             }
             __syncwarp();
             for (int item = lane; item < 3 * Tb; item += 32) {
@@ -117,49 +117,81 @@ rys_grad_kernel(CGGradLaunch P)
                 const double *rec = term + t * CG_TERMW_GRAD;
                 double g00 = (ax == 2) ? rec[9] : 1.0;
                 g_axis(L, rec[0], rec[1], rec[2], rec[3 + ax], rec[6 + ax], g00, pij.AB[ax],
-                       pkl.AB[ax], greg + T * 3 * G + lane * L.scr, greg + (size_t)(t * 3 + ax) * G);
+                       pkl.AB[ax], ws + L.off_scr + lane * L.scr, greg + (size_t)t * L.gstride + ax * G);
             }
             __syncwarp();
             /* items: (term, chunk); chunks are longest first so a round of lanes runs chunks of
              * similar length */
             const int items = Tb * cl.nchunk;
-            for (int it = lane; it < items; it += 32) {
-                int t = it / cl.nchunk;
-                const CGGradChunk ch = chunks[it - t * cl.nchunk];
-                const int a = ch.axis_u & 3, u = ch.axis_u >> 2;
+            for (int base = 0; base < items; base += 32) {
+                const int it = base + lane;
+                const bool act = it < items;
+                /* coordinates only: chunk-major order (a round of lanes shares one chunk and its
+                 * length across terms); exponents: term-major, so a round usually holds one term
+                 * and its four primitive sums reduce across the warp */
+                int t, k;
+                if (MODE == CG_MODE_GRAD) { k = it / Tb; t = it - k * Tb; }
+                else { t = it / cl.nchunk; k = it - t * cl.nchunk; }
+                if (!act) { t = (MODE == CG_MODE_GRAD) ? 0 : Tb - 1; k = 0; }
+                double al0 = 0.0, al1 = 0.0, al2 = 0.0, al3 = 0.0;
+                if (act) {
+                const CGGradChunk &ch = chunks[k];
+                const int a = ch.axis_u & 3;
                 const int b = a == 2 ? 0 : a + 1, c = 3 - a - b;
-                const double *ga = greg + (size_t)(t * 3 + a) * G;
-                const double *gb = greg + (size_t)(t * 3 + b) * G;
-                const double *gc = greg + (size_t)(t * 3 + c) * G;
+                const double *gt = greg + (size_t)t * L.gstride;
+                const double *ga = gt + a * G;
+                const double *gb = gt + b * G;
+                const double *gc = gt + c * G;
                 double H = 0.0;
-                for (int e = 0; e < ch.len; e++) {
-                    const int2 en2 = __ldg(reinterpret_cast<const int2 *>(ents) + ch.ent + e);
-                    const CGGradEnt en = {en2.x, en2.y};
-                    H = fma(W[en.c] * gb[en.ob_oc & 0xffff], gc[en.ob_oc >> 16], H);
-                }
-                int p0, p1, p2, p3;
-                {
-                    int r = u;
-                    p0 = r % (li + 1); r /= (li + 1);
-                    p1 = r % (lj + 1); r /= (lj + 1);
-                    p2 = r % (lk + 1); p3 = r / (lk + 1);
+                const int2 *ep = reinterpret_cast<const int2 *>(ents) + ch.ent;
+                const int len = ch.len;
+                for (int e = 0; e < len; e++) {
+                    const int2 en = __ldg(ep + e);
+                    H = fma(W[en.y] * gb[en.x & 0xffff], gc[en.x >> 16], H);
                 }
                 const double *rec = term + t * CG_TERMW_GRAD;
-                const int ou = ((p0 * L.dJ + p1) * L.dK + p2) * L.dL + p3;
-                double dA = rec[10] * ga[ou + sI];
-                if (p0) dA = fma(-(double)p0, ga[ou - sI], dA);
-                double dB = rec[11] * ga[ou + sJ];
-                if (p1) dB = fma(-(double)p1, ga[ou - sJ], dB);
-                double dC = rec[12] * ga[ou + sK];
-                if (p2) dC = fma(-(double)p2, ga[ou - sK], dC);
+                const int ou = ch.ou;
+                double dA = fma(-ch.p[0], ga[ch.om[0]], rec[10] * ga[ou + sI]);
+                double dB = fma(-ch.p[1], ga[ch.om[1]], rec[11] * ga[ou + sJ]);
+                double dC = fma(-ch.p[2], ga[ch.om[2]], rec[12] * ga[ou + sK]);
                 gA[a] = fma(H, dA, gA[a]);
                 gB[a] = fma(H, dB, gB[a]);
                 gC[a] = fma(H, dC, gC[a]);
                 if (MODE == CG_MODE_GRADA) {
-                    atomicAdd(aacc + 0 * CG_GRAD_MAXPRIM + (int)rec[14], -H * ga[ou + 2 * sI]);
-                    atomicAdd(aacc + 1 * CG_GRAD_MAXPRIM + (int)rec[15], -H * ga[ou + 2 * sJ]);
-                    atomicAdd(aacc + 2 * CG_GRAD_MAXPRIM + (int)rec[16], -H * ga[ou + 2 * sK]);
-                    atomicAdd(aacc + 3 * CG_GRAD_MAXPRIM + (int)rec[17], -H * ga[ou + 2]);
+                    al0 = -H * ga[ou + 2 * sI];
+                    al1 = -H * ga[ou + 2 * sJ];
+                    al2 = -H * ga[ou + 2 * sK];
+                    al3 = -H * ga[ou + 2];
+                }
+                }
+                if (MODE == CG_MODE_GRADA) {
+                    /* exponent derivatives belong to the term's four primitives: one warp sum when
+                     * the round holds a single term, shared-memory atomics otherwise */
+                    const int t_first = __shfl_sync(FULL, t, 0);
+                    if (__all_sync(FULL, t == t_first)) {
+                        for (int o = 16; o > 0; o >>= 1) {
+                            al0 += __shfl_xor_sync(FULL, al0, o);
+                            al1 += __shfl_xor_sync(FULL, al1, o);
+                            al2 += __shfl_xor_sync(FULL, al2, o);
+                            al3 += __shfl_xor_sync(FULL, al3, o);
+                        }
+                        if (lane == 0) {
+                            const double *rec = term + t_first * CG_TERMW_GRAD;
+                            const int *ri = reinterpret_cast<const int *>(rec + 14);
+                            aacc[0 * CG_GRAD_MAXPRIM + ri[0]] += al0;
+                            aacc[1 * CG_GRAD_MAXPRIM + ri[1]] += al1;
+                            aacc[2 * CG_GRAD_MAXPRIM + ri[2]] += al2;
+                            aacc[3 * CG_GRAD_MAXPRIM + ri[3]] += al3;
+                        }
+                        __syncwarp();
+                    } else if (act) {
+                        const double *rec = term + t * CG_TERMW_GRAD;
+                        const int *ri = reinterpret_cast<const int *>(rec + 14);
+                        atomicAdd(aacc + 0 * CG_GRAD_MAXPRIM + ri[0], al0);
+                        atomicAdd(aacc + 1 * CG_GRAD_MAXPRIM + ri[1], al1);
+                        atomicAdd(aacc + 2 * CG_GRAD_MAXPRIM + ri[2], al2);
+                        atomicAdd(aacc + 3 * CG_GRAD_MAXPRIM + ri[3], al3);
+                    }
                 }
             }
             __syncwarp();

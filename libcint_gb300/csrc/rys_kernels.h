@@ -19,6 +19,10 @@
 typedef struct {
     int lic, nroots, nmax, mmax;
     int dI, dJ, dK, dL, G, ng, nf, ncomp, scr, T;
+    /* adjoint shared-memory map (doubles from the warp's base): density blocks, exponent sums,
+     * cotangent (when kept in shared memory), g arrays, lane scratch */
+    int off_dij, off_dkl, off_aacc, off_w, off_g, off_scr;
+    int gstride;              /* doubles between consecutive terms' g arrays */
 } CGLayout;
 
 typedef struct {
@@ -66,7 +70,7 @@ typedef struct {
     int64_t wstride;
 } CGGradLaunch;
 
-#define CG_W_SMEM 1296        /* cotangent blocks up to (dd|dd) stay in shared memory */
+#define CG_W_SMEM 256         /* cotangent blocks up to 256 components stay in shared memory */
 
 #ifdef __cplusplus
 extern "C" {
