@@ -226,13 +226,14 @@ def extra_int3c2e(cg, seed=0, npairs=40):
             'fp64_frac': p.flops / dt / 1e12 / FP64_PEAK_TFLOPS}
 
 
-def extra_adjoint(cg, seed=0):
-    """c3: 24 atoms, full unique quartet list; adjoint gradient vs int2e_ip1 formed and contracted
-    on the same GPU; agreement between the two."""
+def extra_adjoint(cg, seed=0, natm=24):
+    """c3: 24 atoms (fewer, in a box of the same density, for profiling), full unique quartet
+    list; adjoint gradient vs int2e_ip1 formed and contracted on the same GPU; agreement between
+    the two."""
     import torch
     from libcint_gb300 import molecules as M
     from libcint_gb300.coulomb import CoulombPlans, grad_via_ip1
-    mol = M.config3(seed=seed)
+    mol = M.config3(seed=seed, natm=natm, box=8.0 * (natm / 24.0) ** (1.0 / 3.0))
     nao = sum(mol.nsph(i) for i in range(mol.nbas))
     rng = np.random.RandomState(seed)
     d = rng.normal(0, 0.1, (nao, nao))
@@ -252,8 +253,8 @@ def extra_adjoint(cg, seed=0):
     diff = float((g_adj[0] - g_ip1[0]).abs().max() / g_ip1[0].abs().max())
     plans_a = CoulombPlans(mol, with_exponents=True)
     t_adj_a = _timed(lambda: plans_a.grad(dm))
-    return {'workload': 'c3: 24 atoms, 8 A, s,p,d x 3-5 prims, all %d unique quartets'
-                        % len(M.unique_quartets(mol.nbas)),
+    return {'workload': 'c3: %d atoms, %.1f A, s,p,d x 3-5 prims, all %d unique quartets'
+                        % (natm, 8.0 * (natm / 24.0) ** (1.0 / 3.0), len(M.unique_quartets(mol.nbas))),
             'forward_J_ms': 1e3 * t_fwd, 'adjoint_grad_ms': 1e3 * t_adj,
             'adjoint_grad_with_exponents_ms': 1e3 * t_adj_a, 'ip1_route_grad_ms': 1e3 * t_ip1,
             'adjoint_speedup_over_ip1': t_ip1 / t_adj, 'max_rel_diff_vs_ip1': diff}
@@ -278,6 +279,13 @@ def run_gpu(args, rank, world):
     dev = int(os.environ.get('LOCAL_RANK', '0'))
     torch.cuda.set_device(dev)
     cg.build_library()
+    if args.only != 'headline':
+        # one side workload alone (profiling); not the benchmark line
+        fn = {'adjoint': lambda: extra_adjoint(cg, natm=args.c3_atoms),
+              'int3c2e': lambda: extra_int3c2e(cg)}[args.only]
+        if rank == 0:
+            print(json.dumps({'extra': args.only, **fn()}), flush=True)
+        return
     mol = M.config1(seed=0)
     qs = load_quartets(args.quartets)
     nint = integrals_of(mol, qs)
@@ -382,6 +390,9 @@ def main():
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-extras', action='store_true', help='skip the drop-in, int3c2e and adjoint lines')
+    ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e'],
+                    help='run one side workload alone and print its line (profiling)')
+    ap.add_argument('--c3-atoms', type=int, default=24, help='atoms of the adjoint workload')
     args = ap.parse_args()
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))

@@ -243,6 +243,11 @@ struct CINTGPUPlan {
     std::vector<CGGradClass> gclass;   /* adjoint iteration tables per class */
     std::vector<CGGradChunk> gchunk;
     std::vector<CGGradEnt> gent;
+    std::vector<CGEriClass> eclass;    /* contraction-first tables per class (ERI mode) */
+    std::vector<CGEriGroup> egroup;
+    std::vector<int> eperm;
+    int hrr_max = 1;               /* doubles of one transfer buffer, largest class */
+    int nef_max = 1;               /* (e0|f0) accumulators, largest class */
     std::vector<int> out_item;     /* item index of each CGOutTask */
     TaskGroup groups[2];           /* [0] regular classes, [1] classes needing 48 KB per warp */
     int64_t gctr_size = 0;
@@ -258,6 +263,9 @@ struct CINTGPUPlan {
     CGGradClass *d_gclass = nullptr;
     CGGradChunk *d_gchunk = nullptr;
     CGGradEnt *d_gent = nullptr;
+    CGEriClass *d_eclass = nullptr;
+    CGEriGroup *d_egroup = nullptr;
+    int *d_eperm = nullptr;
     double *d_gctr = nullptr;
     int *d_counters = nullptr;     /* [0], [1]: task counters of the groups; [2]: status */
     int *d_nonempty = nullptr;
@@ -403,6 +411,15 @@ double flops_per_primq(int li, int lj, int lk, int ll, int mode)
     for (int j = 1; j < L.dJ; j++) hrr += (L.nmax - j + 1) * (L.mmax + 1);
     for (int l = 1; l < L.dL; l++) hrr += L.dI * L.dJ * (L.mmax - l + 1);
     double vrr = (double)(L.nmax + 1) * (L.mmax + 1);
+    if (mode == CG_MODE_ERI) {
+        /* contraction first: VRR, then per group one product and 2 flops per member; the
+         * transfer is per contracted quartet and not counted */
+        auto nc = [](int l) { return (l + 1) * (l + 2) / 2; };
+        auto range = [&](int l0, int l1) { int t = 0; for (int l = l0; l <= l0 + l1; l++) t += nc(l); return t; };
+        double ngroup = (double)nc(li + lj) * nc(lk + ll);
+        double nef = (double)range(li, lj) * range(lk, ll);
+        return n * (20 + 3 * 5 * vrr + ngroup + 2 * nef);
+    }
     double per_root = 20 + 3 * 5 * vrr + 3 * 2 * hrr;
     if (mode == CG_MODE_IP1) per_root += 3 * 3 * (double)L.G / L.dI * (L.dI - 1) + 9.0 * L.nf;
     else if (mode == CG_MODE_GRAD || mode == CG_MODE_GRADA) {
@@ -413,6 +430,83 @@ double flops_per_primq(int li, int lj, int lk, int ll, int mode)
 }
 
 }  // namespace
+
+/* Contraction-first tables of one int2e / int3c2e class in kernel order (li >= lj, lk >= ll;
+ * na = li + lj + 1 is the row length of the VRR arrays): the stage-3 groups, the permutations
+ * from the transfer's Cartesian order to the accumulator rows/columns, and the transfer's buffer
+ * size.  Layout described with CGEriClass. */
+static int build_eri_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
+{
+    struct Side {
+        std::vector<int> x, y, z0, nz, base, pidx;
+        int n = 0, lmax = 0;
+    };
+    auto side = [](int l0, int l1) {
+        Side S;
+        S.lmax = l0 + l1;
+        S.pidx.assign((S.lmax + 1) * (S.lmax + 1), -1);
+        for (int x = 0; x <= S.lmax; x++)
+            for (int y = 0; x + y <= S.lmax; y++) {
+                int z0 = std::max(0, l0 - x - y);
+                S.pidx[x * (S.lmax + 1) + y] = (int)S.x.size();
+                S.x.push_back(x); S.y.push_back(y); S.z0.push_back(z0);
+                S.nz.push_back(S.lmax - x - y - z0 + 1);
+                S.base.push_back(S.n);
+                S.n += S.lmax - x - y - z0 + 1;
+            }
+        return S;
+    };
+    const Side E = side(li, lj), F = side(lk, ll);
+    const int na = li + lj + 1;
+    CGEriClass c;
+    c.nE = E.n;
+    c.nF = F.n;
+    c.group_off = (int)P->egroup.size();
+    std::vector<CGEriGroup> g;
+    for (size_t p = 0; p < E.x.size(); p++)
+        for (size_t q = 0; q < F.x.size(); q++) {
+            CGEriGroup e;
+            e.oxy = (E.x[p] + na * F.x[q]) | ((E.y[p] + na * F.y[q]) << 16);
+            e.oz = E.z0[p] + na * F.z0[q];
+            e.acc = E.base[p] * F.n + F.base[q];
+            e.mn = E.nz[p] | (F.nz[q] << 8);
+            g.push_back(e);
+        }
+    std::stable_sort(g.begin(), g.end(), [](const CGEriGroup &a, const CGEriGroup &b) {
+        return (a.mn & 0xff) * (a.mn >> 8) > (b.mn & 0xff) * (b.mn >> 8);
+    });
+    P->egroup.insert(P->egroup.end(), g.begin(), g.end());
+    c.ngroup = (int)g.size();
+    c.split = 0;
+    if (c.ngroup <= 32) {
+        int sp = 1;
+        while (2 * sp * c.ngroup <= 32) sp *= 2;
+        c.split = sp;
+    }
+    c.perm_off = (int)P->eperm.size();
+    auto perm = [&](const Side &S, int l0) {
+        for (int l = l0; l <= S.lmax; l++)
+            for (int x = l; x >= 0; x--)
+                for (int y = l - x; y >= 0; y--) {
+                    int p = S.pidx[x * (S.lmax + 1) + y];
+                    P->eperm.push_back(S.base[p] + (l - x - y) - S.z0[p]);
+                }
+    };
+    perm(E, li);
+    perm(F, lk);
+    auto below = [](int l) { return l * (l + 1) * (l + 2) / 6; };
+    int need = std::max(c.nE * c.nF, ncart_l(li) * ncart_l(lj) * ncart_l(lk) * ncart_l(ll));
+    for (int b = 1; b <= lj; b++)
+        need = std::max(need, (below(li + lj - b + 1) - below(li)) * ncart_l(b) * c.nF);
+    for (int d = 1; d <= ll; d++)
+        need = std::max(need, ncart_l(li) * ncart_l(lj) * (below(lk + ll - d + 1) - below(lk)) * ncart_l(d));
+    c.hrr_need = need;
+    c.maxab = (lj + 1) | ((ll + 1) << 8);
+    P->hrr_max = std::max(P->hrr_max, need);
+    P->nef_max = std::max(P->nef_max, c.nE * c.nF);
+    P->eclass.push_back(c);
+    return (int)P->eclass.size() - 1;
+}
 
 /* Adjoint iteration tables of one class (kernel order li, lj, lk, ll): for every axis a and a-axis
  * power tuple u, the Cartesian components sharing u, as (partner g offsets, component index),
@@ -662,7 +756,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     }
     struct TaskCost { CGTask t; double cost; int group; };
     std::vector<TaskCost> tc;
-    std::unordered_map<int, int> grad_cls;
+    std::unordered_map<int, int> grad_cls, eri_cls;
     int64_t gpos = 0;
     for (const Work &w : work) {
         const Pending &pe = pend[w.pe];
@@ -686,11 +780,23 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         CGOutTask &o = P->outs[pe.out];
         o.cart_off = gpos;
         int cls = 0;
+        const int key = ((pe.l[0] * 16 + pe.l[1]) * 16 + pe.l[2]) * 16 + pe.l[3];
         if (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) {
-            int key = ((pe.l[0] * 16 + pe.l[1]) * 16 + pe.l[2]) * 16 + pe.l[3];
             auto it = grad_cls.find(key);
             cls = it != grad_cls.end() ? it->second
                                        : (grad_cls[key] = build_grad_class(P, pe.l[0], pe.l[1], pe.l[2], pe.l[3]));
+        } else if (P->mode == CG_MODE_ERI) {
+            auto it = eri_cls.find(key);
+            cls = it != eri_cls.end() ? it->second
+                                      : (eri_cls[key] = build_eri_class(P, pe.l[0], pe.l[1], pe.l[2], pe.l[3]));
+            const CGEriClass &ec = P->eclass[cls];
+            slot = (int64_t)ec.nE * ec.nF;
+            o.flags |= 2;
+            o.ecls = cls;
+            for (int c = 0; c < 3; c++) {
+                o.AB[c] = P->pairs[pe.pij].AB[c];
+                o.CD[c] = P->pairs[pe.pkl].AB[c];
+            }
         }
         for (int64_t a0 = 0; a0 < w.n; a0 += slice) {
             TaskCost x;
@@ -730,7 +836,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
 }
 
 struct DevLayout {
-    size_t pairs, prims, tasks, outs, pq, gcl, gch, gen, gctr, cnt, ne, scr, wscr;
+    size_t pairs, prims, tasks, outs, pq, gcl, gch, gen, ecl, egr, epm, gctr, cnt, ne, scr, wscr;
+    int64_t wstride;
     int wwarps;
     size_t upload, total;
     int out_blocks;
@@ -742,7 +849,8 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     auto al = [](size_t x) { return (x + 255) / 256 * 256; };
     DevLayout D;
     D.out_blocks = std::max(1, std::min<int>((int)((P->outs.size() + 3) / 4), g_ctx.sm_count * 8));
-    D.spw = 2 * (int64_t)P->max_nf;
+    /* output scratch per warp: two cart->sph buffers, two transfer buffers (ERI mode) */
+    D.spw = 2 * (int64_t)P->max_nf + (P->eclass.empty() ? 0 : 2 * (int64_t)P->hrr_max);
     D.pairs = al(sizeof(CGPair) * std::max<size_t>(P->pairs.size(), 1));
     D.prims = al(sizeof(CGPrimPair) * std::max<size_t>(P->prims.size(), 1));
     D.tasks = al(sizeof(CGTask) * std::max<size_t>(P->tasks.size(), 1));
@@ -751,6 +859,9 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     D.gcl = al(sizeof(CGGradClass) * std::max<size_t>(P->gclass.size(), 1));
     D.gch = al(sizeof(CGGradChunk) * std::max<size_t>(P->gchunk.size(), 1));
     D.gen = al(sizeof(CGGradEnt) * std::max<size_t>(P->gent.size(), 1));
+    D.ecl = al(sizeof(CGEriClass) * std::max<size_t>(P->eclass.size(), 1));
+    D.egr = al(sizeof(CGEriGroup) * std::max<size_t>(P->egroup.size(), 1));
+    D.epm = al(sizeof(int) * std::max<size_t>(P->eperm.size(), 1));
     D.gctr = al(sizeof(double) * P->gctr_size);
     D.cnt = al(sizeof(int) * 4);
     D.ne = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
@@ -758,18 +869,61 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     D.wwarps = 0;
     D.wscr = 0;
     const bool grad = P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA;
+    /* per-warp slots: J mode holds (e0|f0) and two transfer buffers, the adjoint a cotangent */
+    D.wstride = P->jmode ? (int64_t)P->nef_max + 2 * (int64_t)P->hrr_max : (int64_t)P->max_nf;
     if (P->jmode || (grad && P->max_nf > CG_W_SMEM)) {
         D.wwarps = g_ctx.sm_count * 4 * (P->groups[0].blocks_per_sm + P->groups[1].blocks_per_sm);
-        D.wscr = al(sizeof(double) * (size_t)D.wwarps * P->max_nf);
+        D.wscr = al(sizeof(double) * (size_t)D.wwarps * D.wstride);
     }
     if (P->jmode || grad) D.gctr = al(sizeof(double));   /* no per-task accumulators */
-    D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq + D.gcl + D.gch + D.gen;
+    D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq + D.gcl + D.gch + D.gen + D.ecl + D.egr + D.epm;
     D.total = D.upload + D.gctr + D.cnt + D.ne + D.scr + D.wscr;
     return D;
 }
 
 static size_t plan_device_bytes(const CINTGPUPlan *P) { return dev_layout(P).total; }
 static size_t plan_upload_bytes(const CINTGPUPlan *P) { return dev_layout(P).upload; }
+
+/* Device pointers of every plan array inside one region laid out by D (upload part first). */
+static void carve_plan(CINTGPUPlan *P, const DevLayout &D, char *p)
+{
+    P->out_blocks = D.out_blocks;
+    P->scratch_per_warp = D.spw;
+    P->d_pairs = (CGPair *)p; p += D.pairs;
+    P->d_prims = (CGPrimPair *)p; p += D.prims;
+    P->d_tasks = (CGTask *)p; p += D.tasks;
+    P->d_outs = (CGOutTask *)p; p += D.outs;
+    P->d_pqlist = (int *)p; p += D.pq;
+    P->d_gclass = (CGGradClass *)p; p += D.gcl;
+    P->d_gchunk = (CGGradChunk *)p; p += D.gch;
+    P->d_gent = (CGGradEnt *)p; p += D.gen;
+    P->d_eclass = (CGEriClass *)p; p += D.ecl;
+    P->d_egroup = (CGEriGroup *)p; p += D.egr;
+    P->d_eperm = (int *)p; p += D.epm;
+    P->d_gctr = (double *)p; p += D.gctr;
+    P->d_counters = (int *)p; p += D.cnt;
+    P->d_nonempty = (int *)p; p += D.ne;
+    P->d_scratch = (double *)p; p += D.scr;
+    P->d_wscratch = (double *)p; p += D.wscr;
+    P->wscratch_stride = D.wstride;
+    P->wscratch_warps = D.wwarps;
+}
+
+/* Host image of the upload part of the region (D.upload bytes). */
+static void fill_image(const CINTGPUPlan *P, const DevLayout &D, char *q)
+{
+    memcpy(q, P->pairs.data(), sizeof(CGPair) * P->pairs.size()); q += D.pairs;
+    memcpy(q, P->prims.data(), sizeof(CGPrimPair) * P->prims.size()); q += D.prims;
+    memcpy(q, P->tasks.data(), sizeof(CGTask) * P->tasks.size()); q += D.tasks;
+    memcpy(q, P->outs.data(), sizeof(CGOutTask) * P->outs.size()); q += D.outs;
+    memcpy(q, P->pqlist.data(), sizeof(int) * P->pqlist.size()); q += D.pq;
+    memcpy(q, P->gclass.data(), sizeof(CGGradClass) * P->gclass.size()); q += D.gcl;
+    memcpy(q, P->gchunk.data(), sizeof(CGGradChunk) * P->gchunk.size()); q += D.gch;
+    memcpy(q, P->gent.data(), sizeof(CGGradEnt) * P->gent.size()); q += D.gen;
+    memcpy(q, P->eclass.data(), sizeof(CGEriClass) * P->eclass.size()); q += D.ecl;
+    memcpy(q, P->egroup.data(), sizeof(CGEriGroup) * P->egroup.size()); q += D.egr;
+    memcpy(q, P->eperm.data(), sizeof(int) * P->eperm.size());
+}
 
 /* Place the plan in device memory (a caller arena or its own allocation) and copy the host
  * images: pinned + async on `stream` for the drop-in, synchronous otherwise. */
@@ -791,35 +945,12 @@ static int upload_plan(CINTGPUPlan *P, char *arena, size_t arena_size, cudaStrea
         }
         P->dbuf_size = D.total; P->owns_dbuf = true;
     }
-    char *p = P->dbuf;
-    P->d_pairs = (CGPair *)p; p += D.pairs;
-    P->d_prims = (CGPrimPair *)p; p += D.prims;
-    P->d_tasks = (CGTask *)p; p += D.tasks;
-    P->d_outs = (CGOutTask *)p; p += D.outs;
-    P->d_pqlist = (int *)p; p += D.pq;
-    P->d_gclass = (CGGradClass *)p; p += D.gcl;
-    P->d_gchunk = (CGGradChunk *)p; p += D.gch;
-    P->d_gent = (CGGradEnt *)p; p += D.gen;
-    P->d_gctr = (double *)p; p += D.gctr;
-    P->d_counters = (int *)p; p += D.cnt;
-    P->d_nonempty = (int *)p; p += D.ne;
-    P->d_scratch = (double *)p; p += D.scr;
-    P->d_wscratch = (double *)p; p += D.wscr;
-    P->wscratch_stride = P->max_nf;
-    P->wscratch_warps = D.wwarps;
+    carve_plan(P, D, P->dbuf);
     std::vector<char> tmp;
     char *src;
     if (async_from_pinned) src = pinned;
     else { tmp.resize(D.upload); src = tmp.data(); }
-    char *q = src;
-    memcpy(q, P->pairs.data(), sizeof(CGPair) * P->pairs.size()); q += D.pairs;
-    memcpy(q, P->prims.data(), sizeof(CGPrimPair) * P->prims.size()); q += D.prims;
-    memcpy(q, P->tasks.data(), sizeof(CGTask) * P->tasks.size()); q += D.tasks;
-    memcpy(q, P->outs.data(), sizeof(CGOutTask) * P->outs.size()); q += D.outs;
-    memcpy(q, P->pqlist.data(), sizeof(int) * P->pqlist.size()); q += D.pq;
-    memcpy(q, P->gclass.data(), sizeof(CGGradClass) * P->gclass.size()); q += D.gcl;
-    memcpy(q, P->gchunk.data(), sizeof(CGGradChunk) * P->gchunk.size()); q += D.gch;
-    memcpy(q, P->gent.data(), sizeof(CGGradEnt) * P->gent.size()); q += D.gen;
+    fill_image(P, D, src);
     if (async_from_pinned) {
         CUDA_OK(cudaMemcpyAsync(P->dbuf, src, D.upload, cudaMemcpyHostToDevice, stream));
     } else {
@@ -883,11 +1014,16 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.jmode = P->jmode;
     L.wscratch = P->d_wscratch;
     if (P->jmode && g == 1)   /* the groups run concurrently: separate warp slots */
-        L.wscratch += (size_t)g_ctx.sm_count * 4 * P->groups[0].blocks_per_sm * P->max_nf;
+        L.wscratch += (size_t)g_ctx.sm_count * 4 * P->groups[0].blocks_per_sm * P->wscratch_stride;
     L.wscratch_stride = P->wscratch_stride;
     L.dm = P->cur_dm;
     L.vj = P->cur_vj;
     L.nao = P->nao_cart;
+    L.eclass = P->d_eclass;
+    L.egroup = P->d_egroup;
+    L.eperm = P->d_eperm;
+    L.hrr_off1 = P->nef_max;
+    L.hrr_off2 = (int64_t)P->nef_max + P->hrr_max;
     int nblocks = std::min(g_ctx.sm_count * G.blocks_per_sm, std::max(1, (G.ntasks + 3) / 4));
     int rc = cg_launch_eri(&L, P->mode, nblocks, stream);
     if (rc) { set_error("ERI kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
@@ -917,7 +1053,8 @@ static int execute_plan(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
     }
     if (P->jmode || P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) return 0;
     int rc = cg_launch_output(P->d_outs, (int)P->outs.size(), P->d_gctr, P->d_nonempty, P->d_scratch,
-                              P->scratch_per_warp, P->out_blocks, out_dev, P->ncomp, P->out_size, stream);
+                              P->scratch_per_warp, P->max_nf, P->d_eclass, P->d_eperm, P->out_blocks,
+                              out_dev, P->ncomp, P->out_size, stream);
     if (rc) { set_error("output kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
     return 0;
 }
@@ -1339,6 +1476,21 @@ void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas)
 int cg_init(void) { return ensure_init(); }
 int cg_sm_count(void) { return g_ctx.sm_count; }
 void cg_set_error_msg(const char *msg) { set_error("%s", msg); }
+/* Contraction-first tables of one class, for host-side tests of the table logic:
+ * info[8] = CGEriClass fields, groups[4 * ngroup], perm[nE + nF]. */
+extern "C" int cg_eri_tables(int li, int lj, int lk, int ll, int *info, int *groups, int maxg,
+                             int *perm, int maxp)
+{
+    CINTGPUPlan P;
+    build_eri_class(&P, li, lj, lk, ll);
+    const CGEriClass &c = P.eclass[0];
+    if (c.ngroup > maxg || c.nE + c.nF > maxp) return -1;
+    memcpy(info, &c, sizeof(CGEriClass));
+    memcpy(groups, P.egroup.data(), sizeof(CGEriGroup) * P.egroup.size());
+    memcpy(perm, P.eperm.data(), sizeof(int) * P.eperm.size());
+    return 0;
+}
+
 CINTGPUPlan *cg_plan_new(void) { return new CINTGPUPlan(); }
 void cg_plan_free_host(CINTGPUPlan *P) { P->dbuf = nullptr; delete P; }
 
@@ -1355,35 +1507,10 @@ int cg_plan_place(CINTGPUPlan *P, char *region, size_t region_bytes, cudaStream_
 {
     DevLayout D = dev_layout(P);
     if (D.total > region_bytes) { set_error("plan needs %zu bytes, region has %zu", D.total, region_bytes); return CINTGPU_ERR_NOMEM; }
-    P->out_blocks = D.out_blocks;
-    P->scratch_per_warp = D.spw;
     P->dbuf = region; P->dbuf_size = region_bytes; P->owns_dbuf = false;
-    char *p = region;
-    P->d_pairs = (CGPair *)p; p += D.pairs;
-    P->d_prims = (CGPrimPair *)p; p += D.prims;
-    P->d_tasks = (CGTask *)p; p += D.tasks;
-    P->d_outs = (CGOutTask *)p; p += D.outs;
-    P->d_pqlist = (int *)p; p += D.pq;
-    P->d_gclass = (CGGradClass *)p; p += D.gcl;
-    P->d_gchunk = (CGGradChunk *)p; p += D.gch;
-    P->d_gent = (CGGradEnt *)p; p += D.gen;
-    P->d_gctr = (double *)p; p += D.gctr;
-    P->d_counters = (int *)p; p += D.cnt;
-    P->d_nonempty = (int *)p; p += D.ne;
-    P->d_scratch = (double *)p; p += D.scr;
-    P->d_wscratch = (double *)p; p += D.wscr;
-    P->wscratch_stride = P->max_nf;
-    P->wscratch_warps = D.wwarps;
+    carve_plan(P, D, region);
     std::vector<char> img(D.upload);
-    char *q = img.data();
-    memcpy(q, P->pairs.data(), sizeof(CGPair) * P->pairs.size()); q += D.pairs;
-    memcpy(q, P->prims.data(), sizeof(CGPrimPair) * P->prims.size()); q += D.prims;
-    memcpy(q, P->tasks.data(), sizeof(CGTask) * P->tasks.size()); q += D.tasks;
-    memcpy(q, P->outs.data(), sizeof(CGOutTask) * P->outs.size()); q += D.outs;
-    memcpy(q, P->pqlist.data(), sizeof(int) * P->pqlist.size()); q += D.pq;
-    memcpy(q, P->gclass.data(), sizeof(CGGradClass) * P->gclass.size()); q += D.gcl;
-    memcpy(q, P->gchunk.data(), sizeof(CGGradChunk) * P->gchunk.size()); q += D.gch;
-    memcpy(q, P->gent.data(), sizeof(CGGradEnt) * P->gent.size());
+    fill_image(P, D, img.data());
     /* pageable source: returns once the data is staged, so img may be released afterwards */
     CUDA_OK(cudaMemcpyAsync(region, img.data(), D.upload, cudaMemcpyHostToDevice, stream));
     return 0;

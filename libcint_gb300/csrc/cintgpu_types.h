@@ -45,7 +45,7 @@ typedef struct {
     int64_t cart_off;    /* accumulator slot in gctr */
     int out;             /* CGOutTask index (for the non-empty flag) */
     int sym;             /* unique-quartet flags: bit0 I != J, bit1 K != L, bit2 IJ != KL */
-    int cls;             /* adjoint only: index of the class's iteration tables (CGGradClass) */
+    int cls;             /* class tables: CGGradClass (adjoint) or CGEriClass (int2e, int3c2e, J) */
     int pad;
 } CGTask;
 
@@ -64,13 +64,40 @@ typedef struct {
 } CGGradChunk;
 typedef struct { int ob_oc; int c; } CGGradEnt;                          /* ob | oc << 16 */
 
+/* Contraction-first int2e/int3c2e tables, one set per angular-momentum class (kernel order,
+ * li >= lj, lk >= ll).  The kernel accumulates (e0|f0) = sum over primitive quartets and roots of
+ * gx gy gz for every Cartesian e = (ex,ey,ez) with li <= |e| <= li+lj and f likewise, and the
+ * horizontal transfer to (ij|kl) runs once per contracted quartet.  A group is one
+ * (ex, ey, fx, fy): the product gx gy is formed once and multiplies gz for each (ez, fz) member.
+ * Accumulator layout: row baseE(ex,ey) + (ez - ez0), column baseF(fx,fy) + (fz - fz0), nF columns;
+ * eperm/fperm map the transfer's Cartesian order (shells ascending, libcint order within a shell)
+ * to those rows/columns. */
 typedef struct {
-    int64_t cart_off;    /* first accumulator slot; nparts slots follow, each ncomp*nf long */
+    int group_off, ngroup;   /* CGEriGroup range, sorted by member count (largest first) */
+    int perm_off;            /* eperm[nE] then fperm[nF] */
+    int nE, nF;
+    int split;               /* ngroup <= 32: lanes per group (power of two); 0: groups in rounds */
+    int hrr_need;            /* doubles of each of the two transfer buffers */
+    int maxab;               /* (lj + 1) | (ll + 1) << 8: member box of the class */
+} CGEriClass;
+typedef struct {
+    int oxy;             /* ox | oy << 16: offsets of (ex, fx) and (ey, fy) in the VRR arrays */
+    int oz;              /* offset of (ez0, fz0) in the z array */
+    int acc;             /* accumulator index of member (0, 0) */
+    int mn;              /* nez | nfz << 8 */
+} CGEriGroup;
+
+typedef struct {
+    int64_t cart_off;    /* first accumulator slot; nparts slots follow, each ncomp*nf long
+                            (nE*nF with flags bit1) */
     int64_t out_off;     /* element offset in the output array */
     int st[4];           /* output strides of the four shell indices (kernel order I,J,K,L) */
     int l[4];            /* angular momenta in kernel order */
     int nparts;
-    int flags;           /* bit0: 1 = spherical output */
+    int flags;           /* bit0: 1 = spherical output; bit1: slots hold (e0|f0) of class ecls */
+    int ecls;
+    int pad;
+    double AB[3], CD[3]; /* transfer vectors R_I - R_J, R_K - R_L */
 } CGOutTask;
 
 #endif

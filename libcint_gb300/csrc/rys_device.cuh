@@ -69,7 +69,17 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     L->scr = (L->nmax + 1) * (L->mmax + 1) + (L->nmax + 1) + (L->mmax + 1);
     const bool grad = mode == CG_MODE_GRAD || mode == CG_MODE_GRADA;
     int T = 0;
-    if (!grad) {
+    if (mode == CG_MODE_ERI) {
+        /* contraction first: per term only the VRR arrays g(e, f), e <= li+lj, f <= lk+ll */
+        L->G = (L->nmax + 1) * (L->mmax + 1);
+        L->scr = 0;
+        L->gstride = 3 * L->G + ((3 * L->G) % 2 == 0 ? 1 : 0);
+        T = (ws_doubles - CG_TERMW * 32) / L->gstride;
+        if (T > 32) T = 32;
+        if (T < 0) T = 0;
+        L->off_dij = L->off_dkl = L->off_aacc = L->off_w = L->off_scr = 0;
+        L->off_g = CG_TERMW * 32;
+    } else if (!grad) {
         int avail = ws_doubles - CG_TERMW * 32;     /* term records */
         /* T terms need T*3*ng*G doubles of g arrays and min(32, 3T) lane scratch areas */
         for (int t = 32; t >= 1; t--) {
@@ -207,6 +217,137 @@ __device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10
             }
         }
     }
+}
+
+
+/* VRR only (contraction-first path): g(a, m) = out[a + (nmax+1) m] for a <= nmax, m <= mmax,
+ * written straight into the term's g array (libcint CINTg0_2e_2d, src/g2e.c:272-330). */
+__device__ __forceinline__ void vrr_axis(int nmax, int mmax, double b00, double b10, double b01,
+                                         double c00, double c0p, double g00, double *out)
+{
+    const int na = nmax + 1;
+    out[0] = g00;
+    if (nmax > 0) {
+        double p0 = g00, p1 = c00 * g00, nb = b10;
+        out[1] = p1;
+        for (int a = 1; a < nmax; a++) {
+            double p2 = fma(c00, p1, nb * p0);
+            out[a + 1] = p2;
+            p0 = p1; p1 = p2;
+            nb += b10;
+        }
+    }
+    double mb = 0.0;
+    for (int m = 0; m < mmax; m++) {
+        const double *cm = out + m * na;
+        double *cn = out + (m + 1) * na;
+        double ab = 0.0;                  /* a * b00 */
+        for (int a = 0; a <= nmax; a++) {
+            double v = c0p * cm[a];
+            if (m > 0) v = fma(mb, cm[a - na], v);
+            if (a > 0) v = fma(ab, cm[a - 1], v);
+            cn[a] = v;
+            ab += b00;
+        }
+        mb += b01;
+    }
+}
+
+/* libcint Cartesian order within a shell of momentum l: index of (x, y, l-x-y) */
+__host__ __device__ __forceinline__ int cidx_l(int l, int x, int y)
+{
+    int r = l - x;
+    return r * (r + 1) / 2 + (r - y);
+}
+/* components of all shells below l: l (l+1) (l+2) / 6 */
+__host__ __device__ __forceinline__ int ncart_below(int l) { return l * (l + 1) * (l + 2) / 6; }
+
+/* index q of the range of shells l0, l0+1, ... (ascending, libcint order inside) -> shell and
+ * powers */
+__device__ __forceinline__ void range_pow(int l0, int q, int &l, int &x, int &y, int &z)
+{
+    l = l0;
+    const int b = ncart_below(l0);
+    while (ncart_below(l + 1) - b <= q) l++;
+    cart_pow(l, q - (ncart_below(l) - b), x, y, z);
+}
+
+
+/* Horizontal transfer of one contracted quartet, warp-cooperative (libcint CINTg0_2e_il2d4d /
+ * CINTg0_2e_lj2d4d, src/g2e.c:560-693, applied to the contracted (e0|f0) block instead of each
+ * primitive's 2D integrals):
+ *   (e, j+1_x | = (e+1_x, j| + AB_x (e, j|      on the bra, the lowest non-zero axis of j,
+ *   |f, l+1_x)  = |f+1_x, l) + CD_x |f, l)      then on the ket.
+ * src holds the accumulators in the class's group layout; the Cartesian block comes back in
+ * gctr order (i + nfi (k + nfk (l + nfl j))) in h1 or h2 (the returned pointer). */
+__device__ inline double *cg_hrr(const double *src, const int *__restrict__ eperm,
+                                 const int *__restrict__ fperm, int li, int lj, int lk, int ll,
+                                 const double *AB, const double *CD, double *h1, double *h2,
+                                 int lane)
+{
+    const int bE = ncart_below(li), bF = ncart_below(lk);
+    const int nE = ncart_below(li + lj + 1) - bE, nF = ncart_below(lk + ll + 1) - bF;
+    for (int e = lane; e < nE * nF; e += 32) {
+        int ei = e / nF, fi = e - ei * nF;
+        h1[e] = src[__ldg(eperm + ei) * nF + __ldg(fperm + fi)];
+    }
+    __syncwarp();
+    double *cur = h1, *nxt = h2;
+    /* bra: level b holds [(ei nc(b) + jb) nF + f], ei over shells li .. li+lj-b */
+    for (int b = 1; b <= lj; b++) {
+        const int nEp = ncart_below(li + lj - b + 1) - bE;
+        const int ncb = ncart(b), ncb1 = ncart(b - 1);
+        const int tot = nEp * ncb * nF;
+        for (int e = lane; e < tot; e += 32) {
+            int f = e % nF, r = e / nF;
+            int jb = r % ncb, ei = r / ncb;
+            int el, x, y, z, jx, jy, jz;
+            range_pow(li, ei, el, x, y, z);
+            cart_pow(b, jb, jx, jy, jz);
+            const int ax = jx > 0 ? 0 : (jy > 0 ? 1 : 2);
+            const int dx = ax == 0, dy = ax == 1;
+            const int jp = cidx_l(b - 1, jx - dx, jy - dy);
+            const int eu = ncart_below(el + 1) - bE + cidx_l(el + 1, x + dx, y + dy);
+            nxt[e] = fma(AB[ax], cur[(ei * ncb1 + jp) * nF + f], cur[(eu * ncb1 + jp) * nF + f]);
+        }
+        __syncwarp();
+        double *t = cur; cur = nxt; nxt = t;
+    }
+    /* ket: level d holds [(ij nFp + fi) nc(d) + ld], fi over shells lk .. lk+ll-d */
+    const int nfi = ncart(li), nfj = ncart(lj), nfk = ncart(lk), nfl = ncart(ll);
+    const int nij = nfi * nfj;
+    int nFprev = nF;
+    for (int d = 1; d <= ll; d++) {
+        const int nFp = ncart_below(lk + ll - d + 1) - bF;
+        const int ncd = ncart(d), ncd1 = ncart(d - 1);
+        const int tot = nij * nFp * ncd;
+        for (int e = lane; e < tot; e += 32) {
+            int ld = e % ncd, r = e / ncd;
+            int fi = r % nFp, ij = r / nFp;
+            int fl, x, y, z, lx, ly, lz;
+            range_pow(lk, fi, fl, x, y, z);
+            cart_pow(d, ld, lx, ly, lz);
+            const int ax = lx > 0 ? 0 : (ly > 0 ? 1 : 2);
+            const int dx = ax == 0, dy = ax == 1;
+            const int lp = cidx_l(d - 1, lx - dx, ly - dy);
+            const int fu = ncart_below(fl + 1) - bF + cidx_l(fl + 1, x + dx, y + dy);
+            nxt[e] = fma(CD[ax], cur[(ij * nFprev + fi) * ncd1 + lp],
+                         cur[(ij * nFprev + fu) * ncd1 + lp]);
+        }
+        __syncwarp();
+        double *t = cur; cur = nxt; nxt = t;
+        nFprev = nFp;
+    }
+    /* cur[((i nfj + j) nfk + k) nfl + l] -> gctr order */
+    const int nf = nij * nfk * nfl;
+    for (int e = lane; e < nf; e += 32) {
+        int i = e % nfi, r = e / nfi;
+        int k = r % nfk; r /= nfk;
+        int l = r % nfl, j = r / nfl;
+        nxt[e] = cur[((i * nfj + j) * nfk + k) * nfl + l];
+    }
+    __syncwarp();
+    return nxt;
 }
 
 

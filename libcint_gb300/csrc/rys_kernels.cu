@@ -66,8 +66,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
     const double common = P.common_base * common_fac_sp(li) * common_fac_sp(lj)
                         * common_fac_sp(lk) * (P.three ? 1.0 : common_fac_sp(ll));
     double *scr_base = greg + T * 3 * L.ng * L.G;
-    double *acc = P.jmode ? P.wscratch + (size_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * P.wscratch_stride
-                          : P.gctr + tk.cart_off;
+    double *acc = P.gctr + tk.cart_off;
 
     /* per-lane component offsets into the g arrays, packed 10 bits per axis */
     int offs[NS > 0 ? NS : 1];
@@ -147,47 +146,32 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                 if (lane + 32 * s >= L.nf) continue;
                 const int ox = offs[s] & 1023, oy = (offs[s] >> 10) & 1023, oz = offs[s] >> 20;
                 const double *gb = greg;
-                if (MODE == CG_MODE_ERI) {
-                    double s0 = ra[s][0];
-                    for (int t = 0; t < Tb; t++, gb += stride_t)
-                        s0 = fma(gb[ox] * gb[G + oy], gb[2 * G + oz], s0);
-                    ra[s][0] = s0;
-                } else {
-                    double sx = ra[s][0], sy = ra[s][MODE == CG_MODE_IP1 ? 1 : 0],
-                           sz = ra[s][MODE == CG_MODE_IP1 ? 2 : 0];
-                    for (int t = 0; t < Tb; t++, gb += stride_t) {
-                        double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
-                        double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
-                        sx = fma(fx, gy * gz, sx);
-                        sy = fma(fy, gx * gz, sy);
-                        sz = fma(fz, gx * gy, sz);
-                    }
-                    ra[s][0] = sx;
-                    ra[s][MODE == CG_MODE_IP1 ? 1 : 0] = sy;
-                    ra[s][MODE == CG_MODE_IP1 ? 2 : 0] = sz;
+                double sx = ra[s][0], sy = ra[s][1], sz = ra[s][2];
+                for (int t = 0; t < Tb; t++, gb += stride_t) {
+                    double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
+                    double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
+                    sx = fma(fx, gy * gz, sx);
+                    sy = fma(fy, gx * gz, sy);
+                    sz = fma(fz, gx * gy, sz);
                 }
+                ra[s][0] = sx;
+                ra[s][1] = sy;
+                ra[s][2] = sz;
             }
         } else {
             for (int c = lane; c < L.nf; c += 32) {
                 const int o3 = comp_offsets(c);
                 const int ox = o3 & 1023, oy = (o3 >> 10) & 1023, oz = o3 >> 20;
                 const double *gb = greg;
-                if (MODE == CG_MODE_ERI) {
-                    double s0 = acc[c];
-                    for (int t = 0; t < Tb; t++, gb += stride_t)
-                        s0 = fma(gb[ox] * gb[G + oy], gb[2 * G + oz], s0);
-                    acc[c] = s0;
-                } else {
-                    double sx = acc[c], sy = acc[L.nf + c], sz = acc[2 * L.nf + c];
-                    for (int t = 0; t < Tb; t++, gb += stride_t) {
-                        double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
-                        double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
-                        sx = fma(fx, gy * gz, sx);
-                        sy = fma(fy, gx * gz, sy);
-                        sz = fma(fz, gx * gy, sz);
-                    }
-                    acc[c] = sx; acc[L.nf + c] = sy; acc[2 * L.nf + c] = sz;
+                double sx = acc[c], sy = acc[L.nf + c], sz = acc[2 * L.nf + c];
+                for (int t = 0; t < Tb; t++, gb += stride_t) {
+                    double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
+                    double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
+                    sx = fma(fx, gy * gz, sx);
+                    sy = fma(fy, gx * gz, sy);
+                    sz = fma(fz, gx * gy, sz);
                 }
+                acc[c] = sx; acc[L.nf + c] = sy; acc[2 * L.nf + c] = sz;
             }
         }
         __syncwarp();
@@ -202,11 +186,174 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             }
         }
     }
-    if (MODE == CG_MODE_ERI && P.jmode) {
+    if (lane == 0) P.nonempty[tk.out] = 1;
+}
+
+/* ---------------------------------------------------------- contraction-first int2e path */
+/* Stage 3 of one group over terms t_begin, t_begin + tstep, ... < Tb: p = gx gy once, then
+ * r[b * 4 + a] += p gz(ez0 + a, fz0 + b) for the group's nez x nfz members (MA x MB bound). */
+template <int MA, int MB>
+__device__ __forceinline__ void e0f0_terms(const double *__restrict__ greg, int gstride, int G,
+                                           int na, int t_begin, int Tb, int tstep, int oxy,
+                                           int oz, int mn, double (&r)[16])
+{
+    const int ox = oxy & 0xffff, oy = oxy >> 16;
+    const int nez = mn & 0xff, nfz = mn >> 8;
+    for (int t = t_begin; t < Tb; t += tstep) {
+        const double *g = greg + (size_t)t * gstride;
+        const double p = g[ox] * g[G + oy];
+        const double *gz = g + 2 * G + oz;
+#pragma unroll
+        for (int b = 0; b < MB; b++)
+#pragma unroll
+            for (int a = 0; a < MA; a++)
+                if (a < nez && b < nfz) r[b * 4 + a] = fma(p, gz[a + na * b], r[b * 4 + a]);
+    }
+}
+
+__device__ __forceinline__ void e0f0_dispatch(int mab, const double *greg, int gstride, int G,
+                                              int na, int t_begin, int Tb, int tstep, int oxy,
+                                              int oz, int mn, double (&r)[16])
+{
+#define CG_E0F0_CASE(A, B) \
+    case (A - 1) + 4 * (B - 1): e0f0_terms<A, B>(greg, gstride, G, na, t_begin, Tb, tstep, oxy, oz, mn, r); break;
+    switch (mab) {
+    CG_E0F0_CASE(1, 1) CG_E0F0_CASE(2, 1) CG_E0F0_CASE(3, 1) CG_E0F0_CASE(4, 1)
+    CG_E0F0_CASE(1, 2) CG_E0F0_CASE(2, 2) CG_E0F0_CASE(3, 2) CG_E0F0_CASE(4, 2)
+    CG_E0F0_CASE(1, 3) CG_E0F0_CASE(2, 3) CG_E0F0_CASE(3, 3) CG_E0F0_CASE(4, 3)
+    CG_E0F0_CASE(1, 4) CG_E0F0_CASE(2, 4) CG_E0F0_CASE(3, 4) CG_E0F0_CASE(4, 4)
+    default: break;
+    }
+#undef CG_E0F0_CASE
+}
+
+/* One int2e / int3c2e / J task, contraction first: per term the VRR arrays only; stage 3
+ * accumulates (e0|f0) of the task's slice; the horizontal transfer runs in the output kernel
+ * (once per contracted quartet) or, for J, at the end of the task. */
+__device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &tk, const CGLayout &L,
+                                              double *term, double *greg, int lane)
+{
+    const CGPair pij = P.pairs[tk.pij];
+    const CGPair pkl = P.pairs[tk.pkl];
+    const CGPrimPair *__restrict__ ppij = P.prims + pij.prim_off;
+    const CGPrimPair *__restrict__ ppkl = P.prims + pkl.prim_off;
+    const int *__restrict__ pql = P.pqlist + tk.pq_off;
+    const int nij = pij.npa * pij.npb;
+    const int li = pij.la, lj = pij.lb, lk = pkl.la, ll = pkl.lb;
+    const int n = L.nroots, T = L.T, G = L.G, gstride = L.gstride, na = L.nmax + 1;
+    const double common = P.common_base * common_fac_sp(li) * common_fac_sp(lj)
+                        * common_fac_sp(lk) * (P.three ? 1.0 : common_fac_sp(ll));
+    const CGEriClass ec = P.eclass[tk.cls];
+    const CGEriGroup *__restrict__ grp = P.egroup + ec.group_off;
+    const int nF = ec.nF, nEF = ec.nE * ec.nF;
+    double *wbase = P.jmode ? P.wscratch + (size_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * P.wscratch_stride
+                            : nullptr;
+    double *acc = P.jmode ? wbase : P.gctr + tk.cart_off;
+    const int MA = ec.maxab & 0xff, MB = ec.maxab >> 8;
+    const bool boxed = MA <= 4 && MB <= 4;
+    const int mab = (MA - 1) + 4 * (MB - 1);
+    const int S = ec.split;
+
+    double r[16];
+#pragma unroll
+    for (int m = 0; m < 16; m++) r[m] = 0.0;
+    int sp = 0;
+    bool own = false;
+    CGEriGroup mine = {0, 0, 0, 0};
+    if (S > 0) {
+        /* lane = group + ngroup * split: one group per lane for the whole task */
+        const int gi = lane % ec.ngroup;
+        sp = lane / ec.ngroup;
+        own = sp < S;
+        if (own) mine = grp[gi];
+    } else {
+        for (int c = lane; c < nEF; c += 32) acc[c] = 0.0;
+        __syncwarp();
+    }
+
+    const int nterm = tk.npq * n;
+    for (int t0 = 0; t0 < nterm; t0 += T) {
+        const int Tb = min(T, nterm - t0);
+        /* ---- stage 1: one lane per term */
+        if (lane < Tb) {
+            int g = t0 + lane;
+            int p = g / n, rr = g - p * n;
+            int q = __ldg(pql + p);
+            int kl = q / nij, ij = q - kl * nij;
+            cg_term(ppij[ij], ppkl[kl], pij, pkl, n, rr, common, P.rys_coef, term + lane * CG_TERMW);
+        }
+        __syncwarp();
+        /* ---- stage 2: one lane per (term, axis), VRR only */
+        for (int item = lane; item < 3 * Tb; item += 32) {
+            int t = item / 3, ax = item - 3 * t;
+            const double *rec = term + t * CG_TERMW;
+            double g00 = (ax == 2) ? rec[9] : 1.0;
+            vrr_axis(L.nmax, L.mmax, rec[0], rec[1], rec[2], rec[3 + ax], rec[6 + ax], g00,
+                     greg + (size_t)t * gstride + ax * G);
+        }
+        __syncwarp();
+        /* ---- stage 3: groups */
+        if (S > 0) {
+            if (own) e0f0_dispatch(mab, greg, gstride, G, na, sp, Tb, S, mine.oxy, mine.oz, mine.mn, r);
+        } else if (boxed) {
+            for (int gi = lane; gi < ec.ngroup; gi += 32) {
+                const CGEriGroup q = grp[gi];
+                const int nez = q.mn & 0xff, nfz = q.mn >> 8;
+                double v[16];
+#pragma unroll
+                for (int b = 0; b < 4; b++)
+#pragma unroll
+                    for (int a = 0; a < 4; a++)
+                        v[b * 4 + a] = (a < nez && b < nfz) ? acc[q.acc + a * nF + b] : 0.0;
+                e0f0_dispatch(mab, greg, gstride, G, na, 0, Tb, 1, q.oxy, q.oz, q.mn, v);
+#pragma unroll
+                for (int b = 0; b < 4; b++)
+#pragma unroll
+                    for (int a = 0; a < 4; a++)
+                        if (a < nez && b < nfz) acc[q.acc + a * nF + b] = v[b * 4 + a];
+            }
+        } else {
+            /* member at a time (lj or ll above 3) */
+            for (int gi = lane; gi < ec.ngroup; gi += 32) {
+                const CGEriGroup q = grp[gi];
+                const int ox = q.oxy & 0xffff, oy = q.oxy >> 16;
+                const int nez = q.mn & 0xff, nfz = q.mn >> 8;
+                for (int b = 0; b < nfz; b++)
+                    for (int a = 0; a < nez; a++) {
+                        double s0 = acc[q.acc + a * nF + b];
+                        const double *g = greg;
+                        for (int t = 0; t < Tb; t++, g += gstride)
+                            s0 = fma(g[ox] * g[G + oy], g[2 * G + q.oz + a + na * b], s0);
+                        acc[q.acc + a * nF + b] = s0;
+                    }
+            }
+        }
+        __syncwarp();
+    }
+    if (S > 0) {
+        /* sum the splits (lanes gi + ngroup * sp), then the first split stores its members */
+        for (int off = S >> 1; off >= 1; off >>= 1) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) r[m] += __shfl_down_sync(FULL, r[m], off * ec.ngroup);
+        }
+        if (own && sp == 0) {
+            const int nez = mine.mn & 0xff, nfz = mine.mn >> 8;
+#pragma unroll
+            for (int b = 0; b < 4; b++)
+#pragma unroll
+                for (int a = 0; a < 4; a++)
+                    if (a < nez && b < nfz) acc[mine.acc + a * nF + b] = r[b * 4 + a];
+        }
+        __syncwarp();
+    }
+    if (P.jmode) {
         /* J contraction of this slice (linear, so slices contract independently):
          * X[i,j] += s_kl sum_kl (ij|kl) D[k,l];  X[k,l] += s_ij sum_ij (ij|kl) D[i,j] if IJ != KL,
          * s = 2 for an off-diagonal shell pair of the unique list (D and (ij|kl) symmetric). */
-        __syncwarp();
+        const double *cart = cg_hrr(acc, P.eperm + ec.perm_off, P.eperm + ec.perm_off + ec.nE,
+                                    li, lj, lk, ll, pij.AB, pkl.AB, wbase + P.hrr_off1,
+                                    wbase + P.hrr_off2, lane);
+        const int nfi = ncart(li), nfj = ncart(lj), nfk = ncart(lk), nfl = ncart(ll);
         const int nao = P.nao;
         const double skl = (tk.sym & 2) ? 2.0 : 1.0, sij = (tk.sym & 1) ? 2.0 : 1.0;
         const double *Dkl = P.dm + (size_t)pkl.ao_a * nao + pkl.ao_b;
@@ -215,7 +362,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             double v = 0.0;
             for (int l = 0; l < nfl; l++)
                 for (int k = 0; k < nfk; k++)
-                    v = fma(acc[i + nfi * (k + nfk * (l + nfl * j))], __ldg(Dkl + (size_t)k * nao + l), v);
+                    v = fma(cart[i + nfi * (k + nfk * (l + nfl * j))], __ldg(Dkl + (size_t)k * nao + l), v);
             atomicAdd(P.vj + (size_t)(pij.ao_a + i) * nao + pij.ao_b + j, skl * v);
         }
         if (tk.sym & 4) {
@@ -225,13 +372,14 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                 double v = 0.0;
                 for (int j = 0; j < nfj; j++)
                     for (int i = 0; i < nfi; i++)
-                        v = fma(acc[i + nfi * (k + nfk * (l + nfl * j))], __ldg(Dij + (size_t)i * nao + j), v);
+                        v = fma(cart[i + nfi * (k + nfk * (l + nfl * j))], __ldg(Dij + (size_t)i * nao + j), v);
                 atomicAdd(P.vj + (size_t)(pkl.ao_a + k) * nao + pkl.ao_b + l, sij * v);
             }
         }
         __syncwarp();
+    } else if (lane == 0) {
+        P.nonempty[tk.out] = 1;
     }
-    if (lane == 0 && !P.jmode) P.nonempty[tk.out] = 1;
 }
 
 template <int MODE>
@@ -260,9 +408,9 @@ rys_eri_kernel(CGLaunch P)
             if (lane == 0) atomicOr(P.status, 1);
             continue;
         }
-        if (ns <= 1) run_task<MODE, 1>(P, tk, L, term, greg, lane);
+        if (MODE == CG_MODE_ERI) run_task_e0f0(P, tk, L, term, ws + L.off_g, lane);
+        else if (ns <= 1) run_task<MODE, 1>(P, tk, L, term, greg, lane);
         else if (ns <= 4) run_task<MODE, 4>(P, tk, L, term, greg, lane);
-        else if (ns <= 16 && MODE == CG_MODE_ERI) run_task<MODE, 16>(P, tk, L, term, greg, lane);
         else run_task<MODE, 0>(P, tk, L, term, greg, lane);
     }
 }
@@ -298,14 +446,17 @@ __device__ __forceinline__ void c2s_pass(const double *src, double *dst, int lsh
 
 __global__ void __launch_bounds__(128)
 cg_output_kernel(const CGOutTask *__restrict__ ot, int nout, double *gctr, const int *nonempty,
-                 double *scratch, int64_t scratch_per_warp, double *out, int ncomp,
-                 int64_t comp_stride)
+                 double *scratch, int64_t scratch_per_warp, int64_t nf_max,
+                 const CGEriClass *__restrict__ eclass, const int *__restrict__ eperm,
+                 double *out, int ncomp, int64_t comp_stride)
 {
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     double *s1 = scratch + (size_t)gw * scratch_per_warp;
-    double *s2 = s1 + scratch_per_warp / 2;
+    double *s2 = s1 + nf_max;
+    double *h1 = s2 + nf_max;
+    double *h2 = h1 + (scratch_per_warp - 2 * nf_max) / 2;
     for (int q = gw; q < nout; q += nw) {
         const CGOutTask o = ot[q];
         const int sph = o.flags & 1;
@@ -316,12 +467,15 @@ cg_output_kernel(const CGOutTask *__restrict__ ot, int nout, double *gctr, const
         }
         const int nf = nfc[0] * nfc[1] * nfc[2] * nfc[3];
         const bool ne = nonempty[q] != 0;
+        const bool e0f0 = (o.flags & 2) != 0;
+        const CGEriClass ec = e0f0 ? eclass[o.ecls] : CGEriClass{0, 0, 0, 0, 0, 0, 0, 0};
+        const int slot = e0f0 ? ec.nE * ec.nF : nf;   /* accumulators per part and component */
         for (int comp = 0; comp < ncomp; comp++) {
-            double *g0 = gctr + o.cart_off + (size_t)comp * nf;
+            double *g0 = gctr + o.cart_off + (size_t)comp * slot;
             if (ne && o.nparts > 1) {
-                for (int c = lane; c < nf; c += 32) {
+                for (int c = lane; c < slot; c += 32) {
                     double v = g0[c];
-                    for (int p = 1; p < o.nparts; p++) v += g0[(size_t)p * ncomp * nf + c];
+                    for (int p = 1; p < o.nparts; p++) v += g0[(size_t)p * ncomp * slot + c];
                     g0[c] = v;
                 }
                 __syncwarp();
@@ -340,6 +494,9 @@ cg_output_kernel(const CGOutTask *__restrict__ ot, int nout, double *gctr, const
             }
             /* gctr order: i fastest, then k, l, j.  Pass j: inner = nfi*nfk*nfl, t = j */
             const double *cur = g0;
+            if (e0f0)
+                cur = cg_hrr(g0, eperm + ec.perm_off, eperm + ec.perm_off + ec.nE, o.l[0], o.l[1],
+                             o.l[2], o.l[3], o.AB, o.CD, h1, h2, lane);
             c2s_pass(cur, s1, o.l[1], sph, nfc[0] * nfc[2] * nfc[3], nfc[1], 1, lane);
             __syncwarp();
             /* pass l: (i,k | l | js) */
@@ -415,11 +572,13 @@ extern "C" int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStrea
 }
 
 extern "C" int cg_launch_output(const CGOutTask *ot, int nout, double *gctr, const int *nonempty,
-                                double *scratch, int64_t scratch_per_warp, int nblocks, double *out,
+                                double *scratch, int64_t scratch_per_warp, int64_t nf_max,
+                                const CGEriClass *eclass, const int *eperm, int nblocks, double *out,
                                 int ncomp, int64_t comp_stride, cudaStream_t stream)
 {
     cg_output_kernel<<<nblocks, 128, 0, stream>>>(ot, nout, gctr, nonempty, scratch,
-                                                  scratch_per_warp, out, ncomp, comp_stride);
+                                                  scratch_per_warp, nf_max, eclass, eperm, out,
+                                                  ncomp, comp_stride);
     return (int)cudaGetLastError();
 }
 

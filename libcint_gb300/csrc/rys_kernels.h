@@ -46,6 +46,11 @@ typedef struct {
     const double *dm;         /* Cartesian density, nao x nao, row major */
     double *vj;               /* J accumulator (one triangle of shell blocks, see the host) */
     int nao;
+    /* contraction-first tables (ERI mode) */
+    const CGEriClass *eclass;
+    const CGEriGroup *egroup;
+    const int *eperm;
+    int64_t hrr_off1, hrr_off2;   /* J mode: transfer buffers inside the warp's slot */
 } CGLaunch;
 
 typedef struct {
@@ -82,8 +87,11 @@ int cg_blocks_per_sm(int mode, int ws_doubles);
 int cg_rys_deg(void);
 void cg_layout(int li, int lj, int lk, int ll, int mode, int ws_doubles, CGLayout *L);
 int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStream_t stream);
+/* scratch per warp: two cart->sph buffers of nf_max doubles, then two transfer buffers of
+ * (scratch_per_warp - 2 nf_max) / 2 doubles */
 int cg_launch_output(const CGOutTask *ot, int nout, double *gctr, const int *nonempty,
-                     double *scratch, int64_t scratch_per_warp, int nblocks, double *out,
+                     double *scratch, int64_t scratch_per_warp, int64_t nf_max,
+                     const CGEriClass *eclass, const int *eperm, int nblocks, double *out,
                      int ncomp, int64_t comp_stride, cudaStream_t stream);
 int cg_grad_tu_init(const int *c2s_nnz, const int *c2s_idx, const double *c2s_val);
 int cg_launch_grad(const CGGradLaunch *P, int mode, int nblocks, cudaStream_t stream);

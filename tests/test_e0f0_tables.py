@@ -1,0 +1,185 @@
+"""Host logic of the contraction-first int2e path, CPU only: the class tables built by the
+planner (stage-3 groups, accumulator permutations, transfer buffer size), replayed in numpy the
+way the kernel uses them, give the same Cartesian block as the per-term horizontal transfer
+(libcint's order of operations, src/g2e.c:560-693 then src/cint2e.c:961-1183) on random VRR
+arrays."""
+import ctypes
+import itertools
+
+import numpy as np
+import pytest
+
+from tests import _oracle  # noqa: F401  (puts the repo root on sys.path)
+import libcint_gb300 as cg
+
+
+def nc(l):
+    return (l + 1) * (l + 2) // 2
+
+
+def below(l):
+    return l * (l + 1) * (l + 2) // 6
+
+
+def cart_list(l):
+    return [(x, y, l - x - y) for x in range(l, -1, -1) for y in range(l - x, -1, -1)]
+
+
+def cidx(l, x, y):
+    r = l - x
+    return r * (r + 1) // 2 + (r - y)
+
+
+def range_pow(l0, q):
+    l = l0
+    while below(l + 1) - below(l0) <= q:
+        l += 1
+    return (l,) + cart_list(l)[q - (below(l) - below(l0))]
+
+
+def tables(li, lj, lk, ll):
+    f = cg.lib().cg_eri_tables
+    f.restype = ctypes.c_int
+    info = np.zeros(8, np.int32)
+    groups = np.zeros(4 * 20000, np.int32)
+    perm = np.zeros(4000, np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    assert f(li, lj, lk, ll, P(info), P(groups), 20000, P(perm), 4000) == 0
+    keys = ['group_off', 'ngroup', 'perm_off', 'nE', 'nF', 'split', 'hrr_need', 'maxab']
+    c = dict(zip(keys, info.tolist()))
+    return c, groups[:4 * c['ngroup']].reshape(-1, 4), perm[:c['nE'] + c['nF']]
+
+
+def hrr(src, eperm, fperm, li, lj, lk, ll, AB, CD, need):
+    """cg_hrr replayed: returns the Cartesian block in gctr order and the largest buffer used."""
+    bE, bF = below(li), below(lk)
+    nE, nF = below(li + lj + 1) - bE, below(lk + ll + 1) - bF
+    cur = np.array([src[eperm[e] * nF + fperm[f]] for e in range(nE) for f in range(nF)])
+    used = cur.size
+    for b in range(1, lj + 1):
+        nEp = below(li + lj - b + 1) - bE
+        ncb, ncb1 = nc(b), nc(b - 1)
+        nxt = np.zeros(nEp * ncb * nF)
+        for e in range(nxt.size):
+            f, r = e % nF, e // nF
+            jb, ei = r % ncb, r // ncb
+            el, x, y, z = range_pow(li, ei)
+            jx, jy, jz = cart_list(b)[jb]
+            ax = 0 if jx > 0 else (1 if jy > 0 else 2)
+            dx, dy = int(ax == 0), int(ax == 1)
+            jp = cidx(b - 1, jx - dx, jy - dy)
+            eu = below(el + 1) - bE + cidx(el + 1, x + dx, y + dy)
+            nxt[e] = AB[ax] * cur[(ei * ncb1 + jp) * nF + f] + cur[(eu * ncb1 + jp) * nF + f]
+        cur = nxt
+        used = max(used, cur.size)
+    nfi, nfj, nfk, nfl = nc(li), nc(lj), nc(lk), nc(ll)
+    nij = nfi * nfj
+    nFprev = nF
+    for d in range(1, ll + 1):
+        nFp = below(lk + ll - d + 1) - bF
+        ncd, ncd1 = nc(d), nc(d - 1)
+        nxt = np.zeros(nij * nFp * ncd)
+        for e in range(nxt.size):
+            ld, r = e % ncd, e // ncd
+            fi, ij = r % nFp, r // nFp
+            fl, x, y, z = range_pow(lk, fi)
+            lx, ly, lz = cart_list(d)[ld]
+            ax = 0 if lx > 0 else (1 if ly > 0 else 2)
+            dx, dy = int(ax == 0), int(ax == 1)
+            lp = cidx(d - 1, lx - dx, ly - dy)
+            fu = below(fl + 1) - bF + cidx(fl + 1, x + dx, y + dy)
+            nxt[e] = CD[ax] * cur[(ij * nFprev + fi) * ncd1 + lp] + cur[(ij * nFprev + fu) * ncd1 + lp]
+        cur = nxt
+        nFprev = nFp
+        used = max(used, cur.size)
+    out = np.zeros(nij * nfk * nfl)
+    for e in range(out.size):
+        i, r = e % nfi, e // nfi
+        k, r = r % nfk, r // nfk
+        l, j = r % nfl, r // nfl
+        out[e] = cur[((i * nfj + j) * nfk + k) * nfl + l]
+    assert max(used, out.size) <= need
+    return out
+
+
+def direct(g, li, lj, lk, ll, AB, CD):
+    """Per-term transfer of each axis, then the product over axes summed over terms."""
+    nT, _, nm, na = g.shape
+    # g4[t, ax, i, j, k, l]
+    g4 = np.zeros((nT, 3, li + 1, lj + 1, lk + 1, ll + 1))
+    for ax in range(3):
+        # bra: h[e, j, m]
+        h = np.zeros((nT, na, lj + 1, nm))
+        h[:, :, 0, :] = np.transpose(g[:, ax], (0, 2, 1))
+        for j in range(1, lj + 1):
+            for e in range(na - j):
+                h[:, e, j] = h[:, e + 1, j - 1] + AB[ax] * h[:, e, j - 1]
+        for i in range(li + 1):
+            for j in range(lj + 1):
+                q = np.zeros((nT, nm, ll + 1))
+                q[:, :, 0] = h[:, i, j, :]
+                for l in range(1, ll + 1):
+                    for f in range(nm - l):
+                        q[:, f, l] = q[:, f + 1, l - 1] + CD[ax] * q[:, f, l - 1]
+                g4[:, ax, i, j] = q[:, :lk + 1, :]
+    nfi, nfj, nfk, nfl = nc(li), nc(lj), nc(lk), nc(ll)
+    out = np.zeros(nfi * nfj * nfk * nfl)
+    ci, cj, ck, cl = cart_list(li), cart_list(lj), cart_list(lk), cart_list(ll)
+    for e in range(out.size):
+        i, r = e % nfi, e // nfi
+        k, r = r % nfk, r // nfk
+        l, j = r % nfl, r // nfl
+        v = np.ones(nT)
+        for ax in range(3):
+            v = v * g4[:, ax, ci[i][ax], cj[j][ax], ck[k][ax], cl[l][ax]]
+        out[e] = v.sum()
+    return out
+
+
+CLASSES = [(0, 0, 0, 0), (1, 0, 0, 0), (1, 1, 0, 0), (1, 1, 1, 1), (2, 1, 1, 0), (2, 2, 2, 1),
+           (3, 2, 2, 1), (3, 3, 2, 2), (3, 1, 3, 0), (4, 2, 3, 3), (5, 4, 1, 0), (4, 4, 4, 4)]
+
+
+@pytest.mark.parametrize('cls', CLASSES)
+def test_e0f0_tables_replay(cls):
+    li, lj, lk, ll = cls
+    c, groups, perm = tables(*cls)
+    na, nm = li + lj + 1, lk + ll + 1
+    nE, nF = c['nE'], c['nF']
+    assert nE == below(li + lj + 1) - below(li) and nF == below(lk + ll + 1) - below(lk)
+    assert c['ngroup'] == nc(li + lj) * nc(lk + ll)
+    assert c['maxab'] == (lj + 1) | ((ll + 1) << 8)
+    if c['ngroup'] <= 32:
+        s = c['split']
+        assert s >= 1 and s & (s - 1) == 0 and s * c['ngroup'] <= 32 < 2 * s * c['ngroup']
+    else:
+        assert c['split'] == 0
+    # every accumulator is covered by exactly one (group, member)
+    hit = np.zeros(nE * nF, int)
+    sizes = []
+    for oxy, oz, acc, mn in groups:
+        nez, nfz = mn & 0xff, mn >> 8
+        assert 1 <= nez <= lj + 1 and 1 <= nfz <= ll + 1
+        sizes.append(nez * nfz)
+        for a in range(nez):
+            for b in range(nfz):
+                hit[acc + a * nF + b] += 1
+    assert (hit == 1).all()
+    assert sizes == sorted(sizes, reverse=True)
+    assert sorted(perm[:nE]) == list(range(nE)) and sorted(perm[nE:]) == list(range(nF))
+    rng = np.random.RandomState(sum(cls))
+    nT = 5
+    g = rng.normal(size=(nT, 3, nm, na))
+    AB, CD = rng.normal(size=3), rng.normal(size=3)
+    acc = np.zeros(nE * nF)
+    for oxy, oz, a0, mn in groups:
+        ox, oy = oxy & 0xffff, oxy >> 16
+        nez, nfz = mn & 0xff, mn >> 8
+        gx, gy, gz = (g[:, ax].reshape(nT, -1) for ax in range(3))
+        p = gx[:, ox] * gy[:, oy]
+        for a in range(nez):
+            for b in range(nfz):
+                acc[a0 + a * nF + b] += (p * gz[:, oz + a + na * b]).sum()
+    got = hrr(acc, perm[:nE], perm[nE:], li, lj, lk, ll, AB, CD, c['hrr_need'])
+    ref = direct(g, li, lj, lk, ll, AB, CD)
+    np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-11 * np.abs(ref).max())
