@@ -161,10 +161,15 @@ class Plan:
 
 def batch_host(kind, mol, shls, offsets=None):
     """One-shot host-buffer evaluation: returns (ncomp, output_size) float64 numpy array."""
-    shls = np.ascontiguousarray(shls, dtype=np.int32).reshape(-1, _KIND_NSH[kind])
-    p = Plan(kind, mol, shls, offsets)
-    size, ncomp = p.output_size, p.ncomp
-    p.close()
+    shls = np.ascontiguousarray(shls, dtype=np.int32).reshape(-1, _KIND_NSH.get(kind, 4))
+    sph = kind in (INT2E_SPH, INT2E_IP1_SPH, INT3C2E_SPH)
+    ncomp = 3 if kind in (INT2E_IP1_SPH, INT2E_IP1_CART) else 1
+    per = np.array([mol.nsph(s) if sph else mol.ncart(s) for s in range(mol.nbas)], dtype=np.int64)
+    blocks = np.prod(per[shls], axis=1) if len(shls) else np.zeros(0, np.int64)
+    if offsets is None:
+        size = int(blocks.sum())
+    else:
+        size = int((np.asarray(offsets, dtype=np.int64) + blocks).max(initial=0))
     out = np.zeros(ncomp * size)
     off = None if offsets is None else np.ascontiguousarray(offsets, dtype=np.int64)
     rc = lib().cintgpu_batch_host(kind, _ptr(out), _ptr(shls), shls.shape[0], _ptr(off),

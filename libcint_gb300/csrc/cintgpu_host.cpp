@@ -29,8 +29,11 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -1366,12 +1369,184 @@ void cintgpu_plan_destroy(CINTGPUPlan *plan)
     delete plan;
 }
 
+namespace {
+/* Per-thread buffers of the pipelined host-buffer call (two slots each, grown on demand). */
+struct BatchCtx {
+    cudaStream_t s_exec = nullptr, s_copy = nullptr;
+    cudaEvent_t ev_exec[2] = {nullptr, nullptr}, ev_d2h[2] = {nullptr, nullptr};
+    char *arena[2] = {nullptr, nullptr}, *dout[2] = {nullptr, nullptr};
+    char *pin_in[2] = {nullptr, nullptr}, *pin_out[2] = {nullptr, nullptr};
+    size_t arena_cap[2] = {0, 0}, dout_cap[2] = {0, 0}, pin_in_cap[2] = {0, 0}, pin_out_cap[2] = {0, 0};
+    ~BatchCtx()
+    {
+        /* process teardown may already have destroyed the context; ignore errors */
+        for (int s = 0; s < 2; s++) {
+            if (arena[s]) cudaFree(arena[s]);
+            if (dout[s]) cudaFree(dout[s]);
+            if (pin_in[s]) cudaFreeHost(pin_in[s]);
+            if (pin_out[s]) cudaFreeHost(pin_out[s]);
+            if (ev_exec[s]) cudaEventDestroy(ev_exec[s]);
+            if (ev_d2h[s]) cudaEventDestroy(ev_d2h[s]);
+        }
+        if (s_exec) cudaStreamDestroy(s_exec);
+        if (s_copy) cudaStreamDestroy(s_copy);
+    }
+    int init()
+    {
+        if (s_exec) return 0;
+        if (cudaStreamCreateWithFlags(&s_exec, cudaStreamNonBlocking) != cudaSuccess
+            || cudaStreamCreateWithFlags(&s_copy, cudaStreamNonBlocking) != cudaSuccess) {
+            set_error("stream creation failed");
+            return CINTGPU_ERR_CUDA;
+        }
+        for (int s = 0; s < 2; s++)
+            if (cudaEventCreateWithFlags(&ev_exec[s], cudaEventDisableTiming) != cudaSuccess
+                || cudaEventCreateWithFlags(&ev_d2h[s], cudaEventDisableTiming) != cudaSuccess) {
+                set_error("event creation failed");
+                return CINTGPU_ERR_CUDA;
+            }
+        return 0;
+    }
+};
+thread_local BatchCtx tl_batch;
+
+/* doubles of one component of item q's output block (libcint's dims for the kind) */
+int64_t item_block(int kind, const int *q, const int *bas)
+{
+    const bool three = kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART;
+    const bool sph = kind == CINTGPU_INT2E_SPH || kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT3C2E_SPH;
+    int64_t b = 1;
+    for (int a = 0; a < (three ? 3 : 4); a++) {
+        const int *s = bas + BAS_SLOTS * q[a];
+        b *= (int64_t)(sph ? nsph_l(s[ANG_OF]) : ncart_l(s[ANG_OF])) * s[NCTR_OF];
+    }
+    return b;
+}
+}  // namespace
+
+/* Host-buffer form over a packed output: the item list is cut into chunks whose plans are built
+ * by host threads while the GPU runs the chunks before them; each chunk is uploaded from pinned
+ * memory, executed and copied back on two streams, two slots in flight. */
+static int batch_host_pipelined(int kind, double *out_host, const int *shls, int64_t n,
+                                const int *atm, int natm, const int *bas, int nbas,
+                                const double *env)
+{
+    BatchCtx &X = tl_batch;
+    int rc = X.init();
+    if (rc) return rc;
+    const int nsh = (kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART) ? 3 : 4;
+    for (int64_t q = 0; q < n; q++)
+        for (int a = 0; a < nsh; a++)
+            if (shls[nsh * q + a] < 0 || shls[nsh * q + a] >= nbas) {
+                set_error("item %lld: shell %d outside 0..%d", (long long)q, shls[nsh * q + a], nbas - 1);
+                return CINTGPU_ERR_ARG;
+            }
+    const int64_t chunk_items = 4096;
+    const int C = (int)std::min<int64_t>(64, std::max<int64_t>(1, (n + chunk_items - 1) / chunk_items));
+    struct Chunk {
+        int64_t i0 = 0, n = 0, base = 0;
+        CINTGPUPlan *P = nullptr;
+        int rc = 0;
+        std::string err;
+        bool done = false;
+    };
+    std::vector<Chunk> ch(C);
+    int64_t total = 0;
+    for (int c = 0; c < C; c++) {
+        ch[c].i0 = n * c / C;
+        ch[c].n = n * (c + 1) / C - ch[c].i0;
+        ch[c].base = total;
+        for (int64_t q = ch[c].i0; q < ch[c].i0 + ch[c].n; q++) total += item_block(kind, shls + nsh * q, bas);
+    }
+    std::mutex mu;
+    std::condition_variable cv;
+    std::atomic<int> next{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    auto worker = [&]() {
+        cudaSetDevice(dev);   /* the planner queries kernel occupancy on the caller's device */
+        for (;;) {
+            int c = next.fetch_add(1);
+            if (c >= C) return;
+            CINTGPUPlan *P = new CINTGPUPlan();
+            int r = build_plan(P, kind, shls + nsh * ch[c].i0, ch[c].n, nullptr, atm, natm, bas, nbas, env, 0);
+            std::string e = r ? std::string(cintgpu_last_error()) : std::string();
+            std::lock_guard<std::mutex> lk(mu);
+            ch[c].P = P; ch[c].rc = r; ch[c].err = e; ch[c].done = true;
+            cv.notify_all();
+        }
+    };
+    const int nthreads = std::max(1, std::min<int>(C, std::min<int>(16, (int)std::thread::hardware_concurrency())));
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; t++) pool.emplace_back(worker);
+
+    int ncomp = 1;
+    auto complete = [&](int c) -> int {   /* wait for chunk c's copy, scatter it to out_host */
+        const int s = c & 1;
+        if (cudaEventSynchronize(X.ev_d2h[s]) != cudaSuccess) {
+            set_error("chunk %d: %s", c, cudaGetErrorString(cudaGetLastError()));
+            return CINTGPU_ERR_CUDA;
+        }
+        const CINTGPUPlan *P = ch[c].P;
+        for (int k = 0; k < ncomp; k++)
+            memcpy(out_host + (size_t)k * total + ch[c].base, X.pin_out[s] + sizeof(double) * k * P->out_size,
+                   sizeof(double) * P->out_size);
+        return 0;
+    };
+    for (int c = 0; c < C && !rc; c++) {
+        const int s = c & 1;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv.wait(lk, [&] { return ch[c].done; });
+        }
+        if (ch[c].rc) { set_error("%s", ch[c].err.c_str()); rc = ch[c].rc; break; }
+        CINTGPUPlan *P = ch[c].P;
+        ncomp = P->ncomp;
+        const size_t outb = sizeof(double) * std::max<int64_t>(P->out_size * P->ncomp, 1);
+        if ((rc = grow_dev(&X.arena[s], &X.arena_cap[s], plan_device_bytes(P)))
+            || (rc = grow_dev(&X.dout[s], &X.dout_cap[s], outb))
+            || (rc = grow_host(&X.pin_in[s], &X.pin_in_cap[s], plan_upload_bytes(P)))
+            || (rc = grow_host(&X.pin_out[s], &X.pin_out_cap[s], outb)))
+            break;
+        if ((rc = upload_plan(P, X.arena[s], X.arena_cap[s], X.s_exec, true, X.pin_in[s]))) break;
+        if ((rc = execute_plan(P, (double *)X.dout[s], X.s_exec))) break;
+        if (cudaEventRecord(X.ev_exec[s], X.s_exec) != cudaSuccess
+            || cudaStreamWaitEvent(X.s_copy, X.ev_exec[s], 0) != cudaSuccess
+            || cudaMemcpyAsync(X.pin_out[s], X.dout[s], outb, cudaMemcpyDeviceToHost, X.s_copy) != cudaSuccess
+            || cudaEventRecord(X.ev_d2h[s], X.s_copy) != cudaSuccess) {
+            set_error("chunk %d: %s", c, cudaGetErrorString(cudaGetLastError()));
+            rc = CINTGPU_ERR_CUDA;
+            break;
+        }
+        if (c > 0) {
+            if ((rc = complete(c - 1))) break;
+            delete ch[c - 1].P;   /* the arena is caller-owned: nothing on the device to free */
+            ch[c - 1].P = nullptr;
+        }
+        if (c == C - 1) rc = complete(c);
+    }
+    for (std::thread &t : pool) t.join();
+    cudaStreamSynchronize(X.s_exec);
+    cudaStreamSynchronize(X.s_copy);
+    for (Chunk &x : ch) delete x.P;
+    return rc;
+}
+
 int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,
                        const int64_t *offsets, const int *atm, int natm, const int *bas,
                        int nbas, const double *env)
 {
+    if (kind == CINTGPU_J_BUILD || kind == CINTGPU_J_GRAD || kind == CINTGPU_J_GRAD_EXP) {
+        set_error("cintgpu_batch_host computes integral blocks; J and its gradient need a density "
+                  "(cintgpu_plan_execute_j / cintgpu_plan_execute_grad)");
+        return CINTGPU_ERR_ARG;
+    }
+    if (n <= 0) return 0;
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (!offsets) return batch_host_pipelined(kind, out_host, shls, n, atm, natm, bas, nbas, env);
     CINTGPUPlan *P = nullptr;
-    int rc = cintgpu_plan_create(&P, kind, shls, n, offsets, atm, natm, bas, nbas, env);
+    rc = cintgpu_plan_create(&P, kind, shls, n, offsets, atm, natm, bas, nbas, env);
     if (rc) return rc;
     size_t outb = sizeof(double) * P->out_size * P->ncomp;
     double *dout = nullptr;
