@@ -1424,8 +1424,8 @@ int64_t item_block(int kind, const int *q, const int *bas)
 }
 }  // namespace
 
-/* Host-buffer form over a packed output: the item list is cut into chunks whose plans are built
- * by host threads while the GPU runs the chunks before them; each chunk is uploaded from pinned
+/* Host-buffer form over a packed output: the item list is cut into chunks (growing from 2048 to
+ * 16384 items) whose plans are built by host threads while the GPU runs the chunks before them; each chunk is uploaded from pinned
  * memory, executed and copied back on two streams, two slots in flight. */
 static int batch_host_pipelined(int kind, double *out_host, const int *shls, int64_t n,
                                 const int *atm, int natm, const int *bas, int nbas,
@@ -1441,8 +1441,6 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
                 set_error("item %lld: shell %d outside 0..%d", (long long)q, shls[nsh * q + a], nbas - 1);
                 return CINTGPU_ERR_ARG;
             }
-    const int64_t chunk_items = 4096;
-    const int C = (int)std::min<int64_t>(64, std::max<int64_t>(1, (n + chunk_items - 1) / chunk_items));
     struct Chunk {
         int64_t i0 = 0, n = 0, base = 0;
         CINTGPUPlan *P = nullptr;
@@ -1450,14 +1448,19 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
         std::string err;
         bool done = false;
     };
-    std::vector<Chunk> ch(C);
+    /* chunk sizes 2048, 4096, ... up to 16384 items: the GPU starts after one small plan, later
+     * chunks are large enough that their kernels' tails stay short */
+    std::vector<Chunk> ch;
     int64_t total = 0;
-    for (int c = 0; c < C; c++) {
-        ch[c].i0 = n * c / C;
-        ch[c].n = n * (c + 1) / C - ch[c].i0;
-        ch[c].base = total;
-        for (int64_t q = ch[c].i0; q < ch[c].i0 + ch[c].n; q++) total += item_block(kind, shls + nsh * q, bas);
+    for (int64_t i0 = 0, len = 2048; i0 < n; i0 += len, len = std::min<int64_t>(2 * len, 16384)) {
+        Chunk x;
+        x.i0 = i0;
+        x.n = std::min(len, n - i0);
+        x.base = total;
+        for (int64_t q = x.i0; q < x.i0 + x.n; q++) total += item_block(kind, shls + nsh * q, bas);
+        ch.push_back(x);
     }
+    const int C = (int)ch.size();
     std::mutex mu;
     std::condition_variable cv;
     std::atomic<int> next{0};
