@@ -475,9 +475,21 @@ static int build_eri_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
             e.mn = E.nz[p] | (F.nz[q] << 8);
             g.push_back(e);
         }
+    /* shapes (nez, nfz) descending, so a round of 32 groups mostly shares one shape; every group
+     * carries its round's member box (bits 16+: (MA-1) + 4 (MB-1)) for the kernel's dispatch */
     std::stable_sort(g.begin(), g.end(), [](const CGEriGroup &a, const CGEriGroup &b) {
-        return (a.mn & 0xff) * (a.mn >> 8) > (b.mn & 0xff) * (b.mn >> 8);
+        if ((a.mn & 0xff) != (b.mn & 0xff)) return (a.mn & 0xff) > (b.mn & 0xff);
+        return (a.mn >> 8) > (b.mn >> 8);
     });
+    for (size_t r0 = 0; r0 < g.size(); r0 += 32) {
+        int ma = 1, mb = 1;
+        for (size_t k = r0; k < std::min(g.size(), r0 + 32); k++) {
+            ma = std::max(ma, g[k].mn & 0xff);
+            mb = std::max(mb, g[k].mn >> 8);
+        }
+        const int box = (ma <= 4 && mb <= 4) ? (ma - 1) + 4 * (mb - 1) : 0xff;
+        for (size_t k = r0; k < std::min(g.size(), r0 + 32); k++) g[k].mn |= box << 16;
+    }
     P->egroup.insert(P->egroup.end(), g.begin(), g.end());
     c.ngroup = (int)g.size();
     c.split = 0;

@@ -73,7 +73,7 @@ typedef struct { int ob_oc; int c; } CGGradEnt;                          /* ob |
  * eperm/fperm map the transfer's Cartesian order (shells ascending, libcint order within a shell)
  * to those rows/columns. */
 typedef struct {
-    int group_off, ngroup;   /* CGEriGroup range, sorted by member count (largest first) */
+    int group_off, ngroup;   /* CGEriGroup range, sorted by shape (nez, nfz), largest first */
     int perm_off;            /* eperm[nE] then fperm[nF] */
     int nE, nF;
     int split;               /* ngroup <= 32: lanes per group (power of two); 0: groups in rounds */
@@ -84,7 +84,8 @@ typedef struct {
     int oxy;             /* ox | oy << 16: offsets of (ex, fx) and (ey, fy) in the VRR arrays */
     int oz;              /* offset of (ez0, fz0) in the z array */
     int acc;             /* accumulator index of member (0, 0) */
-    int mn;              /* nez | nfz << 8 */
+    int mn;              /* nez | nfz << 8 | box << 16: box = (MA-1) + 4 (MB-1), the largest
+                            nez (MA) and nfz (MB) among the 32 groups of this group's round */
 } CGEriGroup;
 
 typedef struct {

@@ -198,7 +198,7 @@ __device__ __forceinline__ void e0f0_terms(const double *__restrict__ greg, int 
                                            int oz, int mn, double (&r)[16])
 {
     const int ox = oxy & 0xffff, oy = oxy >> 16;
-    const int nez = mn & 0xff, nfz = mn >> 8;
+    const int nez = mn & 0xff, nfz = (mn >> 8) & 0xff;
     for (int t = t_begin; t < Tb; t += tstep) {
         const double *g = greg + (size_t)t * gstride;
         const double p = g[ox] * g[G + oy];
@@ -296,16 +296,19 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
         if (S > 0) {
             if (own) e0f0_dispatch(mab, greg, gstride, G, na, sp, Tb, S, mine.oxy, mine.oz, mine.mn, r);
         } else if (boxed) {
-            for (int gi = lane; gi < ec.ngroup; gi += 32) {
+            /* rounds of 32 groups, each dispatched on its own member box (warp-uniform) */
+            for (int r0 = 0; r0 < ec.ngroup; r0 += 32) {
+                const int gi = r0 + lane;
+                if (gi >= ec.ngroup) break;
                 const CGEriGroup q = grp[gi];
-                const int nez = q.mn & 0xff, nfz = q.mn >> 8;
+                const int nez = q.mn & 0xff, nfz = (q.mn >> 8) & 0xff;
                 double v[16];
 #pragma unroll
                 for (int b = 0; b < 4; b++)
 #pragma unroll
                     for (int a = 0; a < 4; a++)
                         v[b * 4 + a] = (a < nez && b < nfz) ? acc[q.acc + a * nF + b] : 0.0;
-                e0f0_dispatch(mab, greg, gstride, G, na, 0, Tb, 1, q.oxy, q.oz, q.mn, v);
+                e0f0_dispatch(q.mn >> 16, greg, gstride, G, na, 0, Tb, 1, q.oxy, q.oz, q.mn, v);
 #pragma unroll
                 for (int b = 0; b < 4; b++)
 #pragma unroll
@@ -317,7 +320,7 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
             for (int gi = lane; gi < ec.ngroup; gi += 32) {
                 const CGEriGroup q = grp[gi];
                 const int ox = q.oxy & 0xffff, oy = q.oxy >> 16;
-                const int nez = q.mn & 0xff, nfz = q.mn >> 8;
+                const int nez = q.mn & 0xff, nfz = (q.mn >> 8) & 0xff;
                 for (int b = 0; b < nfz; b++)
                     for (int a = 0; a < nez; a++) {
                         double s0 = acc[q.acc + a * nF + b];
@@ -337,7 +340,7 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
             for (int m = 0; m < 16; m++) r[m] += __shfl_down_sync(FULL, r[m], off * ec.ngroup);
         }
         if (own && sp == 0) {
-            const int nez = mine.mn & 0xff, nfz = mine.mn >> 8;
+            const int nez = mine.mn & 0xff, nfz = (mine.mn >> 8) & 0xff;
 #pragma unroll
             for (int b = 0; b < 4; b++)
 #pragma unroll

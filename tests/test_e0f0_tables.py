@@ -4,7 +4,6 @@ way the kernel uses them, give the same Cartesian block as the per-term horizont
 (libcint's order of operations, src/g2e.c:560-693 then src/cint2e.c:961-1183) on random VRR
 arrays."""
 import ctypes
-import itertools
 
 import numpy as np
 import pytest
@@ -156,16 +155,22 @@ def test_e0f0_tables_replay(cls):
         assert c['split'] == 0
     # every accumulator is covered by exactly one (group, member)
     hit = np.zeros(nE * nF, int)
-    sizes = []
+    shapes = []
     for oxy, oz, acc, mn in groups:
-        nez, nfz = mn & 0xff, mn >> 8
+        nez, nfz = mn & 0xff, (mn >> 8) & 0xff
         assert 1 <= nez <= lj + 1 and 1 <= nfz <= ll + 1
-        sizes.append(nez * nfz)
+        shapes.append((nez, nfz))
         for a in range(nez):
             for b in range(nfz):
                 hit[acc + a * nF + b] += 1
     assert (hit == 1).all()
-    assert sizes == sorted(sizes, reverse=True)
+    assert shapes == sorted(shapes, reverse=True)
+    # each round of 32 groups carries the box of its largest nez and nfz
+    for r0 in range(0, len(groups), 32):
+        rnd = shapes[r0:r0 + 32]
+        ma, mb = max(x[0] for x in rnd), max(x[1] for x in rnd)
+        box = (ma - 1) + 4 * (mb - 1) if ma <= 4 and mb <= 4 else 0xff
+        assert all((g[3] >> 16) == box for g in groups[r0:r0 + 32])
     assert sorted(perm[:nE]) == list(range(nE)) and sorted(perm[nE:]) == list(range(nF))
     rng = np.random.RandomState(sum(cls))
     nT = 5
@@ -174,7 +179,7 @@ def test_e0f0_tables_replay(cls):
     acc = np.zeros(nE * nF)
     for oxy, oz, a0, mn in groups:
         ox, oy = oxy & 0xffff, oxy >> 16
-        nez, nfz = mn & 0xff, mn >> 8
+        nez, nfz = mn & 0xff, (mn >> 8) & 0xff
         gx, gy, gz = (g[:, ax].reshape(nT, -1) for ax in range(3))
         p = gx[:, ox] * gy[:, oy]
         for a in range(nez):
