@@ -12,8 +12,9 @@ does not fit a bench step.  GPU and CPU legs evaluate the same list.  Metric: sp
              stream, L2 flushed (256 MiB memset) before every step outside the events.
   e2e        the one-shot host-buffer C-ABI call cintgpu_batch_host (host planning, H2D, kernels,
              D2H of every integral) per step, wall clock.
-  roofline   the Rys kernels are FP64-issue bound: achieved = algorithmic FP64 flops of the step
-             (model of cintgpu_plan_flops) / step time, against the measured DFMA peak.
+  roofline   the Rys kernels are FP64-issue bound: achieved = algorithmic FP64 flops of a launch
+             (model of cintgpu_plan_flops) / the integral kernel's own duration (CUDA events the
+             plan records around it on the launching stream), against the measured DFMA peak.
   cpu_baseline  the C restatement (oracle/, "port") with OpenMP on all host cores over a bounded
              sample of the same quartet list.
 
@@ -39,6 +40,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FP64_PEAK_TFLOPS = 1.196      # measured DFMA peak of this GB300 pool, profiles/fp64_peak_gb300.md
+# DRAM read + write of one rys_eri_kernel launch per c1 quartet: 251.6 MB over the first 20k
+# quartets of the committed list (ncu capture, profiles/rys_eri_kernel_c1.md), scaled by quartets
+ERI_DRAM_BYTES_PER_QUARTET = 251.6e6 / 20000
 SCHWARZ = 1e-12
 L2_FLUSH_BYTES = 256 << 20
 
@@ -304,6 +308,7 @@ def run_gpu(args, rank, world):
                        if os.path.isdir(os.path.join(ROOT, 'gpurun_out')) else
                        os.path.join(tempfile.gettempdir(), 'cintgpu_clocks.csv'))
     evs = []
+    kernel_ms = []
     with clk:
         time.sleep(0.3)
         torch.cuda.synchronize()
@@ -316,6 +321,9 @@ def run_gpu(args, rank, world):
             plan.execute(out, stream)
             e1.record(stream)
             evs.append((e0, e1))
+            # the integral kernel alone (events the plan records on the same stream); waits for
+            # this step, outside the step's own events
+            kernel_ms.append(plan.compute_ms())
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     step_ms = [a.elapsed_time(b) for a, b in evs]
@@ -343,7 +351,8 @@ def run_gpu(args, rank, world):
     if rank != 0:
         return
     value = nint * world * args.steps / tot_s
-    achieved = plan.flops * args.steps / tot_s / 1e12
+    kern_s = sum(kernel_ms) / 1e3
+    achieved = plan.flops * args.steps / kern_s / 1e12
     clocks = clk.summary(dev)
     line = {
         'metric': 'int2e_sph integrals/s (c1 Schwarz-screened quartets, batched plan)',
@@ -357,9 +366,13 @@ def run_gpu(args, rank, world):
                    'wall_s_timed_region': wall},
         'quartets_per_s': len(qs) * world * args.steps / tot_s,
         'gpu_launches': plan.launches * args.steps,
-        'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': FP64_PEAK_TFLOPS,
+        'roofline': {'bound': 'fp64', 'kernel': 'rys_eri_kernel',
+                     'kernel_ms_per_launch': 1e3 * kern_s / args.steps,
+                     'achieved': achieved, 'peak': FP64_PEAK_TFLOPS,
                      'unit': 'TFLOP/s', 'frac': achieved / FP64_PEAK_TFLOPS,
-                     'traffic': None,
+                     'traffic': ERI_DRAM_BYTES_PER_QUARTET * len(qs),
+                     'traffic_source': 'ncu dram__bytes_read+write of a 20k-quartet launch, '
+                                       'scaled to the step (profiles/rys_eri_kernel_c1.md)',
                      'peak_source': 'measured DFMA peak (profiles/fp64_peak_gb300.md); '
                                     'MEASURED_PEAKS.json carries no FP64 figure'},
         'e2e': {'value': nint / statistics.median(e2e_times) if e2e_times else None,

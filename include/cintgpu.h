@@ -161,6 +161,10 @@ int cintgpu_plan_execute(CINTGPUPlan *plan, double *out_dev, void *stream);
 int64_t cintgpu_plan_upload_bytes(const CINTGPUPlan *plan);
 /* number of kernel launches one execution enqueues */
 int cintgpu_plan_launches(const CINTGPUPlan *plan);
+/* milliseconds between the start of the last execution's integral kernels and their end (the
+ * output transform excluded), from CUDA events recorded on the execution's stream; synchronises
+ * with that point; -1 before the first execution.  No libcint counterpart (measurement aid). */
+float cintgpu_plan_compute_ms(const CINTGPUPlan *plan);
 /* device-side error flags of the last execution (synchronises): 0 = fine, bit0 = a task's class
  * did not fit the kernel's shared-memory layout (its contribution is missing) */
 int cintgpu_plan_status(const CINTGPUPlan *plan);

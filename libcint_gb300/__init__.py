@@ -65,6 +65,8 @@ def lib():
     L.cintgpu_plan_upload_bytes.restype = i64
     L.cintgpu_plan_launches.argtypes = [vp]
     L.cintgpu_plan_launches.restype = i32
+    L.cintgpu_plan_compute_ms.argtypes = [vp]
+    L.cintgpu_plan_compute_ms.restype = ctypes.c_float
     L.cintgpu_plan_execute.argtypes = [vp, vp, vp]
     L.cintgpu_plan_execute.restype = i32
     L.cintgpu_plan_nonempty.argtypes = [vp, vp]
@@ -146,6 +148,11 @@ class Plan:
         flags = np.zeros(self.n, dtype=np.int32)
         _check(lib().cintgpu_plan_nonempty(self._h, _ptr(flags)), 'cintgpu_plan_nonempty')
         return flags
+
+    def compute_ms(self):
+        """Device time of the last execution's integral kernels (output transform excluded),
+        from CUDA events on its stream; synchronises."""
+        return float(lib().cintgpu_plan_compute_ms(self._h))
 
     def close(self):
         if getattr(self, '_h', None):

@@ -29,6 +29,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <condition_variable>
 #include <mutex>
@@ -249,6 +250,7 @@ struct CINTGPUPlan {
     std::vector<CGEriClass> eclass;    /* contraction-first tables per class (ERI mode) */
     std::vector<CGEriGroup> egroup;
     std::vector<int> eperm;
+    std::vector<int> hprog;        /* horizontal-transfer programs of the classes */
     int hrr_max = 1;               /* doubles of one transfer buffer, largest class */
     int nef_max = 1;               /* (e0|f0) accumulators, largest class */
     std::vector<int> out_item;     /* item index of each CGOutTask */
@@ -269,6 +271,7 @@ struct CINTGPUPlan {
     CGEriClass *d_eclass = nullptr;
     CGEriGroup *d_egroup = nullptr;
     int *d_eperm = nullptr;
+    int *d_hprog = nullptr;
     double *d_gctr = nullptr;
     int *d_counters = nullptr;     /* [0], [1]: task counters of the groups; [2]: status */
     int *d_nonempty = nullptr;
@@ -283,6 +286,8 @@ struct CINTGPUPlan {
     int wscratch_warps = 0;
     cudaStream_t side = nullptr;   /* second stream for the large-class group */
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;   /* around the compute kernels (timing) */
+    bool timed = false;            /* ev_t0/ev_t1 recorded at least once */
 };
 
 namespace {
@@ -517,6 +522,58 @@ static int build_eri_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
         need = std::max(need, ncart_l(li) * ncart_l(lj) * (below(lk + ll - d + 1) - below(lk)) * ncart_l(d));
     c.hrr_need = need;
     c.maxab = (lj + 1) | ((ll + 1) << 8);
+    /* transfer program: per bra level b = 1..lj, nrows then (hi, lo, axis) per row (e, jb):
+     * row = e_hi(e + 1_ax, jb - 1_ax), lo = (e, jb - 1_ax), ax = lowest non-zero axis of jb;
+     * per ket level d = 1..ll, nent, in_stride, out_stride, then (hi, lo, axis) per (f, ld) */
+    c.hprog_off = (int)P->hprog.size();
+    c.pad0 = c.pad1 = c.pad2 = 0;
+    auto cidx = [](int l, int x, int y) { int r = l - x; return r * (r + 1) / 2 + (r - y); };
+    auto comps = [](int l) {
+        std::vector<std::array<int, 3>> v;
+        for (int x = l; x >= 0; x--)
+            for (int y = l - x; y >= 0; y--) v.push_back({x, y, l - x - y});
+        return v;
+    };
+    for (int b = 1; b <= lj; b++) {
+        const int ncb1 = ncart_l(b - 1);
+        const auto jb_list = comps(b);
+        int nrows = (below(li + lj - b + 1) - below(li)) * ncart_l(b);
+        P->hprog.push_back(nrows);
+        for (int el = li; el <= li + lj - b; el++)
+            for (const auto &e : comps(el))
+                for (const auto &j : jb_list) {
+                    const int ax = j[0] > 0 ? 0 : (j[1] > 0 ? 1 : 2);
+                    const int dx = ax == 0, dy = ax == 1;
+                    const int jp = cidx(b - 1, j[0] - dx, j[1] - dy);
+                    const int ei = below(el) - below(li) + cidx(el, e[0], e[1]);
+                    const int eu = below(el + 1) - below(li) + cidx(el + 1, e[0] + dx, e[1] + dy);
+                    P->hprog.push_back(eu * ncb1 + jp);
+                    P->hprog.push_back(ei * ncb1 + jp);
+                    P->hprog.push_back(ax);
+                }
+    }
+    int nFprev = c.nF;
+    for (int d = 1; d <= ll; d++) {
+        const int ncd = ncart_l(d), ncd1 = ncart_l(d - 1);
+        const int nFp = below(lk + ll - d + 1) - below(lk);
+        P->hprog.push_back(nFp * ncd);
+        P->hprog.push_back(nFprev * ncd1);
+        P->hprog.push_back(nFp * ncd);
+        const auto ld_list = comps(d);
+        for (int fl = lk; fl <= lk + ll - d; fl++)
+            for (const auto &f : comps(fl))
+                for (const auto &l : ld_list) {
+                    const int ax = l[0] > 0 ? 0 : (l[1] > 0 ? 1 : 2);
+                    const int dx = ax == 0, dy = ax == 1;
+                    const int lp = cidx(d - 1, l[0] - dx, l[1] - dy);
+                    const int fi = below(fl) - below(lk) + cidx(fl, f[0], f[1]);
+                    const int fu = below(fl + 1) - below(lk) + cidx(fl + 1, f[0] + dx, f[1] + dy);
+                    P->hprog.push_back(fu * ncd1 + lp);
+                    P->hprog.push_back(fi * ncd1 + lp);
+                    P->hprog.push_back(ax);
+                }
+        nFprev = nFp;
+    }
     P->hrr_max = std::max(P->hrr_max, need);
     P->nef_max = std::max(P->nef_max, c.nE * c.nF);
     P->eclass.push_back(c);
@@ -594,6 +651,9 @@ static void free_plan_device(CINTGPUPlan *p)
     p->dbuf = nullptr;
     if (p->ev_fork) cudaEventDestroy(p->ev_fork);
     if (p->ev_join) cudaEventDestroy(p->ev_join);
+    if (p->ev_t0) cudaEventDestroy(p->ev_t0);
+    if (p->ev_t1) cudaEventDestroy(p->ev_t1);
+    p->ev_t0 = p->ev_t1 = nullptr;
     if (p->side) cudaStreamDestroy(p->side);
     p->ev_fork = p->ev_join = nullptr;
     p->side = nullptr;
@@ -851,7 +911,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
 }
 
 struct DevLayout {
-    size_t pairs, prims, tasks, outs, pq, gcl, gch, gen, ecl, egr, epm, gctr, cnt, ne, scr, wscr;
+    size_t pairs, prims, tasks, outs, pq, gcl, gch, gen, ecl, egr, epm, hpg, gctr, cnt, ne, scr, wscr;
     int64_t wstride;
     int wwarps;
     size_t upload, total;
@@ -877,6 +937,7 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     D.ecl = al(sizeof(CGEriClass) * std::max<size_t>(P->eclass.size(), 1));
     D.egr = al(sizeof(CGEriGroup) * std::max<size_t>(P->egroup.size(), 1));
     D.epm = al(sizeof(int) * std::max<size_t>(P->eperm.size(), 1));
+    D.hpg = al(sizeof(int) * std::max<size_t>(P->hprog.size(), 1));
     D.gctr = al(sizeof(double) * P->gctr_size);
     D.cnt = al(sizeof(int) * 4);
     D.ne = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
@@ -891,7 +952,7 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
         D.wscr = al(sizeof(double) * (size_t)D.wwarps * D.wstride);
     }
     if (P->jmode || grad) D.gctr = al(sizeof(double));   /* no per-task accumulators */
-    D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq + D.gcl + D.gch + D.gen + D.ecl + D.egr + D.epm;
+    D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq + D.gcl + D.gch + D.gen + D.ecl + D.egr + D.epm + D.hpg;
     D.total = D.upload + D.gctr + D.cnt + D.ne + D.scr + D.wscr;
     return D;
 }
@@ -915,6 +976,7 @@ static void carve_plan(CINTGPUPlan *P, const DevLayout &D, char *p)
     P->d_eclass = (CGEriClass *)p; p += D.ecl;
     P->d_egroup = (CGEriGroup *)p; p += D.egr;
     P->d_eperm = (int *)p; p += D.epm;
+    P->d_hprog = (int *)p; p += D.hpg;
     P->d_gctr = (double *)p; p += D.gctr;
     P->d_counters = (int *)p; p += D.cnt;
     P->d_nonempty = (int *)p; p += D.ne;
@@ -937,7 +999,8 @@ static void fill_image(const CINTGPUPlan *P, const DevLayout &D, char *q)
     memcpy(q, P->gent.data(), sizeof(CGGradEnt) * P->gent.size()); q += D.gen;
     memcpy(q, P->eclass.data(), sizeof(CGEriClass) * P->eclass.size()); q += D.ecl;
     memcpy(q, P->egroup.data(), sizeof(CGEriGroup) * P->egroup.size()); q += D.egr;
-    memcpy(q, P->eperm.data(), sizeof(int) * P->eperm.size());
+    memcpy(q, P->eperm.data(), sizeof(int) * P->eperm.size()); q += D.epm;
+    memcpy(q, P->hprog.data(), sizeof(int) * P->hprog.size());
 }
 
 /* Place the plan in device memory (a caller arena or its own allocation) and copy the host
@@ -1037,6 +1100,7 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.eclass = P->d_eclass;
     L.egroup = P->d_egroup;
     L.eperm = P->d_eperm;
+    L.hprog = P->d_hprog;
     L.hrr_off1 = P->nef_max;
     L.hrr_off2 = (int64_t)P->nef_max + P->hrr_max;
     int nblocks = std::min(g_ctx.sm_count * G.blocks_per_sm, std::max(1, (G.ntasks + 3) / 4));
@@ -1052,6 +1116,7 @@ static int execute_plan(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
     CUDA_OK(cudaMemsetAsync(P->d_nonempty, 0, sizeof(int) * std::max<size_t>(P->outs.size(), 1), stream));
     CUDA_OK(cudaMemsetAsync(P->d_counters, 0, sizeof(int) * 4, stream));
     bool fork = P->side && P->groups[1].ntasks > 0 && P->groups[0].ntasks > 0;
+    if (P->ev_t0) CUDA_OK(cudaEventRecord(P->ev_t0, stream));
     if (fork) {
         CUDA_OK(cudaEventRecord(P->ev_fork, stream));
         CUDA_OK(cudaStreamWaitEvent(P->side, P->ev_fork, 0));
@@ -1066,9 +1131,13 @@ static int execute_plan(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
         if (!rc) rc = launch_group(P, 0, stream);
         if (rc) return rc;
     }
+    if (P->ev_t1) {
+        CUDA_OK(cudaEventRecord(P->ev_t1, stream));
+        P->timed = true;
+    }
     if (P->jmode || P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) return 0;
     int rc = cg_launch_output(P->d_outs, (int)P->outs.size(), P->d_gctr, P->d_nonempty, P->d_scratch,
-                              P->scratch_per_warp, P->max_nf, P->d_eclass, P->d_eperm, P->out_blocks,
+                              P->scratch_per_warp, P->max_nf, P->d_eclass, P->d_eperm, P->d_hprog, P->out_blocks,
                               out_dev, P->ncomp, P->out_size, stream);
     if (rc) { set_error("output kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
     return 0;
@@ -1274,7 +1343,8 @@ int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n
     if (!rc) rc = upload_plan(P, nullptr, 0, 0, false, nullptr);
     if (!rc && (cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking) != cudaSuccess
                 || cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming) != cudaSuccess
-                || cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming) != cudaSuccess)) {
+                || cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming) != cudaSuccess
+                || cudaEventCreate(&P->ev_t0) != cudaSuccess || cudaEventCreate(&P->ev_t1) != cudaSuccess)) {
         set_error("stream/event creation failed");
         rc = CINTGPU_ERR_CUDA;
     }
@@ -1299,6 +1369,18 @@ int cintgpu_plan_execute(CINTGPUPlan *plan, double *out_dev, void *stream)
 }
 
 int cintgpu_plan_nao_cart(const CINTGPUPlan *plan) { return plan->nao_cart; }
+
+float cintgpu_plan_compute_ms(const CINTGPUPlan *plan)
+{
+    if (!plan || !plan->timed) return -1.0f;
+    float ms = -1.0f;
+    if (cudaEventSynchronize(plan->ev_t1) != cudaSuccess
+        || cudaEventElapsedTime(&ms, plan->ev_t0, plan->ev_t1) != cudaSuccess) {
+        set_error("compute timing unavailable: %s", cudaGetErrorString(cudaGetLastError()));
+        return -1.0f;
+    }
+    return ms;
+}
 
 int cintgpu_plan_status(const CINTGPUPlan *plan)
 {
@@ -1384,7 +1466,7 @@ void cintgpu_plan_destroy(CINTGPUPlan *plan)
 namespace {
 /* Per-thread buffers of the pipelined host-buffer call (two slots each, grown on demand). */
 struct BatchCtx {
-    cudaStream_t s_exec = nullptr, s_copy = nullptr;
+    cudaStream_t s_exec[2] = {nullptr, nullptr}, s_copy = nullptr;
     cudaEvent_t ev_exec[2] = {nullptr, nullptr}, ev_d2h[2] = {nullptr, nullptr};
     char *arena[2] = {nullptr, nullptr}, *dout[2] = {nullptr, nullptr};
     char *pin_in[2] = {nullptr, nullptr}, *pin_out[2] = {nullptr, nullptr};
@@ -1400,13 +1482,15 @@ struct BatchCtx {
             if (ev_exec[s]) cudaEventDestroy(ev_exec[s]);
             if (ev_d2h[s]) cudaEventDestroy(ev_d2h[s]);
         }
-        if (s_exec) cudaStreamDestroy(s_exec);
+        for (int s = 0; s < 2; s++)
+            if (s_exec[s]) cudaStreamDestroy(s_exec[s]);
         if (s_copy) cudaStreamDestroy(s_copy);
     }
     int init()
     {
-        if (s_exec) return 0;
-        if (cudaStreamCreateWithFlags(&s_exec, cudaStreamNonBlocking) != cudaSuccess
+        if (s_copy) return 0;
+        if (cudaStreamCreateWithFlags(&s_exec[0], cudaStreamNonBlocking) != cudaSuccess
+            || cudaStreamCreateWithFlags(&s_exec[1], cudaStreamNonBlocking) != cudaSuccess
             || cudaStreamCreateWithFlags(&s_copy, cudaStreamNonBlocking) != cudaSuccess) {
             set_error("stream creation failed");
             return CINTGPU_ERR_CUDA;
@@ -1436,9 +1520,10 @@ int64_t item_block(int kind, const int *q, const int *bas)
 }
 }  // namespace
 
-/* Host-buffer form over a packed output: the item list is cut into chunks (growing from 2048 to
- * 16384 items) whose plans are built by host threads while the GPU runs the chunks before them; each chunk is uploaded from pinned
- * memory, executed and copied back on two streams, two slots in flight. */
+/* Host-buffer form over a packed output: the item list is cut into chunks (2048 items, then
+ * 4096) whose plans are built by host threads while the GPU runs the chunks before them; each
+ * chunk is uploaded from pinned memory and executed on its slot's stream (two slots, so one
+ * chunk's kernel tail overlaps the next chunk's start) and copied back on a third stream. */
 static int batch_host_pipelined(int kind, double *out_host, const int *shls, int64_t n,
                                 const int *atm, int natm, const int *bas, int nbas,
                                 const double *env)
@@ -1460,11 +1545,11 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
         std::string err;
         bool done = false;
     };
-    /* chunk sizes 2048, 4096, ... up to 16384 items: the GPU starts after one small plan, later
-     * chunks are large enough that their kernels' tails stay short */
+    /* the GPU starts after one small plan; the host threads build the later chunks faster than
+     * the GPU runs them */
     std::vector<Chunk> ch;
     int64_t total = 0;
-    for (int64_t i0 = 0, len = 2048; i0 < n; i0 += len, len = std::min<int64_t>(2 * len, 16384)) {
+    for (int64_t i0 = 0, len = 2048; i0 < n; i0 += len, len = 4096) {
         Chunk x;
         x.i0 = i0;
         x.n = std::min(len, n - i0);
@@ -1523,9 +1608,9 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
             || (rc = grow_host(&X.pin_in[s], &X.pin_in_cap[s], plan_upload_bytes(P)))
             || (rc = grow_host(&X.pin_out[s], &X.pin_out_cap[s], outb)))
             break;
-        if ((rc = upload_plan(P, X.arena[s], X.arena_cap[s], X.s_exec, true, X.pin_in[s]))) break;
-        if ((rc = execute_plan(P, (double *)X.dout[s], X.s_exec))) break;
-        if (cudaEventRecord(X.ev_exec[s], X.s_exec) != cudaSuccess
+        if ((rc = upload_plan(P, X.arena[s], X.arena_cap[s], X.s_exec[s], true, X.pin_in[s]))) break;
+        if ((rc = execute_plan(P, (double *)X.dout[s], X.s_exec[s]))) break;
+        if (cudaEventRecord(X.ev_exec[s], X.s_exec[s]) != cudaSuccess
             || cudaStreamWaitEvent(X.s_copy, X.ev_exec[s], 0) != cudaSuccess
             || cudaMemcpyAsync(X.pin_out[s], X.dout[s], outb, cudaMemcpyDeviceToHost, X.s_copy) != cudaSuccess
             || cudaEventRecord(X.ev_d2h[s], X.s_copy) != cudaSuccess) {
@@ -1541,7 +1626,8 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
         if (c == C - 1) rc = complete(c);
     }
     for (std::thread &t : pool) t.join();
-    cudaStreamSynchronize(X.s_exec);
+    cudaStreamSynchronize(X.s_exec[0]);
+    cudaStreamSynchronize(X.s_exec[1]);
     cudaStreamSynchronize(X.s_copy);
     for (Chunk &x : ch) delete x.P;
     return rc;
@@ -1667,18 +1753,20 @@ int cg_init(void) { return ensure_init(); }
 int cg_sm_count(void) { return g_ctx.sm_count; }
 void cg_set_error_msg(const char *msg) { set_error("%s", msg); }
 /* Contraction-first tables of one class, for host-side tests of the table logic:
- * info[8] = CGEriClass fields, groups[4 * ngroup], perm[nE + nF]. */
+ * info[12] = CGEriClass fields, groups[4 * ngroup], perm[nE + nF], prog (the transfer program);
+ * returns the program length or -1 when a buffer is too small. */
 extern "C" int cg_eri_tables(int li, int lj, int lk, int ll, int *info, int *groups, int maxg,
-                             int *perm, int maxp)
+                             int *perm, int maxp, int *prog, int maxprog)
 {
     CINTGPUPlan P;
     build_eri_class(&P, li, lj, lk, ll);
     const CGEriClass &c = P.eclass[0];
-    if (c.ngroup > maxg || c.nE + c.nF > maxp) return -1;
+    if (c.ngroup > maxg || c.nE + c.nF > maxp || (int)P.hprog.size() > maxprog) return -1;
     memcpy(info, &c, sizeof(CGEriClass));
     memcpy(groups, P.egroup.data(), sizeof(CGEriGroup) * P.egroup.size());
     memcpy(perm, P.eperm.data(), sizeof(int) * P.eperm.size());
-    return 0;
+    memcpy(prog, P.hprog.data(), sizeof(int) * P.hprog.size());
+    return (int)P.hprog.size();
 }
 
 CINTGPUPlan *cg_plan_new(void) { return new CINTGPUPlan(); }

@@ -79,6 +79,8 @@ typedef struct {
     int split;               /* ngroup <= 32: lanes per group (power of two); 0: groups in rounds */
     int hrr_need;            /* doubles of each of the two transfer buffers */
     int maxab;               /* (lj + 1) | (ll + 1) << 8: member box of the class */
+    int hprog_off;           /* horizontal-transfer program (ints), see cg_hrr */
+    int pad0, pad1, pad2;
 } CGEriClass;
 typedef struct {
     int oxy;             /* ox | oy << 16: offsets of (ex, fx) and (ey, fy) in the VRR arrays */

@@ -253,90 +253,61 @@ __device__ __forceinline__ void vrr_axis(int nmax, int mmax, double b00, double 
     }
 }
 
-/* libcint Cartesian order within a shell of momentum l: index of (x, y, l-x-y) */
-__host__ __device__ __forceinline__ int cidx_l(int l, int x, int y)
-{
-    int r = l - x;
-    return r * (r + 1) / 2 + (r - y);
-}
 /* components of all shells below l: l (l+1) (l+2) / 6 */
 __host__ __device__ __forceinline__ int ncart_below(int l) { return l * (l + 1) * (l + 2) / 6; }
-
-/* index q of the range of shells l0, l0+1, ... (ascending, libcint order inside) -> shell and
- * powers */
-__device__ __forceinline__ void range_pow(int l0, int q, int &l, int &x, int &y, int &z)
-{
-    l = l0;
-    const int b = ncart_below(l0);
-    while (ncart_below(l + 1) - b <= q) l++;
-    cart_pow(l, q - (ncart_below(l) - b), x, y, z);
-}
-
 
 /* Horizontal transfer of one contracted quartet, warp-cooperative (libcint CINTg0_2e_il2d4d /
  * CINTg0_2e_lj2d4d, src/g2e.c:560-693, applied to the contracted (e0|f0) block instead of each
  * primitive's 2D integrals):
  *   (e, j+1_x | = (e+1_x, j| + AB_x (e, j|      on the bra, the lowest non-zero axis of j,
  *   |f, l+1_x)  = |f+1_x, l) + CD_x |f, l)      then on the ket.
- * src holds the accumulators in the class's group layout; the Cartesian block comes back in
- * gctr order (i + nfi (k + nfk (l + nfl j))) in h1 or h2 (the returned pointer). */
+ * src holds the accumulators in the class's group layout; prog is the class's transfer program
+ * (built on the host: per level the source rows and the axis of every target row).  The
+ * Cartesian block comes back in gctr order (i + nfi (k + nfk (l + nfl j))) in h1 or h2 (the
+ * returned pointer). */
 __device__ inline double *cg_hrr(const double *src, const int *__restrict__ eperm,
-                                 const int *__restrict__ fperm, int li, int lj, int lk, int ll,
-                                 const double *AB, const double *CD, double *h1, double *h2,
-                                 int lane)
+                                 const int *__restrict__ fperm, const int *__restrict__ prog,
+                                 int li, int lj, int lk, int ll, const double *AB, const double *CD,
+                                 double *h1, double *h2, int lane)
 {
-    const int bE = ncart_below(li), bF = ncart_below(lk);
-    const int nE = ncart_below(li + lj + 1) - bE, nF = ncart_below(lk + ll + 1) - bF;
+    const int nE = ncart_below(li + lj + 1) - ncart_below(li);
+    const int nF = ncart_below(lk + ll + 1) - ncart_below(lk);
     for (int e = lane; e < nE * nF; e += 32) {
         int ei = e / nF, fi = e - ei * nF;
         h1[e] = src[__ldg(eperm + ei) * nF + __ldg(fperm + fi)];
     }
     __syncwarp();
     double *cur = h1, *nxt = h2;
-    /* bra: level b holds [(ei nc(b) + jb) nF + f], ei over shells li .. li+lj-b */
+    const double ab0 = AB[0], ab1 = AB[1], ab2 = AB[2], cd0 = CD[0], cd1 = CD[1], cd2 = CD[2];
+    /* bra: level b holds [(ei nc(b) + jb) nF + f] */
     for (int b = 1; b <= lj; b++) {
-        const int nEp = ncart_below(li + lj - b + 1) - bE;
-        const int ncb = ncart(b), ncb1 = ncart(b - 1);
-        const int tot = nEp * ncb * nF;
-        for (int e = lane; e < tot; e += 32) {
-            int f = e % nF, r = e / nF;
-            int jb = r % ncb, ei = r / ncb;
-            int el, x, y, z, jx, jy, jz;
-            range_pow(li, ei, el, x, y, z);
-            cart_pow(b, jb, jx, jy, jz);
-            const int ax = jx > 0 ? 0 : (jy > 0 ? 1 : 2);
-            const int dx = ax == 0, dy = ax == 1;
-            const int jp = cidx_l(b - 1, jx - dx, jy - dy);
-            const int eu = ncart_below(el + 1) - bE + cidx_l(el + 1, x + dx, y + dy);
-            nxt[e] = fma(AB[ax], cur[(ei * ncb1 + jp) * nF + f], cur[(eu * ncb1 + jp) * nF + f]);
+        const int nrows = __ldg(prog);
+        const int *rows = prog + 1;
+        for (int e = lane; e < nrows * nF; e += 32) {
+            const int r = e / nF, f = e - r * nF;
+            const int hi = __ldg(rows + 3 * r), lo = __ldg(rows + 3 * r + 1), ax = __ldg(rows + 3 * r + 2);
+            const double t = ax == 0 ? ab0 : (ax == 1 ? ab1 : ab2);
+            nxt[e] = fma(t, cur[lo * nF + f], cur[hi * nF + f]);
         }
+        prog += 1 + 3 * nrows;
         __syncwarp();
         double *t = cur; cur = nxt; nxt = t;
     }
-    /* ket: level d holds [(ij nFp + fi) nc(d) + ld], fi over shells lk .. lk+ll-d */
+    /* ket: level d holds [ij out_stride + (fi nc(d) + ld)] */
     const int nfi = ncart(li), nfj = ncart(lj), nfk = ncart(lk), nfl = ncart(ll);
     const int nij = nfi * nfj;
-    int nFprev = nF;
     for (int d = 1; d <= ll; d++) {
-        const int nFp = ncart_below(lk + ll - d + 1) - bF;
-        const int ncd = ncart(d), ncd1 = ncart(d - 1);
-        const int tot = nij * nFp * ncd;
-        for (int e = lane; e < tot; e += 32) {
-            int ld = e % ncd, r = e / ncd;
-            int fi = r % nFp, ij = r / nFp;
-            int fl, x, y, z, lx, ly, lz;
-            range_pow(lk, fi, fl, x, y, z);
-            cart_pow(d, ld, lx, ly, lz);
-            const int ax = lx > 0 ? 0 : (ly > 0 ? 1 : 2);
-            const int dx = ax == 0, dy = ax == 1;
-            const int lp = cidx_l(d - 1, lx - dx, ly - dy);
-            const int fu = ncart_below(fl + 1) - bF + cidx_l(fl + 1, x + dx, y + dy);
-            nxt[e] = fma(CD[ax], cur[(ij * nFprev + fi) * ncd1 + lp],
-                         cur[(ij * nFprev + fu) * ncd1 + lp]);
+        const int nent = __ldg(prog), sin = __ldg(prog + 1), sout = __ldg(prog + 2);
+        const int *ents = prog + 3;
+        for (int e = lane; e < nij * nent; e += 32) {
+            const int ij = e / nent, q = e - ij * nent;
+            const int hi = __ldg(ents + 3 * q), lo = __ldg(ents + 3 * q + 1), ax = __ldg(ents + 3 * q + 2);
+            const double t = ax == 0 ? cd0 : (ax == 1 ? cd1 : cd2);
+            nxt[ij * sout + q] = fma(t, cur[ij * sin + lo], cur[ij * sin + hi]);
         }
+        prog += 3 + 3 * nent;
         __syncwarp();
         double *t = cur; cur = nxt; nxt = t;
-        nFprev = nFp;
     }
     /* cur[((i nfj + j) nfk + k) nfl + l] -> gctr order */
     const int nf = nij * nfk * nfl;
@@ -349,7 +320,6 @@ __device__ inline double *cg_hrr(const double *src, const int *__restrict__ eper
     __syncwarp();
     return nxt;
 }
-
 
 /* fill this translation unit's copies of the tables */
 static int cg_tu_tables_init(const int *c2s_nnz, const int *c2s_idx, const double *c2s_val)

@@ -354,8 +354,8 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
          * X[i,j] += s_kl sum_kl (ij|kl) D[k,l];  X[k,l] += s_ij sum_ij (ij|kl) D[i,j] if IJ != KL,
          * s = 2 for an off-diagonal shell pair of the unique list (D and (ij|kl) symmetric). */
         const double *cart = cg_hrr(acc, P.eperm + ec.perm_off, P.eperm + ec.perm_off + ec.nE,
-                                    li, lj, lk, ll, pij.AB, pkl.AB, wbase + P.hrr_off1,
-                                    wbase + P.hrr_off2, lane);
+                                    P.hprog + ec.hprog_off, li, lj, lk, ll, pij.AB, pkl.AB,
+                                    wbase + P.hrr_off1, wbase + P.hrr_off2, lane);
         const int nfi = ncart(li), nfj = ncart(lj), nfk = ncart(lk), nfl = ncart(ll);
         const int nao = P.nao;
         const double skl = (tk.sym & 2) ? 2.0 : 1.0, sij = (tk.sym & 1) ? 2.0 : 1.0;
@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(128)
 cg_output_kernel(const CGOutTask *__restrict__ ot, int nout, double *gctr, const int *nonempty,
                  double *scratch, int64_t scratch_per_warp, int64_t nf_max,
                  const CGEriClass *__restrict__ eclass, const int *__restrict__ eperm,
-                 double *out, int ncomp, int64_t comp_stride)
+                 const int *__restrict__ hprog, double *out, int ncomp, int64_t comp_stride)
 {
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -471,7 +471,7 @@ cg_output_kernel(const CGOutTask *__restrict__ ot, int nout, double *gctr, const
         const int nf = nfc[0] * nfc[1] * nfc[2] * nfc[3];
         const bool ne = nonempty[q] != 0;
         const bool e0f0 = (o.flags & 2) != 0;
-        const CGEriClass ec = e0f0 ? eclass[o.ecls] : CGEriClass{0, 0, 0, 0, 0, 0, 0, 0};
+        const CGEriClass ec = e0f0 ? eclass[o.ecls] : CGEriClass{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         const int slot = e0f0 ? ec.nE * ec.nF : nf;   /* accumulators per part and component */
         for (int comp = 0; comp < ncomp; comp++) {
             double *g0 = gctr + o.cart_off + (size_t)comp * slot;
@@ -498,8 +498,9 @@ cg_output_kernel(const CGOutTask *__restrict__ ot, int nout, double *gctr, const
             /* gctr order: i fastest, then k, l, j.  Pass j: inner = nfi*nfk*nfl, t = j */
             const double *cur = g0;
             if (e0f0)
-                cur = cg_hrr(g0, eperm + ec.perm_off, eperm + ec.perm_off + ec.nE, o.l[0], o.l[1],
-                             o.l[2], o.l[3], o.AB, o.CD, h1, h2, lane);
+                cur = cg_hrr(g0, eperm + ec.perm_off, eperm + ec.perm_off + ec.nE,
+                             hprog + ec.hprog_off, o.l[0], o.l[1], o.l[2], o.l[3], o.AB, o.CD,
+                             h1, h2, lane);
             c2s_pass(cur, s1, o.l[1], sph, nfc[0] * nfc[2] * nfc[3], nfc[1], 1, lane);
             __syncwarp();
             /* pass l: (i,k | l | js) */
@@ -576,12 +577,13 @@ extern "C" int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStrea
 
 extern "C" int cg_launch_output(const CGOutTask *ot, int nout, double *gctr, const int *nonempty,
                                 double *scratch, int64_t scratch_per_warp, int64_t nf_max,
-                                const CGEriClass *eclass, const int *eperm, int nblocks, double *out,
-                                int ncomp, int64_t comp_stride, cudaStream_t stream)
+                                const CGEriClass *eclass, const int *eperm, const int *hprog,
+                                int nblocks, double *out, int ncomp, int64_t comp_stride,
+                                cudaStream_t stream)
 {
     cg_output_kernel<<<nblocks, 128, 0, stream>>>(ot, nout, gctr, nonempty, scratch,
-                                                  scratch_per_warp, nf_max, eclass, eperm, out,
-                                                  ncomp, comp_stride);
+                                                  scratch_per_warp, nf_max, eclass, eperm, hprog,
+                                                  out, ncomp, comp_stride);
     return (int)cudaGetLastError();
 }
 

@@ -50,6 +50,7 @@ typedef struct {
     const CGEriClass *eclass;
     const CGEriGroup *egroup;
     const int *eperm;
+    const int *hprog;
     int64_t hrr_off1, hrr_off2;   /* J mode: transfer buffers inside the warp's slot */
 } CGLaunch;
 
@@ -91,8 +92,8 @@ int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStream_t stream)
  * (scratch_per_warp - 2 nf_max) / 2 doubles */
 int cg_launch_output(const CGOutTask *ot, int nout, double *gctr, const int *nonempty,
                      double *scratch, int64_t scratch_per_warp, int64_t nf_max,
-                     const CGEriClass *eclass, const int *eperm, int nblocks, double *out,
-                     int ncomp, int64_t comp_stride, cudaStream_t stream);
+                     const CGEriClass *eclass, const int *eperm, const int *hprog, int nblocks,
+                     double *out, int ncomp, int64_t comp_stride, cudaStream_t stream);
 int cg_grad_tu_init(const int *c2s_nnz, const int *c2s_idx, const double *c2s_val);
 int cg_launch_grad(const CGGradLaunch *P, int mode, int nblocks, cudaStream_t stream);
 int cg_grad_blocks_per_sm(int mode, int ws_doubles);

@@ -1,6 +1,6 @@
 """Host logic of the contraction-first int2e path, CPU only: the class tables built by the
-planner (stage-3 groups, accumulator permutations, transfer buffer size), replayed in numpy the
-way the kernel uses them, give the same Cartesian block as the per-term horizontal transfer
+planner (stage-3 groups, accumulator permutations, the horizontal-transfer program and its buffer
+size), replayed in numpy the way the kernels use them, give the same Cartesian block as the per-term horizontal transfer
 (libcint's order of operations, src/g2e.c:560-693 then src/cint2e.c:961-1183) on random VRR
 arrays."""
 import ctypes
@@ -24,73 +24,53 @@ def cart_list(l):
     return [(x, y, l - x - y) for x in range(l, -1, -1) for y in range(l - x, -1, -1)]
 
 
-def cidx(l, x, y):
-    r = l - x
-    return r * (r + 1) // 2 + (r - y)
-
-
-def range_pow(l0, q):
-    l = l0
-    while below(l + 1) - below(l0) <= q:
-        l += 1
-    return (l,) + cart_list(l)[q - (below(l) - below(l0))]
-
-
 def tables(li, lj, lk, ll):
     f = cg.lib().cg_eri_tables
     f.restype = ctypes.c_int
-    info = np.zeros(8, np.int32)
+    info = np.zeros(12, np.int32)
     groups = np.zeros(4 * 20000, np.int32)
     perm = np.zeros(4000, np.int32)
+    prog = np.zeros(400000, np.int32)
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
-    assert f(li, lj, lk, ll, P(info), P(groups), 20000, P(perm), 4000) == 0
-    keys = ['group_off', 'ngroup', 'perm_off', 'nE', 'nF', 'split', 'hrr_need', 'maxab']
+    nprog = f(li, lj, lk, ll, P(info), P(groups), 20000, P(perm), 4000, P(prog), prog.size)
+    assert nprog >= 0
+    keys = ['group_off', 'ngroup', 'perm_off', 'nE', 'nF', 'split', 'hrr_need', 'maxab', 'hprog_off']
     c = dict(zip(keys, info.tolist()))
-    return c, groups[:4 * c['ngroup']].reshape(-1, 4), perm[:c['nE'] + c['nF']]
+    return c, groups[:4 * c['ngroup']].reshape(-1, 4), perm[:c['nE'] + c['nF']], prog[:nprog]
 
 
-def hrr(src, eperm, fperm, li, lj, lk, ll, AB, CD, need):
-    """cg_hrr replayed: returns the Cartesian block in gctr order and the largest buffer used."""
+def hrr(src, eperm, fperm, prog, li, lj, lk, ll, AB, CD, need):
+    """cg_hrr replayed on the class's transfer program: returns the Cartesian block in gctr order
+    and checks the buffers stay within the class's hrr_need."""
     bE, bF = below(li), below(lk)
     nE, nF = below(li + lj + 1) - bE, below(lk + ll + 1) - bF
     cur = np.array([src[eperm[e] * nF + fperm[f]] for e in range(nE) for f in range(nF)])
     used = cur.size
+    p = 0
     for b in range(1, lj + 1):
-        nEp = below(li + lj - b + 1) - bE
-        ncb, ncb1 = nc(b), nc(b - 1)
-        nxt = np.zeros(nEp * ncb * nF)
-        for e in range(nxt.size):
-            f, r = e % nF, e // nF
-            jb, ei = r % ncb, r // ncb
-            el, x, y, z = range_pow(li, ei)
-            jx, jy, jz = cart_list(b)[jb]
-            ax = 0 if jx > 0 else (1 if jy > 0 else 2)
-            dx, dy = int(ax == 0), int(ax == 1)
-            jp = cidx(b - 1, jx - dx, jy - dy)
-            eu = below(el + 1) - bE + cidx(el + 1, x + dx, y + dy)
-            nxt[e] = AB[ax] * cur[(ei * ncb1 + jp) * nF + f] + cur[(eu * ncb1 + jp) * nF + f]
+        nrows = prog[p]
+        rows = prog[p + 1:p + 1 + 3 * nrows].reshape(-1, 3)
+        nxt = np.zeros(nrows * nF)
+        for r, (hi, lo, ax) in enumerate(rows):
+            assert 0 <= hi * nF and (hi + 1) * nF <= cur.size and (lo + 1) * nF <= cur.size
+            nxt[r * nF:(r + 1) * nF] = AB[ax] * cur[lo * nF:(lo + 1) * nF] + cur[hi * nF:(hi + 1) * nF]
+        p += 1 + 3 * nrows
         cur = nxt
         used = max(used, cur.size)
     nfi, nfj, nfk, nfl = nc(li), nc(lj), nc(lk), nc(ll)
     nij = nfi * nfj
-    nFprev = nF
     for d in range(1, ll + 1):
-        nFp = below(lk + ll - d + 1) - bF
-        ncd, ncd1 = nc(d), nc(d - 1)
-        nxt = np.zeros(nij * nFp * ncd)
-        for e in range(nxt.size):
-            ld, r = e % ncd, e // ncd
-            fi, ij = r % nFp, r // nFp
-            fl, x, y, z = range_pow(lk, fi)
-            lx, ly, lz = cart_list(d)[ld]
-            ax = 0 if lx > 0 else (1 if ly > 0 else 2)
-            dx, dy = int(ax == 0), int(ax == 1)
-            lp = cidx(d - 1, lx - dx, ly - dy)
-            fu = below(fl + 1) - bF + cidx(fl + 1, x + dx, y + dy)
-            nxt[e] = CD[ax] * cur[(ij * nFprev + fi) * ncd1 + lp] + cur[(ij * nFprev + fu) * ncd1 + lp]
+        nent, sin, sout = prog[p:p + 3]
+        ents = prog[p + 3:p + 3 + 3 * nent].reshape(-1, 3)
+        nxt = np.zeros(nij * sout)
+        for ij in range(nij):
+            for q, (hi, lo, ax) in enumerate(ents):
+                assert hi < sin and lo < sin
+                nxt[ij * sout + q] = CD[ax] * cur[ij * sin + lo] + cur[ij * sin + hi]
+        p += 3 + 3 * nent
         cur = nxt
-        nFprev = nFp
         used = max(used, cur.size)
+    assert p == len(prog)
     out = np.zeros(nij * nfk * nfl)
     for e in range(out.size):
         i, r = e % nfi, e // nfi
@@ -142,7 +122,7 @@ CLASSES = [(0, 0, 0, 0), (1, 0, 0, 0), (1, 1, 0, 0), (1, 1, 1, 1), (2, 1, 1, 0),
 @pytest.mark.parametrize('cls', CLASSES)
 def test_e0f0_tables_replay(cls):
     li, lj, lk, ll = cls
-    c, groups, perm = tables(*cls)
+    c, groups, perm, prog = tables(*cls)
     na, nm = li + lj + 1, lk + ll + 1
     nE, nF = c['nE'], c['nF']
     assert nE == below(li + lj + 1) - below(li) and nF == below(lk + ll + 1) - below(lk)
@@ -185,6 +165,6 @@ def test_e0f0_tables_replay(cls):
         for a in range(nez):
             for b in range(nfz):
                 acc[a0 + a * nF + b] += (p * gz[:, oz + a + na * b]).sum()
-    got = hrr(acc, perm[:nE], perm[nE:], li, lj, lk, ll, AB, CD, c['hrr_need'])
+    got = hrr(acc, perm[:nE], perm[nE:], prog, li, lj, lk, ll, AB, CD, c['hrr_need'])
     ref = direct(g, li, lj, lk, ll, AB, CD)
     np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-11 * np.abs(ref).max())
