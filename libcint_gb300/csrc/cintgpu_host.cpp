@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <array>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <mutex>
 #include <string>
@@ -1464,21 +1465,25 @@ void cintgpu_plan_destroy(CINTGPUPlan *plan)
 }
 
 namespace {
-/* Per-thread buffers of the pipelined host-buffer call (two slots each, grown on demand). */
+/* Per-thread buffers of the pipelined host-buffer call: a ring of CG_BATCH_SLOTS slots (device
+ * arena + output, pinned image + output), grown on demand and kept between calls. */
+#define CG_BATCH_SLOTS 4
 struct BatchCtx {
     cudaStream_t s_exec[2] = {nullptr, nullptr}, s_copy = nullptr;
-    cudaEvent_t ev_exec[2] = {nullptr, nullptr}, ev_d2h[2] = {nullptr, nullptr};
-    char *arena[2] = {nullptr, nullptr}, *dout[2] = {nullptr, nullptr};
-    char *pin_in[2] = {nullptr, nullptr}, *pin_out[2] = {nullptr, nullptr};
-    size_t arena_cap[2] = {0, 0}, dout_cap[2] = {0, 0}, pin_in_cap[2] = {0, 0}, pin_out_cap[2] = {0, 0};
+    cudaEvent_t ev_h2d[CG_BATCH_SLOTS] = {}, ev_exec[CG_BATCH_SLOTS] = {}, ev_d2h[CG_BATCH_SLOTS] = {};
+    char *arena[CG_BATCH_SLOTS] = {}, *dout[CG_BATCH_SLOTS] = {};
+    char *pin_in[CG_BATCH_SLOTS] = {}, *pin_out[CG_BATCH_SLOTS] = {};
+    size_t arena_cap[CG_BATCH_SLOTS] = {}, dout_cap[CG_BATCH_SLOTS] = {};
+    size_t pin_in_cap[CG_BATCH_SLOTS] = {}, pin_out_cap[CG_BATCH_SLOTS] = {};
     ~BatchCtx()
     {
         /* process teardown may already have destroyed the context; ignore errors */
-        for (int s = 0; s < 2; s++) {
+        for (int s = 0; s < CG_BATCH_SLOTS; s++) {
             if (arena[s]) cudaFree(arena[s]);
             if (dout[s]) cudaFree(dout[s]);
             if (pin_in[s]) cudaFreeHost(pin_in[s]);
             if (pin_out[s]) cudaFreeHost(pin_out[s]);
+            if (ev_h2d[s]) cudaEventDestroy(ev_h2d[s]);
             if (ev_exec[s]) cudaEventDestroy(ev_exec[s]);
             if (ev_d2h[s]) cudaEventDestroy(ev_d2h[s]);
         }
@@ -1495,8 +1500,9 @@ struct BatchCtx {
             set_error("stream creation failed");
             return CINTGPU_ERR_CUDA;
         }
-        for (int s = 0; s < 2; s++)
-            if (cudaEventCreateWithFlags(&ev_exec[s], cudaEventDisableTiming) != cudaSuccess
+        for (int s = 0; s < CG_BATCH_SLOTS; s++)
+            if (cudaEventCreateWithFlags(&ev_h2d[s], cudaEventDisableTiming) != cudaSuccess
+                || cudaEventCreateWithFlags(&ev_exec[s], cudaEventDisableTiming) != cudaSuccess
                 || cudaEventCreateWithFlags(&ev_d2h[s], cudaEventDisableTiming) != cudaSuccess) {
                 set_error("event creation failed");
                 return CINTGPU_ERR_CUDA;
@@ -1520,10 +1526,15 @@ int64_t item_block(int kind, const int *q, const int *bas)
 }
 }  // namespace
 
-/* Host-buffer form over a packed output: the item list is cut into chunks (2048 items, then
- * 4096) whose plans are built by host threads while the GPU runs the chunks before them; each
- * chunk is uploaded from pinned memory and executed on its slot's stream (two slots, so one
- * chunk's kernel tail overlaps the next chunk's start) and copied back on a third stream. */
+/* Host-buffer form over a packed output.  The item list is cut into chunks (2048 items, then
+ * 4096); chunk c uses slot c % CG_BATCH_SLOTS of a ring and execution stream c % 2.
+ *   builder threads  build chunk plans and, once the slot's previous upload has completed, write
+ *                    the plan's image into the slot's pinned buffer;
+ *   the caller       uploads each image, executes the plan and queues the copy back, never
+ *                    waiting on the GPU except for a slot whose previous chunk is not scattered;
+ *   scatter threads  wait for each chunk's copy and move it into out_host.
+ * So planning, image writing and scattering all overlap the GPU, and one chunk's kernel tail
+ * overlaps the next chunk on the other stream. */
 static int batch_host_pipelined(int kind, double *out_host, const int *shls, int64_t n,
                                 const int *atm, int natm, const int *bas, int nbas,
                                 const double *env)
@@ -1539,14 +1550,15 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
                 return CINTGPU_ERR_ARG;
             }
     struct Chunk {
-        int64_t i0 = 0, n = 0, base = 0;
+        int64_t i0 = 0, n = 0, base = 0, out_size = 0;
+        int ncomp = 1;
         CINTGPUPlan *P = nullptr;
+        DevLayout D;
         int rc = 0;
         std::string err;
-        bool done = false;
+        bool image = false, h2d = false, d2h = false, scattered = false;
     };
-    /* the GPU starts after one small plan; the host threads build the later chunks faster than
-     * the GPU runs them */
+    /* the GPU starts after one small plan; the builders outpace the GPU on the later chunks */
     std::vector<Chunk> ch;
     int64_t total = 0;
     for (int64_t i0 = 0, len = 2048; i0 < n; i0 += len, len = 4096) {
@@ -1557,79 +1569,155 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
         for (int64_t q = x.i0; q < x.i0 + x.n; q++) total += item_block(kind, shls + nsh * q, bas);
         ch.push_back(x);
     }
-    const int C = (int)ch.size();
+    const int C = (int)ch.size(), R = CG_BATCH_SLOTS;
     std::mutex mu;
     std::condition_variable cv;
-    std::atomic<int> next{0};
+    bool abort = false;
+    std::atomic<int> next_build{0}, next_scatter{0};
     int dev = 0;
     cudaGetDevice(&dev);
-    auto worker = [&]() {
+    auto fail = [&](int c, int r, const std::string &e) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!abort) { ch[c].rc = r; ch[c].err = e; }
+        abort = true;
+        cv.notify_all();
+    };
+    auto builder = [&]() {
         cudaSetDevice(dev);   /* the planner queries kernel occupancy on the caller's device */
         for (;;) {
-            int c = next.fetch_add(1);
+            const int c = next_build.fetch_add(1);
             if (c >= C) return;
             CINTGPUPlan *P = new CINTGPUPlan();
             int r = build_plan(P, kind, shls + nsh * ch[c].i0, ch[c].n, nullptr, atm, natm, bas, nbas, env, 0);
-            std::string e = r ? std::string(cintgpu_last_error()) : std::string();
+            if (r) { fail(c, r, cintgpu_last_error()); delete P; return; }
+            const int slot = c % R;
+            if (c >= R) {   /* the slot's image buffer is free once chunk c - R is uploaded */
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return abort || ch[c - R].h2d; });
+                if (abort) { delete P; return; }
+                lk.unlock();
+                if (cudaEventSynchronize(X.ev_h2d[slot]) != cudaSuccess) {
+                    fail(c, CINTGPU_ERR_CUDA, "upload failed");
+                    delete P;
+                    return;
+                }
+            }
+            DevLayout D = dev_layout(P);
+            if ((r = grow_host(&X.pin_in[slot], &X.pin_in_cap[slot], D.upload))) {
+                fail(c, r, cintgpu_last_error());
+                delete P;
+                return;
+            }
+            fill_image(P, D, X.pin_in[slot]);
             std::lock_guard<std::mutex> lk(mu);
-            ch[c].P = P; ch[c].rc = r; ch[c].err = e; ch[c].done = true;
+            ch[c].P = P;
+            ch[c].D = D;
+            ch[c].out_size = P->out_size;
+            ch[c].ncomp = P->ncomp;
+            ch[c].image = true;
             cv.notify_all();
         }
     };
-    const int nthreads = std::max(1, std::min<int>(C, std::min<int>(16, (int)std::thread::hardware_concurrency())));
-    std::vector<std::thread> pool;
-    for (int t = 0; t < nthreads; t++) pool.emplace_back(worker);
-
-    int ncomp = 1;
-    auto complete = [&](int c) -> int {   /* wait for chunk c's copy, scatter it to out_host */
-        const int s = c & 1;
-        if (cudaEventSynchronize(X.ev_d2h[s]) != cudaSuccess) {
-            set_error("chunk %d: %s", c, cudaGetErrorString(cudaGetLastError()));
-            return CINTGPU_ERR_CUDA;
+    auto scatter = [&]() {
+        for (;;) {
+            const int c = next_scatter.fetch_add(1);
+            if (c >= C) return;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return abort || ch[c].d2h; });
+                if (abort) return;
+            }
+            const int slot = c % R;
+            if (cudaEventSynchronize(X.ev_d2h[slot]) != cudaSuccess) {
+                fail(c, CINTGPU_ERR_CUDA, "copy back failed");
+                return;
+            }
+            for (int k = 0; k < ch[c].ncomp; k++)
+                memcpy(out_host + (size_t)k * total + ch[c].base,
+                       X.pin_out[slot] + sizeof(double) * k * ch[c].out_size, sizeof(double) * ch[c].out_size);
+            std::lock_guard<std::mutex> lk(mu);
+            ch[c].scattered = true;
+            cv.notify_all();
         }
-        const CINTGPUPlan *P = ch[c].P;
-        for (int k = 0; k < ncomp; k++)
-            memcpy(out_host + (size_t)k * total + ch[c].base, X.pin_out[s] + sizeof(double) * k * P->out_size,
-                   sizeof(double) * P->out_size);
-        return 0;
     };
-    for (int c = 0; c < C && !rc; c++) {
-        const int s = c & 1;
+    const int nbuild = std::max(1, std::min<int>(C, std::min<int>(14, (int)std::thread::hardware_concurrency())));
+    const int nscatter = std::min(C, 2);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nbuild; t++) pool.emplace_back(builder);
+    for (int t = 0; t < nscatter; t++) pool.emplace_back(scatter);
+
+    /* CINTGPU_TRACE=1: the caller's time per phase, printed to stderr at the end */
+    using clk = std::chrono::steady_clock;
+    const bool trace = getenv("CINTGPU_TRACE") != nullptr;
+    double t_image = 0, t_slot = 0, t_enqueue = 0;
+    const auto t_start = clk::now();
+    auto since = [](clk::time_point a) { return std::chrono::duration<double, std::milli>(clk::now() - a).count(); };
+    for (int c = 0; c < C; c++) {
+        const int slot = c % R;
+        cudaStream_t st = X.s_exec[c & 1];
+        CINTGPUPlan *P;
         {
+            auto t0 = clk::now();
             std::unique_lock<std::mutex> lk(mu);
-            cv.wait(lk, [&] { return ch[c].done; });
+            cv.wait(lk, [&] { return abort || ch[c].image; });
+            t_image += since(t0);
+            if (abort) break;
+            t0 = clk::now();
+            /* slot reuse: chunk c - R copied back and scattered (so its kernels are done too) */
+            if (c >= R) cv.wait(lk, [&] { return abort || ch[c - R].scattered; });
+            t_slot += since(t0);
+            if (abort) break;
+            P = ch[c].P;
         }
-        if (ch[c].rc) { set_error("%s", ch[c].err.c_str()); rc = ch[c].rc; break; }
-        CINTGPUPlan *P = ch[c].P;
-        ncomp = P->ncomp;
+        auto t0 = clk::now();
+        const DevLayout &D = ch[c].D;
         const size_t outb = sizeof(double) * std::max<int64_t>(P->out_size * P->ncomp, 1);
-        if ((rc = grow_dev(&X.arena[s], &X.arena_cap[s], plan_device_bytes(P)))
-            || (rc = grow_dev(&X.dout[s], &X.dout_cap[s], outb))
-            || (rc = grow_host(&X.pin_in[s], &X.pin_in_cap[s], plan_upload_bytes(P)))
-            || (rc = grow_host(&X.pin_out[s], &X.pin_out_cap[s], outb)))
-            break;
-        if ((rc = upload_plan(P, X.arena[s], X.arena_cap[s], X.s_exec[s], true, X.pin_in[s]))) break;
-        if ((rc = execute_plan(P, (double *)X.dout[s], X.s_exec[s]))) break;
-        if (cudaEventRecord(X.ev_exec[s], X.s_exec[s]) != cudaSuccess
-            || cudaStreamWaitEvent(X.s_copy, X.ev_exec[s], 0) != cudaSuccess
-            || cudaMemcpyAsync(X.pin_out[s], X.dout[s], outb, cudaMemcpyDeviceToHost, X.s_copy) != cudaSuccess
-            || cudaEventRecord(X.ev_d2h[s], X.s_copy) != cudaSuccess) {
-            set_error("chunk %d: %s", c, cudaGetErrorString(cudaGetLastError()));
-            rc = CINTGPU_ERR_CUDA;
+        int r;
+        if ((r = grow_dev(&X.arena[slot], &X.arena_cap[slot], D.total))
+            || (r = grow_dev(&X.dout[slot], &X.dout_cap[slot], outb))
+            || (r = grow_host(&X.pin_out[slot], &X.pin_out_cap[slot], outb))) {
+            fail(c, r, cintgpu_last_error());
             break;
         }
-        if (c > 0) {
-            if ((rc = complete(c - 1))) break;
-            delete ch[c - 1].P;   /* the arena is caller-owned: nothing on the device to free */
-            ch[c - 1].P = nullptr;
+        P->dbuf = X.arena[slot]; P->dbuf_size = X.arena_cap[slot]; P->owns_dbuf = false;
+        carve_plan(P, D, X.arena[slot]);
+        bool ok = cudaMemcpyAsync(X.arena[slot], X.pin_in[slot], D.upload, cudaMemcpyHostToDevice, st) == cudaSuccess
+                  && cudaEventRecord(X.ev_h2d[slot], st) == cudaSuccess;
+        if (ok) {
+            std::lock_guard<std::mutex> lk(mu);
+            ch[c].h2d = true;
+            cv.notify_all();
         }
-        if (c == C - 1) rc = complete(c);
+        if (ok && (r = execute_plan(P, (double *)X.dout[slot], st))) { fail(c, r, cintgpu_last_error()); break; }
+        ok = ok && cudaEventRecord(X.ev_exec[slot], st) == cudaSuccess
+             && cudaStreamWaitEvent(X.s_copy, X.ev_exec[slot], 0) == cudaSuccess
+             && cudaMemcpyAsync(X.pin_out[slot], X.dout[slot], outb, cudaMemcpyDeviceToHost, X.s_copy) == cudaSuccess
+             && cudaEventRecord(X.ev_d2h[slot], X.s_copy) == cudaSuccess;
+        if (!ok) {
+            fail(c, CINTGPU_ERR_CUDA, std::string("chunk enqueue failed: ") + cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            ch[c].d2h = true;
+            ch[c].P = nullptr;
+            cv.notify_all();
+        }
+        delete P;   /* its device data live in the slot's arena; the host images are not needed */
+        t_enqueue += since(t0);
     }
     for (std::thread &t : pool) t.join();
     cudaStreamSynchronize(X.s_exec[0]);
     cudaStreamSynchronize(X.s_exec[1]);
     cudaStreamSynchronize(X.s_copy);
-    for (Chunk &x : ch) delete x.P;
+    for (Chunk &x : ch) {
+        delete x.P;
+        if (x.rc && !rc) { rc = x.rc; set_error("%s", x.err.c_str()); }
+    }
+    if (trace)
+        fprintf(stderr, "cintgpu_batch_host: %lld items, %d chunks, %d builders; caller ms: waiting for "
+                        "images %.1f, waiting for free slots %.1f, enqueue %.1f, total %.1f\n",
+                (long long)n, C, nbuild, t_image, t_slot, t_enqueue, since(t_start));
     return rc;
 }
 

@@ -283,11 +283,13 @@ __device__ inline double *cg_hrr(const double *src, const int *__restrict__ eper
     for (int b = 1; b <= lj; b++) {
         const int nrows = __ldg(prog);
         const int *rows = prog + 1;
+        const double *__restrict__ c = cur;
+        double *__restrict__ x = nxt;
         for (int e = lane; e < nrows * nF; e += 32) {
             const int r = e / nF, f = e - r * nF;
             const int hi = __ldg(rows + 3 * r), lo = __ldg(rows + 3 * r + 1), ax = __ldg(rows + 3 * r + 2);
             const double t = ax == 0 ? ab0 : (ax == 1 ? ab1 : ab2);
-            nxt[e] = fma(t, cur[lo * nF + f], cur[hi * nF + f]);
+            x[e] = fma(t, c[lo * nF + f], c[hi * nF + f]);
         }
         prog += 1 + 3 * nrows;
         __syncwarp();
@@ -299,11 +301,13 @@ __device__ inline double *cg_hrr(const double *src, const int *__restrict__ eper
     for (int d = 1; d <= ll; d++) {
         const int nent = __ldg(prog), sin = __ldg(prog + 1), sout = __ldg(prog + 2);
         const int *ents = prog + 3;
+        const double *__restrict__ c = cur;
+        double *__restrict__ x = nxt;
         for (int e = lane; e < nij * nent; e += 32) {
             const int ij = e / nent, q = e - ij * nent;
             const int hi = __ldg(ents + 3 * q), lo = __ldg(ents + 3 * q + 1), ax = __ldg(ents + 3 * q + 2);
             const double t = ax == 0 ? cd0 : (ax == 1 ? cd1 : cd2);
-            nxt[ij * sout + q] = fma(t, cur[ij * sin + lo], cur[ij * sin + hi]);
+            x[ij * sout + q] = fma(t, c[ij * sin + lo], c[ij * sin + hi]);
         }
         prog += 3 + 3 * nent;
         __syncwarp();
@@ -311,11 +315,15 @@ __device__ inline double *cg_hrr(const double *src, const int *__restrict__ eper
     }
     /* cur[((i nfj + j) nfk + k) nfl + l] -> gctr order */
     const int nf = nij * nfk * nfl;
-    for (int e = lane; e < nf; e += 32) {
-        int i = e % nfi, r = e / nfi;
-        int k = r % nfk; r /= nfk;
-        int l = r % nfl, j = r / nfl;
-        nxt[e] = cur[((i * nfj + j) * nfk + k) * nfl + l];
+    {
+        const double *__restrict__ c = cur;
+        double *__restrict__ x = nxt;
+        for (int e = lane; e < nf; e += 32) {
+            int i = e % nfi, r = e / nfi;
+            int k = r % nfk; r /= nfk;
+            int l = r % nfl, j = r / nfl;
+            x[e] = c[((i * nfj + j) * nfk + k) * nfl + l];
+        }
     }
     __syncwarp();
     return nxt;

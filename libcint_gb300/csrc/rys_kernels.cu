@@ -422,8 +422,8 @@ rys_eri_kernel(CGLaunch P)
 /* One warp per contracted quartet: sum partial slots, then transform the four indices one at a
  * time (j, l, k, i as c2s_sph_2e1 does) through a per-warp scratch in global memory, and store
  * with the task's strides. */
-__device__ __forceinline__ void c2s_pass(const double *src, double *dst, int lsh, int sph,
-                                         int inner, int ncart_t, int outer, int lane)
+__device__ __forceinline__ void c2s_pass(const double *__restrict__ src, double *__restrict__ dst,
+                                         int lsh, int sph, int inner, int ncart_t, int outer, int lane)
 {
     /* src[(a, t, b)] with a < inner, t < ncart_t, b < outer  ->  dst[(a, m, b)] */
     int nm = sph ? (lsh <= 1 ? ncart_t : 2 * lsh + 1) : ncart_t;
