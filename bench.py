@@ -373,6 +373,13 @@ def run_gpu(args, rank, world):
                      'traffic': ERI_DRAM_BYTES_PER_QUARTET * len(qs),
                      'traffic_source': 'ncu dram__bytes_read+write of a 20k-quartet launch, '
                                        'scaled to the step (profiles/rys_eri_kernel_c1.md)',
+                     'flop_model': 'this implementation: per term 20 + 15 VRR entries + groups '
+                                   '+ 2 nE nF (FMA = 2)',
+                     'libcint_algorithm_tflops': plan.flops_libcint * args.steps / kern_s / 1e12,
+                     'libcint_algorithm_note': "the same quartets counted with libcint's "
+                                               'per-primitive VRR + HRR + gout model, over the '
+                                               'same kernel time (exceeds the pipe peak by the '
+                                               'work contraction-first saves)',
                      'peak_source': 'measured DFMA peak (profiles/fp64_peak_gb300.md); '
                                     'MEASURED_PEAKS.json carries no FP64 figure'},
         'e2e': {'value': nint / statistics.median(e2e_times) if e2e_times else None,

@@ -151,8 +151,13 @@ int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n
 /* doubles per component of the output (max offset + block), and the component count */
 int64_t cintgpu_plan_output_size(const CINTGPUPlan *plan);
 int cintgpu_plan_ncomp(const CINTGPUPlan *plan);
-/* FP64 flops of one execution by the algorithmic model (sum over surviving primitive quartets) */
+/* FP64 flops of one execution by the algorithmic model of this implementation (sum over
+ * surviving primitive quartets; int2e/int3c2e: VRR per term, grouped (e0|f0) accumulation) */
 double cintgpu_plan_flops(const CINTGPUPlan *plan);
+/* the same quartets counted with libcint's per-primitive algorithm (roots setup, VRR, HRR and
+ * gout per primitive quartet, src/g2e.c:272-693 and src/cint2e.c:961-1183); int2e/int3c2e kinds,
+ * 0 otherwise.  No libcint counterpart (measurement aid). */
+double cintgpu_plan_flops_libcint(const CINTGPUPlan *plan);
 int64_t cintgpu_plan_prim_quartets(const CINTGPUPlan *plan);
 /* Launch the plan on `stream` (a cudaStream_t; NULL = legacy default stream) writing
  * out_dev[comp * output_size + offsets[q] + ...].  Asynchronous; enqueue only. */

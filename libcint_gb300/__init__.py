@@ -65,6 +65,8 @@ def lib():
     L.cintgpu_plan_upload_bytes.restype = i64
     L.cintgpu_plan_launches.argtypes = [vp]
     L.cintgpu_plan_launches.restype = i32
+    L.cintgpu_plan_flops_libcint.argtypes = [vp]
+    L.cintgpu_plan_flops_libcint.restype = ctypes.c_double
     L.cintgpu_plan_compute_ms.argtypes = [vp]
     L.cintgpu_plan_compute_ms.restype = ctypes.c_float
     L.cintgpu_plan_execute.argtypes = [vp, vp, vp]
@@ -129,6 +131,7 @@ class Plan:
         self.output_size = L.cintgpu_plan_output_size(h)
         self.ncomp = L.cintgpu_plan_ncomp(h)
         self.flops = L.cintgpu_plan_flops(h)
+        self.flops_libcint = L.cintgpu_plan_flops_libcint(h)
         self.prim_quartets = L.cintgpu_plan_prim_quartets(h)
         self.launches = L.cintgpu_plan_launches(h)
 

@@ -237,6 +237,7 @@ struct CINTGPUPlan {
     int64_t nitems = 0;
     int64_t out_size = 0;          /* doubles per component */
     double flops = 0;
+    double flops_ref = 0;          /* the same quartets by libcint's per-primitive algorithm */
     int64_t prim_quartets = 0;
     int max_nf = 1;
     /* host images */
@@ -252,6 +253,7 @@ struct CINTGPUPlan {
     std::vector<CGEriGroup> egroup;
     std::vector<int> eperm;
     std::vector<int> hprog;        /* horizontal-transfer programs of the classes */
+    std::vector<int> eround;       /* stage-3 rounds: start | count << 16 | box << 24 */
     int hrr_max = 1;               /* doubles of one transfer buffer, largest class */
     int nef_max = 1;               /* (e0|f0) accumulators, largest class */
     std::vector<int> out_item;     /* item index of each CGOutTask */
@@ -273,6 +275,7 @@ struct CINTGPUPlan {
     CGEriGroup *d_egroup = nullptr;
     int *d_eperm = nullptr;
     int *d_hprog = nullptr;
+    int *d_eround = nullptr;
     double *d_gctr = nullptr;
     int *d_counters = nullptr;     /* [0], [1]: task counters of the groups; [2]: status */
     int *d_nonempty = nullptr;
@@ -410,6 +413,20 @@ struct Builder {
     }
 };
 
+/* libcint's per-primitive algorithm for one surviving primitive quartet of an int2e class (FMA =
+ * 2): per root, coefficient setup 20, VRR 15 per (e, f) entry, 2 per HRR entry written and axis,
+ * gout 3 per Cartesian component (src/g2e.c:272-693, src/cint2e.c:961-1183) */
+double flops_libcint_primq(int li, int lj, int lk, int ll)
+{
+    CGLayout L;
+    cg_layout(li, lj, lk, ll, CG_MODE_ERI, CG_WS_MAX, &L);
+    double hrr = 0;
+    for (int j = 1; j < L.dJ; j++) hrr += (L.nmax - j + 1) * (L.mmax + 1);
+    for (int l = 1; l < L.dL; l++) hrr += L.dI * L.dJ * (L.mmax - l + 1);
+    double vrr = (double)(L.nmax + 1) * (L.mmax + 1);
+    return L.nroots * (20 + 3 * 5 * vrr + 3 * 2 * hrr + 3.0 * L.nf);
+}
+
 /* algorithmic FP64 flop model per surviving primitive quartet (FMA = 2) */
 double flops_per_primq(int li, int lj, int lk, int ll, int mode)
 {
@@ -481,22 +498,54 @@ static int build_eri_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
             e.mn = E.nz[p] | (F.nz[q] << 8);
             g.push_back(e);
         }
-    /* shapes (nez, nfz) descending, so a round of 32 groups mostly shares one shape; every group
-     * carries its round's member box (bits 16+: (MA-1) + 4 (MB-1)) for the kernel's dispatch */
-    std::stable_sort(g.begin(), g.end(), [](const CGEriGroup &a, const CGEriGroup &b) {
-        if ((a.mn & 0xff) != (b.mn & 0xff)) return (a.mn & 0xff) > (b.mn & 0xff);
-        return (a.mn >> 8) > (b.mn >> 8);
+    /* Rounds: the kernel runs a class's groups in rounds of <= 32 (one per lane), each round
+     * dispatched on its member box (largest nez x largest nfz).  A round costs 32 (box + 1) FP64
+     * slots per term whatever its lanes need, so the groups are ordered by shape and cut into
+     * rounds by dynamic programming over that order (two orders tried, the cheaper kept). */
+    auto nez_of = [](const CGEriGroup &x) { return x.mn & 0xff; };
+    auto nfz_of = [](const CGEriGroup &x) { return (x.mn >> 8) & 0xff; };
+    auto cut = [&](const std::vector<CGEriGroup> &v, std::vector<std::pair<int, int>> *rounds) {
+        const int n = (int)v.size();
+        std::vector<double> best(n + 1, 1e300);
+        std::vector<int> from(n + 1, 0);
+        best[0] = 0;
+        for (int i = 1; i <= n; i++) {
+            int ma = 0, mb = 0;
+            for (int j = i - 1; j >= std::max(0, i - 32); j--) {
+                ma = std::max(ma, nez_of(v[j]));
+                mb = std::max(mb, nfz_of(v[j]));
+                double c = best[j] + 32.0 * (ma * mb + 1);
+                if (c < best[i]) { best[i] = c; from[i] = j; }
+            }
+        }
+        rounds->clear();
+        for (int i = n; i > 0; i = from[i]) rounds->push_back({from[i], i - from[i]});
+        std::reverse(rounds->begin(), rounds->end());
+        return best[n];
+    };
+    std::vector<CGEriGroup> g2 = g;
+    std::stable_sort(g.begin(), g.end(), [&](const CGEriGroup &a, const CGEriGroup &b) {
+        if (nez_of(a) != nez_of(b)) return nez_of(a) > nez_of(b);
+        return nfz_of(a) > nfz_of(b);
     });
-    for (size_t r0 = 0; r0 < g.size(); r0 += 32) {
+    std::stable_sort(g2.begin(), g2.end(), [&](const CGEriGroup &a, const CGEriGroup &b) {
+        if (nfz_of(a) != nfz_of(b)) return nfz_of(a) > nfz_of(b);
+        return nez_of(a) > nez_of(b);
+    });
+    std::vector<std::pair<int, int>> r1, r2;
+    if (cut(g2, &r2) < cut(g, &r1)) { g.swap(g2); r1.swap(r2); }
+    P->egroup.insert(P->egroup.end(), g.begin(), g.end());
+    c.round_off = (int)P->eround.size();
+    c.nround = (int)r1.size();
+    for (const auto &r : r1) {
         int ma = 1, mb = 1;
-        for (size_t k = r0; k < std::min(g.size(), r0 + 32); k++) {
-            ma = std::max(ma, g[k].mn & 0xff);
-            mb = std::max(mb, g[k].mn >> 8);
+        for (int k = r.first; k < r.first + r.second; k++) {
+            ma = std::max(ma, nez_of(g[k]));
+            mb = std::max(mb, nfz_of(g[k]));
         }
         const int box = (ma <= 4 && mb <= 4) ? (ma - 1) + 4 * (mb - 1) : 0xff;
-        for (size_t k = r0; k < std::min(g.size(), r0 + 32); k++) g[k].mn |= box << 16;
+        P->eround.push_back(r.first | (r.second << 16) | (box << 24));
     }
-    P->egroup.insert(P->egroup.end(), g.begin(), g.end());
     c.ngroup = (int)g.size();
     c.split = 0;
     if (c.ngroup <= 32) {
@@ -527,7 +576,7 @@ static int build_eri_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
      * row = e_hi(e + 1_ax, jb - 1_ax), lo = (e, jb - 1_ax), ax = lowest non-zero axis of jb;
      * per ket level d = 1..ll, nent, in_stride, out_stride, then (hi, lo, axis) per (f, ld) */
     c.hprog_off = (int)P->hprog.size();
-    c.pad0 = c.pad1 = c.pad2 = 0;
+    c.pad0 = 0;
     auto cidx = [](int l, int x, int y) { int r = l - x; return r * (r + 1) / 2 + (r - y); };
     auto comps = [](int l) {
         std::vector<std::array<int, 3>> v;
@@ -815,6 +864,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         int64_t n = (int64_t)P->pqlist.size() - off;
         double cpq = flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode);
         fl += n * cpq;
+        if (P->mode == CG_MODE_ERI) P->flops_ref += n * flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3]);
         if (n > 0) work.push_back({(int)w, off, n, cpq});
     }
     if (P->pqlist.size() > (size_t)INT32_MAX) { set_error("too many primitive quartets in one plan"); return CINTGPU_ERR_ARG; }
@@ -848,9 +898,16 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
                       pe.l[0], pe.l[1], pe.l[2], pe.l[3], L.nroots, cg_rys_nmax());
             return CINTGPU_ERR_UNSUPPORTED;
         }
-        /* at least one batch of terms per slice, at least 4 primitive quartets */
+        /* at least one batch of terms per slice, at least 4 primitive quartets; slices hold whole
+         * batches (terms a multiple of T) so only a quartet's last slice has a partial batch */
         int64_t slice = std::max<int64_t>(std::max<int64_t>(4, (L.T + L.nroots - 1) / L.nroots),
                                           (int64_t)(target / w.cost_pq));
+        {
+            int a = L.T, b = L.nroots;
+            while (b) { int t = a % b; a = b; b = t; }
+            const int64_t m = L.T / a;
+            slice = (slice + m - 1) / m * m;
+        }
         int nf = ncart_l(pe.l[0]) * ncart_l(pe.l[1]) * ncart_l(pe.l[2]) * ncart_l(pe.l[3]);
         int64_t slot = (int64_t)nf * P->ncomp;
         CGOutTask &o = P->outs[pe.out];
@@ -912,7 +969,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
 }
 
 struct DevLayout {
-    size_t pairs, prims, tasks, outs, pq, gcl, gch, gen, ecl, egr, epm, hpg, gctr, cnt, ne, scr, wscr;
+    size_t pairs, prims, tasks, outs, pq, gcl, gch, gen, ecl, egr, epm, hpg, erd, gctr, cnt, ne, scr, wscr;
     int64_t wstride;
     int wwarps;
     size_t upload, total;
@@ -939,6 +996,7 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     D.egr = al(sizeof(CGEriGroup) * std::max<size_t>(P->egroup.size(), 1));
     D.epm = al(sizeof(int) * std::max<size_t>(P->eperm.size(), 1));
     D.hpg = al(sizeof(int) * std::max<size_t>(P->hprog.size(), 1));
+    D.erd = al(sizeof(int) * std::max<size_t>(P->eround.size(), 1));
     D.gctr = al(sizeof(double) * P->gctr_size);
     D.cnt = al(sizeof(int) * 4);
     D.ne = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
@@ -953,7 +1011,7 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
         D.wscr = al(sizeof(double) * (size_t)D.wwarps * D.wstride);
     }
     if (P->jmode || grad) D.gctr = al(sizeof(double));   /* no per-task accumulators */
-    D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq + D.gcl + D.gch + D.gen + D.ecl + D.egr + D.epm + D.hpg;
+    D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq + D.gcl + D.gch + D.gen + D.ecl + D.egr + D.epm + D.hpg + D.erd;
     D.total = D.upload + D.gctr + D.cnt + D.ne + D.scr + D.wscr;
     return D;
 }
@@ -978,6 +1036,7 @@ static void carve_plan(CINTGPUPlan *P, const DevLayout &D, char *p)
     P->d_egroup = (CGEriGroup *)p; p += D.egr;
     P->d_eperm = (int *)p; p += D.epm;
     P->d_hprog = (int *)p; p += D.hpg;
+    P->d_eround = (int *)p; p += D.erd;
     P->d_gctr = (double *)p; p += D.gctr;
     P->d_counters = (int *)p; p += D.cnt;
     P->d_nonempty = (int *)p; p += D.ne;
@@ -1001,7 +1060,8 @@ static void fill_image(const CINTGPUPlan *P, const DevLayout &D, char *q)
     memcpy(q, P->eclass.data(), sizeof(CGEriClass) * P->eclass.size()); q += D.ecl;
     memcpy(q, P->egroup.data(), sizeof(CGEriGroup) * P->egroup.size()); q += D.egr;
     memcpy(q, P->eperm.data(), sizeof(int) * P->eperm.size()); q += D.epm;
-    memcpy(q, P->hprog.data(), sizeof(int) * P->hprog.size());
+    memcpy(q, P->hprog.data(), sizeof(int) * P->hprog.size()); q += D.hpg;
+    memcpy(q, P->eround.data(), sizeof(int) * P->eround.size());
 }
 
 /* Place the plan in device memory (a caller arena or its own allocation) and copy the host
@@ -1102,6 +1162,7 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.egroup = P->d_egroup;
     L.eperm = P->d_eperm;
     L.hprog = P->d_hprog;
+    L.eround = P->d_eround;
     L.hrr_off1 = P->nef_max;
     L.hrr_off2 = (int64_t)P->nef_max + P->hrr_max;
     int nblocks = std::min(g_ctx.sm_count * G.blocks_per_sm, std::max(1, (G.ntasks + 3) / 4));
@@ -1357,6 +1418,7 @@ int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n
 int64_t cintgpu_plan_output_size(const CINTGPUPlan *plan) { return plan->out_size; }
 int cintgpu_plan_ncomp(const CINTGPUPlan *plan) { return plan->ncomp; }
 double cintgpu_plan_flops(const CINTGPUPlan *plan) { return plan->flops; }
+double cintgpu_plan_flops_libcint(const CINTGPUPlan *plan) { return plan->flops_ref; }
 int64_t cintgpu_plan_prim_quartets(const CINTGPUPlan *plan) { return plan->prim_quartets; }
 int cintgpu_plan_launches(const CINTGPUPlan *plan)
 {
@@ -1526,8 +1588,9 @@ int64_t item_block(int kind, const int *q, const int *bas)
 }
 }  // namespace
 
-/* Host-buffer form over a packed output.  The item list is cut into chunks (2048 items, then
- * 4096); chunk c uses slot c % CG_BATCH_SLOTS of a ring and execution stream c % 2.
+/* Host-buffer form over a packed output.  The item list is cut into chunks (512 items, growing
+ * by a quarter per chunk up to 8192); chunk c uses slot c % CG_BATCH_SLOTS of a ring and
+ * execution stream c % 2.
  *   builder threads  build chunk plans and, once the slot's previous upload has completed, write
  *                    the plan's image into the slot's pinned buffer;
  *   the caller       uploads each image, executes the plan and queues the copy back, never
@@ -1558,10 +1621,11 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
         std::string err;
         bool image = false, h2d = false, d2h = false, scattered = false;
     };
-    /* the GPU starts after one small plan; the builders outpace the GPU on the later chunks */
+    /* chunk sizes 512, 640, 800, ... (x 1.25) up to 8192 items: the GPU starts after one small
+     * plan, and each later chunk's plan (built by one thread) is ready before the GPU needs it */
     std::vector<Chunk> ch;
     int64_t total = 0;
-    for (int64_t i0 = 0, len = 2048; i0 < n; i0 += len, len = 4096) {
+    for (int64_t i0 = 0, len = 512; i0 < n; i0 += len, len = std::min<int64_t>(len + len / 4, 8192)) {
         Chunk x;
         x.i0 = i0;
         x.n = std::min(len, n - i0);
@@ -1841,19 +1905,20 @@ int cg_init(void) { return ensure_init(); }
 int cg_sm_count(void) { return g_ctx.sm_count; }
 void cg_set_error_msg(const char *msg) { set_error("%s", msg); }
 /* Contraction-first tables of one class, for host-side tests of the table logic:
- * info[12] = CGEriClass fields, groups[4 * ngroup], perm[nE + nF], prog (the transfer program);
- * returns the program length or -1 when a buffer is too small. */
+ * info[12] = CGEriClass fields, groups[4 * ngroup], perm[nE + nF], prog (the transfer program),
+ * rounds[nround]; returns the program length or -1 when a buffer is too small. */
 extern "C" int cg_eri_tables(int li, int lj, int lk, int ll, int *info, int *groups, int maxg,
-                             int *perm, int maxp, int *prog, int maxprog)
+                             int *perm, int maxp, int *prog, int maxprog, int *rounds, int maxr)
 {
     CINTGPUPlan P;
     build_eri_class(&P, li, lj, lk, ll);
     const CGEriClass &c = P.eclass[0];
-    if (c.ngroup > maxg || c.nE + c.nF > maxp || (int)P.hprog.size() > maxprog) return -1;
+    if (c.ngroup > maxg || c.nE + c.nF > maxp || (int)P.hprog.size() > maxprog || c.nround > maxr) return -1;
     memcpy(info, &c, sizeof(CGEriClass));
     memcpy(groups, P.egroup.data(), sizeof(CGEriGroup) * P.egroup.size());
     memcpy(perm, P.eperm.data(), sizeof(int) * P.eperm.size());
     memcpy(prog, P.hprog.data(), sizeof(int) * P.hprog.size());
+    memcpy(rounds, P.eround.data(), sizeof(int) * P.eround.size());
     return (int)P.hprog.size();
 }
 

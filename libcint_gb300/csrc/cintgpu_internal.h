@@ -20,5 +20,5 @@ size_t cg_plan_bytes(const CINTGPUPlan *P);
 int cg_plan_place(CINTGPUPlan *P, char *region, size_t region_bytes, cudaStream_t stream);
 int cg_plan_run(CINTGPUPlan *P, double *out_dev, cudaStream_t stream);
 extern "C" int cg_eri_tables(int li, int lj, int lk, int ll, int *info, int *groups, int maxg,
-                             int *perm, int maxp, int *prog, int maxprog);
+                             int *perm, int maxp, int *prog, int maxprog, int *rounds, int maxr);
 #endif

@@ -73,21 +73,22 @@ typedef struct { int ob_oc; int c; } CGGradEnt;                          /* ob |
  * eperm/fperm map the transfer's Cartesian order (shells ascending, libcint order within a shell)
  * to those rows/columns. */
 typedef struct {
-    int group_off, ngroup;   /* CGEriGroup range, sorted by shape (nez, nfz), largest first */
+    int group_off, ngroup;   /* CGEriGroup range, ordered by shape (nez, nfz) */
     int perm_off;            /* eperm[nE] then fperm[nF] */
     int nE, nF;
     int split;               /* ngroup <= 32: lanes per group (power of two); 0: groups in rounds */
     int hrr_need;            /* doubles of each of the two transfer buffers */
     int maxab;               /* (lj + 1) | (ll + 1) << 8: member box of the class */
     int hprog_off;           /* horizontal-transfer program (ints), see cg_hrr */
-    int pad0, pad1, pad2;
+    int round_off, nround;   /* stage-3 rounds (ints: first group | count << 16 | box << 24,
+                                box = (MA-1) + 4 (MB-1) of the round's largest nez, nfz) */
+    int pad0;
 } CGEriClass;
 typedef struct {
     int oxy;             /* ox | oy << 16: offsets of (ex, fx) and (ey, fy) in the VRR arrays */
     int oz;              /* offset of (ez0, fz0) in the z array */
     int acc;             /* accumulator index of member (0, 0) */
-    int mn;              /* nez | nfz << 8 | box << 16: box = (MA-1) + 4 (MB-1), the largest
-                            nez (MA) and nfz (MB) among the 32 groups of this group's round */
+    int mn;              /* nez | nfz << 8 */
 } CGEriGroup;
 
 typedef struct {

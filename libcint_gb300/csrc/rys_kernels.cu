@@ -296,11 +296,11 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
         if (S > 0) {
             if (own) e0f0_dispatch(mab, greg, gstride, G, na, sp, Tb, S, mine.oxy, mine.oz, mine.mn, r);
         } else if (boxed) {
-            /* rounds of 32 groups, each dispatched on its own member box (warp-uniform) */
-            for (int r0 = 0; r0 < ec.ngroup; r0 += 32) {
-                const int gi = r0 + lane;
-                if (gi >= ec.ngroup) break;
-                const CGEriGroup q = grp[gi];
+            /* the class's rounds (<= 32 groups, one per lane), each dispatched on its member box */
+            for (int r = 0; r < ec.nround; r++) {
+                const int rd = __ldg(P.eround + ec.round_off + r);
+                if (lane >= (int)(((unsigned)rd >> 16) & 0xffu)) continue;
+                const CGEriGroup q = grp[(rd & 0xffff) + lane];
                 const int nez = q.mn & 0xff, nfz = (q.mn >> 8) & 0xff;
                 double v[16];
 #pragma unroll
@@ -308,7 +308,7 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
 #pragma unroll
                     for (int a = 0; a < 4; a++)
                         v[b * 4 + a] = (a < nez && b < nfz) ? acc[q.acc + a * nF + b] : 0.0;
-                e0f0_dispatch(q.mn >> 16, greg, gstride, G, na, 0, Tb, 1, q.oxy, q.oz, q.mn, v);
+                e0f0_dispatch((int)((unsigned)rd >> 24), greg, gstride, G, na, 0, Tb, 1, q.oxy, q.oz, q.mn, v);
 #pragma unroll
                 for (int b = 0; b < 4; b++)
 #pragma unroll
@@ -471,7 +471,9 @@ cg_output_kernel(const CGOutTask *__restrict__ ot, int nout, double *gctr, const
         const int nf = nfc[0] * nfc[1] * nfc[2] * nfc[3];
         const bool ne = nonempty[q] != 0;
         const bool e0f0 = (o.flags & 2) != 0;
-        const CGEriClass ec = e0f0 ? eclass[o.ecls] : CGEriClass{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        CGEriClass ec;
+        memset(&ec, 0, sizeof(ec));
+        if (e0f0) ec = eclass[o.ecls];
         const int slot = e0f0 ? ec.nE * ec.nF : nf;   /* accumulators per part and component */
         for (int comp = 0; comp < ncomp; comp++) {
             double *g0 = gctr + o.cart_off + (size_t)comp * slot;

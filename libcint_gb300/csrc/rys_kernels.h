@@ -51,6 +51,7 @@ typedef struct {
     const CGEriGroup *egroup;
     const int *eperm;
     const int *hprog;
+    const int *eround;
     int64_t hrr_off1, hrr_off2;   /* J mode: transfer buffers inside the warp's slot */
 } CGLaunch;
 

@@ -31,12 +31,16 @@ def tables(li, lj, lk, ll):
     groups = np.zeros(4 * 20000, np.int32)
     perm = np.zeros(4000, np.int32)
     prog = np.zeros(400000, np.int32)
+    rounds = np.zeros(20000, np.int32)
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
-    nprog = f(li, lj, lk, ll, P(info), P(groups), 20000, P(perm), 4000, P(prog), prog.size)
+    nprog = f(li, lj, lk, ll, P(info), P(groups), 20000, P(perm), 4000, P(prog), prog.size,
+              P(rounds), rounds.size)
     assert nprog >= 0
-    keys = ['group_off', 'ngroup', 'perm_off', 'nE', 'nF', 'split', 'hrr_need', 'maxab', 'hprog_off']
+    keys = ['group_off', 'ngroup', 'perm_off', 'nE', 'nF', 'split', 'hrr_need', 'maxab', 'hprog_off',
+            'round_off', 'nround']
     c = dict(zip(keys, info.tolist()))
-    return c, groups[:4 * c['ngroup']].reshape(-1, 4), perm[:c['nE'] + c['nF']], prog[:nprog]
+    return (c, groups[:4 * c['ngroup']].reshape(-1, 4), perm[:c['nE'] + c['nF']], prog[:nprog],
+            rounds[:c['nround']].astype(np.int64) & 0xffffffff)
 
 
 def hrr(src, eperm, fperm, prog, li, lj, lk, ll, AB, CD, need):
@@ -122,7 +126,7 @@ CLASSES = [(0, 0, 0, 0), (1, 0, 0, 0), (1, 1, 0, 0), (1, 1, 1, 1), (2, 1, 1, 0),
 @pytest.mark.parametrize('cls', CLASSES)
 def test_e0f0_tables_replay(cls):
     li, lj, lk, ll = cls
-    c, groups, perm, prog = tables(*cls)
+    c, groups, perm, prog, rounds = tables(*cls)
     na, nm = li + lj + 1, lk + ll + 1
     nE, nF = c['nE'], c['nF']
     assert nE == below(li + lj + 1) - below(li) and nF == below(lk + ll + 1) - below(lk)
@@ -144,13 +148,21 @@ def test_e0f0_tables_replay(cls):
             for b in range(nfz):
                 hit[acc + a * nF + b] += 1
     assert (hit == 1).all()
-    assert shapes == sorted(shapes, reverse=True)
-    # each round of 32 groups carries the box of its largest nez and nfz
-    for r0 in range(0, len(groups), 32):
-        rnd = shapes[r0:r0 + 32]
-        ma, mb = max(x[0] for x in rnd), max(x[1] for x in rnd)
-        box = (ma - 1) + 4 * (mb - 1) if ma <= 4 and mb <= 4 else 0xff
-        assert all((g[3] >> 16) == box for g in groups[r0:r0 + 32])
+    assert shapes in (sorted(shapes, reverse=True), sorted(shapes, key=lambda x: (x[1], x[0]), reverse=True))
+    # rounds: contiguous, <= 32 groups, cover every group once, box = largest nez x largest nfz
+    pos, cost = 0, 0
+    for rd in rounds:
+        start, cnt, box = rd & 0xffff, (rd >> 16) & 0xff, rd >> 24
+        assert start == pos and 1 <= cnt <= 32
+        ma, mb = max(x[0] for x in shapes[start:start + cnt]), max(x[1] for x in shapes[start:start + cnt])
+        assert box == ((ma - 1) + 4 * (mb - 1) if ma <= 4 and mb <= 4 else 0xff)
+        cost += 32 * (ma * mb + 1)
+        pos += cnt
+    assert pos == len(groups)
+    # never worse than plain rounds of 32 in the same order
+    plain = sum(32 * (max(x[0] for x in shapes[r:r + 32]) * max(x[1] for x in shapes[r:r + 32]) + 1)
+                for r in range(0, len(shapes), 32))
+    assert cost <= plain
     assert sorted(perm[:nE]) == list(range(nE)) and sorted(perm[nE:]) == list(range(nF))
     rng = np.random.RandomState(sum(cls))
     nT = 5

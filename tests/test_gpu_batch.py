@@ -1,5 +1,5 @@
 """The one-shot host-buffer entry cintgpu_batch_host, through the C-ABI.  Without offsets it cuts
-the item list into chunks (2048 items, then 4096) planned on host threads while the GPU runs
+the item list into chunks (512 items, growing to 8192) planned on host threads while the GPU runs
 earlier chunks; its output must equal one device plan over the whole list (same layout:
 component-major, blocks back to back) to the tolerance of the other parity tests, and the checker
 on a sample."""
@@ -46,7 +46,7 @@ def test_batch_host_chunks_match_plan(gpulib, oracle, kind, n):
     sizes = np.array([np.prod([mol.nsph(s) if sph else mol.ncart(s) for s in it]) for it in items])
     offs = np.concatenate([[0], np.cumsum(sizes)[:-1]])
     ncomp = got.shape[0]
-    for q in sorted({0, 2047, 2048, 6143, 6144, 8191, n - 1} & set(range(n))):
+    for q in sorted({0, 511, 512, 1151, 1152, 4095, 4096, n - 1} & set(range(n))):
         _, ref = oracle.port.call(name, mol, items[q][:nsh])
         for c in range(ncomp):
             r = ref[..., c] if ncomp > 1 else ref
