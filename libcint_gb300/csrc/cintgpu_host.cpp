@@ -1646,13 +1646,19 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
         abort = true;
         cv.notify_all();
     };
+    using clk = std::chrono::steady_clock;
+    auto since = [](clk::time_point a) { return std::chrono::duration<double, std::milli>(clk::now() - a).count(); };
+    const auto t_start = clk::now();
+    std::atomic<int64_t> us_build{0}, us_image{0}, us_first{-1};
     auto builder = [&]() {
         cudaSetDevice(dev);   /* the planner queries kernel occupancy on the caller's device */
         for (;;) {
             const int c = next_build.fetch_add(1);
             if (c >= C) return;
+            auto tb = clk::now();
             CINTGPUPlan *P = new CINTGPUPlan();
             int r = build_plan(P, kind, shls + nsh * ch[c].i0, ch[c].n, nullptr, atm, natm, bas, nbas, env, 0);
+            us_build += (int64_t)(1e3 * since(tb));
             if (r) { fail(c, r, cintgpu_last_error()); delete P; return; }
             const int slot = c % R;
             if (c >= R) {   /* the slot's image buffer is free once chunk c - R is uploaded */
@@ -1672,7 +1678,10 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
                 delete P;
                 return;
             }
+            auto ti = clk::now();
             fill_image(P, D, X.pin_in[slot]);
+            us_image += (int64_t)(1e3 * since(ti));
+            if (c == 0) us_first = (int64_t)(1e3 * since(t_start));
             std::lock_guard<std::mutex> lk(mu);
             ch[c].P = P;
             ch[c].D = D;
@@ -1711,11 +1720,8 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
     for (int t = 0; t < nscatter; t++) pool.emplace_back(scatter);
 
     /* CINTGPU_TRACE=1: the caller's time per phase, printed to stderr at the end */
-    using clk = std::chrono::steady_clock;
     const bool trace = getenv("CINTGPU_TRACE") != nullptr;
     double t_image = 0, t_slot = 0, t_enqueue = 0;
-    const auto t_start = clk::now();
-    auto since = [](clk::time_point a) { return std::chrono::duration<double, std::milli>(clk::now() - a).count(); };
     for (int c = 0; c < C; c++) {
         const int slot = c % R;
         cudaStream_t st = X.s_exec[c & 1];
@@ -1780,8 +1786,10 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
     }
     if (trace)
         fprintf(stderr, "cintgpu_batch_host: %lld items, %d chunks, %d builders; caller ms: waiting for "
-                        "images %.1f, waiting for free slots %.1f, enqueue %.1f, total %.1f\n",
-                (long long)n, C, nbuild, t_image, t_slot, t_enqueue, since(t_start));
+                        "images %.1f, waiting for free slots %.1f, enqueue %.1f, total %.1f; builders ms: "
+                        "planning %.1f, images %.1f, first image at %.1f\n",
+                (long long)n, C, nbuild, t_image, t_slot, t_enqueue, since(t_start), 1e-3 * us_build,
+                1e-3 * us_image, 1e-3 * us_first);
     return rc;
 }
 
