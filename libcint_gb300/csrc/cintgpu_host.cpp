@@ -254,6 +254,8 @@ struct CINTGPUPlan {
     std::vector<int> eperm;
     std::vector<int> hprog;        /* horizontal-transfer programs of the classes */
     std::vector<int> eround;       /* stage-3 rounds: start | count << 16 | box << 24 */
+    std::vector<int> empty_outs;   /* output quartets without any task (zero-filled) */
+    bool fuse_out = true;          /* the integral kernel stores finished quartets itself */
     int hrr_max = 1;               /* doubles of one transfer buffer, largest class */
     int nef_max = 1;               /* (e0|f0) accumulators, largest class */
     std::vector<int> out_item;     /* item index of each CGOutTask */
@@ -276,6 +278,10 @@ struct CINTGPUPlan {
     int *d_eperm = nullptr;
     int *d_hprog = nullptr;
     int *d_eround = nullptr;
+    int *d_empty = nullptr;
+    int *d_done = nullptr;         /* finished slices per output quartet (fused output) */
+    double *d_oscr = nullptr;      /* per-warp transform scratch of the integral kernel */
+    double *cur_out = nullptr;
     double *d_gctr = nullptr;
     int *d_counters = nullptr;     /* [0], [1]: task counters of the groups; [2]: status */
     int *d_nonempty = nullptr;
@@ -965,11 +971,16 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
                                          : cg_blocks_per_sm(P->mode, P->groups[g].ws);
     }
     P->gctr_size = std::max<int64_t>(gpos, 1);
+    P->empty_outs.clear();
+    for (size_t q = 0; q < P->outs.size(); q++)
+        if (P->outs[q].nparts == 0) P->empty_outs.push_back((int)q);
     return 0;
 }
 
 struct DevLayout {
-    size_t pairs, prims, tasks, outs, pq, gcl, gch, gen, ecl, egr, epm, hpg, erd, gctr, cnt, ne, scr, wscr;
+    size_t pairs, prims, tasks, outs, pq, gcl, gch, gen, ecl, egr, epm, hpg, erd, emp, gctr, cnt, ne, scr, wscr;
+    size_t done, oscr;
+    int oscr_warps;
     int64_t wstride;
     int wwarps;
     size_t upload, total;
@@ -977,11 +988,20 @@ struct DevLayout {
     int64_t spw;
 };
 
+/* the integral kernel transforms and stores finished quartets itself (int2e, int3c2e, ip1) */
+static bool fused(const CINTGPUPlan *P)
+{
+    return P->fuse_out && !P->jmode && (P->mode == CG_MODE_ERI || P->mode == CG_MODE_IP1);
+}
+
 static DevLayout dev_layout(const CINTGPUPlan *P)
 {
     auto al = [](size_t x) { return (x + 255) / 256 * 256; };
     DevLayout D;
-    D.out_blocks = std::max(1, std::min<int>((int)((P->outs.size() + 3) / 4), g_ctx.sm_count * 8));
+    const bool fo = fused(P);
+    /* the output kernel transforms every quartet, or (fused) only zero-fills the empty ones */
+    const size_t nout_k = fo ? P->empty_outs.size() : P->outs.size();
+    D.out_blocks = std::max(1, std::min<int>((int)((nout_k + 3) / 4), g_ctx.sm_count * 8));
     /* output scratch per warp: two cart->sph buffers, two transfer buffers (ERI mode) */
     D.spw = 2 * (int64_t)P->max_nf + (P->eclass.empty() ? 0 : 2 * (int64_t)P->hrr_max);
     D.pairs = al(sizeof(CGPair) * std::max<size_t>(P->pairs.size(), 1));
@@ -997,10 +1017,14 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     D.epm = al(sizeof(int) * std::max<size_t>(P->eperm.size(), 1));
     D.hpg = al(sizeof(int) * std::max<size_t>(P->hprog.size(), 1));
     D.erd = al(sizeof(int) * std::max<size_t>(P->eround.size(), 1));
+    D.emp = al(sizeof(int) * std::max<size_t>(P->empty_outs.size(), 1));
+    D.done = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
+    D.oscr_warps = fo ? g_ctx.sm_count * 4 * (P->groups[0].blocks_per_sm + P->groups[1].blocks_per_sm) : 0;
+    D.oscr = fo ? al(sizeof(double) * (size_t)D.oscr_warps * D.spw) : 0;
     D.gctr = al(sizeof(double) * P->gctr_size);
     D.cnt = al(sizeof(int) * 4);
     D.ne = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
-    D.scr = al(sizeof(double) * D.spw * D.out_blocks * 4);
+    D.scr = fo ? al(sizeof(double)) : al(sizeof(double) * D.spw * D.out_blocks * 4);
     D.wwarps = 0;
     D.wscr = 0;
     const bool grad = P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA;
@@ -1011,8 +1035,8 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
         D.wscr = al(sizeof(double) * (size_t)D.wwarps * D.wstride);
     }
     if (P->jmode || grad) D.gctr = al(sizeof(double));   /* no per-task accumulators */
-    D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq + D.gcl + D.gch + D.gen + D.ecl + D.egr + D.epm + D.hpg + D.erd;
-    D.total = D.upload + D.gctr + D.cnt + D.ne + D.scr + D.wscr;
+    D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq + D.gcl + D.gch + D.gen + D.ecl + D.egr + D.epm + D.hpg + D.erd + D.emp;
+    D.total = D.upload + D.gctr + D.cnt + D.ne + D.scr + D.wscr + D.done + D.oscr;
     return D;
 }
 
@@ -1037,11 +1061,14 @@ static void carve_plan(CINTGPUPlan *P, const DevLayout &D, char *p)
     P->d_eperm = (int *)p; p += D.epm;
     P->d_hprog = (int *)p; p += D.hpg;
     P->d_eround = (int *)p; p += D.erd;
+    P->d_empty = (int *)p; p += D.emp;
     P->d_gctr = (double *)p; p += D.gctr;
     P->d_counters = (int *)p; p += D.cnt;
     P->d_nonempty = (int *)p; p += D.ne;
     P->d_scratch = (double *)p; p += D.scr;
     P->d_wscratch = (double *)p; p += D.wscr;
+    P->d_done = (int *)p; p += D.done;
+    P->d_oscr = D.oscr ? (double *)p : nullptr; p += D.oscr;
     P->wscratch_stride = D.wstride;
     P->wscratch_warps = D.wwarps;
 }
@@ -1061,7 +1088,8 @@ static void fill_image(const CINTGPUPlan *P, const DevLayout &D, char *q)
     memcpy(q, P->egroup.data(), sizeof(CGEriGroup) * P->egroup.size()); q += D.egr;
     memcpy(q, P->eperm.data(), sizeof(int) * P->eperm.size()); q += D.epm;
     memcpy(q, P->hprog.data(), sizeof(int) * P->hprog.size()); q += D.hpg;
-    memcpy(q, P->eround.data(), sizeof(int) * P->eround.size());
+    memcpy(q, P->eround.data(), sizeof(int) * P->eround.size()); q += D.erd;
+    memcpy(q, P->empty_outs.data(), sizeof(int) * P->empty_outs.size());
 }
 
 /* Place the plan in device memory (a caller arena or its own allocation) and copy the host
@@ -1163,6 +1191,16 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.eperm = P->d_eperm;
     L.hprog = P->d_hprog;
     L.eround = P->d_eround;
+    L.fuse_out = fused(P) ? 1 : 0;
+    L.outs = P->d_outs;
+    L.done = P->d_done;
+    L.oscr = P->d_oscr;
+    if (L.oscr && g == 1) L.oscr += (size_t)g_ctx.sm_count * 4 * P->groups[0].blocks_per_sm * P->scratch_per_warp;
+    L.oscr_stride = P->scratch_per_warp;
+    L.nf_max = P->max_nf;
+    L.out = P->cur_out;
+    L.ncomp = P->ncomp;
+    L.comp_stride = P->out_size;
     L.hrr_off1 = P->nef_max;
     L.hrr_off2 = (int64_t)P->nef_max + P->hrr_max;
     int nblocks = std::min(g_ctx.sm_count * G.blocks_per_sm, std::max(1, (G.ntasks + 3) / 4));
@@ -1177,6 +1215,9 @@ static int execute_plan(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
 {
     CUDA_OK(cudaMemsetAsync(P->d_nonempty, 0, sizeof(int) * std::max<size_t>(P->outs.size(), 1), stream));
     CUDA_OK(cudaMemsetAsync(P->d_counters, 0, sizeof(int) * 4, stream));
+    const bool fo = fused(P);
+    if (fo) CUDA_OK(cudaMemsetAsync(P->d_done, 0, sizeof(int) * std::max<size_t>(P->outs.size(), 1), stream));
+    P->cur_out = out_dev;
     bool fork = P->side && P->groups[1].ntasks > 0 && P->groups[0].ntasks > 0;
     if (P->ev_t0) CUDA_OK(cudaEventRecord(P->ev_t0, stream));
     if (fork) {
@@ -1198,7 +1239,9 @@ static int execute_plan(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
         P->timed = true;
     }
     if (P->jmode || P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) return 0;
-    int rc = cg_launch_output(P->d_outs, (int)P->outs.size(), P->d_gctr, P->d_nonempty, P->d_scratch,
+    if (fo && P->empty_outs.empty()) return 0;
+    int rc = cg_launch_output(P->d_outs, fo ? P->d_empty : nullptr,
+                              fo ? (int)P->empty_outs.size() : (int)P->outs.size(), P->d_gctr, P->d_nonempty, P->d_scratch,
                               P->scratch_per_warp, P->max_nf, P->d_eclass, P->d_eperm, P->d_hprog, P->out_blocks,
                               out_dev, P->ncomp, P->out_size, stream);
     if (rc) { set_error("output kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
@@ -1657,6 +1700,9 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
             if (c >= C) return;
             auto tb = clk::now();
             CINTGPUPlan *P = new CINTGPUPlan();
+            /* chunks are small: a separate output kernel on the chunk's stream beats transforms
+             * at the integral kernel's tail */
+            P->fuse_out = false;
             int r = build_plan(P, kind, shls + nsh * ch[c].i0, ch[c].n, nullptr, atm, natm, bas, nbas, env, 0);
             us_build += (int64_t)(1e3 * since(tb));
             if (r) { fail(c, r, cintgpu_last_error()); delete P; return; }
@@ -1931,6 +1977,7 @@ extern "C" int cg_eri_tables(int li, int lj, int lk, int ll, int *info, int *gro
 }
 
 CINTGPUPlan *cg_plan_new(void) { return new CINTGPUPlan(); }
+void cg_plan_separate_output(CINTGPUPlan *P) { P->fuse_out = false; }
 void cg_plan_free_host(CINTGPUPlan *P) { P->dbuf = nullptr; delete P; }
 
 int cg_plan_build(CINTGPUPlan *P, int kind, const int *shls, int64_t n, const int64_t *offsets,

@@ -14,6 +14,9 @@ void cg_plan_free_host(CINTGPUPlan *P);
 int cg_plan_build(CINTGPUPlan *P, int kind, const int *shls, int64_t n, const int64_t *offsets,
                   const int *atm, int natm, const int *bas, int nbas, const double *env,
                   int64_t split_target);
+/* transform outputs in a separate kernel instead of inside the integral kernel (smaller device
+ * footprint: no per-warp transform scratch for the integral kernel's warps) */
+void cg_plan_separate_output(CINTGPUPlan *P);
 size_t cg_plan_bytes(const CINTGPUPlan *P);
 /* lay the plan out in a caller-owned device region and copy its host images there
  * (stream-ordered, from pageable memory); allocates no device memory */

@@ -67,6 +67,7 @@ extern "C" int cintgpu_int2e_sph_noalloc(double *out_dev, const int *shls, int64
     rc = noalloc_region(&region);
     if (rc) return rc;
     CINTGPUPlan *P = cg_plan_new();
+    cg_plan_separate_output(P);   /* keeps the footprint inside the static array */
     int64_t split = n < (int64_t)cg_sm_count() * 16 ? (int64_t)cg_sm_count() * 8 : 0;
     rc = cg_plan_build(P, CINTGPU_INT2E_SPH, shls, n, nullptr, atm, natm, bas, nbas, env, split);
     if (!rc) {

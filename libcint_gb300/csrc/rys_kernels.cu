@@ -189,6 +189,119 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
     if (lane == 0) P.nonempty[tk.out] = 1;
 }
 
+/* ------------------------------------------------------------------ output transform */
+/* One warp, one contracted quartet: sum its slices, run the class's horizontal transfer (int2e /
+ * int3c2e accumulators), transform j, l, k, i to real spherical harmonics (c2s_sph_2e1 /
+ * c2s_sph_3c2e1 semantics, src/cart2sph.c:5324-5383, 5884-5925) and store with the task's strides;
+ * an empty quartet is zero-filled (c2s_dset0).  Scratch per warp: s1, s2 (nf_max each), then two
+ * transfer buffers sharing the rest of spw.  peer_slots: slices were written by other warps of the
+ * running kernel, so they are read past L1. */
+__device__ __forceinline__ void c2s_pass(const double *__restrict__ src, double *__restrict__ dst,
+                                         int lsh, int sph, int inner, int ncart_t, int outer, int lane)
+{
+    /* src[(a, t, b)] with a < inner, t < ncart_t, b < outer  ->  dst[(a, m, b)] */
+    int nm = sph ? (lsh <= 1 ? ncart_t : 2 * lsh + 1) : ncart_t;
+    int total = inner * nm * outer;
+    for (int e = lane; e < total; e += 32) {
+        int a = e % inner, rest = e / inner;
+        int m = rest % nm, b = rest / nm;
+        double v;
+        if (!sph || lsh <= 1) {
+            v = src[(size_t)(b * ncart_t + m) * inner + a];
+        } else {
+            int row = lsh * lsh + m;     /* rows of l start at l^2 (sum of 2l'+1 for l' < l) */
+            int nnz = g_c2s_nnz[row];
+            v = 0.0;
+            for (int z = 0; z < nnz; z++) {
+                v = fma(g_c2s_val[row * C2S_MAXNNZ + z],
+                        src[(size_t)(b * ncart_t + g_c2s_idx[row * C2S_MAXNNZ + z]) * inner + a], v);
+            }
+        }
+        dst[(size_t)(b * nm + m) * inner + a] = v;
+    }
+}
+
+__device__ inline void cg_out_quartet(const CGOutTask &o, bool ne, bool peer_slots, double *gctr,
+                                      const CGEriClass *__restrict__ eclass,
+                                      const int *__restrict__ eperm, const int *__restrict__ hprog,
+                                      double *out, int ncomp, int64_t comp_stride, double *s1,
+                                      int64_t nf_max, int64_t spw, int lane)
+{
+    double *s2 = s1 + nf_max;
+    double *h1 = s2 + nf_max;
+    double *h2 = h1 + (spw - 2 * nf_max) / 2;
+    const int sph = o.flags & 1;
+    int nfc[4], nd[4];
+    for (int a = 0; a < 4; a++) {
+        nfc[a] = ncart(o.l[a]);
+        nd[a] = sph ? (o.l[a] <= 1 ? nfc[a] : 2 * o.l[a] + 1) : nfc[a];
+    }
+    const int nf = nfc[0] * nfc[1] * nfc[2] * nfc[3];
+    const bool e0f0 = (o.flags & 2) != 0;
+    CGEriClass ec;
+    memset(&ec, 0, sizeof(ec));
+    if (e0f0) ec = eclass[o.ecls];
+    const int slot = e0f0 ? ec.nE * ec.nF : nf;   /* accumulators per part and component */
+    for (int comp = 0; comp < ncomp; comp++) {
+        double *g0 = gctr + o.cart_off + (size_t)comp * slot;
+        if (ne && o.nparts > 1) {
+            for (int c = lane; c < slot; c += 32) {
+                double v = peer_slots ? __ldcg(g0 + c) : g0[c];
+                for (int p = 1; p < o.nparts; p++) {
+                    const double *gp = g0 + (size_t)p * ncomp * slot + c;
+                    v += peer_slots ? __ldcg(gp) : *gp;
+                }
+                g0[c] = v;
+            }
+            __syncwarp();
+        }
+        double *dst = out + o.out_off + (size_t)comp * comp_stride;
+        if (!ne) {
+            int tot = nd[0] * nd[1] * nd[2] * nd[3];
+            for (int e = lane; e < tot; e += 32) {
+                int i = e % nd[0], r = e / nd[0];
+                int j = r % nd[1]; r /= nd[1];
+                int k = r % nd[2], l = r / nd[2];
+                dst[(int64_t)i * o.st[0] + (int64_t)j * o.st[1] + (int64_t)k * o.st[2]
+                    + (int64_t)l * o.st[3]] = 0.0;
+            }
+            continue;
+        }
+        /* a single slice written by another warp: read it past L1 through the transfer's gather */
+        if (peer_slots && o.nparts == 1) {
+            for (int c = lane; c < slot; c += 32) g0[c] = __ldcg(g0 + c);
+            __syncwarp();
+        }
+        /* gctr order: i fastest, then k, l, j.  Pass j: inner = nfi*nfk*nfl, t = j */
+        const double *cur = g0;
+        if (e0f0)
+            cur = cg_hrr(g0, eperm + ec.perm_off, eperm + ec.perm_off + ec.nE,
+                         hprog + ec.hprog_off, o.l[0], o.l[1], o.l[2], o.l[3], o.AB, o.CD,
+                         h1, h2, lane);
+        c2s_pass(cur, s1, o.l[1], sph, nfc[0] * nfc[2] * nfc[3], nfc[1], 1, lane);
+        __syncwarp();
+        /* pass l: (i,k | l | js) */
+        c2s_pass(s1, s2, o.l[3], sph, nfc[0] * nfc[2], nfc[3], nd[1], lane);
+        __syncwarp();
+        /* pass k: (i | k | ls, js) */
+        c2s_pass(s2, s1, o.l[2], sph, nfc[0], nfc[2], nd[3] * nd[1], lane);
+        __syncwarp();
+        /* pass i: (1 | i | ks, ls, js) */
+        c2s_pass(s1, s2, o.l[0], sph, 1, nfc[0], nd[2] * nd[3] * nd[1], lane);
+        __syncwarp();
+        /* s2 layout: (is, ks, ls, js) */
+        int tot = nd[0] * nd[2] * nd[3] * nd[1];
+        for (int e = lane; e < tot; e += 32) {
+            int i = e % nd[0], r = e / nd[0];
+            int k = r % nd[2]; r /= nd[2];
+            int l = r % nd[3], j = r / nd[3];
+            dst[(int64_t)i * o.st[0] + (int64_t)j * o.st[1] + (int64_t)k * o.st[2]
+                + (int64_t)l * o.st[3]] = s2[e];
+        }
+        __syncwarp();
+    }
+}
+
 /* ---------------------------------------------------------- contraction-first int2e path */
 /* Stage 3 of one group over terms t_begin, t_begin + tstep, ... < Tb: p = gx gy once, then
  * r[b * 4 + a] += p gz(ez0 + a, fz0 + b) for the group's nez x nfz members (MA x MB bound). */
@@ -415,116 +528,41 @@ rys_eri_kernel(CGLaunch P)
         else if (ns <= 1) run_task<MODE, 1>(P, tk, L, term, greg, lane);
         else if (ns <= 4) run_task<MODE, 4>(P, tk, L, term, greg, lane);
         else run_task<MODE, 0>(P, tk, L, term, greg, lane);
+        if (P.fuse_out) {
+            /* publish this slice; the warp completing the quartet's last slice transforms it
+             * (slot writes fenced before the count, reads past L1 after it) */
+            __syncwarp();
+            __threadfence();
+            int last = 0;
+            if (lane == 0) last = atomicAdd(P.done + tk.out, 1) == P.outs[tk.out].nparts - 1;
+            last = __shfl_sync(FULL, last, 0);
+            if (last) {
+                __threadfence();
+                const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+                cg_out_quartet(P.outs[tk.out], true, true, P.gctr, P.eclass, P.eperm, P.hprog, P.out,
+                               P.ncomp, P.comp_stride, P.oscr + (size_t)gw * P.oscr_stride, P.nf_max,
+                               P.oscr_stride, lane);
+            }
+        }
     }
 }
 
 /* ------------------------------------------------------------------ output kernel */
-/* One warp per contracted quartet: sum partial slots, then transform the four indices one at a
- * time (j, l, k, i as c2s_sph_2e1 does) through a per-warp scratch in global memory, and store
- * with the task's strides. */
-__device__ __forceinline__ void c2s_pass(const double *__restrict__ src, double *__restrict__ dst,
-                                         int lsh, int sph, int inner, int ncart_t, int outer, int lane)
-{
-    /* src[(a, t, b)] with a < inner, t < ncart_t, b < outer  ->  dst[(a, m, b)] */
-    int nm = sph ? (lsh <= 1 ? ncart_t : 2 * lsh + 1) : ncart_t;
-    int total = inner * nm * outer;
-    for (int e = lane; e < total; e += 32) {
-        int a = e % inner, rest = e / inner;
-        int m = rest % nm, b = rest / nm;
-        double v;
-        if (!sph || lsh <= 1) {
-            v = src[(size_t)(b * ncart_t + m) * inner + a];
-        } else {
-            int row = lsh * lsh + m;     /* rows of l start at l^2 (sum of 2l'+1 for l' < l) */
-            int nnz = g_c2s_nnz[row];
-            v = 0.0;
-            for (int z = 0; z < nnz; z++) {
-                v = fma(g_c2s_val[row * C2S_MAXNNZ + z],
-                        src[(size_t)(b * ncart_t + g_c2s_idx[row * C2S_MAXNNZ + z]) * inner + a], v);
-            }
-        }
-        dst[(size_t)(b * nm + m) * inner + a] = v;
-    }
-}
-
 __global__ void __launch_bounds__(128)
-cg_output_kernel(const CGOutTask *__restrict__ ot, int nout, double *gctr, const int *nonempty,
-                 double *scratch, int64_t scratch_per_warp, int64_t nf_max,
-                 const CGEriClass *__restrict__ eclass, const int *__restrict__ eperm,
-                 const int *__restrict__ hprog, double *out, int ncomp, int64_t comp_stride)
+cg_output_kernel(const CGOutTask *__restrict__ ot, const int *__restrict__ idx, int nout,
+                 double *gctr, const int *nonempty, double *scratch, int64_t scratch_per_warp,
+                 int64_t nf_max, const CGEriClass *__restrict__ eclass,
+                 const int *__restrict__ eperm, const int *__restrict__ hprog, double *out,
+                 int ncomp, int64_t comp_stride)
 {
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     double *s1 = scratch + (size_t)gw * scratch_per_warp;
-    double *s2 = s1 + nf_max;
-    double *h1 = s2 + nf_max;
-    double *h2 = h1 + (scratch_per_warp - 2 * nf_max) / 2;
-    for (int q = gw; q < nout; q += nw) {
-        const CGOutTask o = ot[q];
-        const int sph = o.flags & 1;
-        int nfc[4], nd[4];
-        for (int a = 0; a < 4; a++) {
-            nfc[a] = ncart(o.l[a]);
-            nd[a] = sph ? (o.l[a] <= 1 ? nfc[a] : 2 * o.l[a] + 1) : nfc[a];
-        }
-        const int nf = nfc[0] * nfc[1] * nfc[2] * nfc[3];
-        const bool ne = nonempty[q] != 0;
-        const bool e0f0 = (o.flags & 2) != 0;
-        CGEriClass ec;
-        memset(&ec, 0, sizeof(ec));
-        if (e0f0) ec = eclass[o.ecls];
-        const int slot = e0f0 ? ec.nE * ec.nF : nf;   /* accumulators per part and component */
-        for (int comp = 0; comp < ncomp; comp++) {
-            double *g0 = gctr + o.cart_off + (size_t)comp * slot;
-            if (ne && o.nparts > 1) {
-                for (int c = lane; c < slot; c += 32) {
-                    double v = g0[c];
-                    for (int p = 1; p < o.nparts; p++) v += g0[(size_t)p * ncomp * slot + c];
-                    g0[c] = v;
-                }
-                __syncwarp();
-            }
-            double *dst = out + o.out_off + (size_t)comp * comp_stride;
-            if (!ne) {
-                int tot = nd[0] * nd[1] * nd[2] * nd[3];
-                for (int e = lane; e < tot; e += 32) {
-                    int i = e % nd[0], r = e / nd[0];
-                    int j = r % nd[1]; r /= nd[1];
-                    int k = r % nd[2], l = r / nd[2];
-                    dst[(int64_t)i * o.st[0] + (int64_t)j * o.st[1] + (int64_t)k * o.st[2]
-                        + (int64_t)l * o.st[3]] = 0.0;
-                }
-                continue;
-            }
-            /* gctr order: i fastest, then k, l, j.  Pass j: inner = nfi*nfk*nfl, t = j */
-            const double *cur = g0;
-            if (e0f0)
-                cur = cg_hrr(g0, eperm + ec.perm_off, eperm + ec.perm_off + ec.nE,
-                             hprog + ec.hprog_off, o.l[0], o.l[1], o.l[2], o.l[3], o.AB, o.CD,
-                             h1, h2, lane);
-            c2s_pass(cur, s1, o.l[1], sph, nfc[0] * nfc[2] * nfc[3], nfc[1], 1, lane);
-            __syncwarp();
-            /* pass l: (i,k | l | js) */
-            c2s_pass(s1, s2, o.l[3], sph, nfc[0] * nfc[2], nfc[3], nd[1], lane);
-            __syncwarp();
-            /* pass k: (i | k | ls, js) */
-            c2s_pass(s2, s1, o.l[2], sph, nfc[0], nfc[2], nd[3] * nd[1], lane);
-            __syncwarp();
-            /* pass i: (1 | i | ks, ls, js) */
-            c2s_pass(s1, s2, o.l[0], sph, 1, nfc[0], nd[2] * nd[3] * nd[1], lane);
-            __syncwarp();
-            /* s2 layout: (is, ks, ls, js) */
-            int tot = nd[0] * nd[2] * nd[3] * nd[1];
-            for (int e = lane; e < tot; e += 32) {
-                int i = e % nd[0], r = e / nd[0];
-                int k = r % nd[2]; r /= nd[2];
-                int l = r % nd[3], j = r / nd[3];
-                dst[(int64_t)i * o.st[0] + (int64_t)j * o.st[1] + (int64_t)k * o.st[2]
-                    + (int64_t)l * o.st[3]] = s2[e];
-            }
-            __syncwarp();
-        }
+    for (int k = gw; k < nout; k += nw) {
+        const int q = idx ? idx[k] : k;
+        cg_out_quartet(ot[q], nonempty[q] != 0, false, gctr, eclass, eperm, hprog, out, ncomp,
+                       comp_stride, s1, nf_max, scratch_per_warp, lane);
     }
 }
 
@@ -577,13 +615,13 @@ extern "C" int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStrea
     return (int)cudaGetLastError();
 }
 
-extern "C" int cg_launch_output(const CGOutTask *ot, int nout, double *gctr, const int *nonempty,
+extern "C" int cg_launch_output(const CGOutTask *ot, const int *idx, int nout, double *gctr, const int *nonempty,
                                 double *scratch, int64_t scratch_per_warp, int64_t nf_max,
                                 const CGEriClass *eclass, const int *eperm, const int *hprog,
                                 int nblocks, double *out, int ncomp, int64_t comp_stride,
                                 cudaStream_t stream)
 {
-    cg_output_kernel<<<nblocks, 128, 0, stream>>>(ot, nout, gctr, nonempty, scratch,
+    cg_output_kernel<<<nblocks, 128, 0, stream>>>(ot, idx, nout, gctr, nonempty, scratch,
                                                   scratch_per_warp, nf_max, eclass, eperm, hprog,
                                                   out, ncomp, comp_stride);
     return (int)cudaGetLastError();

@@ -52,6 +52,15 @@ typedef struct {
     const int *eperm;
     const int *hprog;
     const int *eround;
+    /* fused output: the warp that finishes a quartet's last slice transforms and stores it */
+    int fuse_out;
+    const CGOutTask *outs;
+    int *done;                /* finished slices per output quartet */
+    double *oscr;             /* per-warp transform scratch */
+    int64_t oscr_stride, nf_max;
+    double *out;
+    int ncomp;
+    int64_t comp_stride;
     int64_t hrr_off1, hrr_off2;   /* J mode: transfer buffers inside the warp's slot */
 } CGLaunch;
 
@@ -89,9 +98,9 @@ int cg_blocks_per_sm(int mode, int ws_doubles);
 int cg_rys_deg(void);
 void cg_layout(int li, int lj, int lk, int ll, int mode, int ws_doubles, CGLayout *L);
 int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStream_t stream);
-/* scratch per warp: two cart->sph buffers of nf_max doubles, then two transfer buffers of
- * (scratch_per_warp - 2 nf_max) / 2 doubles */
-int cg_launch_output(const CGOutTask *ot, int nout, double *gctr, const int *nonempty,
+/* idx: the output quartets to transform (NULL: all nout); scratch per warp: two cart->sph buffers
+ * of nf_max doubles, then two transfer buffers of (scratch_per_warp - 2 nf_max) / 2 doubles */
+int cg_launch_output(const CGOutTask *ot, const int *idx, int nout, double *gctr, const int *nonempty,
                      double *scratch, int64_t scratch_per_warp, int64_t nf_max,
                      const CGEriClass *eclass, const int *eperm, const int *hprog, int nblocks,
                      double *out, int ncomp, int64_t comp_stride, cudaStream_t stream);
