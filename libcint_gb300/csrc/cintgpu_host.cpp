@@ -198,19 +198,54 @@ double common_fac_sp(int l)    /* src/g1e.c:565-572 */
     return l == 0 ? 0.282094791773878143 : l == 1 ? 0.488602511902919921 : 1.0;
 }
 
-struct PairKey {
-    int a, ca, b, cb, lsum, kind;
-    bool operator==(const PairKey &o) const
+/* shell-pair key packed into 60 bits: shell indices + 1 (21 bits each), contraction columns
+ * (6 bits each), the l ceiling entering libcint's log_rr (5 bits), pair kind (1 bit) */
+inline uint64_t pair_key(int a, int ca, int b, int cb, int lsum, int kind)
+{
+    return (uint64_t)(a + 1) | ((uint64_t)(b + 1) << 21) | ((uint64_t)ca << 42) | ((uint64_t)cb << 48)
+           | ((uint64_t)lsum << 54) | ((uint64_t)kind << 59);
+}
+const int PAIR_KEY_MAX_SHELL = (1 << 21) - 2;
+
+/* open-addressing map from packed pair keys (never 0) to pair ids */
+struct PairMap {
+    std::vector<uint64_t> keys;
+    std::vector<int> vals;
+    size_t mask = 0, n = 0;
+    static uint64_t mix(uint64_t x)
     {
-        return a == o.a && ca == o.ca && b == o.b && cb == o.cb && lsum == o.lsum && kind == o.kind;
+        x ^= x >> 33; x *= 0xff51afd7ed558ccdULL;
+        x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL;
+        return x ^ (x >> 33);
     }
-};
-struct PairKeyHash {
-    size_t operator()(const PairKey &k) const
+    int find(uint64_t k) const
     {
-        uint64_t h = (uint64_t)k.a * 1000003u ^ ((uint64_t)k.b << 21) ^ ((uint64_t)k.ca << 42)
-                   ^ ((uint64_t)k.cb << 50) ^ ((uint64_t)k.lsum << 58) ^ ((uint64_t)k.kind << 62);
-        return std::hash<uint64_t>()(h);
+        if (!mask) return -1;
+        for (size_t i = mix(k) & mask;; i = (i + 1) & mask) {
+            if (keys[i] == k) return vals[i];
+            if (keys[i] == 0) return -1;
+        }
+    }
+    void insert(uint64_t k, int v)
+    {
+        if (2 * (n + 1) > mask + 1) {
+            std::vector<uint64_t> ok;
+            std::vector<int> ov;
+            ok.swap(keys);
+            ov.swap(vals);
+            size_t cap = std::max<size_t>(1024, 2 * (mask + 1));
+            keys.assign(cap, 0);
+            vals.assign(cap, 0);
+            mask = cap - 1;
+            n = 0;
+            for (size_t i = 0; i < ok.size(); i++)
+                if (ok[i]) insert(ok[i], ov[i]);
+        }
+        size_t i = mix(k) & mask;
+        while (keys[i]) i = (i + 1) & mask;
+        keys[i] = k;
+        vals[i] = v;
+        n++;
     }
 };
 
@@ -308,7 +343,7 @@ struct Builder {
     int natm;
     const int *bas;
     const double *env;
-    std::unordered_map<PairKey, int, PairKeyHash> pair_index;
+    PairMap pair_index;
     std::vector<char> pair_empty;
     std::unordered_map<int, std::vector<double>> logmaxc;   /* per original shell */
     const std::vector<int> *ao_loc = nullptr;     /* Cartesian AO offset per shell (J/adjoint) */
@@ -344,9 +379,9 @@ struct Builder {
     /* ordered pair (A col ca, B col cb); lsum = l ceilings entering libcint's log_rr */
     int pair(int sa, const ShellView &A, int ca, int sb, const ShellView &B, int cb, int lsum)
     {
-        PairKey key{sa, ca, sb, cb, lsum, 0};
-        auto it = pair_index.find(key);
-        if (it != pair_index.end()) return it->second;
+        const uint64_t key = pair_key(sa, ca, sb, cb, lsum, 0);
+        const int found = pair_index.find(key);
+        if (found >= 0) return found;
         CGPair p;
         for (int c = 0; c < 3; c++) { p.AB[c] = A.R[c] - B.R[c]; p.A[c] = A.R[c]; }
         p.prim_off = (int)P->prims.size();
@@ -386,16 +421,16 @@ struct Builder {
         int id = (int)P->pairs.size();
         P->pairs.push_back(p);
         pair_empty.push_back(empty ? 1 : 0);
-        pair_index.emplace(key, id);
+        pair_index.insert(key, id);
         return id;
     }
 
     /* the ket of int3c2e: shell k with a zero-exponent s partner; no ket screening */
     int single(int sk, const ShellView &K, int ck)
     {
-        PairKey key{sk, ck, -1, 0, 0, 1};
-        auto it = pair_index.find(key);
-        if (it != pair_index.end()) return it->second;
+        const uint64_t key = pair_key(sk, ck, -1, 0, 0, 1);
+        const int found = pair_index.find(key);
+        if (found >= 0) return found;
         CGPair p;
         for (int c = 0; c < 3; c++) { p.AB[c] = 0.0; p.A[c] = K.R[c]; }
         p.prim_off = (int)P->prims.size();
@@ -414,7 +449,7 @@ struct Builder {
         int id = (int)P->pairs.size();
         P->pairs.push_back(p);
         pair_empty.push_back(0);
-        pair_index.emplace(key, id);
+        pair_index.insert(key, id);
         return id;
     }
 };
@@ -773,6 +808,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         for (int a = 0; a < nsh; a++) {
             int rc = read_shell(s[a], atm, natm, bas, env, &sv[a]);
             if (rc) return rc;
+            if (s[a] > PAIR_KEY_MAX_SHELL) { set_error("shell index %d above %d", s[a], PAIR_KEY_MAX_SHELL); return CINTGPU_ERR_ARG; }
             if (contracting && s[a] >= nbas) { set_error("shell %d outside nbas %d", s[a], nbas); return CINTGPU_ERR_ARG; }
             if (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) {
                 if (sv[a].l > 4) { set_error("adjoint supports l <= 4 (shell %d has %d)", s[a], sv[a].l); return CINTGPU_ERR_UNSUPPORTED; }
@@ -854,6 +890,13 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     struct Work { int pe; int64_t off, n; double cost_pq; };
     std::vector<Work> work;
     work.reserve(pend.size());
+    /* per-class constants, indexed by ((li 8 + lj) 8 + lk) 8 + ll (l <= 7 with derivatives) */
+    std::vector<double> cls_cost(8 * 8 * 8 * 8, -1.0), cls_ref(8 * 8 * 8 * 8, 0.0);
+    {
+        int64_t npq_all = 0;
+        for (const Pending &pe : pend) npq_all += pe.npq;
+        P->pqlist.reserve((size_t)npq_all);
+    }
     double fl = 0;
     for (size_t w = 0; w < pend.size(); w++) {
         const Pending &pe = pend[w];
@@ -861,16 +904,26 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         const CGPrimPair *pa = &P->prims[a.prim_off], *pb = &P->prims[b.prim_off];
         int nij = a.npa * a.npb, nkl = b.npa * b.npb;
         int64_t off = (int64_t)P->pqlist.size();
+        P->pqlist.resize((size_t)off + (size_t)nij * nkl);
+        int *dst = P->pqlist.data() + off;
+        int m = 0;
         for (int kl = 0; kl < nkl; kl++) {
-            double ck = pb[kl].cce;
+            const double ck = pb[kl].cce;
             if (ck > P->expcutoff) continue;
+            const double lim = P->expcutoff - ck;
             for (int ij = 0; ij < nij; ij++)
-                if (!(pa[ij].cce > P->expcutoff - ck)) P->pqlist.push_back(kl * nij + ij);
+                if (!(pa[ij].cce > lim)) dst[m++] = kl * nij + ij;
         }
+        P->pqlist.resize((size_t)off + m);
         int64_t n = (int64_t)P->pqlist.size() - off;
-        double cpq = flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode);
+        const int ck = ((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3];
+        if (cls_cost[ck] < 0) {
+            cls_cost[ck] = flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode);
+            cls_ref[ck] = P->mode == CG_MODE_ERI ? flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3]) : 0.0;
+        }
+        const double cpq = cls_cost[ck];
         fl += n * cpq;
-        if (P->mode == CG_MODE_ERI) P->flops_ref += n * flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3]);
+        P->flops_ref += n * cls_ref[ck];
         if (n > 0) work.push_back({(int)w, off, n, cpq});
     }
     if (P->pqlist.size() > (size_t)INT32_MAX) { set_error("too many primitive quartets in one plan"); return CINTGPU_ERR_ARG; }
@@ -886,19 +939,27 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         int kb = atoi(e);
         if (kb >= 8 && kb <= 48) ws_small = kb * 1024 / 8;
     }
+    std::vector<int> cls_group(8 * 8 * 8 * 8, -1);
+    std::vector<CGLayout> cls_layout(8 * 8 * 8 * 8);
     struct TaskCost { CGTask t; double cost; int group; };
     std::vector<TaskCost> tc;
     std::unordered_map<int, int> grad_cls, eri_cls;
     int64_t gpos = 0;
     for (const Work &w : work) {
         const Pending &pe = pend[w.pe];
-        CGLayout L;
-        cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, ws_small, &L);
-        int group = 0;
-        if (L.T < 2) {
-            cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_MAX, &L);
-            group = 1;
+        const int ck = ((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3];
+        if (cls_group[ck] < 0) {
+            CGLayout Lc;
+            cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, ws_small, &Lc);
+            cls_group[ck] = 0;
+            if (Lc.T < 2) {
+                cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_MAX, &Lc);
+                cls_group[ck] = 1;
+            }
+            cls_layout[ck] = Lc;
         }
+        const CGLayout &L = cls_layout[ck];
+        const int group = cls_group[ck];
         if (L.nroots > cg_rys_nmax() || L.T < 1 || L.G >= 1024) {
             set_error("class (%d %d|%d %d) beyond the kernel limits (nroots %d, max %d)",
                       pe.l[0], pe.l[1], pe.l[2], pe.l[3], L.nroots, cg_rys_nmax());
@@ -1658,6 +1719,7 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
     struct Chunk {
         int64_t i0 = 0, n = 0, base = 0, out_size = 0;
         int ncomp = 1;
+        double t_ready = 0, t_enq = 0;     /* ms since the call started (trace) */
         CINTGPUPlan *P = nullptr;
         DevLayout D;
         int rc = 0;
@@ -1733,6 +1795,7 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
             ch[c].D = D;
             ch[c].out_size = P->out_size;
             ch[c].ncomp = P->ncomp;
+            ch[c].t_ready = since(t_start);
             ch[c].image = true;
             cv.notify_all();
         }
@@ -1786,6 +1849,7 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
             P = ch[c].P;
         }
         auto t0 = clk::now();
+        ch[c].t_enq = since(t_start);
         const DevLayout &D = ch[c].D;
         const size_t outb = sizeof(double) * std::max<int64_t>(P->out_size * P->ncomp, 1);
         int r;
@@ -1836,6 +1900,11 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
                         "planning %.1f, images %.1f, first image at %.1f\n",
                 (long long)n, C, nbuild, t_image, t_slot, t_enqueue, since(t_start), 1e-3 * us_build,
                 1e-3 * us_image, 1e-3 * us_first);
+    if (trace) {
+        fprintf(stderr, "cintgpu_batch_host chunks (items: image ready / enqueued, ms):");
+        for (int c = 0; c < C; c++) fprintf(stderr, " %lld:%.1f/%.1f", (long long)ch[c].n, ch[c].t_ready, ch[c].t_enq);
+        fprintf(stderr, "\n");
+    }
     return rc;
 }
 
