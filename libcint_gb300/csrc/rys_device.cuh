@@ -51,6 +51,7 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     int inc[4];
     cg_mode_incs(mode, inc);
     L->lic = li + inc[0];
+    L->termw = mode == CG_MODE_GRAD || mode == CG_MODE_GRADA ? CG_TERMW_GRAD : CG_TERMW;
     const int ljc = lj + inc[1], lkc = lk + inc[2], llc = ll + inc[3];
     /* every product the adjoint forms raises ONE center (by 1 for a coordinate, by 2 for an
      * exponent), so the quadrature needs only that much above li+lj+lk+ll even though the g
@@ -70,15 +71,18 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     const bool grad = mode == CG_MODE_GRAD || mode == CG_MODE_GRADA;
     int T = 0;
     if (mode == CG_MODE_ERI) {
-        /* contraction first: per term only the VRR arrays g(e, f), e <= li+lj, f <= lk+ll */
+        /* contraction first: per term only the VRR arrays g(e, f), e <= li+lj, f <= lk+ll; term
+         * records hold the 10 stage-1 values and m b01 for m <= mmax (odd length) */
         L->G = (L->nmax + 1) * (L->mmax + 1);
         L->scr = 0;
         L->gstride = 3 * L->G + ((3 * L->G) % 2 == 0 ? 1 : 0);
-        T = (ws_doubles - CG_TERMW * 32) / L->gstride;
+        L->termw = 10 + L->mmax + 1;
+        if (L->termw % 2 == 0) L->termw++;
+        T = ws_doubles / (L->termw + L->gstride);
         if (T > 32) T = 32;
         if (T < 0) T = 0;
         L->off_dij = L->off_dkl = L->off_aacc = L->off_w = L->off_scr = 0;
-        L->off_g = CG_TERMW * 32;
+        L->off_g = T * L->termw;
     } else if (!grad) {
         int avail = ws_doubles - CG_TERMW * 32;     /* term records */
         /* T terms need T*3*ng*G doubles of g arrays and min(32, 3T) lane scratch areas */
@@ -221,35 +225,32 @@ __device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10
 
 
 /* VRR only (contraction-first path): g(a, m) = out[a + (nmax+1) m] for a <= nmax, m <= mmax,
- * written straight into the term's g array (libcint CINTg0_2e_2d, src/g2e.c:272-330). */
-__device__ __forceinline__ void vrr_axis(int nmax, int mmax, double b00, double b10, double b01,
-                                         double c00, double c0p, double g00, double *out)
+ * written straight into the term's g array (libcint CINTg0_2e_2d, src/g2e.c:272-330):
+ *   g(a+1, 0)   = c00 g(a, 0) + a b10 g(a-1, 0)
+ *   g(a, m+1)   = c0p g(a, m) + m b01 g(a, m-1) + a b00 g(a-1, m)
+ * computed column by column (a outer), so a b00 is one running sum per column, and m b01 comes
+ * from mb[] (computed once per term for the three axes): 3 FP64 operations per entry. */
+__device__ __forceinline__ void vrr_axis(int nmax, int mmax, double b00, double b10,
+                                         const double *__restrict__ mb, double c00, double c0p,
+                                         double g00, double *out)
 {
     const int na = nmax + 1;
     out[0] = g00;
-    if (nmax > 0) {
-        double p0 = g00, p1 = c00 * g00, nb = b10;
-        out[1] = p1;
-        for (int a = 1; a < nmax; a++) {
-            double p2 = fma(c00, p1, nb * p0);
-            out[a + 1] = p2;
-            p0 = p1; p1 = p2;
-            nb += b10;
+    if (mmax > 0) out[na] = c0p * g00;
+    for (int m = 1; m < mmax; m++)
+        out[(m + 1) * na] = fma(mb[m], out[(m - 1) * na], c0p * out[m * na]);
+    double nb = 0.0, ab = b00;       /* (a-1) b10, a b00 */
+    for (int a = 1; a <= nmax; a++) {
+        double v0 = c00 * out[a - 1];
+        if (a >= 2) v0 = fma(nb, out[a - 2], v0);
+        out[a] = v0;
+        for (int m = 0; m < mmax; m++) {
+            double v = fma(ab, out[a - 1 + m * na], c0p * out[a + m * na]);
+            if (m > 0) v = fma(mb[m], out[a + (m - 1) * na], v);
+            out[a + (m + 1) * na] = v;
         }
-    }
-    double mb = 0.0;
-    for (int m = 0; m < mmax; m++) {
-        const double *cm = out + m * na;
-        double *cn = out + (m + 1) * na;
-        double ab = 0.0;                  /* a * b00 */
-        for (int a = 0; a <= nmax; a++) {
-            double v = c0p * cm[a];
-            if (m > 0) v = fma(mb, cm[a - na], v);
-            if (a > 0) v = fma(ab, cm[a - 1], v);
-            cn[a] = v;
-            ab += b00;
-        }
-        mb += b01;
+        nb += b10;
+        ab += b00;
     }
 }
 

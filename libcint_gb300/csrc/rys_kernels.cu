@@ -393,15 +393,18 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
             int p = g / n, rr = g - p * n;
             int q = __ldg(pql + p);
             int kl = q / nij, ij = q - kl * nij;
-            cg_term(ppij[ij], ppkl[kl], pij, pkl, n, rr, common, P.rys_coef, term + lane * CG_TERMW);
+            double *rec = term + lane * L.termw;
+            cg_term(ppij[ij], ppkl[kl], pij, pkl, n, rr, common, P.rys_coef, rec);
+            double mb = 0.0;
+            for (int m = 0; m <= L.mmax; m++) { rec[10 + m] = mb; mb += rec[2]; }   /* m b01 */
         }
         __syncwarp();
         /* ---- stage 2: one lane per (term, axis), VRR only */
         for (int item = lane; item < 3 * Tb; item += 32) {
             int t = item / 3, ax = item - 3 * t;
-            const double *rec = term + t * CG_TERMW;
+            const double *rec = term + t * L.termw;
             double g00 = (ax == 2) ? rec[9] : 1.0;
-            vrr_axis(L.nmax, L.mmax, rec[0], rec[1], rec[2], rec[3 + ax], rec[6 + ax], g00,
+            vrr_axis(L.nmax, L.mmax, rec[0], rec[1], rec + 10, rec[3 + ax], rec[6 + ax], g00,
                      greg + (size_t)t * gstride + ax * G);
         }
         __syncwarp();

@@ -23,6 +23,7 @@ typedef struct {
      * cotangent (when kept in shared memory), g arrays, lane scratch */
     int off_dij, off_dkl, off_aacc, off_w, off_g, off_scr;
     int gstride;              /* doubles between consecutive terms' g arrays */
+    int termw;                /* doubles per term record */
 } CGLayout;
 
 typedef struct {
