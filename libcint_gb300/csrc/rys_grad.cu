@@ -154,9 +154,17 @@ rys_grad_kernel(CGGradLaunch P)
                 double dA = fma(-ch.p[0], ga[ch.om[0]], rec[10] * ga[ou + sI]);
                 double dB = fma(-ch.p[1], ga[ch.om[1]], rec[11] * ga[ou + sJ]);
                 double dC = fma(-ch.p[2], ga[ch.om[2]], rec[12] * ga[ou + sK]);
-                gA[a] = fma(H, dA, gA[a]);
-                gB[a] = fma(H, dB, gB[a]);
-                gC[a] = fma(H, dC, gC[a]);
+                /* the axis is a runtime value: select the accumulators (registers, not a local
+                 * array indexed at run time) */
+                double xa = a == 0 ? gA[0] : (a == 1 ? gA[1] : gA[2]);
+                double xb = a == 0 ? gB[0] : (a == 1 ? gB[1] : gB[2]);
+                double xc = a == 0 ? gC[0] : (a == 1 ? gC[1] : gC[2]);
+                xa = fma(H, dA, xa);
+                xb = fma(H, dB, xb);
+                xc = fma(H, dC, xc);
+                if (a == 0) { gA[0] = xa; gB[0] = xb; gC[0] = xc; }
+                else if (a == 1) { gA[1] = xa; gB[1] = xb; gC[1] = xc; }
+                else { gA[2] = xa; gB[2] = xb; gC[2] = xc; }
                 if (MODE == CG_MODE_GRADA) {
                     al0 = -H * ga[ou + 2 * sI];
                     al1 = -H * ga[ou + 2 * sJ];
