@@ -156,74 +156,6 @@ __device__ __forceinline__ void cart_pow(int l, int p, int &lx, int &ly, int &lz
     lz = q;
 }
 
-/* ------------------------------------------------------------------ stage 2 */
-/* One Cartesian axis of one term: VRR into T2[a + (nmax+1) m], then the two horizontal
- * transfers; final g[((i dJ + j) dK + k) dL + l] goes to gout.  Lane scratch: T2, a*b00, and a
- * vector of length mmax+1. */
-__device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10, double b01,
-                                       double c00, double c0p, double g00, double AB, double CD,
-                                       double *scr, double *gout)
-{
-    const int nmax = L.nmax, mmax = L.mmax, na = nmax + 1, nm = mmax + 1;
-    double *T2 = scr;
-    double *ab00 = scr + na * nm;
-    /* a * b00 */
-    {
-        double acc = 0.0;
-        for (int a = 0; a <= nmax; a++) { ab00[a] = acc; acc += b00; }
-    }
-    T2[0] = g00;
-    if (nmax > 0) {
-        double p0 = g00, p1 = c00 * g00, nb = b10;
-        T2[1] = p1;
-        for (int a = 1; a < nmax; a++) {
-            double p2 = fma(c00, p1, nb * p0);
-            T2[a + 1] = p2;
-            p0 = p1; p1 = p2;
-            nb += b10;
-        }
-    }
-    double mb = 0.0;
-    for (int m = 0; m < mmax; m++) {
-        const double *cm = T2 + m * na;
-        const double *cm1 = T2 + (m - 1) * na;
-        double *cn = T2 + (m + 1) * na;
-        for (int a = 0; a <= nmax; a++) {
-            double v = c0p * cm[a];
-            if (m > 0) v = fma(mb, cm1[a], v);
-            if (a > 0) v = fma(ab00[a], cm[a - 1], v);
-            cn[a] = v;
-        }
-        mb += b01;
-    }
-    /* (a,0| -> (i,j| one j level at a time, in place on every column m:
-     * col[a] = col[a+1] + AB col[a]; after level j, row i of all columns is g(i,j,m) and goes
-     * through |m,0) -> |k,l) in a short vector, so no (i,j,m) intermediate is stored. */
-    double *tmp = ab00 + na;
-    for (int j = 0; j < L.dJ; j++) {
-        if (j > 0) {
-            for (int m = 0; m <= mmax; m++) {
-                double *col = T2 + m * na;
-                for (int a = 0; a <= nmax - j; a++) col[a] = fma(AB, col[a], col[a + 1]);
-            }
-        }
-        for (int i = 0; i < L.dI; i++) {
-            double *go = gout + (i * L.dJ + j) * L.dK * L.dL;
-            if (L.dL == 1) {
-                for (int k = 0; k < L.dK; k++) go[k] = T2[i + na * k];
-                continue;
-            }
-            for (int m = 0; m <= mmax; m++) tmp[m] = T2[i + na * m];
-            for (int k = 0; k < L.dK; k++) go[k * L.dL] = tmp[k];
-            for (int l = 1; l < L.dL; l++) {
-                for (int m = 0; m <= mmax - l; m++) tmp[m] = fma(CD, tmp[m], tmp[m + 1]);
-                for (int k = 0; k < L.dK; k++) go[k * L.dL + l] = tmp[k];
-            }
-        }
-    }
-}
-
-
 /* VRR only (contraction-first path): g(a, m) = out[a + (nmax+1) m] for a <= nmax, m <= mmax,
  * written straight into the term's g array (libcint CINTg0_2e_2d, src/g2e.c:272-330):
  *   g(a+1, 0)   = c00 g(a, 0) + a b10 g(a-1, 0)
@@ -253,6 +185,51 @@ __device__ __forceinline__ void vrr_axis(int nmax, int mmax, double b00, double 
         ab += b00;
     }
 }
+
+/* ------------------------------------------------------------------ stage 2 */
+/* One Cartesian axis of one term: VRR into T2[a + (nmax+1) m], then the two horizontal
+ * transfers; final g[((i dJ + j) dK + k) dL + l] goes to gout.  Lane scratch: T2, a*b00, and a
+ * vector of length mmax+1. */
+__device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10, double b01,
+                                       double c00, double c0p, double g00, double AB, double CD,
+                                       double *scr, double *gout)
+{
+    const int nmax = L.nmax, mmax = L.mmax, na = nmax + 1, nm = mmax + 1;
+    double *T2 = scr;
+    /* m b01 in the vector the transfers use later, then the column-order VRR */
+    {
+        double *mbv = scr + na * nm + na;
+        double mb = 0.0;
+        for (int m = 0; m <= mmax; m++) { mbv[m] = mb; mb += b01; }
+        vrr_axis(nmax, mmax, b00, b10, mbv, c00, c0p, g00, T2);
+    }
+    /* (a,0| -> (i,j| one j level at a time, in place on every column m:
+     * col[a] = col[a+1] + AB col[a]; after level j, row i of all columns is g(i,j,m) and goes
+     * through |m,0) -> |k,l) in a short vector, so no (i,j,m) intermediate is stored. */
+    double *tmp = scr + na * nm + na;
+    for (int j = 0; j < L.dJ; j++) {
+        if (j > 0) {
+            for (int m = 0; m <= mmax; m++) {
+                double *col = T2 + m * na;
+                for (int a = 0; a <= nmax - j; a++) col[a] = fma(AB, col[a], col[a + 1]);
+            }
+        }
+        for (int i = 0; i < L.dI; i++) {
+            double *go = gout + (i * L.dJ + j) * L.dK * L.dL;
+            if (L.dL == 1) {
+                for (int k = 0; k < L.dK; k++) go[k] = T2[i + na * k];
+                continue;
+            }
+            for (int m = 0; m <= mmax; m++) tmp[m] = T2[i + na * m];
+            for (int k = 0; k < L.dK; k++) go[k * L.dL] = tmp[k];
+            for (int l = 1; l < L.dL; l++) {
+                for (int m = 0; m <= mmax - l; m++) tmp[m] = fma(CD, tmp[m], tmp[m + 1]);
+                for (int k = 0; k < L.dK; k++) go[k * L.dL + l] = tmp[k];
+            }
+        }
+    }
+}
+
 
 /* components of all shells below l: l (l+1) (l+2) / 6 */
 __host__ __device__ __forceinline__ int ncart_below(int l) { return l * (l + 1) * (l + 2) / 6; }

@@ -24,7 +24,7 @@
 #include "rys_device.cuh"
 
 template <int MODE>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 2)   /* 2 CTAs/SM (shared memory); no register cap below 255 */
 rys_grad_kernel(CGGradLaunch P)
 {
     extern __shared__ double smem[];
