@@ -256,6 +256,7 @@ struct TaskGroup {              /* one kernel launch: tasks [task0, task0 + ntas
     int task0 = 0, ntasks = 0;
     int ws = CG_WS_SMALL;       /* shared-memory doubles per warp */
     int blocks_per_sm = 2;
+    int nblocks = 1;            /* CTAs of the launch (4 warps each) */
 };
 
 struct CINTGPUPlan {
@@ -291,10 +292,13 @@ struct CINTGPUPlan {
     std::vector<int> eround;       /* stage-3 rounds: start | count << 16 | box << 24 */
     std::vector<int> empty_outs;   /* output quartets without any task (zero-filled) */
     bool fuse_out = true;          /* the integral kernel stores finished quartets itself */
+    int prim_l = 4;                /* int2e classes with lj or ll >= prim_l transfer per primitive
+                                      (CINTGPU_PER_PRIMITIVE_L overrides, 0 = every class) */
     int hrr_max = 1;               /* doubles of one transfer buffer, largest class */
     int nef_max = 1;               /* (e0|f0) accumulators, largest class */
     std::vector<int> out_item;     /* item index of each CGOutTask */
-    TaskGroup groups[2];           /* [0] regular classes, [1] classes needing 48 KB per warp */
+    TaskGroup groups[3];           /* [0] regular classes, [1] classes needing 48 KB per warp,
+                                      [2] int2e classes evaluated per primitive (lj or ll >= 4) */
     int64_t gctr_size = 0;
     /* device */
     char *dbuf = nullptr;
@@ -318,7 +322,7 @@ struct CINTGPUPlan {
     double *d_oscr = nullptr;      /* per-warp transform scratch of the integral kernel */
     double *cur_out = nullptr;
     double *d_gctr = nullptr;
-    int *d_counters = nullptr;     /* [0], [1]: task counters of the groups; [2]: status */
+    int *d_counters = nullptr;     /* [0], [1], [3]: task counters of groups 0, 1, 2; [2]: status */
     int *d_nonempty = nullptr;
     double *d_scratch = nullptr;
     int out_blocks = 1;
@@ -750,6 +754,18 @@ static void free_plan_device(CINTGPUPlan *p)
     p->side = nullptr;
 }
 
+/* int2e classes whose horizontal transfer is applied per primitive (libcint's order) instead of
+ * after contraction: with lj or ll >= 4 the 3D transfer of contracted blocks multiplies the
+ * per-axis rounding amplifications and leaves the 1e-12 bar (measured on (ih|ih): 1.2e-12 vs
+ * libcint's 1e-14); kernel order, so lj <= li and ll <= lk */
+static bool per_primitive(const CINTGPUPlan *P, const int *l)
+{
+    if (P->mode != CG_MODE_ERI || (l[1] < P->prim_l && l[3] < P->prim_l)) return false;
+    CGLayout L;   /* the per-primitive g arrays of the largest classes do not fit: (ii|ii) */
+    cg_layout(l[0], l[1], l[2], l[3], CG_MODE_ERIP, CG_WS_MAX, &L);
+    return L.T >= 1 && L.G < 2048;
+}
+
 /* Build the host images. split_target: minimum number of compute tasks wanted (0 = no split). */
 static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, const int64_t *offsets,
                       const int *atm, int natm, const int *bas, int nbas, const double *env,
@@ -757,6 +773,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
 {
     (void)nbas;
     P->kind = kind;
+    if (const char *e = getenv("CINTGPU_PER_PRIMITIVE_L")) P->prim_l = std::max(0, atoi(e));
     switch (kind) {
     case CINTGPU_INT2E_SPH: P->mode = CG_MODE_ERI; P->sph = 1; P->three = 0; break;
     case CINTGPU_INT2E_CART: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; break;
@@ -918,7 +935,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         int64_t n = (int64_t)P->pqlist.size() - off;
         const int ck = ((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3];
         if (cls_cost[ck] < 0) {
-            cls_cost[ck] = flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode);
+            cls_cost[ck] = per_primitive(P, pe.l) ? flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3])
+                                                 : flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode);
             cls_ref[ck] = P->mode == CG_MODE_ERI ? flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3]) : 0.0;
         }
         const double cpq = cls_cost[ck];
@@ -952,7 +970,10 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             CGLayout Lc;
             cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, ws_small, &Lc);
             cls_group[ck] = 0;
-            if (Lc.T < 2) {
+            if (per_primitive(P, pe.l)) {
+                cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], CG_MODE_ERIP, CG_WS_MAX, &Lc);
+                cls_group[ck] = 2;
+            } else if (Lc.T < 2) {
                 cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_MAX, &Lc);
                 cls_group[ck] = 1;
             }
@@ -960,7 +981,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         }
         const CGLayout &L = cls_layout[ck];
         const int group = cls_group[ck];
-        if (L.nroots > cg_rys_nmax() || L.T < 1 || L.G >= 1024) {
+        if (L.nroots > cg_rys_nmax() || L.T < 1 || L.G >= (group == 2 ? 2048 : 1024)) {
             set_error("class (%d %d|%d %d) beyond the kernel limits (nroots %d, max %d)",
                       pe.l[0], pe.l[1], pe.l[2], pe.l[3], L.nroots, cg_rys_nmax());
             return CINTGPU_ERR_UNSUPPORTED;
@@ -985,6 +1006,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             auto it = grad_cls.find(key);
             cls = it != grad_cls.end() ? it->second
                                        : (grad_cls[key] = build_grad_class(P, pe.l[0], pe.l[1], pe.l[2], pe.l[3]));
+        } else if (group == 2) {
+            cls = -1;   /* per primitive: Cartesian slots, no contraction-first tables */
         } else if (P->mode == CG_MODE_ERI) {
             auto it = eri_cls.find(key);
             cls = it != eri_cls.end() ? it->second
@@ -1021,7 +1044,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         return x.cost > y.cost;
     });
     P->tasks.reserve(tc.size());
-    for (int g = 0; g < 2; g++) {
+    for (int g = 0; g < 3; g++) {
         P->groups[g].task0 = (int)P->tasks.size();
         for (const TaskCost &x : tc)
             if (x.group == g) P->tasks.push_back(x.t);
@@ -1029,7 +1052,9 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         P->groups[g].ws = g == 0 ? ws_small : CG_WS_MAX;
         P->groups[g].blocks_per_sm = (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA)
                                          ? cg_grad_blocks_per_sm(P->mode, P->groups[g].ws)
-                                         : cg_blocks_per_sm(P->mode, P->groups[g].ws);
+                                         : cg_blocks_per_sm(g == 2 ? CG_MODE_ERIP : P->mode, P->groups[g].ws);
+        P->groups[g].nblocks = std::min(std::max(1, g_ctx.sm_count) * P->groups[g].blocks_per_sm,
+                                        std::max(1, (P->groups[g].ntasks + 3) / 4));
     }
     P->gctr_size = std::max<int64_t>(gpos, 1);
     P->empty_outs.clear();
@@ -1052,7 +1077,12 @@ struct DevLayout {
 /* the integral kernel transforms and stores finished quartets itself (int2e, int3c2e, ip1) */
 static bool fused(const CINTGPUPlan *P)
 {
-    return P->fuse_out && !P->jmode && (P->mode == CG_MODE_ERI || P->mode == CG_MODE_IP1);
+    if (!P->fuse_out || P->jmode || !(P->mode == CG_MODE_ERI || P->mode == CG_MODE_IP1)) return false;
+    /* one transform slot per launched warp; classes with huge blocks (l = 5, 6) would need
+     * gigabytes, so such plans transform in the separate kernel */
+    const int64_t spw = 2 * (int64_t)P->max_nf + (P->eclass.empty() ? 0 : 2 * (int64_t)P->hrr_max);
+    const int64_t warps = 4 * (int64_t)(P->groups[0].nblocks + P->groups[1].nblocks + P->groups[2].nblocks);
+    return (double)spw * 8.0 * warps <= 512.0 * (1 << 20);
 }
 
 static DevLayout dev_layout(const CINTGPUPlan *P)
@@ -1080,7 +1110,7 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     D.erd = al(sizeof(int) * std::max<size_t>(P->eround.size(), 1));
     D.emp = al(sizeof(int) * std::max<size_t>(P->empty_outs.size(), 1));
     D.done = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
-    D.oscr_warps = fo ? g_ctx.sm_count * 4 * (P->groups[0].blocks_per_sm + P->groups[1].blocks_per_sm) : 0;
+    D.oscr_warps = fo ? 4 * (P->groups[0].nblocks + P->groups[1].nblocks + P->groups[2].nblocks) : 0;
     D.oscr = fo ? al(sizeof(double) * (size_t)D.oscr_warps * D.spw) : 0;
     D.gctr = al(sizeof(double) * P->gctr_size);
     D.cnt = al(sizeof(int) * 4);
@@ -1092,7 +1122,8 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     /* per-warp slots: J mode holds (e0|f0) and two transfer buffers, the adjoint a cotangent */
     D.wstride = P->jmode ? (int64_t)P->nef_max + 2 * (int64_t)P->hrr_max : (int64_t)P->max_nf;
     if (P->jmode || (grad && P->max_nf > CG_W_SMEM)) {
-        D.wwarps = g_ctx.sm_count * 4 * (P->groups[0].blocks_per_sm + P->groups[1].blocks_per_sm);
+        D.wwarps = g_ctx.sm_count * 4 * (P->groups[0].blocks_per_sm + P->groups[1].blocks_per_sm
+                                         + P->groups[2].blocks_per_sm);
         D.wscr = al(sizeof(double) * (size_t)D.wwarps * D.wstride);
     }
     if (P->jmode || grad) D.gctr = al(sizeof(double));   /* no per-task accumulators */
@@ -1213,7 +1244,7 @@ static int launch_grad_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     if (g == 1 && P->d_wscratch)
         L.wglobal += (size_t)g_ctx.sm_count * 4 * P->groups[0].blocks_per_sm * P->max_nf;
     L.wstride = P->max_nf;
-    int nblocks = std::min(g_ctx.sm_count * G.blocks_per_sm, std::max(1, (G.ntasks + 3) / 4));
+    const int nblocks = G.nblocks;
     int rc = cg_launch_grad(&L, P->mode, nblocks, stream);
     if (rc) { set_error("adjoint kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
     return 0;
@@ -1232,7 +1263,7 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.prims = P->d_prims;
     L.pqlist = P->d_pqlist;
     L.gctr = P->d_gctr;
-    L.counter = P->d_counters + g;
+    L.counter = P->d_counters + (g == 2 ? 3 : g);   /* [2] is the status word */
     L.nonempty = P->d_nonempty;
     L.status = P->d_counters + 2;
     L.rys_coef = g_ctx.rys_coef;
@@ -1241,8 +1272,9 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.ws_doubles = G.ws;
     L.jmode = P->jmode;
     L.wscratch = P->d_wscratch;
-    if (P->jmode && g == 1)   /* the groups run concurrently: separate warp slots */
-        L.wscratch += (size_t)g_ctx.sm_count * 4 * P->groups[0].blocks_per_sm * P->wscratch_stride;
+    if (P->jmode && g >= 1)   /* the groups may run concurrently: separate warp slots */
+        L.wscratch += (size_t)g_ctx.sm_count * 4
+                      * (P->groups[0].blocks_per_sm + (g == 2 ? P->groups[1].blocks_per_sm : 0)) * P->wscratch_stride;
     L.wscratch_stride = P->wscratch_stride;
     L.dm = P->cur_dm;
     L.vj = P->cur_vj;
@@ -1256,7 +1288,8 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.outs = P->d_outs;
     L.done = P->d_done;
     L.oscr = P->d_oscr;
-    if (L.oscr && g == 1) L.oscr += (size_t)g_ctx.sm_count * 4 * P->groups[0].blocks_per_sm * P->scratch_per_warp;
+    if (L.oscr && g >= 1)
+        L.oscr += (size_t)4 * (P->groups[0].nblocks + (g == 2 ? P->groups[1].nblocks : 0)) * P->scratch_per_warp;
     L.oscr_stride = P->scratch_per_warp;
     L.nf_max = P->max_nf;
     L.out = P->cur_out;
@@ -1264,8 +1297,8 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.comp_stride = P->out_size;
     L.hrr_off1 = P->nef_max;
     L.hrr_off2 = (int64_t)P->nef_max + P->hrr_max;
-    int nblocks = std::min(g_ctx.sm_count * G.blocks_per_sm, std::max(1, (G.ntasks + 3) / 4));
-    int rc = cg_launch_eri(&L, P->mode, nblocks, stream);
+    const int nblocks = G.nblocks;
+    int rc = cg_launch_eri(&L, g == 2 ? CG_MODE_ERIP : P->mode, nblocks, stream);
     if (rc) { set_error("ERI kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
     return 0;
 }
@@ -1293,6 +1326,10 @@ static int execute_plan(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
     } else {
         int rc = launch_group(P, 1, stream);
         if (!rc) rc = launch_group(P, 0, stream);
+        if (rc) return rc;
+    }
+    if (P->groups[2].ntasks > 0) {
+        int rc = launch_group(P, 2, stream);
         if (rc) return rc;
     }
     if (P->ev_t1) {
@@ -1427,6 +1464,7 @@ CACHE_SIZE_T dropin(int kind, double *out, FINT *dims, FINT *shls, FINT *atm, FI
         return 0;
     }
     CINTGPUPlan P;
+    P.fuse_out = false;   /* one quartet: a separate transform needs far less scratch */
     int rc = build_plan(&P, kind, shls, 1, NULL, atm, natm, bas, nbas, env,
                         (int64_t)g_ctx.sm_count * 8);
     if (rc) { zero_fill(); return 0; }
@@ -1504,6 +1542,8 @@ int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n
     int rc = ensure_init();
     if (rc) return rc;
     CINTGPUPlan *P = new CINTGPUPlan();
+    /* CINTGPU_SEPARATE_OUTPUT=1: transform outputs in their own kernel (tuning) */
+    if (const char *e = getenv("CINTGPU_SEPARATE_OUTPUT")) P->fuse_out = atoi(e) == 0;
     int64_t target = n < (int64_t)g_ctx.sm_count * 16 ? (int64_t)g_ctx.sm_count * 8 : 0;
     rc = build_plan(P, kind, shls, n, offsets, atm, natm, bas, nbas, env, target);
     if (!rc) rc = upload_plan(P, nullptr, 0, 0, false, nullptr);
@@ -1526,7 +1566,7 @@ double cintgpu_plan_flops_libcint(const CINTGPUPlan *plan) { return plan->flops_
 int64_t cintgpu_plan_prim_quartets(const CINTGPUPlan *plan) { return plan->prim_quartets; }
 int cintgpu_plan_launches(const CINTGPUPlan *plan)
 {
-    return (plan->groups[0].ntasks > 0) + (plan->groups[1].ntasks > 0) + 1;
+    return (plan->groups[0].ntasks > 0) + (plan->groups[1].ntasks > 0) + (plan->groups[2].ntasks > 0) + 1;
 }
 int64_t cintgpu_plan_upload_bytes(const CINTGPUPlan *plan) { return (int64_t)plan_upload_bytes(plan); }
 

@@ -84,13 +84,14 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
         L->off_dij = L->off_dkl = L->off_aacc = L->off_w = L->off_scr = 0;
         L->off_g = T * L->termw;
     } else if (!grad) {
-        int avail = ws_doubles - CG_TERMW * 32;     /* term records */
-        /* T terms need T*3*ng*G doubles of g arrays and min(32, 3T) lane scratch areas */
+        /* T terms need T term records, T*3*ng*G doubles of g arrays and min(32, 3T) lane
+         * scratch areas */
         for (int t = 32; t >= 1; t--) {
             int items = 3 * t < 32 ? 3 * t : 32;
-            if (t * 3 * L->ng * L->G + items * L->scr <= avail) { T = t; break; }
+            if (t * (CG_TERMW + 3 * L->ng * L->G) + items * L->scr <= ws_doubles) { T = t; break; }
         }
-        L->off_dij = L->off_dkl = L->off_aacc = L->off_w = L->off_g = L->off_scr = 0;
+        L->off_dij = L->off_dkl = L->off_aacc = L->off_w = L->off_scr = 0;
+        L->off_g = T * CG_TERMW;
         L->gstride = 3 * L->ng * L->G;
     } else {
         /* adjoint: term records scale with T; density blocks, exponent sums (GRADA) and the

@@ -46,9 +46,47 @@ __global__ void rys_roots_kernel(const double *__restrict__ xs, int count, int n
 
 /* ------------------------------------------------------------------ main kernel */
 
-/* One task: a slice of the surviving primitive quartets of one contracted quartet.
+/* J contraction of one slice's Cartesian block (gctr order; linear, so slices contract
+ * independently): X[i,j] += s_kl sum_kl (ij|kl) D[k,l];  X[k,l] += s_ij sum_ij (ij|kl) D[i,j] if
+ * IJ != KL, s = 2 for an off-diagonal shell pair of the unique list (D and (ij|kl) symmetric). */
+__device__ __forceinline__ void cg_j_contract(const CGLaunch &P, const CGTask &tk, const CGPair &pij,
+                                              const CGPair &pkl, const double *cart, int lane)
+{
+    const int li = pij.la, lj = pij.lb, lk = pkl.la, ll = pkl.lb;
+    const int nfi = ncart(li), nfj = ncart(lj), nfk = ncart(lk), nfl = ncart(ll);
+    const int nao = P.nao;
+    const double skl = (tk.sym & 2) ? 2.0 : 1.0, sij = (tk.sym & 1) ? 2.0 : 1.0;
+    const double *Dkl = P.dm + (size_t)pkl.ao_a * nao + pkl.ao_b;
+    for (int e = lane; e < nfi * nfj; e += 32) {
+        int i = e % nfi, j = e / nfi;
+        double v = 0.0;
+        for (int l = 0; l < nfl; l++)
+            for (int k = 0; k < nfk; k++)
+                v = fma(cart[i + nfi * (k + nfk * (l + nfl * j))], __ldg(Dkl + (size_t)k * nao + l), v);
+        atomicAdd(P.vj + (size_t)(pij.ao_a + i) * nao + pij.ao_b + j, skl * v);
+    }
+    if (tk.sym & 4) {
+        const double *Dij = P.dm + (size_t)pij.ao_a * nao + pij.ao_b;
+        for (int e = lane; e < nfk * nfl; e += 32) {
+            int k = e % nfk, l = e / nfk;
+            double v = 0.0;
+            for (int j = 0; j < nfj; j++)
+                for (int i = 0; i < nfi; i++)
+                    v = fma(cart[i + nfi * (k + nfk * (l + nfl * j))], __ldg(Dij + (size_t)i * nao + j), v);
+            atomicAdd(P.vj + (size_t)(pkl.ao_a + k) * nao + pkl.ao_b + l, sij * v);
+        }
+    }
+    __syncwarp();
+}
+
+
+
+/* One task in libcint's order (per primitive: VRR and both transfers, then the products per
+ * Cartesian component): int2e_ip1, and int2e classes whose transfers after contraction would
+ * amplify rounding beyond 1e-12 (lj or ll >= 4: the 3D transfer multiplies the per-axis
+ * amplifications that libcint's per-axis transfers only add).
  * NS > 0: lane-private register accumulators for components c = lane + 32 s, s < NS
- * NS = 0: accumulators in the task's gctr slot (large classes). */
+ * NS = 0: accumulators in the task's slot (large classes). */
 template <int MODE, int NS>
 __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, const CGLayout &L,
                                          double *term, double *greg, int lane)
@@ -66,12 +104,13 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
     const double common = P.common_base * common_fac_sp(li) * common_fac_sp(lj)
                         * common_fac_sp(lk) * (P.three ? 1.0 : common_fac_sp(ll));
     double *scr_base = greg + T * 3 * L.ng * L.G;
-    double *acc = P.gctr + tk.cart_off;
+    double *acc = P.jmode ? P.wscratch + (size_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * P.wscratch_stride
+                          : P.gctr + tk.cart_off;
 
-    /* per-lane component offsets into the g arrays, packed 10 bits per axis */
+    /* per-lane component offsets into the g arrays (register path: packed 10 bits per axis, G < 1024) */
     int offs[NS > 0 ? NS : 1];
     double ra[NS > 0 ? NS : 1][MODE == CG_MODE_IP1 ? 3 : 1];
-    auto comp_offsets = [&](int c) -> int {
+    auto comp_offsets3 = [&](int c, int &ox, int &oy, int &oz) {
         int ic = c % nfi, rest = c / nfi;
         int kc = rest % nfk; rest /= nfk;
         int lc = rest % nfl;
@@ -81,9 +120,13 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
         cart_pow(lj, jc, jx, jy, jz);
         cart_pow(lk, kc, kx, ky, kz);
         cart_pow(ll, lc, lx, ly, lz);
-        int ox = ((ix * L.dJ + jx) * L.dK + kx) * L.dL + lx;
-        int oy = ((iy * L.dJ + jy) * L.dK + ky) * L.dL + ly;
-        int oz = ((iz * L.dJ + jz) * L.dK + kz) * L.dL + lz;
+        ox = ((ix * L.dJ + jx) * L.dK + kx) * L.dL + lx;
+        oy = ((iy * L.dJ + jy) * L.dK + ky) * L.dL + ly;
+        oz = ((iz * L.dJ + jz) * L.dK + kz) * L.dL + lz;
+    };
+    auto comp_offsets = [&](int c) -> int {
+        int ox, oy, oz;
+        comp_offsets3(c, ox, oy, oz);
         return ox | (oy << 10) | (oz << 20);
     };
     if (NS > 0) {
@@ -146,32 +189,47 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                 if (lane + 32 * s >= L.nf) continue;
                 const int ox = offs[s] & 1023, oy = (offs[s] >> 10) & 1023, oz = offs[s] >> 20;
                 const double *gb = greg;
-                double sx = ra[s][0], sy = ra[s][1], sz = ra[s][2];
-                for (int t = 0; t < Tb; t++, gb += stride_t) {
-                    double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
-                    double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
-                    sx = fma(fx, gy * gz, sx);
-                    sy = fma(fy, gx * gz, sy);
-                    sz = fma(fz, gx * gy, sz);
+                if (MODE == CG_MODE_IP1) {
+                    double sx = ra[s][0], sy = ra[s][MODE == CG_MODE_IP1 ? 1 : 0],
+                           sz = ra[s][MODE == CG_MODE_IP1 ? 2 : 0];
+                    for (int t = 0; t < Tb; t++, gb += stride_t) {
+                        double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
+                        double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
+                        sx = fma(fx, gy * gz, sx);
+                        sy = fma(fy, gx * gz, sy);
+                        sz = fma(fz, gx * gy, sz);
+                    }
+                    ra[s][0] = sx;
+                    ra[s][MODE == CG_MODE_IP1 ? 1 : 0] = sy;
+                    ra[s][MODE == CG_MODE_IP1 ? 2 : 0] = sz;
+                } else {
+                    double s0 = ra[s][0];
+                    for (int t = 0; t < Tb; t++, gb += stride_t)
+                        s0 = fma(gb[ox] * gb[G + oy], gb[2 * G + oz], s0);
+                    ra[s][0] = s0;
                 }
-                ra[s][0] = sx;
-                ra[s][1] = sy;
-                ra[s][2] = sz;
             }
         } else {
             for (int c = lane; c < L.nf; c += 32) {
-                const int o3 = comp_offsets(c);
-                const int ox = o3 & 1023, oy = (o3 >> 10) & 1023, oz = o3 >> 20;
+                int ox, oy, oz;
+                comp_offsets3(c, ox, oy, oz);
                 const double *gb = greg;
-                double sx = acc[c], sy = acc[L.nf + c], sz = acc[2 * L.nf + c];
-                for (int t = 0; t < Tb; t++, gb += stride_t) {
-                    double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
-                    double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
-                    sx = fma(fx, gy * gz, sx);
-                    sy = fma(fy, gx * gz, sy);
-                    sz = fma(fz, gx * gy, sz);
+                if (MODE == CG_MODE_IP1) {
+                    double sx = acc[c], sy = acc[L.nf + c], sz = acc[2 * L.nf + c];
+                    for (int t = 0; t < Tb; t++, gb += stride_t) {
+                        double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
+                        double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
+                        sx = fma(fx, gy * gz, sx);
+                        sy = fma(fy, gx * gz, sy);
+                        sz = fma(fz, gx * gy, sz);
+                    }
+                    acc[c] = sx; acc[L.nf + c] = sy; acc[2 * L.nf + c] = sz;
+                } else {
+                    double s0 = acc[c];
+                    for (int t = 0; t < Tb; t++, gb += stride_t)
+                        s0 = fma(gb[ox] * gb[G + oy], gb[2 * G + oz], s0);
+                    acc[c] = s0;
                 }
-                acc[c] = sx; acc[L.nf + c] = sy; acc[2 * L.nf + c] = sz;
             }
         }
         __syncwarp();
@@ -186,7 +244,12 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             }
         }
     }
-    if (lane == 0) P.nonempty[tk.out] = 1;
+    if (MODE == CG_MODE_ERIP && P.jmode) {
+        __syncwarp();
+        cg_j_contract(P, tk, pij, pkl, acc, lane);
+    } else if (lane == 0) {
+        P.nonempty[tk.out] = 1;
+    }
 }
 
 /* ------------------------------------------------------------------ output transform */
@@ -466,36 +529,11 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
         __syncwarp();
     }
     if (P.jmode) {
-        /* J contraction of this slice (linear, so slices contract independently):
-         * X[i,j] += s_kl sum_kl (ij|kl) D[k,l];  X[k,l] += s_ij sum_ij (ij|kl) D[i,j] if IJ != KL,
-         * s = 2 for an off-diagonal shell pair of the unique list (D and (ij|kl) symmetric). */
+        /* J contraction of this slice's transferred block */
         const double *cart = cg_hrr(acc, P.eperm + ec.perm_off, P.eperm + ec.perm_off + ec.nE,
                                     P.hprog + ec.hprog_off, li, lj, lk, ll, pij.AB, pkl.AB,
                                     wbase + P.hrr_off1, wbase + P.hrr_off2, lane);
-        const int nfi = ncart(li), nfj = ncart(lj), nfk = ncart(lk), nfl = ncart(ll);
-        const int nao = P.nao;
-        const double skl = (tk.sym & 2) ? 2.0 : 1.0, sij = (tk.sym & 1) ? 2.0 : 1.0;
-        const double *Dkl = P.dm + (size_t)pkl.ao_a * nao + pkl.ao_b;
-        for (int e = lane; e < nfi * nfj; e += 32) {
-            int i = e % nfi, j = e / nfi;
-            double v = 0.0;
-            for (int l = 0; l < nfl; l++)
-                for (int k = 0; k < nfk; k++)
-                    v = fma(cart[i + nfi * (k + nfk * (l + nfl * j))], __ldg(Dkl + (size_t)k * nao + l), v);
-            atomicAdd(P.vj + (size_t)(pij.ao_a + i) * nao + pij.ao_b + j, skl * v);
-        }
-        if (tk.sym & 4) {
-            const double *Dij = P.dm + (size_t)pij.ao_a * nao + pij.ao_b;
-            for (int e = lane; e < nfk * nfl; e += 32) {
-                int k = e % nfk, l = e / nfk;
-                double v = 0.0;
-                for (int j = 0; j < nfj; j++)
-                    for (int i = 0; i < nfi; i++)
-                        v = fma(cart[i + nfi * (k + nfk * (l + nfl * j))], __ldg(Dij + (size_t)i * nao + j), v);
-                atomicAdd(P.vj + (size_t)(pkl.ao_a + k) * nao + pkl.ao_b + l, sij * v);
-            }
-        }
-        __syncwarp();
+        cg_j_contract(P, tk, pij, pkl, cart, lane);
     } else if (lane == 0) {
         P.nonempty[tk.out] = 1;
     }
@@ -508,8 +546,7 @@ __device__ __forceinline__ void rys_eri_body(const CGLaunch &P)
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     double *ws = smem + (size_t)warp * P.ws_doubles;
-    double *term = ws;                                   /* CG_TERMW * 32 */
-    double *greg = ws + CG_TERMW * 32;
+    double *term = ws;                                   /* term records, then g arrays at L.off_g */
 
     for (;;) {
         int tid = 0;
@@ -527,9 +564,11 @@ __device__ __forceinline__ void rys_eri_body(const CGLaunch &P)
             continue;
         }
         if (MODE == CG_MODE_ERI) run_task_e0f0(P, tk, L, term, ws + L.off_g, lane);
-        else if (ns <= 1) run_task<MODE, 1>(P, tk, L, term, greg, lane);
-        else if (ns <= 4) run_task<MODE, 4>(P, tk, L, term, greg, lane);
-        else run_task<MODE, 0>(P, tk, L, term, greg, lane);
+        else if (L.G >= 1024) run_task<MODE, 0>(P, tk, L, term, ws + L.off_g, lane);
+        else if (ns <= 1) run_task<MODE, 1>(P, tk, L, term, ws + L.off_g, lane);
+        else if (ns <= 4) run_task<MODE, 4>(P, tk, L, term, ws + L.off_g, lane);
+        else if (ns <= 16 && MODE == CG_MODE_ERIP) run_task<MODE, 16>(P, tk, L, term, ws + L.off_g, lane);
+        else run_task<MODE, 0>(P, tk, L, term, ws + L.off_g, lane);
         if (P.fuse_out) {
             /* publish this slice; the warp completing the quartet's last slice transforms it
              * (slot writes fenced before the count, reads past L1 after it) */
@@ -550,10 +589,17 @@ __device__ __forceinline__ void rys_eri_body(const CGLaunch &P)
 }
 
 /* int2e / int3c2e / J: the register allocation ptxas picks under the plain bound measured fastest;
- * int2e_ip1: two CTAs per SM (what shared memory allows anyway) lets it keep every value in
- * registers instead of spilling */
+ * int2e_ip1 and per-primitive int2e: two CTAs per SM (what shared memory allows anyway) lets them
+ * keep every value in registers instead of spilling */
 __global__ void __launch_bounds__(128) rys_eri_kernel_e0f0(CGLaunch P) { rys_eri_body<CG_MODE_ERI>(P); }
 __global__ void __launch_bounds__(128, 2) rys_eri_kernel_ip1(CGLaunch P) { rys_eri_body<CG_MODE_IP1>(P); }
+__global__ void __launch_bounds__(128, 2) rys_eri_kernel_prim(CGLaunch P) { rys_eri_body<CG_MODE_ERIP>(P); }
+
+static void *eri_kernel_of(int mode)
+{
+    return mode == CG_MODE_ERI ? (void *)rys_eri_kernel_e0f0
+         : mode == CG_MODE_IP1 ? (void *)rys_eri_kernel_ip1 : (void *)rys_eri_kernel_prim;
+}
 
 /* ------------------------------------------------------------------ output kernel */
 __global__ void __launch_bounds__(128)
@@ -588,9 +634,8 @@ extern "C" int cg_kernels_init(const int *c2s_nnz, const int *c2s_idx, const dou
     double *d = nullptr;
     if ((e = cudaGetSymbolAddress((void **)&d, g_rys_coef)) != cudaSuccess) return (int)e;
     *rys_coef_dev = d;
-    for (int mode = 0; mode < 2; mode++) {
-        void *fn = mode == 0 ? (void *)rys_eri_kernel_e0f0 : (void *)rys_eri_kernel_ip1;
-        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 8 * CG_WS_MAX);
+    for (int mode : {CG_MODE_ERI, CG_MODE_IP1, CG_MODE_ERIP}) {
+        e = cudaFuncSetAttribute(eri_kernel_of(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 8 * CG_WS_MAX);
         if (e != cudaSuccess) return (int)e;
     }
     return 0;
@@ -600,8 +645,7 @@ extern "C" int cg_blocks_per_sm(int mode, int ws_doubles)
 {
     int nb = 0;
     size_t smem = (size_t)4 * ws_doubles * sizeof(double);
-    void *fn = mode == CG_MODE_ERI ? (void *)rys_eri_kernel_e0f0 : (void *)rys_eri_kernel_ip1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eri_kernel_of(mode), 128, smem) != cudaSuccess) return 1;
     return nb > 0 ? nb : 1;
 }
 
@@ -618,8 +662,10 @@ extern "C" int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStrea
     size_t smem = (size_t)4 * P->ws_doubles * sizeof(double);
     if (mode == CG_MODE_ERI)
         rys_eri_kernel_e0f0<<<nblocks, 128, smem, stream>>>(*P);
-    else
+    else if (mode == CG_MODE_IP1)
         rys_eri_kernel_ip1<<<nblocks, 128, smem, stream>>>(*P);
+    else
+        rys_eri_kernel_prim<<<nblocks, 128, smem, stream>>>(*P);
     return (int)cudaGetLastError();
 }
 

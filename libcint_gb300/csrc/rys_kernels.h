@@ -9,6 +9,8 @@
 #define CG_MODE_IP1 1
 #define CG_MODE_GRAD 2               /* adjoint, nuclear-coordinate gradient */
 #define CG_MODE_GRADA 3              /* adjoint, coordinates and primitive exponents */
+#define CG_MODE_ERIP 4               /* int2e classes evaluated per primitive (transfer before
+                                        contraction, libcint's order): lj or ll >= 4 */
 #define CG_TERMW 12                  /* doubles per term record in shared memory */
 #define CG_TERMW_GRAD 20             /* term record of the adjoint kernel */
 #define CG_GRAD_MAXPRIM 16           /* primitives per shell supported by the exponent adjoint */
