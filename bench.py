@@ -40,9 +40,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FP64_PEAK_TFLOPS = 1.196      # measured DFMA peak of this GB300 pool, profiles/fp64_peak_gb300.md
-# DRAM read + write of one rys_eri_kernel launch per c1 quartet: 251.6 MB over the first 20k
+# DRAM read + write of one integral-kernel launch per c1 quartet: 706.0 MB over the first 50k
 # quartets of the committed list (ncu capture, profiles/rys_eri_kernel_c1.md), scaled by quartets
-ERI_DRAM_BYTES_PER_QUARTET = 251.6e6 / 20000
+ERI_DRAM_BYTES_PER_QUARTET = 706.0e6 / 50000
 SCHWARZ = 1e-12
 L2_FLUSH_BYTES = 256 << 20
 
@@ -366,12 +366,12 @@ def run_gpu(args, rank, world):
                    'wall_s_timed_region': wall},
         'quartets_per_s': len(qs) * world * args.steps / tot_s,
         'gpu_launches': plan.launches * args.steps,
-        'roofline': {'bound': 'fp64', 'kernel': 'rys_eri_kernel',
+        'roofline': {'bound': 'fp64', 'kernel': 'rys_eri_kernel_e0f0',
                      'kernel_ms_per_launch': 1e3 * kern_s / args.steps,
                      'achieved': achieved, 'peak': FP64_PEAK_TFLOPS,
                      'unit': 'TFLOP/s', 'frac': achieved / FP64_PEAK_TFLOPS,
                      'traffic': ERI_DRAM_BYTES_PER_QUARTET * len(qs),
-                     'traffic_source': 'ncu dram__bytes_read+write of a 20k-quartet launch, '
+                     'traffic_source': 'ncu dram__bytes_read+write of a 50k-quartet launch, '
                                        'scaled to the step (profiles/rys_eri_kernel_c1.md)',
                      'flop_model': 'this implementation: per term 20 + 15 VRR entries + groups '
                                    '+ 2 nE nF (FMA = 2)',
