@@ -248,7 +248,7 @@ def extra_adjoint(cg, seed=0, natm=24):
 
     def adj():
         g_adj[0] = plans.grad(dm)[0]
-    t_adj = _timed(adj)
+    t_adj = _timed(adj, reps=2)
     g_ip1 = [None]
 
     def ip1():
@@ -256,7 +256,7 @@ def extra_adjoint(cg, seed=0, natm=24):
     t_ip1 = _timed(ip1, reps=1)
     diff = float((g_adj[0] - g_ip1[0]).abs().max() / g_ip1[0].abs().max())
     plans_a = CoulombPlans(mol, with_exponents=True)
-    t_adj_a = _timed(lambda: plans_a.grad(dm))
+    t_adj_a = _timed(lambda: plans_a.grad(dm), reps=1)
     return {'workload': 'c3: %d atoms, %.1f A, s,p,d x 3-5 prims, all %d unique quartets'
                         % (natm, 8.0 * (natm / 24.0) ** (1.0 / 3.0), len(M.unique_quartets(mol.nbas))),
             'forward_J_ms': 1e3 * t_fwd, 'adjoint_grad_ms': 1e3 * t_adj,
