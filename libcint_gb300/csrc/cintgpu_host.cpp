@@ -1770,7 +1770,17 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
      * plan, and each later chunk's plan (built by one thread) is ready before the GPU needs it */
     std::vector<Chunk> ch;
     int64_t total = 0;
-    for (int64_t i0 = 0, len = 512; i0 < n; i0 += len, len = std::min<int64_t>(len + len / 4, 8192)) {
+    int64_t first = 512, cap = 8192;
+    double growth = 1.25;
+    if (const char *e = getenv("CINTGPU_CHUNK")) {   /* "first,growth,cap" (tuning) */
+        long long f = 0, c = 0;
+        double g = 0;
+        if (sscanf(e, "%lld,%lf,%lld", &f, &g, &c) == 3 && f >= 1 && g >= 1.0 && c >= f) {
+            first = f; growth = g; cap = c;
+        }
+    }
+    for (int64_t i0 = 0, len = first; i0 < n;
+         i0 += len, len = std::min<int64_t>(std::max<int64_t>(len + 1, (int64_t)(len * growth)), cap)) {
         Chunk x;
         x.i0 = i0;
         x.n = std::min(len, n - i0);

@@ -67,7 +67,10 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     L->ng = (mode == CG_MODE_IP1) ? 2 : 1;
     L->nf = ncart(li) * ncart(lj) * ncart(lk) * ncart(ll);
     L->ncomp = (mode == CG_MODE_IP1) ? 3 : 1;
+    /* per-lane scratch of g_axis; an odd stride keeps the 32 lanes' equal offsets in distinct
+     * shared-memory banks */
     L->scr = (L->nmax + 1) * (L->mmax + 1) + (L->nmax + 1) + (L->mmax + 1);
+    L->scr |= 1;
     const bool grad = mode == CG_MODE_GRAD || mode == CG_MODE_GRADA;
     int T = 0;
     if (mode == CG_MODE_ERI) {
