@@ -136,3 +136,23 @@ def test_autograd_function(gpulib):
     np.testing.assert_allclose(exps.grad.cpu().numpy(), ga.cpu().numpy(), rtol=0, atol=1e-12)
     _, J = CoulombPlans(mol).energy(dmt.detach())
     np.testing.assert_allclose(dmt.grad.cpu().numpy(), J.cpu().numpy(), rtol=0, atol=1e-12)
+
+
+def test_j_high_l_per_primitive_classes(gpulib, oracle):
+    """J over every unique quartet of a basis with g, h and i shells: classes with lj or ll >= 4
+    take the per-primitive kernel (third task group, its own J scratch slots), the rest the
+    contraction-first one; both against the checker's ERIs contracted on the host."""
+    import torch
+    from libcint_gb300.coulomb import CoulombPlans
+    from tests.test_gpu_high_l import high_l_basis
+    mol = high_l_basis()
+    nao = sum(mol.nsph(i) for i in range(mol.nbas))
+    rng = np.random.RandomState(2)
+    d = rng.normal(0, 0.1, (nao, nao))
+    dm = 0.5 * (d + d.T)
+    Jref, Eref = _oracle_j_energy(oracle, mol, dm)
+    plans = CoulombPlans(mol)
+    E, J = plans.energy(torch.as_tensor(dm, device='cuda'))
+    J = J.cpu().numpy()
+    assert np.abs(J - Jref).max() <= 1e-10 * np.abs(Jref).max()
+    assert abs(float(E) - Eref) <= 1e-10 * abs(Eref)
