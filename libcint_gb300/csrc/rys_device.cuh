@@ -78,7 +78,8 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
          * records hold the 10 stage-1 values and m b01 for m <= mmax (odd length) */
         L->G = (L->nmax + 1) * (L->mmax + 1);
         L->scr = 0;
-        L->gstride = 3 * L->G + ((3 * L->G) % 2 == 0 ? 1 : 0);
+        L->gax = L->G | 1;
+        L->gstride = 3 * L->gax;
         L->termw = 10 + L->mmax + 1;
         if (L->termw % 2 == 0) L->termw++;
         T = ws_doubles / (L->termw + L->gstride);
@@ -89,13 +90,14 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     } else if (!grad) {
         /* T terms need T term records, T*3*ng*G doubles of g arrays and min(32, 3T) lane
          * scratch areas */
+        L->gax = (L->ng * L->G) | 1;
+        L->gstride = 3 * L->gax;
         for (int t = 32; t >= 1; t--) {
             int items = 3 * t < 32 ? 3 * t : 32;
-            if (t * (CG_TERMW + 3 * L->ng * L->G) + items * L->scr <= ws_doubles) { T = t; break; }
+            if (t * (CG_TERMW + L->gstride) + items * L->scr <= ws_doubles) { T = t; break; }
         }
         L->off_dij = L->off_dkl = L->off_aacc = L->off_w = L->off_scr = 0;
         L->off_g = T * CG_TERMW;
-        L->gstride = 3 * L->ng * L->G;
     } else {
         /* adjoint: term records scale with T; density blocks, exponent sums (GRADA) and the
          * cotangent (nf <= CG_W_SMEM) are per task */
@@ -105,7 +107,8 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
         int fixed = d1 + d2 + aa + wsm;
         /* odd per-term stride of the g arrays: lanes reading the same offset of different terms
          * hit distinct shared-memory banks */
-        L->gstride = 3 * L->G + ((3 * L->G) % 2 == 0 ? 1 : 0);
+        L->gax = L->G | 1;
+        L->gstride = 3 * L->gax;
         for (int t = 32; t >= 1; t--) {
             int items = 3 * t < 32 ? 3 * t : 32;
             if (t * (CG_TERMW_GRAD + L->gstride) + items * L->scr + fixed <= ws_doubles) { T = t; break; }

@@ -49,7 +49,7 @@ rys_grad_kernel(CGGradLaunch P)
             if (lane == 0) atomicOr(P.status, 1);
             continue;
         }
-        const int T = L.T, n = L.nroots, G = L.G;
+        const int T = L.T, n = L.nroots, G = L.gax;   /* axis stride of a term's g arrays */
         double *Dij = ws + L.off_dij, *Dkl = ws + L.off_dkl, *aacc = ws + L.off_aacc;
         const int nfi = ncart(li), nfj = ncart(lj), nfk = ncart(lk), nfl = ncart(ll);
         const int nao = P.nao;

@@ -103,7 +103,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
     const int T = L.T;
     const double common = P.common_base * common_fac_sp(li) * common_fac_sp(lj)
                         * common_fac_sp(lk) * (P.three ? 1.0 : common_fac_sp(ll));
-    double *scr_base = greg + T * 3 * L.ng * L.G;
+    double *scr_base = greg + T * L.gstride;
     double *acc = P.jmode ? P.wscratch + (size_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * P.wscratch_stride
                           : P.gctr + tk.cart_off;
 
@@ -162,7 +162,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             int t = item / 3, ax = item - 3 * t;
             const double *rec = term + t * CG_TERMW;
             double g00 = (ax == 2) ? rec[9] : 1.0;
-            double *gdst = greg + (size_t)(t * 3 + ax) * L.ng * L.G;
+            double *gdst = greg + (size_t)(t * 3 + ax) * L.gax;
             g_axis(L, rec[0], rec[1], rec[2], rec[3 + ax], rec[6 + ax], g00,
                    pij.AB[ax], pkl.AB[ax], scr_base + lane * L.scr, gdst);
             if (MODE == CG_MODE_IP1) {
@@ -181,8 +181,8 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
         }
         __syncwarp();
         /* ---- stage 3: one lane per Cartesian component */
-        const int stride_t = 3 * L.ng * L.G;
-        const int G = L.G;
+        const int stride_t = L.gstride;
+        const int G = L.G, A = L.gax;   /* f arrays at +G inside an axis block; axis blocks A apart */
         if (NS > 0) {
 #pragma unroll
             for (int s = 0; s < (NS > 0 ? NS : 1); s++) {
@@ -193,8 +193,8 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                     double sx = ra[s][0], sy = ra[s][MODE == CG_MODE_IP1 ? 1 : 0],
                            sz = ra[s][MODE == CG_MODE_IP1 ? 2 : 0];
                     for (int t = 0; t < Tb; t++, gb += stride_t) {
-                        double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
-                        double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
+                        double gx = gb[ox], gy = gb[A + oy], gz = gb[2 * A + oz];
+                        double fx = gb[G + ox], fy = gb[A + G + oy], fz = gb[2 * A + G + oz];
                         sx = fma(fx, gy * gz, sx);
                         sy = fma(fy, gx * gz, sy);
                         sz = fma(fz, gx * gy, sz);
@@ -205,7 +205,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                 } else {
                     double s0 = ra[s][0];
                     for (int t = 0; t < Tb; t++, gb += stride_t)
-                        s0 = fma(gb[ox] * gb[G + oy], gb[2 * G + oz], s0);
+                        s0 = fma(gb[ox] * gb[A + oy], gb[2 * A + oz], s0);
                     ra[s][0] = s0;
                 }
             }
@@ -217,8 +217,8 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                 if (MODE == CG_MODE_IP1) {
                     double sx = acc[c], sy = acc[L.nf + c], sz = acc[2 * L.nf + c];
                     for (int t = 0; t < Tb; t++, gb += stride_t) {
-                        double gx = gb[ox], gy = gb[2 * G + oy], gz = gb[4 * G + oz];
-                        double fx = gb[G + ox], fy = gb[3 * G + oy], fz = gb[5 * G + oz];
+                        double gx = gb[ox], gy = gb[A + oy], gz = gb[2 * A + oz];
+                        double fx = gb[G + ox], fy = gb[A + G + oy], fz = gb[2 * A + G + oz];
                         sx = fma(fx, gy * gz, sx);
                         sy = fma(fy, gx * gz, sy);
                         sz = fma(fz, gx * gy, sz);
@@ -227,7 +227,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                 } else {
                     double s0 = acc[c];
                     for (int t = 0; t < Tb; t++, gb += stride_t)
-                        s0 = fma(gb[ox] * gb[G + oy], gb[2 * G + oz], s0);
+                        s0 = fma(gb[ox] * gb[A + oy], gb[2 * A + oz], s0);
                     acc[c] = s0;
                 }
             }
@@ -416,7 +416,7 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
     const int *__restrict__ pql = P.pqlist + tk.pq_off;
     const int nij = pij.npa * pij.npb;
     const int li = pij.la, lj = pij.lb, lk = pkl.la, ll = pkl.lb;
-    const int n = L.nroots, T = L.T, G = L.G, gstride = L.gstride, na = L.nmax + 1;
+    const int n = L.nroots, T = L.T, G = L.gax, gstride = L.gstride, na = L.nmax + 1;   /* G: axis stride */
     const double common = P.common_base * common_fac_sp(li) * common_fac_sp(lj)
                         * common_fac_sp(lk) * (P.three ? 1.0 : common_fac_sp(ll));
     const CGEriClass ec = P.eclass[tk.cls];

@@ -24,7 +24,9 @@ typedef struct {
     /* adjoint shared-memory map (doubles from the warp's base): density blocks, exponent sums,
      * cotangent (when kept in shared memory), g arrays, lane scratch */
     int off_dij, off_dkl, off_aacc, off_w, off_g, off_scr;
-    int gstride;              /* doubles between consecutive terms' g arrays */
+    int gstride;              /* doubles between consecutive terms' g arrays (3 gax) */
+    int gax;                  /* doubles between a term's axis arrays: odd, so the 32 lanes of
+                                 stage 2 (item = 3 term + axis) start in distinct banks */
     int termw;                /* doubles per term record */
 } CGLayout;
 
