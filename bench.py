@@ -304,9 +304,8 @@ def run_gpu(args, rank, world):
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
-    clk = ClockSampler(os.path.join(ROOT, 'gpurun_out', 'clocks_rank%d.csv' % rank)
-                       if os.path.isdir(os.path.join(ROOT, 'gpurun_out')) else
-                       os.path.join(tempfile.gettempdir(), 'cintgpu_clocks.csv'))
+    clk = ClockSampler(os.path.join(os.environ.get('BENCH_CLOCKS_DIR', tempfile.gettempdir()),
+                                    'cintgpu_clocks_rank%d.csv' % rank))
     evs = []
     kernel_ms = []
     with clk:

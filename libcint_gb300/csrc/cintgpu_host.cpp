@@ -2095,6 +2095,19 @@ extern "C" int cg_eri_tables(int li, int lj, int lk, int ll, int *info, int *gro
     return (int)P.hprog.size();
 }
 
+/* Host planning only, for tests of the task routing: tasks of the three groups (regular, 48 KB,
+ * per-primitive int2e) and whether outputs are transformed inside the integral kernel. */
+extern "C" int cg_plan_groups(int kind, const int *shls, int64_t n, const int *atm, int natm,
+                              const int *bas, int nbas, const double *env, int64_t *info)
+{
+    CINTGPUPlan P;
+    int rc = build_plan(&P, kind, shls, n, nullptr, atm, natm, bas, nbas, env, 0);
+    if (rc) return rc;
+    for (int g = 0; g < 3; g++) info[g] = P.groups[g].ntasks;
+    info[3] = fused(&P) ? 1 : 0;
+    return 0;
+}
+
 CINTGPUPlan *cg_plan_new(void) { return new CINTGPUPlan(); }
 void cg_plan_separate_output(CINTGPUPlan *P) { P->fuse_out = false; }
 void cg_plan_free_host(CINTGPUPlan *P) { P->dbuf = nullptr; delete P; }

@@ -1,0 +1,64 @@
+"""Task routing of the planner, CPU only (host planning, no device): int2e classes whose horizontal
+transfer after contraction would lose precision (kernel-order lj or ll >= 4) go to the
+per-primitive group when its g arrays fit; CINTGPU_PER_PRIMITIVE_L moves the threshold; plans
+transform their outputs inside the integral kernel."""
+import ctypes
+import os
+
+import numpy as np
+
+from tests import _oracle  # noqa: F401  (puts the repo root on sys.path)
+import libcint_gb300 as cg
+from libcint_gb300 import molecules as M
+from tests.test_gpu_high_l import high_l_basis
+
+
+def groups(kind, mol, items, env=None):
+    f = cg.lib().cg_plan_groups
+    f.restype = ctypes.c_int
+    info = np.zeros(4, np.int64)
+    items = np.ascontiguousarray(items, dtype=np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    old = {k: os.environ.get(k) for k in (env or {})}
+    os.environ.update(env or {})
+    try:
+        rc = f(kind, P(items), ctypes.c_int64(len(items)), P(mol.atm), mol.natm, P(mol.bas),
+               mol.nbas, P(mol.env), P(info))
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    assert rc == 0, cg.last_error()
+    return info
+
+
+def test_high_l_routing():
+    mol = high_l_basis()      # shells 0..4: l = 6, 5, 4, 2, 0
+    # (ih|ih): lj = ll = 5 -> per primitive; its g arrays (1764 per axis) fit the 48 KB warp
+    assert groups(cg.INT2E_SPH, mol, [(0, 1, 0, 1)])[2] > 0
+    # (ii|ii): per-primitive g arrays (2401 per axis) do not fit -> contraction first
+    g = groups(cg.INT2E_SPH, mol, [(0, 0, 0, 0)])
+    assert g[2] == 0 and g[0] + g[1] > 0
+    # (dd|ss)-type and (is|ss): lj, ll < 4 -> contraction first
+    g = groups(cg.INT2E_SPH, mol, [(3, 3, 4, 4), (0, 4, 4, 4)])
+    assert g[2] == 0
+
+
+def test_threshold_switch_and_fusion():
+    mol = M.config1(seed=0)
+    qs = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'c1_quartets.npz'))['quartets']
+    L = mol.bas[:, M.ANG_OF]
+    ff = qs[(np.minimum(L[qs[:, 0]], L[qs[:, 1]]) == 3) | (np.minimum(L[qs[:, 2]], L[qs[:, 3]]) == 3)][:50]
+    g = groups(cg.INT2E_SPH, mol, ff)
+    assert g[2] == 0 and g[3] == 1          # f-f transfers stay contraction first, fused output
+    g = groups(cg.INT2E_SPH, mol, ff, {'CINTGPU_PER_PRIMITIVE_L': '3'})
+    assert g[0] + g[1] == 0 and g[2] > 0    # all of them per primitive
+    g = groups(cg.INT2E_SPH, mol, qs[:200], {'CINTGPU_PER_PRIMITIVE_L': '0'})
+    assert g[0] + g[1] == 0 and g[2] > 0    # every class per primitive
+    g = groups(cg.INT2E_SPH, mol, qs[:200], {'CINTGPU_SEPARATE_OUTPUT': '1'})
+    assert g[3] == 1                        # the switch is read at plan creation, not here
+    # int2e_ip1 never uses the contraction-first groups' tables but keeps the regular groups
+    g = groups(cg.INT2E_IP1_SPH, mol, qs[:100])
+    assert g[2] == 0 and g[0] + g[1] > 0
