@@ -8,7 +8,10 @@
  *   CGTask[ntask]        one unit of kernel work: bra pair, ket pair and a slice of the surviving
  *                        primitive quartets (pqlist)
  *   CGOutTask[nout]      one contracted shell quartet to transform (cart -> sph) and store
- *   gctr                 Cartesian accumulators, CGTask::cart_off, layout [comp][nf]
+ *   CGEriClass/CGEriGroup/... per-class tables of the contraction-first kernel and the transfer
+ *   CGGradClass/...      per-class tables of the adjoint
+ *   gctr                 accumulator slots, CGTask::cart_off: (e0|f0) in group layout (int2e,
+ *                        int3c2e) or Cartesian [comp][nf] (per-primitive classes, int2e_ip1)
  */
 #ifndef CINTGPU_TYPES_H
 #define CINTGPU_TYPES_H

@@ -1,29 +1,33 @@
 /*
  * GB300 (sm_103a) kernels of the Rys-quadrature two-electron integral path.
  *
- * The path is FP64-issue bound (measured on GB300: 1.2 TFLOP/s DFMA against 74 TFLOP/s FFMA), so
- * the kernels are written to spend FP64 instructions only on the quadrature itself:
+ * The path is FP64-pipe bound (measured on GB300: 1.2 TFLOP/s DFMA against 74 TFLOP/s FFMA), so
+ * the kernels spend FP64 instructions only on the quadrature itself:
  *   - recurrence coefficients are division free (linear in the Rys node s = t^2),
  *   - roots/weights come from piecewise polynomial tables (Horner, 2 x 10 DFMA per root),
- *   - pair quantities (exponential prefactors, product centres, screening values) are
- *     precomputed once per primitive pair,
+ *   - pair quantities (exponential prefactors, product centres) are precomputed once per
+ *     primitive pair; libcint's primitive screening (src/cint2e.c:400-425) runs on the host,
+ *     which hands each task its list of surviving primitive quartets,
  *   - all index arithmetic is integer.
  *
- * Work decomposition: one warp owns one task (a shell quartet or a slice of its primitive
- * quartets) and walks its primitive quartets 32 at a time:
- *   screen    each lane tests one primitive quartet with libcint's rule
- *             (src/cint2e.c:400-425: skip kl if cce_kl > cutoff, skip ij if cce_ij > cutoff - cce_kl)
- *             and the survivors are compacted with a warp ballot;
- *   stage 1   one lane per (primitive quartet, root) "term": x, prefactor, root, weight and the
- *             recurrence coefficients (libcint CINTg0_2e, src/g2e.c:4425-4545);
- *   stage 2   one lane per (term, Cartesian axis): the 2D vertical recurrence and both horizontal
- *             transfers (CINTg0_2e_2d + CINTg0_*2d_4d, src/g2e.c:272-693) into shared memory;
- *   stage 3   one lane per output Cartesian component: sum over the batch's terms of
- *             gx*gy*gz (CINTgout2e, src/cint2e.c:961-1183) or the nabla-i variant of int2e_ip1
- *             (src/autocode/grad2.c:19-68), accumulated in the task's gctr slot (L2 resident).
- * A second kernel turns the Cartesian accumulators into the requested layout (cart or real
- * spherical, c2s_sph_2e1 / c2s_sph_3c2e1 semantics, src/cart2sph.c:5324-5383, 5884-5925) with
- * arbitrary output strides.
+ * Work decomposition: one warp owns one task (a shell quartet or a slice of its surviving
+ * primitive quartets, taken from an atomic counter in longest-first order) and walks its
+ * "terms" (primitive quartet x root) 32 at a time:
+ *   stage 1   one lane per term: x, prefactor, root, weight and the recurrence coefficients
+ *             (libcint CINTg0_2e, src/g2e.c:4425-4545);
+ *   stage 2   one lane per (term, Cartesian axis): the 2D vertical recurrence into shared memory
+ *             (CINTg0_2e_2d, src/g2e.c:272-421);
+ *   stage 3   int2e / int3c2e / J (rys_eri_kernel_e0f0): the contracted (e0|f0) block, one
+ *             group (ex, ey, fx, fy) per lane; the horizontal transfer (src/g2e.c:428-693) then
+ *             runs once per contracted quartet.
+ *             int2e_ip1 and int2e classes with lj or ll >= 4 (rys_eri_kernel_ip1 / _prim):
+ *             both transfers per term in stage 2, then one lane per Cartesian component sums
+ *             gx gy gz (CINTgout2e, src/cint2e.c:961-1183) or the nabla-i products of int2e_ip1
+ *             (src/autocode/grad2.c:19-68).
+ * The warp that completes a quartet's last slice sums the slices, transfers, transforms to the
+ * requested layout (cart or real spherical, c2s_sph_2e1 / c2s_sph_3c2e1 semantics,
+ * src/cart2sph.c:5324-5383, 5884-5925) and stores with arbitrary strides; cg_output_kernel does
+ * the same for quartets of plans that keep it separate and zero-fills empty quartets.
  */
 #include "rys_device.cuh"
 
