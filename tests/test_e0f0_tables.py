@@ -121,6 +121,11 @@ def direct(g, li, lj, lk, ll, AB, CD):
 
 CLASSES = [(0, 0, 0, 0), (1, 0, 0, 0), (1, 1, 0, 0), (1, 1, 1, 1), (2, 1, 1, 0), (2, 2, 2, 1),
            (3, 2, 2, 1), (3, 3, 2, 2), (3, 1, 3, 0), (4, 2, 3, 3), (5, 4, 1, 0), (4, 4, 4, 4)]
+# plus a seeded sample of the other kernel-order classes up to f (li >= lj, lk >= ll)
+_rng = np.random.RandomState(17)
+_all = [(a, b, c, d) for a in range(4) for b in range(a + 1) for c in range(4) for d in range(c + 1)
+        if (a, b, c, d) not in CLASSES]
+CLASSES += [_all[i] for i in _rng.choice(len(_all), 16, replace=False)]
 
 
 @pytest.mark.parametrize('cls', CLASSES)
