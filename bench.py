@@ -395,6 +395,10 @@ def run_gpu(args, rank, world):
                                 'cores': res['threads'], 'kind': 'port',
                                 'sample': 'first %d quartets of the step list (%.1f s)'
                                           % (res['quartets'], res['seconds'])}
+        one = cpu_port_rate(mol, qs, 1, target_s=3.0)
+        line['cpu_baseline']['one_thread'] = {'value': one['integrals'] / one['seconds'],
+                                              'sample': 'first %d quartets (%.1f s)'
+                                                        % (one['quartets'], one['seconds'])}
     print(json.dumps(line), flush=True)
 
 
