@@ -62,3 +62,47 @@ def test_threshold_switch_and_fusion():
     # int2e_ip1 never uses the contraction-first groups' tables but keeps the regular groups
     g = groups(cg.INT2E_IP1_SPH, mol, qs[:100])
     assert g[2] == 0 and g[0] + g[1] > 0
+
+
+def _build(kind, mol, items):
+    f = cg.lib().cg_plan_groups
+    f.restype = ctypes.c_int
+    info = np.zeros(4, np.int64)
+    items = np.ascontiguousarray(items, dtype=np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    return f(kind, P(items), ctypes.c_int64(len(items)), P(mol.atm), mol.natm, P(mol.bas),
+             mol.nbas, P(mol.env), P(info))
+
+
+def _variant(mol, arr, idx, val):
+    atm, bas, env = mol.atm.copy(), mol.bas.copy(), mol.env.copy()
+    {'atm': atm, 'bas': bas, 'env': env}[arr][idx] = val
+    return M.Mol(atm, bas, env, mol.name)
+
+
+def test_invalid_input_is_rejected_with_a_message():
+    """The planner's argument checks (the drop-in returns 0 with a zero block on these, the plan
+    API the status): libcint asserts or exits on such input, this library never aborts."""
+    mol = M.config0(seed=1)
+    q = [(3, 1, 2, 0)]
+    assert _build(cg.INT2E_SPH, mol, q) == 0
+    cases = [
+        ('negative shell', mol, [(-1, 1, 2, 0)], -1, 'negative shell'),
+        ('l = 7', _variant(mol, 'bas', (3, M.ANG_OF), 7), q, -3, 'angular momentum'),
+        ('nprim = 65', _variant(mol, 'bas', (3, M.NPRIM_OF), 65), q, -1, 'nprim'),
+        ('atom out of range', _variant(mol, 'bas', (3, M.ATOM_OF), 99), q, -1, 'atom'),
+        ('omega != 0', _variant(mol, 'env', 8, 0.3), q, -3, 'range-separated'),
+    ]
+    for what, m, items, code, text in cases:
+        assert _build(cg.INT2E_SPH, m, items) == code, what
+        assert text in cg.last_error(), (what, cg.last_error())
+    # adjoint limits: l <= 4; exponent adjoint: nprim <= 16
+    lg = _variant(mol, 'bas', (3, M.ANG_OF), 5)
+    assert _build(8, lg, q) == -3 and 'adjoint' in cg.last_error()
+    # the host-buffer entry computes blocks only; J kinds go through plan_execute_j
+    f = cg.lib().cintgpu_batch_host
+    out = np.zeros(16)
+    items = np.array(q, dtype=np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    assert f(7, P(out), P(items), 1, None, P(mol.atm), mol.natm, P(mol.bas), mol.nbas, P(mol.env)) == -1
+    assert 'density' in cg.last_error()
