@@ -1597,6 +1597,9 @@ int cintgpu_plan_status(const CINTGPUPlan *plan)
     return st;
 }
 
+/* Diagnostics (not in the public header): info[0..11] = tasks, tasks of groups 0 and 1, adjoint
+ * classes / chunks / entries, shared-memory doubles per warp of group 0, CTAs per SM of groups 0
+ * and 1, mode, tasks of group 2 (per-primitive int2e), fused outputs (0/1). */
 int cintgpu_plan_debug(const CINTGPUPlan *plan, int64_t *info)
 {
     info[0] = (int64_t)plan->tasks.size();
@@ -1609,6 +1612,8 @@ int cintgpu_plan_debug(const CINTGPUPlan *plan, int64_t *info)
     info[7] = plan->groups[0].blocks_per_sm;
     info[8] = plan->groups[1].blocks_per_sm;
     info[9] = plan->mode;
+    info[10] = plan->groups[2].ntasks;
+    info[11] = fused(plan) ? 1 : 0;
     return 0;
 }
 
