@@ -185,3 +185,44 @@ def test_e0f0_tables_replay(cls):
     got = hrr(acc, perm[:nE], perm[nE:], prog, li, lj, lk, ll, AB, CD, c['hrr_need'])
     ref = direct(g, li, lj, lk, ll, AB, CD)
     np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-11 * np.abs(ref).max())
+
+
+def test_all_class_tables_stay_in_bounds():
+    """Every kernel-order class up to l = 6: stage-3 offsets inside the per-axis VRR arrays,
+    accumulator indices inside the nE x nF slot, transfer-program sources inside the previous
+    level and targets inside hrr_need (the buffers the kernels index with these tables)."""
+    for li in range(7):
+        for lj in range(li + 1):
+            for lk in range(7):
+                for ll in range(lk + 1):
+                    c, groups, perm, prog, rounds = tables(li, lj, lk, ll)
+                    na, nm = li + lj + 1, lk + ll + 1
+                    G = na * nm
+                    nE, nF = c['nE'], c['nF']
+                    ox, oy = groups[:, 0] & 0xffff, groups[:, 0] >> 16
+                    nez, nfz = groups[:, 3] & 0xff, (groups[:, 3] >> 8) & 0xff
+                    assert ox.max() < G and oy.max() < G
+                    assert (groups[:, 1] + (nez - 1) + na * (nfz - 1)).max() < G
+                    assert (groups[:, 2] + (nez - 1) * nF + (nfz - 1)).max() < nE * nF
+                    assert perm[:nE].max() < nE and perm[nE:].max() < nF
+                    starts, cnts = rounds & 0xffff, (rounds >> 16) & 0xff
+                    assert (cnts >= 1).all() and (cnts <= 32).all()
+                    assert (starts + cnts).max() <= len(groups) and cnts.sum() == len(groups)
+                    need = c['hrr_need']
+                    assert nE * nF <= need
+                    p, size = 0, nE * nF
+                    for b in range(1, lj + 1):
+                        nrows = prog[p]
+                        rows = prog[p + 1:p + 1 + 3 * nrows].reshape(-1, 3)
+                        assert rows[:, :2].max() < size // nF and set(rows[:, 2]) <= {0, 1, 2}
+                        size = nrows * nF
+                        assert size <= need
+                        p += 1 + 3 * nrows
+                    nij = nc(li) * nc(lj)
+                    for d in range(1, ll + 1):
+                        nent, sin, sout = prog[p:p + 3]
+                        ents = prog[p + 3:p + 3 + 3 * nent].reshape(-1, 3)
+                        assert ents[:, :2].max() < sin and nij * sin <= need and nij * sout <= need
+                        assert sout == nent
+                        p += 3 + 3 * nent
+                    assert p == len(prog)
