@@ -1,0 +1,78 @@
+"""Shared-memory layouts of every class in every kernel mode, CPU only: what the kernels place in
+a warp's shared memory (term records, g arrays, lane scratch, adjoint blocks) fits the budget the
+planner launches them with, and the strides keep their bank-spreading properties."""
+import ctypes
+
+import pytest
+
+from tests import _oracle  # noqa: F401  (puts the repo root on sys.path)
+import libcint_gb300 as cg
+
+ERI, IP1, GRAD, GRADA, ERIP = 0, 1, 2, 3, 4
+TERMW, TERMW_GRAD, GRAD_MAXPRIM, W_SMEM = 12, 20, 16, 256
+WS_SMALL, WS_MAX = 24 * 1024 // 8, 48 * 1024 // 8
+
+
+class Layout(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in
+                ('lic nroots nmax mmax dI dJ dK dL G ng nf ncomp scr T off_dij off_dkl off_aacc '
+                 'off_w off_g off_scr gstride gax termw').split()]
+
+
+def layout(l, mode, ws):
+    L = Layout()
+    cg.lib().cg_layout(*l, mode, ws, ctypes.byref(L))
+    return L
+
+
+def nc(l):
+    return (l + 1) * (l + 2) // 2
+
+
+def classes(lmax):
+    return [(a, b, c, d) for a in range(lmax + 1) for b in range(a + 1)
+            for c in range(lmax + 1) for d in range(c + 1)]
+
+
+@pytest.mark.parametrize('mode', [ERI, ERIP, IP1])
+def test_integral_layouts_fit(mode):
+    for l in classes(6):
+        for ws in (WS_SMALL, WS_MAX):
+            L = layout(l, mode, ws)
+            if L.T < 1:
+                continue          # the planner rejects such a class or moves it to another group
+            assert L.gax % 2 == 1 and L.gstride == 3 * L.gax
+            if mode == ERI:
+                assert L.termw % 2 == 1 and L.termw >= 10 + L.mmax + 1
+                assert L.off_g == L.T * L.termw
+                assert L.off_g + L.T * L.gstride <= ws
+            else:
+                assert L.scr % 2 == 1
+                items = min(32, 3 * L.T)
+                assert L.off_g == L.T * TERMW
+                assert L.off_g + L.T * L.gstride + items * L.scr <= ws
+                assert L.gax >= L.ng * L.G
+
+
+# the exponent adjoint raises l by 2 on all four centres: these g-g / f-g classes exceed 48 KB
+# per warp and the planner rejects them (CINTGPU_ERR_UNSUPPORTED)
+GRADA_TOO_LARGE = {(3, 3, 4, 4), (4, 3, 4, 3), (4, 3, 4, 4), (4, 4, 3, 3), (4, 4, 4, 3), (4, 4, 4, 4)}
+
+
+@pytest.mark.parametrize('mode', [GRAD, GRADA])
+def test_adjoint_layouts_fit(mode):
+    for l in classes(4):
+        L = layout(l, mode, WS_MAX)
+        if mode == GRADA and l in GRADA_TOO_LARGE:
+            assert L.T < 1
+            continue
+        assert L.T >= 1, l
+        assert L.gax % 2 == 1 and L.gstride == 3 * L.gax and L.scr % 2 == 1
+        items = min(32, 3 * L.T)
+        assert L.off_scr + items * L.scr <= WS_MAX
+        assert L.off_g >= L.off_w and L.off_scr == L.off_g + L.T * L.gstride
+        assert L.off_dkl - L.off_dij >= nc(l[0]) * nc(l[1])
+        if mode == GRADA:
+            assert L.off_w - L.off_aacc >= 4 * GRAD_MAXPRIM
+        if L.nf <= W_SMEM:
+            assert L.off_g - L.off_w >= L.nf
