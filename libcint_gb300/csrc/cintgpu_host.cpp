@@ -1785,7 +1785,7 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
         }
     }
     for (int64_t i0 = 0, len = first; i0 < n;
-         i0 += len, len = std::min<int64_t>(std::max<int64_t>(len + 1, (int64_t)(len * growth)), cap)) {
+         i0 += len, len = std::min<int64_t>(std::max<int64_t>(len + (growth > 1.0), (int64_t)(len * growth)), cap)) {
         Chunk x;
         x.i0 = i0;
         x.n = std::min(len, n - i0);

@@ -480,8 +480,8 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
             if (own) e0f0_dispatch(mab, greg, gstride, G, na, sp, Tb, S, mine.oxy, mine.oz, mine.mn, r);
         } else if (boxed) {
             /* the class's rounds (<= 32 groups, one per lane), each dispatched on its member box */
-            for (int r = 0; r < ec.nround; r++) {
-                const int rd = __ldg(P.eround + ec.round_off + r);
+            for (int ri = 0; ri < ec.nround; ri++) {
+                const int rd = __ldg(P.eround + ec.round_off + ri);
                 if (lane >= (int)(((unsigned)rd >> 16) & 0xffu)) continue;
                 const CGEriGroup q = grp[(rd & 0xffff) + lane];
                 const int nez = q.mn & 0xff, nfz = (q.mn >> 8) & 0xff;
@@ -575,9 +575,10 @@ __device__ __forceinline__ void rys_eri_body(const CGLaunch &P)
         else run_task<MODE, 0>(P, tk, L, term, ws + L.off_g, lane);
         if (P.fuse_out) {
             /* publish this slice; the warp completing the quartet's last slice transforms it
-             * (slot writes fenced before the count, reads past L1 after it) */
-            __syncwarp();
+             * (every lane fences its slot writes, the warp syncs, then lane 0 counts; the reader
+             * fences after the count and reads past L1) */
             __threadfence();
+            __syncwarp();
             int last = 0;
             if (lane == 0) last = atomicAdd(P.done + tk.out, 1) == P.outs[tk.out].nparts - 1;
             last = __shfl_sync(FULL, last, 0);
