@@ -264,11 +264,43 @@ def extra_adjoint(cg, seed=0, natm=24):
             'adjoint_speedup_over_ip1': t_ip1 / t_adj, 'max_rel_diff_vs_ip1': diff}
 
 
+def extra_jk(cg, seed=0, natm=24):
+    """c3 J/K build (the contraction a direct-SCF driver makes of each unique quartet): J alone,
+    K alone, and J and K from one evaluation of each quartet; the JK plan's J against the J
+    plan's, and K's symmetry."""
+    import torch
+    from libcint_gb300 import molecules as M
+    from libcint_gb300.coulomb import CoulombPlans
+    box = 8.0 * (natm / 24.0) ** (1.0 / 3.0)
+    mol = M.config3(seed=seed, natm=natm, box=box)
+    nao = sum(mol.nsph(i) for i in range(mol.nbas))
+    rng = np.random.RandomState(seed)
+    d = rng.normal(0, 0.1, (nao, nao))
+    dm = torch.as_tensor(0.5 * (d + d.T), device='cuda')
+    plans = CoulombPlans(mol)
+    t_j = _timed(lambda: plans.vj(dm), reps=2)
+    t_k = _timed(lambda: plans.vk(dm), reps=2)
+    res = [None]
+
+    def jk():
+        res[0] = plans.get_jk(dm)
+    t_jk = _timed(jk, reps=2)
+    J, K = res[0]
+    J1 = plans.vj(dm)
+    return {'workload': 'c3: %d atoms, %.1f A, s,p,d x 3-5 prims, all %d unique quartets'
+                        % (natm, box, len(M.unique_quartets(mol.nbas))),
+            'J_ms': 1e3 * t_j, 'K_ms': 1e3 * t_k, 'JK_ms': 1e3 * t_jk, 'JK_over_J': t_jk / t_j,
+            'jk_J_vs_J_max_rel': float((J - J1).abs().max() / J1.abs().max()),
+            'K_asymmetry_max_rel': float((K - K.T).abs().max() / K.abs().max()),
+            'coulomb_energy': float(0.5 * (dm * J).sum()), 'exchange_energy': float(-0.25 * (dm * K).sum())}
+
+
 def run_extras(cg, mol, qs, value, args):
     out = {}
     for name, fn in (('dropin', lambda: extra_dropin(cg, mol, qs, value)),
                      ('int3c2e', lambda: extra_int3c2e(cg)),
-                     ('adjoint', lambda: extra_adjoint(cg))):
+                     ('adjoint', lambda: extra_adjoint(cg)),
+                     ('jk', lambda: extra_jk(cg))):
         try:
             out[name] = fn()
         except Exception as e:  # an extra must not hide the headline line
@@ -286,6 +318,7 @@ def run_gpu(args, rank, world):
     if args.only != 'headline':
         # one side workload alone (profiling); not the benchmark line
         fn = {'adjoint': lambda: extra_adjoint(cg, natm=args.c3_atoms),
+              'jk': lambda: extra_jk(cg, natm=args.c3_atoms),
               'int3c2e': lambda: extra_int3c2e(cg)}[args.only]
         if rank == 0:
             print(json.dumps({'extra': args.only, **fn()}), flush=True)
@@ -412,8 +445,8 @@ def main():
     ap.add_argument('--e2e-steps', type=int, default=3)
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--no-extras', action='store_true', help='skip the drop-in, int3c2e and adjoint lines')
-    ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e'],
+    ap.add_argument('--no-extras', action='store_true', help='skip the drop-in, int3c2e, adjoint and J/K lines')
+    ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk'],
                     help='run one side workload alone and print its line (profiling)')
     ap.add_argument('--c3-atoms', type=int, default=24, help='atoms of the adjoint workload')
     args = ap.parse_args()

@@ -138,6 +138,8 @@ void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas);
 #define CINTGPU_J_BUILD        7   /* J[ij] += sum_kl (ij|kl) D[kl] over the list */
 #define CINTGPU_J_GRAD         8   /* adjoint: dL/dR for L = 1/2 sum D (ij|kl) D */
 #define CINTGPU_J_GRAD_EXP     9   /* adjoint: dL/dR and dL/d(primitive exponent) */
+#define CINTGPU_K_BUILD        10  /* K[ik] += sum_jl (ij|kl) D[jl] over the list (exchange) */
+#define CINTGPU_JK_BUILD       11  /* J and K from one evaluation of each quartet */
 
 typedef struct CINTGPUPlan CINTGPUPlan;
 
@@ -179,6 +181,12 @@ int cintgpu_plan_nao_cart(const CINTGPUPlan *plan);
  * dm_dev (Cartesian, symmetric).  Only the (I >= J) shell blocks of the pair order the plan uses
  * are written; symmetrise with J = X + X^T - diag-blocks(X) (done by the Python layer). */
 int cintgpu_plan_execute_j(CINTGPUPlan *plan, const double *dm_dev, double *vj_dev, void *stream);
+/* J_BUILD / K_BUILD / JK_BUILD plans: vj_dev as above (J and JK kinds), and vk_dev (nao_cart^2, row
+ * major; K and JK kinds) += X with K = X + X^T for the symmetric dm_dev.  The pointer a kind does
+ * not use may be NULL.  No libcint counterpart: the J/K builds of direct-SCF drivers (callers of
+ * int2e_sph with the 8-fold unique quartet loop) contract each block as it is computed. */
+int cintgpu_plan_execute_jk(CINTGPUPlan *plan, const double *dm_dev, double *vj_dev, double *vk_dev,
+                            void *stream);
 /* adjoint kinds: grad_dev (natm x 3) += dL/dR; galpha_dev (sum of nprim over shells, shell
  * order; J_GRAD_EXP only, may be NULL otherwise) += dL/d(exponent) at fixed env coefficients */
 int cintgpu_plan_execute_grad(CINTGPUPlan *plan, const double *dm_dev, double *grad_dev,

@@ -86,6 +86,8 @@ def lib():
     L.cintgpu_plan_nao_cart.restype = i32
     L.cintgpu_plan_execute_j.argtypes = [vp, vp, vp, vp]
     L.cintgpu_plan_execute_j.restype = i32
+    L.cintgpu_plan_execute_jk.argtypes = [vp, vp, vp, vp, vp]
+    L.cintgpu_plan_execute_jk.restype = i32
     L.cintgpu_plan_execute_grad.argtypes = [vp, vp, vp, vp, vp]
     L.cintgpu_plan_execute_grad.restype = i32
     L.cintgpu_cart2sph.argtypes = [i32, vp]

@@ -1,4 +1,4 @@
-"""Build the CUDA library (libcintgpu.so, sm_103a) in-tree and the CPU checker libraries.
+"""Build the CUDA library (libcintgpu.so, sm_103a) in-tree and the CPU oracle libraries.
 
 The product library is compiled with nvcc from the two translation units under csrc/ in
 parallel; output goes to libcint_gb300/_build/ (git-ignored).  No cmake and no torch build step:
@@ -62,7 +62,7 @@ def build_library(force=False, verbose=False):
 
 
 def build_oracle():
-    """CPU checker: the C restatement always; libcint itself where its sources are present."""
+    """CPU oracle: the C restatement always; libcint itself where its sources are present."""
     odir = os.path.join(ROOT, 'oracle')
     subprocess.run(['make', '-s', '-C', odir, 'oracle'], check=True)
     subprocess.run(['make', '-s', '-j8', '-C', odir, 'ref-if-present'], check=True)

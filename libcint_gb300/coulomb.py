@@ -1,8 +1,9 @@
-"""Coulomb-like contraction L = 1/2 sum D_ij (ij|kl) D_kl, its J matrix, and the hand-written
-adjoint exposed through torch.autograd.Function.
+"""Coulomb-like contraction L = 1/2 sum D_ij (ij|kl) D_kl, its J matrix, the exchange matrix K,
+and the hand-written adjoint exposed through torch.autograd.Function.
 
 Forward: the CUDA kernels evaluate each unique shell quartet (i>=j, k>=l, ij>=kl) and contract it
-with the density on the fly (J_BUILD plans); no (ij|kl) is stored.  Backward: the adjoint kernel
+with the density on the fly (J_BUILD, K_BUILD and JK_BUILD plans, the J/K build of a direct-SCF
+driver); no (ij|kl) is stored.  Backward: the adjoint kernel
 (J_GRAD / J_GRAD_EXP plans) recomputes Rys roots and g arrays with raised angular momenta and
 returns dL/dR for every atom and, on request, dL/d(alpha) for every primitive exponent, at fixed
 env coefficients.  dL/dD is J itself.  Comparator: `grad_via_ip1` forms int2e_ip1 blocks on the
@@ -18,7 +19,7 @@ import numpy as np
 from . import INT2E_IP1_SPH, _check, _ptr, lib
 from .molecules import ANG_OF, ATOM_OF, NCTR_OF, NPRIM_OF, PTR_COORD, PTR_EXP, unique_quartets
 
-J_BUILD, J_GRAD, J_GRAD_EXP = 7, 8, 9
+J_BUILD, J_GRAD, J_GRAD_EXP, K_BUILD, JK_BUILD = 7, 8, 9, 10, 11
 
 
 def cart2sph_matrix(mol):
@@ -111,7 +112,7 @@ def _stream_ptr(stream):
 
 
 class CoulombPlans:
-    """Plans for one geometry: J contraction and (optionally) the adjoint."""
+    """Plans for one geometry: J and K contractions and (optionally) the adjoint."""
 
     def __init__(self, mol, quartets=None, with_exponents=False):
         import torch
@@ -121,6 +122,7 @@ class CoulombPlans:
         self.diag = torch.as_tensor(_shell_diag_mask(mol, cart=True), device='cuda')
         self.with_exponents = with_exponents
         self.jplan = _KindPlan(J_BUILD, mol, self.quartets)
+        self.kplans = {}
         self.gplan = None
 
     def dm_cart(self, dm):
@@ -128,14 +130,37 @@ class CoulombPlans:
 
     def vj(self, dm, stream=None):
         """J (spherical) for the density dm (torch, cuda, float64, symmetric)."""
+        return self.get_jk(dm, True, False, stream)[0]
+
+    def vk(self, dm, stream=None):
+        """K[i,k] = sum_jl (ij|kl) D[j,l] (spherical) for the symmetric density dm."""
+        return self.get_jk(dm, False, True, stream)[1]
+
+    def get_jk(self, dm, with_j=True, with_k=True, stream=None):
+        """(J, K) for the symmetric density dm (None for the one not asked); with both, each
+        quartet is evaluated once and contracted into both."""
         import torch
+        if not (with_j or with_k):
+            return None, None
+        kind = JK_BUILD if (with_j and with_k) else (J_BUILD if with_j else K_BUILD)
+        if kind == J_BUILD:
+            plan = self.jplan
+        else:
+            if kind not in self.kplans:
+                self.kplans[kind] = _KindPlan(kind, self.mol, self.quartets)
+            plan = self.kplans[kind]
         dmc = self.dm_cart(dm)
-        X = torch.zeros_like(dmc)
-        _check(lib().cintgpu_plan_execute_j(self.jplan._h, ctypes.c_void_p(dmc.data_ptr()),
-                                            ctypes.c_void_p(X.data_ptr()), _stream_ptr(stream)),
-               'cintgpu_plan_execute_j')
-        Jc = X + X.T - torch.where(self.diag, X, torch.zeros_like(X))
-        return self.C @ Jc @ self.C.T
+        XJ = torch.zeros_like(dmc) if with_j else None
+        XK = torch.zeros_like(dmc) if with_k else None
+        ptr = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+        _check(lib().cintgpu_plan_execute_jk(plan._h, ptr(dmc), ptr(XJ), ptr(XK), _stream_ptr(stream)),
+               'cintgpu_plan_execute_jk')
+        J = K = None
+        if with_j:
+            J = self.C @ (XJ + XJ.T - torch.where(self.diag, XJ, torch.zeros_like(XJ))) @ self.C.T
+        if with_k:
+            K = self.C @ (XK + XK.T) @ self.C.T
+        return J, K
 
     def energy(self, dm, stream=None):
         J = self.vj(dm, stream)

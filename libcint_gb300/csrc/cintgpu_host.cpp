@@ -265,7 +265,7 @@ struct CINTGPUPlan {
     int ncomp = 1;
     int sph = 1;
     int three = 0;
-    int jmode = 0;                 /* J contraction instead of stored integrals */
+    int jmode = 0;                 /* J (bit 0) / K (bit 1) contraction instead of stored integrals */
     int nao_cart = 0;
     int natm = 0;
     int64_t nprim_tot = 0;
@@ -330,6 +330,7 @@ struct CINTGPUPlan {
     double *d_wscratch = nullptr;  /* per-warp accumulators of the J contraction */
     const double *cur_dm = nullptr;  /* density / J / gradient of the execution being enqueued */
     double *cur_vj = nullptr;
+    double *cur_vk = nullptr;
     double *cur_grad = nullptr, *cur_galpha = nullptr;
     int64_t wscratch_stride = 0;
     int wscratch_warps = 0;
@@ -782,6 +783,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     case CINTGPU_INT3C2E_SPH: P->mode = CG_MODE_ERI; P->sph = 1; P->three = 1; break;
     case CINTGPU_INT3C2E_CART: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 1; break;
     case CINTGPU_J_BUILD: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; P->jmode = 1; break;
+    case CINTGPU_K_BUILD: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; P->jmode = 2; break;
+    case CINTGPU_JK_BUILD: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; P->jmode = 3; break;
     case CINTGPU_J_GRAD: P->mode = CG_MODE_GRAD; P->sph = 0; P->three = 0; break;
     case CINTGPU_J_GRAD_EXP: P->mode = CG_MODE_GRADA; P->sph = 0; P->three = 0; break;
     default: set_error("unknown integral kind %d", kind); return CINTGPU_ERR_ARG;
@@ -1278,6 +1281,7 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.wscratch_stride = P->wscratch_stride;
     L.dm = P->cur_dm;
     L.vj = P->cur_vj;
+    L.vk = P->cur_vk;
     L.nao = P->nao_cart;
     L.eclass = P->d_eclass;
     L.egroup = P->d_egroup;
@@ -1619,9 +1623,21 @@ int cintgpu_plan_debug(const CINTGPUPlan *plan, int64_t *info)
 
 int cintgpu_plan_execute_j(CINTGPUPlan *plan, const double *dm_dev, double *vj_dev, void *stream)
 {
-    if (!plan->jmode) { set_error("plan is not a J_BUILD plan"); return CINTGPU_ERR_ARG; }
+    if (plan->jmode != 1) { set_error("plan is not a J_BUILD plan"); return CINTGPU_ERR_ARG; }
+    return cintgpu_plan_execute_jk(plan, dm_dev, vj_dev, nullptr, stream);
+}
+
+int cintgpu_plan_execute_jk(CINTGPUPlan *plan, const double *dm_dev, double *vj_dev, double *vk_dev,
+                            void *stream)
+{
+    if (!plan->jmode) { set_error("plan is not a J_BUILD, K_BUILD or JK_BUILD plan"); return CINTGPU_ERR_ARG; }
+    if (!dm_dev || ((plan->jmode & 1) && !vj_dev) || ((plan->jmode & 2) && !vk_dev)) {
+        set_error("the plan needs dm%s%s", (plan->jmode & 1) ? ", vj" : "", (plan->jmode & 2) ? ", vk" : "");
+        return CINTGPU_ERR_ARG;
+    }
     plan->cur_dm = dm_dev;
-    plan->cur_vj = vj_dev;
+    plan->cur_vj = (plan->jmode & 1) ? vj_dev : nullptr;
+    plan->cur_vk = (plan->jmode & 2) ? vk_dev : nullptr;
     return execute_plan(plan, nullptr, (cudaStream_t)stream);
 }
 
@@ -1967,9 +1983,10 @@ int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,
                        const int64_t *offsets, const int *atm, int natm, const int *bas,
                        int nbas, const double *env)
 {
-    if (kind == CINTGPU_J_BUILD || kind == CINTGPU_J_GRAD || kind == CINTGPU_J_GRAD_EXP) {
-        set_error("cintgpu_batch_host computes integral blocks; J and its gradient need a density "
-                  "(cintgpu_plan_execute_j / cintgpu_plan_execute_grad)");
+    if (kind == CINTGPU_J_BUILD || kind == CINTGPU_K_BUILD || kind == CINTGPU_JK_BUILD
+        || kind == CINTGPU_J_GRAD || kind == CINTGPU_J_GRAD_EXP) {
+        set_error("cintgpu_batch_host computes integral blocks; J, K and the gradient need a density "
+                  "(cintgpu_plan_execute_jk / cintgpu_plan_execute_grad)");
         return CINTGPU_ERR_ARG;
     }
     if (n <= 0) return 0;

@@ -15,7 +15,7 @@ Layout written (all doubles as exact hexadecimal literals):
   rys_coef[off_n + ((k * n + i) * (DEG + 1) + j) * 2 + {0: s, 1: w}]   k = interval, i = root,
                                                                         j = power of y
   rys_large_r[n(n-1)/2 + i], rys_large_w[n(n-1)/2 + i]
-The checker never uses these tables: the oracle computes its roots independently.
+The oracle never uses these tables: it computes its roots independently.
 """
 import argparse
 import math

@@ -50,12 +50,58 @@ __global__ void rys_roots_kernel(const double *__restrict__ xs, int count, int n
 
 /* ------------------------------------------------------------------ main kernel */
 
-/* J contraction of one slice's Cartesian block (gctr order; linear, so slices contract
- * independently): X[i,j] += s_kl sum_kl (ij|kl) D[k,l];  X[k,l] += s_ij sum_ij (ij|kl) D[i,j] if
- * IJ != KL, s = 2 for an off-diagonal shell pair of the unique list (D and (ij|kl) symmetric). */
+/* J and K contractions of one slice's Cartesian block (gctr order; linear, so slices contract
+ * independently).  Unique quartet (ij|kl) in kernel order, D symmetric:
+ *   J (jmode bit 0): X[i,j] += s_kl sum_kl (ij|kl) D[k,l];  X[k,l] += s_ij sum_ij (ij|kl) D[i,j] if
+ *       IJ != KL, s = 2 for a pair of two different shells;  J = X + X^T - diag-blocks(X);
+ *   K (jmode bit 1): X[i,k] += w sum_jl (ij|kl) D[j,l],  X[j,k] += w sum_il (ij|kl) D[i,l],
+ *       X[i,l] += w sum_jk (ij|kl) D[j,k],  X[j,l] += w sum_ik (ij|kl) D[i,k], w halved for each
+ *       coincidence (I = J, K = L, IJ = KL): the four transposed pairs of the 8 permutations, each
+ *       counted once per distinct permutation;  K = X + X^T. */
+__device__ __forceinline__ void cg_k_contract(const CGLaunch &P, const CGTask &tk, const CGPair &pij,
+                                              const CGPair &pkl, const double *cart, int lane)
+{
+    const int nfi = ncart(pij.la), nfj = ncart(pij.lb), nfk = ncart(pkl.la), nfl = ncart(pkl.lb);
+    const int nao = P.nao;
+    const double w = ((tk.sym & 1) ? 1.0 : 0.5) * ((tk.sym & 2) ? 1.0 : 0.5) * ((tk.sym & 4) ? 1.0 : 0.5);
+    const int oi = pij.ao_a, oj = pij.ao_b, ok = pkl.ao_a, ol = pkl.ao_b;
+    const double *__restrict__ D = P.dm;
+    auto at = [&](int i, int j, int k, int l) { return cart[i + nfi * (k + nfk * (l + nfl * j))]; };
+    for (int e = lane; e < nfi * nfk; e += 32) {            /* X[i,k]: D[j,l] */
+        const int i = e % nfi, k = e / nfi;
+        double v = 0.0;
+        for (int j = 0; j < nfj; j++)
+            for (int l = 0; l < nfl; l++) v = fma(at(i, j, k, l), __ldg(D + (size_t)(oj + j) * nao + ol + l), v);
+        atomicAdd(P.vk + (size_t)(oi + i) * nao + ok + k, w * v);
+    }
+    for (int e = lane; e < nfj * nfk; e += 32) {            /* X[j,k]: D[i,l] */
+        const int j = e % nfj, k = e / nfj;
+        double v = 0.0;
+        for (int l = 0; l < nfl; l++)
+            for (int i = 0; i < nfi; i++) v = fma(at(i, j, k, l), __ldg(D + (size_t)(oi + i) * nao + ol + l), v);
+        atomicAdd(P.vk + (size_t)(oj + j) * nao + ok + k, w * v);
+    }
+    for (int e = lane; e < nfi * nfl; e += 32) {            /* X[i,l]: D[j,k] */
+        const int i = e % nfi, l = e / nfi;
+        double v = 0.0;
+        for (int j = 0; j < nfj; j++)
+            for (int k = 0; k < nfk; k++) v = fma(at(i, j, k, l), __ldg(D + (size_t)(oj + j) * nao + ok + k), v);
+        atomicAdd(P.vk + (size_t)(oi + i) * nao + ol + l, w * v);
+    }
+    for (int e = lane; e < nfj * nfl; e += 32) {            /* X[j,l]: D[i,k] */
+        const int j = e % nfj, l = e / nfj;
+        double v = 0.0;
+        for (int k = 0; k < nfk; k++)
+            for (int i = 0; i < nfi; i++) v = fma(at(i, j, k, l), __ldg(D + (size_t)(oi + i) * nao + ok + k), v);
+        atomicAdd(P.vk + (size_t)(oj + j) * nao + ol + l, w * v);
+    }
+}
+
 __device__ __forceinline__ void cg_j_contract(const CGLaunch &P, const CGTask &tk, const CGPair &pij,
                                               const CGPair &pkl, const double *cart, int lane)
 {
+    if (P.jmode & 2) cg_k_contract(P, tk, pij, pkl, cart, lane);
+    if (!(P.jmode & 1)) { __syncwarp(); return; }
     const int li = pij.la, lj = pij.lb, lk = pkl.la, ll = pkl.lb;
     const int nfi = ncart(li), nfj = ncart(lj), nfk = ncart(lk), nfl = ncart(ll);
     const int nao = P.nao;

@@ -44,12 +44,14 @@ typedef struct {
     double common_base;       /* 2 pi^3 / sqrt(pi); times the s/p factors per task */
     int three;                /* int3c2e: the fourth shell is the unit s partner */
     int ws_doubles;
-    /* J contraction (ERI mode only): accumulators in a per-warp slot, contracted at task end */
+    /* J/K contraction (ERI mode only): accumulators in a per-warp slot, contracted at task end;
+     * jmode bit 0 = J into vj, bit 1 = K into vk */
     int jmode;
     double *wscratch;         /* per-warp accumulator slots */
     int64_t wscratch_stride;
     const double *dm;         /* Cartesian density, nao x nao, row major */
     double *vj;               /* J accumulator (one triangle of shell blocks, see the host) */
+    double *vk;               /* K accumulator (X with K = X + X^T) */
     int nao;
     /* contraction-first tables (ERI mode) */
     const CGEriClass *eclass;

@@ -1,5 +1,5 @@
 /*
- * CPU restatement of libcint 6.1.1's Rys-quadrature ERIs -- TEST INFRASTRUCTURE (the checker).
+ * CPU restatement of libcint 6.1.1's Rys-quadrature ERIs -- TEST INFRASTRUCTURE (the oracle).
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU legs load this library; the product
  * (libcintgpu.so) never does.  Every function cites the libcint code whose behaviour it
@@ -35,7 +35,7 @@
 #define BAS_SLOTS       8
 
 #define MAXROOTS 24
-#define MAXL     8          /* per-shell ceiling supported by the checker (l <= 7, +1 for ip1) */
+#define MAXL     8          /* per-shell ceiling supported by the oracle (l <= 7, +1 for ip1) */
 #define MAXCART  36         /* (MAXL)(MAXL+1)/2 for l=7 */
 #define NGL      200
 
@@ -619,7 +619,7 @@ static int driver(double *out, int *dims, int *shls, int *atm, int *bas, double 
     int nf = ncart(E.l[0]) * ncart(E.l[1]) * ncart(E.l[2]) * ncart(E.l[3]);
     int nc = E.nctr[0] * E.nctr[1] * E.nctr[2] * E.nctr[3];
     if (out == NULL) {
-        /* a cache size query: the checker needs no cache, report a harmless positive size */
+        /* a cache size query: the oracle needs no cache, report a harmless positive size */
         return nf * nc * ncomp + 1;
     }
     double *gctr = malloc(sizeof(double) * (size_t)nf * nc * ncomp);

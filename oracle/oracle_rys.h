@@ -1,5 +1,5 @@
 /*
- * CPU restatement of libcint 6.1.1's Rys-quadrature two-electron integrals (the checker).
+ * CPU restatement of libcint 6.1.1's Rys-quadrature two-electron integrals (the oracle).
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and bench.py's CPU legs load
  * this library, and only as the thing the CUDA path is checked against (or as the timed CPU

@@ -1,4 +1,4 @@
-"""Loader for the CPU checker libraries (tests only).
+"""Loader for the CPU oracle libraries (tests only).
 
 liboracle.so is the C restatement in oracle/ (always built); libcint.so is the reference itself,
 compiled from its sources into oracle/_ref/ where those sources exist (not on every machine).

@@ -1,5 +1,5 @@
 """Generate tests/golden/ref_blocks.npz: libcint's own output blocks for a fixed set of shell
-quartets/triples, so the checker and the CUDA path can be compared with the reference itself on
+quartets/triples, so the oracle and the CUDA path can be compared with the reference itself on
 machines where libcint's sources (and so oracle/_ref/libcint.so) are absent.
 
 Run where libcint's sources exist:  make -C oracle ref && python tests/golden/make_ref_blocks.py

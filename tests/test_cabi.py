@@ -36,7 +36,7 @@ def test_library_exports_every_declared_function(gpulib):
     assert not missing, missing
 
 
-def test_cart2sph_rows_match_checker(gpulib, oracle):
+def test_cart2sph_rows_match_oracle(gpulib, oracle):
     L = gpulib.lib()
     ol = oracle.port.lib
     for l in range(0, 7):

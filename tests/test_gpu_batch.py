@@ -1,7 +1,7 @@
 """The one-shot host-buffer entry cintgpu_batch_host, through the C-ABI.  Without offsets it cuts
 the item list into chunks (512 items, growing to 8192) planned on host threads while the GPU runs
 earlier chunks; its output must equal one device plan over the whole list (same layout:
-component-major, blocks back to back) to the tolerance of the other parity tests, and the checker
+component-major, blocks back to back) to the tolerance of the other parity tests, and the oracle
 on a sample."""
 import numpy as np
 import pytest
@@ -39,7 +39,7 @@ def test_batch_host_chunks_match_plan(gpulib, oracle, kind, n):
     want = _plan_out(cg, k, mol, items)
     assert got.shape == want.shape
     assert_block_close(got, want, 'batch_host %s' % kind)
-    # a few items against the checker, across the chunk boundaries
+    # a few items against the oracle, across the chunk boundaries
     name = kind.lower()
     sph = name.endswith('_sph')
     nsh = items.shape[1]

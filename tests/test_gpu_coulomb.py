@@ -1,8 +1,8 @@
-"""Coulomb-like contraction and its adjoint on the GPU, checked against the checker's ERIs and
-int2e_ip1 (contracted on the host), against int2e_ip1 formed on the GPU, and against central
-finite differences (h = 1e-4 Bohr for coordinates, relative 1e-5 for exponents).
+"""Coulomb-like (J) and exchange (K) contractions and the adjoint on the GPU, checked against the
+oracle's ERIs and int2e_ip1 (contracted on the host), against int2e_ip1 formed on the GPU, and
+against central finite differences (h = 1e-4 Bohr for coordinates, relative 1e-5 for exponents).
 
-Tolerances: J and the gradients agree with the integral-level references to 1e-10 relative to
+Tolerances: J, K and the gradients agree with the integral-level references to 1e-10 relative to
 their largest element (the adjoint's target); finite differences to 1e-7 (their truncation error
 is ~h^2 |d3L|)."""
 import numpy as np
@@ -52,6 +52,38 @@ def test_j_and_energy_match_oracle(gpulib, oracle):
     J = J.cpu().numpy()
     assert np.abs(J - Jref).max() <= 1e-10 * np.abs(Jref).max()
     assert abs(float(E) - Eref) <= 1e-10 * abs(Eref)
+
+
+@pytest.mark.parametrize('basis', ['c3', 'two_column'])
+def test_k_and_jk_match_oracle(gpulib, oracle, basis):
+    """K = einsum('ijkl,jl->ik') of the oracle's full ERI tensor, from a K_BUILD plan and from a
+    JK_BUILD plan (whose J must equal the J_BUILD plan's); the two_column basis has d shells with
+    two contraction columns (shell-level coincidences across columns)."""
+    import torch
+    from libcint_gb300.coulomb import CoulombPlans
+    from tests.test_jk_algebra import _basis, _eri_full
+    if basis == 'c3':
+        mol, _ = _system()
+    else:
+        mol = _basis()
+    eri, _ = _eri_full(oracle, mol)
+    n = eri.shape[0]
+    rng = np.random.RandomState(4)
+    d = rng.normal(0, 0.1, (n, n))
+    dm = 0.5 * (d + d.T)
+    Jref = np.einsum('ijkl,kl->ij', eri, dm)
+    Kref = np.einsum('ijkl,jl->ik', eri, dm)
+    plans = CoulombPlans(mol)
+    dmt = torch.as_tensor(dm, device='cuda')
+    K = plans.vk(dmt).cpu().numpy()
+    J2, K2 = (x.cpu().numpy() for x in plans.get_jk(dmt))
+    J = plans.vj(dmt).cpu().numpy()
+    tol = 1e-10
+    assert np.abs(K - Kref).max() <= tol * np.abs(Kref).max(), np.abs(K - Kref).max()
+    assert np.abs(K2 - Kref).max() <= tol * np.abs(Kref).max(), np.abs(K2 - Kref).max()
+    assert np.abs(J2 - Jref).max() <= tol * np.abs(Jref).max(), np.abs(J2 - Jref).max()
+    assert np.abs(J2 - J).max() <= 1e-13 * np.abs(Jref).max()
+    assert np.abs(K - K.T).max() <= 1e-14 * np.abs(Kref).max()
 
 
 def _oracle_grad_ip1(oracle, mol, dm):
@@ -141,7 +173,7 @@ def test_autograd_function(gpulib):
 def test_j_high_l_per_primitive_classes(gpulib, oracle):
     """J over every unique quartet of a basis with g, h and i shells: classes with lj or ll >= 4
     take the per-primitive kernel (third task group, its own J scratch slots), the rest the
-    contraction-first one; both against the checker's ERIs contracted on the host."""
+    contraction-first one; both against the oracle's ERIs contracted on the host."""
     import torch
     from libcint_gb300.coulomb import CoulombPlans
     from tests.test_gpu_high_l import high_l_basis

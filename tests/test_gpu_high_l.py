@@ -1,7 +1,7 @@
 """h and i shells (l = 5, 6), the top of the drop-in's range: the contraction-first kernel takes its
 member-at-a-time stage 3 (lj or ll above 3), 12-13 Rys roots, the 48 KB shared-memory group and the
 separate output transform (the fused one would need gigabytes of per-warp scratch for such
-blocks).  Blocks are compared with the checker element by element through both the drop-in and a
+blocks).  Blocks are compared with the oracle element by element through both the drop-in and a
 batched plan, for int2e (sph, cart) and int3c2e (sph)."""
 import numpy as np
 import pytest
@@ -98,7 +98,7 @@ def _plan_blocks(gpulib, mol, items, env=None):
 
 def test_c1_ff_classes(gpulib, oracle):
     """Benchmark quartets whose transfer side holds an f shell (kernel-order lj or ll = 3, the
-    largest transfers the contraction-first kernel takes by default), against the checker.
+    largest transfers the contraction-first kernel takes by default), against the oracle.
     Default plans: the 1e-12 absolute bar, and 1e-8 relative on uncancelled elements (the transfer
     after contraction multiplies the three axes' rounding amplifications; measured up to 1.4e-9 on
     these quartets, i.e. ~1e-13 of the block scale).  With CINTGPU_PER_PRIMITIVE_L=3 these classes

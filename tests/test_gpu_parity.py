@@ -1,4 +1,4 @@
-"""Parity of the CUDA path (through the C-ABI) with the CPU checker and libcint's golden values.
+"""Parity of the CUDA path (through the C-ABI) with the CPU oracle and libcint's golden values.
 
 Tolerances: the reference's own accuracy statement is ~1e-12 relative (libcint README.rst:217)
 and its root fits deviate from 60-digit values by up to ~4e-12 (n = 7), so element-wise gates are
@@ -33,7 +33,7 @@ def assert_block_close(a, b, what='', scale=None):
     transfer (ij| = (i+1,j-1| + AB (i,j-1| cancels as well, so relative agreement of the cancelled
     elements is bounded by the conditioning, for libcint itself as well: elements below 1e-3 of
     the block's largest Cartesian element carry ~1e-14 of that maximum as rounding, i.e. up to
-    ~1e-10 of themselves (libcint vs the checker: 2.1e-10 at 1.1e-4 of the maximum)."""
+    ~1e-10 of themselves (libcint vs the oracle: 2.1e-10 at 1.1e-4 of the maximum)."""
     a = np.asarray(a).ravel()
     b = np.asarray(b).ravel()
     d = np.abs(a - b)

@@ -1,4 +1,4 @@
-"""The checker pinned before it is trusted: the C restatement (oracle/) against libcint's golden
+"""The oracle pinned before it is trusted: the C restatement (oracle/) against libcint's golden
 values, against libcint's own output blocks (fixture made by tests/golden/make_ref_blocks.py) and,
 where libcint was built from its sources here, against libcint live.  CPU only."""
 import os
