@@ -83,6 +83,13 @@ CACHE_SIZE_T int3c2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT na
 CACHE_SIZE_T int3c2e_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
                           FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
 void int3c2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
+/* (i|k), the density-fitting metric, real spherical / Cartesian; libcint src/cint2c2e.c:351-375
+ * (dims holds 2 entries) */
+CACHE_SIZE_T int2c2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                         FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+CACHE_SIZE_T int2c2e_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                          FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+void int2c2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
 /* libcint src/optimizer.c:40-72 */
 void CINTdel_2e_optimizer(CINTOpt **opt);
 void CINTdel_optimizer(CINTOpt **opt);
@@ -106,6 +113,12 @@ FINT cint3c2e_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FIN
                    double *env, CINTOpt *opt);
 void cint3c2e_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas,
                             double *env);
+FINT cint2c2e_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                  double *env, CINTOpt *opt);
+FINT cint2c2e_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                   double *env, CINTOpt *opt);
+void cint2c2e_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                            double *env);
 
 /* basis helpers; libcint src/misc.c:86-93, src/cint_bas.c:25-147 */
 double CINTgto_norm(FINT n, double a);
@@ -124,6 +137,8 @@ void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas);
 #define CINTGPU_INT2E_IP1_CART 4
 #define CINTGPU_INT3C2E_SPH    5
 #define CINTGPU_INT3C2E_CART   6
+#define CINTGPU_INT2C2E_SPH    12
+#define CINTGPU_INT2C2E_CART   13
 
 #define CINTGPU_OK              0
 #define CINTGPU_ERR_ARG        -1   /* invalid argument (shell index, l, nprim, omega != 0) */
@@ -143,7 +158,7 @@ void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas);
 
 typedef struct CINTGPUPlan CINTGPUPlan;
 
-/* Build a plan for n items (4 shell indices each, 3 for int3c2e) of one integral kind.
+/* Build a plan for n items (4 shell indices each, 3 for int3c2e, 2 for int2c2e) of one kind.
  * offsets[q] (may be NULL) is the element offset of item q's dense block in the output of one
  * component; NULL packs the blocks back to back in item order.  The plan copies everything it
  * needs; atm/bas/env may be freed afterwards. */

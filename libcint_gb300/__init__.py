@@ -13,7 +13,8 @@ from .build import LIB as _LIB_PATH, build, build_library  # noqa: F401
 from . import molecules  # noqa: F401
 
 INT2E_SPH, INT2E_CART, INT2E_IP1_SPH, INT2E_IP1_CART, INT3C2E_SPH, INT3C2E_CART = 1, 2, 3, 4, 5, 6
-_KIND_NSH = {1: 4, 2: 4, 3: 4, 4: 4, 5: 3, 6: 3}
+INT2C2E_SPH, INT2C2E_CART = 12, 13
+_KIND_NSH = {1: 4, 2: 4, 3: 4, 4: 4, 5: 3, 6: 3, 12: 2, 13: 2}
 
 _lib = None
 
@@ -34,16 +35,16 @@ def lib():
     L = ctypes.CDLL(_LIB_PATH)
     vp, i32, i64, dbl = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
     for name in ('int2e_sph', 'int2e_cart', 'int2e_ip1_sph', 'int2e_ip1_cart', 'int3c2e_sph',
-                 'int3c2e_cart'):
+                 'int3c2e_cart', 'int2c2e_sph', 'int2c2e_cart'):
         f = getattr(L, name)
         f.restype = i32
         f.argtypes = [vp, vp, vp, vp, i32, vp, i32, vp, vp, vp]
     for name in ('cint2e_sph', 'cint2e_cart', 'cint2e_ip1_sph', 'cint2e_ip1_cart', 'cint3c2e_sph',
-                 'cint3c2e_cart'):
+                 'cint3c2e_cart', 'cint2c2e_sph', 'cint2c2e_cart'):
         f = getattr(L, name)
         f.restype = i32
         f.argtypes = [vp, vp, vp, i32, vp, i32, vp, vp]
-    for name in ('int2e_optimizer', 'int2e_ip1_optimizer', 'int3c2e_optimizer'):
+    for name in ('int2e_optimizer', 'int2e_ip1_optimizer', 'int3c2e_optimizer', 'int2c2e_optimizer'):
         f = getattr(L, name)
         f.restype = None
         f.argtypes = [vp, vp, i32, vp, i32, vp]
@@ -112,7 +113,8 @@ def _check(rc, what):
 
 
 class Plan:
-    """A batched evaluation plan: n items (shell quartets, or triples for int3c2e) of one kind.
+    """A batched evaluation plan: n items (shell quartets; triples for int3c2e, pairs for int2c2e)
+    of one kind.
 
     execute(out) enqueues the kernels writing into a CUDA float64 buffer (a torch tensor or a raw
     device pointer) of ncomp * output_size elements; block q of component c starts at
@@ -174,7 +176,7 @@ class Plan:
 def batch_host(kind, mol, shls, offsets=None):
     """One-shot host-buffer evaluation: returns (ncomp, output_size) float64 numpy array."""
     shls = np.ascontiguousarray(shls, dtype=np.int32).reshape(-1, _KIND_NSH.get(kind, 4))
-    sph = kind in (INT2E_SPH, INT2E_IP1_SPH, INT3C2E_SPH)
+    sph = kind in (INT2E_SPH, INT2E_IP1_SPH, INT3C2E_SPH, INT2C2E_SPH)
     ncomp = 3 if kind in (INT2E_IP1_SPH, INT2E_IP1_CART) else 1
     per = np.array([mol.nsph(s) if sph else mol.ncart(s) for s in range(mol.nbas)], dtype=np.int64)
     blocks = np.prod(per[shls], axis=1) if len(shls) else np.zeros(0, np.int64)
@@ -195,7 +197,7 @@ def dropin(name, mol, shls, dims=None, nbas=None):
     block; returns (flag, out) with out the dense block (Fortran order, components last)."""
     L = lib()
     f = getattr(L, name)
-    nsh = 3 if 'int3c2e' in name else 4
+    nsh = 3 if 'int3c2e' in name else (2 if 'int2c2e' in name else 4)
     shls = np.ascontiguousarray(shls, dtype=np.int32)
     sph = name.endswith('_sph')
     ncomp = 3 if '_ip1' in name else 1

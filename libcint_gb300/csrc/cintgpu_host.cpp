@@ -264,7 +264,8 @@ struct CINTGPUPlan {
     int mode = CG_MODE_ERI;
     int ncomp = 1;
     int sph = 1;
-    int three = 0;
+    int three = 0;                 /* int3c2e and int2c2e: slot 3 is a unit s partner */
+    int two = 0;                   /* int2c2e: slot 1 is a unit s partner as well */
     int jmode = 0;                 /* J (bit 0) / K (bit 1) contraction instead of stored integrals */
     int nao_cart = 0;
     int natm = 0;
@@ -768,6 +769,20 @@ static bool per_primitive(const CINTGPUPlan *P, const int *l)
 }
 
 /* Build the host images. split_target: minimum number of compute tasks wanted (0 = no split). */
+/* shell indices per item of an integral kind */
+static int kind_shells(int kind)
+{
+    if (kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART) return 3;
+    if (kind == CINTGPU_INT2C2E_SPH || kind == CINTGPU_INT2C2E_CART) return 2;
+    return 4;
+}
+
+static bool kind_sph(int kind)
+{
+    return kind == CINTGPU_INT2E_SPH || kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT3C2E_SPH
+        || kind == CINTGPU_INT2C2E_SPH;
+}
+
 static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, const int64_t *offsets,
                       const int *atm, int natm, const int *bas, int nbas, const double *env,
                       int64_t split_target)
@@ -782,6 +797,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     case CINTGPU_INT2E_IP1_CART: P->mode = CG_MODE_IP1; P->sph = 0; P->three = 0; break;
     case CINTGPU_INT3C2E_SPH: P->mode = CG_MODE_ERI; P->sph = 1; P->three = 1; break;
     case CINTGPU_INT3C2E_CART: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 1; break;
+    case CINTGPU_INT2C2E_SPH: P->mode = CG_MODE_ERI; P->sph = 1; P->three = 1; P->two = 1; break;
+    case CINTGPU_INT2C2E_CART: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 1; P->two = 1; break;
     case CINTGPU_J_BUILD: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; P->jmode = 1; break;
     case CINTGPU_K_BUILD: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; P->jmode = 2; break;
     case CINTGPU_JK_BUILD: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; P->jmode = 3; break;
@@ -794,7 +811,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         set_error("range-separated Coulomb (env[PTR_RANGE_OMEGA] = %g) is not supported", env[PTR_RANGE_OMEGA]);
         return CINTGPU_ERR_UNSUPPORTED;
     }
-    /* src/g2e.c:57-62 (+1) and src/g3c2e.c:55-59 (no +1) */
+    /* src/g2e.c:57-62 (+1), src/g3c2e.c:55-59 and src/g2c2e.c:44-48 (no +1) */
     if (env[PTR_EXPCUTOFF] == 0) P->expcutoff = 60;
     else P->expcutoff = std::max(40.0, env[PTR_EXPCUTOFF]) + (P->three ? 0 : 1);
     P->nitems = n;
@@ -816,7 +833,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         B.ao_loc = &ao_loc;
         B.prim_loc = &prim_loc;
     }
-    const int nsh = P->three ? 3 : 4;
+    const int nsh = kind_shells(kind);
     const int dinc = P->mode == CG_MODE_IP1 ? 1 : 0;
 
     struct Pending { int pij, pkl, out; int64_t npq; int l[4]; int sym; };
@@ -838,14 +855,18 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
                 }
             }
         }
+        /* int2c2e (i|k) runs as (i s0|k s0): request shells 0, 1 in kernel slots 0, 2 */
+        if (P->two) { sv[2] = sv[1]; sv[1] = sv[0]; sv[1].l = 0; sv[1].nprim = 1; sv[1].nctr = 1; }
         if (P->three) { sv[3] = sv[2]; sv[3].l = 0; sv[3].nprim = 1; sv[3].nctr = 1; }
+        auto unit = [&](int a) { return (a == 3 && P->three) || (a == 1 && P->two); };
         int d[4], nd[4];
         for (int a = 0; a < 4; a++) {
-            d[a] = (a == 3 && P->three) ? 1 : (P->sph ? nsph_l(sv[a].l) : ncart_l(sv[a].l));
-            nd[a] = d[a] * ((a == 3 && P->three) ? 1 : sv[a].nctr);
+            d[a] = unit(a) ? 1 : (P->sph ? nsph_l(sv[a].l) : ncart_l(sv[a].l));
+            nd[a] = d[a] * (unit(a) ? 1 : sv[a].nctr);
         }
         int64_t req_st[4] = {1, nd[0], (int64_t)nd[0] * nd[1], (int64_t)nd[0] * nd[1] * nd[2]};
         if (P->three) req_st[3] = 0;
+        if (P->two) req_st[1] = 0;
         int64_t block = (int64_t)nd[0] * nd[1] * nd[2] * nd[3];
         int64_t base = offsets ? offsets[q] : next_off;
         next_off = std::max(next_off, base + block);
@@ -861,7 +882,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         }
         const ShellView *kv[4] = {&sv[perm[0]], &sv[perm[1]], &sv[perm[2]], &sv[perm[3]]};
         int ksh[4];
-        for (int k = 0; k < 4; k++) ksh[k] = (P->three && k == 3) ? -1 : s[perm[k]];
+        for (int k = 0; k < 4; k++) ksh[k] = unit(k) ? -1 : s[P->two ? perm[k] / 2 : perm[k]];
         /* permutation flags of the unique quartet, in kernel order (the J epilogue weights the
          * kernel's bra and ket blocks with them) */
         int qsym = 0;
@@ -878,7 +899,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         for (int c1 = 0; c1 < nct[1]; c1++)
         for (int c0 = 0; c0 < nct[0]; c0++) {
             int cc[4] = {c0, c1, c2, c3};
-            int pij = B.pair(ksh[0], *kv[0], c0, ksh[1], *kv[1], c1, kl_[0] + dinc + kl_[1]);
+            int pij = P->two ? B.single(ksh[0], *kv[0], c0)
+                             : B.pair(ksh[0], *kv[0], c0, ksh[1], *kv[1], c1, kl_[0] + dinc + kl_[1]);
             int pkl = P->three ? B.single(ksh[2], *kv[2], c2)
                                : B.pair(ksh[2], *kv[2], c2, ksh[3], *kv[3], c3, kl_[2] + kl_[3]);
             CGOutTask o;
@@ -1259,6 +1281,7 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     const TaskGroup &G = P->groups[g];
     if (G.ntasks == 0) return 0;
     CGLaunch L;
+    memset(&L, 0, sizeof(L));
     L.tasks = P->d_tasks;
     L.task0 = G.task0;
     L.ntasks = G.ntasks;
@@ -1272,6 +1295,7 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.rys_coef = g_ctx.rys_coef;
     L.common_base = M_PI * M_PI * M_PI * 2 / 1.7724538509055160272981674833411451;
     L.three = P->three;
+    L.two = P->two;
     L.ws_doubles = G.ws;
     L.jmode = P->jmode;
     L.wscratch = P->d_wscratch;
@@ -1393,10 +1417,22 @@ int grow_host(char **p, size_t *cap, size_t need)
     return 0;
 }
 
-/* libcint cache-size formula of CINT2e_drv / CINT3c2e_drv (src/cint2e.c:779-816,
- * src/cint3c2e.c:545-567) so out == NULL queries return the same number. */
+/* libcint cache-size formula of CINT2e_drv / CINT3c2e_drv / CINT2c2e_drv (src/cint2e.c:779-816,
+ * src/cint3c2e.c:545-567, src/cint2c2e.c:244-246 with int1e_cache_size, src/cint1e.c:163-183) so
+ * out == NULL queries return the same number. */
 CACHE_SIZE_T cache_size_query(int kind, const int *shls, const int *bas)
 {
+    if (kind_shells(kind) == 2) {
+        /* CINTinit_int2c2e_EnvVars: g_size = nroots (li+1) (lk+1), i and k in the 1e slots */
+        const int *bi = bas + BAS_SLOTS * shls[0], *bk = bas + BAS_SLOTS * shls[1];
+        const int64_t li = bi[ANG_OF], lk = bk[ANG_OF];
+        const int64_t ip = bi[NPRIM_OF], kp = bk[NPRIM_OF], ic = bi[NCTR_OF], kc = bk[NCTR_OF];
+        const int64_t nf = (int64_t)ncart_l((int)li) * ncart_l((int)lk);
+        const int64_t nc = nf * ic * kc;
+        const int64_t leng = ((li + lk) / 2 + 1) * (li + 1) * (lk + 1) * 3 * 2;
+        const int64_t pdata = ip * kp * 5 + ip * ic + kp * kc + (ip + kp) * 2 + nf * 3;
+        return (CACHE_SIZE_T)std::max(nc + leng + nf * nc + nf * ic + nf + pdata, nc + nf * 8 * 2);
+    }
     int three = kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART;
     int ip1 = kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT2E_IP1_CART;
     int nsh = three ? 3 : 4;
@@ -1440,18 +1476,19 @@ CACHE_SIZE_T dropin(int kind, double *out, FINT *dims, FINT *shls, FINT *atm, FI
                     FINT *bas, FINT nbas, double *env)
 {
     if (out == NULL) return cache_size_query(kind, shls, bas);
-    int three = kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART;
-    int nsh = three ? 3 : 4;
+    const int nsh = kind_shells(kind);
     int ncomp = (kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT2E_IP1_CART) ? 3 : 1;
-    int sph = kind == CINTGPU_INT2E_SPH || kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT3C2E_SPH;
+    int sph = kind_sph(kind);
     int counts[4] = {1, 1, 1, 1};
     for (int a = 0; a < nsh; a++) {
         const int *b = bas + BAS_SLOTS * shls[a];
         int l = b[ANG_OF];
         counts[a] = (sph ? nsph_l(l) : ncart_l(l)) * b[NCTR_OF];
     }
-    int *d = dims ? dims : counts;
-    int64_t nout = (int64_t)d[0] * d[1] * d[2] * (three ? 1 : d[3]);
+    /* the caller's dims hold one entry per shell (2, 3 or 4); padded with 1 */
+    int d[4] = {1, 1, 1, 1};
+    for (int a = 0; a < nsh; a++) d[a] = dims ? dims[a] : counts[a];
+    int64_t nout = (int64_t)d[0] * d[1] * d[2] * d[3];
     auto zero_fill = [&]() {
         for (int comp = 0; comp < ncomp; comp++)
             for (int l = 0; l < counts[3]; l++)
@@ -1742,10 +1779,9 @@ thread_local BatchCtx tl_batch;
 /* doubles of one component of item q's output block (libcint's dims for the kind) */
 int64_t item_block(int kind, const int *q, const int *bas)
 {
-    const bool three = kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART;
-    const bool sph = kind == CINTGPU_INT2E_SPH || kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT3C2E_SPH;
+    const bool sph = kind_sph(kind);
     int64_t b = 1;
-    for (int a = 0; a < (three ? 3 : 4); a++) {
+    for (int a = 0; a < kind_shells(kind); a++) {
         const int *s = bas + BAS_SLOTS * q[a];
         b *= (int64_t)(sph ? nsph_l(s[ANG_OF]) : ncart_l(s[ANG_OF])) * s[NCTR_OF];
     }
@@ -1770,7 +1806,7 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
     BatchCtx &X = tl_batch;
     int rc = X.init();
     if (rc) return rc;
-    const int nsh = (kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART) ? 3 : 4;
+    const int nsh = kind_shells(kind);
     for (int64_t q = 0; q < n; q++)
         for (int a = 0; a < nsh; a++)
             if (shls[nsh * q + a] < 0 || shls[nsh * q + a] >= nbas) {
@@ -2033,6 +2069,12 @@ CACHE_SIZE_T int3c2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT na
 CACHE_SIZE_T int3c2e_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                           FINT nbas, double *env, CINTOpt *opt, double *cache)
 { (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int2c2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                         FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT2C2E_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int2c2e_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                          FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT2C2E_CART, out, dims, shls, atm, natm, bas, nbas, env); }
 
 /* The optimizer holds no precomputed data here: pair data are rebuilt per call on the host,
  * which is exactly what libcint's pair tables save it; the struct keeps libcint's layout. */
@@ -2041,6 +2083,8 @@ void int2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, 
 void int2e_ip1_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
 { (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
 void int3c2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
+void int2c2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
 { (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
 void CINTdel_2e_optimizer(CINTOpt **opt)
 {
@@ -2068,6 +2112,12 @@ FINT cint3c2e_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FIN
 { return int3c2e_cart(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
 void cint3c2e_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
 { int3c2e_optimizer(opt, atm, natm, bas, nbas, env); }
+FINT cint2c2e_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int2c2e_sph(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+FINT cint2c2e_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int2c2e_cart(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+void cint2c2e_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ int2c2e_optimizer(opt, atm, natm, bas, nbas, env); }
 
 /* ---- basis helpers (libcint src/misc.c:72-93, src/cint_bas.c) ------------------------------ */
 double CINTgto_norm(FINT n, double a)

@@ -151,7 +151,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
     const int nfi = ncart(li), nfj = ncart(lj), nfk = ncart(lk), nfl = ncart(ll);
     const int n = L.nroots;
     const int T = L.T;
-    const double common = P.common_base * common_fac_sp(li) * common_fac_sp(lj)
+    const double common = P.common_base * common_fac_sp(li) * (P.two ? 1.0 : common_fac_sp(lj))
                         * common_fac_sp(lk) * (P.three ? 1.0 : common_fac_sp(ll));
     double *scr_base = greg + T * L.gstride;
     double *acc = P.jmode ? P.wscratch + (size_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * P.wscratch_stride
@@ -467,7 +467,7 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
     const int nij = pij.npa * pij.npb;
     const int li = pij.la, lj = pij.lb, lk = pkl.la, ll = pkl.lb;
     const int n = L.nroots, T = L.T, G = L.gax, gstride = L.gstride, na = L.nmax + 1;   /* G: axis stride */
-    const double common = P.common_base * common_fac_sp(li) * common_fac_sp(lj)
+    const double common = P.common_base * common_fac_sp(li) * (P.two ? 1.0 : common_fac_sp(lj))
                         * common_fac_sp(lk) * (P.three ? 1.0 : common_fac_sp(ll));
     const CGEriClass ec = P.eclass[tk.cls];
     const CGEriGroup *__restrict__ grp = P.egroup + ec.group_off;

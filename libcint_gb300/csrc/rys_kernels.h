@@ -42,7 +42,8 @@ typedef struct {
     int *status;
     const double *rys_coef;
     double common_base;       /* 2 pi^3 / sqrt(pi); times the s/p factors per task */
-    int three;                /* int3c2e: the fourth shell is the unit s partner */
+    int three;                /* int3c2e, int2c2e: the fourth shell is the unit s partner */
+    int two;                  /* int2c2e: the second shell is a unit s partner as well */
     int ws_doubles;
     /* J/K contraction (ERI mode only): accumulators in a per-warp slot, contracted at task end;
      * jmode bit 0 = J into vj, bit 1 = K into vk */

@@ -233,7 +233,8 @@ int oracle_cart2sph_coeff(int l, double *c)
 
 /* ------------------------------------------------------------------ integral engine */
 typedef struct {
-    int l[4];          /* angular momentum per slot (slot 3 is a dummy s shell for 3c2e) */
+    int l[4];          /* angular momentum per slot (slot 3 is a dummy s shell for 3c2e, slots 1
+                          and 3 for 2c2e) */
     int lc[4];         /* g-array ceilings, l + derivative increment */
     int nprim[4], nctr[4];
     double r[4][3];
@@ -241,7 +242,7 @@ typedef struct {
     double dummy_exp, dummy_cf;
     double common;
     double expcutoff;
-    int three_center;
+    int three_center;  /* 0 int2e, 1 int3c2e, 2 int2c2e */
     int deriv_i;       /* 1 for ip1 */
     int nroots;
 } OEnv;
@@ -265,14 +266,36 @@ static void load_shell(OEnv *E, int slot, int sh, int *atm, int *bas, double *en
     E->cf[slot] = env + b[PTR_COEFF];
 }
 
-/* CINTinit_int2e_EnvVars (src/g2e.c:21-172) / CINTinit_int3c2e_EnvVars (src/g3c2e.c:21-132) */
+/* CINTinit_int2e_EnvVars (src/g2e.c:21-172) / CINTinit_int3c2e_EnvVars (src/g3c2e.c:21-132) /
+ * CINTinit_int2c2e_EnvVars (src/g2c2e.c:16-56): int2c2e's (i|k) is (i s0|k s0) with two dummy
+ * zero-exponent unit s shells, the common factor of i and k only and no +1 on the cutoff */
 static void init_env(OEnv *E, int *shls, int *atm, int *bas, double *env, int three, int dinc)
 {
     memset(E, 0, sizeof(*E));
+    E->three_center = three;
+    if (three == 2) {
+        load_shell(E, 0, shls[0], atm, bas, env);
+        load_shell(E, 2, shls[1], atm, bas, env);
+        E->dummy_exp = 0; E->dummy_cf = 1;
+        const int units[2] = {1, 3};
+        for (int u = 0; u < 2; u++) {
+            const int s = units[u];
+            E->l[s] = 0; E->nprim[s] = 1; E->nctr[s] = 1;
+            memcpy(E->r[s], E->r[s - 1], sizeof(double) * 3);
+            E->ex[s] = &E->dummy_exp; E->cf[s] = &E->dummy_cf;
+        }
+        E->common = M_PI * M_PI * M_PI * 2 / 1.7724538509055160272981674833411451
+                  * common_fac_sp(E->l[0]) * common_fac_sp(E->l[2]);
+        E->expcutoff = env[PTR_EXPCUTOFF] == 0 ? 60 : fmax(40, env[PTR_EXPCUTOFF]);
+        E->deriv_i = dinc;
+        for (int s = 0; s < 4; s++) E->lc[s] = E->l[s];
+        E->lc[0] += dinc;
+        E->nroots = (E->lc[0] + E->lc[2]) / 2 + 1;
+        return;
+    }
     load_shell(E, 0, shls[0], atm, bas, env);
     load_shell(E, 1, shls[1], atm, bas, env);
     load_shell(E, 2, shls[2], atm, bas, env);
-    E->three_center = three;
     if (three) {
         E->l[3] = 0; E->nprim[3] = 1; E->nctr[3] = 1;
         memcpy(E->r[3], E->r[2], sizeof(double) * 3);
@@ -481,8 +504,15 @@ static int contracted(const OEnv *E, double *gctr, int ncomp)
     log_maxc(E->cf[2], E->nprim[2], E->nctr[2], lck);
     log_maxc(E->cf[3], E->nprim[3], E->nctr[3], lcl);
     OPair *pij = malloc(sizeof(OPair) * E->nprim[0] * E->nprim[1]);
-    if (set_pairdata(pij, E->ex[0], E->ex[1], E->r[0], E->r[1], lci, lcj, E->lc[0], E->lc[1],
-                     E->nprim[0], E->nprim[1], E->expcutoff)) {
+    if (E->three_center == 2) {
+        /* CINT2c2e_loop_nopt (src/cint2c2e.c:58-150): no primitive screening */
+        for (int ip = 0; ip < E->nprim[0]; ip++) {
+            memcpy(pij[ip].r, E->r[0], sizeof(double) * 3);
+            pij[ip].e = 1.0;
+            pij[ip].cce = -HUGE_VAL;
+        }
+    } else if (set_pairdata(pij, E->ex[0], E->ex[1], E->r[0], E->r[1], lci, lcj, E->lc[0], E->lc[1],
+                            E->nprim[0], E->nprim[1], E->expcutoff)) {
         free(pij);
         return 0;
     }
@@ -563,7 +593,8 @@ static void write_out(const OEnv *E, const double *gctr, double *out, int *dims,
     int counts[4];
     for (int s = 0; s < 4; s++) counts[s] = nds[s] * E->nctr[s];
     int d[4];
-    if (dims) { d[0] = dims[0]; d[1] = dims[1]; d[2] = dims[2]; d[3] = E->three_center ? 1 : dims[3]; }
+    if (dims && E->three_center == 2) { d[0] = dims[0]; d[1] = 1; d[2] = dims[1]; d[3] = 1; }
+    else if (dims) { d[0] = dims[0]; d[1] = dims[1]; d[2] = dims[2]; d[3] = E->three_center ? 1 : dims[3]; }
     else memcpy(d, counts, sizeof(d));
     size_t nout = (size_t)d[0] * d[1] * d[2] * d[3];
     const int nf = nfs[0] * nfs[1] * nfs[2] * nfs[3];
@@ -647,6 +678,12 @@ int oracle_int3c2e_sph(double *out, int *dims, int *shls, int *atm, int natm,
 int oracle_int3c2e_cart(double *out, int *dims, int *shls, int *atm, int natm,
                         int *bas, int nbas, double *env, void *opt, double *cache)
 { (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 1, 0, 0); }
+int oracle_int2c2e_sph(double *out, int *dims, int *shls, int *atm, int natm,
+                       int *bas, int nbas, double *env, void *opt, double *cache)
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 2, 0, 1); }
+int oracle_int2c2e_cart(double *out, int *dims, int *shls, int *atm, int natm,
+                        int *bas, int nbas, double *env, void *opt, double *cache)
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 2, 0, 0); }
 
 double oracle_int2e_sph_list(const int *quartets, long nq, double *out, const long *offsets,
                              int *atm, int natm, int *bas, int nbas, double *env, int nthreads)

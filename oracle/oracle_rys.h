@@ -37,6 +37,10 @@ int oracle_int3c2e_sph(double *out, int *dims, int *shls, int *atm, int natm,
                        int *bas, int nbas, double *env, void *opt, double *cache);
 int oracle_int3c2e_cart(double *out, int *dims, int *shls, int *atm, int natm,
                         int *bas, int nbas, double *env, void *opt, double *cache);
+int oracle_int2c2e_sph(double *out, int *dims, int *shls, int *atm, int natm,
+                       int *bas, int nbas, double *env, void *opt, double *cache);
+int oracle_int2c2e_cart(double *out, int *dims, int *shls, int *atm, int natm,
+                        int *bas, int nbas, double *env, void *opt, double *cache);
 
 /* Cartesian -> real solid harmonic coefficient matrix for angular momentum l, written as
  * c[m*ncart + icart] (2l+1 rows).  l = 0,1 give the identity (their factors live in the

@@ -14,7 +14,8 @@ ODIR = os.path.join(ROOT, 'oracle')
 ORACLE_SO = os.path.join(ODIR, '_build', 'liboracle.so')
 REF_SO = os.path.join(ODIR, '_ref', 'libcint.so')
 
-_SIG = ('int2e_sph', 'int2e_cart', 'int2e_ip1_sph', 'int2e_ip1_cart', 'int3c2e_sph', 'int3c2e_cart')
+_SIG = ('int2e_sph', 'int2e_cart', 'int2e_ip1_sph', 'int2e_ip1_cart', 'int3c2e_sph', 'int3c2e_cart',
+        'int2c2e_sph', 'int2c2e_cart')
 
 
 class _Lib:
@@ -29,7 +30,7 @@ class _Lib:
 
     def call(self, name, mol, shls, dims=None, nbas=None):
         f = getattr(self.lib, self.prefix + name)
-        nsh = 3 if 'int3c2e' in name else 4
+        nsh = 3 if 'int3c2e' in name else (2 if 'int2c2e' in name else 4)
         shls = np.ascontiguousarray(shls, dtype=np.int32)
         sph = name.endswith('_sph')
         ncomp = 3 if '_ip1' in name else 1

@@ -10,7 +10,9 @@ Contents (all through libcint 6.1.1 built by oracle/Makefile, opt = NULL, cache 
                                      (nbas = 4 passed, 8 shells)
   c0_int2e_sph / c0_int2e_cart / c0_int2e_ip1_sph   60 unique quartets of molecules.config0(3)
   c2_int3c2e_sph                     60 (ij|P) triples of molecules.config2(1, natm=6, box=5)
-  cache_sizes                        the out == NULL cache-size answers for a few quartets
+  c2_int2c2e_sph / c2_int2c2e_cart   60 (i|k) pairs of the same molecule (orbital and auxiliary)
+  kat_int2c2e_sph                    all 8 x 8 shell pairs of the self-contained basis
+  cache_sizes                        the out == NULL cache-size answers for a few items
 Each block is stored flattened in libcint's (Fortran) order with its item list.
 """
 import ctypes
@@ -61,12 +63,23 @@ def main():
     out['c2_int3c2e_sph_items'] = tr
     out['c2_int3c2e_sph'] = np.concatenate([o.ref.call('int3c2e_sph', mol2, t)[1].ravel(order='F')
                                             for t in tr])
+    pr = np.array([(rng.randint(0, mol2.nbas), rng.randint(0, mol2.nbas)) for _ in range(60)],
+                  dtype=np.int32)
+    for name in ('int2c2e_sph', 'int2c2e_cart'):
+        out['c2_' + name + '_items'] = pr
+        out['c2_' + name] = np.concatenate([o.ref.call(name, mol2, t)[1].ravel(order='F') for t in pr])
+    kp = np.array([(i, k) for k in range(8) for i in range(8)], dtype=np.int32)
+    out['kat_int2c2e_sph_items'] = kp
+    out['kat_int2c2e_sph'] = np.concatenate([o.ref.call('int2c2e_sph', mol, t, nbas=nbas)[1]
+                                             .ravel(order='F') for t in kp])
     # cache-size answers (out == NULL)
     f = o.ref.lib
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     cs = []
     for name, q in (('int2e_sph', (1, 3, 5, 7)), ('int2e_ip1_sph', (3, 1, 2, 0)),
-                    ('int2e_cart', (1, 1, 0, 0)), ('int3c2e_sph', (2, 1, 3, 0))):
+                    ('int2e_cart', (1, 1, 0, 0)), ('int3c2e_sph', (2, 1, 3, 0)),
+                    ('int2c2e_sph', (1, 3, 0, 0)), ('int2c2e_cart', (6, 2, 0, 0)),
+                    ('int2c2e_sph', (5, 5, 0, 0))):
         shls = np.array(q, dtype=np.int32)
         r = getattr(f, name)(None, None, P(shls), P(mol.atm), mol.natm, P(mol.bas), nbas,
                              P(mol.env), None, None)
