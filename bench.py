@@ -224,10 +224,20 @@ def extra_int3c2e(cg, seed=0, npairs=40):
     out = torch.empty(p.output_size, dtype=torch.float64, device='cuda')
     dt = _timed(lambda: p.execute(out))
     nint = sum(mol.nsph(int(a)) * mol.nsph(int(b)) * mol.nsph(int(c)) for a, b, c in tri)
+    # int2c2e: the metric (P|Q) over every unique pair of auxiliary shells (P >= Q)
+    pi, qi = np.tril_indices(len(aux))
+    pq = np.stack([aux[pi], aux[qi]], 1).astype(np.int32)
+    p2 = cg.Plan(cg.INT2C2E_SPH, mol, pq)
+    out2 = torch.empty(p2.output_size, dtype=torch.float64, device='cuda')
+    dt2 = _timed(lambda: p2.execute(out2))
+    ns = np.array([mol.nsph(int(a)) for a in aux], dtype=np.int64)
+    nint2 = int((ns[pi] * ns[qi]).sum())
     return {'workload': 'c2: 200 atoms, 18 A; %d screened orbital pairs x all 2000 aux shells '
                         '(Q_ij Q_P >= 1e-12)' % len(pr),
             'triples': int(len(tri)), 'integrals_per_s': nint / dt, 'ms': 1e3 * dt,
-            'fp64_frac': p.flops / dt / 1e12 / FP64_PEAK_TFLOPS}
+            'fp64_frac': p.flops / dt / 1e12 / FP64_PEAK_TFLOPS,
+            'int2c2e_metric': {'pairs': int(len(pq)), 'integrals': nint2, 'ms': 1e3 * dt2,
+                               'integrals_per_s': nint2 / dt2}}
 
 
 def extra_adjoint(cg, seed=0, natm=24):
