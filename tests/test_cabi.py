@@ -85,3 +85,27 @@ def test_no_gpu_fails_loudly(gpulib):
         gpulib.Plan(gpulib.INT2E_SPH, mol, M.unique_quartets(mol.nbas)[:4])
     flag, blk = gpulib.dropin('int2e_sph', mol, (1, 0, 0, 0))
     assert flag == 0 and not blk.any() and gpulib.last_error()
+
+
+@pytest.mark.parametrize('name,nsh', [('int2e_sph', 4), ('int2e_cart', 4), ('int2e_ip1_sph', 4),
+                                      ('int2e_ip1_cart', 4), ('int3c2e_sph', 3),
+                                      ('int3c2e_cart', 3), ('int2c2e_sph', 2), ('int2c2e_cart', 2)])
+def test_cache_size_query_matches_libcint_live(gpulib, oracle, name, nsh):
+    """out == NULL answers for 200 random shell sets of the KAT basis (general contractions,
+    l <= 4) and of c2 (1-6 primitives, auxiliary l <= 4), against libcint compiled from its
+    sources; a pure host path."""
+    if oracle.ref is None:
+        pytest.skip('libcint not built from sources on this machine')
+    L = gpulib.lib()
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    kat, nk = M.kat_basis()
+    c2, _ = M.config2(seed=1, natm=4, box=4.0)
+    rng = np.random.RandomState(nsh)
+    for mol, nb, top in ((kat, nk, 8), (c2, c2.nbas, c2.nbas)):
+        for _ in range(100):
+            s = np.ascontiguousarray(rng.randint(0, top, 4), dtype=np.int32)
+            got = getattr(L, name)(None, None, P(s), P(mol.atm), mol.natm, P(mol.bas), nb,
+                                   P(mol.env), None, None)
+            want = getattr(oracle.ref.lib, name)(None, None, P(s), P(mol.atm), mol.natm,
+                                                 P(mol.bas), nb, P(mol.env), None, None)
+            assert got == want, (name, s[:nsh].tolist(), got, want)
