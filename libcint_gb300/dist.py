@@ -48,3 +48,40 @@ def balanced_order(costs, world):
         owner[i] = r
         load[r] += costs[i]
     return owner
+
+
+def quartet_costs(mol, quartets):
+    """Relative cost of each shell quartet: primitive quartets x Cartesian components x
+    contraction-column combinations (each combination is its own task)."""
+    from .molecules import ANG_OF, NCTR_OF, NPRIM_OF
+    q = np.asarray(quartets, dtype=np.int64).reshape(-1, 4)
+    l = mol.bas[:, ANG_OF].astype(np.int64)
+    per = mol.bas[:, NPRIM_OF].astype(np.float64) * ((l + 1) * (l + 2) // 2) \
+        * mol.bas[:, NCTR_OF].astype(np.float64)
+    return np.prod(per[q], axis=1)
+
+
+def shard_quartets(mol, quartets, rank, world):
+    """This rank's quartets of a list, balanced by estimated cost (longest processing time)."""
+    quartets = np.asarray(quartets)
+    if world == 1:
+        return quartets
+    return quartets[balanced_order(quartet_costs(mol, quartets), world) == rank]
+
+
+def get_jk_sharded(mol, dm, with_j=True, with_k=True, quartets=None):
+    """J and K over all ranks: each rank contracts its cost-balanced share of the unique quartet
+    list on its own GPU, then one sum over ranks (the path's only exchange)."""
+    import torch.distributed as dist
+    from .coulomb import CoulombPlans
+    from .molecules import unique_quartets
+    rank = dist.get_rank() if dist.is_initialized() else 0
+    world = dist.get_world_size() if dist.is_initialized() else 1
+    qs = unique_quartets(mol.nbas) if quartets is None else np.asarray(quartets)
+    plans = CoulombPlans(mol, shard_quartets(mol, qs, rank, world))
+    J, K = plans.get_jk(dm, with_j, with_k)
+    for t in (J, K):
+        if t is not None:
+            sum_over_ranks(t)
+    return J, K
+
