@@ -106,3 +106,30 @@ def test_invalid_input_is_rejected_with_a_message():
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     assert f(7, P(out), P(items), 1, None, P(mol.atm), mol.natm, P(mol.bas), mol.nbas, P(mol.env)) == -1
     assert 'density' in cg.last_error()
+
+
+def test_2c2e_and_contraction_kinds_on_the_host():
+    """int2c2e plans every pair (libcint's 2c2e loop screens no primitive) on the contraction-first
+    groups (no transfer: lj = ll = 0); the J, K and J/K kinds plan the same unique list and never
+    transform outputs (they store none); bad int2c2e items and contraction kinds given to the
+    host-buffer entry are rejected."""
+    mol2, _ = M.config2(seed=1, natm=4, box=4.0)
+    pairs = [(i, k) for i in range(0, mol2.nbas, 3) for k in range(0, mol2.nbas, 5)]
+    for kind in (cg.INT2C2E_SPH, cg.INT2C2E_CART):
+        g = groups(kind, mol2, pairs)
+        assert g[2] == 0 and g[0] + g[1] >= len(pairs)
+    assert _build(cg.INT2C2E_SPH, mol2, [(-1, 2)]) == -1 and 'negative shell' in cg.last_error()
+    mol = M.config3(seed=2, natm=3, box=3.5)
+    qs = M.unique_quartets(mol.nbas)
+    tasks = [groups(kind, mol, qs)[:3].sum() for kind in (7, 10, 11)]
+    assert tasks[0] == tasks[1] == tasks[2] > 0
+    for kind in (7, 10, 11):
+        assert groups(kind, mol, qs)[3] == 0
+    f = cg.lib().cintgpu_batch_host
+    out = np.zeros(16)
+    items = np.array(qs[:1], dtype=np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    for kind in (10, 11):
+        assert f(kind, P(out), P(items), 1, None, P(mol.atm), mol.natm, P(mol.bas), mol.nbas,
+                 P(mol.env)) == -1
+        assert 'density' in cg.last_error()
