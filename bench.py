@@ -305,6 +305,30 @@ def extra_jk(cg, seed=0, natm=24):
             'coulomb_energy': float(0.5 * (dm * J).sum()), 'exchange_energy': float(-0.25 * (dm * K).sum())}
 
 
+def extra_df(cg, seed=0, natm=20):
+    """Density-fitted J on a c2-type system (orbital s,s,p,p,d with 1-6 primitives, auxiliary
+    l <= 4 x 2 per atom, same density of atoms as c2): set-up (both plans, metric Cholesky) and
+    one J build."""
+    import torch
+    from libcint_gb300 import molecules as M
+    from libcint_gb300.df import DFCoulomb
+    box = 18.0 * (natm / 200.0) ** (1.0 / 3.0)
+    mol, norb = M.config2(seed=seed, natm=natm, box=box)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fit = DFCoulomb(mol, norb)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    rng = np.random.RandomState(seed)
+    d = rng.normal(0, 0.1, (fit.nao, fit.nao))
+    dm = torch.as_tensor(0.5 * (d + d.T), device='cuda')
+    t_j = _timed(lambda: fit.vj(dm))
+    return {'workload': 'c2-type: %d atoms, %.1f A, all %d orbital shell pairs x %d aux shells'
+                        % (natm, box, norb * (norb + 1) // 2, mol.nbas - norb),
+            'nao': fit.nao, 'naux': fit.naux, 'three_index_elements': int(fit.T.numel()),
+            'setup_s': t_setup, 'vj_ms': 1e3 * t_j}
+
+
 def run_extras(cg, mol, qs, value, args):
     out = {}
     for name, fn in (('dropin', lambda: extra_dropin(cg, mol, qs, value)),
@@ -329,6 +353,7 @@ def run_gpu(args, rank, world):
         # one side workload alone (profiling); not the benchmark line
         fn = {'adjoint': lambda: extra_adjoint(cg, natm=args.c3_atoms),
               'jk': lambda: extra_jk(cg, natm=args.c3_atoms),
+              'df': lambda: extra_df(cg),
               'int3c2e': lambda: extra_int3c2e(cg)}[args.only]
         if rank == 0:
             print(json.dumps({'extra': args.only, **fn()}), flush=True)
@@ -456,7 +481,7 @@ def main():
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-extras', action='store_true', help='skip the drop-in, int3c2e, adjoint and J/K lines')
-    ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk'],
+    ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk', 'df'],
                     help='run one side workload alone and print its line (profiling)')
     ap.add_argument('--c3-atoms', type=int, default=24, help='atoms of the adjoint workload')
     args = ap.parse_args()
