@@ -51,7 +51,7 @@ def test_two_gloo_ranks_reduce_like_one_process():
     import torch.multiprocessing as mp
     pytest.importorskip('torch.distributed')
     port = 29500 + os.getpid() % 2000
-    mgr = mp.Manager()
+    mgr = mp.get_context('spawn').Manager()
     result = mgr.dict()
     mp.spawn(_worker, args=(2, port, result), nprocs=2, join=True)
     rng = np.random.RandomState(0)
@@ -98,7 +98,7 @@ def test_two_gloo_ranks_shard_jk(oracle):
     loads = [quartet_costs(mol, p).sum() for p in parts]
     assert abs(loads[0] - loads[1]) <= quartet_costs(mol, qs).max()
     port = 31500 + os.getpid() % 2000
-    mgr = mp.Manager()
+    mgr = mp.get_context('spawn').Manager()
     result = mgr.dict()
     mp.spawn(_jk_worker, args=(2, port, result), nprocs=2, join=True)
     eri, _ = _eri_full(oracle, mol)
