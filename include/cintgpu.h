@@ -165,6 +165,13 @@ typedef struct CINTGPUPlan CINTGPUPlan;
 int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
                         const int64_t *offsets, const int *atm, int natm, const int *bas,
                         int nbas, const double *env);
+/* The same with the launch parameters an autotuner picks (no libcint counterpart): ws_kb = shared
+ * memory per warp of the regular task group in KB, 8..48 (it fixes the terms per batch of every
+ * class and the CTAs per SM; 0 = the default 24 or CINTGPU_WS_KB), separate_output = 1 to
+ * transform outputs in their own kernel instead of at the integral kernel's tail (0 = default). */
+int cintgpu_plan_create_tuned(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
+                              const int64_t *offsets, const int *atm, int natm, const int *bas,
+                              int nbas, const double *env, int ws_kb, int separate_output);
 /* doubles per component of the output (max offset + block), and the component count */
 int64_t cintgpu_plan_output_size(const CINTGPUPlan *plan);
 int cintgpu_plan_ncomp(const CINTGPUPlan *plan);

@@ -54,6 +54,8 @@ def lib():
     L.CINTgto_norm.restype = dbl
     L.cintgpu_plan_create.argtypes = [vp, i32, vp, i64, vp, vp, i32, vp, i32, vp]
     L.cintgpu_plan_create.restype = i32
+    L.cintgpu_plan_create_tuned.argtypes = [vp, i32, vp, i64, vp, vp, i32, vp, i32, vp, i32, i32]
+    L.cintgpu_plan_create_tuned.restype = i32
     L.cintgpu_plan_output_size.argtypes = [vp]
     L.cintgpu_plan_output_size.restype = i64
     L.cintgpu_plan_ncomp.argtypes = [vp]
@@ -118,9 +120,11 @@ class Plan:
 
     execute(out) enqueues the kernels writing into a CUDA float64 buffer (a torch tensor or a raw
     device pointer) of ncomp * output_size elements; block q of component c starts at
-    c * output_size + offsets[q] and is laid out like libcint's dense output (i fastest)."""
+    c * output_size + offsets[q] and is laid out like libcint's dense output (i fastest).
+    ws_kb / separate_output: the launch parameters of cintgpu_plan_create_tuned (0 = defaults);
+    autotune.tuned_plan picks them."""
 
-    def __init__(self, kind, mol, shls, offsets=None):
+    def __init__(self, kind, mol, shls, offsets=None, ws_kb=0, separate_output=0):
         L = lib()
         self.kind = kind
         self.mol = mol
@@ -128,9 +132,14 @@ class Plan:
         self.n = shls.shape[0]
         off = None if offsets is None else np.ascontiguousarray(offsets, dtype=np.int64)
         h = ctypes.c_void_p()
-        rc = L.cintgpu_plan_create(ctypes.byref(h), kind, _ptr(shls), self.n, _ptr(off),
-                                   _ptr(mol.atm), mol.natm, _ptr(mol.bas), mol.nbas, _ptr(mol.env))
+        args = (ctypes.byref(h), kind, _ptr(shls), self.n, _ptr(off), _ptr(mol.atm), mol.natm,
+                _ptr(mol.bas), mol.nbas, _ptr(mol.env))
+        if ws_kb or separate_output:
+            rc = L.cintgpu_plan_create_tuned(*args, int(ws_kb), int(separate_output))
+        else:
+            rc = L.cintgpu_plan_create(*args)
         _check(rc, 'cintgpu_plan_create')
+        self.ws_kb, self.separate_output = int(ws_kb), int(separate_output)
         self._h = h
         self.output_size = L.cintgpu_plan_output_size(h)
         self.ncomp = L.cintgpu_plan_ncomp(h)

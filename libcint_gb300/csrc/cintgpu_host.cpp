@@ -293,6 +293,8 @@ struct CINTGPUPlan {
     std::vector<int> eround;       /* stage-3 rounds: start | count << 16 | box << 24 */
     std::vector<int> empty_outs;   /* output quartets without any task (zero-filled) */
     bool fuse_out = true;          /* the integral kernel stores finished quartets itself */
+    int ws_kb = 0;                 /* shared memory per warp of the regular group in KB (0: the
+                                      CINTGPU_WS_KB override or the default 24) */
     int prim_l = 4;                /* int2e classes with lj or ll >= prim_l transfer per primitive
                                       (CINTGPU_PER_PRIMITIVE_L overrides, 0 = every class) */
     int hrr_max = 1;               /* doubles of one transfer buffer, largest class */
@@ -976,10 +978,13 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     const double warps = (double)std::max(1, g_ctx.sm_count) * 8.0;
     double target = std::max(fl / (warps * 32.0), 2.0e5);
     if (split_target > 0) target = std::min(target, fl / (double)split_target);
-    /* shared memory per warp of the regular group: 24 KB unless CINTGPU_WS_KB overrides (tuning) */
+    /* shared memory per warp of the regular group: 24 KB unless the plan's tuned value or
+     * CINTGPU_WS_KB overrides it */
     int ws_small = CG_WS_SMALL;
-    if (const char *e = getenv("CINTGPU_WS_KB")) {
-        int kb = atoi(e);
+    {
+        int kb = P->ws_kb;
+        if (!kb)
+            if (const char *e = getenv("CINTGPU_WS_KB")) kb = atoi(e);
         if (kb >= 8 && kb <= 48) ws_small = kb * 1024 / 8;
     }
     std::vector<int> cls_group(8 * 8 * 8 * 8, -1);
@@ -1575,16 +1580,18 @@ int cintgpu_rys_roots_dev(int nroots, const double *xs_dev, int count, double *s
     return 0;
 }
 
-int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
-                        const int64_t *offsets, const int *atm, int natm, const int *bas,
-                        int nbas, const double *env)
+static int plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
+                       const int64_t *offsets, const int *atm, int natm, const int *bas,
+                       int nbas, const double *env, int ws_kb, int separate_output)
 {
     *plan = nullptr;
     int rc = ensure_init();
     if (rc) return rc;
     CINTGPUPlan *P = new CINTGPUPlan();
+    P->ws_kb = ws_kb;
     /* CINTGPU_SEPARATE_OUTPUT=1: transform outputs in their own kernel (tuning) */
     if (const char *e = getenv("CINTGPU_SEPARATE_OUTPUT")) P->fuse_out = atoi(e) == 0;
+    if (separate_output) P->fuse_out = false;
     int64_t target = n < (int64_t)g_ctx.sm_count * 16 ? (int64_t)g_ctx.sm_count * 8 : 0;
     rc = build_plan(P, kind, shls, n, offsets, atm, natm, bas, nbas, env, target);
     if (!rc) rc = upload_plan(P, nullptr, 0, 0, false, nullptr);
@@ -1598,6 +1605,30 @@ int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n
     if (rc) { free_plan_device(P); delete P; return rc; }
     *plan = P;
     return 0;
+}
+
+int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
+                        const int64_t *offsets, const int *atm, int natm, const int *bas,
+                        int nbas, const double *env)
+{
+    return plan_create(plan, kind, shls, n, offsets, atm, natm, bas, nbas, env, 0, 0);
+}
+
+int cintgpu_plan_create_tuned(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
+                              const int64_t *offsets, const int *atm, int natm, const int *bas,
+                              int nbas, const double *env, int ws_kb, int separate_output)
+{
+    if (plan) *plan = nullptr;
+    if (ws_kb != 0 && (ws_kb < 8 || ws_kb > 48)) {
+        set_error("ws_kb %d outside 8..48 (0 = default)", ws_kb);
+        return CINTGPU_ERR_ARG;
+    }
+    if (separate_output != 0 && separate_output != 1) {
+        set_error("separate_output must be 0 or 1");
+        return CINTGPU_ERR_ARG;
+    }
+    return plan_create(plan, kind, shls, n, offsets, atm, natm, bas, nbas, env, ws_kb,
+                       separate_output);
 }
 
 int64_t cintgpu_plan_output_size(const CINTGPUPlan *plan) { return plan->out_size; }
@@ -2177,6 +2208,22 @@ extern "C" int cg_plan_groups(int kind, const int *shls, int64_t n, const int *a
     if (rc) return rc;
     for (int g = 0; g < 3; g++) info[g] = P.groups[g].ntasks;
     info[3] = fused(&P) ? 1 : 0;
+    return 0;
+}
+
+/* the same with the regular group's shared memory per warp set (KB); info[4] = that group's
+ * doubles per warp */
+extern "C" int cg_plan_groups_ws(int kind, const int *shls, int64_t n, const int *atm, int natm,
+                                 const int *bas, int nbas, const double *env, int ws_kb,
+                                 int64_t *info)
+{
+    CINTGPUPlan P;
+    P.ws_kb = ws_kb;
+    int rc = build_plan(&P, kind, shls, n, nullptr, atm, natm, bas, nbas, env, 0);
+    if (rc) return rc;
+    for (int g = 0; g < 3; g++) info[g] = P.groups[g].ntasks;
+    info[3] = fused(&P) ? 1 : 0;
+    info[4] = P.groups[0].ws;
     return 0;
 }
 

@@ -1,0 +1,133 @@
+"""The launch-parameter autotuner's host logic on the CPU: workload keys, the cache file (missing,
+damaged, foreign, merged, written atomically), candidate selection with an injected timer, cache
+hits without tuning; and the C side: cintgpu_plan_create_tuned's argument checks and the shared
+memory per warp reaching the planner."""
+import ctypes
+import json
+import os
+
+import numpy as np
+
+from tests import _oracle  # noqa: F401  (puts the repo root on sys.path)
+import libcint_gb300 as cg
+from libcint_gb300 import autotune as at
+from libcint_gb300 import molecules as M
+
+
+def _c0():
+    mol = M.config0(seed=1)
+    return mol, M.unique_quartets(mol.nbas)[:500]
+
+
+def test_workload_key_is_stable_and_discriminating():
+    mol, qs = _c0()
+    k = at.workload_key(cg.INT2E_SPH, mol, qs)
+    perm = qs[np.random.RandomState(0).permutation(len(qs))]
+    assert at.workload_key(cg.INT2E_SPH, mol, perm) == k                  # order-free
+    swapped = qs[:, [1, 0, 3, 2]]                                          # same classes
+    assert at.workload_key(cg.INT2E_SPH, mol, swapped) == k
+    assert at.workload_key(cg.INT2E_CART, mol, qs) != k                   # kind
+    assert at.workload_key(cg.INT2E_SPH, mol, qs[:20]) != k               # length magnitude
+    L = mol.bas[:, M.ANG_OF]
+    dd = qs[(L[qs] == 2).all(1)]
+    assert len(dd) > 0 and at.workload_key(cg.INT2E_SPH, mol, np.tile(dd, (40, 1))[:500]) != k
+    prof = at.class_profile(mol, qs)
+    assert abs(sum(prof.values()) - 1.0) < 0.05
+    assert all(len(c.split(',')) == 4 for c in prof if c != 'rest')
+
+
+def test_cache_file_robustness(tmp_path):
+    p = str(tmp_path / 'sub' / 'tuning.json')
+    assert at.load_cache(p) == {}                                          # missing
+    at.store('a', (16, 0), {(16, 0): 1.5, (24, 0): 2.0}, p)
+    at.store('b', (24, 1), None, p)                                        # merged
+    e = at.load_cache(p)
+    assert e['a']['ws_kb'] == 16 and e['a']['ms']['16,0'] == 1.5 and e['b']['separate_output'] == 1
+    assert [f for f in os.listdir(os.path.dirname(p)) if f.endswith('.tmp')] == []
+    with open(p, 'w') as f:
+        f.write('{not json')
+    assert at.load_cache(p) == {}                                          # damaged
+    with open(p, 'w') as f:
+        json.dump({'format': 99, 'entries': {'a': {'ws_kb': 16, 'separate_output': 0}}}, f)
+    assert at.load_cache(p) == {}                                          # foreign format
+    with open(p, 'w') as f:
+        json.dump({'format': at.FORMAT, 'entries': {'a': {'ws_kb': 99, 'separate_output': 0},
+                                                    'b': {'ws_kb': 20, 'separate_output': 0}}}, f)
+    assert list(at.load_cache(p)) == ['b']                                 # invalid entry dropped
+    at.store('c', (32, 0), None, p)                                        # rewrite over it
+    assert sorted(at.load_cache(p)) == ['b', 'c']
+
+
+class _FakePlan:
+    closed = 0
+
+    def __init__(self, ws, sep):
+        self.ws, self.sep = ws, sep
+
+    def close(self):
+        _FakePlan.closed += 1
+
+
+def test_tune_picks_the_fastest_and_closes_every_plan():
+    mol, qs = _c0()
+    ms = {(24, 0): 3.0, (16, 0): 2.5, (20, 0): 2.2, (32, 0): 4.0, (24, 1): 3.1}
+    _FakePlan.closed = 0
+    best, times = at.tune(cg.INT2E_SPH, mol, qs, make_plan=_FakePlan,
+                          timer=lambda p: ms[(p.ws, p.sep)])
+    assert best == (20, 0) and times == ms and _FakePlan.closed == len(at.CANDIDATES)
+
+
+def test_choose_uses_the_cache_before_tuning(tmp_path):
+    mol, qs = _c0()
+    p = str(tmp_path / 'tuning.json')
+    calls = []
+
+    def tuner(kind, mol_, items):
+        calls.append(kind)
+        return (16, 1), {(16, 1): 1.0}
+    dev = 'GB300 test|cuda 13.0'
+    assert at.choose(cg.INT2E_SPH, mol, qs, p, device=dev, tuner=tuner) == (16, 1)
+    assert at.choose(cg.INT2E_SPH, mol, qs, p, device=dev, tuner=tuner) == (16, 1)
+    assert len(calls) == 1                                                  # second call: hit
+    at.choose(cg.INT2E_SPH, mol, qs, p, device='other GPU|cuda 13.0', tuner=tuner)
+    assert len(calls) == 2                                                  # keyed by device
+    at.choose(cg.INT2E_SPH, mol, qs, p, retune=True, device=dev, tuner=tuner)
+    assert len(calls) == 3
+
+
+def test_tuned_create_checks_its_arguments():
+    L = cg.lib()
+    mol, qs = _c0()
+    items = np.ascontiguousarray(qs[:4], dtype=np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    h = ctypes.c_void_p()
+    for ws, sep in ((4, 0), (64, 0), (24, 2)):
+        rc = L.cintgpu_plan_create_tuned(ctypes.byref(h), cg.INT2E_SPH, P(items), 4, None,
+                                         P(mol.atm), mol.natm, P(mol.bas), mol.nbas, P(mol.env),
+                                         ws, sep)
+        assert rc == -1 and not h.value
+        assert 'ws_kb' in cg.last_error() or 'separate_output' in cg.last_error()
+
+
+def test_shared_memory_per_warp_reaches_the_planner():
+    """ws_kb sets the regular group's doubles per warp (0 = the default 24 KB); with 8 KB the
+    (ii|ii)-type classes of an l = 6 basis no longer fit it and move to the 48 KB group."""
+    from tests.test_gpu_high_l import high_l_basis
+    f = cg.lib().cg_plan_groups_ws
+    f.restype = ctypes.c_int
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+
+    def plan_info(mol, qs, ws):
+        items = np.ascontiguousarray(qs, dtype=np.int32)
+        info = np.zeros(5, np.int64)
+        assert f(cg.INT2E_SPH, P(items), ctypes.c_int64(len(items)), P(mol.atm), mol.natm,
+                 P(mol.bas), mol.nbas, P(mol.env), ws, P(info)) == 0, cg.last_error()
+        return info
+    mol = M.config1(seed=0)
+    qs = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'c1_quartets.npz'))['quartets'][:400]
+    res = {ws: plan_info(mol, qs, ws) for ws in (0, 8, 16, 24, 32)}
+    assert (res[0] == res[24]).all() and res[0][4] == 24 * 1024 // 8
+    assert all(res[ws][4] == ws * 1024 // 8 for ws in (8, 16, 32))
+    hl = high_l_basis()
+    big = [(0, 0, 0, 0), (1, 1, 1, 1), (2, 2, 2, 2)]
+    assert plan_info(hl, big, 24)[1] == 0 and plan_info(hl, big, 8)[1] > 0

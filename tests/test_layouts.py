@@ -34,10 +34,15 @@ def classes(lmax):
             for c in range(lmax + 1) for d in range(c + 1)]
 
 
+# every shared-memory size per warp the regular group can be launched with (CINTGPU_WS_KB and the
+# autotuner's candidates, 8..48 KB)
+WS_ALL = [kb * 1024 // 8 for kb in (8, 12, 16, 20, 24, 28, 32, 40, 48)]
+
+
 @pytest.mark.parametrize('mode', [ERI, ERIP, IP1])
 def test_integral_layouts_fit(mode):
     for l in classes(6):
-        for ws in (WS_SMALL, WS_MAX):
+        for ws in WS_ALL:
             L = layout(l, mode, ws)
             if L.T < 1:
                 continue          # the planner rejects such a class or moves it to another group
