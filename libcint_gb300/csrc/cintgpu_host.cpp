@@ -23,6 +23,7 @@
  */
 #include <cuda_runtime.h>
 #include <math.h>
+#include <cmath>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -164,6 +165,19 @@ struct ShellView {
     double R[3];
     const double *ex, *cf;
 };
+
+/* NaN or Inf in a shell's coordinates, exponents or coefficients: rejected with a message (libcint
+ * would carry them into its root finder, which exits on failure, src/rys_roots.c:115-121) */
+int check_finite(int sh, const ShellView &s)
+{
+    for (int c = 0; c < 3; c++)
+        if (!std::isfinite(s.R[c])) { set_error("shell %d: non-finite coordinate", sh); return CINTGPU_ERR_ARG; }
+    for (int i = 0; i < s.nprim; i++)
+        if (!std::isfinite(s.ex[i])) { set_error("shell %d: non-finite exponent", sh); return CINTGPU_ERR_ARG; }
+    for (int i = 0; i < s.nprim * s.nctr; i++)
+        if (!std::isfinite(s.cf[i])) { set_error("shell %d: non-finite coefficient", sh); return CINTGPU_ERR_ARG; }
+    return 0;
+}
 
 int read_shell(int sh, const int *atm, int natm, const int *bas, const double *env, ShellView *s)
 {
@@ -840,6 +854,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
 
     struct Pending { int pij, pkl, out; int64_t npq; int l[4]; int sym; };
     std::vector<Pending> pend;
+    std::vector<char> finite_checked;   /* per shell index: data checked once per plan */
     int64_t next_off = 0;
     for (int64_t q = 0; q < n; q++) {
         const int *s = shls + nsh * q;
@@ -848,6 +863,11 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             int rc = read_shell(s[a], atm, natm, bas, env, &sv[a]);
             if (rc) return rc;
             if (s[a] > PAIR_KEY_MAX_SHELL) { set_error("shell index %d above %d", s[a], PAIR_KEY_MAX_SHELL); return CINTGPU_ERR_ARG; }
+            if ((size_t)s[a] >= finite_checked.size()) finite_checked.resize((size_t)s[a] + 1, 0);
+            if (!finite_checked[s[a]]) {
+                if ((rc = check_finite(s[a], sv[a]))) return rc;
+                finite_checked[s[a]] = 1;
+            }
             if (contracting && s[a] >= nbas) { set_error("shell %d outside nbas %d", s[a], nbas); return CINTGPU_ERR_ARG; }
             if (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) {
                 if (sv[a].l > 4) { set_error("adjoint supports l <= 4 (shell %d has %d)", s[a], sv[a].l); return CINTGPU_ERR_UNSUPPORTED; }

@@ -92,6 +92,12 @@ def test_invalid_input_is_rejected_with_a_message():
         ('nprim = 65', _variant(mol, 'bas', (3, M.NPRIM_OF), 65), q, -1, 'nprim'),
         ('atom out of range', _variant(mol, 'bas', (3, M.ATOM_OF), 99), q, -1, 'atom'),
         ('omega != 0', _variant(mol, 'env', 8, 0.3), q, -3, 'range-separated'),
+        ('NaN coordinate', _variant(mol, 'env', int(mol.atm[mol.bas[2, M.ATOM_OF], M.PTR_COORD]) + 1,
+                                    float('nan')), q, -1, 'non-finite coordinate'),
+        ('Inf exponent', _variant(mol, 'env', int(mol.bas[1, M.PTR_EXP]), float('inf')), q, -1,
+         'non-finite exponent'),
+        ('NaN coefficient', _variant(mol, 'env', int(mol.bas[0, M.PTR_COEFF]) + 1, float('nan')), q,
+         -1, 'non-finite coefficient'),
     ]
     for what, m, items, code, text in cases:
         assert _build(cg.INT2E_SPH, m, items) == code, what
