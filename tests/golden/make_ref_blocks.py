@@ -12,6 +12,9 @@ Contents (all through libcint 6.1.1 built by oracle/Makefile, opt = NULL, cache 
   c2_int3c2e_sph                     60 (ij|P) triples of molecules.config2(1, natm=6, box=5)
   c2_int2c2e_sph / c2_int2c2e_cart   60 (i|k) pairs of the same molecule (orbital and auxiliary)
   kat_int2c2e_sph                    all 8 x 8 shell pairs of the self-contained basis
+  hl_int2e_sph / hl_int2e_cart / hl_int3c2e_sph / hl_int2e_ip1_sph
+                                     small blocks of the l = 6 / 5 / 4 / 2 / 0 basis of
+                                     tests/test_gpu_high_l.py (i, h with two columns, g, d, s)
   cache_sizes                        the out == NULL cache-size answers for a few items
 Each block is stored flattened in libcint's (Fortran) order with its item list.
 """
@@ -27,6 +30,15 @@ sys.path.insert(0, ROOT)
 
 from libcint_gb300 import molecules as M  # noqa: E402
 from tests import _oracle  # noqa: E402
+from tests.test_gpu_high_l import high_l_basis  # noqa: E402
+
+HL_ITEMS = {
+    'int2e_sph': [(0, 4, 0, 3), (0, 0, 4, 4), (2, 1, 3, 4), (1, 4, 3, 4), (0, 3, 3, 4), (1, 2, 3, 4),
+                  (0, 2, 4, 3), (1, 3, 1, 4), (0, 1, 3, 4)],
+    'int2e_cart': [(0, 4, 0, 3), (0, 0, 4, 4), (2, 1, 3, 4), (1, 4, 3, 4), (0, 3, 3, 4), (1, 2, 3, 4)],
+    'int3c2e_sph': [(3, 4, 0), (0, 3, 2), (1, 4, 2), (0, 0, 4)],
+    'int2e_ip1_sph': [(1, 2, 3, 4), (0, 3, 4, 4), (2, 0, 3, 4)],
+}
 
 
 def main():
@@ -68,6 +80,11 @@ def main():
     for name in ('int2c2e_sph', 'int2c2e_cart'):
         out['c2_' + name + '_items'] = pr
         out['c2_' + name] = np.concatenate([o.ref.call(name, mol2, t)[1].ravel(order='F') for t in pr])
+    hl = high_l_basis()
+    for name, items in HL_ITEMS.items():
+        it = np.array(items, dtype=np.int32)
+        out['hl_' + name + '_items'] = it
+        out['hl_' + name] = np.concatenate([o.ref.call(name, hl, t)[1].ravel(order='F') for t in it])
     kp = np.array([(i, k) for k in range(8) for i in range(8)], dtype=np.int32)
     out['kat_int2c2e_sph_items'] = kp
     out['kat_int2c2e_sph'] = np.concatenate([o.ref.call('int2c2e_sph', mol, t, nbas=nbas)[1]

@@ -107,7 +107,9 @@ def _compare(got, ref, scale, atol=1e-12):
                                          ('c0_int2e_sph', 'c0'), ('c0_int2e_cart', 'c0'),
                                          ('c0_int2e_ip1_sph', 'c0'), ('c2_int3c2e_sph', 'c2'),
                                          ('c2_int2c2e_sph', 'c2'), ('c2_int2c2e_cart', 'c2'),
-                                         ('kat_int2c2e_sph', 'kat')])
+                                         ('kat_int2c2e_sph', 'kat'), ('hl_int2e_sph', 'hl'),
+                                         ('hl_int2e_cart', 'hl'), ('hl_int3c2e_sph', 'hl'),
+                                         ('hl_int2e_ip1_sph', 'hl')])
 def test_oracle_matches_libcint_blocks(oracle, key, molname):
     fx = np.load(os.path.join(GOLD, 'ref_blocks.npz'))
     items, ref = fx[key + '_items'], fx[key]
@@ -117,6 +119,9 @@ def test_oracle_matches_libcint_blocks(oracle, key, molname):
         mol, nbas = M.kat_basis()
     elif molname == 'c0':
         mol = M.config0(seed=3)
+    elif molname == 'hl':
+        from tests.test_gpu_high_l import high_l_basis
+        mol = high_l_basis()
     else:
         mol, _ = M.config2(seed=1, natm=6, box=5.0)
     off = 0
@@ -132,6 +137,24 @@ def test_oracle_matches_libcint_blocks(oracle, key, molname):
         _compare(b, ref[off:off + b.size], scale, atol)
         off += b.size
     assert off == ref.size
+
+
+def test_oracle_matches_libcint_live_high_l(oracle):
+    """every quartet and triple of the GPU's l = 5 / 6 tests (i, h with two columns, g, d, s), the
+    oracle against libcint compiled from its sources: the checks at the top of the drop-in's range
+    rest on a pinned oracle"""
+    if oracle.ref is None:
+        pytest.skip('libcint not built from sources on this machine')
+    from tests.test_gpu_high_l import QUARTETS, TRIPLES, high_l_basis
+    mol = high_l_basis()
+    for name, items in (('int2e_sph', QUARTETS), ('int2e_cart', QUARTETS), ('int3c2e_sph', TRIPLES),
+                        ('int2e_ip1_sph', [(1, 2, 3, 4), (2, 1, 1, 3), (0, 3, 4, 4)])):
+        for it in items:
+            fa, a = oracle.port.call(name, mol, it)
+            fb, b = oracle.ref.call(name, mol, it)
+            assert fa == fb
+            c = oracle.ref.call(name.replace('_sph', '_cart'), mol, it)[1]
+            _compare(a.ravel(), b.ravel(), np.abs(c).max(initial=0))
 
 
 def test_oracle_matches_libcint_live_c1(oracle):
