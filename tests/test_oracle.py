@@ -157,6 +157,35 @@ def test_oracle_matches_libcint_live_high_l(oracle):
             _compare(a.ravel(), b.ravel(), np.abs(c).max(initial=0))
 
 
+def test_oracle_matches_libcint_with_optimizer(oracle):
+    """libcint's optimised loop (CINT2e_loop with int2e_optimizer's tables, src/cint2e.c:388-758,
+    src/optimizer.c) against the oracle, which restates the screening of the NULL-optimizer loop:
+    same blocks and return flags, so the drop-in may ignore opt (as it does)"""
+    if oracle.ref is None:
+        pytest.skip('libcint not built from sources on this machine')
+    import ctypes
+    L = oracle.ref.lib
+    vp = ctypes.c_void_p
+    L.int2e_optimizer.argtypes = [vp, vp, ctypes.c_int, vp, ctypes.c_int, vp]
+    L.CINTdel_optimizer.argtypes = [vp]
+    mol = M.config1(seed=0)
+    qs = np.load(os.path.join(GOLD, 'c1_quartets.npz'))['quartets'][:200]
+    P = lambda a: a.ctypes.data_as(vp)
+    opt = vp()
+    L.int2e_optimizer(ctypes.byref(opt), P(mol.atm), mol.natm, P(mol.bas), mol.nbas, P(mol.env))
+    try:
+        for q in qs:
+            s = np.ascontiguousarray(q, dtype=np.int32)
+            b = np.zeros(int(np.prod([mol.nsph(x) for x in q])))
+            fb = L.int2e_sph(P(b), None, P(s), P(mol.atm), mol.natm, P(mol.bas), mol.nbas,
+                             P(mol.env), opt, None)
+            fa, a = oracle.port.call('int2e_sph', mol, q)
+            assert fa == fb
+            assert np.abs(a.ravel(order='F') - b).max() <= 1e-12
+    finally:
+        L.CINTdel_optimizer(ctypes.byref(opt))
+
+
 def test_oracle_matches_libcint_live_c1(oracle):
     if oracle.ref is None:
         pytest.skip('libcint not built from sources on this machine')
