@@ -427,17 +427,22 @@ static void gout(const OEnv *E, const GArr *G, double ai, double *out, int ncomp
     int nf[4];
     for (int s = 0; s < 4; s++) { cart_comp(E->l[s], nx[s], ny[s], nz[s]); nf[s] = ncart(E->l[s]); }
     const int n = E->nroots;
+    /* offsets of root 0 per axis; consecutive roots are rs apart (GIDX layout) */
+    const size_t rs = (size_t)G->di * G->dj * G->dk * G->dl;
     size_t idx = 0;
     for (int j = 0; j < nf[1]; j++)
     for (int l = 0; l < nf[3]; l++)
     for (int k = 0; k < nf[2]; k++)
     for (int i = 0; i < nf[0]; i++, idx++) {
         int ix = nx[0][i], iy = ny[0][i], iz = nz[0][i];
+        const double *px = G->g + GIDX(G, 0, 0, ix, nx[1][j], nx[2][k], nx[3][l]);
+        const double *py = G->g + GIDX(G, 1, 0, iy, ny[1][j], ny[2][k], ny[3][l]);
+        const double *pz = G->g + GIDX(G, 2, 0, iz, nz[1][j], nz[2][k], nz[3][l]);
         double s0 = 0, sx = 0, sy = 0, sz = 0;
         for (int r = 0; r < n; r++) {
-            double gx = G->g[GIDX(G, 0, r, ix, nx[1][j], nx[2][k], nx[3][l])];
-            double gy = G->g[GIDX(G, 1, r, iy, ny[1][j], ny[2][k], ny[3][l])];
-            double gz = G->g[GIDX(G, 2, r, iz, nz[1][j], nz[2][k], nz[3][l])];
+            double gx = px[r * rs];
+            double gy = py[r * rs];
+            double gz = pz[r * rs];
             if (ncomp == 1) {
                 s0 += gx * gy * gz;
             } else {
