@@ -37,17 +37,14 @@
 #define MAXROOTS 24
 #define MAXL     8          /* per-shell ceiling supported by the oracle (l <= 7, +1 for ip1) */
 #define MAXCART  36         /* (MAXL)(MAXL+1)/2 for l=7 */
-/* Gauss-Legendre node sets on [0,1] for the discretised Stieltjes procedure: 64 nodes for up to
- * 10 roots, 128 beyond (both agree with a 200-node set to <= 1e-14 of F0 in the weights and 1e-15
- * in the nodes for n <= 24, x < 400; 64 nodes alone drift from n = 14) */
-#define NGL_SMALL 64
-#define NGL      128
-static double gl_t[NGL], gl_w[NGL];
-static double gls_t[NGL_SMALL], gls_w[NGL_SMALL];
+#define NGL      200
+
+static double gl_t[NGL], gl_w[NGL];   /* Gauss-Legendre on [0,1] */
 
 /* Legendre nodes by Newton iteration on P_n (standard three-term recurrence). */
-static void gauss_legendre(int n, double *gt, double *gw)
+__attribute__((constructor)) static void init_gauss_legendre(void)
 {
+    const int n = NGL;
     for (int i = 0; i < (n + 1) / 2; i++) {
         double z = cos(M_PI * (i + 0.75) / (n + 0.5));
         double pp = 0;
@@ -64,15 +61,9 @@ static void gauss_legendre(int n, double *gt, double *gw)
         }
         double w = 2.0 / ((1 - z * z) * pp * pp);
         /* map [-1,1] -> [0,1] */
-        gt[i] = 0.5 * (1 - z);         gw[i] = 0.5 * w;
-        gt[n - 1 - i] = 0.5 * (1 + z); gw[n - 1 - i] = 0.5 * w;
+        gl_t[i] = 0.5 * (1 - z);         gl_w[i] = 0.5 * w;
+        gl_t[n - 1 - i] = 0.5 * (1 + z); gl_w[n - 1 - i] = 0.5 * w;
     }
-}
-
-__attribute__((constructor)) static void init_gauss_legendre(void)
-{
-    gauss_legendre(NGL, gl_t, gl_w);
-    gauss_legendre(NGL_SMALL, gls_t, gls_w);
 }
 
 /* Implicit QL on a symmetric tridiagonal matrix; d: diagonal (-> eigenvalues), e: e[i]
@@ -129,14 +120,13 @@ int oracle_rys_roots(int nroots, double x, double *u, double *w)
     double K = 80.0 + 8.0 * nroots;
     if (x * 1.0 > K) tmax = sqrt(K / x);
     double s[NGL], W[NGL], q[NGL], qp[NGL], r[NGL];
-    const int M = nroots <= 10 ? NGL_SMALL : NGL;
-    const double *gt = nroots <= 10 ? gls_t : gl_t, *gw = nroots <= 10 ? gls_w : gl_w;
+    static const int M = NGL;
     double Q[MAXROOTS + 1][NGL];
     double mu0 = 0;
     for (int j = 0; j < M; j++) {
-        double t = tmax * gt[j];
+        double t = tmax * gl_t[j];
         s[j] = t * t;
-        W[j] = tmax * gw[j] * exp(-x * t * t);
+        W[j] = tmax * gl_w[j] * exp(-x * t * t);
         mu0 += W[j];
     }
     double alpha[MAXROOTS], beta[MAXROOTS + 1];
