@@ -156,6 +156,9 @@ void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas);
 #define CINTGPU_K_BUILD        10  /* K[ik] += sum_jl (ij|kl) D[jl] over the list (exchange) */
 #define CINTGPU_JK_BUILD       11  /* J and K from one evaluation of each quartet */
 
+/* A plan is created once and may be executed any number of times, on any stream, but by one
+ * thread at a time: an execution records its arguments (density, outputs) and timing events in
+ * the plan.  Different plans are independent. */
 typedef struct CINTGPUPlan CINTGPUPlan;
 
 /* Build a plan for n items (4 shell indices each, 3 for int3c2e, 2 for int2c2e) of one kind.
