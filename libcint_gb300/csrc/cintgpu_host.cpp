@@ -266,6 +266,15 @@ struct PairMap {
 }  // namespace
 
 /* ------------------------------------------------------------------ plan */
+/* allocator whose resize leaves new elements uninitialised (for tables filled right after) */
+template <class T> struct NoInitAlloc : std::allocator<T> {
+    template <class U> struct rebind { using other = NoInitAlloc<U>; };
+    NoInitAlloc() = default;
+    template <class U> NoInitAlloc(const NoInitAlloc<U> &) {}
+    template <class U> void construct(U *p) noexcept { ::new ((void *)p) U; }
+    template <class U, class... A> void construct(U *p, A &&...a) { ::new ((void *)p) U(std::forward<A>(a)...); }
+};
+
 struct TaskGroup {              /* one kernel launch: tasks [task0, task0 + ntasks) */
     int task0 = 0, ntasks = 0;
     int ws = CG_WS_SMALL;       /* shared-memory doubles per warp */
@@ -296,7 +305,7 @@ struct CINTGPUPlan {
     std::vector<CGPrimPair> prims;
     std::vector<CGTask> tasks;
     std::vector<CGOutTask> outs;
-    std::vector<int> pqlist;       /* surviving primitive quartets, per task slice */
+    std::vector<int, NoInitAlloc<int>> pqlist;   /* surviving primitive quartets, per task slice */
     std::vector<CGGradClass> gclass;   /* adjoint iteration tables per class */
     std::vector<CGGradChunk> gchunk;
     std::vector<CGGradEnt> gent;
@@ -367,7 +376,7 @@ struct Builder {
     const double *env;
     PairMap pair_index;
     std::vector<char> pair_empty;
-    std::unordered_map<int, std::vector<double>> logmaxc;   /* per original shell */
+    std::vector<std::vector<double>> logmaxc;   /* per original shell index (empty: not yet) */
     const std::vector<int> *ao_loc = nullptr;     /* Cartesian AO offset per shell (J/adjoint) */
     const std::vector<int> *prim_loc = nullptr;   /* first primitive per shell (J/adjoint) */
 
@@ -385,17 +394,19 @@ struct Builder {
         }
     }
 
-    const std::vector<double> &log_maxc(int sh, const ShellView &s)
+    /* the returned data stay valid while the cache grows (inner buffers move with their vectors) */
+    const double *log_maxc(int sh, const ShellView &s)
     {
-        auto it = logmaxc.find(sh);
-        if (it != logmaxc.end()) return it->second;
-        std::vector<double> v(s.nprim);
+        if ((size_t)sh >= logmaxc.size()) logmaxc.resize((size_t)sh + 1);
+        std::vector<double> &v = logmaxc[sh];
+        if (!v.empty()) return v.data();
+        v.resize(s.nprim);
         for (int ip = 0; ip < s.nprim; ip++) {     /* CINTOpt_log_max_pgto_coeff, :248-259 */
             double m = 0;
             for (int c = 0; c < s.nctr; c++) m = std::max(m, fabs(s.cf[c * s.nprim + ip]));
             v[ip] = log(m);
         }
-        return logmaxc.emplace(sh, std::move(v)).first->second;
+        return v.data();
     }
 
     /* ordered pair (A col ca, B col cb); lsum = l ceilings entering libcint's log_rr */
@@ -414,8 +425,8 @@ struct Builder {
         double aij_last = A.ex[A.nprim - 1] + B.ex[B.nprim - 1];
         double log_rr = 1.7 - 1.5 * log(aij_last);
         if (lsum > 0) log_rr += lsum * log(sqrt(rr) + 1.);
-        const std::vector<double> &lca = log_maxc(sa, A);
-        const std::vector<double> &lcb = log_maxc(sb, B);
+        const double *lca = log_maxc(sa, A);
+        const double *lcb = log_maxc(sb, B);
         bool empty = true;
         for (int jp = 0; jp < B.nprim; jp++)
             for (int ip = 0; ip < A.nprim; ip++) {
@@ -854,6 +865,9 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
 
     struct Pending { int pij, pkl, out; int64_t npq; int l[4]; int sym; };
     std::vector<Pending> pend;
+    pend.reserve((size_t)n);            /* at least one entry per item (more with nctr > 1) */
+    P->outs.reserve(P->outs.size() + (size_t)n);
+    P->out_item.reserve(P->out_item.size() + (size_t)n);
     std::vector<char> finite_checked;   /* per shell index: data checked once per plan */
     int64_t next_off = 0;
     for (int64_t q = 0; q < n; q++) {
@@ -961,6 +975,18 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         for (const Pending &pe : pend) npq_all += pe.npq;
         P->pqlist.reserve((size_t)npq_all);
     }
+    /* largest screening value of each pair's primitive pairs (NaN counts as +inf): when it is
+     * within a ket primitive's limit every bra primitive pair survives and the test is skipped */
+    std::vector<double> cce_max(P->pairs.size());
+    for (size_t p = 0; p < P->pairs.size(); p++) {
+        const CGPair &q = P->pairs[p];
+        double mx = -INFINITY;
+        for (int i = 0; i < q.npa * q.npb; i++) {
+            const double c = P->prims[q.prim_off + i].cce;
+            mx = std::max(mx, std::isnan(c) ? INFINITY : c);
+        }
+        cce_max[p] = mx;
+    }
     double fl = 0;
     for (size_t w = 0; w < pend.size(); w++) {
         const Pending &pe = pend[w];
@@ -971,12 +997,17 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         P->pqlist.resize((size_t)off + (size_t)nij * nkl);
         int *dst = P->pqlist.data() + off;
         int m = 0;
+        const double amax = cce_max[pe.pij];
         for (int kl = 0; kl < nkl; kl++) {
             const double ck = pb[kl].cce;
             if (ck > P->expcutoff) continue;
             const double lim = P->expcutoff - ck;
-            for (int ij = 0; ij < nij; ij++)
-                if (!(pa[ij].cce > lim)) dst[m++] = kl * nij + ij;
+            if (!(amax > lim)) {
+                for (int ij = 0; ij < nij; ij++) dst[m++] = kl * nij + ij;
+            } else {
+                for (int ij = 0; ij < nij; ij++)
+                    if (!(pa[ij].cce > lim)) dst[m++] = kl * nij + ij;
+            }
         }
         P->pqlist.resize((size_t)off + m);
         int64_t n = (int64_t)P->pqlist.size() - off;
@@ -1088,16 +1119,20 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             gpos += slot;
         }
     }
-    /* longest tasks first within each launch (LPT order for the dynamic work counter) */
-    std::stable_sort(tc.begin(), tc.end(), [](const TaskCost &x, const TaskCost &y) {
+    /* longest tasks first within each launch (LPT order for the dynamic work counter); a stable
+     * sort of indices, so equal costs keep their creation order */
+    struct Key { double cost; int64_t idx; int group; };
+    std::vector<Key> ord(tc.size());
+    for (size_t i = 0; i < ord.size(); i++) ord[i] = {tc[i].cost, (int64_t)i, tc[i].group};
+    std::stable_sort(ord.begin(), ord.end(), [](const Key &x, const Key &y) {
         if (x.group != y.group) return x.group < y.group;
         return x.cost > y.cost;
     });
     P->tasks.reserve(tc.size());
     for (int g = 0; g < 3; g++) {
         P->groups[g].task0 = (int)P->tasks.size();
-        for (const TaskCost &x : tc)
-            if (x.group == g) P->tasks.push_back(x.t);
+        for (const Key &k : ord)
+            if (k.group == g) P->tasks.push_back(tc[k.idx].t);
         P->groups[g].ntasks = (int)P->tasks.size() - P->groups[g].task0;
         P->groups[g].ws = g == 0 ? ws_small : CG_WS_MAX;
         P->groups[g].blocks_per_sm = (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA)
@@ -2244,6 +2279,38 @@ extern "C" int cg_plan_groups_ws(int kind, const int *shls, int64_t n, const int
     for (int g = 0; g < 3; g++) info[g] = P.groups[g].ntasks;
     info[3] = fused(&P) ? 1 : 0;
     info[4] = P.groups[0].ws;
+    return 0;
+}
+
+/* Test hook: FNV-1a hash of a host-built plan's upload image, its launch groups and the scalars
+ * its executions read, so that changes to the planner can be checked to produce identical plans. */
+extern "C" int cg_plan_image_hash(int kind, const int *shls, int64_t n, const int *atm, int natm,
+                                  const int *bas, int nbas, const double *env, int64_t split_target,
+                                  uint64_t *hash)
+{
+    CINTGPUPlan P;
+    int rc = build_plan(&P, kind, shls, n, nullptr, atm, natm, bas, nbas, env, split_target);
+    if (rc) return rc;
+    DevLayout D = dev_layout(&P);
+    std::vector<char> img(D.upload);
+    fill_image(&P, D, img.data());
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const void *p, size_t len) {
+        const unsigned char *c = (const unsigned char *)p;
+        for (size_t i = 0; i < len; i++) { h ^= c[i]; h *= 1099511628211ull; }
+    };
+    mix(img.data(), img.size());
+    for (int g = 0; g < 3; g++) {
+        const TaskGroup &G = P.groups[g];
+        int v[5] = {G.task0, G.ntasks, G.ws, G.blocks_per_sm, G.nblocks};
+        mix(v, sizeof(v));
+    }
+    int64_t s[8] = {P.out_size, P.max_nf, P.hrr_max, P.nef_max, P.prim_quartets, P.nao_cart,
+                    (int64_t)P.fuse_out, (int64_t)P.empty_outs.size()};
+    mix(s, sizeof(s));
+    double f[2] = {P.flops, P.flops_ref};
+    mix(f, sizeof(f));
+    *hash = h;
     return 0;
 }
 

@@ -139,3 +139,25 @@ def test_2c2e_and_contraction_kinds_on_the_host():
         assert f(kind, P(out), P(items), 1, None, P(mol.atm), mol.natm, P(mol.bas), mol.nbas,
                  P(mol.env)) == -1
         assert 'density' in cg.last_error()
+
+
+def test_plan_image_hash_is_deterministic():
+    """The planner is deterministic: the same list gives the same upload image, launch groups and
+    scalars (FNV-1a hash of all of them), and a changed exponent changes it.  Changes to the
+    planner's speed are checked against such hashes."""
+    f = cg.lib().cg_plan_image_hash
+    f.restype = ctypes.c_int
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+
+    def h(mol, items, kind=cg.INT2E_SPH):
+        items = np.ascontiguousarray(items, dtype=np.int32)
+        out = np.zeros(1, np.uint64)
+        assert f(kind, P(items), ctypes.c_int64(len(items)), P(mol.atm), mol.natm, P(mol.bas),
+                 mol.nbas, P(mol.env), ctypes.c_int64(0), P(out)) == 0, cg.last_error()
+        return int(out[0])
+    mol = M.config0(seed=4)
+    qs = M.unique_quartets(mol.nbas)[:3000]
+    assert h(mol, qs) == h(mol, qs)
+    assert h(mol, qs, 7) == h(mol, qs, 7)
+    moved = _variant(mol, 'env', int(mol.bas[2, M.PTR_EXP]), mol.env[mol.bas[2, M.PTR_EXP]] * 1.01)
+    assert h(moved, qs) != h(mol, qs)
