@@ -37,6 +37,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <functional>
 #include <unordered_map>
 #include <vector>
 
@@ -970,11 +971,6 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     work.reserve(pend.size());
     /* per-class constants, indexed by ((li 8 + lj) 8 + lk) 8 + ll (l <= 7 with derivatives) */
     std::vector<double> cls_cost(8 * 8 * 8 * 8, -1.0), cls_ref(8 * 8 * 8 * 8, 0.0);
-    {
-        int64_t npq_all = 0;
-        for (const Pending &pe : pend) npq_all += pe.npq;
-        P->pqlist.reserve((size_t)npq_all);
-    }
     /* largest screening value of each pair's primitive pairs (NaN counts as +inf): when it is
      * within a ket primitive's limit every bra primitive pair survives and the test is skipped */
     std::vector<double> cce_max(P->pairs.size());
@@ -987,30 +983,55 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         }
         cce_max[p] = mx;
     }
-    double fl = 0;
-    for (size_t w = 0; w < pend.size(); w++) {
-        const Pending &pe = pend[w];
+    /* survivors of one pending quartet in libcint's order (kl outer, ij inner), written to dst
+     * unless it is null; returns their count */
+    auto screen = [&](const Pending &pe, int *dst) -> int64_t {
         const CGPair &a = P->pairs[pe.pij], &b = P->pairs[pe.pkl];
         const CGPrimPair *pa = &P->prims[a.prim_off], *pb = &P->prims[b.prim_off];
-        int nij = a.npa * a.npb, nkl = b.npa * b.npb;
-        int64_t off = (int64_t)P->pqlist.size();
-        P->pqlist.resize((size_t)off + (size_t)nij * nkl);
-        int *dst = P->pqlist.data() + off;
-        int m = 0;
+        const int nij = a.npa * a.npb, nkl = b.npa * b.npb;
         const double amax = cce_max[pe.pij];
+        int64_t m = 0;
         for (int kl = 0; kl < nkl; kl++) {
             const double ck = pb[kl].cce;
             if (ck > P->expcutoff) continue;
             const double lim = P->expcutoff - ck;
             if (!(amax > lim)) {
-                for (int ij = 0; ij < nij; ij++) dst[m++] = kl * nij + ij;
+                if (dst)
+                    for (int ij = 0; ij < nij; ij++) dst[m + ij] = kl * nij + ij;
+                m += nij;
             } else {
                 for (int ij = 0; ij < nij; ij++)
-                    if (!(pa[ij].cce > lim)) dst[m++] = kl * nij + ij;
+                    if (!(pa[ij].cce > lim)) {
+                        if (dst) dst[m] = kl * nij + ij;
+                        m++;
+                    }
             }
         }
-        P->pqlist.resize((size_t)off + m);
-        int64_t n = (int64_t)P->pqlist.size() - off;
+        return m;
+    };
+    /* count, prefix-sum, fill: on several threads for large lists (the positions, and so the
+     * table, are the same as one thread's) */
+    const size_t npend = pend.size();
+    std::vector<int64_t> pos(npend + 1, 0);
+    const int nthr = npend >= 50000 ? std::max(1, std::min(16, (int)std::thread::hardware_concurrency())) : 1;
+    auto over_pending = [&](const std::function<void(size_t, size_t)> &body) {
+        if (nthr == 1) { body(0, npend); return; }
+        std::vector<std::thread> th;
+        for (int t = 0; t < nthr; t++) th.emplace_back(body, npend * t / nthr, npend * (t + 1) / nthr);
+        for (std::thread &x : th) x.join();
+    };
+    over_pending([&](size_t b, size_t e) { for (size_t w = b; w < e; w++) pos[w + 1] = screen(pend[w], nullptr); });
+    const int64_t base = (int64_t)P->pqlist.size();
+    pos[0] = base;
+    for (size_t w = 0; w < npend; w++) pos[w + 1] += pos[w];
+    P->pqlist.resize((size_t)pos[npend]);
+    over_pending([&](size_t b, size_t e) {
+        for (size_t w = b; w < e; w++) screen(pend[w], P->pqlist.data() + pos[w]);
+    });
+    double fl = 0;
+    for (size_t w = 0; w < npend; w++) {
+        const Pending &pe = pend[w];
+        const int64_t off = pos[w], n = pos[w + 1] - pos[w];
         const int ck = ((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3];
         if (cls_cost[ck] < 0) {
             cls_cost[ck] = per_primitive(P, pe.l) ? flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3])
