@@ -317,6 +317,8 @@ struct CINTGPUPlan {
     std::vector<int> eround;       /* stage-3 rounds: start | count << 16 | box << 24 */
     std::vector<int> empty_outs;   /* output quartets without any task (zero-filled) */
     bool fuse_out = true;          /* the integral kernel stores finished quartets itself */
+    int plan_threads = 1;          /* host threads for the planner's screening (plans created by
+                                      cintgpu_plan_create*; chunk plans are built in parallel) */
     int ws_kb = 0;                 /* shared memory per warp of the regular group in KB (0: the
                                       CINTGPU_WS_KB override or the default 24) */
     int prim_l = 4;                /* int2e classes with lj or ll >= prim_l transfer per primitive
@@ -1013,7 +1015,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
      * table, are the same as one thread's) */
     const size_t npend = pend.size();
     std::vector<int64_t> pos(npend + 1, 0);
-    const int nthr = npend >= 50000 ? std::max(1, std::min(16, (int)std::thread::hardware_concurrency())) : 1;
+    const int nthr = npend >= 50000 ? std::max(1, std::min(16, P->plan_threads)) : 1;
     auto over_pending = [&](const std::function<void(size_t, size_t)> &body) {
         if (nthr == 1) { body(0, npend); return; }
         std::vector<std::thread> th;
@@ -1665,6 +1667,7 @@ static int plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
     if (rc) return rc;
     CINTGPUPlan *P = new CINTGPUPlan();
     P->ws_kb = ws_kb;
+    P->plan_threads = (int)std::thread::hardware_concurrency();
     /* CINTGPU_SEPARATE_OUTPUT=1: transform outputs in their own kernel (tuning) */
     if (const char *e = getenv("CINTGPU_SEPARATE_OUTPUT")) P->fuse_out = atoi(e) == 0;
     if (separate_output) P->fuse_out = false;
@@ -2310,6 +2313,7 @@ extern "C" int cg_plan_image_hash(int kind, const int *shls, int64_t n, const in
                                   uint64_t *hash)
 {
     CINTGPUPlan P;
+    P.plan_threads = (int)std::thread::hardware_concurrency();
     int rc = build_plan(&P, kind, shls, n, nullptr, atm, natm, bas, nbas, env, split_target);
     if (rc) return rc;
     DevLayout D = dev_layout(&P);
