@@ -57,6 +57,29 @@ def df_items(norb, nbas, pairs=None):
     return items3, items2
 
 
+def df_index(pairs, nsph, offs, nao, naux):
+    """packed_index for the df_items layout, by its structure: orbital pair p's (ij|P) blocks over
+    all auxiliary shells form one segment of naux * di * dj elements in which the di * dj AO-pair
+    pattern (i fastest) repeats for every auxiliary function.  Same arrays, built by one slice
+    assignment per pair instead of per-element arithmetic."""
+    pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+    di, dj = nsph[pairs[:, 0]], nsph[pairs[:, 1]]
+    seg = di * dj * naux
+    start = np.concatenate([[0], np.cumsum(seg)])
+    pair = np.empty(int(start[-1]), dtype=np.int64)
+    aux = np.empty(int(start[-1]), dtype=np.int64)
+    aux_pattern = {}
+    for p, (i, j) in enumerate(pairs):
+        a, b = int(di[p]), int(dj[p])
+        ab = (offs[i] + np.arange(a))[:, None] * nao + (offs[j] + np.arange(b))[None, :]
+        s0, s1 = int(start[p]), int(start[p + 1])
+        pair[s0:s1] = np.tile(ab.ravel(order='F'), naux)
+        if a * b not in aux_pattern:
+            aux_pattern[a * b] = np.repeat(np.arange(naux, dtype=np.int64), a * b)
+        aux[s0:s1] = aux_pattern[a * b]
+    return pair, aux
+
+
 def fit_weights(items3, nsph):
     """Per packed element of the (ij|P) buffer: 2 for a pair of two different shells (it stands
     for (ab|P) and (ba|P) in rho), else 1."""
@@ -106,11 +129,15 @@ class DFCoulomb:
         self.naux = int(loc[-1] - loc[norb])
         offs = loc[:-1].copy()
         offs[norb:] -= loc[norb]                          # auxiliary functions counted from 0
+        if pairs is None:
+            ii, jj = np.tril_indices(norb)
+            pairs = np.stack([ii, jj], 1)
+        pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
         items3, items2 = df_items(norb, mol.nbas, pairs)
         p3 = Plan(INT3C2E_SPH, mol, items3)
         self.T = torch.empty(p3.output_size, dtype=torch.float64, device='cuda')
         p3.execute(self.T)
-        pair_idx, aux_idx = packed_index(items3, nsph, offs, self.nao)
+        pair_idx, aux_idx = df_index(pairs, nsph, offs, self.nao, self.naux)
         dev = self.T.device
         self.pair_idx = torch.as_tensor(pair_idx, device=dev)
         self.aux_idx = torch.as_tensor(aux_idx, device=dev)

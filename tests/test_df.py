@@ -125,3 +125,21 @@ def test_df_exact_in_the_auxiliary_span(oracle):
     _, _, _, Jdf = _dense_df(oracle, mol, norb, dm)
     Jx = _exact_j(oracle, mol, norb, dm)
     assert np.abs(Jdf - Jx).max() <= 1e-12 * np.abs(Jx).max()
+
+
+def test_structured_index_equals_generic():
+    """df_index (one slice per orbital pair) builds exactly packed_index's arrays for the
+    df_items layout, for all pairs and for a subset"""
+    mol, norb = M.config2(seed=2, natm=4, box=4.0)
+    nsph = df._nsph(mol)
+    loc = np.concatenate([[0], np.cumsum(nsph)])
+    offs = loc[:-1].copy()
+    offs[norb:] -= loc[norb]
+    nao, naux = int(loc[norb]), int(loc[-1] - loc[norb])
+    ii, jj = np.tril_indices(norb)
+    full = np.stack([ii, jj], 1)
+    for pairs in (full, full[::3]):
+        items3, _ = df.df_items(norb, mol.nbas, pairs)
+        a1, b1 = df.packed_index(items3, nsph, offs, nao)
+        a2, b2 = df.df_index(pairs, nsph, offs, nao, naux)
+        assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
