@@ -115,6 +115,26 @@ def contract_j(T, pair_idx, aux_idx, c, nao, diag):
     return X + X.T - torch.where(diag, X, torch.zeros_like(X))
 
 
+def dense_fitted(T, pair_idx, aux_idx, L, nao, naux):
+    """B~ = L^-1 B with B[q, a, b] = (ab|q) for every AO pair (both orders) from the packed (ij|P)
+    buffer, L the metric's Cholesky factor: (naux, nao, nao), so that (ab|cd) ~ sum_q
+    B~[q, a, b] B~[q, c, d].  Memory naux * nao^2 doubles (torch, any device)."""
+    import torch
+    B = torch.zeros(naux * nao * nao, dtype=T.dtype, device=T.device)
+    a, b = pair_idx // nao, pair_idx % nao
+    B[aux_idx * (nao * nao) + pair_idx] = T
+    B[aux_idx * (nao * nao) + b * nao + a] = T          # the (ba|q) half (same values)
+    B = torch.linalg.solve_triangular(L, B.view(naux, nao * nao), upper=False)
+    return B.view(naux, nao, nao)
+
+
+def contract_k(Bt, dm):
+    """K[i, k] = sum_q sum_jl B~[q, i, j] D[j, l] B~[q, k, l] (density-fitted exchange)."""
+    naux, nao, _ = Bt.shape
+    X = (Bt.reshape(naux * nao, nao) @ dm).view(naux, nao, nao)          # X_q = B~_q D
+    return X.permute(1, 0, 2).reshape(nao, naux * nao) @ Bt.permute(1, 0, 2).reshape(nao, naux * nao).T
+
+
 class DFCoulomb:
     """RI-J for one geometry: orbital shells 0..norb-1, auxiliary shells norb..nbas-1 of mol.
     pairs: orbital shell pairs (i >= j) to include (default: all)."""
@@ -170,3 +190,10 @@ class DFCoulomb:
         """Density-fitted J (spherical) for the symmetric density dm."""
         return contract_j(self.T, self.pair_idx, self.aux_idx, self.coefficients(dm), self.nao,
                           self.diag)
+
+    def vk(self, dm):
+        """Density-fitted K (spherical) for the symmetric density dm; the whitened three-index
+        tensor (naux * nao^2 doubles) is formed on first use and kept."""
+        if getattr(self, 'Bt', None) is None:
+            self.Bt = dense_fitted(self.T, self.pair_idx, self.aux_idx, self.L, self.nao, self.naux)
+        return contract_k(self.Bt, dm)

@@ -143,3 +143,60 @@ def test_structured_index_equals_generic():
         a1, b1 = df.packed_index(items3, nsph, offs, nao)
         a2, b2 = df.df_index(pairs, nsph, offs, nao, naux)
         assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
+
+
+def _k_pieces(oracle, mol, norb):
+    import torch
+    nsph = df._nsph(mol)
+    loc = np.concatenate([[0], np.cumsum(nsph)])
+    offs = loc[:-1].copy()
+    offs[norb:] -= loc[norb]
+    nao, naux = int(loc[norb]), int(loc[-1] - loc[norb])
+    ii, jj = np.tril_indices(norb)
+    pairs = np.stack([ii, jj], 1)
+    items3, items2 = df.df_items(norb, mol.nbas, pairs)
+    T = torch.as_tensor(_packed(oracle, 'int3c2e_sph', mol, items3))
+    pair_idx, aux_idx = df.df_index(pairs, nsph, offs, nao, naux)
+    vi, _ = df.packed_index(items2, nsph, offs, naux)
+    V = df.mirror_metric(torch.as_tensor(_packed(oracle, 'int2c2e_sph', mol, items2)),
+                         torch.as_tensor(vi), naux)
+    Bt = df.dense_fitted(T, torch.as_tensor(pair_idx), torch.as_tensor(aux_idx),
+                         torch.linalg.cholesky(V), nao, naux)
+    return Bt, nao
+
+
+def test_df_k_matches_dense(oracle):
+    """density-fitted K from the module's whitened tensor against the dense formula
+    K = T V^-1 T contracted with D, on the oracle's blocks"""
+    import torch
+    mol, norb, dm = _system()
+    Bt, nao = _k_pieces(oracle, mol, norb)
+    T3, V, _, _ = _dense_df(oracle, mol, norb, dm)
+    W = np.einsum('ijp,pq->ijq', T3, np.linalg.inv(V), optimize=True)
+    Kref = np.einsum('ijq,jl,klq->ik', W, dm, T3, optimize=True)
+    K = df.contract_k(Bt, torch.as_tensor(dm)).numpy()
+    assert np.abs(K - Kref).max() <= 1e-10 * np.abs(Kref).max()
+    assert np.abs(K - K.T).max() <= 1e-12 * np.abs(Kref).max()
+    # the same tensor reproduces the fitted J
+    _, _, _, Jref = _dense_df(oracle, mol, norb, dm)
+    J = torch.einsum('qab,qcd,cd->ab', Bt, Bt, torch.as_tensor(dm)).numpy()
+    assert np.abs(J - Jref).max() <= 1e-10 * np.abs(Jref).max()
+
+
+def test_df_k_exact_in_the_auxiliary_span(oracle):
+    """one orbital s shell (exponent a) and the auxiliary s Gaussian of exponent 2a on its atom:
+    every orbital product is in the auxiliary span, so DF K equals exact K = (ss|ss) D"""
+    import torch
+    b = M._Builder()
+    a0 = b.atom(1, (0.0, 0.0, 0.0))
+    a1 = b.atom(1, (0.0, 0.4, 1.1))
+    b.shell(a0, 0, [0.8], [M.gto_norm(0, 0.8)])
+    b.shell(a0, 0, [1.6], [M.gto_norm(0, 1.6)])
+    b.shell(a1, 1, [0.9], [M.gto_norm(1, 0.9)])
+    mol = b.mol('aux span k')
+    Bt, nao = _k_pieces(oracle, mol, 1)
+    dm = np.array([[0.7]])
+    K = df.contract_k(Bt, torch.as_tensor(dm)).numpy()
+    _, eri = oracle.port.call('int2e_sph', M.Mol(mol.atm, mol.bas[:1].copy(), mol.env, 'o'),
+                              (0, 0, 0, 0))
+    assert abs(K[0, 0] - eri.ravel()[0] * 0.7) <= 1e-12 * abs(eri.ravel()[0])
