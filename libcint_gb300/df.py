@@ -14,12 +14,9 @@ triangular solve.  Densities and J are spherical (libcint's int2e_sph AO order).
 """
 import numpy as np
 
-from .molecules import ANG_OF, NCTR_OF
+from .molecules import shell_nsph as _nsph
 
 
-def _nsph(mol):
-    l = mol.bas[:, ANG_OF].astype(np.int64)
-    return np.where(l > 1, 2 * l + 1, (l + 1) * (l + 2) // 2) * mol.bas[:, NCTR_OF].astype(np.int64)
 
 
 def packed_index(items, dims, offs, nao):

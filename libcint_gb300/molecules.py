@@ -246,6 +246,13 @@ def kat_basis_3c2e():
     return Mol(mol.atm, bas, np.array(env), 'test_3c2e.py basis'), 4
 
 
+def shell_nsph(mol):
+    """Real-spherical functions of every shell (all contraction columns); libcint's
+    CINTcgto_spheric, with l <= 1 kept Cartesian as libcint does."""
+    l = mol.bas[:, ANG_OF].astype(np.int64)
+    return np.where(l > 1, 2 * l + 1, (l + 1) * (l + 2) // 2) * mol.bas[:, NCTR_OF].astype(np.int64)
+
+
 def unique_quartets(nbas):
     """All 8-fold unique shell quartets i>=j, k>=l, ij>=kl (row order of libcint's time_c2h6)."""
     out = []
