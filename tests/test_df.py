@@ -59,7 +59,7 @@ def test_packed_df_matches_dense(oracle):
     assert len(pair_idx) == T.numel() and len(vi) == v.numel()
     w = torch.as_tensor(df.fit_weights(items3, nsph))
     V = df.mirror_metric(v, torch.as_tensor(vi), naux)
-    T3, Vref, rho_ref, Jref = _dense_df(oracle, mol, norb, dm)
+    _, Vref, rho_ref, Jref = _dense_df(oracle, mol, norb, dm)
     assert np.abs(V.numpy() - Vref).max() <= 1e-13 * np.abs(Vref).max()
     dmt = torch.as_tensor(dm)
     rho = df.contract_rho(T, w, torch.as_tensor(pair_idx), torch.as_tensor(aux_idx), dmt, naux)
@@ -170,7 +170,7 @@ def test_df_k_matches_dense(oracle):
     K = T V^-1 T contracted with D, on the oracle's blocks"""
     import torch
     mol, norb, dm = _system()
-    Bt, nao = _k_pieces(oracle, mol, norb)
+    Bt, _ = _k_pieces(oracle, mol, norb)
     T3, V, _, _ = _dense_df(oracle, mol, norb, dm)
     W = np.einsum('ijp,pq->ijq', T3, np.linalg.inv(V), optimize=True)
     Kref = np.einsum('ijq,jl,klq->ik', W, dm, T3, optimize=True)
@@ -194,7 +194,7 @@ def test_df_k_exact_in_the_auxiliary_span(oracle):
     b.shell(a0, 0, [1.6], [M.gto_norm(0, 1.6)])
     b.shell(a1, 1, [0.9], [M.gto_norm(1, 0.9)])
     mol = b.mol('aux span k')
-    Bt, nao = _k_pieces(oracle, mol, 1)
+    Bt, _ = _k_pieces(oracle, mol, 1)
     dm = np.array([[0.7]])
     K = df.contract_k(Bt, torch.as_tensor(dm)).numpy()
     _, eri = oracle.port.call('int2e_sph', M.Mol(mol.atm, mol.bas[:1].copy(), mol.env, 'o'),

@@ -26,7 +26,6 @@ def _oracle_j_energy(oracle, mol, dm):
     J = np.zeros_like(dm)
     for (i, j, k, l) in M.unique_quartets(mol.nbas):
         _, blk = oracle.port.call('int2e_sph', mol, (i, j, k, l))
-        si, sj, sk, sl = (slice(loc[x], loc[x + 1]) for x in (i, j, k, l))
         # every distinct permutation of the unique quartet contributes
         seen = set()
         for (a, b, c, d, t) in ((i, j, k, l, 'ijkl'), (j, i, k, l, 'jikl'), (i, j, l, k, 'ijlk'),
@@ -38,7 +37,6 @@ def _oracle_j_energy(oracle, mol, dm):
             g = np.transpose(blk, ['ijkl'.index(ch) for ch in t])
             J[loc[a]:loc[a + 1], loc[b]:loc[b + 1]] += np.einsum(
                 'abcd,cd->ab', g, dm[loc[c]:loc[c + 1], loc[d]:loc[d + 1]])
-        del si, sj, sk, sl
     return J, 0.5 * (dm * J).sum()
 
 

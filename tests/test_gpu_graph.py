@@ -3,8 +3,6 @@ on the caller's stream and a forked side stream, the output kernel), so they can
 CUDA graph and replayed.  A captured int2e_sph / int3c2e_sph execution replayed twice must give the
 eager result bit for bit (every task owns its accumulator slot, the output kernel sums slots in a
 fixed order); a captured J contraction (atomic adds) must agree to 1e-12."""
-import ctypes
-
 import numpy as np
 import pytest
 

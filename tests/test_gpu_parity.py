@@ -106,7 +106,7 @@ def test_kat_3c2e(gpulib, oracle):
         mol.bas[fit, M.ATOM_OF] = mol.bas[k, M.ATOM_OF]
         for j in range(nbas):
             for i in range(nbas):
-                flag, blk = gpulib.dropin('int3c2e_sph', mol, (i, j, k), nbas=nbas)
+                _, blk = gpulib.dropin('int3c2e_sph', mol, (i, j, k), nbas=nbas)
                 _, oblk = oracle.port.call('int3c2e_sph', mol, (i, j, k), nbas=nbas)
                 assert_block_close(blk, oblk, '3c2e %d %d %d' % (i, j, k),
                                    cart_scale(oracle, 'int3c2e_sph', mol, (i, j, k), nbas))

@@ -80,7 +80,7 @@ def test_oracle_2c2e_matches_libcint_live(oracle):
     as the spherical transform cancels."""
     if oracle.ref is None:
         pytest.skip('libcint not built from sources on this machine')
-    mol, norb = M.config2(seed=1, natm=4, box=4.0)
+    mol, _ = M.config2(seed=1, natm=4, box=4.0)
     rng = np.random.RandomState(0)
     pairs = [(int(a), int(b)) for a, b in rng.randint(0, mol.nbas, (120, 2))]
     kat, nk = M.kat_basis()

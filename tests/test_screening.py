@@ -43,7 +43,7 @@ def test_schwarz_bounds_every_quartet(oracle):
 def test_screened_jk_error_is_bounded(oracle):
     mol = _mol()
     blocks = _blocks(oracle, mol)
-    pairs, items = S.diagonal_pairs(mol.nbas)
+    pairs, _ = S.diagonal_pairs(mol.nbas)
     Q = np.zeros((mol.nbas, mol.nbas))
     for i, j in pairs:
         Q[i, j] = Q[j, i] = np.sqrt(np.abs(np.einsum('abab->ab', blocks[(i, j, i, j)])).max())
