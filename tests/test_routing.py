@@ -161,3 +161,19 @@ def test_plan_image_hash_is_deterministic():
     assert h(mol, qs, 7) == h(mol, qs, 7)
     moved = _variant(mol, 'env', int(mol.bas[2, M.PTR_EXP]), mol.env[mol.bas[2, M.PTR_EXP]] * 1.01)
     assert h(moved, qs) != h(mol, qs)
+
+
+def test_empty_lists_plan_for_every_kind():
+    """n = 0 plans build (no tasks, no groups launched; the output kernel, where one runs, has
+    one block and no quartets) for every kind"""
+    f = cg.lib().cg_plan_groups
+    f.restype = ctypes.c_int
+    mol = M.config0(seed=1)
+    items = np.zeros((1, 4), dtype=np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    for kind in (cg.INT2E_SPH, cg.INT2E_CART, cg.INT2E_IP1_SPH, cg.INT2E_IP1_CART, cg.INT3C2E_SPH,
+                 cg.INT3C2E_CART, cg.INT2C2E_SPH, cg.INT2C2E_CART, 7, 8, 9, 10, 11):
+        info = np.full(4, -1, np.int64)
+        assert f(kind, P(items), ctypes.c_int64(0), P(mol.atm), mol.natm, P(mol.bas), mol.nbas,
+                 P(mol.env), P(info)) == 0, (kind, cg.last_error())
+        assert info[:3].sum() == 0
