@@ -1,5 +1,5 @@
-"""Density fitting (RI) of the Coulomb matrix on the GPU, assembled from the batched int3c2e and
-int2c2e plans:
+"""Density fitting (RI) of the Coulomb and exchange matrices on the GPU, assembled from the
+batched int3c2e and int2c2e plans:
 
     rho_Q = sum_cd (Q|cd) D_cd,   V c = rho  (V_PQ = (P|Q), Cholesky once per geometry),
     J_ab  = sum_P (ab|P) c_P.
@@ -10,13 +10,13 @@ src/cint2c2e.c:351-358).  The three-centre integrals of every orbital shell pair
 auxiliary shell are computed once by one plan and stay in HBM in the plan's packed layout (blocks
 (di, dj, dP) back to back, i fastest); host-built index maps give each packed element its AO pair
 and auxiliary function, so a J build is two gathers and two scatter-adds over that buffer plus a
-triangular solve.  Densities and J are spherical (libcint's int2e_sph AO order).
+triangular solve.  K uses the buffer scattered into a dense (naux, nao, nao) tensor whitened by
+the metric's Cholesky factor: K = sum_q B~_q D B~_q^T.  Densities, J and K are spherical
+(libcint's int2e_sph AO order).
 """
 import numpy as np
 
 from .molecules import shell_nsph as _nsph
-
-
 
 
 def packed_index(items, dims, offs, nao):

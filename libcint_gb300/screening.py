@@ -12,8 +12,6 @@ import numpy as np
 from .molecules import shell_nsph as _nsph
 
 
-
-
 def diagonal_pairs(nbas):
     """Shell pairs i >= j and their diagonal quartets (i, j, i, j)."""
     ii, jj = np.tril_indices(nbas)
