@@ -81,3 +81,46 @@ def test_c_program_against_the_header(gpulib, tmp_path):
         s = np.array(shls, np.int32)
         got = getattr(L, name)(None, None, P(s), P(atm), 1, P(bas), 2, P(env), None, None)
         assert got == int(vals[key]), (name, got, vals[key])
+
+
+C_PLAN_SRC = r"""
+#include <stddef.h>
+#include <cuda_runtime.h>
+#include "cintgpu.h"
+
+/* the batched and J/K usage shown in INTEGRATION.md, compiled and linked (not run: it needs a GPU) */
+int run(const int *quartets, long n, const int *atm, int natm, const int *bas, int nbas,
+        const double *env, double *out_dev, const double *dm_cart, double *xj, double *xk,
+        size_t nao_cart, cudaStream_t stream)
+{
+    CINTGPUPlan *p;
+    int rc = cintgpu_plan_create(&p, CINTGPU_INT2E_SPH, quartets, n, NULL, atm, natm, bas, nbas, env);
+    if (rc) return rc;
+    rc = cintgpu_plan_execute(p, out_dev, stream);
+    cintgpu_plan_destroy(p);
+    if (rc) return rc;
+    rc = cintgpu_plan_create(&p, CINTGPU_JK_BUILD, quartets, n, NULL, atm, natm, bas, nbas, env);
+    if (rc) return rc;
+    cudaMemsetAsync(xj, 0, nao_cart * nao_cart * 8, stream);
+    cudaMemsetAsync(xk, 0, nao_cart * nao_cart * 8, stream);
+    rc = cintgpu_plan_execute_jk(p, dm_cart, xj, xk, stream);
+    cintgpu_plan_destroy(p);
+    return rc;
+}
+
+int main(void) { return 0; }
+"""
+
+
+def test_documented_plan_usage_compiles(gpulib, tmp_path):
+    import shutil
+    cc = shutil.which('gcc') or shutil.which('cc')
+    cuda_inc = '/usr/local/cuda/include'
+    if cc is None or not os.path.exists(os.path.join(cuda_inc, 'cuda_runtime.h')):
+        pytest.skip('no C compiler or CUDA headers')
+    lib = gpulib.lib()._name
+    src = tmp_path / 'plans.c'
+    src.write_text(C_PLAN_SRC)
+    subprocess.run([cc, '-std=c99', '-Wall', '-Werror', '-I', os.path.join(ROOT, 'include'), '-I', cuda_inc,
+                    str(src), lib, '-L/usr/local/cuda/lib64', '-lcudart', '-o', str(tmp_path / 'plans'),
+                    '-Wl,-rpath,' + os.path.dirname(lib)], check=True)
