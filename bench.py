@@ -329,12 +329,54 @@ def extra_df(cg, seed=0, natm=20):
             'setup_s': t_setup, 'vj_ms': 1e3 * t_j}
 
 
+def extra_screening(cg, seed=0, natm=24, threshold=1e-10):
+    """c3 J/K with Schwarz/density screening against the full unique list: Schwarz bounds (one
+    int2e_sph plan over the diagonal quartets), the screened plan's size and time, and the largest
+    change of J and K."""
+    import torch
+    from libcint_gb300 import molecules as M
+    from libcint_gb300.coulomb import CoulombPlans
+    from libcint_gb300.screening import schwarz_bounds, screened_coulomb_plans
+    box = 8.0 * (natm / 24.0) ** (1.0 / 3.0)
+    mol = M.config3(seed=seed, natm=natm, box=box)
+    nao = sum(mol.nsph(i) for i in range(mol.nbas))
+    rng = np.random.RandomState(seed)
+    d = rng.normal(0, 0.1, (nao, nao))
+    dm = torch.as_tensor(0.5 * (d + d.T), device='cuda')
+    full = CoulombPlans(mol)
+    res = [None]
+
+    def jk_full():
+        res[0] = full.get_jk(dm)
+    t_full = _timed(jk_full, reps=2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Q = schwarz_bounds(mol)
+    t_q = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sp = screened_coulomb_plans(mol, dm, threshold, Q)
+    t_plan = time.perf_counter() - t0
+    res2 = [None]
+
+    def jk_scr():
+        res2[0] = sp.get_jk(dm)
+    t_scr = _timed(jk_scr, reps=2)
+    (J0, K0), (J1, K1) = res[0], res2[0]
+    return {'workload': 'c3: %d atoms, %.1f A, random symmetric density, threshold %g' % (natm, box, threshold),
+            'quartets': int(len(full.quartets)), 'kept': int(len(sp.quartets)),
+            'jk_ms': 1e3 * t_full, 'screened_jk_ms': 1e3 * t_scr, 'schwarz_ms': 1e3 * t_q,
+            'screened_plan_s': t_plan,
+            'max_abs_dJ': float((J1 - J0).abs().max()), 'max_abs_dK': float((K1 - K0).abs().max())}
+
+
 def run_extras(cg, mol, qs, value, args):
     out = {}
     for name, fn in (('dropin', lambda: extra_dropin(cg, mol, qs, value)),
                      ('int3c2e', lambda: extra_int3c2e(cg)),
                      ('adjoint', lambda: extra_adjoint(cg)),
-                     ('jk', lambda: extra_jk(cg))):
+                     ('jk', lambda: extra_jk(cg)),
+                     ('screening', lambda: extra_screening(cg)),
+                     ('df', lambda: extra_df(cg))):
         try:
             out[name] = fn()
         except Exception as e:  # an extra must not hide the headline line
@@ -354,6 +396,7 @@ def run_gpu(args, rank, world):
         fn = {'adjoint': lambda: extra_adjoint(cg, natm=args.c3_atoms),
               'jk': lambda: extra_jk(cg, natm=args.c3_atoms),
               'df': lambda: extra_df(cg),
+              'screening': lambda: extra_screening(cg, natm=args.c3_atoms),
               'int3c2e': lambda: extra_int3c2e(cg)}[args.only]
         if rank == 0:
             print(json.dumps({'extra': args.only, **fn()}), flush=True)
@@ -480,8 +523,8 @@ def main():
     ap.add_argument('--e2e-steps', type=int, default=3)
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--no-extras', action='store_true', help='skip the drop-in, int3c2e, adjoint and J/K lines')
-    ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk', 'df'],
+    ap.add_argument('--no-extras', action='store_true', help='skip the side workloads (drop-in, int3c2e, adjoint, J/K, screening, DF)')
+    ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk', 'df', 'screening'],
                     help='run one side workload alone and print its line (profiling)')
     ap.add_argument('--c3-atoms', type=int, default=24, help='atoms of the adjoint workload')
     args = ap.parse_args()

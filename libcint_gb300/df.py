@@ -155,6 +155,9 @@ class DFCoulomb:
         self.T = torch.empty(p3.output_size, dtype=torch.float64, device='cuda')
         p3.execute(self.T)
         pair_idx, aux_idx = df_index(pairs, nsph, offs, self.nao, self.naux)
+        if len(pair_idx) != self.T.numel() or (len(pair_idx) and (
+                pair_idx.max() >= self.nao * self.nao or aux_idx.max() >= self.naux)):
+            raise ValueError('index maps do not match the (ij|P) buffer')   # host-side check
         dev = self.T.device
         self.pair_idx = torch.as_tensor(pair_idx, device=dev)
         self.aux_idx = torch.as_tensor(aux_idx, device=dev)
@@ -167,6 +170,8 @@ class DFCoulomb:
         p3.close()
         p2.close()
         vi, _ = packed_index(items2, nsph, offs, self.naux)
+        if len(vi) != v.numel() or (len(vi) and vi.max() >= self.naux * self.naux):
+            raise ValueError('metric index map does not match the (P|Q) buffer')
         self.V = mirror_metric(v, torch.as_tensor(vi, device=dev), self.naux)
         self.L = torch.linalg.cholesky(self.V)
         diag = np.zeros((self.nao, self.nao), dtype=bool)

@@ -54,6 +54,8 @@ def schwarz_bounds(mol):
     out = torch.empty(plan.output_size, dtype=torch.float64, device='cuda')
     plan.execute(out)
     pos, cnt = diagonal_index(mol, pairs)
+    if len(pos) and (pos.min() < 0 or pos.max() >= plan.output_size):   # checked on the host
+        raise ValueError('diagonal positions outside the plan output')
     diag = out[torch.as_tensor(pos, device=out.device)].cpu().numpy()
     plan.close()
     return schwarz_from_diagonal(mol.nbas, pairs, diag, cnt)
