@@ -39,11 +39,13 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-FP64_PEAK_TFLOPS = 1.196      # measured DFMA peak of this GB300 pool, profiles/fp64_peak_gb300.md
+FP64_PEAK_TFLOPS = 1.196      # measured DFMA peak of this GB300 pool (bench.py --only fp64peak)
 # DRAM read + write of one integral-kernel launch per c1 quartet: 706.0 MB over the first 50k
-# quartets of the committed list (ncu capture, profiles/rys_eri_kernel_c1.md), scaled by quartets
+# quartets of the committed list (one ncu capture of that launch), scaled by quartets
 ERI_DRAM_BYTES_PER_QUARTET = 706.0e6 / 50000
 SCHWARZ = 1e-12
+# one metric string for both arms, so the two lines are directly comparable
+METRIC = 'int2e_sph integrals/s (c1 Schwarz-screened quartets)'
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -138,7 +140,7 @@ def run_reference(args, rank, world):
             rates.append(res['integrals'] / res['seconds'])
     v = float(np.median(rates))
     line = {
-        'impl': 'reference', 'metric': 'int2e_sph integrals/s (c1 Schwarz-screened quartets)',
+        'impl': 'reference', 'metric': METRIC,
         'value': v, 'unit': 'integrals/s', 'n_gpus': args.gpus, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': 1e3 * res['seconds'], 'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
@@ -369,6 +371,25 @@ def extra_screening(cg, seed=0, natm=24, threshold=1e-10):
             'max_abs_dJ': float((J1 - J0).abs().max()), 'max_abs_dK': float((K1 - K0).abs().max())}
 
 
+def extra_fp64peak():
+    """Issue-rate peaks of this GPU (bench_fp64_peak.cu): DFMA, DMMA (FP64 tensor cores) and FFMA
+    in TFLOP/s, the best launch shape of each."""
+    src = os.path.join(ROOT, 'bench_fp64_peak.cu')
+    with tempfile.TemporaryDirectory() as td:
+        exe = os.path.join(td, 'fp64_peak')
+        subprocess.run(['nvcc', '-gencode', 'arch=compute_103a,code=sm_103a', '-O3', '-o', exe, src],
+                       check=True)
+        r = subprocess.run([exe], capture_output=True, text=True, check=True)
+    best = {}
+    for line in r.stdout.splitlines():
+        parts = line.split()
+        if parts and parts[0] in ('DFMA', 'DMMA', 'FFMA') and line.endswith('TFLOP/s'):
+            v = float(parts[-2])
+            best[parts[0]] = max(best.get(parts[0], 0.0), v)
+    return {'tflops': best, 'dmma_over_dfma': best.get('DMMA', 0) / max(best.get('DFMA', 1e-9), 1e-9),
+            'raw': r.stdout.strip().splitlines()}
+
+
 def run_extras(cg, mol, qs, value, args):
     out = {}
     for name, fn in (('dropin', lambda: extra_dropin(cg, mol, qs, value)),
@@ -397,7 +418,8 @@ def run_gpu(args, rank, world):
               'jk': lambda: extra_jk(cg, natm=args.c3_atoms),
               'df': lambda: extra_df(cg),
               'screening': lambda: extra_screening(cg, natm=args.c3_atoms),
-              'int3c2e': lambda: extra_int3c2e(cg)}[args.only]
+              'int3c2e': lambda: extra_int3c2e(cg),
+              'fp64peak': extra_fp64peak}[args.only]
         if rank == 0:
             print(json.dumps({'extra': args.only, **fn()}), flush=True)
         return
@@ -465,7 +487,7 @@ def run_gpu(args, rank, world):
     achieved = plan.flops * args.steps / kern_s / 1e12
     clocks = clk.summary(dev)
     line = {
-        'metric': 'int2e_sph integrals/s (c1 Schwarz-screened quartets, batched plan)',
+        'metric': METRIC,
         'value': value, 'unit': 'integrals/s', 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': 1e3 * tot_s / args.steps, 'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
@@ -482,7 +504,7 @@ def run_gpu(args, rank, world):
                      'unit': 'TFLOP/s', 'frac': achieved / FP64_PEAK_TFLOPS,
                      'traffic': ERI_DRAM_BYTES_PER_QUARTET * len(qs),
                      'traffic_source': 'ncu dram__bytes_read+write of a 50k-quartet launch, '
-                                       'scaled to the step (profiles/rys_eri_kernel_c1.md)',
+                                       'scaled to the step',
                      'flop_model': 'this implementation: per term 20 + 15 VRR entries + groups '
                                    '+ 2 nE nF (FMA = 2)',
                      'libcint_algorithm_tflops': plan.flops_libcint * args.steps / kern_s / 1e12,
@@ -490,7 +512,7 @@ def run_gpu(args, rank, world):
                                                'per-primitive VRR + HRR + gout model, over the '
                                                'same kernel time (exceeds the pipe peak by the '
                                                'work contraction-first saves)',
-                     'peak_source': 'measured DFMA peak (profiles/fp64_peak_gb300.md); '
+                     'peak_source': 'measured DFMA peak (bench.py --only fp64peak); '
                                     'MEASURED_PEAKS.json carries no FP64 figure'},
         'e2e': {'value': nint / statistics.median(e2e_times) if e2e_times else None,
                 'unit': 'integrals/s',
@@ -524,7 +546,8 @@ def main():
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-extras', action='store_true', help='skip the side workloads (drop-in, int3c2e, adjoint, J/K, screening, DF)')
-    ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk', 'df', 'screening'],
+    ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk', 'df', 'screening',
+                                                          'fp64peak'],
                     help='run one side workload alone and print its line (profiling)')
     ap.add_argument('--c3-atoms', type=int, default=24, help='atoms of the adjoint workload')
     args = ap.parse_args()

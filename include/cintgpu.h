@@ -63,7 +63,9 @@ typedef struct {
 #endif
 
 /* ---- Part 1: libcint drop-in ------------------------------------------------------------- */
-/* (ij|kl), real spherical; libcint src/cint2e.c:1186-1194, include/cint_funcs.h:20-23 */
+/* Range separation: env[PTR_RANGE_OMEGA] = omega > 0 gives every integral below with the
+ * long-range Coulomb erf(omega r)/r (libcint src/g2e.c:4477-4492); omega < 0 (short range) is
+ * rejected.  (ij|kl), real spherical; libcint src/cint2e.c:1186-1194, include/cint_funcs.h:20-23 */
 CACHE_SIZE_T int2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
                        FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
 /* (ij|kl), Cartesian; libcint src/cint2e.c:1202-1210 */
@@ -77,6 +79,24 @@ CACHE_SIZE_T int2e_ip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT 
 CACHE_SIZE_T int2e_ip1_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
                             FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
 void int2e_ip1_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
+/* (ij|nabla k l), 3 components; libcint src/autocode/grad2.c:163-176 (ng = {0,0,1,0,...}) */
+CACHE_SIZE_T int2e_ip2_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                           FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+CACHE_SIZE_T int2e_ip2_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                            FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+void int2e_ip2_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
+/* (nabla i j|k) and (ij|nabla k), 3 components each; libcint src/autocode/int3c2e.c:72-87 and
+ * :153-168 */
+CACHE_SIZE_T int3c2e_ip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                             FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+CACHE_SIZE_T int3c2e_ip1_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                              FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+void int3c2e_ip1_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
+CACHE_SIZE_T int3c2e_ip2_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                             FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+CACHE_SIZE_T int3c2e_ip2_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                              FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+void int3c2e_ip2_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
 /* (ij|k), real spherical / Cartesian; libcint src/cint3c2e.c:693-717 */
 CACHE_SIZE_T int3c2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
                          FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
@@ -107,6 +127,20 @@ FINT cint2e_ip1_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, F
                      double *env, CINTOpt *opt);
 void cint2e_ip1_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas,
                               double *env);
+FINT cint2e_ip2_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                    double *env, CINTOpt *opt);
+FINT cint2e_ip2_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                     double *env, CINTOpt *opt);
+void cint2e_ip2_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                              double *env);
+FINT cint3c2e_ip1_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                      double *env, CINTOpt *opt);
+FINT cint3c2e_ip1_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                       double *env, CINTOpt *opt);
+FINT cint3c2e_ip2_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                      double *env, CINTOpt *opt);
+FINT cint3c2e_ip2_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                       double *env, CINTOpt *opt);
 FINT cint3c2e_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
                   double *env, CINTOpt *opt);
 FINT cint3c2e_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
@@ -139,6 +173,12 @@ void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas);
 #define CINTGPU_INT3C2E_CART   6
 #define CINTGPU_INT2C2E_SPH    12
 #define CINTGPU_INT2C2E_CART   13
+#define CINTGPU_INT2E_IP2_SPH  14   /* (ij|nabla k l), 3 components */
+#define CINTGPU_INT2E_IP2_CART 15
+#define CINTGPU_INT3C2E_IP1_SPH  16 /* (nabla i j|k), 3 components */
+#define CINTGPU_INT3C2E_IP1_CART 17
+#define CINTGPU_INT3C2E_IP2_SPH  18 /* (ij|nabla k), 3 components */
+#define CINTGPU_INT3C2E_IP2_CART 19
 
 #define CINTGPU_OK              0
 #define CINTGPU_ERR_ARG        -1   /* invalid argument (shell index, l, nprim, omega != 0) */
@@ -229,13 +269,13 @@ int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,
                        int nbas, const double *env);
 
 /* Allocation-free batched int2e_sph (no libcint counterpart).  For callers that cannot allocate
- * device memory during a call (work enqueued inside a CUDA stream capture, or frameworks that own
- * the device memory budget).  Same result as a CINTGPU_INT2E_SPH plan with offsets = NULL: out_dev
- * receives the dense blocks of the n quartets back to back (sum of di*dj*dk*dl doubles).  All
- * device scratch lives in one static device array of CINTGPU_NOALLOC_BYTES (32 MiB, held by every
- * GPU that loads the library until exit); a batch needing more returns CINTGPU_ERR_NOMEM with a
- * message.  The first call on a device sets up the array's address (make it before any stream
- * capture).  Calls share the array: calls that overlap on the GPU race, so serialise them.
+ * device memory during a call (frameworks that own the device memory budget through their own
+ * allocator).  Same result as a CINTGPU_INT2E_SPH plan with offsets = NULL: out_dev receives the
+ * dense blocks of the n quartets back to back (sum of di*dj*dk*dl doubles).  All device scratch
+ * lives in one static device array of CINTGPU_NOALLOC_BYTES (32 MiB, held by every GPU that loads
+ * the library until exit); a batch needing more returns CINTGPU_ERR_NOMEM with a message.  The
+ * first call on a device looks up the array's address (valid until a cudaDeviceReset of that
+ * device).  Calls share the array: calls that overlap on the GPU race, so serialise them.
  * Asynchronous on `stream` (a cudaStream_t); calls no cudaMalloc/cudaFree. */
 #define CINTGPU_NOALLOC_BYTES (32 << 20)
 int cintgpu_int2e_sph_noalloc(double *out_dev, const int *shls, int64_t n, const int *atm,
@@ -247,6 +287,12 @@ int cintgpu_rys_roots_dev(int nroots, const double *xs_dev, int count, double *s
 int cintgpu_rys_nmax(void);
 
 const char *cintgpu_last_error(void);
+/* Number of libcint drop-in calls (int2e_sph, ..., cint2e_sph, ...) that failed since the library
+ * was loaded (no libcint counterpart).  A failed call (no usable device, a CUDA error, input the
+ * kernels reject) returns 0 like a screened block but fills its block with NaN, so it cannot be
+ * mistaken for one; the first failure is also reported on stderr, and cintgpu_last_error() holds
+ * the calling thread's message. */
+int64_t cintgpu_dropin_failures(void);
 int cintgpu_device_sm_count(void);
 
 #ifdef __cplusplus

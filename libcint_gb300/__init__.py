@@ -14,7 +14,9 @@ from . import molecules  # noqa: F401
 
 INT2E_SPH, INT2E_CART, INT2E_IP1_SPH, INT2E_IP1_CART, INT3C2E_SPH, INT3C2E_CART = 1, 2, 3, 4, 5, 6
 INT2C2E_SPH, INT2C2E_CART = 12, 13
-_KIND_NSH = {1: 4, 2: 4, 3: 4, 4: 4, 5: 3, 6: 3, 12: 2, 13: 2}
+INT2E_IP2_SPH, INT2E_IP2_CART = 14, 15
+INT3C2E_IP1_SPH, INT3C2E_IP1_CART, INT3C2E_IP2_SPH, INT3C2E_IP2_CART = 16, 17, 18, 19
+_KIND_NSH = {1: 4, 2: 4, 3: 4, 4: 4, 5: 3, 6: 3, 12: 2, 13: 2, 14: 4, 15: 4, 16: 3, 17: 3, 18: 3, 19: 3}
 
 _lib = None
 
@@ -35,16 +37,20 @@ def lib():
     L = ctypes.CDLL(_LIB_PATH)
     vp, i32, i64, dbl = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
     for name in ('int2e_sph', 'int2e_cart', 'int2e_ip1_sph', 'int2e_ip1_cart', 'int3c2e_sph',
-                 'int3c2e_cart', 'int2c2e_sph', 'int2c2e_cart'):
+                 'int3c2e_cart', 'int2c2e_sph', 'int2c2e_cart', 'int2e_ip2_sph', 'int2e_ip2_cart',
+                 'int3c2e_ip1_sph', 'int3c2e_ip1_cart', 'int3c2e_ip2_sph', 'int3c2e_ip2_cart'):
         f = getattr(L, name)
         f.restype = i32
         f.argtypes = [vp, vp, vp, vp, i32, vp, i32, vp, vp, vp]
     for name in ('cint2e_sph', 'cint2e_cart', 'cint2e_ip1_sph', 'cint2e_ip1_cart', 'cint3c2e_sph',
-                 'cint3c2e_cart', 'cint2c2e_sph', 'cint2c2e_cart'):
+                 'cint3c2e_cart', 'cint2c2e_sph', 'cint2c2e_cart', 'cint2e_ip2_sph',
+                 'cint2e_ip2_cart', 'cint3c2e_ip1_sph', 'cint3c2e_ip1_cart', 'cint3c2e_ip2_sph',
+                 'cint3c2e_ip2_cart'):
         f = getattr(L, name)
         f.restype = i32
         f.argtypes = [vp, vp, vp, i32, vp, i32, vp, vp]
-    for name in ('int2e_optimizer', 'int2e_ip1_optimizer', 'int3c2e_optimizer', 'int2c2e_optimizer'):
+    for name in ('int2e_optimizer', 'int2e_ip1_optimizer', 'int3c2e_optimizer', 'int2c2e_optimizer',
+                 'int2e_ip2_optimizer', 'int3c2e_ip1_optimizer', 'int3c2e_ip2_optimizer'):
         f = getattr(L, name)
         f.restype = None
         f.argtypes = [vp, vp, i32, vp, i32, vp]
@@ -96,6 +102,8 @@ def lib():
     L.cintgpu_cart2sph.argtypes = [i32, vp]
     L.cintgpu_cart2sph.restype = i32
     L.cintgpu_last_error.restype = ctypes.c_char_p
+    L.cintgpu_dropin_failures.restype = i64
+    L.cintgpu_dropin_failures.argtypes = []
     L.cintgpu_device_sm_count.restype = i32
     _lib = L
     return L
@@ -209,7 +217,7 @@ def dropin(name, mol, shls, dims=None, nbas=None):
     nsh = 3 if 'int3c2e' in name else (2 if 'int2c2e' in name else 4)
     shls = np.ascontiguousarray(shls, dtype=np.int32)
     sph = name.endswith('_sph')
-    ncomp = 3 if '_ip1' in name else 1
+    ncomp = 3 if ('_ip1' in name or '_ip2' in name) else 1
     cnt = [(mol.nsph(s) if sph else mol.ncart(s)) for s in shls[:nsh]]
     n = int(np.prod(cnt)) * ncomp
     out = np.zeros(n if dims is None else int(np.prod(dims)) * ncomp)

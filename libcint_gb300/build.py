@@ -1,8 +1,9 @@
-"""Build the CUDA library (libcintgpu.so, sm_103a) in-tree and the CPU oracle libraries.
+"""Build the CUDA library (libcintgpu.so, sm_103a) in-tree.
 
-The product library is compiled with nvcc from the two translation units under csrc/ in
-parallel; output goes to libcint_gb300/_build/ (git-ignored).  No cmake and no torch build step:
-the library is plain C-ABI and is loaded with ctypes.
+The product library is compiled with nvcc from the translation units under csrc/ in parallel;
+output goes to libcint_gb300/_build/ (git-ignored).  No cmake and no torch build step: the library
+is plain C-ABI and is loaded with ctypes.  (The CPU oracle the tests check against is built by the
+repository's build entry, not here.)
 """
 import os
 import subprocess
@@ -61,16 +62,8 @@ def build_library(force=False, verbose=False):
     return LIB
 
 
-def build_oracle():
-    """CPU oracle: the C restatement always; libcint itself where its sources are present."""
-    odir = os.path.join(ROOT, 'oracle')
-    subprocess.run(['make', '-s', '-C', odir, 'oracle'], check=True)
-    subprocess.run(['make', '-s', '-j8', '-C', odir, 'ref-if-present'], check=True)
-
-
 def build(force=False):
     build_library(force=force)
-    build_oracle()
     return LIB
 
 

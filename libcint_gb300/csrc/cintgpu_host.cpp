@@ -12,10 +12,14 @@
  *               A pair whose every primitive pair is screened makes the quartet empty, like
  *               libcint's NOVALUE pairs (src/cint2e.c:281-285).
  *   tasks       quartets are put in a canonical order (larger l first inside each pair, larger
- *               pair first) for the int2e kinds, grouped by angular-momentum class, and split
- *               into primitive-quartet slices when there are too few to fill the GPU.
- *   execution   per class one launch of the warp-per-task kernel, then one launch of the output
- *               kernel (sum of slices, cart->sph, strided store).
+ *               pair first) for the int2e kinds, cut into primitive-quartet slices by a cost
+ *               model, and sorted longest first within three task groups: regular classes,
+ *               classes needing 48 KB of shared memory per warp, and int2e classes evaluated
+ *               per primitive.
+ *   execution   one launch of the warp-per-task kernel per non-empty group (warps take tasks
+ *               from an atomic counter; the warp finishing a quartet's last slice transforms
+ *               and stores it), then an output kernel for empty quartets (or, for plans that
+ *               keep it separate, for every quartet: sum of slices, cart->sph, strided store).
  *
  * Thread safety: the drop-in entry points keep one CUDA stream, device arena and pinned staging
  * buffer per calling thread, so OpenMP callers may call them concurrently (libcint's contract,
@@ -38,6 +42,7 @@
 #include <string>
 #include <thread>
 #include <functional>
+#include <limits>
 #include <unordered_map>
 #include <vector>
 
@@ -295,6 +300,7 @@ struct CINTGPUPlan {
     int natm = 0;
     int64_t nprim_tot = 0;
     double expcutoff = 60;
+    double omega2 = 0;             /* omega^2 of the long-range Coulomb (0: 1/r) */
     int64_t nitems = 0;
     int64_t out_size = 0;          /* doubles per component */
     double flops = 0;
@@ -321,8 +327,11 @@ struct CINTGPUPlan {
                                       cintgpu_plan_create*; chunk plans are built in parallel) */
     int ws_kb = 0;                 /* shared memory per warp of the regular group in KB (0: the
                                       CINTGPU_WS_KB override or the default 24) */
-    int prim_l = 4;                /* int2e classes with lj or ll >= prim_l transfer per primitive
+    int prim_l = 3;                /* int2e classes with ll >= prim_l (or lj >= prim_l when the
+                                      bra route does not take them) transfer per primitive
                                       (CINTGPU_PER_PRIMITIVE_L overrides, 0 = every class) */
+    int bra_l = 2;                 /* classes with lj >= bra_l and ll < prim_l transfer the bra per
+                                      term (CINTGPU_BRA_TERM_L overrides, e.g. 99 = never) */
     int hrr_max = 1;               /* doubles of one transfer buffer, largest class */
     int nef_max = 1;               /* (e0|f0) accumulators, largest class */
     std::vector<int> out_item;     /* item index of each CGOutTask */
@@ -523,8 +532,21 @@ double flops_per_primq(int li, int lj, int lk, int ll, int mode)
         double nef = (double)range(li, lj) * range(lk, ll);
         return n * (20 + 3 * 5 * vrr + ngroup + 2 * nef);
     }
+    if (mode == CG_MODE_ERIB) {
+        /* bra per term: VRR, the bra transfer of each axis, then per (ij, fx, fy) group one
+         * product and 2 flops per f member; the ket transfer is per contracted quartet */
+        auto nc = [](int l) { return (l + 1) * (l + 2) / 2; };
+        double hrr_bra = 0;
+        for (int j = 1; j <= lj; j++) hrr_bra += (double)(li + lj - j + 1) * (lk + ll + 1);
+        double vrr2 = (double)(li + lj + 1) * (lk + ll + 1);
+        double nij = (double)nc(li) * nc(lj);
+        double nfr = 0;
+        for (int l = lk; l <= lk + ll; l++) nfr += nc(l);
+        return n * (20 + 3 * 5 * vrr2 + 3 * 2 * hrr_bra + nij * nc(lk + ll) + 2 * nij * nfr);
+    }
     double per_root = 20 + 3 * 5 * vrr + 3 * 2 * hrr;
     if (mode == CG_MODE_IP1) per_root += 3 * 3 * (double)L.G / L.dI * (L.dI - 1) + 9.0 * L.nf;
+    else if (mode == CG_MODE_IP2) per_root += 3 * 3 * (double)L.G / L.dK * (L.dK - 1) + 9.0 * L.nf;
     else if (mode == CG_MODE_GRAD || mode == CG_MODE_GRADA) {
         double nT = (double)(li + 1) * (lj + 1) * (lk + 1) * (ll + 1);
         per_root += 9.0 * L.nf + 3 * nT * (mode == CG_MODE_GRADA ? 20 : 12);
@@ -538,7 +560,7 @@ double flops_per_primq(int li, int lj, int lk, int ll, int mode)
  * na = li + lj + 1 is the row length of the VRR arrays): the stage-3 groups, the permutations
  * from the transfer's Cartesian order to the accumulator rows/columns, and the transfer's buffer
  * size.  Layout described with CGEriClass. */
-static int build_eri_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
+static int build_eri_class(CINTGPUPlan *P, int li, int lj, int lk, int ll, bool bra)
 {
     struct Side {
         std::vector<int> x, y, z0, nz, base, pidx;
@@ -559,8 +581,28 @@ static int build_eri_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
             }
         return S;
     };
-    const Side E = side(li, lj), F = side(lk, ll);
-    const int na = li + lj + 1;
+    /* bra classes: one E entry per Cartesian pair (i, j), row i nfj + j, axis offsets
+     * i + dI j in the per-term arrays g(i, j, f) (dI = li + 1); z powers fixed (one member) */
+    auto bra_side = [&]() {
+        Side S;
+        S.lmax = li + lj;
+        const int dI = li + 1;
+        for (int ix = li; ix >= 0; ix--)
+            for (int iy = li - ix; iy >= 0; iy--)
+                for (int jx = lj; jx >= 0; jx--)
+                    for (int jy = lj - jx; jy >= 0; jy--) {
+                        S.x.push_back(ix + dI * jx);
+                        S.y.push_back(iy + dI * jy);
+                        S.z0.push_back((li - ix - iy) + dI * (lj - jx - jy));
+                        S.nz.push_back(1);
+                        S.base.push_back(S.n);
+                        S.n++;
+                    }
+        return S;
+    };
+    const Side E = bra ? bra_side() : side(li, lj), F = side(lk, ll);
+    /* stride of f in the per-term axis arrays */
+    const int na = bra ? (li + 1) * (lj + 1) : li + lj + 1;
     CGEriClass c;
     c.nE = E.n;
     c.nF = F.n;
@@ -639,21 +681,24 @@ static int build_eri_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
                     P->eperm.push_back(S.base[p] + (l - x - y) - S.z0[p]);
                 }
     };
-    perm(E, li);
+    if (bra)   /* rows are already in the transfer's order (i nfj + j) */
+        for (int e = 0; e < c.nE; e++) P->eperm.push_back(e);
+    else
+        perm(E, li);
     perm(F, lk);
     auto below = [](int l) { return l * (l + 1) * (l + 2) / 6; };
     int need = std::max(c.nE * c.nF, ncart_l(li) * ncart_l(lj) * ncart_l(lk) * ncart_l(ll));
-    for (int b = 1; b <= lj; b++)
+    for (int b = 1; b <= (bra ? 0 : lj); b++)
         need = std::max(need, (below(li + lj - b + 1) - below(li)) * ncart_l(b) * c.nF);
     for (int d = 1; d <= ll; d++)
         need = std::max(need, ncart_l(li) * ncart_l(lj) * (below(lk + ll - d + 1) - below(lk)) * ncart_l(d));
     c.hrr_need = need;
-    c.maxab = (lj + 1) | ((ll + 1) << 8);
+    c.maxab = (bra ? 1 : lj + 1) | ((ll + 1) << 8);
     /* transfer program: per bra level b = 1..lj, nrows then (hi, lo, axis) per row (e, jb):
      * row = e_hi(e + 1_ax, jb - 1_ax), lo = (e, jb - 1_ax), ax = lowest non-zero axis of jb;
      * per ket level d = 1..ll, nent, in_stride, out_stride, then (hi, lo, axis) per (f, ld) */
     c.hprog_off = (int)P->hprog.size();
-    c.pad0 = 0;
+    c.bra = bra ? 1 : 0;
     auto cidx = [](int l, int x, int y) { int r = l - x; return r * (r + 1) / 2 + (r - y); };
     auto comps = [](int l) {
         std::vector<std::array<int, 3>> v;
@@ -661,7 +706,7 @@ static int build_eri_class(CINTGPUPlan *P, int li, int lj, int lk, int ll)
             for (int y = l - x; y >= 0; y--) v.push_back({x, y, l - x - y});
         return v;
     };
-    for (int b = 1; b <= lj; b++) {
+    for (int b = 1; b <= (bra ? 0 : lj); b++) {
         const int ncb1 = ncart_l(b - 1);
         const auto jb_list = comps(b);
         int nrows = (below(li + lj - b + 1) - below(li)) * ncart_l(b);
@@ -786,23 +831,49 @@ static void free_plan_device(CINTGPUPlan *p)
     p->side = nullptr;
 }
 
-/* int2e classes whose horizontal transfer is applied per primitive (libcint's order) instead of
- * after contraction: with lj or ll >= 4 the 3D transfer of contracted blocks multiplies the
- * per-axis rounding amplifications and leaves the 1e-12 bar (measured on (ih|ih): 1.2e-12 vs
- * libcint's 1e-14); kernel order, so lj <= li and ll <= lk */
+/* Where the horizontal transfers run (kernel order, so lj <= li and ll <= lk).  Transferring a
+ * contracted 3D block multiplies the three axes' rounding amplifications, where libcint's
+ * per-axis transfers of each primitive's 2D integrals only add them.  Measured against a
+ * long-double evaluation on the c1 classes: contraction first leaves up to 6.8e-9 relative error
+ * on uncancelled Cartesian elements of f-f transfers and ~5e-12 of the block scale on (fd|dd)
+ * (libcint: 1.1e-10 and 7e-15); with lj or ll >= 4 it even leaves the 1e-12 absolute bar
+ * ((ih|ih): 1.2e-12).  So:
+ *   ll >= prim_l (default 3)          both transfers per primitive (CG_MODE_ERIP);
+ *   lj >= bra_l (default 2), ll < prim_l   the bra transfer per term, the ket transfer (ll <= 2,
+ *                                     whose amplification stays small) after contraction
+ *                                     (CG_MODE_ERIB);
+ *   otherwise                         both transfers after contraction (contraction first).
+ * A class whose per-term arrays do not fit the largest per-warp shared memory falls back to the
+ * next route that fits ((ii|ii)-type classes: contraction first). */
+static bool erip_fits(const int *l)
+{
+    CGLayout L;
+    cg_layout(l[0], l[1], l[2], l[3], CG_MODE_ERIP, CG_WS_MAX, &L);
+    return L.T >= 1 && L.G < 2048;
+}
+static bool bra_term(const CINTGPUPlan *P, const int *l)
+{
+    if (P->mode != CG_MODE_ERI || l[1] < P->bra_l || l[3] >= P->prim_l) return false;
+    /* stage-3 rounds address groups with 16 bits */
+    if (ncart_l(l[0]) * ncart_l(l[1]) * ncart_l(l[2] + l[3]) >= 65536) return false;
+    CGLayout L;
+    cg_layout(l[0], l[1], l[2], l[3], CG_MODE_ERIB, CG_WS_MAX, &L);
+    return L.T >= 1;
+}
 static bool per_primitive(const CINTGPUPlan *P, const int *l)
 {
     if (P->mode != CG_MODE_ERI || (l[1] < P->prim_l && l[3] < P->prim_l)) return false;
-    CGLayout L;   /* the per-primitive g arrays of the largest classes do not fit: (ii|ii) */
-    cg_layout(l[0], l[1], l[2], l[3], CG_MODE_ERIP, CG_WS_MAX, &L);
-    return L.T >= 1 && L.G < 2048;
+    if (bra_term(P, l)) return false;
+    return erip_fits(l);
 }
 
 /* Build the host images. split_target: minimum number of compute tasks wanted (0 = no split). */
 /* shell indices per item of an integral kind */
 static int kind_shells(int kind)
 {
-    if (kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART) return 3;
+    if (kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART || kind == CINTGPU_INT3C2E_IP1_SPH
+        || kind == CINTGPU_INT3C2E_IP1_CART || kind == CINTGPU_INT3C2E_IP2_SPH
+        || kind == CINTGPU_INT3C2E_IP2_CART) return 3;
     if (kind == CINTGPU_INT2C2E_SPH || kind == CINTGPU_INT2C2E_CART) return 2;
     return 4;
 }
@@ -810,7 +881,8 @@ static int kind_shells(int kind)
 static bool kind_sph(int kind)
 {
     return kind == CINTGPU_INT2E_SPH || kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT3C2E_SPH
-        || kind == CINTGPU_INT2C2E_SPH;
+        || kind == CINTGPU_INT2C2E_SPH || kind == CINTGPU_INT2E_IP2_SPH
+        || kind == CINTGPU_INT3C2E_IP1_SPH || kind == CINTGPU_INT3C2E_IP2_SPH;
 }
 
 static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, const int64_t *offsets,
@@ -820,11 +892,18 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     (void)nbas;
     P->kind = kind;
     if (const char *e = getenv("CINTGPU_PER_PRIMITIVE_L")) P->prim_l = std::max(0, atoi(e));
+    if (const char *e = getenv("CINTGPU_BRA_TERM_L")) P->bra_l = std::max(0, atoi(e));
     switch (kind) {
     case CINTGPU_INT2E_SPH: P->mode = CG_MODE_ERI; P->sph = 1; P->three = 0; break;
     case CINTGPU_INT2E_CART: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; break;
     case CINTGPU_INT2E_IP1_SPH: P->mode = CG_MODE_IP1; P->sph = 1; P->three = 0; break;
     case CINTGPU_INT2E_IP1_CART: P->mode = CG_MODE_IP1; P->sph = 0; P->three = 0; break;
+    case CINTGPU_INT2E_IP2_SPH: P->mode = CG_MODE_IP2; P->sph = 1; P->three = 0; break;
+    case CINTGPU_INT2E_IP2_CART: P->mode = CG_MODE_IP2; P->sph = 0; P->three = 0; break;
+    case CINTGPU_INT3C2E_IP1_SPH: P->mode = CG_MODE_IP1; P->sph = 1; P->three = 1; break;
+    case CINTGPU_INT3C2E_IP1_CART: P->mode = CG_MODE_IP1; P->sph = 0; P->three = 1; break;
+    case CINTGPU_INT3C2E_IP2_SPH: P->mode = CG_MODE_IP2; P->sph = 1; P->three = 1; break;
+    case CINTGPU_INT3C2E_IP2_CART: P->mode = CG_MODE_IP2; P->sph = 0; P->three = 1; break;
     case CINTGPU_INT3C2E_SPH: P->mode = CG_MODE_ERI; P->sph = 1; P->three = 1; break;
     case CINTGPU_INT3C2E_CART: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 1; break;
     case CINTGPU_INT2C2E_SPH: P->mode = CG_MODE_ERI; P->sph = 1; P->three = 1; P->two = 1; break;
@@ -836,11 +915,14 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     case CINTGPU_J_GRAD_EXP: P->mode = CG_MODE_GRADA; P->sph = 0; P->three = 0; break;
     default: set_error("unknown integral kind %d", kind); return CINTGPU_ERR_ARG;
     }
-    P->ncomp = P->mode == CG_MODE_IP1 ? 3 : 1;
-    if (env[PTR_RANGE_OMEGA] != 0.0) {
-        set_error("range-separated Coulomb (env[PTR_RANGE_OMEGA] = %g) is not supported", env[PTR_RANGE_OMEGA]);
+    P->ncomp = CG_IS_IP(P->mode) ? 3 : 1;
+    /* env[PTR_RANGE_OMEGA] > 0: long-range Coulomb erf(omega r)/r (src/g2e.c:4477-4492), the same
+     * screening as 1/r; < 0 (short-range erfc, src/g2e.c:4447-4476) is not provided */
+    if (!(env[PTR_RANGE_OMEGA] >= 0.0) || !std::isfinite(env[PTR_RANGE_OMEGA])) {
+        set_error("short-range Coulomb (env[PTR_RANGE_OMEGA] = %g < 0) is not supported", env[PTR_RANGE_OMEGA]);
         return CINTGPU_ERR_UNSUPPORTED;
     }
+    P->omega2 = env[PTR_RANGE_OMEGA] * env[PTR_RANGE_OMEGA];
     /* src/g2e.c:57-62 (+1), src/g3c2e.c:55-59 and src/g2c2e.c:44-48 (no +1) */
     if (env[PTR_EXPCUTOFF] == 0) P->expcutoff = 60;
     else P->expcutoff = std::max(40.0, env[PTR_EXPCUTOFF]) + (P->three ? 0 : 1);
@@ -864,7 +946,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         B.prim_loc = &prim_loc;
     }
     const int nsh = kind_shells(kind);
-    const int dinc = P->mode == CG_MODE_IP1 ? 1 : 0;
+    /* the derivative raises the l ceiling entering libcint's log_rr of the differentiated pair */
+    const int dinc = P->mode == CG_MODE_IP1 ? 1 : 0, dinc_k = P->mode == CG_MODE_IP2 ? 1 : 0;
 
     struct Pending { int pij, pkl, out; int64_t npq; int l[4]; int sym; };
     std::vector<Pending> pend;
@@ -909,12 +992,21 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         int64_t block = (int64_t)nd[0] * nd[1] * nd[2] * nd[3];
         int64_t base = offsets ? offsets[q] : next_off;
         next_off = std::max(next_off, base + block);
-        /* kernel order: perm[k] = request index placed at kernel slot k */
+        /* kernel order: perm[k] = request index placed at kernel slot k.  Inside a pair the
+         * larger l comes first (it is the recurrence base); for equal l the shell whose most
+         * diffuse exponent is larger: the product densities then sit near the base centre, so
+         * the transfer (i, j+1) = (i+1, j) + AB (i, j) does not build (i j| from large moments
+         * about a distant centre (a distant, exponent-asymmetric f-f pair loses ~3e-7 of its
+         * largest diagonal element with the base on the diffuse shell, libcint included). */
+        auto amin = [](const ShellView &v) { return *std::min_element(v.ex, v.ex + v.nprim); };
+        auto first = [&](int a, int b) {   /* shell a goes before shell b */
+            return sv[a].l > sv[b].l || (sv[a].l == sv[b].l && amin(sv[a]) >= amin(sv[b]));
+        };
         int perm[4] = {0, 1, 2, 3};
-        if (P->mode != CG_MODE_IP1) {
-            if (sv[0].l < sv[1].l) std::swap(perm[0], perm[1]);
+        if (!CG_IS_IP(P->mode)) {   /* the nabla's shell keeps its slot */
+            if (P->two ? sv[0].l < sv[1].l : !first(0, 1)) std::swap(perm[0], perm[1]);
             if (!P->three) {
-                if (sv[2].l < sv[3].l) std::swap(perm[2], perm[3]);
+                if (!first(2, 3)) std::swap(perm[2], perm[3]);
                 int lij = sv[perm[0]].l * 16 + sv[perm[1]].l, lkl = sv[perm[2]].l * 16 + sv[perm[3]].l;
                 if (lij < lkl) { std::swap(perm[0], perm[2]); std::swap(perm[1], perm[3]); }
             }
@@ -941,7 +1033,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             int pij = P->two ? B.single(ksh[0], *kv[0], c0)
                              : B.pair(ksh[0], *kv[0], c0, ksh[1], *kv[1], c1, kl_[0] + dinc + kl_[1]);
             int pkl = P->three ? B.single(ksh[2], *kv[2], c2)
-                               : B.pair(ksh[2], *kv[2], c2, ksh[3], *kv[3], c3, kl_[2] + kl_[3]);
+                               : B.pair(ksh[2], *kv[2], c2, ksh[3], *kv[3], c3, kl_[2] + dinc_k + kl_[3]);
             CGOutTask o;
             memset(&o, 0, sizeof(o));
             o.out_off = base;
@@ -1037,7 +1129,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         const int ck = ((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3];
         if (cls_cost[ck] < 0) {
             cls_cost[ck] = per_primitive(P, pe.l) ? flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3])
-                                                 : flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode);
+                         : flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3],
+                                           bra_term(P, pe.l) ? CG_MODE_ERIB : P->mode);
             cls_ref[ck] = P->mode == CG_MODE_ERI ? flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3]) : 0.0;
         }
         const double cpq = cls_cost[ck];
@@ -1061,6 +1154,22 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             if (const char *e = getenv("CINTGPU_WS_KB")) kb = atoi(e);
         if (kb >= 8 && kb <= 48) ws_small = kb * 1024 / 8;
     }
+    /* per-primitive kernels run a pair's recurrences about its second centre when that shell is
+     * the tighter one (larger smallest exponent): see g_axis */
+    std::vector<signed char> swap_of(P->pairs.size(), -1);
+    auto pair_swap = [&](int p) -> bool {
+        if (swap_of[p] < 0) {
+            const CGPair &q = P->pairs[p];
+            double ma = INFINITY, mb = INFINITY;
+            for (int t = 0; t < q.npa * q.npb; t++) {
+                const CGPrimPair &pp = P->prims[q.prim_off + t];
+                ma = std::min(ma, pp.aA);
+                mb = std::min(mb, pp.a - pp.aA);
+            }
+            swap_of[p] = mb > ma ? 1 : 0;
+        }
+        return swap_of[p] == 1;
+    };
     std::vector<int> cls_group(8 * 8 * 8 * 8, -1);
     std::vector<CGLayout> cls_layout(8 * 8 * 8 * 8);
     struct TaskCost { CGTask t; double cost; int group; };
@@ -1072,13 +1181,14 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         const int ck = ((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3];
         if (cls_group[ck] < 0) {
             CGLayout Lc;
-            cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, ws_small, &Lc);
+            const int lmode = bra_term(P, pe.l) ? CG_MODE_ERIB : P->mode;
+            cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], lmode, ws_small, &Lc);
             cls_group[ck] = 0;
             if (per_primitive(P, pe.l)) {
                 cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], CG_MODE_ERIP, CG_WS_MAX, &Lc);
                 cls_group[ck] = 2;
             } else if (Lc.T < 2) {
-                cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], P->mode, CG_WS_MAX, &Lc);
+                cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], lmode, CG_WS_MAX, &Lc);
                 cls_group[ck] = 1;
             }
             cls_layout[ck] = Lc;
@@ -1115,7 +1225,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         } else if (P->mode == CG_MODE_ERI) {
             auto it = eri_cls.find(key);
             cls = it != eri_cls.end() ? it->second
-                                      : (eri_cls[key] = build_eri_class(P, pe.l[0], pe.l[1], pe.l[2], pe.l[3]));
+                                      : (eri_cls[key] = build_eri_class(P, pe.l[0], pe.l[1], pe.l[2], pe.l[3],
+                                                                        bra_term(P, pe.l)));
             const CGEriClass &ec = P->eclass[cls];
             slot = (int64_t)ec.nE * ec.nF;
             o.flags |= 2;
@@ -1133,6 +1244,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             x.t.cart_off = gpos;
             x.t.out = pe.out;
             x.t.sym = pe.sym;
+            if (group == 2 || CG_IS_IP(P->mode))   /* per-primitive recurrences: base choice */
+                x.t.sym |= (pair_swap(pe.pij) ? 8 : 0) | (pair_swap(pe.pkl) ? 16 : 0);
             x.t.cls = cls;
             x.t.pad = 0;
             x.cost = x.t.npq * w.cost_pq;
@@ -1185,7 +1298,7 @@ struct DevLayout {
 /* the integral kernel transforms and stores finished quartets itself (int2e, int3c2e, ip1) */
 static bool fused(const CINTGPUPlan *P)
 {
-    if (!P->fuse_out || P->jmode || !(P->mode == CG_MODE_ERI || P->mode == CG_MODE_IP1)) return false;
+    if (!P->fuse_out || P->jmode || !(P->mode == CG_MODE_ERI || CG_IS_IP(P->mode))) return false;
     /* one transform slot per launched warp; classes with huge blocks (l = 5, 6) would need
      * gigabytes, so such plans transform in the separate kernel */
     const int64_t spw = 2 * (int64_t)P->max_nf + (P->eclass.empty() ? 0 : 2 * (int64_t)P->hrr_max);
@@ -1340,6 +1453,7 @@ static int launch_grad_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.status = P->d_counters + 2;
     L.rys_coef = g_ctx.rys_coef;
     L.common_base = M_PI * M_PI * M_PI * 2 / 1.7724538509055160272981674833411451;
+    L.omega2 = P->omega2;
     L.ws_doubles = G.ws;
     L.dm = P->cur_dm;
     L.nao = P->nao_cart;
@@ -1377,6 +1491,7 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.status = P->d_counters + 2;
     L.rys_coef = g_ctx.rys_coef;
     L.common_base = M_PI * M_PI * M_PI * 2 / 1.7724538509055160272981674833411451;
+    L.omega2 = P->omega2;
     L.three = P->three;
     L.two = P->two;
     L.ws_doubles = G.ws;
@@ -1516,8 +1631,14 @@ CACHE_SIZE_T cache_size_query(int kind, const int *shls, const int *bas)
         const int64_t pdata = ip * kp * 5 + ip * ic + kp * kc + (ip + kp) * 2 + nf * 3;
         return (CACHE_SIZE_T)std::max(nc + leng + nf * nc + nf * ic + nf + pdata, nc + nf * 8 * 2);
     }
-    int three = kind == CINTGPU_INT3C2E_SPH || kind == CINTGPU_INT3C2E_CART;
-    int ip1 = kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT2E_IP1_CART;
+    int three = kind_shells(kind) == 3;
+    /* ng increments of libcint's autocode (grad2.c, int3c2e.c): IINC for the ip1 kinds, KINC
+     * for ip2; one g-array shift and 3 components for both */
+    int iinc = kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT2E_IP1_CART
+            || kind == CINTGPU_INT3C2E_IP1_SPH || kind == CINTGPU_INT3C2E_IP1_CART;
+    int kinc = kind == CINTGPU_INT2E_IP2_SPH || kind == CINTGPU_INT2E_IP2_CART
+            || kind == CINTGPU_INT3C2E_IP2_SPH || kind == CINTGPU_INT3C2E_IP2_CART;
+    int ip1 = iinc || kinc;
     int nsh = three ? 3 : 4;
     int l[4] = {0, 0, 0, 0}, np[4] = {1, 1, 1, 1}, nc[4] = {1, 1, 1, 1};
     for (int a = 0; a < nsh; a++) {
@@ -1525,17 +1646,17 @@ CACHE_SIZE_T cache_size_query(int kind, const int *shls, const int *bas)
         l[a] = b[ANG_OF]; np[a] = b[NPRIM_OF]; nc[a] = b[NCTR_OF];
     }
     int ncomp = ip1 ? 3 : 1, gbits = ip1 ? 1 : 0;
-    int lic = l[0] + (ip1 ? 1 : 0), ljc = l[1], lkc = l[2], llc = l[3];
+    int lic = l[0] + iinc, ljc = l[1], lkc = l[2] + kinc, llc = l[3];
     size_t nf = (size_t)ncart_l(l[0]) * ncart_l(l[1]) * ncart_l(l[2]) * (three ? 1 : ncart_l(l[3]));
     size_t ncx = nf * nc[0] * nc[1] * nc[2] * (three ? 1 : nc[3]);
     size_t gsize;
     int nroots;
     if (three) {
-        /* CINTinit_int3c2e_EnvVars: lk_ceil = 0, ll_ceil = k_l */
-        nroots = (lic + ljc + l[2]) / 2 + 1;
+        /* CINTinit_int3c2e_EnvVars (src/g3c2e.c:21-132): lk_ceil = 0, ll_ceil = k_l + KINC */
+        nroots = (lic + ljc + lkc) / 2 + 1;
         int dli, dlj;
         if (lic > ljc) { dli = lic + ljc + 1; dlj = ljc + 1; } else { dli = lic + 1; dlj = lic + ljc + 1; }
-        gsize = (size_t)nroots * dli * (l[2] + 1) * dlj;
+        gsize = (size_t)nroots * dli * (lkc + 1) * dlj;
         size_t leng = gsize * 3 * ((1 << gbits) + 1);
         size_t len0 = nf * ncomp;
         size_t ps = (size_t)np[0] * np[1] * 5 + np[0] * nc[0] + np[1] * nc[1] + np[2] * nc[2]
@@ -1554,13 +1675,17 @@ CACHE_SIZE_T cache_size_query(int kind, const int *shls, const int *bas)
     return (CACHE_SIZE_T)std::max(leng + len0 + ncx * ncomp * 3 + ps, ncx * ncomp + nf * 4);
 }
 
+/* drop-in calls that failed since the library was loaded */
+std::atomic<int64_t> g_dropin_failures{0};
+
 /* One shell block through the GPU (the plain drop-in path). */
 CACHE_SIZE_T dropin(int kind, double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
                     FINT *bas, FINT nbas, double *env)
 {
     if (out == NULL) return cache_size_query(kind, shls, bas);
     const int nsh = kind_shells(kind);
-    int ncomp = (kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT2E_IP1_CART) ? 3 : 1;
+    int ncomp = (kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT2E_IP1_CART
+                 || (kind >= CINTGPU_INT2E_IP2_SPH && kind <= CINTGPU_INT3C2E_IP2_CART)) ? 3 : 1;
     int sph = kind_sph(kind);
     int counts[4] = {1, 1, 1, 1};
     for (int a = 0; a < nsh; a++) {
@@ -1572,35 +1697,43 @@ CACHE_SIZE_T dropin(int kind, double *out, FINT *dims, FINT *shls, FINT *atm, FI
     int d[4] = {1, 1, 1, 1};
     for (int a = 0; a < nsh; a++) d[a] = dims ? dims[a] : counts[a];
     int64_t nout = (int64_t)d[0] * d[1] * d[2] * d[3];
-    auto zero_fill = [&]() {
+    auto fill = [&](double v) {
         for (int comp = 0; comp < ncomp; comp++)
             for (int l = 0; l < counts[3]; l++)
                 for (int k = 0; k < counts[2]; k++)
                     for (int j = 0; j < counts[1]; j++)
                         for (int i = 0; i < counts[0]; i++)
-                            out[comp * nout + i + (int64_t)d[0] * (j + (int64_t)d[1] * (k + (int64_t)d[2] * l))] = 0;
+                            out[comp * nout + i + (int64_t)d[0] * (j + (int64_t)d[1] * (k + (int64_t)d[2] * l))] = v;
     };
-    if (ensure_init()) { zero_fill(); return 0; }
+    auto zero_fill = [&]() { fill(0.0); };
+    /* A failed call (no device, a CUDA error, bad input) must not look like a screened block,
+     * which libcint returns as zeros with 0: the block is filled with NaN, the call returns 0,
+     * the failure is counted (cintgpu_dropin_failures) and the first one is reported on stderr. */
+    auto failed = [&]() -> CACHE_SIZE_T {
+        fill(std::numeric_limits<double>::quiet_NaN());
+        if (g_dropin_failures.fetch_add(1) == 0)
+            fprintf(stderr, "libcintgpu: a drop-in integral call failed (%s); its block is filled "
+                            "with NaN (cintgpu_dropin_failures counts such calls)\n", tl_error.c_str());
+        return 0;
+    };
+    if (ensure_init()) return failed();
     ThreadCtx &T = tl_ctx;
     if (!T.stream && cudaStreamCreateWithFlags(&T.stream, cudaStreamNonBlocking) != cudaSuccess) {
         set_error("cudaStreamCreate failed");
-        zero_fill();
-        return 0;
+        return failed();
     }
     CINTGPUPlan P;
     P.fuse_out = false;   /* one quartet: a separate transform needs far less scratch */
     int rc = build_plan(&P, kind, shls, 1, NULL, atm, natm, bas, nbas, env,
                         (int64_t)g_ctx.sm_count * 8);
-    if (rc) { zero_fill(); return 0; }
+    if (rc) return failed();
     size_t need = plan_device_bytes(&P);
     size_t up = plan_upload_bytes(&P);
     size_t outb = sizeof(double) * P.out_size * ncomp;
     if (grow_dev(&T.arena, &T.arena_size, need) || grow_dev((char **)&T.dout, &T.dout_size, outb)
         || grow_host(&T.pinned, &T.pinned_size, up + sizeof(int) * P.outs.size())
-        || grow_host((char **)&T.hout, &T.hout_size, outb)) {
-        zero_fill();
-        return 0;
-    }
+        || grow_host((char **)&T.hout, &T.hout_size, outb))
+        return failed();
     rc = upload_plan(&P, T.arena, T.arena_size, T.stream, true, T.pinned);
     if (!rc) rc = execute_plan(&P, T.dout, T.stream);
     int *ne_host = (int *)(T.pinned + up);
@@ -1608,7 +1741,7 @@ CACHE_SIZE_T dropin(int kind, double *out, FINT *dims, FINT *shls, FINT *atm, FI
     if (!rc && cudaMemcpyAsync(ne_host, P.d_nonempty, sizeof(int) * P.outs.size(), cudaMemcpyDeviceToHost, T.stream) != cudaSuccess) rc = -1;
     if (!rc && cudaStreamSynchronize(T.stream) != cudaSuccess) { set_error("kernel execution failed: %s", cudaGetErrorString(cudaGetLastError())); rc = -1; }
     P.dbuf = nullptr;
-    if (rc) { zero_fill(); return 0; }
+    if (rc) return failed();
     int nonempty = 0;
     for (size_t o = 0; o < P.outs.size(); o++) nonempty |= ne_host[o];
     if (!nonempty) { zero_fill(); return 0; }
@@ -1638,6 +1771,8 @@ void make_opt(CINTOpt **opt, FINT nbas)
 extern "C" {
 
 const char *cintgpu_last_error(void) { return tl_error.c_str(); }
+
+int64_t cintgpu_dropin_failures(void) { return g_dropin_failures.load(); }
 
 int cintgpu_device_sm_count(void)
 {
@@ -2173,6 +2308,24 @@ CACHE_SIZE_T int2e_ip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT 
 CACHE_SIZE_T int2e_ip1_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                             FINT nbas, double *env, CINTOpt *opt, double *cache)
 { (void)opt; (void)cache; return dropin(CINTGPU_INT2E_IP1_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int2e_ip2_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                           FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_IP2_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int2e_ip2_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                            FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_IP2_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int3c2e_ip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                             FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_IP1_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int3c2e_ip1_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                              FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_IP1_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int3c2e_ip2_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                             FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_IP2_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+CACHE_SIZE_T int3c2e_ip2_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                              FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_IP2_CART, out, dims, shls, atm, natm, bas, nbas, env); }
 CACHE_SIZE_T int3c2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                          FINT nbas, double *env, CINTOpt *opt, double *cache)
 { (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
@@ -2196,6 +2349,12 @@ void int3c2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas
 { (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
 void int2c2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
 { (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
+void int2e_ip2_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
+void int3c2e_ip1_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
+void int3c2e_ip2_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
 void CINTdel_2e_optimizer(CINTOpt **opt)
 {
     if (opt && *opt) { free(*opt); *opt = NULL; }
@@ -2216,6 +2375,20 @@ FINT cint2e_ip1_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, F
 { return int2e_ip1_cart(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
 void cint2e_ip1_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
 { int2e_ip1_optimizer(opt, atm, natm, bas, nbas, env); }
+FINT cint2e_ip2_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int2e_ip2_sph(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+FINT cint2e_ip2_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int2e_ip2_cart(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+void cint2e_ip2_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ int2e_ip2_optimizer(opt, atm, natm, bas, nbas, env); }
+FINT cint3c2e_ip1_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int3c2e_ip1_sph(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+FINT cint3c2e_ip1_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int3c2e_ip1_cart(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+FINT cint3c2e_ip2_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int3c2e_ip2_sph(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+FINT cint3c2e_ip2_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int3c2e_ip2_cart(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
 FINT cint3c2e_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
 { return int3c2e_sph(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
 FINT cint3c2e_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
@@ -2259,14 +2432,15 @@ void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas)
 int cg_init(void) { return ensure_init(); }
 int cg_sm_count(void) { return g_ctx.sm_count; }
 void cg_set_error_msg(const char *msg) { set_error("%s", msg); }
-/* Contraction-first tables of one class, for host-side tests of the table logic:
- * info[12] = CGEriClass fields, groups[4 * ngroup], perm[nE + nF], prog (the transfer program),
+/* Contraction-first tables of one class (bra = 1: the bra-per-term tables), for host-side tests
+ * of the table logic: info[12] = CGEriClass fields, groups[4 * ngroup], perm[nE + nF], prog (the transfer program),
  * rounds[nround]; returns the program length or -1 when a buffer is too small. */
-extern "C" int cg_eri_tables(int li, int lj, int lk, int ll, int *info, int *groups, int maxg,
-                             int *perm, int maxp, int *prog, int maxprog, int *rounds, int maxr)
+extern "C" int cg_eri_tables(int li, int lj, int lk, int ll, int bra, int *info, int *groups,
+                             int maxg, int *perm, int maxp, int *prog, int maxprog, int *rounds,
+                             int maxr)
 {
     CINTGPUPlan P;
-    build_eri_class(&P, li, lj, lk, ll);
+    build_eri_class(&P, li, lj, lk, ll, bra != 0);
     const CGEriClass &c = P.eclass[0];
     if (c.ngroup > maxg || c.nE + c.nF > maxp || (int)P.hprog.size() > maxprog || c.nround > maxr) return -1;
     memcpy(info, &c, sizeof(CGEriClass));
@@ -2277,8 +2451,19 @@ extern "C" int cg_eri_tables(int li, int lj, int lk, int ll, int *info, int *gro
     return (int)P.hprog.size();
 }
 
-/* Host planning only, for tests of the task routing: tasks of the three groups (regular, 48 KB,
- * per-primitive int2e) and whether outputs are transformed inside the integral kernel. */
+/* tasks of a built plan whose class transfers the bra per term */
+static int64_t bra_tasks(const CINTGPUPlan &P)
+{
+    int64_t n = 0;
+    for (int g = 0; g < 2; g++)
+        for (int t = P.groups[g].task0; t < P.groups[g].task0 + P.groups[g].ntasks; t++)
+            n += P.eclass.empty() ? 0 : P.eclass[P.tasks[t].cls].bra;
+    return n;
+}
+
+/* Host planning only, for tests of the task routing: info[0..2] = tasks of the three groups
+ * (regular, 48 KB, per-primitive int2e), info[3] = 1 when outputs are transformed inside the
+ * integral kernel, info[4] = tasks of classes transferring the bra per term. */
 extern "C" int cg_plan_groups(int kind, const int *shls, int64_t n, const int *atm, int natm,
                               const int *bas, int nbas, const double *env, int64_t *info)
 {
@@ -2287,6 +2472,7 @@ extern "C" int cg_plan_groups(int kind, const int *shls, int64_t n, const int *a
     if (rc) return rc;
     for (int g = 0; g < 3; g++) info[g] = P.groups[g].ntasks;
     info[3] = fused(&P) ? 1 : 0;
+    info[4] = P.mode == CG_MODE_ERI ? bra_tasks(P) : 0;
     return 0;
 }
 

@@ -22,6 +22,7 @@ size_t cg_plan_bytes(const CINTGPUPlan *P);
  * (stream-ordered, from pageable memory); allocates no device memory */
 int cg_plan_place(CINTGPUPlan *P, char *region, size_t region_bytes, cudaStream_t stream);
 int cg_plan_run(CINTGPUPlan *P, double *out_dev, cudaStream_t stream);
-extern "C" int cg_eri_tables(int li, int lj, int lk, int ll, int *info, int *groups, int maxg,
-                             int *perm, int maxp, int *prog, int maxprog, int *rounds, int maxr);
+extern "C" int cg_eri_tables(int li, int lj, int lk, int ll, int bra, int *info, int *groups,
+                             int maxg, int *perm, int maxp, int *prog, int maxprog, int *rounds,
+                             int maxr);
 #endif

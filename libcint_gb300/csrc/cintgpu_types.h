@@ -47,7 +47,9 @@ typedef struct {
                             each encoded kl * nij + ij */
     int64_t cart_off;    /* accumulator slot in gctr */
     int out;             /* CGOutTask index (for the non-empty flag) */
-    int sym;             /* unique-quartet flags: bit0 I != J, bit1 K != L, bit2 IJ != KL */
+    int sym;             /* unique-quartet flags: bit0 I != J, bit1 K != L, bit2 IJ != KL;
+                            per-primitive kernels: bit3 (bit4) runs the bra (ket) recurrences
+                            about the pair's second centre (see g_axis) */
     int cls;             /* class tables: CGGradClass (adjoint) or CGEriClass (int2e, int3c2e, J) */
     int pad;
 } CGTask;
@@ -74,7 +76,9 @@ typedef struct { int ob_oc; int c; } CGGradEnt;                          /* ob |
  * (ex, ey, fx, fy): the product gx gy is formed once and multiplies gz for each (ez, fz) member.
  * Accumulator layout: row baseE(ex,ey) + (ez - ez0), column baseF(fx,fy) + (fz - fz0), nF columns;
  * eperm/fperm map the transfer's Cartesian order (shells ascending, libcint order within a shell)
- * to those rows/columns. */
+ * to those rows/columns.  Classes with bra = 1 replace e by the Cartesian pair (i, j) of the bra
+ * shells: a group is one (ix jx, iy jy, fx, fy), its z powers of i and j are fixed, so it has one
+ * row (i nfj + j) and the nfz members of f. */
 typedef struct {
     int group_off, ngroup;   /* CGEriGroup range, ordered by shape (nez, nfz) */
     int perm_off;            /* eperm[nE] then fperm[nF] */
@@ -85,7 +89,9 @@ typedef struct {
     int hprog_off;           /* horizontal-transfer program (ints), see cg_hrr */
     int round_off, nround;   /* stage-3 rounds (ints: first group | count << 16 | box << 24,
                                 box = (MA-1) + 4 (MB-1) of the round's largest nez, nfz) */
-    int pad0;
+    int bra;                 /* 1: the bra transfer runs per term on each axis's 2D integrals
+                                (libcint's order on the bra), the accumulators hold (ij|f0) with
+                                rows i nfj + j, and only the ket transfer follows contraction */
 } CGEriClass;
 typedef struct {
     int oxy;             /* ox | oy << 16: offsets of (ex, fx) and (ey, fy) in the VRR arrays */

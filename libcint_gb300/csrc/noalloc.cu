@@ -1,21 +1,23 @@
 /*
  * Allocation-free batched int2e_sph.
  *
- * Some callers cannot allocate device memory during a call: code enqueuing work inside a CUDA
- * stream capture (where cudaMalloc is not permitted), or frameworks that own the device memory
- * budget through their own allocator and forbid side allocations.  cintgpu_int2e_sph_noalloc
- * serves them: it evaluates the same kernels as cintgpu_plan_execute, but every piece of device
- * scratch (pair tables, surviving-primitive lists, task lists, Cartesian accumulators, output
- * staging) lives in one file-scope __device__ array of CINTGPU_NOALLOC_BYTES (32 MiB) that every
- * GPU loading this library holds until the process exits.  The caller passes the inputs (host
+ * Some callers cannot allocate device memory during a call: frameworks that own the device memory
+ * budget through their own allocator and forbid side allocations, or code running where a
+ * cudaMalloc would synchronise the device or fail outright.  cintgpu_int2e_sph_noalloc serves
+ * them: it evaluates the same kernels as cintgpu_plan_execute, but every piece of device scratch
+ * (pair tables, surviving-primitive lists, task lists, Cartesian accumulators, output staging)
+ * lives in one file-scope __device__ array of CINTGPU_NOALLOC_BYTES (32 MiB) that every GPU
+ * loading this library holds until the process exits.  The caller passes the inputs (host
  * atm/bas/env and shell quartets) and the device output buffer.
  *
  * Set-up: the first call on a device (with that device current) looks up the array's device
- * address with cudaGetSymbolAddress and caches it; make that first call before any stream
- * capture.  All calls share the array and it keeps the last call's contents; the kernels clear
- * what must start at zero (counters, flags, accumulators) on every call.  Calls that overlap on the
- * GPU (different streams, or a graph replayed while another call runs) race on the array: the
- * caller serialises them.
+ * address with cudaGetSymbolAddress and caches it for that device.  The cached address belongs to
+ * the device's primary context: do not keep using the library on a device after
+ * cudaDeviceReset.  All calls share the array and it keeps the last call's contents; the kernels
+ * clear what must start at zero (counters, flags, accumulators) on every call.  Calls that overlap
+ * on the GPU (different streams) race on the array: the caller serialises them.  The plan image
+ * is copied into the array from host memory with a stream-ordered copy that returns once the
+ * data is staged.
  */
 #include <cuda_runtime.h>
 #include <stdio.h>

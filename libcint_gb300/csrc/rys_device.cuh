@@ -41,6 +41,7 @@ __host__ __device__ inline void cg_mode_incs(int mode, int inc[4])
 {
     inc[0] = inc[1] = inc[2] = inc[3] = 0;
     if (mode == CG_MODE_IP1) inc[0] = 1;
+    else if (mode == CG_MODE_IP2) inc[2] = 1;   /* libcint grad2.c ng = {0,0,1,0,...} */
     else if (mode == CG_MODE_GRAD) { inc[0] = 1; inc[1] = 1; inc[2] = 1; }
     else if (mode == CG_MODE_GRADA) { inc[0] = 2; inc[1] = 2; inc[2] = 2; inc[3] = 2; }
 }
@@ -64,9 +65,9 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     L->mmax = lkc + llc;
     L->dI = L->lic + 1; L->dJ = ljc + 1; L->dK = lkc + 1; L->dL = llc + 1;
     L->G = L->dI * L->dJ * L->dK * L->dL;
-    L->ng = (mode == CG_MODE_IP1) ? 2 : 1;
+    L->ng = CG_IS_IP(mode) ? 2 : 1;
     L->nf = ncart(li) * ncart(lj) * ncart(lk) * ncart(ll);
-    L->ncomp = (mode == CG_MODE_IP1) ? 3 : 1;
+    L->ncomp = CG_IS_IP(mode) ? 3 : 1;
     /* per-lane scratch of g_axis; an odd stride keeps the 32 lanes' equal offsets in distinct
      * shared-memory banks */
     L->scr = (L->nmax + 1) * (L->mmax + 1) + (L->nmax + 1) + (L->mmax + 1);
@@ -87,6 +88,23 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
         if (T < 0) T = 0;
         L->off_dij = L->off_dkl = L->off_aacc = L->off_w = L->off_scr = 0;
         L->off_g = T * L->termw;
+    } else if (mode == CG_MODE_ERIB) {
+        /* bra transferred per term: per axis g(i, j, f) = out[(i + dI j) + dI dJ f] for i <= li,
+         * j <= lj, f <= lk+ll (the VRR array fits inside it, since dI dJ >= li+lj+1); the lane
+         * scratch holds one VRR column */
+        L->G = L->dI * L->dJ * (L->mmax + 1);
+        L->gax = L->G | 1;
+        L->gstride = 3 * L->gax;
+        L->termw = 10 + L->mmax + 1;
+        if (L->termw % 2 == 0) L->termw++;
+        L->scr = (L->nmax + 1) | 1;
+        for (int t = 32; t >= 1; t--) {
+            int items = 3 * t < 32 ? 3 * t : 32;
+            if (t * (L->termw + L->gstride) + items * L->scr <= ws_doubles) { T = t; break; }
+        }
+        L->off_dij = L->off_dkl = L->off_aacc = L->off_w = 0;
+        L->off_g = T * L->termw;
+        L->off_scr = L->off_g + T * L->gstride;
     } else if (!grad) {
         /* T terms need T term records, T*3*ng*G doubles of g arrays and min(32, 3T) lane
          * scratch areas */
@@ -193,15 +211,48 @@ __device__ __forceinline__ void vrr_axis(int nmax, int mmax, double b00, double 
     }
 }
 
+/* VRR plus the bra transfer of one axis of one term (the libcint order on the bra,
+ * CINTg0_2e_lj2d4d / _il2d4d, src/g2e.c:560-693: (i, j+1) = (i+1, j) + AB (i, j) on every column
+ * f of the 2D integrals):  out[(i + dI j) + dI dJ f] for i < dI, j < dJ, f <= mmax.  The VRR
+ * array g(a, f) = out[a + (nmax+1) f] is built in place first; columns are then transferred from
+ * the highest f down, through the lane's one-column scratch col[nmax+1], so every write lands
+ * above the VRR columns still to be read (dI dJ >= nmax + 1). */
+__device__ __forceinline__ void vrr_bra_axis(int nmax, int mmax, int dI, int dJ, double b00,
+                                             double b10, const double *__restrict__ mb, double c00,
+                                             double c0p, double g00, double AB, double *col,
+                                             double *out)
+{
+    const int na = nmax + 1, B = dI * dJ;
+    vrr_axis(nmax, mmax, b00, b10, mb, c00, c0p, g00, out);
+    for (int m = mmax; m >= 0; m--) {
+        const double *v = out + na * m;
+        for (int a = 0; a < na; a++) col[a] = v[a];
+        double *o = out + B * m;
+        for (int i = 0; i < dI; i++) o[i] = col[i];
+        for (int j = 1; j < dJ; j++) {
+            for (int a = 0; a <= nmax - j; a++) col[a] = fma(AB, col[a], col[a + 1]);
+            for (int i = 0; i < dI; i++) o[i + dI * j] = col[i];
+        }
+    }
+}
+
 /* ------------------------------------------------------------------ stage 2 */
 /* One Cartesian axis of one term: VRR into T2[a + (nmax+1) m], then the two horizontal
- * transfers; final g[((i dJ + j) dK + k) dL + l] goes to gout.  Lane scratch: T2, a*b00, and a
- * vector of length mmax+1. */
+ * transfers; final g[((i dJ + j) dK + k) dL + l] goes to gout.  Lane scratch: T2, and a vector of
+ * length mmax+1 (m b01, then the ket transfer).
+ * swap bit 0: the bra recurrences run about B = A - AB instead of A (the transfer then builds i
+ * from j: (i+1, j) = (i, j+1) + BA (i, j)); bit 1 likewise on the ket.  The planner sets them when
+ * the second shell of a pair is the tighter one: the product densities sit near the tighter
+ * centre, and moments about the other, distant one make the transfer cancel (a distant,
+ * exponent-asymmetric pair loses up to 1e-7 relative that way). */
 __device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10, double b01,
                                        double c00, double c0p, double g00, double AB, double CD,
-                                       double *scr, double *gout)
+                                       double *scr, double *gout, int swap = 0)
 {
     const int nmax = L.nmax, mmax = L.mmax, na = nmax + 1, nm = mmax + 1;
+    const bool sij = (swap & 1) != 0, skl = (swap & 2) != 0;
+    if (sij) { c00 += AB; AB = -AB; }
+    if (skl) { c0p += CD; CD = -CD; }
     double *T2 = scr;
     /* m b01 in the vector the transfers use later, then the column-order VRR */
     {
@@ -210,28 +261,30 @@ __device__ __forceinline__ void g_axis(const CGLayout &L, double b00, double b10
         for (int m = 0; m <= mmax; m++) { mbv[m] = mb; mb += b01; }
         vrr_axis(nmax, mmax, b00, b10, mbv, c00, c0p, g00, T2);
     }
-    /* (a,0| -> (i,j| one j level at a time, in place on every column m:
-     * col[a] = col[a+1] + AB col[a]; after level j, row i of all columns is g(i,j,m) and goes
-     * through |m,0) -> |k,l) in a short vector, so no (i,j,m) intermediate is stored. */
+    /* (a,0| -> (base, other| one transfer level t at a time, in place on every column m:
+     * col[a] = col[a+1] + AB col[a]; after level t, row b of all columns is g(b, t, m) and goes
+     * through |m,0) -> |base, other) in a short vector, so no (i,j,m) intermediate is stored. */
     double *tmp = scr + na * nm + na;
-    for (int j = 0; j < L.dJ; j++) {
-        if (j > 0) {
+    const int nb = sij ? L.dJ : L.dI, nt = sij ? L.dI : L.dJ;     /* bra: base / transfer count */
+    const int mb = skl ? L.dL : L.dK, mt = skl ? L.dK : L.dL;     /* ket */
+    for (int t = 0; t < nt; t++) {
+        if (t > 0) {
             for (int m = 0; m <= mmax; m++) {
                 double *col = T2 + m * na;
-                for (int a = 0; a <= nmax - j; a++) col[a] = fma(AB, col[a], col[a + 1]);
+                for (int a = 0; a <= nmax - t; a++) col[a] = fma(AB, col[a], col[a + 1]);
             }
         }
-        for (int i = 0; i < L.dI; i++) {
+        for (int b = 0; b < nb; b++) {
+            const int i = sij ? t : b, j = sij ? b : t;
             double *go = gout + (i * L.dJ + j) * L.dK * L.dL;
-            if (L.dL == 1) {
-                for (int k = 0; k < L.dK; k++) go[k] = T2[i + na * k];
-                continue;
-            }
-            for (int m = 0; m <= mmax; m++) tmp[m] = T2[i + na * m];
-            for (int k = 0; k < L.dK; k++) go[k * L.dL] = tmp[k];
-            for (int l = 1; l < L.dL; l++) {
-                for (int m = 0; m <= mmax - l; m++) tmp[m] = fma(CD, tmp[m], tmp[m + 1]);
-                for (int k = 0; k < L.dK; k++) go[k * L.dL + l] = tmp[k];
+            for (int m = 0; m <= mmax; m++) tmp[m] = T2[b + na * m];
+            for (int u = 0; u < mt; u++) {
+                if (u > 0)
+                    for (int m = 0; m <= mmax - u; m++) tmp[m] = fma(CD, tmp[m], tmp[m + 1]);
+                for (int v = 0; v < mb; v++) {
+                    const int k = skl ? u : v, l = skl ? v : u;
+                    go[k * L.dL + l] = tmp[v];
+                }
             }
         }
     }
@@ -253,9 +306,10 @@ __host__ __device__ __forceinline__ int ncart_below(int l) { return l * (l + 1) 
 __device__ inline double *cg_hrr(const double *src, const int *__restrict__ eperm,
                                  const int *__restrict__ fperm, const int *__restrict__ prog,
                                  int li, int lj, int lk, int ll, const double *AB, const double *CD,
-                                 double *h1, double *h2, int lane)
+                                 double *h1, double *h2, int lane, int bra_done)
 {
-    const int nE = ncart_below(li + lj + 1) - ncart_below(li);
+    /* bra_done: src rows are already (i j| in the order i nfj + j; only the ket levels run */
+    const int nE = bra_done ? ncart(li) * ncart(lj) : ncart_below(li + lj + 1) - ncart_below(li);
     const int nF = ncart_below(lk + ll + 1) - ncart_below(lk);
     for (int e = lane; e < nE * nF; e += 32) {
         int ei = e / nF, fi = e - ei * nF;
@@ -265,7 +319,7 @@ __device__ inline double *cg_hrr(const double *src, const int *__restrict__ eper
     double *cur = h1, *nxt = h2;
     const double ab0 = AB[0], ab1 = AB[1], ab2 = AB[2], cd0 = CD[0], cd1 = CD[1], cd2 = CD[2];
     /* bra: level b holds [(ei nc(b) + jb) nF + f] */
-    for (int b = 1; b <= lj; b++) {
+    for (int b = 1; b <= (bra_done ? 0 : lj); b++) {
         const int nrows = __ldg(prog);
         const int *rows = prog + 1;
         const double *__restrict__ c = cur;
@@ -342,7 +396,8 @@ __device__ __forceinline__ double common_fac_sp(int l)   /* libcint src/g1e.c:56
  * c00 = PA - s akl/(aij+akl) PQ, c0p = QC + s aij/(aij+akl) PQ).  rec[9] = weight * prefactor. */
 __device__ __forceinline__ void cg_term(const CGPrimPair &A, const CGPrimPair &B, const CGPair &pij,
                                         const CGPair &pkl, int n, int r, double common,
-                                        const double *__restrict__ coef, double *rec)
+                                        const double *__restrict__ coef, double *rec,
+                                        double omega2 = 0.0)
 {
     double aijkl = A.a + B.a;
     double rs = rsqrt(aijkl);
@@ -352,8 +407,18 @@ __device__ __forceinline__ void cg_term(const CGPrimPair &A, const CGPrimPair &B
     double rho = A.a * B.a * inv;
     double x = rho * rr;
     double s, w;
-    rys_node(n, x, r, coef, s, w);
     double fac1 = common * A.K * B.K * rs * A.inv_a * B.inv_a;
+    if (omega2 > 0.0) {
+        /* long-range Coulomb erf(omega r)/r (libcint CINTg0_2e, src/g2e.c:4477-4492): the
+         * quadrature of theta x, theta = omega^2 / (omega^2 + rho), weights times sqrt(theta),
+         * nodes t^2 -> theta t^2 (in s = t^2 the coefficients below stay linear in s) */
+        const double theta = omega2 / (omega2 + rho);
+        rys_node(n, x * theta, r, coef, s, w);
+        s *= theta;
+        fac1 *= sqrt(theta);
+    } else {
+        rys_node(n, x, r, coef, s, w);
+    }
     double tb = s * inv;                 /* 2 b00 */
     double b00 = 0.5 * tb;
     double oms = 1.0 - s;

@@ -98,7 +98,7 @@ rys_grad_kernel(CGGradLaunch P)
                 const CGPrimPair A = ppij[ij];
                 const CGPrimPair B = ppkl[kl];
                 double *rec = term + lane * CG_TERMW_GRAD;
-                cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec);
+                cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec, P.omega2);
                 rec[10] = 2.0 * A.aA;
                 rec[11] = 2.0 * (A.a - A.aA);
                 rec[12] = 2.0 * B.aA;

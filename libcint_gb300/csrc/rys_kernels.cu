@@ -159,7 +159,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
 
     /* per-lane component offsets into the g arrays (register path: packed 10 bits per axis, G < 1024) */
     int offs[NS > 0 ? NS : 1];
-    double ra[NS > 0 ? NS : 1][MODE == CG_MODE_IP1 ? 3 : 1];
+    double ra[NS > 0 ? NS : 1][CG_IS_IP(MODE) ? 3 : 1];
     auto comp_offsets3 = [&](int c, int &ox, int &oy, int &oz) {
         int ic = c % nfi, rest = c / nfi;
         int kc = rest % nfk; rest /= nfk;
@@ -185,7 +185,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             int c = lane + 32 * s;
             offs[s] = c < L.nf ? comp_offsets(c) : 0;
 #pragma unroll
-            for (int q = 0; q < (MODE == CG_MODE_IP1 ? 3 : 1); q++) ra[s][q] = 0.0;
+            for (int q = 0; q < (CG_IS_IP(MODE) ? 3 : 1); q++) ra[s][q] = 0.0;
         }
     } else {
         for (int c = lane; c < L.nf * L.ncomp; c += 32) acc[c] = 0.0;
@@ -203,8 +203,8 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             const CGPrimPair A = ppij[ij];
             const CGPrimPair B = ppkl[kl];
             double *rec = term + lane * CG_TERMW;
-            cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec);
-            rec[10] = -2.0 * A.aA;
+            cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec, P.omega2);
+            rec[10] = -2.0 * (MODE == CG_MODE_IP2 ? B.aA : A.aA);   /* -2 a of the nabla shell */
         }
         __syncwarp();
         /* ---- stage 2: one lane per (term, axis) */
@@ -214,7 +214,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             double g00 = (ax == 2) ? rec[9] : 1.0;
             double *gdst = greg + (size_t)(t * 3 + ax) * L.gax;
             g_axis(L, rec[0], rec[1], rec[2], rec[3 + ax], rec[6 + ax], g00,
-                   pij.AB[ax], pkl.AB[ax], scr_base + lane * L.scr, gdst);
+                   pij.AB[ax], pkl.AB[ax], scr_base + lane * L.scr, gdst, (tk.sym >> 3) & 3);
             if (MODE == CG_MODE_IP1) {
                 /* f(i) = i g(i-1) - 2 a_i g(i+1)   (CINTnabla1i_2e, src/g2e.c:4550-4591) */
                 const double ai2 = rec[10];
@@ -226,6 +226,21 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                         if (i > 0) v = fma((double)i, gdst[(i - 1) * sI + o], v);
                         f[i * sI + o] = v;
                     }
+                }
+            } else if (MODE == CG_MODE_IP2) {
+                /* f(k) = k g(k-1) - 2 a_k g(k+1) along k (CINTnabla1k_2e, src/g2e.c:4651-4701) */
+                const double ak2 = rec[10];
+                const int dK = L.dK, dL = L.dL, nij = L.dI * L.dJ;
+                double *f = gdst + L.G;
+                for (int ij = 0; ij < nij; ij++) {
+                    const double *g0 = gdst + ij * dK * dL;
+                    double *f0 = f + ij * dK * dL;
+                    for (int k = 0; k < dK - 1; k++)
+                        for (int l = 0; l < dL; l++) {
+                            double v = ak2 * g0[(k + 1) * dL + l];
+                            if (k > 0) v = fma((double)k, g0[(k - 1) * dL + l], v);
+                            f0[k * dL + l] = v;
+                        }
                 }
             }
         }
@@ -239,9 +254,9 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                 if (lane + 32 * s >= L.nf) continue;
                 const int ox = offs[s] & 1023, oy = (offs[s] >> 10) & 1023, oz = offs[s] >> 20;
                 const double *gb = greg;
-                if (MODE == CG_MODE_IP1) {
-                    double sx = ra[s][0], sy = ra[s][MODE == CG_MODE_IP1 ? 1 : 0],
-                           sz = ra[s][MODE == CG_MODE_IP1 ? 2 : 0];
+                if (CG_IS_IP(MODE)) {
+                    double sx = ra[s][0], sy = ra[s][CG_IS_IP(MODE) ? 1 : 0],
+                           sz = ra[s][CG_IS_IP(MODE) ? 2 : 0];
                     for (int t = 0; t < Tb; t++, gb += stride_t) {
                         double gx = gb[ox], gy = gb[A + oy], gz = gb[2 * A + oz];
                         double fx = gb[G + ox], fy = gb[A + G + oy], fz = gb[2 * A + G + oz];
@@ -250,8 +265,8 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                         sz = fma(fz, gx * gy, sz);
                     }
                     ra[s][0] = sx;
-                    ra[s][MODE == CG_MODE_IP1 ? 1 : 0] = sy;
-                    ra[s][MODE == CG_MODE_IP1 ? 2 : 0] = sz;
+                    ra[s][CG_IS_IP(MODE) ? 1 : 0] = sy;
+                    ra[s][CG_IS_IP(MODE) ? 2 : 0] = sz;
                 } else {
                     double s0 = ra[s][0];
                     for (int t = 0; t < Tb; t++, gb += stride_t)
@@ -264,7 +279,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                 int ox, oy, oz;
                 comp_offsets3(c, ox, oy, oz);
                 const double *gb = greg;
-                if (MODE == CG_MODE_IP1) {
+                if (CG_IS_IP(MODE)) {
                     double sx = acc[c], sy = acc[L.nf + c], sz = acc[2 * L.nf + c];
                     for (int t = 0; t < Tb; t++, gb += stride_t) {
                         double gx = gb[ox], gy = gb[A + oy], gz = gb[2 * A + oz];
@@ -290,7 +305,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             int c = lane + 32 * s;
             if (c < L.nf) {
 #pragma unroll
-                for (int q = 0; q < (MODE == CG_MODE_IP1 ? 3 : 1); q++) acc[q * L.nf + c] = ra[s][q];
+                for (int q = 0; q < (CG_IS_IP(MODE) ? 3 : 1); q++) acc[q * L.nf + c] = ra[s][q];
             }
         }
     }
@@ -390,7 +405,7 @@ __device__ inline void cg_out_quartet(const CGOutTask &o, bool ne, bool peer_slo
         if (e0f0)
             cur = cg_hrr(g0, eperm + ec.perm_off, eperm + ec.perm_off + ec.nE,
                          hprog + ec.hprog_off, o.l[0], o.l[1], o.l[2], o.l[3], o.AB, o.CD,
-                         h1, h2, lane);
+                         h1, h2, lane, ec.bra);
         c2s_pass(cur, s1, o.l[1], sph, nfc[0] * nfc[2] * nfc[3], nfc[1], 1, lane);
         __syncwarp();
         /* pass l: (i,k | l | js) */
@@ -455,7 +470,8 @@ __device__ __forceinline__ void e0f0_dispatch(int mab, const double *greg, int g
 
 /* One int2e / int3c2e / J task, contraction first: per term the VRR arrays only; stage 3
  * accumulates (e0|f0) of the task's slice; the horizontal transfer runs in the output kernel
- * (once per contracted quartet) or, for J, at the end of the task. */
+ * (once per contracted quartet) or, for J, at the end of the task.  Classes with ec.bra (layout
+ * CG_MODE_ERIB) transfer the bra per term in stage 2 and accumulate (ij|f0) instead. */
 __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &tk, const CGLayout &L,
                                               double *term, double *greg, int lane)
 {
@@ -466,10 +482,12 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
     const int *__restrict__ pql = P.pqlist + tk.pq_off;
     const int nij = pij.npa * pij.npb;
     const int li = pij.la, lj = pij.lb, lk = pkl.la, ll = pkl.lb;
-    const int n = L.nroots, T = L.T, G = L.gax, gstride = L.gstride, na = L.nmax + 1;   /* G: axis stride */
+    const CGEriClass ec = P.eclass[tk.cls];
+    /* G: axis stride; na: stride between the f members of a group (f's step in the axis array) */
+    const int n = L.nroots, T = L.T, G = L.gax, gstride = L.gstride;
+    const int na = ec.bra ? L.dI * L.dJ : L.nmax + 1;
     const double common = P.common_base * common_fac_sp(li) * (P.two ? 1.0 : common_fac_sp(lj))
                         * common_fac_sp(lk) * (P.three ? 1.0 : common_fac_sp(ll));
-    const CGEriClass ec = P.eclass[tk.cls];
     const CGEriGroup *__restrict__ grp = P.egroup + ec.group_off;
     const int nF = ec.nF, nEF = ec.nE * ec.nF;
     double *wbase = P.jmode ? P.wscratch + (size_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * P.wscratch_stride
@@ -507,18 +525,23 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
             int q = __ldg(pql + p);
             int kl = q / nij, ij = q - kl * nij;
             double *rec = term + lane * L.termw;
-            cg_term(ppij[ij], ppkl[kl], pij, pkl, n, rr, common, P.rys_coef, rec);
+            cg_term(ppij[ij], ppkl[kl], pij, pkl, n, rr, common, P.rys_coef, rec, P.omega2);
             double mb = 0.0;
             for (int m = 0; m <= L.mmax; m++) { rec[10 + m] = mb; mb += rec[2]; }   /* m b01 */
         }
         __syncwarp();
-        /* ---- stage 2: one lane per (term, axis), VRR only */
+        /* ---- stage 2: one lane per (term, axis), VRR only (bra classes: and the bra transfer) */
         for (int item = lane; item < 3 * Tb; item += 32) {
             int t = item / 3, ax = item - 3 * t;
             const double *rec = term + t * L.termw;
             double g00 = (ax == 2) ? rec[9] : 1.0;
-            vrr_axis(L.nmax, L.mmax, rec[0], rec[1], rec + 10, rec[3 + ax], rec[6 + ax], g00,
-                     greg + (size_t)t * gstride + ax * G);
+            if (ec.bra)
+                vrr_bra_axis(L.nmax, L.mmax, L.dI, L.dJ, rec[0], rec[1], rec + 10, rec[3 + ax],
+                             rec[6 + ax], g00, pij.AB[ax], greg + (size_t)T * gstride + lane * L.scr,
+                             greg + (size_t)t * gstride + ax * G);
+            else
+                vrr_axis(L.nmax, L.mmax, rec[0], rec[1], rec + 10, rec[3 + ax], rec[6 + ax], g00,
+                         greg + (size_t)t * gstride + ax * G);
         }
         __syncwarp();
         /* ---- stage 3: groups */
@@ -582,7 +605,7 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
         /* J contraction of this slice's transferred block */
         const double *cart = cg_hrr(acc, P.eperm + ec.perm_off, P.eperm + ec.perm_off + ec.nE,
                                     P.hprog + ec.hprog_off, li, lj, lk, ll, pij.AB, pkl.AB,
-                                    wbase + P.hrr_off1, wbase + P.hrr_off2, lane);
+                                    wbase + P.hrr_off1, wbase + P.hrr_off2, lane, ec.bra);
         cg_j_contract(P, tk, pij, pkl, cart, lane);
     } else if (lane == 0) {
         P.nonempty[tk.out] = 1;
@@ -607,7 +630,8 @@ __device__ __forceinline__ void rys_eri_body(const CGLaunch &P)
         const int la = P.pairs[tk.pij].la, lb = P.pairs[tk.pij].lb;
         const int lc = P.pairs[tk.pkl].la, ld = P.pairs[tk.pkl].lb;
         CGLayout L;
-        cg_class_layout(la, lb, lc, ld, MODE, P.ws_doubles, &L);
+        const int lmode = (MODE == CG_MODE_ERI && P.eclass[tk.cls].bra) ? CG_MODE_ERIB : MODE;
+        cg_class_layout(la, lb, lc, ld, lmode, P.ws_doubles, &L);
         const int ns = (L.nf + 31) >> 5;
         if (L.T < 1) {
             if (lane == 0) atomicOr(P.status, 1);
@@ -644,12 +668,14 @@ __device__ __forceinline__ void rys_eri_body(const CGLaunch &P)
  * keep every value in registers instead of spilling */
 __global__ void __launch_bounds__(128) rys_eri_kernel_e0f0(CGLaunch P) { rys_eri_body<CG_MODE_ERI>(P); }
 __global__ void __launch_bounds__(128, 2) rys_eri_kernel_ip1(CGLaunch P) { rys_eri_body<CG_MODE_IP1>(P); }
+__global__ void __launch_bounds__(128, 2) rys_eri_kernel_ip2(CGLaunch P) { rys_eri_body<CG_MODE_IP2>(P); }
 __global__ void __launch_bounds__(128, 2) rys_eri_kernel_prim(CGLaunch P) { rys_eri_body<CG_MODE_ERIP>(P); }
 
 static void *eri_kernel_of(int mode)
 {
     return mode == CG_MODE_ERI ? (void *)rys_eri_kernel_e0f0
-         : mode == CG_MODE_IP1 ? (void *)rys_eri_kernel_ip1 : (void *)rys_eri_kernel_prim;
+         : mode == CG_MODE_IP1 ? (void *)rys_eri_kernel_ip1
+         : mode == CG_MODE_IP2 ? (void *)rys_eri_kernel_ip2 : (void *)rys_eri_kernel_prim;
 }
 
 /* ------------------------------------------------------------------ output kernel */
@@ -685,7 +711,7 @@ extern "C" int cg_kernels_init(const int *c2s_nnz, const int *c2s_idx, const dou
     double *d = nullptr;
     if ((e = cudaGetSymbolAddress((void **)&d, g_rys_coef)) != cudaSuccess) return (int)e;
     *rys_coef_dev = d;
-    for (int mode : {CG_MODE_ERI, CG_MODE_IP1, CG_MODE_ERIP}) {
+    for (int mode : {CG_MODE_ERI, CG_MODE_IP1, CG_MODE_IP2, CG_MODE_ERIP}) {
         e = cudaFuncSetAttribute(eri_kernel_of(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 8 * CG_WS_MAX);
         if (e != cudaSuccess) return (int)e;
     }
@@ -715,6 +741,8 @@ extern "C" int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStrea
         rys_eri_kernel_e0f0<<<nblocks, 128, smem, stream>>>(*P);
     else if (mode == CG_MODE_IP1)
         rys_eri_kernel_ip1<<<nblocks, 128, smem, stream>>>(*P);
+    else if (mode == CG_MODE_IP2)
+        rys_eri_kernel_ip2<<<nblocks, 128, smem, stream>>>(*P);
     else
         rys_eri_kernel_prim<<<nblocks, 128, smem, stream>>>(*P);
     return (int)cudaGetLastError();

@@ -6,17 +6,22 @@
 #include "cintgpu_types.h"
 
 #define CG_MODE_ERI 0
-#define CG_MODE_IP1 1
+#define CG_MODE_IP1 1                /* one nabla on kernel slot 0 (i): int2e_ip1, int3c2e_ip1 */
 #define CG_MODE_GRAD 2               /* adjoint, nuclear-coordinate gradient */
 #define CG_MODE_GRADA 3              /* adjoint, coordinates and primitive exponents */
-#define CG_MODE_ERIP 4               /* int2e classes evaluated per primitive (transfer before
-                                        contraction, libcint's order): lj or ll >= 4 */
+#define CG_MODE_ERIP 4               /* int2e classes evaluated per primitive (both transfers
+                                        before contraction, libcint's order): ll >= 3 */
+#define CG_MODE_IP2 6                /* one nabla on kernel slot 2 (k): int2e_ip2, int3c2e_ip2 */
+#define CG_MODE_ERIB 5               /* int2e / int3c2e classes with lj >= 3 and ll <= 2: the bra
+                                        transfer per term (libcint's order on the bra), the ket
+                                        transfer after contraction */
 #define CG_TERMW 12                  /* doubles per term record in shared memory */
 #define CG_TERMW_GRAD 20             /* term record of the adjoint kernel */
 #define CG_GRAD_MAXPRIM 16           /* primitives per shell supported by the exponent adjoint */
 #define CG_WS_SMALL (24 * 1024 / 8)  /* doubles of shared memory per warp, default */
 #define CG_WS_MAX (48 * 1024 / 8)    /* doubles of shared memory per warp, large classes */
 #define CG_C2S_MAXNNZ 16
+#define CG_IS_IP(m) ((m) == CG_MODE_IP1 || (m) == CG_MODE_IP2)
 
 typedef struct {
     int lic, nroots, nmax, mmax;
@@ -42,6 +47,7 @@ typedef struct {
     int *status;
     const double *rys_coef;
     double common_base;       /* 2 pi^3 / sqrt(pi); times the s/p factors per task */
+    double omega2;            /* omega^2 of the long-range Coulomb erf(omega r)/r; 0: 1/r */
     int three;                /* int3c2e, int2c2e: the fourth shell is the unit s partner */
     int two;                  /* int2c2e: the second shell is a unit s partner as well */
     int ws_doubles;
@@ -82,6 +88,7 @@ typedef struct {
     int *status;
     const double *rys_coef;
     double common_base;
+    double omega2;            /* omega^2 of the long-range Coulomb; 0: 1/r */
     int ws_doubles;
     const double *dm;         /* Cartesian density, nao x nao */
     int nao;

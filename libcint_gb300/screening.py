@@ -45,11 +45,13 @@ def schwarz_from_diagonal(nbas, pairs, diag, cnt):
     return Q
 
 
-def schwarz_bounds(mol):
-    """Q_ij for every shell pair, from one int2e_sph plan over the diagonal quartets (GPU)."""
+def pair_bounds(mol, pairs):
+    """Q for the given shell pairs (rows (i, j)): sqrt(max |(ab|ab)|) over the pair's functions,
+    from one int2e_sph plan over the diagonal quartets (i, j, i, j) on the GPU."""
     import torch
     from . import INT2E_SPH, Plan
-    pairs, items = diagonal_pairs(mol.nbas)
+    pairs = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
+    items = np.concatenate([pairs, pairs], 1).astype(np.int32)
     plan = Plan(INT2E_SPH, mol, items)
     out = torch.empty(plan.output_size, dtype=torch.float64, device='cuda')
     plan.execute(out)
@@ -58,7 +60,19 @@ def schwarz_bounds(mol):
         raise ValueError('diagonal positions outside the plan output')
     diag = out[torch.as_tensor(pos, device=out.device)].cpu().numpy()
     plan.close()
-    return schwarz_from_diagonal(mol.nbas, pairs, diag, cnt)
+    seg = np.concatenate([[0], np.cumsum(cnt)[:-1]])
+    return np.maximum.reduceat(np.sqrt(np.abs(diag)), seg) if len(diag) else np.zeros(0)
+
+
+def schwarz_bounds(mol):
+    """Q_ij for every shell pair (nbas x nbas, symmetric), from one int2e_sph plan over the
+    diagonal quartets (GPU)."""
+    pairs, _ = diagonal_pairs(mol.nbas)
+    m = pair_bounds(mol, pairs)
+    Q = np.zeros((mol.nbas, mol.nbas))
+    Q[pairs[:, 0], pairs[:, 1]] = m
+    Q[pairs[:, 1], pairs[:, 0]] = m
+    return Q
 
 
 def shell_density_max(mol, dm):

@@ -242,8 +242,10 @@ typedef struct {
     double dummy_exp, dummy_cf;
     double common;
     double expcutoff;
+    double omega;      /* env[PTR_RANGE_OMEGA]: > 0 long-range erf(omega r)/r Coulomb */
     int three_center;  /* 0 int2e, 1 int3c2e, 2 int2c2e */
-    int deriv_i;       /* 1 for ip1 */
+    int deriv_i;       /* 1 for a nabla on one shell (ip1: i, ip2: k) */
+    int dslot;         /* the nabla's shell slot: 0 (i) or 2 (k) */
     int nroots;
 } OEnv;
 
@@ -269,10 +271,12 @@ static void load_shell(OEnv *E, int slot, int sh, int *atm, int *bas, double *en
 /* CINTinit_int2e_EnvVars (src/g2e.c:21-172) / CINTinit_int3c2e_EnvVars (src/g3c2e.c:21-132) /
  * CINTinit_int2c2e_EnvVars (src/g2c2e.c:16-56): int2c2e's (i|k) is (i s0|k s0) with two dummy
  * zero-exponent unit s shells, the common factor of i and k only and no +1 on the cutoff */
-static void init_env(OEnv *E, int *shls, int *atm, int *bas, double *env, int three, int dinc)
+static void init_env(OEnv *E, int *shls, int *atm, int *bas, double *env, int three, int dinc,
+                     int dslot)
 {
     memset(E, 0, sizeof(*E));
     E->three_center = three;
+    E->omega = env[PTR_RANGE_OMEGA];
     if (three == 2) {
         load_shell(E, 0, shls[0], atm, bas, env);
         load_shell(E, 2, shls[1], atm, bas, env);
@@ -312,8 +316,9 @@ static void init_env(OEnv *E, int *shls, int *atm, int *bas, double *env, int th
         E->expcutoff = env[PTR_EXPCUTOFF] == 0 ? 60 : fmax(40, env[PTR_EXPCUTOFF]) + 1;
     }
     E->deriv_i = dinc;
+    E->dslot = dslot;
     for (int s = 0; s < 4; s++) E->lc[s] = E->l[s];
-    E->lc[0] += dinc;
+    E->lc[dslot] += dinc;   /* libcint's ng IINC / KINC (src/autocode/grad2.c, int3c2e.c) */
     E->nroots = (E->lc[0] + E->lc[1] + E->lc[2] + E->lc[3]) / 2 + 1;
 }
 
@@ -342,7 +347,18 @@ static int g0_2e(const OEnv *E, GArr *G, const double *P, const double *Q,
     double a0 = a1 / (aij + akl);
     double fac1 = sqrt(a0 / (a1 * a1 * a1)) * fac;
     double x = a0 * rr;
+    double theta = 1;
+    if (E->omega > 0) {
+        /* long-range Coulomb erf(omega r)/r (src/g2e.c:4477-4492): the Rys quadrature of
+         * x' = theta x with theta = omega^2/(omega^2 + a0), weights times sqrt(theta), and every
+         * node mapped to t^2 -> theta t^2, i.e. u -> theta u / (1 + u - theta u) */
+        theta = E->omega * E->omega / (E->omega * E->omega + a0);
+        x *= theta;
+        fac1 *= sqrt(theta);
+    }
     if (oracle_rys_roots(n, x, u, w)) return -1;
+    if (E->omega > 0)
+        for (int r = 0; r < n; r++) u[r] = theta * u[r] / (1 + u[r] - theta * u[r]);
     const int nmax = E->lc[0] + E->lc[1];
     const int mmax = E->lc[2] + E->lc[3];
     /* 2D table per root and coordinate: T[n][m] */
@@ -435,14 +451,26 @@ static void gout(const OEnv *E, const GArr *G, double ai, double *out, int ncomp
             double gz = pz[r * rs];
             if (ncomp == 1) {
                 s0 += gx * gy * gz;
-            } else {
-                /* f(i) = i g(i-1) - 2 a_i g(i+1) */
+            } else if (E->dslot == 0) {
+                /* f(i) = i g(i-1) - 2 a_i g(i+1)   (CINTnabla1i_2e, src/g2e.c:4550-4591) */
                 double fx = -2 * ai * G->g[GIDX(G, 0, r, ix + 1, nx[1][j], nx[2][k], nx[3][l])];
                 double fy = -2 * ai * G->g[GIDX(G, 1, r, iy + 1, ny[1][j], ny[2][k], ny[3][l])];
                 double fz = -2 * ai * G->g[GIDX(G, 2, r, iz + 1, nz[1][j], nz[2][k], nz[3][l])];
                 if (ix) fx += ix * G->g[GIDX(G, 0, r, ix - 1, nx[1][j], nx[2][k], nx[3][l])];
                 if (iy) fy += iy * G->g[GIDX(G, 1, r, iy - 1, ny[1][j], ny[2][k], ny[3][l])];
                 if (iz) fz += iz * G->g[GIDX(G, 2, r, iz - 1, nz[1][j], nz[2][k], nz[3][l])];
+                sx += fx * gy * gz;
+                sy += gx * fy * gz;
+                sz += gx * gy * fz;
+            } else {
+                /* f(k) = k g(k-1) - 2 a_k g(k+1)   (CINTnabla1k_2e, src/g2e.c:4651-4701) */
+                const int kx = nx[2][k], ky = ny[2][k], kz = nz[2][k];
+                double fx = -2 * ai * G->g[GIDX(G, 0, r, ix, nx[1][j], kx + 1, nx[3][l])];
+                double fy = -2 * ai * G->g[GIDX(G, 1, r, iy, ny[1][j], ky + 1, ny[3][l])];
+                double fz = -2 * ai * G->g[GIDX(G, 2, r, iz, nz[1][j], kz + 1, nz[3][l])];
+                if (kx) fx += kx * G->g[GIDX(G, 0, r, ix, nx[1][j], kx - 1, nx[3][l])];
+                if (ky) fy += ky * G->g[GIDX(G, 1, r, iy, ny[1][j], ky - 1, ny[3][l])];
+                if (kz) fz += kz * G->g[GIDX(G, 2, r, iz, nz[1][j], kz - 1, nz[3][l])];
                 sx += fx * gy * gz;
                 sy += gx * fy * gz;
                 sz += gx * gy * fz;
@@ -557,7 +585,7 @@ static int contracted(const OEnv *E, double *gctr, int ncomp)
             double aij = E->ex[0][ip] + E->ex[1][jp];
             double fac = E->common * pd->e * ekl;
             if (g0_2e(E, &G, pd->r, Q, aij, akl, fac)) { empty = 1; goto done; }
-            gout(E, &G, E->ex[0][ip], gp, ncomp);
+            gout(E, &G, E->dslot == 2 ? ak : E->ex[0][ip], gp, ncomp);
             empty = 0;
             /* prim -> contracted for every contraction pattern (src/g1e.c:530-559) */
             for (int lc_ = 0; lc_ < E->nctr[3]; lc_++)
@@ -647,10 +675,11 @@ static void write_out(const OEnv *E, const double *gctr, double *out, int *dims,
 }
 
 static int driver(double *out, int *dims, int *shls, int *atm, int *bas, double *env,
-                  int three, int dinc, int sph)
+                  int three, int dinc, int sph, int dslot)
 {
     OEnv E;
-    init_env(&E, shls, atm, bas, env, three, dinc);
+    init_env(&E, shls, atm, bas, env, three, dinc, dslot);
+    if (E.omega < 0) return -1;   /* short-range Coulomb is not restated */
     int ncomp = dinc ? 3 : 1;
     int nf = ncart(E.l[0]) * ncart(E.l[1]) * ncart(E.l[2]) * ncart(E.l[3]);
     int nc = E.nctr[0] * E.nctr[1] * E.nctr[2] * E.nctr[3];
@@ -667,28 +696,47 @@ static int driver(double *out, int *dims, int *shls, int *atm, int *bas, double 
 
 int oracle_int2e_sph(double *out, int *dims, int *shls, int *atm, int natm,
                      int *bas, int nbas, double *env, void *opt, double *cache)
-{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 0, 1); }
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 0, 1, 0); }
 int oracle_int2e_cart(double *out, int *dims, int *shls, int *atm, int natm,
                       int *bas, int nbas, double *env, void *opt, double *cache)
-{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 0, 0); }
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 0, 0, 0); }
 int oracle_int2e_ip1_sph(double *out, int *dims, int *shls, int *atm, int natm,
                          int *bas, int nbas, double *env, void *opt, double *cache)
-{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 1, 1); }
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 1, 1, 0); }
 int oracle_int2e_ip1_cart(double *out, int *dims, int *shls, int *atm, int natm,
                           int *bas, int nbas, double *env, void *opt, double *cache)
-{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 1, 0); }
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 1, 0, 0); }
 int oracle_int3c2e_sph(double *out, int *dims, int *shls, int *atm, int natm,
                        int *bas, int nbas, double *env, void *opt, double *cache)
-{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 1, 0, 1); }
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 1, 0, 1, 0); }
 int oracle_int3c2e_cart(double *out, int *dims, int *shls, int *atm, int natm,
                         int *bas, int nbas, double *env, void *opt, double *cache)
-{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 1, 0, 0); }
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 1, 0, 0, 0); }
 int oracle_int2c2e_sph(double *out, int *dims, int *shls, int *atm, int natm,
                        int *bas, int nbas, double *env, void *opt, double *cache)
-{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 2, 0, 1); }
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 2, 0, 1, 0); }
 int oracle_int2c2e_cart(double *out, int *dims, int *shls, int *atm, int natm,
                         int *bas, int nbas, double *env, void *opt, double *cache)
-{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 2, 0, 0); }
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 2, 0, 0, 0); }
+
+int oracle_int2e_ip2_sph(double *out, int *dims, int *shls, int *atm, int natm,
+                         int *bas, int nbas, double *env, void *opt, double *cache)
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 1, 1, 2); }
+int oracle_int2e_ip2_cart(double *out, int *dims, int *shls, int *atm, int natm,
+                          int *bas, int nbas, double *env, void *opt, double *cache)
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 1, 0, 2); }
+int oracle_int3c2e_ip1_sph(double *out, int *dims, int *shls, int *atm, int natm,
+                           int *bas, int nbas, double *env, void *opt, double *cache)
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 1, 1, 1, 0); }
+int oracle_int3c2e_ip1_cart(double *out, int *dims, int *shls, int *atm, int natm,
+                            int *bas, int nbas, double *env, void *opt, double *cache)
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 1, 1, 0, 0); }
+int oracle_int3c2e_ip2_sph(double *out, int *dims, int *shls, int *atm, int natm,
+                           int *bas, int nbas, double *env, void *opt, double *cache)
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 1, 1, 1, 2); }
+int oracle_int3c2e_ip2_cart(double *out, int *dims, int *shls, int *atm, int natm,
+                            int *bas, int nbas, double *env, void *opt, double *cache)
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 1, 1, 0, 2); }
 
 double oracle_int2e_sph_list(const int *quartets, long nq, double *out, const long *offsets,
                              int *atm, int natm, int *bas, int nbas, double *env, int nthreads)
@@ -719,6 +767,40 @@ double oracle_int2e_sph_list(const int *quartets, long nq, double *out, const lo
         }
         free(scratch);
     }
+#ifdef _OPENMP
+    t1 = omp_get_wtime();
+#endif
+    return t1 - t0;
+}
+
+/* Evaluate n items of one kind (which: 0 int2e_sph, 1 int2e_cart, 2 int2e_ip1_sph, 3 int2e_ip1_cart,
+ * 4 int3c2e_sph, 5 int3c2e_cart, 6 int2c2e_sph, 7 int2c2e_cart; 4, 3 or 2 shell indices per item)
+ * with OpenMP over items; item q writes its dense block (all components) at out + offsets[q].
+ * Returns wall seconds, or -1 for an unknown kind. */
+double oracle_list(int which, const int *items, long n, double *out, const long *offsets,
+                   int *atm, int natm, int *bas, int nbas, double *env, int nthreads)
+{
+    typedef int (*fn_t)(double *, int *, int *, int *, int, int *, int, double *, void *, double *);
+    static const fn_t fns[14] = {oracle_int2e_sph, oracle_int2e_cart, oracle_int2e_ip1_sph,
+                                 oracle_int2e_ip1_cart, oracle_int3c2e_sph, oracle_int3c2e_cart,
+                                 oracle_int2c2e_sph, oracle_int2c2e_cart, oracle_int2e_ip2_sph,
+                                 oracle_int2e_ip2_cart, oracle_int3c2e_ip1_sph,
+                                 oracle_int3c2e_ip1_cart, oracle_int3c2e_ip2_sph,
+                                 oracle_int3c2e_ip2_cart};
+    static const int nshs[14] = {4, 4, 4, 4, 3, 3, 2, 2, 4, 4, 3, 3, 3, 3};
+    if (which < 0 || which > 13) return -1;
+    const int nsh = nshs[which];
+    double t0 = 0, t1 = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    t0 = omp_get_wtime();
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long q = 0; q < n; q++)
+        fns[which](out + offsets[q], NULL, (int *)(items + (long)nsh * q), atm, natm, bas, nbas, env,
+                   NULL, NULL);
 #ifdef _OPENMP
     t1 = omp_get_wtime();
 #endif

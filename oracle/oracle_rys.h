@@ -37,6 +37,20 @@ int oracle_int3c2e_sph(double *out, int *dims, int *shls, int *atm, int natm,
                        int *bas, int nbas, double *env, void *opt, double *cache);
 int oracle_int3c2e_cart(double *out, int *dims, int *shls, int *atm, int natm,
                         int *bas, int nbas, double *env, void *opt, double *cache);
+/* (ij|nabla k l), (nabla i j|k), (ij|nabla k): libcint src/autocode/grad2.c:163-176,
+ * src/autocode/int3c2e.c:72-87, :153-168 */
+int oracle_int2e_ip2_sph(double *out, int *dims, int *shls, int *atm, int natm,
+                         int *bas, int nbas, double *env, void *opt, double *cache);
+int oracle_int2e_ip2_cart(double *out, int *dims, int *shls, int *atm, int natm,
+                          int *bas, int nbas, double *env, void *opt, double *cache);
+int oracle_int3c2e_ip1_sph(double *out, int *dims, int *shls, int *atm, int natm,
+                           int *bas, int nbas, double *env, void *opt, double *cache);
+int oracle_int3c2e_ip1_cart(double *out, int *dims, int *shls, int *atm, int natm,
+                            int *bas, int nbas, double *env, void *opt, double *cache);
+int oracle_int3c2e_ip2_sph(double *out, int *dims, int *shls, int *atm, int natm,
+                           int *bas, int nbas, double *env, void *opt, double *cache);
+int oracle_int3c2e_ip2_cart(double *out, int *dims, int *shls, int *atm, int natm,
+                            int *bas, int nbas, double *env, void *opt, double *cache);
 int oracle_int2c2e_sph(double *out, int *dims, int *shls, int *atm, int natm,
                        int *bas, int nbas, double *env, void *opt, double *cache);
 int oracle_int2c2e_cart(double *out, int *dims, int *shls, int *atm, int natm,
@@ -53,6 +67,14 @@ int oracle_cart2sph_coeff(int l, double *c);
  * seconds.  nthreads <= 0 uses the OpenMP default. */
 double oracle_int2e_sph_list(const int *quartets, long nq, double *out, const long *offsets,
                              int *atm, int natm, int *bas, int nbas, double *env, int nthreads);
+
+/* Any kind over a list of items (which: 0 int2e_sph, 1 int2e_cart, 2 int2e_ip1_sph,
+ * 3 int2e_ip1_cart, 4 int3c2e_sph, 5 int3c2e_cart, 6 int2c2e_sph, 7 int2c2e_cart, 8 int2e_ip2_sph,
+ * 9 int2e_ip2_cart, 10 int3c2e_ip1_sph, 11 int3c2e_ip1_cart, 12 int3c2e_ip2_sph,
+ * 13 int3c2e_ip2_cart), OpenMP over
+ * items, dense blocks (all components) at out + offsets[q].  Returns wall seconds. */
+double oracle_list(int which, const int *items, long n, double *out, const long *offsets,
+                   int *atm, int natm, int *bas, int nbas, double *env, int nthreads);
 
 #ifdef __cplusplus
 }

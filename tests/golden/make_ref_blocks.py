@@ -15,6 +15,18 @@ Contents (all through libcint 6.1.1 built by oracle/Makefile, opt = NULL, cache 
   hl_int2e_sph / hl_int2e_cart / hl_int3c2e_sph / hl_int2e_ip1_sph
                                      small blocks of the l = 6 / 5 / 4 / 2 / 0 basis of
                                      tests/test_gpu_high_l.py (i, h with two columns, g, d, s)
+  c1_int2e_sph / c1_int2e_cart       the first 2 quartets of every kernel-order class of the
+                                     benchmark list (tests/golden/c1_quartets.npz; 110 quartets)
+  c4_int2e_sph / _cart / _ip1_sph    one quartet per kernel-order class (l <= 4, g shells, 1-8
+                                     primitives) of molecules.config4(seed=2, natm=4, box=5.2), and
+                                     (*_liberr) libcint's largest error per quartet against the
+                                     long-double build of the restatement
+  c3_int2e_sph / c3_int2e_ip1_sph    40 unique quartets of molecules.config3(seed=0)
+  c0_int2e_ip2_sph / _cart           40 of the c0 quartets above, (ij|nabla k l)
+  c2_int3c2e_ip1_sph / _cart, c2_int3c2e_ip2_sph / _cart    the 60 c2 triples above
+  lr_c0_int2e_sph / lr_c0_int2e_ip1_sph / lr_c2_int3c2e_sph / lr_c2_int2c2e_sph
+                                     long-range Coulomb erf(omega r)/r (env[PTR_RANGE_OMEGA] =
+                                     0.3 for c0(3), 0.5 for the c2 molecule): 30 / 30 / 40 / 40 items
   cache_sizes                        the out == NULL cache-size answers for a few items
 Each block is stored flattened in libcint's (Fortran) order with its item list.
 """
@@ -39,6 +51,19 @@ HL_ITEMS = {
     'int3c2e_sph': [(3, 4, 0), (0, 3, 2), (1, 4, 2), (0, 0, 4)],
     'int2e_ip1_sph': [(1, 2, 3, 4), (0, 3, 4, 4), (2, 0, 3, 4)],
 }
+
+
+def c4_class_quartets(mol, seed=5):
+    """One unique quartet per kernel-order class (li >= lj, lk >= ll, (li lj) >= (lk ll)) of mol,
+    drawn with a fixed seed; the list every g-shell test uses."""
+    from tests import c1_sample
+    qs = M.unique_quartets(mol.nbas)
+    rng = np.random.RandomState(seed)
+    qs = qs[rng.permutation(len(qs))]
+    k = c1_sample.kernel_class(mol, qs)
+    key = ((k[:, 0] * 8 + k[:, 1]) * 8 + k[:, 2]) * 8 + k[:, 3]
+    _, first = np.unique(key, return_index=True)
+    return np.ascontiguousarray(qs[np.sort(first)], dtype=np.int32)
 
 
 def main():
@@ -85,6 +110,50 @@ def main():
         it = np.array(items, dtype=np.int32)
         out['hl_' + name + '_items'] = it
         out['hl_' + name] = np.concatenate([o.ref.call(name, hl, t)[1].ravel(order='F') for t in it])
+    # the benchmark workload's classes (2 quartets of each, list order)
+    from tests import c1_sample
+    mol1 = M.config1(seed=0)
+    q1, _ = c1_sample.stratified(mol1, c1_sample.c1_quartets(), 2)
+    for name in ('int2e_sph', 'int2e_cart'):
+        out['c1_' + name + '_items'] = q1
+        out['c1_' + name] = np.concatenate([o.ref.call(name, mol1, q)[1].ravel(order='F') for q in q1])
+    # g shells: one quartet per kernel-order class of a small c4-type molecule
+    mol4 = M.config4(seed=2, natm=4, box=5.2)
+    q4 = c4_class_quartets(mol4)
+    for name in ('int2e_sph', 'int2e_cart', 'int2e_ip1_sph'):
+        out['c4_' + name + '_items'] = q4
+        out['c4_' + name] = np.concatenate([o.ref.call(name, mol4, q)[1].ravel(order='F') for q in q4])
+        # libcint's own error per quartet against the long-double restatement (the referee)
+        rf, offs = o.referee(name, mol4, q4)
+        d = np.abs(out['c4_' + name] - rf)
+        out['c4_' + name + '_liberr'] = np.array([d[offs[q]:offs[q + 1]].max() for q in range(len(q4))])
+    mol3 = M.config3(seed=0)
+    q3 = M.unique_quartets(mol3.nbas)
+    q3 = q3[np.random.RandomState(3).choice(len(q3), 40, replace=False)].astype(np.int32)
+    for name in ('int2e_sph', 'int2e_ip1_sph'):
+        out['c3_' + name + '_items'] = q3
+        out['c3_' + name] = np.concatenate([o.ref.call(name, mol3, q)[1].ravel(order='F') for q in q3])
+    # derivative family: (ij|nabla k l) on c0, (nabla i j|k) and (ij|nabla k) on the c2 molecule
+    for name in ('int2e_ip2_sph', 'int2e_ip2_cart'):
+        out['c0_' + name + '_items'] = qs[:40]
+        out['c0_' + name] = np.concatenate([o.ref.call(name, mol0, q)[1].ravel(order='F') for q in qs[:40]])
+    for name in ('int3c2e_ip1_sph', 'int3c2e_ip1_cart', 'int3c2e_ip2_sph', 'int3c2e_ip2_cart'):
+        out['c2_' + name + '_items'] = tr
+        out['c2_' + name] = np.concatenate([o.ref.call(name, mol2, t)[1].ravel(order='F') for t in tr])
+    # long-range Coulomb
+    m0 = mol0.copy()
+    m0.env[8] = 0.3
+    for name in ('int2e_sph', 'int2e_ip1_sph'):
+        out['lr_c0_' + name + '_items'] = qs[:30]
+        out['lr_c0_' + name] = np.concatenate([o.ref.call(name, m0, q)[1].ravel(order='F') for q in qs[:30]])
+    m2 = mol2.copy()
+    m2.env[8] = 0.5
+    out['lr_c2_int3c2e_sph_items'] = tr[:40]
+    out['lr_c2_int3c2e_sph'] = np.concatenate([o.ref.call('int3c2e_sph', m2, t)[1].ravel(order='F')
+                                               for t in tr[:40]])
+    out['lr_c2_int2c2e_sph_items'] = pr[:40]
+    out['lr_c2_int2c2e_sph'] = np.concatenate([o.ref.call('int2c2e_sph', m2, t)[1].ravel(order='F')
+                                               for t in pr[:40]])
     kp = np.array([(i, k) for k in range(8) for i in range(8)], dtype=np.int32)
     out['kat_int2c2e_sph_items'] = kp
     out['kat_int2c2e_sph'] = np.concatenate([o.ref.call('int2c2e_sph', mol, t, nbas=nbas)[1]

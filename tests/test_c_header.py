@@ -88,7 +88,7 @@ C_PLAN_SRC = r"""
 #include <cuda_runtime.h>
 #include "cintgpu.h"
 
-/* the batched and J/K usage shown in INTEGRATION.md, compiled and linked (not run: it needs a GPU) */
+/* the documented batched and J/K C usage, compiled and linked (not run: it needs a GPU) */
 int run(const int *quartets, long n, const int *atm, int natm, const int *bas, int nbas,
         const double *env, double *out_dev, const double *dm_cart, double *xj, double *xk,
         size_t nao_cart, cudaStream_t stream)

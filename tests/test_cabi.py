@@ -83,13 +83,33 @@ def test_no_gpu_fails_loudly(gpulib):
     mol = M.config0(seed=0)
     with pytest.raises(gpulib.CintGpuError, match='CUDA'):
         gpulib.Plan(gpulib.INT2E_SPH, mol, M.unique_quartets(mol.nbas)[:4])
+    L = gpulib.lib()
+    before = L.cintgpu_dropin_failures()
     flag, blk = gpulib.dropin('int2e_sph', mol, (1, 0, 0, 0))
-    assert flag == 0 and not blk.any() and gpulib.last_error()
+    # a failed call returns 0 like a screened block, but its block is NaN (a screened block is
+    # zeros), it is counted and it leaves a message
+    assert flag == 0 and np.isnan(blk).all() and gpulib.last_error()
+    assert L.cintgpu_dropin_failures() == before + 1
+    # the CINT2 form and a strided dims layout: only the block's own elements are NaN
+    out = np.zeros(7 * 7 * 7 * 7)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    shls = np.array([2, 1, 0, 0], np.int32)
+    dims = np.array([7, 7, 7, 7], np.int32)
+    assert L.int2e_sph(P(out), P(dims), P(shls), P(mol.atm), mol.natm, P(mol.bas), mol.nbas,
+                       P(mol.env), None, None) == 0
+    blockview = out.reshape(7, 7, 7, 7, order='F')
+    n = [mol.nsph(int(x)) for x in shls]
+    assert np.isnan(blockview[:n[0], :n[1], :n[2], :n[3]]).all()
+    assert np.isnan(out).sum() == np.prod(n)
+    assert L.cintgpu_dropin_failures() == before + 2
 
 
 @pytest.mark.parametrize('name,nsh', [('int2e_sph', 4), ('int2e_cart', 4), ('int2e_ip1_sph', 4),
                                       ('int2e_ip1_cart', 4), ('int3c2e_sph', 3),
-                                      ('int3c2e_cart', 3), ('int2c2e_sph', 2), ('int2c2e_cart', 2)])
+                                      ('int3c2e_cart', 3), ('int2c2e_sph', 2), ('int2c2e_cart', 2),
+                                      ('int2e_ip2_sph', 4), ('int2e_ip2_cart', 4),
+                                      ('int3c2e_ip1_sph', 3), ('int3c2e_ip1_cart', 3),
+                                      ('int3c2e_ip2_sph', 3), ('int3c2e_ip2_cart', 3)])
 def test_cache_size_query_matches_libcint_live(gpulib, oracle, name, nsh):
     """out == NULL answers for 200 random shell sets of the KAT basis (general contractions,
     l <= 4) and of c2 (1-6 primitives, auxiliary l <= 4), against libcint compiled from its

@@ -21,11 +21,31 @@ def test_rank_slices_cover_once():
             assert max(sizes) - min(sizes) <= 1
 
 
-def test_balanced_order_lpt():
+def test_balanced_order():
     costs = [10, 1, 1, 1, 9, 2, 2]
     owner = balanced_order(costs, 2)
     loads = [sum(c for c, o in zip(costs, owner) if o == r) for r in range(2)]
     assert abs(loads[0] - loads[1]) <= 2
+
+
+def test_balanced_order_at_scale():
+    """The c1 list's costs dealt to 8 ranks: vectorised (well under a second for 100k items, and
+    for 3.45M), every rank within the largest single cost of every other."""
+    import time
+    from libcint_gb300 import molecules as M
+    from libcint_gb300.dist import quartet_costs
+    mol = M.config1(seed=0)
+    qs = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'c1_quartets.npz'))['quartets']
+    costs = quartet_costs(mol, qs)
+    t = time.perf_counter()
+    owner = balanced_order(costs, 8)
+    assert time.perf_counter() - t < 1.0
+    loads = np.bincount(owner, weights=costs, minlength=8)
+    assert loads.max() - loads.min() <= costs.max()
+    big = np.tile(costs, 35)
+    t = time.perf_counter()
+    balanced_order(big, 8)
+    assert time.perf_counter() - t < 5.0
 
 
 def _worker(rank, world, port, result):

@@ -4,6 +4,7 @@ size), replayed in numpy the way the kernels use them, give the same Cartesian b
 (libcint's order of operations, src/g2e.c:560-693 then src/cint2e.c:961-1183) on random VRR
 arrays."""
 import ctypes
+import math
 
 import numpy as np
 import pytest
@@ -24,34 +25,35 @@ def cart_list(l):
     return [(x, y, l - x - y) for x in range(l, -1, -1) for y in range(l - x, -1, -1)]
 
 
-def tables(li, lj, lk, ll):
+def tables(li, lj, lk, ll, bra=0):
     f = cg.lib().cg_eri_tables
     f.restype = ctypes.c_int
     info = np.zeros(12, np.int32)
-    groups = np.zeros(4 * 20000, np.int32)
-    perm = np.zeros(4000, np.int32)
+    groups = np.zeros(4 * 200000, np.int32)
+    perm = np.zeros(8000, np.int32)
     prog = np.zeros(400000, np.int32)
     rounds = np.zeros(20000, np.int32)
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
-    nprog = f(li, lj, lk, ll, P(info), P(groups), 20000, P(perm), 4000, P(prog), prog.size,
+    nprog = f(li, lj, lk, ll, bra, P(info), P(groups), 200000, P(perm), 8000, P(prog), prog.size,
               P(rounds), rounds.size)
     assert nprog >= 0
     keys = ['group_off', 'ngroup', 'perm_off', 'nE', 'nF', 'split', 'hrr_need', 'maxab', 'hprog_off',
-            'round_off', 'nround']
+            'round_off', 'nround', 'bra']
     c = dict(zip(keys, info.tolist()))
     return (c, groups[:4 * c['ngroup']].reshape(-1, 4), perm[:c['nE'] + c['nF']], prog[:nprog],
             rounds[:c['nround']].astype(np.int64) & 0xffffffff)
 
 
-def hrr(src, eperm, fperm, prog, li, lj, lk, ll, AB, CD, need):
+def hrr(src, eperm, fperm, prog, li, lj, lk, ll, AB, CD, need, bra_done=False):
     """cg_hrr replayed on the class's transfer program: returns the Cartesian block in gctr order
-    and checks the buffers stay within the class's hrr_need."""
+    and checks the buffers stay within the class's hrr_need.  bra_done: rows are (i j| already."""
     bE, bF = below(li), below(lk)
-    nE, nF = below(li + lj + 1) - bE, below(lk + ll + 1) - bF
+    nE = nc(li) * nc(lj) if bra_done else below(li + lj + 1) - bE
+    nF = below(lk + ll + 1) - bF
     cur = np.array([src[eperm[e] * nF + fperm[f]] for e in range(nE) for f in range(nF)])
     used = cur.size
     p = 0
-    for b in range(1, lj + 1):
+    for b in range(1, (0 if bra_done else lj) + 1):
         nrows = prog[p]
         rows = prog[p + 1:p + 1 + 3 * nrows].reshape(-1, 3)
         nxt = np.zeros(nrows * nF)
@@ -226,3 +228,199 @@ def test_all_class_tables_stay_in_bounds():
                         assert sout == nent
                         p += 3 + 3 * nent
                     assert p == len(prog)
+
+
+def bra_arrays(g, li, lj):
+    """Per-term bra transfer of each axis's VRR array g[t, ax, f, a] (a <= li+lj): returns
+    out[t, ax, (i + dI j) + dI dJ f], the layout of the kernels' bra classes."""
+    nT, _, nm, na = g.shape
+    dI, dJ = li + 1, lj + 1
+    out = np.zeros((nT, 3, dI * dJ * nm))
+    for ax in range(3):
+        for f in range(nm):
+            col = g[:, ax, f, :].copy()
+            for i in range(dI):
+                out[:, ax, i + dI * dJ * f] = col[:, i]
+            for j in range(1, dJ):
+                col[:, :na - j] = col[:, 1:na - j + 1] + AB_[0][ax] * col[:, :na - j]
+                for i in range(dI):
+                    out[:, ax, i + dI * j + dI * dJ * f] = col[:, i]
+    return out
+
+
+AB_ = [None]
+
+
+def vrr_bra_inplace(vrr, nmax, mmax, dI, dJ, AB):
+    """The memory procedure of vrr_bra_axis (rys_device.cuh) replayed on one buffer: the VRR array
+    at out[a + (nmax+1) f], then columns from the highest f down through a one-column scratch,
+    writing out[(i + dI j) + dI dJ f].  Every read of a VRR entry is checked to see the value the
+    VRR stored (no transfer output overwrote it first)."""
+    na, B = nmax + 1, dI * dJ
+    size = B * (mmax + 1)
+    out = np.full(size, np.nan)
+    fresh = np.zeros(size, bool)
+    for f in range(mmax + 1):
+        out[na * f:na * f + na] = vrr[f]
+        fresh[na * f:na * f + na] = True
+    for m in range(mmax, -1, -1):
+        assert fresh[na * m:na * m + na].all()
+        col = out[na * m:na * m + na].copy()
+        o = B * m
+        def put(k, v):
+            assert 0 <= o + k < size
+            out[o + k] = v
+            fresh[o + k] = False
+        for i in range(dI):
+            put(i, col[i])
+        for j in range(1, dJ):
+            col[:na - j] = col[1:na - j + 1] + AB * col[:na - j]
+            for i in range(dI):
+                put(i + dI * j, col[i])
+    return out
+
+
+@pytest.mark.parametrize('li,lj,mmax', [(3, 3, 0), (3, 3, 4), (4, 3, 2), (6, 6, 12), (3, 1, 3),
+                                        (5, 4, 6), (2, 2, 4), (6, 3, 0)])
+def test_bra_transfer_in_place(li, lj, mmax):
+    """vrr_bra_axis's in-place order reads every VRR column before any transfer output lands on it
+    and stays inside the per-axis array, and it equals the plain per-column transfer."""
+    rng = np.random.RandomState(li * 100 + lj * 10 + mmax)
+    nmax, dI, dJ = li + lj, li + 1, lj + 1
+    vrr = rng.normal(size=(mmax + 1, nmax + 1))
+    AB = 0.7
+    got = vrr_bra_inplace(vrr, nmax, mmax, dI, dJ, AB)
+    ref = np.zeros(dI * dJ * (mmax + 1))
+    for f in range(mmax + 1):
+        for i in range(dI):
+            for j in range(dJ):
+                ref[i + dI * j + dI * dJ * f] = sum(
+                    math.comb(j, k) * AB ** (j - k) * vrr[f, i + k] for k in range(j + 1))
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12)
+
+
+BRA_CLASSES = [(3, 3, 0, 0), (3, 3, 1, 0), (3, 3, 2, 1), (3, 3, 2, 2), (3, 3, 3, 2), (4, 3, 2, 1),
+               (4, 4, 3, 2), (3, 1, 2, 2), (2, 2, 1, 1), (5, 3, 0, 0), (3, 3, 3, 3)]
+
+
+@pytest.mark.parametrize('cls', BRA_CLASSES)
+def test_bra_tables_replay(cls):
+    """Bra classes: the per-term bra arrays, the stage-3 groups (one (ij) row, nfz f members) and
+    the ket-only transfer program reproduce the per-term transfer of both sides."""
+    li, lj, lk, ll = cls
+    c, groups, perm, prog, rounds = tables(*cls, bra=1)
+    nfi, nfj = nc(li), nc(lj)
+    nE, nF = c['nE'], c['nF']
+    assert c['bra'] == 1 and nE == nfi * nfj and nF == below(lk + ll + 1) - below(lk)
+    assert c['ngroup'] == nfi * nfj * nc(lk + ll)
+    assert c['maxab'] == 1 | ((ll + 1) << 8)
+    assert list(perm[:nE]) == list(range(nE))
+    hit = np.zeros(nE * nF, int)
+    for oxy, oz, acc, mn in groups:
+        nez, nfz = mn & 0xff, (mn >> 8) & 0xff
+        assert nez == 1 and 1 <= nfz <= ll + 1
+        for b in range(nfz):
+            hit[acc + b] += 1
+    assert (hit == 1).all()
+    rng = np.random.RandomState(sum(cls) + 3)
+    nT, na, nm = 4, li + lj + 1, lk + ll + 1
+    g = rng.normal(size=(nT, 3, nm, na))
+    AB, CD = rng.normal(size=3), rng.normal(size=3)
+    AB_[0] = AB
+    gb = bra_arrays(g, li, lj)
+    B = (li + 1) * (lj + 1)
+    acc = np.zeros(nE * nF)
+    for oxy, oz, a0, mn in groups:
+        ox, oy = oxy & 0xffff, oxy >> 16
+        nfz = (mn >> 8) & 0xff
+        p = gb[:, 0, ox] * gb[:, 1, oy]
+        for b in range(nfz):
+            acc[a0 + b] += (p * gb[:, 2, oz + B * b]).sum()
+    got = hrr(acc, perm[:nE], perm[nE:], prog, li, lj, lk, ll, AB, CD, c['hrr_need'], bra_done=True)
+    ref = direct(g, li, lj, lk, ll, AB, CD)
+    np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-11 * np.abs(ref).max())
+
+
+def test_all_bra_tables_stay_in_bounds():
+    """Bra classes up to l = 6 (those the planner may route there: fewer than 65536 groups, the
+    rounds' 16-bit group index): stage-3 offsets inside the per-axis g(i, j, f) arrays,
+    accumulator indices inside nE x nF, the ket program inside hrr_need."""
+    for li in range(7):
+        for lj in range(1, li + 1):
+            for lk in range(7):
+                for ll in range(lk + 1):
+                    if nc(li) * nc(lj) * nc(lk + ll) >= 65536:
+                        continue
+                    c, groups, perm, prog, rounds = tables(li, lj, lk, ll, bra=1)
+                    B, nm = (li + 1) * (lj + 1), lk + ll + 1
+                    G = B * nm
+                    nE, nF = c['nE'], c['nF']
+                    ox, oy = groups[:, 0] & 0xffff, groups[:, 0] >> 16
+                    nfz = (groups[:, 3] >> 8) & 0xff
+                    assert ox.max() < G and oy.max() < G
+                    assert (groups[:, 1] + B * (nfz - 1)).max() < G
+                    assert (groups[:, 2] + (nfz - 1)).max() < nE * nF
+                    starts, cnts = rounds & 0xffff, (rounds >> 16) & 0xff
+                    assert (starts + cnts).max() <= len(groups) and cnts.sum() == len(groups)
+                    need = c['hrr_need']
+                    assert nE * nF <= need and nc(li) * nc(lj) * nc(lk) * nc(ll) <= need
+                    p, nij = 0, nc(li) * nc(lj)
+                    for d in range(1, ll + 1):
+                        nent, sin, sout = prog[p:p + 3]
+                        ents = prog[p + 3:p + 3 + 3 * nent].reshape(-1, 3)
+                        assert ents[:, :2].max() < sin and nij * sin <= need and nij * sout <= need
+                        p += 3 + 3 * nent
+                    assert p == len(prog)
+
+
+def g_axis_replay(nmax, mmax, dI, dJ, dK, dL, b00, b10, b01, c00, c0p, AB, CD, swap):
+    """g_axis (rys_device.cuh) restated in numpy: VRR about A (or B = A - AB, swap bit 0) and C
+    (or D, bit 1), then the transfers towards the other centre; returns g[i, j, k, l]."""
+    if swap & 1:
+        c00, AB = c00 + AB, -AB
+    if swap & 2:
+        c0p, CD = c0p + CD, -CD
+    na, nm = nmax + 1, mmax + 1
+    T = np.zeros((nm, na))
+    T[0, 0] = 1.0
+    if mmax > 0:
+        T[1, 0] = c0p
+    for m in range(1, mmax):
+        T[m + 1, 0] = c0p * T[m, 0] + m * b01 * T[m - 1, 0]
+    for a in range(1, na):
+        T[0, a] = c00 * T[0, a - 1] + ((a - 1) * b10 * T[0, a - 2] if a >= 2 else 0)
+        for m in range(mmax):
+            v = c0p * T[m, a] + a * b00 * T[m, a - 1]
+            if m > 0:
+                v += m * b01 * T[m - 1, a]
+            T[m + 1, a] = v
+    nb, nt = (dJ, dI) if swap & 1 else (dI, dJ)
+    mb, mt = (dL, dK) if swap & 2 else (dK, dL)
+    g = np.zeros((dI, dJ, dK, dL))
+    col = T.copy()
+    for t in range(nt):
+        if t > 0:
+            col[:, :na - t] = AB * col[:, :na - t] + col[:, 1:na - t + 1]
+        for b in range(nb):
+            i, j = (t, b) if swap & 1 else (b, t)
+            tmp = col[:, b].copy()
+            for u in range(mt):
+                if u > 0:
+                    tmp[:nm - u] = CD * tmp[:nm - u] + tmp[1:nm - u + 1]
+                for v in range(mb):
+                    k, l = (u, v) if swap & 2 else (v, u)
+                    g[i, j, k, l] = tmp[v]
+    return g
+
+
+@pytest.mark.parametrize('li,lj,lk,ll', [(3, 3, 3, 3), (4, 2, 3, 1), (2, 4, 1, 3), (5, 4, 4, 2)])
+def test_g_axis_base_swap(li, lj, lk, ll):
+    """Running a pair's recurrences about its second centre gives the same 2D integrals."""
+    rng = np.random.RandomState(li + 7 * lj)
+    dI, dJ, dK, dL = li + 1, lj + 1, lk + 1, ll + 1
+    b00, b10, b01 = rng.uniform(0.05, 0.4, 3)
+    c00, c0p, AB, CD = rng.normal(size=4)
+    ref = g_axis_replay(li + lj, lk + ll, dI, dJ, dK, dL, b00, b10, b01, c00, c0p, AB, CD, 0)
+    for swap in (1, 2, 3):
+        got = g_axis_replay(li + lj, lk + ll, dI, dJ, dK, dL, b00, b10, b01, c00, c0p, AB, CD, swap)
+        np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-10 * np.abs(ref).max())

@@ -1,0 +1,170 @@
+"""Parity on the other workloads' shapes, through batched plans and the drop-in, against libcint's
+own blocks (tests/golden/ref_blocks.npz), the CPU restatement and its long-double referee:
+
+  c3   24 atoms, s/p/d with 3-5 primitives (the adjoint's workload): int2e_sph and int2e_ip1_sph
+  c4   g shells with 1-8 primitives (one quartet per kernel-order class, l <= 4): int2e_sph,
+       int2e_cart and int2e_ip1_sph
+  c2   int3c2e_cart (the int3c2e_sph path is covered elsewhere)
+  CINT2  the 8-argument wrappers (cint2e_sph, ...) equal the 10-argument entries.
+Gates as in test_gpu_c1_sweep: 1e-12 absolute everywhere; 1e-10 relative against the referee on
+elements above 1e-3 (Cartesian) or 1e-2 (spherical) of the quartet's largest Cartesian element."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from libcint_gb300 import molecules as M
+from tests import c1_sample
+from tests.test_gpu_c1_sweep import ABS_TOL, CUTOFF, REL_TOL, class_errors, gpu_blocks
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), 'golden')
+
+
+def c4_mol():
+    return M.config4(seed=2, natm=4, box=5.2)
+
+
+def item_major(gpu, mol, items, name):
+    """plan output (component-major: comp * output_size + block offset) -> per item, all
+    components (libcint's per-call layout)"""
+    sph = name.endswith('_sph')
+    ncomp = 3 if ('_ip1' in name or '_ip2' in name) else 1
+    nsh = 3 if 'int3c2e' in name else 4
+    per = np.array([mol.nsph(s) if sph else mol.ncart(s) for s in range(mol.nbas)], dtype=np.int64)
+    size = np.prod(per[np.asarray(items)[:, :nsh]], axis=1)
+    offs = np.concatenate([[0], np.cumsum(size)])
+    S = int(offs[-1])
+    out = np.empty(S * ncomp)
+    pos = 0
+    for q in range(len(items)):
+        for c in range(ncomp):
+            out[pos:pos + size[q]] = gpu[c * S + offs[q]:c * S + offs[q + 1]]
+            pos += size[q]
+    return out
+
+
+def scales(oracle, mol, items, three=False):
+    name = 'int3c2e_cart' if three else 'int2e_cart'
+    cart, offs = oracle.blocks(name, mol, items)
+    return np.array([np.abs(cart[offs[q]:offs[q + 1]]).max(initial=0) for q in range(len(items))])
+
+
+def check(gpu, ref, offs, cs, cls, name, what):
+    d = np.abs(gpu - ref)
+    assert d.max() <= ABS_TOL, '%s: max abs %.3e' % (what, d.max())
+    per = class_errors(gpu, ref, offs, cs, cls, CUTOFF['int2e_sph' if name.endswith('_sph') else 'int2e_cart'])
+    bad = {k: v for k, v in per.items() if v[1] > REL_TOL}
+    assert not bad, (what, {k: '%.2e' % v[1] for k, v in sorted(bad.items())})
+
+
+@pytest.mark.parametrize('name', ['int2e_sph', 'int2e_cart', 'int2e_ip1_sph'])
+def test_c4_g_shell_classes(gpulib, oracle, name):
+    """g shells on a dense 4-atom geometry (the ill-conditioned end of the transfers): libcint
+    itself is up to ~1e-11 off the referee here, so the bar is quartet by quartet: the GPU's
+    largest error against the referee at most twice libcint's own (or 2e-12), plus the relative
+    gate on uncancelled elements."""
+    mol = c4_mol()
+    from tests.golden.make_ref_blocks import c4_class_quartets
+    qs = c4_class_quartets(mol)
+    assert len(qs) == 120 and c1_sample.kernel_class(mol, qs).max() == 4
+    gpu = item_major(gpu_blocks(gpulib, name, mol, qs), mol, qs, name)
+    ref, offs = oracle.referee(name, mol, qs)
+    fx = np.load(os.path.join(GOLD, 'ref_blocks.npz'))
+    np.testing.assert_array_equal(fx['c4_' + name + '_items'], qs)
+    liberr = fx['c4_' + name + '_liberr']
+    worse = []
+    for q in range(len(qs)):
+        e = np.abs(gpu[offs[q]:offs[q + 1]] - ref[offs[q]:offs[q + 1]]).max()
+        if e > max(2e-12, 2 * liberr[q]):
+            worse.append((qs[q].tolist(), '%.2e' % e, '%.2e' % liberr[q]))
+    assert not worse, worse[:8]
+    cls = c1_sample.kernel_class(mol, qs)
+    per = class_errors(gpu, ref, offs, scales(oracle, mol, qs), cls,
+                       CUTOFF['int2e_sph' if name.endswith('_sph') else 'int2e_cart'])
+    bad = {k: v for k, v in per.items() if v[1] > REL_TOL}
+    assert not bad, {k: '%.2e' % v[1] for k, v in sorted(bad.items())}
+    lib = fx['c4_' + name]
+    assert np.abs(gpu - lib).max() <= max(2e-12, 3 * liberr.max())
+
+
+@pytest.mark.parametrize('name', ['int2e_sph', 'int2e_ip1_sph'])
+def test_c3_blocks(gpulib, oracle, name):
+    """c3: a class-stratified sample of the full unique list (plans) and libcint's own 40 blocks
+    (drop-in)."""
+    mol = M.config3(seed=0)
+    allq = M.unique_quartets(mol.nbas)
+    allq = allq[np.random.RandomState(11).permutation(len(allq))]
+    qs, cls = c1_sample.stratified(mol, allq, 40)
+    gpu = item_major(gpu_blocks(gpulib, name, mol, qs), mol, qs, name)
+    ref, offs = oracle.referee(name, mol, qs)
+    check(gpu, ref, offs, scales(oracle, mol, qs), cls, name, 'c3 %s vs referee' % name)
+    fx = np.load(os.path.join(GOLD, 'ref_blocks.npz'))
+    items, lib = fx['c3_' + name + '_items'], fx['c3_' + name]
+    off = 0
+    for it in items:
+        _, blk = gpulib.dropin(name, mol, it)
+        b = blk.ravel(order='F')
+        assert np.abs(b - lib[off:off + b.size]).max() <= ABS_TOL, it
+        off += b.size
+    assert off == lib.size
+
+
+@pytest.mark.parametrize('name', ['int2e_sph', 'int2e_cart'])
+def test_c1_libcint_blocks(gpulib, oracle, name):
+    """The benchmark workload's classes against libcint's own blocks: 2 quartets per class."""
+    mol = M.config1(seed=0)
+    fx = np.load(os.path.join(GOLD, 'ref_blocks.npz'))
+    qs, lib = fx['c1_' + name + '_items'], fx['c1_' + name]
+    gpu = gpu_blocks(gpulib, name, mol, qs)
+    assert gpu.size == lib.size
+    assert np.abs(gpu - lib).max() <= ABS_TOL
+
+
+def test_int3c2e_cart(gpulib, oracle):
+    mol, norb = M.config2(seed=1, natm=6, box=5.0)
+    rng = np.random.RandomState(4)
+    tr = []
+    for _ in range(300):
+        i, j = sorted(rng.randint(0, norb, 2))[::-1]
+        tr.append((i, j, rng.randint(norb, mol.nbas)))
+    tr = np.array(tr, dtype=np.int32)
+    gpu = gpu_blocks(gpulib, 'int3c2e_cart', mol, tr)
+    ref, offs = oracle.referee('int3c2e_cart', mol, tr)
+    cs = np.array([np.abs(ref[offs[q]:offs[q + 1]]).max(initial=0) for q in range(len(tr))])
+    L = mol.bas[:, 1]
+    cls = np.stack([L[tr[:, 0]], L[tr[:, 1]], L[tr[:, 2]], 0 * tr[:, 0]], 1)
+    check(gpu, ref, offs, cs, cls, 'int3c2e_cart', 'int3c2e_cart vs referee')
+    for t in tr[:20]:
+        _, blk = gpulib.dropin('int3c2e_cart', mol, t)
+        _, o = oracle.port.call('int3c2e_cart', mol, t)
+        assert np.abs(blk - o).max() <= ABS_TOL
+
+
+@pytest.mark.parametrize('name,nsh', [('cint2e_sph', 4), ('cint2e_cart', 4), ('cint2e_ip1_sph', 4),
+                                      ('cint2e_ip1_cart', 4), ('cint3c2e_sph', 3),
+                                      ('cint3c2e_cart', 3), ('cint2c2e_sph', 2), ('cint2c2e_cart', 2)])
+def test_cint2_wrappers(gpulib, name, nsh):
+    """libcint's 8-argument CINT2 forms (src/misc.h:34-60) give the 10-argument entries' blocks
+    and return value, with and without an optimizer."""
+    L = gpulib.lib()
+    mol, norb = M.config2(seed=1, natm=4, box=4.0)
+    P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+    rng = np.random.RandomState(nsh)
+    opt = ctypes.c_void_p()
+    optf = {'cint2e_sph': 'cint2e_sph_optimizer', 'cint2e_ip1_sph': 'cint2e_ip1_sph_optimizer',
+            'cint3c2e_sph': 'cint3c2e_sph_optimizer', 'cint2c2e_sph': 'cint2c2e_sph_optimizer'}.get(name)
+    if optf:
+        getattr(L, optf)(ctypes.byref(opt), P(mol.atm), mol.natm, P(mol.bas), mol.nbas, P(mol.env))
+    for _ in range(6):
+        s = np.ascontiguousarray(rng.randint(0, mol.nbas, 4), dtype=np.int32)
+        flag10, ref = gpulib.dropin(name[1:], mol, s[:nsh])
+        out = np.zeros(ref.size)
+        f = getattr(L, name)
+        flag8 = f(P(out), P(s), P(mol.atm), mol.natm, P(mol.bas), mol.nbas, P(mol.env), opt)
+        assert flag8 == flag10
+        np.testing.assert_array_equal(out, ref.ravel(order='F'))
+    if optf:
+        L.CINTdel_optimizer(ctypes.byref(opt))

@@ -8,7 +8,7 @@ import pytest
 from tests import _oracle  # noqa: F401  (puts the repo root on sys.path)
 import libcint_gb300 as cg
 
-ERI, IP1, GRAD, GRADA, ERIP = 0, 1, 2, 3, 4
+ERI, IP1, GRAD, GRADA, ERIP, ERIB = 0, 1, 2, 3, 4, 5
 TERMW, TERMW_GRAD, GRAD_MAXPRIM, W_SMEM = 12, 20, 16, 256
 WS_SMALL, WS_MAX = 24 * 1024 // 8, 48 * 1024 // 8
 
@@ -37,6 +37,26 @@ def classes(lmax):
 # every shared-memory size per warp the regular group can be launched with (CINTGPU_WS_KB and the
 # autotuner's candidates, 8..48 KB)
 WS_ALL = [kb * 1024 // 8 for kb in (8, 12, 16, 20, 24, 28, 32, 40, 48)]
+
+
+def test_bra_term_layouts_fit():
+    """Bra-per-term classes: term records, the per-axis g(i, j, f) arrays (dI dJ (lk+ll+1), which
+    hold the VRR array in place) and one VRR column of lane scratch per active lane fit."""
+    for l in classes(6):
+        if l[1] == 0:
+            continue
+        for ws in WS_ALL:
+            L = layout(l, ERIB, ws)
+            if L.T < 1:
+                continue
+            assert L.G == (l[0] + 1) * (l[1] + 1) * (l[2] + l[3] + 1)
+            assert L.G >= (L.nmax + 1) * (L.mmax + 1)      # the VRR array fits in place
+            assert L.gax % 2 == 1 and L.gax >= L.G and L.gstride == 3 * L.gax
+            assert L.termw % 2 == 1 and L.termw >= 10 + L.mmax + 1
+            assert L.scr % 2 == 1 and L.scr >= L.nmax + 1
+            items = min(32, 3 * L.T)
+            assert L.off_g == L.T * L.termw and L.off_scr == L.off_g + L.T * L.gstride
+            assert L.off_scr + items * L.scr <= ws
 
 
 @pytest.mark.parametrize('mode', [ERI, ERIP, IP1])

@@ -1,6 +1,7 @@
 """Task routing of the planner, CPU only (host planning, no device): int2e classes whose horizontal
-transfer after contraction would lose precision (kernel-order lj or ll >= 4) go to the
-per-primitive group when its g arrays fit; CINTGPU_PER_PRIMITIVE_L moves the threshold; plans
+transfer after contraction would lose precision go elsewhere: kernel-order ll >= 3 to the
+per-primitive group when its g arrays fit, lj >= 3 with ll <= 2 to the bra-per-term tables of the
+regular groups; CINTGPU_PER_PRIMITIVE_L and CINTGPU_BRA_TERM_L move the thresholds; plans
 transform their outputs inside the integral kernel."""
 import ctypes
 import os
@@ -16,7 +17,7 @@ from tests.test_gpu_high_l import high_l_basis
 def groups(kind, mol, items, env=None):
     f = cg.lib().cg_plan_groups
     f.restype = ctypes.c_int
-    info = np.zeros(4, np.int64)
+    info = np.zeros(8, np.int64)
     items = np.ascontiguousarray(items, dtype=np.int32)
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     old = {k: os.environ.get(k) for k in (env or {})}
@@ -50,10 +51,19 @@ def test_threshold_switch_and_fusion():
     mol = M.config1(seed=0)
     qs = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'c1_quartets.npz'))['quartets']
     L = mol.bas[:, M.ANG_OF]
-    ff = qs[(np.minimum(L[qs[:, 0]], L[qs[:, 1]]) == 3) | (np.minimum(L[qs[:, 2]], L[qs[:, 3]]) == 3)][:50]
-    g = groups(cg.INT2E_SPH, mol, ff)
-    assert g[2] == 0 and g[3] == 1          # f-f transfers stay contraction first, fused output
-    g = groups(cg.INT2E_SPH, mol, ff, {'CINTGPU_PER_PRIMITIVE_L': '3'})
+    ff = qs[(np.minimum(L[qs[:, 0]], L[qs[:, 1]]) == 3) | (np.minimum(L[qs[:, 2]], L[qs[:, 3]]) == 3)]
+    K = np.stack([np.maximum(L[ff[:, 0]], L[ff[:, 1]]), np.minimum(L[ff[:, 0]], L[ff[:, 1]]),
+                  np.maximum(L[ff[:, 2]], L[ff[:, 3]]), np.minimum(L[ff[:, 2]], L[ff[:, 3]])], 1)
+    ket_ff = (K[:, 1] == 3) & (K[:, 3] == 3)            # (ff|ff): both transfers per primitive
+    ff = np.concatenate([ff[~ket_ff][:40], ff[ket_ff][:10]])
+    ket_ff = np.arange(len(ff)) >= 40
+    g = groups(cg.INT2E_SPH, mol, ff[~ket_ff])
+    assert g[2] == 0 and g[4] == g[0] + g[1] > 0 and g[3] == 1   # bra per term, fused output
+    g = groups(cg.INT2E_SPH, mol, ff[ket_ff])
+    assert g[2] > 0 and g[0] + g[1] == 0 and g[4] == 0
+    g = groups(cg.INT2E_SPH, mol, ff, {'CINTGPU_BRA_TERM_L': '99', 'CINTGPU_PER_PRIMITIVE_L': '4'})
+    assert g[2] == 0 and g[4] == 0          # the former default: f-f transfers contraction first
+    g = groups(cg.INT2E_SPH, mol, ff, {'CINTGPU_BRA_TERM_L': '99'})
     assert g[0] + g[1] == 0 and g[2] > 0    # all of them per primitive
     g = groups(cg.INT2E_SPH, mol, qs[:200], {'CINTGPU_PER_PRIMITIVE_L': '0'})
     assert g[0] + g[1] == 0 and g[2] > 0    # every class per primitive
@@ -91,7 +101,7 @@ def test_invalid_input_is_rejected_with_a_message():
         ('l = 7', _variant(mol, 'bas', (3, M.ANG_OF), 7), q, -3, 'angular momentum'),
         ('nprim = 65', _variant(mol, 'bas', (3, M.NPRIM_OF), 65), q, -1, 'nprim'),
         ('atom out of range', _variant(mol, 'bas', (3, M.ATOM_OF), 99), q, -1, 'atom'),
-        ('omega != 0', _variant(mol, 'env', 8, 0.3), q, -3, 'range-separated'),
+        ('omega < 0', _variant(mol, 'env', 8, -0.3), q, -3, 'short-range'),
         ('NaN coordinate', _variant(mol, 'env', int(mol.atm[mol.bas[2, M.ATOM_OF], M.PTR_COORD]) + 1,
                                     float('nan')), q, -1, 'non-finite coordinate'),
         ('Inf exponent', _variant(mol, 'env', int(mol.bas[1, M.PTR_EXP]), float('inf')), q, -1,
