@@ -248,7 +248,7 @@ def extra_adjoint(cg, seed=0, natm=24):
     the two."""
     import torch
     from libcint_gb300 import molecules as M
-    from libcint_gb300.coulomb import CoulombPlans, grad_via_ip1
+    from libcint_gb300.coulomb import CoulombPlans, IP1Gradient
     mol = M.config3(seed=seed, natm=natm, box=8.0 * (natm / 24.0) ** (1.0 / 3.0))
     nao = sum(mol.nsph(i) for i in range(mol.nbas))
     rng = np.random.RandomState(seed)
@@ -260,12 +260,16 @@ def extra_adjoint(cg, seed=0, natm=24):
 
     def adj():
         g_adj[0] = plans.grad(dm)[0]
-    t_adj = _timed(adj, reps=2)
+    t_adj = _timed(adj, reps=2)   # the adjoint plan is built by the untimed first call
+    # the comparator's three int2e_ip1 plans are built here, outside the timed region, as the
+    # adjoint's is: both sides time device work (plus the comparator's contraction)
+    route = IP1Gradient(mol)
     g_ip1 = [None]
 
     def ip1():
-        g_ip1[0] = grad_via_ip1(mol, dm)
-    t_ip1 = _timed(ip1, reps=1)
+        g_ip1[0] = route.grad(dm)
+    t_ip1 = _timed(ip1, reps=2)
+    route.close()
     diff = float((g_adj[0] - g_ip1[0]).abs().max() / g_ip1[0].abs().max())
     plans_a = CoulombPlans(mol, with_exponents=True)
     t_adj_a = _timed(lambda: plans_a.grad(dm), reps=1)
@@ -273,7 +277,9 @@ def extra_adjoint(cg, seed=0, natm=24):
                         % (natm, 8.0 * (natm / 24.0) ** (1.0 / 3.0), len(M.unique_quartets(mol.nbas))),
             'forward_J_ms': 1e3 * t_fwd, 'adjoint_grad_ms': 1e3 * t_adj,
             'adjoint_grad_with_exponents_ms': 1e3 * t_adj_a, 'ip1_route_grad_ms': 1e3 * t_ip1,
-            'adjoint_speedup_over_ip1': t_ip1 / t_adj, 'max_rel_diff_vs_ip1': diff}
+            'adjoint_speedup_over_ip1': t_ip1 / t_adj, 'max_rel_diff_vs_ip1': diff,
+            'comparator': 'int2e_ip1 route (three batched plans, built outside the timed region) '
+                          'formed in HBM and contracted with torch'}
 
 
 def extra_jk(cg, seed=0, natm=24):

@@ -263,6 +263,22 @@ int cintgpu_cart2sph(int l, double *c);
 int cintgpu_plan_nonempty(const CINTGPUPlan *plan, int *flags_host);
 void cintgpu_plan_destroy(CINTGPUPlan *plan);
 
+/* Whole-molecule J / K / adjoint over the Schwarz-screened unique quartet list, which is never
+ * stored (no libcint counterpart; the caller loop of libcint examples/time_c2h6.c:719-745 with the
+ * per-pair bound of its optimizer's pair data, src/optimizer.c:344-425).  pairs: npair shell
+ * pairs (2 ints, i >= j), q: their bounds Q_ij = sqrt(max |(ab|ab)|).  The pairs are ordered by
+ * q, largest first; the quartets are (p, q) with q <= p in that order and q_p q_q >= threshold,
+ * for bra positions [p_begin, p_end) (p_end < 0: all).  kind: CINTGPU_J_BUILD, K_BUILD,
+ * JK_BUILD (vj_dev / vk_dev as cintgpu_plan_execute_jk) or J_GRAD, J_GRAD_EXP (grad_dev,
+ * galpha_dev as cintgpu_plan_execute_grad); dm_dev is the Cartesian density.  Chunk plans are
+ * built on host threads and executed as they come; the call returns when all have run, with the
+ * number of quartets in *nquartets (may be NULL). */
+int cintgpu_screened_run(int kind, const int *pairs, const double *q, int64_t npair,
+                         double threshold, int64_t p_begin, int64_t p_end, const int *atm, int natm,
+                         const int *bas, int nbas, const double *env, const double *dm_dev,
+                         double *vj_dev, double *vk_dev, double *grad_dev, double *galpha_dev,
+                         int64_t *nquartets);
+
 /* one-shot host-buffer form: plan, H2D, execute, D2H into out_host (output_size*ncomp doubles) */
 int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,
                        const int64_t *offsets, const int *atm, int natm, const int *bas,

@@ -102,6 +102,9 @@ def lib():
     L.cintgpu_cart2sph.argtypes = [i32, vp]
     L.cintgpu_cart2sph.restype = i32
     L.cintgpu_last_error.restype = ctypes.c_char_p
+    L.cintgpu_screened_run.restype = i32
+    L.cintgpu_screened_run.argtypes = [i32, vp, vp, i64, dbl, i64, i64, vp, i32, vp, i32, vp, vp, vp,
+                                       vp, vp, vp, vp]
     L.cintgpu_dropin_failures.restype = i64
     L.cintgpu_dropin_failures.argtypes = []
     L.cintgpu_device_sm_count.restype = i32

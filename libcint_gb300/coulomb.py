@@ -226,64 +226,97 @@ def coulomb_energy(coords, exps, dm, mol, quartets=None):
     return _CE.apply(coords, exps, dm, mol, quartets)
 
 
-def _ip1_pass(mol, dmd, q, w, perm):
-    """-1/2 w D_ij D_kl (nabla_1 ..|..) summed per quartet for the shell order perm (nq, 3),
-    from int2e_ip1_sph blocks formed by one batched GPU plan (class-contiguous offsets)."""
-    import torch
-    from . import Plan
-    loc = mol.ao_loc()
-    ls = mol.bas[:, ANG_OF]
-    qq = np.ascontiguousarray(q[:, perm])
-    key = ls[qq[:, 0]] * 1000 + ls[qq[:, 1]] * 100 + ls[qq[:, 2]] * 10 + ls[qq[:, 3]]
-    order = np.argsort(key, kind='stable')
-    qs, ws = qq[order], w[order]
-    d = np.array([mol.nsph(s) for s in range(mol.nbas)])
-    sizes = d[qs[:, 0]] * d[qs[:, 1]] * d[qs[:, 2]] * d[qs[:, 3]]
-    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
-    p = Plan(INT2E_IP1_SPH, mol, qs, offs)
-    out = torch.empty(3 * p.output_size, dtype=torch.float64, device='cuda')
-    p.execute(out)
-    out = out.view(3, p.output_size)
-    res = torch.empty((len(qs), 3), dtype=torch.float64, device='cuda')
-    ks = key[order]
-    bounds = np.flatnonzero(np.diff(ks)) + 1
-    for seg in np.split(np.arange(len(qs)), bounds):
-        if len(seg) == 0:
-            continue
-        a, b, c, e = (int(d[qs[seg[0], x]]) for x in range(4))
-        blk = out[:, offs[seg[0]]:offs[seg[0]] + len(seg) * a * b * c * e]
-        blk = blk.reshape(3, len(seg), e, c, b, a)               # i fastest inside a block
-        ii = torch.as_tensor(loc[qs[seg, 0]][:, None] + np.arange(a)[None], device='cuda')
-        jj = torch.as_tensor(loc[qs[seg, 1]][:, None] + np.arange(b)[None], device='cuda')
-        kk = torch.as_tensor(loc[qs[seg, 2]][:, None] + np.arange(c)[None], device='cuda')
-        ll = torch.as_tensor(loc[qs[seg, 3]][:, None] + np.arange(e)[None], device='cuda')
-        Dij = dmd[ii[:, :, None], jj[:, None, :]]
-        Dkl = dmd[kk[:, :, None], ll[:, None, :]]
-        wt = torch.as_tensor(ws[seg], device='cuda')
-        res[torch.as_tensor(seg, device='cuda')] = \
-            torch.einsum('xnlkji,nij,nkl,n->nx', blk, Dij, Dkl, wt) * -0.5
-    p.close()
-    back = torch.empty_like(res)
-    back[torch.as_tensor(order, device='cuda')] = res
-    return back
+class _IP1Pass:
+    """One pass of the comparator: int2e_ip1_sph blocks of the quartets in shell order perm (the
+    derivative on the first shell), formed by one batched GPU plan (class-contiguous offsets) and
+    contracted with -1/2 w D_ij D_kl per quartet.  The plan and the index tensors are built at
+    construction; run() only executes and contracts."""
+
+    def __init__(self, mol, q, w, perm):
+        import torch
+        from . import Plan
+        loc = mol.ao_loc()
+        ls = mol.bas[:, ANG_OF]
+        qq = np.ascontiguousarray(q[:, perm])
+        key = ls[qq[:, 0]] * 1000 + ls[qq[:, 1]] * 100 + ls[qq[:, 2]] * 10 + ls[qq[:, 3]]
+        order = np.argsort(key, kind='stable')
+        qs, ws = qq[order], w[order]
+        d = np.array([mol.nsph(s) for s in range(mol.nbas)])
+        sizes = d[qs[:, 0]] * d[qs[:, 1]] * d[qs[:, 2]] * d[qs[:, 3]]
+        offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+        self.plan = Plan(INT2E_IP1_SPH, mol, qs, offs)
+        self.out = torch.empty(3 * self.plan.output_size, dtype=torch.float64, device='cuda')
+        self.n = len(qs)
+        ks = key[order]
+        bounds = np.flatnonzero(np.diff(ks)) + 1
+        self.segs = []
+        for seg in np.split(np.arange(len(qs)), bounds):
+            if len(seg) == 0:
+                continue
+            a, b, c, e = (int(d[qs[seg[0], x]]) for x in range(4))
+            t = lambda v: torch.as_tensor(v, device='cuda')
+            self.segs.append((int(offs[seg[0]]), len(seg), (a, b, c, e),
+                              t(loc[qs[seg, 0]][:, None] + np.arange(a)[None]),
+                              t(loc[qs[seg, 1]][:, None] + np.arange(b)[None]),
+                              t(loc[qs[seg, 2]][:, None] + np.arange(c)[None]),
+                              t(loc[qs[seg, 3]][:, None] + np.arange(e)[None]),
+                              t(ws[seg]), t(seg)))
+        self.order = torch.as_tensor(order, device='cuda')
+
+    def run(self, dmd):
+        import torch
+        self.plan.execute(self.out)
+        out = self.out.view(3, self.plan.output_size)
+        res = torch.empty((self.n, 3), dtype=torch.float64, device='cuda')
+        for off, n, (a, b, c, e), ii, jj, kk, ll, wt, seg in self.segs:
+            blk = out[:, off:off + n * a * b * c * e].reshape(3, n, e, c, b, a)  # i fastest
+            Dij = dmd[ii[:, :, None], jj[:, None, :]]
+            Dkl = dmd[kk[:, :, None], ll[:, None, :]]
+            res[seg] = torch.einsum('xnlkji,nij,nkl,n->nx', blk, Dij, Dkl, wt) * -0.5
+        back = torch.empty_like(res)
+        back[self.order] = res
+        return back
+
+    def close(self):
+        self.plan.close()
+
+
+class IP1Gradient:
+    """dL/dR from int2e_ip1 integrals formed on the GPU (written to HBM, batched plans) and
+    contracted with the density: the comparator route, libcint's (src/autocode/grad2.c:69-88).
+    Three passes over the unique quartet list put the derivative on i, j and k ((ij|kl), (ji|kl),
+    (kl|ij)); the fourth centre follows from translational invariance, per quartet.  The plans
+    are built once at construction, like the adjoint's."""
+
+    def __init__(self, mol, quartets=None):
+        import torch
+        q = unique_quartets(mol.nbas) if quartets is None else np.asarray(quartets, dtype=np.int32)
+        self.mol = mol
+        w = (np.where(q[:, 0] != q[:, 1], 2.0, 1.0) * np.where(q[:, 2] != q[:, 3], 2.0, 1.0)
+             * np.where((q[:, 0] != q[:, 2]) | (q[:, 1] != q[:, 3]), 2.0, 1.0))
+        self.passes = [_IP1Pass(mol, q, w, perm) for perm in ((0, 1, 2, 3), (1, 0, 2, 3), (2, 3, 0, 1))]
+        atom = mol.bas[:, ATOM_OF]
+        self.atoms = [torch.as_tensor(atom[q[:, col]], device='cuda') for col in range(4)]
+
+    def grad(self, dm):
+        import torch
+        dmd = dm.detach()
+        vi, vj, vk = (p.run(dmd) for p in self.passes)
+        vl = -(vi + vj + vk)
+        grad = torch.zeros((self.mol.natm, 3), dtype=torch.float64, device='cuda')
+        for col, v in enumerate((vi, vj, vk, vl)):
+            grad.index_add_(0, self.atoms[col], v)
+        return grad
+
+    def close(self):
+        for p in self.passes:
+            p.close()
 
 
 def grad_via_ip1(mol, dm, quartets=None):
-    """dL/dR from int2e_ip1 integrals formed on the GPU (written to HBM, batched plans) and
-    contracted with the density: the comparator route.  Three passes over the unique quartet list
-    put the derivative on i, j and k ((ij|kl), (ji|kl), (kl|ij)); the fourth centre follows from
-    translational invariance, per quartet."""
-    import torch
-    q = unique_quartets(mol.nbas) if quartets is None else np.asarray(quartets, dtype=np.int32)
-    atom = mol.bas[:, ATOM_OF]
-    w = (np.where(q[:, 0] != q[:, 1], 2.0, 1.0) * np.where(q[:, 2] != q[:, 3], 2.0, 1.0)
-         * np.where((q[:, 0] != q[:, 2]) | (q[:, 1] != q[:, 3]), 2.0, 1.0))
-    dmd = dm.detach()
-    vi = _ip1_pass(mol, dmd, q, w, (0, 1, 2, 3))
-    vj = _ip1_pass(mol, dmd, q, w, (1, 0, 2, 3))
-    vk = _ip1_pass(mol, dmd, q, w, (2, 3, 0, 1))
-    vl = -(vi + vj + vk)
-    grad = torch.zeros((mol.natm, 3), dtype=torch.float64, device='cuda')
-    for col, v in ((0, vi), (1, vj), (2, vk), (3, vl)):
-        grad.index_add_(0, torch.as_tensor(atom[q[:, col]], device='cuda'), v)
-    return grad
+    """dL/dR through the int2e_ip1 route (IP1Gradient), plans built and released in the call."""
+    r = IP1Gradient(mol, quartets)
+    try:
+        return r.grad(dm)
+    finally:
+        r.close()

@@ -2260,6 +2260,207 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
     return rc;
 }
 
+/* Whole-molecule J / K / adjoint over a Schwarz-screened quartet list that is never stored
+ * (libcint's caller pattern, examples/time_c2h6.c:719-745, with the per-pair bound of its
+ * optimizer's pair data, src/optimizer.c:344-425).  The shell pairs are sorted by their bound
+ * Q, largest first; the unique quartets are the pairs (p, q) of that order with q <= p and
+ * Q_p Q_q >= threshold, so for every bra position p the surviving kets are the prefix
+ * [0, min(p + 1, n_p)) with n_p found by binary search.  The quartets of bra positions
+ * [p_begin, p_end) are cut into chunks in this order; builder threads materialise each chunk's
+ * quartets and build its J / K / adjoint plan (primitive screening as everywhere), the caller
+ * uploads and executes the chunk plans on two streams through a ring of four device slots; the
+ * contraction accumulates into vj / vk / grad on the device, so no integral is stored.
+ * Synchronous: returns when every chunk has run.  *nquartets (may be NULL) receives the number
+ * of quartets evaluated. */
+static int screened_run(int kind, const int *pairs, const double *q, int64_t npair, double threshold,
+                        int64_t p_begin, int64_t p_end, const int *atm, int natm, const int *bas,
+                        int nbas, const double *env, const double *dm_dev, double *vj_dev,
+                        double *vk_dev, double *grad_dev, double *galpha_dev, int64_t *nquartets)
+{
+    if (nquartets) *nquartets = 0;
+    if (!(kind == CINTGPU_J_BUILD || kind == CINTGPU_K_BUILD || kind == CINTGPU_JK_BUILD
+          || kind == CINTGPU_J_GRAD || kind == CINTGPU_J_GRAD_EXP)) {
+        set_error("screened runs take the J, K, J+K and adjoint kinds");
+        return CINTGPU_ERR_ARG;
+    }
+    if (npair < 0 || !(threshold >= 0) || !dm_dev) { set_error("bad pair list, threshold or density"); return CINTGPU_ERR_ARG; }
+    const bool grad = kind == CINTGPU_J_GRAD || kind == CINTGPU_J_GRAD_EXP;
+    if ((grad && !grad_dev) || (kind == CINTGPU_J_GRAD_EXP && !galpha_dev)
+        || ((kind == CINTGPU_J_BUILD || kind == CINTGPU_JK_BUILD) && !vj_dev)
+        || ((kind == CINTGPU_K_BUILD || kind == CINTGPU_JK_BUILD) && !vk_dev)) {
+        set_error("the kind's outputs must be given");
+        return CINTGPU_ERR_ARG;
+    }
+    for (int64_t t = 0; t < npair; t++)
+        if (pairs[2 * t] < 0 || pairs[2 * t] >= nbas || pairs[2 * t + 1] < 0 || pairs[2 * t + 1] >= nbas
+            || !std::isfinite(q[t])) {
+            set_error("pair %lld: shells (%d, %d) outside 0..%d or bound not finite", (long long)t,
+                      pairs[2 * t], pairs[2 * t + 1], nbas - 1);
+            return CINTGPU_ERR_ARG;
+        }
+    int rc = ensure_init();
+    if (rc) return rc;
+    /* order by bound, largest first (stable: equal bounds keep the caller's order) */
+    std::vector<int64_t> ord((size_t)npair);
+    for (int64_t t = 0; t < npair; t++) ord[t] = t;
+    std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return q[a] > q[b]; });
+    std::vector<double> qs((size_t)npair);
+    for (int64_t t = 0; t < npair; t++) qs[t] = q[ord[t]];
+    p_begin = std::max<int64_t>(0, p_begin);
+    p_end = std::min<int64_t>(npair, p_end < 0 ? npair : p_end);
+    /* kets of bra position p: [0, kets(p)) */
+    auto kets = [&](int64_t p) -> int64_t {
+        if (qs[p] <= 0) return 0;
+        const double need = threshold / qs[p];
+        /* first position whose bound is below need */
+        const int64_t n = std::upper_bound(qs.begin(), qs.end(), need,
+                                           [](double v, double e) { return v > e; }) - qs.begin();
+        /* positions [0, n) have qs >= need only when qs[pos] * qs[p] >= threshold exactly */
+        int64_t m = n;
+        while (m > 0 && qs[m - 1] * qs[p] < threshold) m--;
+        while (m < npair && qs[m] * qs[p] >= threshold) m++;
+        return std::min<int64_t>(p + 1, m);
+    };
+    /* chunks of about `target` quartets along (p, q) */
+    struct Span { int64_t p0, q0, p1, q1, n; };   /* from (p0, q0) up to, excluding, (p1, q1) */
+    std::vector<Span> spans;
+    const int64_t target = grad ? 20000 : 40000;
+    int64_t total = 0;
+    {
+        Span cur{p_begin, 0, p_begin, 0, 0};
+        for (int64_t p = p_begin; p < p_end; p++) {
+            const int64_t k = kets(p);
+            int64_t q0 = 0;
+            while (q0 < k) {
+                const int64_t take = std::min(k - q0, target - cur.n);
+                q0 += take;
+                cur.n += take;
+                total += take;
+                if (cur.n == target) {
+                    cur.p1 = p; cur.q1 = q0;
+                    spans.push_back(cur);
+                    cur = Span{p, q0, p, q0, 0};
+                }
+            }
+        }
+        if (cur.n > 0) { cur.p1 = p_end - 1; cur.q1 = kets(p_end - 1); spans.push_back(cur); }
+    }
+    if (nquartets) *nquartets = total;
+    if (spans.empty()) return 0;
+    BatchCtx &X = tl_batch;
+    rc = X.init();
+    if (rc) return rc;
+    const int C = (int)spans.size(), R = CG_BATCH_SLOTS;
+    struct Chunk { CINTGPUPlan *P = nullptr; DevLayout D; bool image = false, h2d = false, done = false; int rc = 0; std::string err; };
+    std::vector<Chunk> ch(C);
+    std::mutex mu;
+    std::condition_variable cv;
+    bool abort = false;
+    std::atomic<int> next{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    auto fail = [&](int c, int r, const std::string &e) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!abort) { ch[c].rc = r; ch[c].err = e; }
+        abort = true;
+        cv.notify_all();
+    };
+    auto builder = [&]() {
+        cudaSetDevice(dev);
+        std::vector<int> items;
+        for (;;) {
+            const int c = next.fetch_add(1);
+            if (c >= C) return;
+            const Span &sp = spans[c];
+            items.clear();
+            items.reserve((size_t)sp.n * 4);
+            for (int64_t p = sp.p0; p <= sp.p1 && p < p_end; p++) {
+                const int64_t k = kets(p);
+                const int64_t qa = p == sp.p0 ? sp.q0 : 0, qb = p == sp.p1 ? std::min(k, sp.q1) : k;
+                const int *bra = pairs + 2 * ord[p];
+                for (int64_t t = qa; t < qb; t++) {
+                    const int *ket = pairs + 2 * ord[t];
+                    items.push_back(bra[0]); items.push_back(bra[1]);
+                    items.push_back(ket[0]); items.push_back(ket[1]);
+                }
+            }
+            CINTGPUPlan *P = new CINTGPUPlan();
+            int r = build_plan(P, kind, items.data(), (int64_t)items.size() / 4, nullptr, atm, natm,
+                               bas, nbas, env, 0);
+            if (r) { fail(c, r, cintgpu_last_error()); delete P; return; }
+            const int slot = c % R;
+            if (c >= R) {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return abort || ch[c - R].h2d; });
+                if (abort) { delete P; return; }
+                lk.unlock();
+                if (cudaEventSynchronize(X.ev_h2d[slot]) != cudaSuccess) { fail(c, CINTGPU_ERR_CUDA, "upload failed"); delete P; return; }
+            }
+            DevLayout D = dev_layout(P);
+            if ((r = grow_host(&X.pin_in[slot], &X.pin_in_cap[slot], D.upload))) { fail(c, r, cintgpu_last_error()); delete P; return; }
+            fill_image(P, D, X.pin_in[slot]);
+            std::lock_guard<std::mutex> lk(mu);
+            ch[c].P = P;
+            ch[c].D = D;
+            ch[c].image = true;
+            cv.notify_all();
+        }
+    };
+    const int nbuild = std::max(1, std::min<int>(C, std::min<int>(14, (int)std::thread::hardware_concurrency())));
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nbuild; t++) pool.emplace_back(builder);
+    for (int c = 0; c < C; c++) {
+        const int slot = c % R;
+        cudaStream_t st = X.s_exec[c & 1];
+        CINTGPUPlan *P;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv.wait(lk, [&] { return abort || ch[c].image; });
+            if (abort) break;
+            P = ch[c].P;
+        }
+        /* the slot's previous chunk must have finished executing before its arena is reused */
+        if (c >= R && cudaEventSynchronize(X.ev_exec[slot]) != cudaSuccess) { fail(c, CINTGPU_ERR_CUDA, "chunk execution failed"); break; }
+        const DevLayout &D = ch[c].D;
+        int r;
+        if ((r = grow_dev(&X.arena[slot], &X.arena_cap[slot], D.total))) { fail(c, r, cintgpu_last_error()); break; }
+        P->dbuf = X.arena[slot]; P->dbuf_size = X.arena_cap[slot]; P->owns_dbuf = false;
+        carve_plan(P, D, X.arena[slot]);
+        bool ok = cudaMemcpyAsync(X.arena[slot], X.pin_in[slot], D.upload, cudaMemcpyHostToDevice, st) == cudaSuccess
+                  && cudaEventRecord(X.ev_h2d[slot], st) == cudaSuccess;
+        if (ok) { std::lock_guard<std::mutex> lk(mu); ch[c].h2d = true; cv.notify_all(); }
+        P->cur_dm = dm_dev;
+        P->cur_vj = P->jmode & 1 ? vj_dev : nullptr;
+        P->cur_vk = P->jmode & 2 ? vk_dev : nullptr;
+        P->cur_grad = grad_dev;
+        P->cur_galpha = galpha_dev;
+        if (ok && (r = execute_plan(P, nullptr, st))) { fail(c, r, cintgpu_last_error()); break; }
+        if (!ok || cudaEventRecord(X.ev_exec[slot], st) != cudaSuccess) { fail(c, CINTGPU_ERR_CUDA, "chunk enqueue failed"); break; }
+        std::lock_guard<std::mutex> lk(mu);
+        ch[c].P = nullptr;
+        delete P;
+    }
+    for (std::thread &t : pool) t.join();
+    cudaStreamSynchronize(X.s_exec[0]);
+    cudaStreamSynchronize(X.s_exec[1]);
+    for (Chunk &x : ch) {
+        delete x.P;
+        if (x.rc && !rc) { rc = x.rc; set_error("%s", x.err.c_str()); }
+    }
+    if (!rc && cudaGetLastError() != cudaSuccess) { set_error("screened run failed on the device"); rc = CINTGPU_ERR_CUDA; }
+    return rc;
+}
+
+int cintgpu_screened_run(int kind, const int *pairs, const double *q, int64_t npair,
+                         double threshold, int64_t p_begin, int64_t p_end, const int *atm, int natm,
+                         const int *bas, int nbas, const double *env, const double *dm_dev,
+                         double *vj_dev, double *vk_dev, double *grad_dev, double *galpha_dev,
+                         int64_t *nquartets)
+{
+    return screened_run(kind, pairs, q, npair, threshold, p_begin, p_end, atm, natm, bas, nbas, env,
+                        dm_dev, vj_dev, vk_dev, grad_dev, galpha_dev, nquartets);
+}
+
 int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,
                        const int64_t *offsets, const int *atm, int natm, const int *bas,
                        int nbas, const double *env)

