@@ -170,23 +170,44 @@ def _timed(fn, reps=3):
     return best
 
 
-def extra_dropin(cg, mol, qs, batched_value, n=2000):
-    """The plain drop-in: one libcint-signature int2e_sph call per quartet (host buffers)."""
-    sub = qs[:n]
-    nint = integrals_of(mol, sub)
-    buf = np.zeros(int(max(np.prod([mol.nsph(s) for s in q]) for q in sub)))
-    f = cg.lib().int2e_sph
+def extra_dropin(cg, mol, qs, batched_value, n=4000):
+    """The plain drop-in on its own workload, configs[0]-style c0 (8 atoms, 6 A, s,s,p,p,d x 4
+    primitives): one libcint-signature int2e_sph call per quartet from host buffers, without and
+    with an int2e_optimizer (whose side table caches the shell pairs' primitive data), on the first
+    n of its 336,610 unique quartets; and the batched plan over the whole c0 list for the ratio."""
+    import torch
+    from libcint_gb300 import molecules as M
+    m0 = M.config0(seed=0)
+    allq = M.unique_quartets(m0.nbas)
+    sub = allq[:n]
+    nint = integrals_of(m0, sub)
+    buf = np.zeros(int(max(np.prod([m0.nsph(s) for s in q]) for q in sub)))
+    L = cg.lib()
+    f = L.int2e_sph
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
-    f(P(buf), None, P(np.ascontiguousarray(sub[0])), P(mol.atm), mol.natm, P(mol.bas), mol.nbas,
-      P(mol.env), None, None)
-    t0 = time.perf_counter()
-    for q in sub:
-        f(P(buf), None, P(np.ascontiguousarray(q)), P(mol.atm), mol.natm, P(mol.bas), mol.nbas,
-          P(mol.env), None, None)
-    dt = time.perf_counter() - t0
-    v = nint / dt
-    return {'workload': 'first %d quartets of the c1 list, one int2e_sph call each' % n,
-            'integrals_per_s': v, 'quartets_per_s': n / dt, 'batched_over_dropin': batched_value / v}
+    opt = ctypes.c_void_p()
+    L.int2e_optimizer(ctypes.byref(opt), P(m0.atm), m0.natm, P(m0.bas), m0.nbas, P(m0.env))
+    res = {'workload': 'c0 (8 atoms, 6 A, s,s,p,p,d x 4 prims): first %d of its %d unique quartets, '
+                       'one int2e_sph call each' % (n, len(allq))}
+    for tag, o in (('no_optimizer', None), ('with_optimizer', opt)):
+        f(P(buf), None, P(np.ascontiguousarray(sub[0])), P(m0.atm), m0.natm, P(m0.bas), m0.nbas,
+          P(m0.env), o, None)
+        t0 = time.perf_counter()
+        for q in sub:
+            f(P(buf), None, P(np.ascontiguousarray(q)), P(m0.atm), m0.natm, P(m0.bas), m0.nbas,
+              P(m0.env), o, None)
+        dt = time.perf_counter() - t0
+        res[tag] = {'integrals_per_s': nint / dt, 'quartets_per_s': n / dt}
+    L.CINTdel_optimizer(ctypes.byref(opt))
+    p = cg.Plan(cg.INT2E_SPH, m0, allq)
+    out = torch.empty(p.output_size, dtype=torch.float64, device='cuda')
+    dtb = _timed(lambda: p.execute(out))
+    p.close()
+    vb = integrals_of(m0, allq) / dtb
+    res['batched_whole_c0_integrals_per_s'] = vb
+    res['batched_over_dropin'] = vb / res['no_optimizer']['integrals_per_s']
+    res['batched_over_dropin_with_optimizer'] = vb / res['with_optimizer']['integrals_per_s']
+    return res
 
 
 def extra_int3c2e(cg, seed=0, npairs=40):
@@ -377,6 +398,142 @@ def extra_screening(cg, seed=0, natm=24, threshold=1e-10):
             'max_abs_dJ': float((J1 - J0).abs().max()), 'max_abs_dK': float((K1 - K0).abs().max())}
 
 
+def _screened_total(q, threshold):
+    """quartets of the whole Schwarz-screened unique list (ScreenedCoulomb's enumeration) and the
+    per-bra-position counts, from the pair bounds alone"""
+    qs = np.sort(np.asarray(q))[::-1]
+    pos = np.arange(len(qs))
+    with np.errstate(divide='ignore'):
+        need = np.where(qs > 0, threshold / np.where(qs > 0, qs, 1.0), np.inf)
+    # kets of position p: pairs with bound >= need, at most p + 1
+    n = len(qs) - np.searchsorted(qs[::-1], need, side='left')
+    k = np.where(qs > 0, np.minimum(pos + 1, n), 0)
+    return int(k.sum()), k
+
+
+def extra_screened(cg, natm_whole=12, slab_quartets=4.0e6, seed=0):
+    """Whole-molecule Schwarz-screened J (c1, Q_ij Q_kl >= 1e-12) through
+    cintgpu_screened_run, which never stores the quartet list: the bounds of all 583k c1 shell
+    pairs, a timed slab of bra pairs around the median bound (extrapolated to the whole list by
+    quartet count), and a whole c1-density molecule of natm_whole atoms timed end to end."""
+    import torch
+    from libcint_gb300 import molecules as M
+    from libcint_gb300.screening import ScreenedCoulomb
+    out = {}
+    for tag, mol in (('c1', M.config1(seed=seed)),
+                     ('whole', M.config1(seed=seed, natm=natm_whole,
+                                         box=14.0 * (natm_whole / 120.0) ** (1.0 / 3.0)))):
+        nao = sum(mol.nsph(i) for i in range(mol.nbas))
+        d = np.random.RandomState(seed).normal(0, 0.1, (nao, nao))
+        dm = torch.as_tensor(0.5 * (d + d.T), device='cuda')
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sc = ScreenedCoulomb(mol, threshold=SCHWARZ)
+        torch.cuda.synchronize()
+        t_q = time.perf_counter() - t0
+        total, k = _screened_total(sc.q, SCHWARZ)
+        if tag == 'c1':
+            mid = len(k) // 2
+            cum = np.cumsum(k[mid:])
+            p1 = mid + int(np.searchsorted(cum, slab_quartets)) + 1
+            rng_ = (mid, min(p1, len(k)))
+        else:
+            rng_ = None
+        sc.get_jk(dm, True, False, bra_range=rng_ if rng_ else (0, min(len(k), 64)))   # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sc.get_jk(dm, True, False, bra_range=rng_)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        nq = sc.last_quartets
+        r = {'atoms': mol.natm, 'shell_pairs': int(len(sc.pairs)), 'bounds_s': t_q,
+             'surviving_quartets': total, 'unique_quartets': int(len(sc.pairs) * (len(sc.pairs) + 1) // 2),
+             'timed_quartets': nq, 'J_s': dt, 'quartets_per_s': nq / dt}
+        if tag == 'c1':
+            r['slab'] = 'bra positions [%d, %d) of %d in bound order' % (rng_[0], rng_[1], len(k))
+            r['extrapolated_whole_J_s'] = dt * total / max(nq, 1)
+        out[tag] = r
+    return out
+
+
+def _slab_list(sc, p0, p1):
+    """the quartets ScreenedCoulomb evaluates for bra positions [p0, p1), materialised"""
+    order = np.argsort(-sc.q, kind='stable')
+    qs = sc.q[order]
+    out = []
+    for p in range(p0, p1):
+        if qs[p] <= 0:
+            continue
+        k = int(np.count_nonzero(qs[:p + 1] * qs[p] >= SCHWARZ))
+        bra = np.broadcast_to(sc.pairs[order[p]], (k, 2))
+        out.append(np.concatenate([bra, sc.pairs[order[:k]]], 1))
+    return np.ascontiguousarray(np.concatenate(out), dtype=np.int32)
+
+
+def extra_c4(cg, seed=0, slab_j=1.5e6, slab_grad=1.5e5):
+    """c4 at full size (400 atoms, 24 A, s:3 p:3 d:2 f:1 g:1, 1-8 primitives, 4000 shells, 8M
+    shell pairs), Schwarz 1e-12: the bounds of every pair, the whole surviving list's size, a
+    timed J slab and a timed adjoint slab (bra pairs around the median bound; the list is streamed,
+    never stored), the int2e_ip1 route on the adjoint's slab (plans built outside the timed
+    region) and the two gradients' agreement."""
+    import torch
+    from libcint_gb300 import molecules as M
+    from libcint_gb300.coulomb import IP1Gradient
+    from libcint_gb300.screening import ScreenedCoulomb
+    mol = M.config4(seed=seed)
+    nao = sum(mol.nsph(i) for i in range(mol.nbas))
+    d = np.random.RandomState(seed).normal(0, 0.1, (nao, nao))
+    dm = torch.as_tensor(0.5 * (d + d.T), device='cuda')
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sc = ScreenedCoulomb(mol, threshold=SCHWARZ)
+    torch.cuda.synchronize()
+    t_q = time.perf_counter() - t0
+    total, k = _screened_total(sc.q, SCHWARZ)
+    mid = len(k) // 2
+    cum = np.cumsum(k[mid:])
+    pj = (mid, mid + int(np.searchsorted(cum, slab_j)) + 1)
+    pg = (mid, mid + int(np.searchsorted(cum, slab_grad)) + 1)
+    res = {'workload': 'c4: 400 atoms, 24 A, 3s3p2d1f1g, 1-8 prims, Schwarz 1e-12',
+           'shell_pairs': int(len(sc.pairs)), 'bounds_s': t_q, 'surviving_quartets': total}
+    from libcint_gb300.coulomb import J_BUILD, J_GRAD
+    dmc = sc.dm_cart(dm)          # the streamed contraction alone is timed
+    XJ = torch.zeros_like(dmc)
+    sc._run(J_BUILD, dmc, vj=XJ, bra_range=(mid, mid + 2))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sc._run(J_BUILD, dmc, vj=XJ, bra_range=pj)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    res['J_slab'] = {'quartets': sc.last_quartets, 's': dt, 'quartets_per_s': sc.last_quartets / dt,
+                     'extrapolated_whole_s': dt * total / max(sc.last_quartets, 1)}
+    g = torch.zeros((mol.natm, 3), dtype=torch.float64, device='cuda')
+    sc._run(J_GRAD, dmc, g=g, bra_range=(mid, mid + 2))
+    g.zero_()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sc._run(J_GRAD, dmc, g=g, bra_range=pg)
+    torch.cuda.synchronize()
+    dg = time.perf_counter() - t0
+    nq = sc.last_quartets
+    lst = _slab_list(sc, *pg)
+    route = IP1Gradient(mol, lst)
+    route.grad(dm)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g1 = route.grad(dm)
+    torch.cuda.synchronize()
+    di = time.perf_counter() - t0
+    route.close()
+    res['adjoint_slab'] = {'quartets': nq, 'listed_quartets': int(len(lst)), 'adjoint_s': dg,
+                           'ip1_route_s': di, 'adjoint_speedup_over_ip1': di / dg,
+                           'max_rel_diff_vs_ip1': float((g - g1).abs().max() / g1.abs().max()),
+                           'extrapolated_whole_adjoint_s': dg * total / max(nq, 1),
+                           'note': 'the adjoint time includes its chunk planning on host threads '
+                                   '(streamed); the ip1 route is timed without its planning'}
+    return res
+
+
 def extra_fp64peak():
     """Issue-rate peaks of this GPU (bench_fp64_peak.cu): DFMA, DMMA (FP64 tensor cores) and FFMA
     in TFLOP/s, the best launch shape of each."""
@@ -425,7 +582,9 @@ def run_gpu(args, rank, world):
               'df': lambda: extra_df(cg),
               'screening': lambda: extra_screening(cg, natm=args.c3_atoms),
               'int3c2e': lambda: extra_int3c2e(cg),
-              'fp64peak': extra_fp64peak}[args.only]
+              'fp64peak': extra_fp64peak,
+              'screened': lambda: extra_screened(cg),
+              'c4': lambda: extra_c4(cg)}[args.only]
         if rank == 0:
             print(json.dumps({'extra': args.only, **fn()}), flush=True)
         return
@@ -553,7 +712,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-extras', action='store_true', help='skip the side workloads (drop-in, int3c2e, adjoint, J/K, screening, DF)')
     ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk', 'df', 'screening',
-                                                          'fp64peak'],
+                                                          'fp64peak', 'screened', 'c4'],
                     help='run one side workload alone and print its line (profiling)')
     ap.add_argument('--c3-atoms', type=int, default=24, help='atoms of the adjoint workload')
     args = ap.parse_args()

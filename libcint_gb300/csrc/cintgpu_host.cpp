@@ -38,6 +38,8 @@
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -380,6 +382,32 @@ struct CINTGPUPlan {
 
 namespace {
 
+/* What an optimizer (int2e_optimizer & co.) keeps for the drop-in calls made with it: the shell
+ * pairs' primitive data (libcint's PairData, src/optimizer.c:288-342: product centres, screening
+ * values, prefactors), built on first use and shared by every thread calling with the same
+ * CINTOpt, which saves each later call that pair work.  Lives in a side table keyed by the
+ * CINTOpt pointer and is freed by CINTdel_optimizer. */
+struct OptPair {
+    CGPair pair;
+    std::vector<CGPrimPair> prims;
+    bool empty;
+};
+struct OptState {
+    std::mutex mu;
+    /* by primitive cutoff (int2e 61, int3c2e 60 by default), then pair_key */
+    std::map<double, std::unordered_map<uint64_t, std::unique_ptr<OptPair>>> pairs;
+};
+std::mutex g_opt_mu;
+std::unordered_map<const void *, std::shared_ptr<OptState>> g_opt_states;
+
+std::shared_ptr<OptState> opt_state(const void *opt)
+{
+    if (!opt) return nullptr;
+    std::lock_guard<std::mutex> lk(g_opt_mu);
+    auto it = g_opt_states.find(opt);
+    return it == g_opt_states.end() ? nullptr : it->second;
+}
+
 struct Builder {
     CINTGPUPlan *P;
     const int *atm;
@@ -391,6 +419,7 @@ struct Builder {
     std::vector<std::vector<double>> logmaxc;   /* per original shell index (empty: not yet) */
     const std::vector<int> *ao_loc = nullptr;     /* Cartesian AO offset per shell (J/adjoint) */
     const std::vector<int> *prim_loc = nullptr;   /* first primitive per shell (J/adjoint) */
+    OptState *opt = nullptr;                      /* optimizer pair cache (drop-in calls) */
 
     void locate(CGPair &p, int sa, const ShellView &A, int ca, int sb, const ShellView &B, int cb)
     {
@@ -427,6 +456,35 @@ struct Builder {
         const uint64_t key = pair_key(sa, ca, sb, cb, lsum, 0);
         const int found = pair_index.find(key);
         if (found >= 0) return found;
+        if (opt) {
+            OptPair *e = nullptr;
+            {
+                std::lock_guard<std::mutex> lk(opt->mu);
+                auto &m = opt->pairs[P->expcutoff];
+                auto it = m.find(key);
+                if (it != m.end()) e = it->second.get();
+            }
+            if (!e) {   /* build it in a scratch plan and publish it (entries never change) */
+                CINTGPUPlan scratch;
+                scratch.expcutoff = P->expcutoff;
+                Builder b2{&scratch, atm, natm, bas, env, {}, {}, {}};
+                const int id = b2.pair(sa, A, ca, sb, B, cb, lsum);
+                auto n = std::make_unique<OptPair>();
+                n->pair = scratch.pairs[id];
+                n->prims.assign(scratch.prims.begin(), scratch.prims.end());
+                n->empty = b2.pair_empty[id] != 0;
+                std::lock_guard<std::mutex> lk(opt->mu);
+                e = opt->pairs[P->expcutoff].emplace(key, std::move(n)).first->second.get();
+            }
+            CGPair p = e->pair;
+            p.prim_off = (int)P->prims.size();
+            P->prims.insert(P->prims.end(), e->prims.begin(), e->prims.end());
+            const int id = (int)P->pairs.size();
+            P->pairs.push_back(p);
+            pair_empty.push_back(e->empty ? 1 : 0);
+            pair_index.insert(key, id);
+            return id;
+        }
         CGPair p;
         for (int c = 0; c < 3; c++) { p.AB[c] = A.R[c] - B.R[c]; p.A[c] = A.R[c]; }
         p.prim_off = (int)P->prims.size();
@@ -560,7 +618,57 @@ double flops_per_primq(int li, int lj, int lk, int ll, int mode)
  * na = li + lj + 1 is the row length of the VRR arrays): the stage-3 groups, the permutations
  * from the transfer's Cartesian order to the accumulator rows/columns, and the transfer's buffer
  * size.  Layout described with CGEriClass. */
+static int build_eri_class_tables(CINTGPUPlan *P, int li, int lj, int lk, int ll, bool bra);
+
+/* The tables of a class depend on (li, lj, lk, ll, bra) alone: built once per process (the round
+ * cutting is a dynamic program over the groups) and appended to each plan that uses the class. */
+namespace {
+struct EriTables {
+    CGEriClass c;
+    std::vector<CGEriGroup> groups;
+    std::vector<int> perm, prog, rounds;
+};
+std::mutex g_eri_cache_mu;
+std::unordered_map<int, std::shared_ptr<const EriTables>> g_eri_cache;
+}  // namespace
+
 static int build_eri_class(CINTGPUPlan *P, int li, int lj, int lk, int ll, bool bra)
+{
+    const int key = (((li * 16 + lj) * 16 + lk) * 16 + ll) * 2 + (bra ? 1 : 0);
+    std::shared_ptr<const EriTables> t;
+    {
+        std::lock_guard<std::mutex> lk_(g_eri_cache_mu);
+        auto it = g_eri_cache.find(key);
+        if (it != g_eri_cache.end()) t = it->second;
+    }
+    if (!t) {
+        CINTGPUPlan tmp;
+        build_eri_class_tables(&tmp, li, lj, lk, ll, bra);
+        auto e = std::make_shared<EriTables>();
+        e->c = tmp.eclass[0];
+        e->groups = tmp.egroup;
+        e->perm = tmp.eperm;
+        e->prog = tmp.hprog;
+        e->rounds = tmp.eround;
+        std::lock_guard<std::mutex> lk_(g_eri_cache_mu);
+        t = g_eri_cache.emplace(key, e).first->second;
+    }
+    CGEriClass c = t->c;
+    c.group_off = (int)P->egroup.size();
+    c.perm_off = (int)P->eperm.size();
+    c.hprog_off = (int)P->hprog.size();
+    c.round_off = (int)P->eround.size();
+    P->egroup.insert(P->egroup.end(), t->groups.begin(), t->groups.end());
+    P->eperm.insert(P->eperm.end(), t->perm.begin(), t->perm.end());
+    P->hprog.insert(P->hprog.end(), t->prog.begin(), t->prog.end());
+    P->eround.insert(P->eround.end(), t->rounds.begin(), t->rounds.end());
+    P->hrr_max = std::max(P->hrr_max, c.hrr_need);
+    P->nef_max = std::max(P->nef_max, c.nE * c.nF);
+    P->eclass.push_back(c);
+    return (int)P->eclass.size() - 1;
+}
+
+static int build_eri_class_tables(CINTGPUPlan *P, int li, int lj, int lk, int ll, bool bra)
 {
     struct Side {
         std::vector<int> x, y, z0, nz, base, pidx;
@@ -887,7 +995,7 @@ static bool kind_sph(int kind)
 
 static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, const int64_t *offsets,
                       const int *atm, int natm, const int *bas, int nbas, const double *env,
-                      int64_t split_target)
+                      int64_t split_target, OptState *opt = nullptr)
 {
     (void)nbas;
     P->kind = kind;
@@ -930,6 +1038,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     P->natm = natm;
     Builder B{P, atm, natm, bas, env, {}, {}, {}};
     const bool contracting = P->jmode || P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA;
+    if (!contracting) B.opt = opt;   /* the cached pairs carry no AO / primitive offsets */
     std::vector<int> ao_loc, prim_loc;
     if (contracting) {
         ao_loc.resize(nbas + 1);
@@ -1063,8 +1172,22 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     struct Work { int pe; int64_t off, n; double cost_pq; };
     std::vector<Work> work;
     work.reserve(pend.size());
-    /* per-class constants, indexed by ((li 8 + lj) 8 + lk) 8 + ll (l <= 7 with derivatives) */
-    std::vector<double> cls_cost(8 * 8 * 8 * 8, -1.0), cls_ref(8 * 8 * 8 * 8, 0.0);
+    /* per-class constants: classes ((li 8 + lj) 8 + lk) 8 + ll (l <= 7 with derivatives) map to
+     * dense slots, so a plan of one quartet does not initialise tables for all 4096 */
+    std::vector<int16_t> cls_slot(8 * 8 * 8 * 8, -1);
+    std::vector<double> cls_cost, cls_ref;
+    std::vector<int> cls_group;
+    std::vector<CGLayout> cls_layout;
+    auto slot_of = [&](int ck) -> int {
+        if (cls_slot[ck] < 0) {
+            cls_slot[ck] = (int16_t)cls_cost.size();
+            cls_cost.push_back(-1.0);
+            cls_ref.push_back(0.0);
+            cls_group.push_back(-1);
+            cls_layout.emplace_back();
+        }
+        return cls_slot[ck];
+    };
     /* largest screening value of each pair's primitive pairs (NaN counts as +inf): when it is
      * within a ket primitive's limit every bra primitive pair survives and the test is skipped */
     std::vector<double> cce_max(P->pairs.size());
@@ -1126,7 +1249,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     for (size_t w = 0; w < npend; w++) {
         const Pending &pe = pend[w];
         const int64_t off = pos[w], n = pos[w + 1] - pos[w];
-        const int ck = ((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3];
+        const int ck = slot_of(((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3]);
         if (cls_cost[ck] < 0) {
             cls_cost[ck] = per_primitive(P, pe.l) ? flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3])
                          : flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3],
@@ -1170,15 +1293,13 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         }
         return swap_of[p] == 1;
     };
-    std::vector<int> cls_group(8 * 8 * 8 * 8, -1);
-    std::vector<CGLayout> cls_layout(8 * 8 * 8 * 8);
     struct TaskCost { CGTask t; double cost; int group; };
     std::vector<TaskCost> tc;
     std::unordered_map<int, int> grad_cls, eri_cls;
     int64_t gpos = 0;
     for (const Work &w : work) {
         const Pending &pe = pend[w.pe];
-        const int ck = ((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3];
+        const int ck = slot_of(((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3]);
         if (cls_group[ck] < 0) {
             CGLayout Lc;
             const int lmode = bra_term(P, pe.l) ? CG_MODE_ERIB : P->mode;
@@ -1538,12 +1659,16 @@ static int execute_plan(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
     const bool fo = fused(P);
     if (fo) CUDA_OK(cudaMemsetAsync(P->d_done, 0, sizeof(int) * std::max<size_t>(P->outs.size(), 1), stream));
     P->cur_out = out_dev;
-    bool fork = P->side && P->groups[1].ntasks > 0 && P->groups[0].ntasks > 0;
+    /* the 48 KB and per-primitive groups run on the side stream beside the regular group: their
+     * CTAs take SMs as the regular group's drain, so the launches' tails overlap */
+    const bool side_work = P->groups[1].ntasks > 0 || P->groups[2].ntasks > 0;
+    bool fork = P->side && side_work && P->groups[0].ntasks > 0;
     if (P->ev_t0) CUDA_OK(cudaEventRecord(P->ev_t0, stream));
     if (fork) {
         CUDA_OK(cudaEventRecord(P->ev_fork, stream));
         CUDA_OK(cudaStreamWaitEvent(P->side, P->ev_fork, 0));
         int rc = launch_group(P, 1, P->side);
+        if (!rc) rc = launch_group(P, 2, P->side);
         if (rc) return rc;
         CUDA_OK(cudaEventRecord(P->ev_join, P->side));
         rc = launch_group(P, 0, stream);
@@ -1552,10 +1677,7 @@ static int execute_plan(CINTGPUPlan *P, double *out_dev, cudaStream_t stream)
     } else {
         int rc = launch_group(P, 1, stream);
         if (!rc) rc = launch_group(P, 0, stream);
-        if (rc) return rc;
-    }
-    if (P->groups[2].ntasks > 0) {
-        int rc = launch_group(P, 2, stream);
+        if (!rc) rc = launch_group(P, 2, stream);
         if (rc) return rc;
     }
     if (P->ev_t1) {
@@ -1680,7 +1802,7 @@ std::atomic<int64_t> g_dropin_failures{0};
 
 /* One shell block through the GPU (the plain drop-in path). */
 CACHE_SIZE_T dropin(int kind, double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
-                    FINT *bas, FINT nbas, double *env)
+                    FINT *bas, FINT nbas, double *env, CINTOpt *opt = nullptr)
 {
     if (out == NULL) return cache_size_query(kind, shls, bas);
     const int nsh = kind_shells(kind);
@@ -1724,8 +1846,9 @@ CACHE_SIZE_T dropin(int kind, double *out, FINT *dims, FINT *shls, FINT *atm, FI
     }
     CINTGPUPlan P;
     P.fuse_out = false;   /* one quartet: a separate transform needs far less scratch */
+    std::shared_ptr<OptState> os = opt_state(opt);
     int rc = build_plan(&P, kind, shls, 1, NULL, atm, natm, bas, nbas, env,
-                        (int64_t)g_ctx.sm_count * 8);
+                        (int64_t)g_ctx.sm_count * 8, os.get());
     if (rc) return failed();
     size_t need = plan_device_bytes(&P);
     size_t up = plan_upload_bytes(&P);
@@ -1763,6 +1886,8 @@ void make_opt(CINTOpt **opt, FINT nbas)
 {
     CINTOpt *o = (CINTOpt *)calloc(1, sizeof(CINTOpt));
     o->nbas = nbas;
+    std::lock_guard<std::mutex> lk(g_opt_mu);
+    g_opt_states[o] = std::make_shared<OptState>();
     *opt = o;
 }
 }  // namespace
@@ -2499,49 +2624,49 @@ int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,
 /* ---- libcint drop-in ---------------------------------------------------------------------- */
 CACHE_SIZE_T int2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                        FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT2E_SPH, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int2e_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                         FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT2E_CART, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int2e_ip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                            FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_IP1_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT2E_IP1_SPH, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int2e_ip1_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                             FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_IP1_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT2E_IP1_CART, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int2e_ip2_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                            FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_IP2_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT2E_IP2_SPH, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int2e_ip2_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                             FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT2E_IP2_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT2E_IP2_CART, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int3c2e_ip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                              FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_IP1_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT3C2E_IP1_SPH, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int3c2e_ip1_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                               FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_IP1_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT3C2E_IP1_CART, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int3c2e_ip2_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                              FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_IP2_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT3C2E_IP2_SPH, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int3c2e_ip2_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                               FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_IP2_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT3C2E_IP2_CART, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int3c2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                          FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT3C2E_SPH, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int3c2e_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                           FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT3C2E_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT3C2E_CART, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int2c2e_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                          FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT2C2E_SPH, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT2C2E_SPH, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int2c2e_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                           FINT nbas, double *env, CINTOpt *opt, double *cache)
-{ (void)opt; (void)cache; return dropin(CINTGPU_INT2C2E_CART, out, dims, shls, atm, natm, bas, nbas, env); }
+{ (void)cache; return dropin(CINTGPU_INT2C2E_CART, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 
-/* The optimizer holds no precomputed data here: pair data are rebuilt per call on the host,
- * which is exactly what libcint's pair tables save it; the struct keeps libcint's layout. */
+/* The optimizer keeps libcint's CINTOpt layout; its content is the side table above (the shell
+ * pairs' primitive data, built on first use by the drop-in calls made with it). */
 void int2e_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
 { (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
 void int2e_ip1_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
@@ -2558,7 +2683,14 @@ void int3c2e_ip2_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT 
 { (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
 void CINTdel_2e_optimizer(CINTOpt **opt)
 {
-    if (opt && *opt) { free(*opt); *opt = NULL; }
+    if (opt && *opt) {
+        {
+            std::lock_guard<std::mutex> lk(g_opt_mu);
+            g_opt_states.erase(*opt);
+        }
+        free(*opt);
+        *opt = NULL;
+    }
 }
 void CINTdel_optimizer(CINTOpt **opt) { CINTdel_2e_optimizer(opt); }
 

@@ -45,12 +45,16 @@ def schwarz_from_diagonal(nbas, pairs, diag, cnt):
     return Q
 
 
-def pair_bounds(mol, pairs):
+def pair_bounds(mol, pairs, chunk=250000):
     """Q for the given shell pairs (rows (i, j)): sqrt(max |(ab|ab)|) over the pair's functions,
-    from one int2e_sph plan over the diagonal quartets (i, j, i, j) on the GPU."""
+    from int2e_sph plans over the diagonal quartets (i, j, i, j) on the GPU, `chunk` pairs per
+    plan (so millions of pairs do not need one plan's host and device tables at once)."""
+    pairs = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
+    if len(pairs) > chunk:
+        return np.concatenate([pair_bounds(mol, pairs[a:a + chunk], chunk)
+                               for a in range(0, len(pairs), chunk)])
     import torch
     from . import INT2E_SPH, Plan
-    pairs = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
     items = np.concatenate([pairs, pairs], 1).astype(np.int32)
     plan = Plan(INT2E_SPH, mol, items)
     out = torch.empty(plan.output_size, dtype=torch.float64, device='cuda')
@@ -145,11 +149,15 @@ class ScreenedCoulomb:
                                       ctypes.byref(n)), 'cintgpu_screened_run')
         self.last_quartets = int(n.value)
 
+    def dm_cart(self, dm):
+        """the spherical density in the Cartesian AO basis the kernels contract with"""
+        return (self.C.T @ dm @ self.C).contiguous()
+
     def get_jk(self, dm, with_j=True, with_k=True, bra_range=None):
         import torch
         from .coulomb import J_BUILD, JK_BUILD, K_BUILD
         kind = JK_BUILD if (with_j and with_k) else (J_BUILD if with_j else K_BUILD)
-        dmc = (self.C.T @ dm @ self.C).contiguous()
+        dmc = self.dm_cart(dm)
         XJ = torch.zeros_like(dmc) if with_j else None
         XK = torch.zeros_like(dmc) if with_k else None
         self._run(kind, dmc, XJ, XK, bra_range=bra_range)
@@ -165,7 +173,7 @@ class ScreenedCoulomb:
         import torch
         from .coulomb import J_GRAD, J_GRAD_EXP
         from .molecules import NPRIM_OF
-        dmc = (self.C.T @ dm @ self.C).contiguous()
+        dmc = self.dm_cart(dm)
         g = torch.zeros((self.mol.natm, 3), dtype=torch.float64, device='cuda')
         ga = (torch.zeros(int(self.mol.bas[:, NPRIM_OF].sum()), dtype=torch.float64, device='cuda')
               if with_exponents else None)
