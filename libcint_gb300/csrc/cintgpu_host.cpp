@@ -329,7 +329,7 @@ struct CINTGPUPlan {
                                       cintgpu_plan_create*; chunk plans are built in parallel) */
     int ws_kb = 0;                 /* shared memory per warp of the regular group in KB (0: the
                                       CINTGPU_WS_KB override or the default 24) */
-    int prim_l = 3;                /* int2e classes with ll >= prim_l (or lj >= prim_l when the
+    int prim_l = 4;                /* int2e classes with ll >= prim_l (or lj >= prim_l when the
                                       bra route does not take them) transfer per primitive
                                       (CINTGPU_PER_PRIMITIVE_L overrides, 0 = every class) */
     int bra_l = 2;                 /* classes with lj >= bra_l and ll < prim_l transfer the bra per
@@ -946,9 +946,10 @@ static void free_plan_device(CINTGPUPlan *p)
  * on uncancelled Cartesian elements of f-f transfers and ~5e-12 of the block scale on (fd|dd)
  * (libcint: 1.1e-10 and 7e-15); with lj or ll >= 4 it even leaves the 1e-12 absolute bar
  * ((ih|ih): 1.2e-12).  So:
- *   ll >= prim_l (default 3)          both transfers per primitive (CG_MODE_ERIP);
- *   lj >= bra_l (default 2), ll < prim_l   the bra transfer per term, the ket transfer (ll <= 2,
- *                                     whose amplification stays small) after contraction
+ *   ll >= prim_l (default 4)          both transfers per primitive (CG_MODE_ERIP);
+ *   lj >= bra_l (default 2), ll < prim_l   the bra transfer per term, the ket transfer (ll <= 3:
+ *                                     (ff|ff) keeps 8.8e-12 relative on uncancelled Cartesian
+ *                                     elements, 5% faster than per primitive) after contraction
  *                                     (CG_MODE_ERIB);
  *   otherwise                         both transfers after contraction (contraction first).
  * A class whose per-term arrays do not fit the largest per-warp shared memory falls back to the

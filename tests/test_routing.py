@@ -1,6 +1,6 @@
 """Task routing of the planner, CPU only (host planning, no device): int2e classes whose horizontal
-transfer after contraction would lose precision go elsewhere: kernel-order ll >= 3 to the
-per-primitive group when its g arrays fit, lj >= 3 with ll <= 2 to the bra-per-term tables of the
+transfer after contraction would lose precision go elsewhere: kernel-order ll >= 4 to the
+per-primitive group when its g arrays fit, lj >= 2 with ll <= 3 to the bra-per-term tables of the
 regular groups; CINTGPU_PER_PRIMITIVE_L and CINTGPU_BRA_TERM_L move the thresholds; plans
 transform their outputs inside the integral kernel."""
 import ctypes
@@ -54,16 +54,16 @@ def test_threshold_switch_and_fusion():
     ff = qs[(np.minimum(L[qs[:, 0]], L[qs[:, 1]]) == 3) | (np.minimum(L[qs[:, 2]], L[qs[:, 3]]) == 3)]
     K = np.stack([np.maximum(L[ff[:, 0]], L[ff[:, 1]]), np.minimum(L[ff[:, 0]], L[ff[:, 1]]),
                   np.maximum(L[ff[:, 2]], L[ff[:, 3]]), np.minimum(L[ff[:, 2]], L[ff[:, 3]])], 1)
-    ket_ff = (K[:, 1] == 3) & (K[:, 3] == 3)            # (ff|ff): both transfers per primitive
+    ket_ff = (K[:, 1] == 3) & (K[:, 3] == 3)            # (ff|ff)
     ff = np.concatenate([ff[~ket_ff][:40], ff[ket_ff][:10]])
     ket_ff = np.arange(len(ff)) >= 40
-    g = groups(cg.INT2E_SPH, mol, ff[~ket_ff])
+    g = groups(cg.INT2E_SPH, mol, ff)
     assert g[2] == 0 and g[4] == g[0] + g[1] > 0 and g[3] == 1   # bra per term, fused output
-    g = groups(cg.INT2E_SPH, mol, ff[ket_ff])
-    assert g[2] > 0 and g[0] + g[1] == 0 and g[4] == 0
+    g = groups(cg.INT2E_SPH, mol, ff[ket_ff], {'CINTGPU_PER_PRIMITIVE_L': '3'})
+    assert g[2] > 0 and g[0] + g[1] == 0 and g[4] == 0  # ll >= 3: both transfers per primitive
     g = groups(cg.INT2E_SPH, mol, ff, {'CINTGPU_BRA_TERM_L': '99', 'CINTGPU_PER_PRIMITIVE_L': '4'})
     assert g[2] == 0 and g[4] == 0          # the former default: f-f transfers contraction first
-    g = groups(cg.INT2E_SPH, mol, ff, {'CINTGPU_BRA_TERM_L': '99'})
+    g = groups(cg.INT2E_SPH, mol, ff, {'CINTGPU_BRA_TERM_L': '99', 'CINTGPU_PER_PRIMITIVE_L': '3'})
     assert g[0] + g[1] == 0 and g[2] > 0    # all of them per primitive
     g = groups(cg.INT2E_SPH, mol, qs[:200], {'CINTGPU_PER_PRIMITIVE_L': '0'})
     assert g[0] + g[1] == 0 and g[2] > 0    # every class per primitive
