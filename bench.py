@@ -39,10 +39,11 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-FP64_PEAK_TFLOPS = 1.196      # measured DFMA peak of this GB300 pool (bench.py --only fp64peak)
-# DRAM read + write of one integral-kernel launch per c1 quartet: 706.0 MB over the first 50k
-# quartets of the committed list (one ncu capture of that launch), scaled by quartets
-ERI_DRAM_BYTES_PER_QUARTET = 706.0e6 / 50000
+FP64_PEAK_TFLOPS = 1.257      # measured DFMA peak of this GB300 pool (bench.py --only fp64peak;
+                              # = 2 DFMA per SM per clock x 152 SMs x 2.07 GHz)
+# DRAM read + write of one integral-kernel launch per c1 quartet: 552.6 MB for the step's 100k
+# quartets (one ncu capture of that launch)
+ERI_DRAM_BYTES_PER_QUARTET = 552.6e6 / 100000
 SCHWARZ = 1e-12
 # one metric string for both arms, so the two lines are directly comparable
 METRIC = 'int2e_sph integrals/s (c1 Schwarz-screened quartets)'
@@ -411,10 +412,20 @@ def _screened_total(q, threshold):
     return int(k.sum()), k
 
 
+def _slab_range(k, nq):
+    """bra positions [p0, p1) that enumerate about nq quartets, starting where half of the whole
+    list has been enumerated (the median quartet, not the median pair: most distant pairs have
+    few partners)"""
+    cum = np.cumsum(k)
+    p0 = int(np.searchsorted(cum, cum[-1] / 2))
+    p1 = int(np.searchsorted(cum, cum[p0] - k[p0] + nq)) + 1
+    return p0, max(p0 + 1, min(p1, len(k)))
+
+
 def extra_screened(cg, natm_whole=12, slab_quartets=4.0e6, seed=0):
     """Whole-molecule Schwarz-screened J (c1, Q_ij Q_kl >= 1e-12) through
     cintgpu_screened_run, which never stores the quartet list: the bounds of all 583k c1 shell
-    pairs, a timed slab of bra pairs around the median bound (extrapolated to the whole list by
+    pairs, a timed slab of bra pairs from the median quartet on (extrapolated to the whole list by
     quartet count), and a whole c1-density molecule of natm_whole atoms timed end to end."""
     import torch
     from libcint_gb300 import molecules as M
@@ -433,10 +444,7 @@ def extra_screened(cg, natm_whole=12, slab_quartets=4.0e6, seed=0):
         t_q = time.perf_counter() - t0
         total, k = _screened_total(sc.q, SCHWARZ)
         if tag == 'c1':
-            mid = len(k) // 2
-            cum = np.cumsum(k[mid:])
-            p1 = mid + int(np.searchsorted(cum, slab_quartets)) + 1
-            rng_ = (mid, min(p1, len(k)))
+            rng_ = _slab_range(k, slab_quartets)
         else:
             rng_ = None
         sc.get_jk(dm, True, False, bra_range=rng_ if rng_ else (0, min(len(k), 64)))   # warm-up
@@ -473,8 +481,8 @@ def _slab_list(sc, p0, p1):
 def extra_c4(cg, seed=0, slab_j=1.5e6, slab_grad=1.5e5):
     """c4 at full size (400 atoms, 24 A, s:3 p:3 d:2 f:1 g:1, 1-8 primitives, 4000 shells, 8M
     shell pairs), Schwarz 1e-12: the bounds of every pair, the whole surviving list's size, a
-    timed J slab and a timed adjoint slab (bra pairs around the median bound; the list is streamed,
-    never stored), the int2e_ip1 route on the adjoint's slab (plans built outside the timed
+    timed J slab and a timed adjoint slab (bra pairs from the median quartet on; the list is
+    streamed, never stored), the int2e_ip1 route on the adjoint's slab (plans built outside the timed
     region) and the two gradients' agreement."""
     import torch
     from libcint_gb300 import molecules as M
@@ -490,10 +498,9 @@ def extra_c4(cg, seed=0, slab_j=1.5e6, slab_grad=1.5e5):
     torch.cuda.synchronize()
     t_q = time.perf_counter() - t0
     total, k = _screened_total(sc.q, SCHWARZ)
-    mid = len(k) // 2
-    cum = np.cumsum(k[mid:])
-    pj = (mid, mid + int(np.searchsorted(cum, slab_j)) + 1)
-    pg = (mid, mid + int(np.searchsorted(cum, slab_grad)) + 1)
+    pj = _slab_range(k, slab_j)
+    pg = _slab_range(k, slab_grad)
+    mid = pj[0]
     res = {'workload': 'c4: 400 atoms, 24 A, 3s3p2d1f1g, 1-8 prims, Schwarz 1e-12',
            'shell_pairs': int(len(sc.pairs)), 'bounds_s': t_q, 'surviving_quartets': total}
     from libcint_gb300.coulomb import J_BUILD, J_GRAD
@@ -543,19 +550,23 @@ def extra_fp64peak():
         subprocess.run(['nvcc', '-gencode', 'arch=compute_103a,code=sm_103a', '-O3', '-o', exe, src],
                        check=True)
         r = subprocess.run([exe], capture_output=True, text=True, check=True)
-    best = {}
+    best, lanes = {}, {}
     for line in r.stdout.splitlines():
         parts = line.split()
         if parts and parts[0] in ('DFMA', 'DMMA', 'FFMA') and line.endswith('TFLOP/s'):
             v = float(parts[-2])
             best[parts[0]] = max(best.get(parts[0], 0.0), v)
+        elif parts and parts[0] == 'DFMA-lanes':
+            lanes[parts[1].split('=')[1]] = float(parts[parts.index('G') - 1])
     return {'tflops': best, 'dmma_over_dfma': best.get('DMMA', 0) / max(best.get('DFMA', 1e-9), 1e-9),
+            'dfma_warp_instr_per_s_by_active_lanes': lanes,
             'raw': r.stdout.strip().splitlines()}
 
 
 def run_extras(cg, mol, qs, value, args):
     out = {}
-    for name, fn in (('dropin', lambda: extra_dropin(cg, mol, qs, value)),
+    for name, fn in (('fp64peak', lambda: {k: v for k, v in extra_fp64peak().items() if k != 'raw'}),
+                     ('dropin', lambda: extra_dropin(cg, mol, qs, value)),
                      ('int3c2e', lambda: extra_int3c2e(cg)),
                      ('adjoint', lambda: extra_adjoint(cg)),
                      ('jk', lambda: extra_jk(cg)),
@@ -591,7 +602,16 @@ def run_gpu(args, rank, world):
     mol = M.config1(seed=0)
     qs = load_quartets(args.quartets)
     nint = integrals_of(mol, qs)
-    plan = cg.Plan(cg.INT2E_SPH, mol, qs)
+    tuning = None
+    if args.tune:
+        # launch parameters picked by the autotuner on this list, before any timing
+        from libcint_gb300 import autotune
+        choice, times = autotune.tune(cg.INT2E_SPH, mol, qs)
+        tuning = {'choice': {'ws_kb': choice[0], 'separate_output': choice[1]},
+                  'candidate_ms': {'%d,%d' % c: round(t, 3) for c, t in times.items()}}
+        plan = cg.Plan(cg.INT2E_SPH, mol, qs, ws_kb=choice[0], separate_output=choice[1])
+    else:
+        plan = cg.Plan(cg.INT2E_SPH, mol, qs)
     out = torch.empty(plan.output_size, dtype=torch.float64, device='cuda')
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device='cuda')
     stream = torch.cuda.current_stream()
@@ -660,7 +680,7 @@ def run_gpu(args, rank, world):
                    'quartets_per_step': int(len(qs)), 'integrals_per_step': nint,
                    'prim_quartets_per_step': int(plan.prim_quartets),
                    'l2': 'flushed before every step (256 MiB memset), outside the step events',
-                   'wall_s_timed_region': wall},
+                   'wall_s_timed_region': wall, 'tuning': tuning},
         'quartets_per_s': len(qs) * world * args.steps / tot_s,
         'gpu_launches': plan.launches * args.steps,
         'roofline': {'bound': 'fp64', 'kernel': 'rys_eri_kernel_e0f0',
@@ -668,10 +688,10 @@ def run_gpu(args, rank, world):
                      'achieved': achieved, 'peak': FP64_PEAK_TFLOPS,
                      'unit': 'TFLOP/s', 'frac': achieved / FP64_PEAK_TFLOPS,
                      'traffic': ERI_DRAM_BYTES_PER_QUARTET * len(qs),
-                     'traffic_source': 'ncu dram__bytes_read+write of a 50k-quartet launch, '
-                                       'scaled to the step',
-                     'flop_model': 'this implementation: per term 20 + 15 VRR entries + groups '
-                                   '+ 2 nE nF (FMA = 2)',
+                     'traffic_source': 'ncu dram__bytes_read+write of the 100k-quartet step '
+                                       '(scaled by quartets for other lengths)',
+                     'flop_model': 'this implementation: per term 20 + 15 VRR entries (+ the bra '
+                                   'transfers of bra-per-term classes) + groups + 2 nE nF (FMA = 2)',
                      'libcint_algorithm_tflops': plan.flops_libcint * args.steps / kern_s / 1e12,
                      'libcint_algorithm_note': "the same quartets counted with libcint's "
                                                'per-primitive VRR + HRR + gout model, over the '
@@ -710,6 +730,8 @@ def main():
     ap.add_argument('--e2e-steps', type=int, default=3)
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-tune', dest='tune', action='store_false',
+                    help='default launch parameters instead of the autotuner\'s choice')
     ap.add_argument('--no-extras', action='store_true', help='skip the side workloads (drop-in, int3c2e, adjoint, J/K, screening, DF)')
     ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk', 'df', 'screening',
                                                           'fp64peak', 'screened', 'c4'],

@@ -41,6 +41,24 @@ __global__ void dfma_kernel(double *out, int iters, double a, double b) {
     for (int c = 0; c < NCHAIN; c++) s += acc[c];
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
+// the same chains on the first `active` lanes of every warp only: whether a partially active
+// warp instruction costs the FP64 pipe the time of a full one
+template<int NCHAIN>
+__global__ void dfma_lanes_kernel(double *out, int iters, double a, double b, int active) {
+    double s = 0;
+    if ((int)(threadIdx.x & 31) < active) {
+        double acc[NCHAIN];
+#pragma unroll
+        for (int c = 0; c < NCHAIN; c++) acc[c] = threadIdx.x * 1e-3 + c;
+        for (int i = 0; i < iters; i++) {
+#pragma unroll
+            for (int c = 0; c < NCHAIN; c++) acc[c] = fma(acc[c], a, b);
+        }
+#pragma unroll
+        for (int c = 0; c < NCHAIN; c++) s += acc[c];
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
 template<int NCHAIN>
 __global__ void ffma_kernel(float *out, int iters, float a, float b) {
     float acc[NCHAIN];
@@ -86,6 +104,20 @@ int main() {
         float ms; cudaEventElapsedTime(&ms, e0, e1);
         double flops = 512.0 * 4 * iters * (double)blocks * (threads / 32);
         printf("DMMA threads=%d blocks/sm=%d : %.3f ms  %.3f TFLOP/s\n", threads, bps, ms, flops / ms / 1e9);
+    }
+    {
+        const int threads = 256, blocks = sms * 2, iters = 20000;
+        const int lanes[] = {32, 16, 8, 4, 1};
+        for (int k : lanes) {
+            dfma_lanes_kernel<8><<<blocks, threads>>>(dout, 100, 0.999, 1e-3, k);
+            cudaEventRecord(e0);
+            dfma_lanes_kernel<8><<<blocks, threads>>>(dout, iters, 0.999, 1e-3, k);
+            cudaEventRecord(e1); cudaEventSynchronize(e1);
+            float ms; cudaEventElapsedTime(&ms, e0, e1);
+            double warp_instr = 8.0 * iters * (double)blocks * (threads / 32);
+            printf("DFMA-lanes active=%d threads=%d blocks/sm=2 : %.3f ms  %.3f G warp-instr/s\n", k, threads,
+                   ms, warp_instr / ms / 1e6);
+        }
     }
     float *fout = (float*)dout;
     for (auto &c : cfgs) {

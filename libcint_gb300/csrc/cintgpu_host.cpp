@@ -298,6 +298,7 @@ struct CINTGPUPlan {
     int three = 0;                 /* int3c2e and int2c2e: slot 3 is a unit s partner */
     int two = 0;                   /* int2c2e: slot 1 is a unit s partner as well */
     int jmode = 0;                 /* J (bit 0) / K (bit 1) contraction instead of stored integrals */
+    int gradj = 0;                 /* J_GRAD: contraction-first adjoint kernel (CG_MODE_GRADJ) */
     int nao_cart = 0;
     int natm = 0;
     int64_t nprim_tot = 0;
@@ -601,6 +602,23 @@ double flops_per_primq(int li, int lj, int lk, int ll, int mode)
         double nfr = 0;
         for (int l = lk; l <= lk + ll; l++) nfr += nc(l);
         return n * (20 + 3 * 5 * vrr2 + 3 * 2 * hrr_bra + nij * nc(lk + ll) + 2 * nij * nfr);
+    }
+    if (mode == CG_MODE_GRADJ) {
+        /* contraction-first adjoint: VRR to (li+lj+1, lk+ll+1); per side three contractions
+         * (z, y, x; 2 flops per product) and the sums over terms (bra: 3 per e', ket: 2 per f';
+         * the derivative weights are per task and not counted) */
+        auto nc = [](int l) { return (l + 1) * (l + 2) / 2; };
+        auto np2 = [](int l) { return (l + 1) * (l + 2) / 2.0; };
+        auto ntet = [](int l) { return l < 0 ? 0.0 : (l + 1) * (l + 2) * (l + 3) / 6.0; };
+        const int Le = li + lj, Lf = lk + ll;
+        double nE = 0, nF = 0;
+        for (int l = li; l <= Le; l++) nE += nc(l);
+        for (int l = lk; l <= Lf; l++) nF += nc(l);
+        const double na = Le + 2, nm = Lf + 2;
+        const double nEp = ntet(Le + 1) - ntet(li - 2), nFp = ntet(Lf + 1) - ntet(lk - 2);
+        const double bra = 2 * nF * na + 2 * np2(Le + 1) * np2(Lf) + nEp * (2 * (Lf + 1) + 5);
+        const double ket = 2 * nE * nm + 2 * np2(Lf + 1) * np2(Le) + nFp * (2 * (Le + 1) + 3);
+        return n * (20 + 3 * 5 * na * nm + bra + ket);
     }
     double per_root = 20 + 3 * 5 * vrr + 3 * 2 * hrr;
     if (mode == CG_MODE_IP1) per_root += 3 * 3 * (double)L.G / L.dI * (L.dI - 1) + 9.0 * L.nf;
@@ -969,6 +987,12 @@ static bool bra_term(const CINTGPUPlan *P, const int *l)
     cg_layout(l[0], l[1], l[2], l[3], CG_MODE_ERIB, CG_WS_MAX, &L);
     return L.T >= 1;
 }
+/* kernel (layout) mode of one class */
+static int class_mode(const CINTGPUPlan *P, const int *l)
+{
+    if (P->mode == CG_MODE_GRAD && P->gradj) return CG_MODE_GRADJ;
+    return bra_term(P, l) ? CG_MODE_ERIB : P->mode;
+}
 static bool per_primitive(const CINTGPUPlan *P, const int *l)
 {
     if (P->mode != CG_MODE_ERI || (l[1] < P->prim_l && l[3] < P->prim_l)) return false;
@@ -1020,7 +1044,14 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     case CINTGPU_J_BUILD: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; P->jmode = 1; break;
     case CINTGPU_K_BUILD: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; P->jmode = 2; break;
     case CINTGPU_JK_BUILD: P->mode = CG_MODE_ERI; P->sph = 0; P->three = 0; P->jmode = 3; break;
-    case CINTGPU_J_GRAD: P->mode = CG_MODE_GRAD; P->sph = 0; P->three = 0; break;
+    case CINTGPU_J_GRAD:
+        P->mode = CG_MODE_GRAD; P->sph = 0; P->three = 0;
+        /* CINTGPU_ADJOINT=component: the per-component adjoint kernel instead */
+        {
+            const char *e = getenv("CINTGPU_ADJOINT");
+            P->gradj = !(e && strcmp(e, "component") == 0);
+        }
+        break;
     case CINTGPU_J_GRAD_EXP: P->mode = CG_MODE_GRADA; P->sph = 0; P->three = 0; break;
     default: set_error("unknown integral kind %d", kind); return CINTGPU_ERR_ARG;
     }
@@ -1253,8 +1284,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         const int ck = slot_of(((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3]);
         if (cls_cost[ck] < 0) {
             cls_cost[ck] = per_primitive(P, pe.l) ? flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3])
-                         : flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3],
-                                           bra_term(P, pe.l) ? CG_MODE_ERIB : P->mode);
+                         : flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3], class_mode(P, pe.l));
             cls_ref[ck] = P->mode == CG_MODE_ERI ? flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3]) : 0.0;
         }
         const double cpq = cls_cost[ck];
@@ -1303,7 +1333,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         const int ck = slot_of(((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3]);
         if (cls_group[ck] < 0) {
             CGLayout Lc;
-            const int lmode = bra_term(P, pe.l) ? CG_MODE_ERIB : P->mode;
+            const int lmode = class_mode(P, pe.l);
             cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], lmode, ws_small, &Lc);
             cls_group[ck] = 0;
             if (per_primitive(P, pe.l)) {
@@ -1338,7 +1368,9 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         o.cart_off = gpos;
         int cls = 0;
         const int key = ((pe.l[0] * 16 + pe.l[1]) * 16 + pe.l[2]) * 16 + pe.l[3];
-        if (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) {
+        if (P->gradj) {
+            cls = -1;   /* contraction-first adjoint: no per-class tables */
+        } else if (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA) {
             auto it = grad_cls.find(key);
             cls = it != grad_cls.end() ? it->second
                                        : (grad_cls[key] = build_grad_class(P, pe.l[0], pe.l[1], pe.l[2], pe.l[3]));
@@ -1394,7 +1426,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         P->groups[g].ntasks = (int)P->tasks.size() - P->groups[g].task0;
         P->groups[g].ws = g == 0 ? ws_small : CG_WS_MAX;
         P->groups[g].blocks_per_sm = (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA)
-                                         ? cg_grad_blocks_per_sm(P->mode, P->groups[g].ws)
+                                         ? cg_grad_blocks_per_sm(P->gradj ? CG_MODE_GRADJ : P->mode, P->groups[g].ws)
                                          : cg_blocks_per_sm(g == 2 ? CG_MODE_ERIP : P->mode, P->groups[g].ws);
         P->groups[g].nblocks = std::min(std::max(1, g_ctx.sm_count) * P->groups[g].blocks_per_sm,
                                         std::max(1, (P->groups[g].ntasks + 3) / 4));
@@ -1464,7 +1496,7 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     const bool grad = P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA;
     /* per-warp slots: J mode holds (e0|f0) and two transfer buffers, the adjoint a cotangent */
     D.wstride = P->jmode ? (int64_t)P->nef_max + 2 * (int64_t)P->hrr_max : (int64_t)P->max_nf;
-    if (P->jmode || (grad && P->max_nf > CG_W_SMEM)) {
+    if (P->jmode || (grad && !P->gradj && P->max_nf > CG_W_SMEM)) {
         D.wwarps = g_ctx.sm_count * 4 * (P->groups[0].blocks_per_sm + P->groups[1].blocks_per_sm
                                          + P->groups[2].blocks_per_sm);
         D.wscr = al(sizeof(double) * (size_t)D.wwarps * D.wstride);
@@ -1589,7 +1621,7 @@ static int launch_grad_group(CINTGPUPlan *P, int g, cudaStream_t stream)
         L.wglobal += (size_t)g_ctx.sm_count * 4 * P->groups[0].blocks_per_sm * P->max_nf;
     L.wstride = P->max_nf;
     const int nblocks = G.nblocks;
-    int rc = cg_launch_grad(&L, P->mode, nblocks, stream);
+    int rc = cg_launch_grad(&L, P->gradj ? CG_MODE_GRADJ : P->mode, nblocks, stream);
     if (rc) { set_error("adjoint kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
     return 0;
 }
@@ -1978,7 +2010,11 @@ double cintgpu_plan_flops_libcint(const CINTGPUPlan *plan) { return plan->flops_
 int64_t cintgpu_plan_prim_quartets(const CINTGPUPlan *plan) { return plan->prim_quartets; }
 int cintgpu_plan_launches(const CINTGPUPlan *plan)
 {
-    return (plan->groups[0].ntasks > 0) + (plan->groups[1].ntasks > 0) + (plan->groups[2].ntasks > 0) + 1;
+    /* the task groups with work, and the output kernel when execute_plan launches it */
+    const bool contracting = plan->jmode || plan->mode == CG_MODE_GRAD || plan->mode == CG_MODE_GRADA;
+    const bool output = !contracting && !(fused(plan) && plan->empty_outs.empty());
+    return (plan->groups[0].ntasks > 0) + (plan->groups[1].ntasks > 0) + (plan->groups[2].ntasks > 0)
+         + (output ? 1 : 0);
 }
 int64_t cintgpu_plan_upload_bytes(const CINTGPUPlan *plan) { return (int64_t)plan_upload_bytes(plan); }
 

@@ -34,6 +34,29 @@ static __device__ double g_c2s_val[C2S_ROWS * C2S_MAXNNZ];
 /* ------------------------------------------------------------------ layout per class */
 __host__ __device__ inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
 
+/* Triangle and tetrahedron indexing of Cartesian power tuples: pairs (x, y) with x + y <= L in
+ * x-major order, triples (x, y, z) with x + y + z <= L likewise (the contraction-first adjoint
+ * keeps its density and contraction arrays in these layouts). */
+__host__ __device__ inline int cg_np2(int L) { return L < 0 ? 0 : (L + 1) * (L + 2) / 2; }
+__host__ __device__ inline int cg_ntet(int L) { return L < 0 ? 0 : (L + 1) * (L + 2) * (L + 3) / 6; }
+__host__ __device__ inline int cg_idx2(int L, int x, int y) { return x * (2 * L + 3 - x) / 2 + y; }
+__host__ __device__ inline int cg_idx3(int L, int x, int y, int z)
+{
+    return cg_ntet(L) - cg_ntet(L - x) + cg_idx2(L - x, y, z);
+}
+__host__ __device__ inline void cg_dec2(int L, int idx, int &x, int &y)
+{
+    x = 0;
+    while (idx > L - x) { idx -= L - x + 1; x++; }
+    y = idx;
+}
+__host__ __device__ inline void cg_dec3(int L, int idx, int &x, int &y, int &z)
+{
+    x = 0;
+    while (idx >= cg_np2(L - x)) { idx -= cg_np2(L - x); x++; }
+    cg_dec2(L - x, idx, y, z);
+}
+
 /* Per-mode increments of the four g-array axes: derivatives raise the angular momentum the
  * recurrences must reach (ip1: i+1, libcint grad2.c ng = {1,0,0,0,...}; coordinate adjoint:
  * i+1, j+1, k+1; exponent adjoint: +2 on all four). */
@@ -74,7 +97,32 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     L->scr |= 1;
     const bool grad = mode == CG_MODE_GRAD || mode == CG_MODE_GRADA;
     int T = 0;
-    if (mode == CG_MODE_ERI) {
+    if (mode == CG_MODE_GRADJ) {
+        /* contraction-first adjoint: per term a record (stage-1 values, 2a 2b 2c, m b01), the VRR
+         * arrays g(e, f) for e <= li+lj+1, f <= lk+ll+1, and the buffers of one side's axis-by-axis
+         * contraction; per task the transferred densities with their AB derivatives and the
+         * per-entry sums over terms (three on the bra, two on the ket) */
+        const int Le = li + lj, Lf = lk + ll;
+        L->nroots = (lsum + 1) / 2 + 1;
+        L->nmax = Le + 1;
+        L->mmax = Lf + 1;
+        const int na = L->nmax + 1, nm = L->mmax + 1;
+        L->G = na * nm;
+        L->gax = L->G | 1;
+        L->gstride = 3 * L->gax;
+        L->termw = (13 + nm) | 1;
+        const int bufb = cg_np2(Lf) * na + (Lf + 1) * cg_np2(L->nmax);
+        const int bufk = cg_np2(Le) * nm + (Le + 1) * cg_np2(L->mmax);
+        L->scr = (bufb > bufk ? bufb : bufk) | 1;
+        const int fixed = 4 * cg_ntet(Le) + 4 * cg_ntet(Lf) + 3 * cg_ntet(Le + 1) + 2 * cg_ntet(Lf + 1);
+        T = (ws_doubles - fixed) / (L->termw + L->gstride + L->scr);
+        if (T > 32) T = 32;
+        if (T < 0) T = 0;
+        L->off_dij = L->off_dkl = L->off_aacc = 0;
+        L->off_w = fixed;                          /* term records */
+        L->off_g = fixed + T * L->termw;
+        L->off_scr = L->off_g + T * L->gstride;
+    } else if (mode == CG_MODE_ERI) {
         /* contraction first: per term only the VRR arrays g(e, f), e <= li+lj, f <= lk+ll; term
          * records hold the 10 stage-1 values and m b01 for m <= mmax (odd length) */
         L->G = (L->nmax + 1) * (L->mmax + 1);

@@ -233,6 +233,314 @@ rys_grad_kernel(CGGradLaunch P)
     }
 }
 
+/* ------------------------------------------------------------------------------------------
+ * Contraction-first adjoint (coordinates), CG_MODE_GRADJ.
+ *
+ * The energy of one unique quartet is E = sum D_ij D_kl (ij|kl) (w_q folded into D_ij).  The
+ * horizontal transfer is linear and depends only on AB = A - B (bra) and CD = C - D (ket):
+ * (ij| = sum_e Tb(AB)[ij, e] (e0|, with Tb the binomial expansion of (x - B) = (x - A) + AB on
+ * each axis (libcint's CINTg0_2e_lj2d4d relation, src/g2e.c:560-693, applied symbolically).  So
+ * E = sum_{e,f} De Df (e0|f0) with the transferred densities De = sum_ij D_ij Tb[ij, e] and
+ * Df = sum_kl D_kl Tk[kl, f], formed once per task.  Differentiating every factor that moves:
+ *
+ *   dE/dA_x = sum De Df [2a (e+1x 0|f0) - e_x (e-1x 0|f0)] + sum dDe/dAB_x Df (e0|f0)
+ *   dE/dB_x = sum De Df 2b [(e+1x 0|f0) + AB_x (e0|f0)]    - sum dDe/dAB_x Df (e0|f0)
+ *   dE/dC_x = sum De Df [2c (e0|f+1x 0) - f_x (e0|f-1x 0)] + sum De dDf/dCD_x (e0|f0)
+ *
+ * (a, b, c: the term's primitive exponents on I, J, K; the Gaussian derivatives of libcint's
+ * nabla, src/g2e.c:4550-4591; D by translational invariance).  Per term the bra quantities need
+ * only Phi[e'] = sum_f Df (e'0|f0) for |e'| in [li-1, li+lj+1], contracted axis by axis (sum
+ * factorisation: z, then y, then x), and the ket ones Psi[f'] = sum_e De (e0|f'0) likewise:
+ *
+ *   Om[fx,fy][ez'] = sum_fz Df[f] gz(ez', fz)      Xi[fx][ey',ez'] = sum_fy gy(ey', fy) Om[fx,fy][ez']
+ *   Phi[e']        = sum_fx gx(ex', fx) Xi[fx][ey',ez']
+ *
+ * The derivative weights are linear in Phi, so only S1 = sum Phi, Sa = sum 2a Phi and
+ * Sb = sum 2b Phi over the task's terms are kept (per e', by the lane owning e'), and the weights
+ * are applied once per task:
+ *
+ *   dE/dA_x = sum_e' Sa[e'] De[e'-1x] + S1[e'] (dDe_x[e'] - (e'_x + 1) De[e'+1x])
+ *   dE/dB_x = sum_e' Sb[e'] (De[e'-1x] + AB_x De[e']) - S1[e'] dDe_x[e']
+ *
+ * (C likewise from Psi).  No Cartesian component of (ij|kl) is formed: the cost per term grows
+ * like l^5 instead of the l^8 of the per-component adjoint above.
+ * ------------------------------------------------------------------------------------------ */
+__constant__ double c_binom5[5][5] = {{1, 0, 0, 0, 0}, {1, 1, 0, 0, 0}, {1, 2, 1, 0, 0},
+                                      {1, 3, 3, 1, 0}, {1, 4, 6, 4, 1}};
+
+__device__ __forceinline__ double ipow_small(double x, int p)
+{
+    double r = 1.0;
+    for (int i = 0; i < p; i++) r *= x;
+    return r;
+}
+
+/* Transferred density of one pair (shells la at A, lb at B = A - AB), tetrahedron layout over
+ * |e| <= la + lb (zero below la): Dout[e] = sum_ij w D_ij Tb[ij, e] and its derivatives along AB
+ * dDout[ax][e].  One lane per e. */
+__device__ __forceinline__ void cg_pair_density(const double *__restrict__ dm, int nao, const CGPair &pr,
+                                                double w, double *Dout, double *dDout, int lane)
+{
+    const int la = pr.la, lb = pr.lb, L = la + lb, t = cg_ntet(L);
+    const int nfa = ncart(la), nfb = ncart(lb);
+    for (int e = lane; e < t; e += 32) {
+        int ex, ey, ez;
+        cg_dec3(L, e, ex, ey, ez);
+        double v = 0.0, d0 = 0.0, d1 = 0.0, d2 = 0.0;
+        if (ex + ey + ez >= la) {
+            for (int ci = 0; ci < nfa; ci++) {
+                int ix, iy, iz;
+                cart_pow(la, ci, ix, iy, iz);
+                const int kx = ex - ix, ky = ey - iy, kz = ez - iz;
+                if (kx < 0 || ky < 0 || kz < 0) continue;
+                for (int cj = 0; cj < nfb; cj++) {
+                    int jx, jy, jz;
+                    cart_pow(lb, cj, jx, jy, jz);
+                    const int px = jx - kx, py = jy - ky, pz = jz - kz;
+                    if (px < 0 || py < 0 || pz < 0) continue;
+                    const double d = w * __ldg(dm + (size_t)(pr.ao_a + ci) * nao + pr.ao_b + cj);
+                    const double c = d * c_binom5[jx][kx] * c_binom5[jy][ky] * c_binom5[jz][kz];
+                    const double qx = ipow_small(pr.AB[0], px), qy = ipow_small(pr.AB[1], py);
+                    const double qz = ipow_small(pr.AB[2], pz);
+                    v = fma(c * qx, qy * qz, v);
+                    if (px) d0 = fma(c * (double)px * ipow_small(pr.AB[0], px - 1), qy * qz, d0);
+                    if (py) d1 = fma(c * (double)py * ipow_small(pr.AB[1], py - 1), qx * qz, d1);
+                    if (pz) d2 = fma(c * (double)pz * ipow_small(pr.AB[2], pz - 1), qx * qy, d2);
+                }
+            }
+        }
+        Dout[e] = v;
+        dDout[e] = d0;
+        dDout[t + e] = d1;
+        dDout[2 * t + e] = d2;
+    }
+}
+
+/* One side's weights applied to its sums (lane-owned entries e' over |e'| <= L + 1, |e'| >= emin):
+ * gP_x += sum Sp[e'] D[e'-1x] + S1[e'] (dD_x[e'] - (e'_x + 1) D[e'+1x]) for the base centre and,
+ * with Sq given, gQ_x += sum Sq[e'] (D[e'-1x] + AB_x D[e']) - S1[e'] dD_x[e'] for the partner. */
+__device__ __forceinline__ void cg_side_weights(const double *D, const double *dD, int L, int emin,
+                                                const double *AB, const double *S1, const double *Sp,
+                                                const double *Sq, double gP[3], double gQ[3], int lane)
+{
+    const int t = cg_ntet(L), t1 = cg_ntet(L + 1);
+    for (int e = lane; e < t1; e += 32) {
+        int x[3];
+        cg_dec3(L + 1, e, x[0], x[1], x[2]);
+        const int s = x[0] + x[1] + x[2];
+        if (s < emin) continue;
+        const int me = s <= L ? cg_idx3(L, x[0], x[1], x[2]) : -1;
+        const double d0 = me >= 0 ? D[me] : 0.0;
+        const double s1 = S1[e], sp = Sp[e], sq = Sq ? Sq[e] : 0.0;
+#pragma unroll
+        for (int ax = 0; ax < 3; ax++) {
+            int y[3] = {x[0], x[1], x[2]};
+            double dp = 0.0, dmn = 0.0;
+            if (s + 1 <= L) { y[ax]++; dp = D[cg_idx3(L, y[0], y[1], y[2])]; y[ax]--; }
+            if (x[ax] >= 1) { y[ax]--; dmn = D[cg_idx3(L, y[0], y[1], y[2])]; }
+            const double tt = me >= 0 ? dD[ax * t + me] : 0.0;
+            gP[ax] += fma(sp, dmn, s1 * fma(-(double)(x[ax] + 1), dp, tt));
+            if (Sq) gQ[ax] += fma(sq, fma(AB[ax], d0, dmn), -s1 * tt);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128, 2)
+rys_gradj_kernel(CGGradLaunch P)
+{
+    extern __shared__ double smem[];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    double *ws = smem + (size_t)warp * P.ws_doubles;
+
+    for (;;) {
+        int tid = 0;
+        if (lane == 0) tid = atomicAdd(P.counter, 1);
+        tid = __shfl_sync(FULL, tid, 0);
+        if (tid >= P.ntasks) break;
+        const CGTask tk = P.tasks[tid];
+        const CGPair pij = P.pairs[tk.pij];
+        const CGPair pkl = P.pairs[tk.pkl];
+        const int li = pij.la, lj = pij.lb, lk = pkl.la, ll = pkl.lb;
+        CGLayout L;
+        cg_class_layout(li, lj, lk, ll, CG_MODE_GRADJ, P.ws_doubles, &L);
+        if (L.T < 1) {
+            if (lane == 0) atomicOr(P.status, 1);
+            continue;
+        }
+        const int T = L.T, n = L.nroots, gax = L.gax, gstride = L.gstride, bstride = L.scr;
+        const int Le = li + lj, Lf = lk + ll, nmax = L.nmax, mmax = L.mmax;
+        const int na = nmax + 1, nm = mmax + 1;
+        const int tE = cg_ntet(Le), tE1 = cg_ntet(Le + 1), tF = cg_ntet(Lf), tF1 = cg_ntet(Lf + 1);
+        /* per task: transferred densities, then the sums over terms of Phi, 2a Phi, 2b Phi (bra,
+         * per e') and of Psi, 2c Psi (ket, per f'); the lane e' mod 32 owns entry e' */
+        double *De = ws, *dDe = De + tE, *Df = dDe + 3 * tE, *dDf = Df + tF;
+        double *S1 = dDf + 3 * tF, *Sa = S1 + tE1, *Sb = Sa + tE1, *S1k = Sb + tE1, *Sc = S1k + tF1;
+        double *term = ws + L.off_w;
+        double *greg = ws + L.off_g;
+        double *buf = ws + L.off_scr;
+        const CGPrimPair *__restrict__ ppij = P.prims + pij.prim_off;
+        const CGPrimPair *__restrict__ ppkl = P.prims + pkl.prim_off;
+        const int *__restrict__ pql = P.pqlist + tk.pq_off;
+        const int nij = pij.npa * pij.npb;
+        const double common = P.common_base * common_fac_sp(li) * common_fac_sp(lj)
+                            * common_fac_sp(lk) * common_fac_sp(ll);
+        const double wq = 0.5 * ((tk.sym & 1) ? 2.0 : 1.0) * ((tk.sym & 2) ? 2.0 : 1.0)
+                        * ((tk.sym & 4) ? 2.0 : 1.0);
+        cg_pair_density(P.dm, P.nao, pij, wq, De, dDe, lane);
+        cg_pair_density(P.dm, P.nao, pkl, 1.0, Df, dDf, lane);
+        for (int e = lane; e < 3 * tE1 + 2 * tF1; e += 32) S1[e] = 0.0;
+        __syncwarp();
+
+        const int nOm = cg_np2(Lf) * na, q2 = cg_np2(nmax);
+        const int nOk = cg_np2(Le) * nm, q2k = cg_np2(mmax);
+        const int emin = li > 0 ? li - 1 : 0, fmin = lk > 0 ? lk - 1 : 0;
+        const int nterm = tk.npq * n;
+        for (int t0 = 0; t0 < nterm; t0 += T) {
+            const int Tb = min(T, nterm - t0);
+            /* ---- stage 1: one lane per term */
+            if (lane < Tb) {
+                int g = t0 + lane;
+                int p = g / n, r = g - p * n;
+                int q = __ldg(pql + p);
+                int kl = q / nij, ij = q - kl * nij;
+                const CGPrimPair A = ppij[ij];
+                const CGPrimPair B = ppkl[kl];
+                double *rec = term + lane * L.termw;
+                cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec, P.omega2);
+                rec[10] = 2.0 * A.aA;
+                rec[11] = 2.0 * (A.a - A.aA);
+                rec[12] = 2.0 * B.aA;
+                double mb = 0.0;
+                for (int m = 0; m <= mmax; m++) { rec[13 + m] = mb; mb += rec[2]; }
+            }
+            __syncwarp();
+            /* ---- stage 2: VRR, one lane per (term, axis) */
+            for (int item = lane; item < 3 * Tb; item += 32) {
+                int t = item / 3, ax = item - 3 * t;
+                const double *rec = term + t * L.termw;
+                vrr_axis(nmax, mmax, rec[0], rec[1], rec + 13, rec[3 + ax], rec[6 + ax],
+                         ax == 2 ? rec[9] : 1.0, greg + (size_t)t * gstride + ax * gax);
+            }
+            __syncwarp();
+            /* ---- bra side: Om (z), Xi (y), then Phi (x) into the lane-owned sums */
+            for (int it = lane; it < Tb * nOm; it += 32) {
+                const int t = it % Tb, r = it / Tb;
+                const int ez = r % na, p = r / na;
+                int fx, fy;
+                cg_dec2(Lf, p, fx, fy);
+                const double *gz = greg + (size_t)t * gstride + 2 * gax;
+                const double *df = Df + cg_idx3(Lf, fx, fy, 0);
+                const int zlo = max(0, lk - fx - fy), zhi = Lf - fx - fy;
+                double s = 0.0;
+                for (int fz = zlo; fz <= zhi; fz++) s = fma(df[fz], gz[ez + na * fz], s);
+                buf[(size_t)t * bstride + p * na + ez] = s;
+            }
+            __syncwarp();
+            for (int it = lane; it < Tb * (Lf + 1) * q2; it += 32) {
+                const int t = it % Tb, r = it / Tb;
+                const int q = r % q2, fx = r / q2;
+                int ey, ez;
+                cg_dec2(nmax, q, ey, ez);
+                const double *gy = greg + (size_t)t * gstride + gax;
+                const double *om = buf + (size_t)t * bstride;
+                double s = 0.0;
+                for (int fy = 0; fy <= Lf - fx; fy++)
+                    s = fma(gy[ey + na * fy], om[cg_idx2(Lf, fx, fy) * na + ez], s);
+                buf[(size_t)t * bstride + nOm + fx * q2 + q] = s;
+            }
+            __syncwarp();
+            for (int e = lane; e < tE1; e += 32) {
+                int x0, x1, x2;
+                cg_dec3(nmax, e, x0, x1, x2);
+                if (x0 + x1 + x2 < emin) continue;
+                const int ixi = nOm + cg_idx2(nmax, x1, x2);
+                double s1 = S1[e], sa = Sa[e], sb = Sb[e];
+                for (int t = 0; t < Tb; t++) {
+                    const double *gx = greg + (size_t)t * gstride + x0;
+                    const double *xi = buf + (size_t)t * bstride + ixi;
+                    double phi = 0.0;
+                    for (int fx = 0; fx <= Lf; fx++) phi = fma(gx[na * fx], xi[fx * q2], phi);
+                    const double *rec = term + t * L.termw;
+                    s1 += phi;
+                    sa = fma(rec[10], phi, sa);
+                    sb = fma(rec[11], phi, sb);
+                }
+                S1[e] = s1;
+                Sa[e] = sa;
+                Sb[e] = sb;
+            }
+            __syncwarp();
+            /* ---- ket side: the same with the pairs' roles exchanged, sums of Psi and 2c Psi */
+            for (int it = lane; it < Tb * nOk; it += 32) {
+                const int t = it % Tb, r = it / Tb;
+                const int fz = r % nm, p = r / nm;
+                int ex, ey;
+                cg_dec2(Le, p, ex, ey);
+                const double *gz = greg + (size_t)t * gstride + 2 * gax;
+                const double *de = De + cg_idx3(Le, ex, ey, 0);
+                const int zlo = max(0, li - ex - ey), zhi = Le - ex - ey;
+                double s = 0.0;
+                for (int ez = zlo; ez <= zhi; ez++) s = fma(de[ez], gz[ez + na * fz], s);
+                buf[(size_t)t * bstride + p * nm + fz] = s;
+            }
+            __syncwarp();
+            for (int it = lane; it < Tb * (Le + 1) * q2k; it += 32) {
+                const int t = it % Tb, r = it / Tb;
+                const int q = r % q2k, ex = r / q2k;
+                int fy, fz;
+                cg_dec2(mmax, q, fy, fz);
+                const double *gy = greg + (size_t)t * gstride + gax;
+                const double *om = buf + (size_t)t * bstride;
+                double s = 0.0;
+                for (int ey = 0; ey <= Le - ex; ey++)
+                    s = fma(gy[ey + na * fy], om[cg_idx2(Le, ex, ey) * nm + fz], s);
+                buf[(size_t)t * bstride + nOk + ex * q2k + q] = s;
+            }
+            __syncwarp();
+            for (int f = lane; f < tF1; f += 32) {
+                int y0, y1, y2;
+                cg_dec3(mmax, f, y0, y1, y2);
+                if (y0 + y1 + y2 < fmin) continue;
+                const int ixi = nOk + cg_idx2(mmax, y1, y2);
+                double s1 = S1k[f], sc = Sc[f];
+                for (int t = 0; t < Tb; t++) {
+                    const double *gx = greg + (size_t)t * gstride + na * y0;
+                    const double *xi = buf + (size_t)t * bstride + ixi;
+                    double psi = 0.0;
+                    for (int ex = 0; ex <= Le; ex++) psi = fma(gx[ex], xi[ex * q2k], psi);
+                    s1 += psi;
+                    sc = fma(term[t * L.termw + 12], psi, sc);
+                }
+                S1k[f] = s1;
+                Sc[f] = sc;
+            }
+            __syncwarp();
+        }
+        /* the derivative weights, once per task */
+        double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+        cg_side_weights(De, dDe, Le, emin, pij.AB, S1, Sa, Sb, gA, gB, lane);
+        cg_side_weights(Df, dDf, Lf, fmin, pkl.AB, S1k, Sc, nullptr, gC, gC, lane);
+        /* warp sums of the nine coordinate derivatives; D by translational invariance */
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            double x = gA[a], y = gB[a], z = gC[a];
+            for (int o = 16; o > 0; o >>= 1) {
+                x += __shfl_xor_sync(FULL, x, o);
+                y += __shfl_xor_sync(FULL, y, o);
+                z += __shfl_xor_sync(FULL, z, o);
+            }
+            if (lane == 0) {
+                atomicAdd(P.grad + pij.atom_a * 3 + a, x);
+                atomicAdd(P.grad + pij.atom_b * 3 + a, y);
+                atomicAdd(P.grad + pkl.atom_a * 3 + a, z);
+                atomicAdd(P.grad + pkl.atom_b * 3 + a, -(x + y + z));
+            }
+        }
+        __syncwarp();
+    }
+}
+
 extern "C" int cg_grad_tu_init(const int *c2s_nnz, const int *c2s_idx, const double *c2s_val)
 {
     int rc = cg_tu_tables_init(c2s_nnz, c2s_idx, c2s_val);
@@ -243,6 +551,9 @@ extern "C" int cg_grad_tu_init(const int *c2s_nnz, const int *c2s_idx, const dou
     if (e != cudaSuccess) return (int)e;
     e = cudaFuncSetAttribute((void *)rys_grad_kernel<CG_MODE_GRADA>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 8 * CG_WS_MAX);
+    if (e != cudaSuccess) return (int)e;
+    e = cudaFuncSetAttribute((void *)rys_gradj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             4 * 8 * CG_WS_MAX);
     return (int)e;
 }
 
@@ -250,7 +561,8 @@ extern "C" int cg_grad_blocks_per_sm(int mode, int ws_doubles)
 {
     int nb = 0;
     size_t smem = (size_t)4 * ws_doubles * sizeof(double);
-    void *fn = mode == CG_MODE_GRAD ? (void *)rys_grad_kernel<CG_MODE_GRAD> : (void *)rys_grad_kernel<CG_MODE_GRADA>;
+    void *fn = mode == CG_MODE_GRAD ? (void *)rys_grad_kernel<CG_MODE_GRAD>
+             : mode == CG_MODE_GRADJ ? (void *)rys_gradj_kernel : (void *)rys_grad_kernel<CG_MODE_GRADA>;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem) != cudaSuccess) return 1;
     return nb > 0 ? nb : 1;
 }
@@ -258,7 +570,9 @@ extern "C" int cg_grad_blocks_per_sm(int mode, int ws_doubles)
 extern "C" int cg_launch_grad(const CGGradLaunch *P, int mode, int nblocks, cudaStream_t stream)
 {
     size_t smem = (size_t)4 * P->ws_doubles * sizeof(double);
-    if (mode == CG_MODE_GRAD)
+    if (mode == CG_MODE_GRADJ)
+        rys_gradj_kernel<<<nblocks, 128, smem, stream>>>(*P);
+    else if (mode == CG_MODE_GRAD)
         rys_grad_kernel<CG_MODE_GRAD><<<nblocks, 128, smem, stream>>>(*P);
     else
         rys_grad_kernel<CG_MODE_GRADA><<<nblocks, 128, smem, stream>>>(*P);

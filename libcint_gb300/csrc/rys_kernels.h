@@ -15,6 +15,9 @@
 #define CG_MODE_ERIB 5               /* int2e / int3c2e classes with lj >= 3 and ll <= 2: the bra
                                         transfer per term (libcint's order on the bra), the ket
                                         transfer after contraction */
+#define CG_MODE_GRADJ 7              /* adjoint, nuclear-coordinate gradient of the Coulomb energy,
+                                        contraction first: the densities are carried through the
+                                        transfers and the 2D integrals contracted axis by axis */
 #define CG_TERMW 12                  /* doubles per term record in shared memory */
 #define CG_TERMW_GRAD 20             /* term record of the adjoint kernel */
 #define CG_GRAD_MAXPRIM 16           /* primitives per shell supported by the exponent adjoint */

@@ -46,3 +46,21 @@ def test_df_j_exact_in_span_gpu(gpulib, oracle):
     J = df.DFCoulomb(mol, norb).vj(torch.as_tensor(dm, device='cuda')).cpu().numpy()
     Jx = _exact_j(oracle, mol, norb, dm)
     assert np.abs(J - Jx).max() <= 1e-12 * np.abs(Jx).max()
+
+
+def test_df_k_matches_oracle_fit(gpulib, oracle):
+    """density-fitted K on the GPU (whitened three-index tensor formed from the int3c2e plan's
+    packed buffer, then two batched products) against K = T V^-1 T contracted with D on the
+    oracle's blocks in dense numpy; K symmetric"""
+    import torch
+    mol, norb = M.config2(seed=1, natm=2, box=3.0)
+    n = int(df._nsph(mol)[:norb].sum())
+    d = np.random.RandomState(7).normal(0, 0.2, (n, n))
+    dm = 0.5 * (d + d.T)
+    fit = df.DFCoulomb(mol, norb)
+    K = fit.vk(torch.as_tensor(dm, device='cuda')).cpu().numpy()
+    T3, V, _, _ = _dense_df(oracle, mol, norb, dm)
+    W = np.einsum('ijp,pq->ijq', T3, np.linalg.inv(V), optimize=True)
+    Kref = np.einsum('ijq,jl,klq->ik', W, dm, T3, optimize=True)
+    assert np.abs(K - Kref).max() <= 1e-10 * np.abs(Kref).max()
+    assert np.abs(K - K.T).max() <= 1e-12 * np.abs(Kref).max()
