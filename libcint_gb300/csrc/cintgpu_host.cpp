@@ -298,7 +298,8 @@ struct CINTGPUPlan {
     int three = 0;                 /* int3c2e and int2c2e: slot 3 is a unit s partner */
     int two = 0;                   /* int2c2e: slot 1 is a unit s partner as well */
     int jmode = 0;                 /* J (bit 0) / K (bit 1) contraction instead of stored integrals */
-    int gradj = 0;                 /* J_GRAD: contraction-first adjoint kernel (CG_MODE_GRADJ) */
+    int gradj = 0;                 /* J_GRAD(_EXP): contraction-first adjoint kernel (CG_MODE_GRADJ,
+                                      CG_MODE_GRADAJ) */
     int nao_cart = 0;
     int natm = 0;
     int64_t nprim_tot = 0;
@@ -603,22 +604,24 @@ double flops_per_primq(int li, int lj, int lk, int ll, int mode)
         for (int l = lk; l <= lk + ll; l++) nfr += nc(l);
         return n * (20 + 3 * 5 * vrr2 + 3 * 2 * hrr_bra + nij * nc(lk + ll) + 2 * nij * nfr);
     }
-    if (mode == CG_MODE_GRADJ) {
-        /* contraction-first adjoint: VRR to (li+lj+1, lk+ll+1); per side three contractions
+    if (mode == CG_MODE_GRADJ || mode == CG_MODE_GRADAJ) {
+        /* contraction-first adjoint: VRR to (li+lj+d, lk+ll+d); per side three contractions
          * (z, y, x; 2 flops per product) and the sums over terms (bra: 3 per e', ket: 2 per f';
-         * the derivative weights are per task and not counted) */
+         * with exponents 4 more per entry and the per-term warp sums; the derivative weights are
+         * per task and not counted) */
         auto nc = [](int l) { return (l + 1) * (l + 2) / 2; };
         auto np2 = [](int l) { return (l + 1) * (l + 2) / 2.0; };
         auto ntet = [](int l) { return l < 0 ? 0.0 : (l + 1) * (l + 2) * (l + 3) / 6.0; };
-        const int Le = li + lj, Lf = lk + ll;
+        const int Le = li + lj, Lf = lk + ll, d = mode == CG_MODE_GRADAJ ? 2 : 1;
         double nE = 0, nF = 0;
         for (int l = li; l <= Le; l++) nE += nc(l);
         for (int l = lk; l <= Lf; l++) nF += nc(l);
-        const double na = Le + 2, nm = Lf + 2;
-        const double nEp = ntet(Le + 1) - ntet(li - 2), nFp = ntet(Lf + 1) - ntet(lk - 2);
-        const double bra = 2 * nF * na + 2 * np2(Le + 1) * np2(Lf) + nEp * (2 * (Lf + 1) + 5);
-        const double ket = 2 * nE * nm + 2 * np2(Lf + 1) * np2(Le) + nFp * (2 * (Le + 1) + 3);
-        return n * (20 + 3 * 5 * na * nm + bra + ket);
+        const double na = Le + d + 1, nm = Lf + d + 1;
+        const double nEp = ntet(Le + d) - ntet(li - 2), nFp = ntet(Lf + d) - ntet(lk - 2);
+        const double xs = d == 2 ? 4 : 0;
+        const double bra = 2 * nF * na + 2 * np2(Le + d) * np2(Lf) + nEp * (2 * (Lf + 1) + 5 + xs);
+        const double ket = 2 * nE * nm + 2 * np2(Lf + d) * np2(Le) + nFp * (2 * (Le + 1) + 3 + xs);
+        return n * (20 + 3 * 5 * na * nm + bra + ket + (d == 2 ? 20 : 0));
     }
     double per_root = 20 + 3 * 5 * vrr + 3 * 2 * hrr;
     if (mode == CG_MODE_IP1) per_root += 3 * 3 * (double)L.G / L.dI * (L.dI - 1) + 9.0 * L.nf;
@@ -987,10 +990,16 @@ static bool bra_term(const CINTGPUPlan *P, const int *l)
     cg_layout(l[0], l[1], l[2], l[3], CG_MODE_ERIB, CG_WS_MAX, &L);
     return L.T >= 1;
 }
+/* adjoint kernel of a plan */
+static int grad_kernel_mode(const CINTGPUPlan *P)
+{
+    if (!P->gradj) return P->mode;
+    return P->mode == CG_MODE_GRADA ? CG_MODE_GRADAJ : CG_MODE_GRADJ;
+}
 /* kernel (layout) mode of one class */
 static int class_mode(const CINTGPUPlan *P, const int *l)
 {
-    if (P->mode == CG_MODE_GRAD && P->gradj) return CG_MODE_GRADJ;
+    if (P->gradj) return P->mode == CG_MODE_GRADA ? CG_MODE_GRADAJ : CG_MODE_GRADJ;
     return bra_term(P, l) ? CG_MODE_ERIB : P->mode;
 }
 static bool per_primitive(const CINTGPUPlan *P, const int *l)
@@ -1052,7 +1061,13 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             P->gradj = !(e && strcmp(e, "component") == 0);
         }
         break;
-    case CINTGPU_J_GRAD_EXP: P->mode = CG_MODE_GRADA; P->sph = 0; P->three = 0; break;
+    case CINTGPU_J_GRAD_EXP:
+        P->mode = CG_MODE_GRADA; P->sph = 0; P->three = 0;
+        {
+            const char *e = getenv("CINTGPU_ADJOINT");
+            P->gradj = !(e && strcmp(e, "component") == 0);
+        }
+        break;
     default: set_error("unknown integral kind %d", kind); return CINTGPU_ERR_ARG;
     }
     P->ncomp = CG_IS_IP(P->mode) ? 3 : 1;
@@ -1426,7 +1441,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         P->groups[g].ntasks = (int)P->tasks.size() - P->groups[g].task0;
         P->groups[g].ws = g == 0 ? ws_small : CG_WS_MAX;
         P->groups[g].blocks_per_sm = (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA)
-                                         ? cg_grad_blocks_per_sm(P->gradj ? CG_MODE_GRADJ : P->mode, P->groups[g].ws)
+                                         ? cg_grad_blocks_per_sm(grad_kernel_mode(P), P->groups[g].ws)
                                          : cg_blocks_per_sm(g == 2 ? CG_MODE_ERIP : P->mode, P->groups[g].ws);
         P->groups[g].nblocks = std::min(std::max(1, g_ctx.sm_count) * P->groups[g].blocks_per_sm,
                                         std::max(1, (P->groups[g].ntasks + 3) / 4));
@@ -1621,7 +1636,7 @@ static int launch_grad_group(CINTGPUPlan *P, int g, cudaStream_t stream)
         L.wglobal += (size_t)g_ctx.sm_count * 4 * P->groups[0].blocks_per_sm * P->max_nf;
     L.wstride = P->max_nf;
     const int nblocks = G.nblocks;
-    int rc = cg_launch_grad(&L, P->gradj ? CG_MODE_GRADJ : P->mode, nblocks, stream);
+    int rc = cg_launch_grad(&L, grad_kernel_mode(P), nblocks, stream);
     if (rc) { set_error("adjoint kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc)); return CINTGPU_ERR_CUDA; }
     return 0;
 }

@@ -97,24 +97,30 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     L->scr |= 1;
     const bool grad = mode == CG_MODE_GRAD || mode == CG_MODE_GRADA;
     int T = 0;
-    if (mode == CG_MODE_GRADJ) {
-        /* contraction-first adjoint: per term a record (stage-1 values, 2a 2b 2c, m b01), the VRR
-         * arrays g(e, f) for e <= li+lj+1, f <= lk+ll+1, and the buffers of one side's axis-by-axis
-         * contraction; per task the transferred densities with their AB derivatives and the
-         * per-entry sums over terms (three on the bra, two on the ket) */
-        const int Le = li + lj, Lf = lk + ll;
-        L->nroots = (lsum + 1) / 2 + 1;
-        L->nmax = Le + 1;
-        L->mmax = Lf + 1;
+    if (mode == CG_MODE_GRADJ || mode == CG_MODE_GRADAJ) {
+        /* contraction-first adjoint: per term a record (stage-1 values, 2a 2b 2c, m b01; with
+         * exponents the term's four primitive indices), the VRR arrays g(e, f) for
+         * e <= li+lj+d, f <= lk+ll+d (d = 1, 2 with exponents), and the buffers of one side's
+         * axis-by-axis contraction (with exponents also the per-lane exponent partials, 64 per
+         * term); per task the transferred densities with their AB derivatives, the per-entry sums
+         * over terms (three on the bra, two on the ket) and, with exponents, the exponent weights
+         * of the four shells and their per-primitive sums */
+        const bool ex = mode == CG_MODE_GRADAJ;
+        const int Le = li + lj, Lf = lk + ll, d = ex ? 2 : 1;
+        L->nroots = (lsum + d) / 2 + 1;
+        L->nmax = Le + d;
+        L->mmax = Lf + d;
         const int na = L->nmax + 1, nm = L->mmax + 1;
         L->G = na * nm;
         L->gax = L->G | 1;
         L->gstride = 3 * L->gax;
-        L->termw = (13 + nm) | 1;
+        L->termw = (13 + nm + (ex ? 2 : 0)) | 1;
         const int bufb = cg_np2(Lf) * na + (Lf + 1) * cg_np2(L->nmax);
         const int bufk = cg_np2(Le) * nm + (Le + 1) * cg_np2(L->mmax);
-        L->scr = (bufb > bufk ? bufb : bufk) | 1;
-        const int fixed = 4 * cg_ntet(Le) + 4 * cg_ntet(Lf) + 3 * cg_ntet(Le + 1) + 2 * cg_ntet(Lf + 1);
+        L->scr = ((bufb > bufk ? bufb : bufk) + (ex ? 64 : 0)) | 1;
+        const int tE = cg_ntet(L->nmax), tF = cg_ntet(L->mmax);
+        const int fixed = 4 * cg_ntet(Le) + 4 * cg_ntet(Lf) + 3 * tE + 2 * tF
+                        + (ex ? 2 * tE + 2 * tF + 4 * CG_GRAD_MAXPRIM : 0);
         T = (ws_doubles - fixed) / (L->termw + L->gstride + L->scr);
         if (T > 32) T = 32;
         if (T < 0) T = 0;

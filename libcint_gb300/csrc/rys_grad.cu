@@ -234,7 +234,7 @@ rys_grad_kernel(CGGradLaunch P)
 }
 
 /* ------------------------------------------------------------------------------------------
- * Contraction-first adjoint (coordinates), CG_MODE_GRADJ.
+ * Contraction-first adjoint, CG_MODE_GRADJ (coordinates) and CG_MODE_GRADAJ (and exponents).
  *
  * The energy of one unique quartet is E = sum D_ij D_kl (ij|kl) (w_q folded into D_ij).  The
  * horizontal transfer is linear and depends only on AB = A - B (bra) and CD = C - D (ket):
@@ -262,8 +262,13 @@ rys_grad_kernel(CGGradLaunch P)
  *   dE/dA_x = sum_e' Sa[e'] De[e'-1x] + S1[e'] (dDe_x[e'] - (e'_x + 1) De[e'+1x])
  *   dE/dB_x = sum_e' Sb[e'] (De[e'-1x] + AB_x De[e']) - S1[e'] dDe_x[e']
  *
- * (C likewise from Psi).  No Cartesian component of (ij|kl) is formed: the cost per term grows
- * like l^5 instead of the l^8 of the per-component adjoint above.
+ * (C likewise from Psi).  Exponent derivatives (coefficients fixed): the base shell's exponent a
+ * multiplies its Gaussian by -|r-A|^2, so dE/da = -sum_x sum_e De Phi[e+2x]; the partner's b by
+ * -|r-B|^2 = -sum_x ((x-A_x)^2 + 2 AB_x (x-A_x) + AB_x^2) (the x1 insertion of libcint,
+ * src/g2e.c:4755-4893, in the transferred basis).  These go to the term's own primitives, so they
+ * are reduced over the warp per term (Phi to |e'| = li+lj+2, Psi likewise).  No Cartesian
+ * component of (ij|kl) is formed: the cost per term grows like l^5 instead of the l^8 of the
+ * per-component adjoint above.
  * ------------------------------------------------------------------------------------------ */
 __constant__ double c_binom5[5][5] = {{1, 0, 0, 0, 0}, {1, 1, 0, 0, 0}, {1, 2, 1, 0, 0},
                                       {1, 3, 3, 1, 0}, {1, 4, 6, 4, 1}};
@@ -316,19 +321,20 @@ __device__ __forceinline__ void cg_pair_density(const double *__restrict__ dm, i
     }
 }
 
-/* One side's weights applied to its sums (lane-owned entries e' over |e'| <= L + 1, |e'| >= emin):
+/* One side's coordinate weights applied to its sums (lane-owned entries e', tetrahedron index
+ * space Lidx >= L + 1; entries with emin <= |e'| <= L + 1):
  * gP_x += sum Sp[e'] D[e'-1x] + S1[e'] (dD_x[e'] - (e'_x + 1) D[e'+1x]) for the base centre and,
  * with Sq given, gQ_x += sum Sq[e'] (D[e'-1x] + AB_x D[e']) - S1[e'] dD_x[e'] for the partner. */
-__device__ __forceinline__ void cg_side_weights(const double *D, const double *dD, int L, int emin,
+__device__ __forceinline__ void cg_side_weights(const double *D, const double *dD, int L, int Lidx, int emin,
                                                 const double *AB, const double *S1, const double *Sp,
                                                 const double *Sq, double gP[3], double gQ[3], int lane)
 {
-    const int t = cg_ntet(L), t1 = cg_ntet(L + 1);
+    const int t = cg_ntet(L), t1 = cg_ntet(Lidx);
     for (int e = lane; e < t1; e += 32) {
         int x[3];
-        cg_dec3(L + 1, e, x[0], x[1], x[2]);
+        cg_dec3(Lidx, e, x[0], x[1], x[2]);
         const int s = x[0] + x[1] + x[2];
-        if (s < emin) continue;
+        if (s < emin || s > L + 1) continue;
         const int me = s <= L ? cg_idx3(L, x[0], x[1], x[2]) : -1;
         const double d0 = me >= 0 ? D[me] : 0.0;
         const double s1 = S1[e], sp = Sp[e], sq = Sq ? Sq[e] : 0.0;
@@ -345,6 +351,45 @@ __device__ __forceinline__ void cg_side_weights(const double *D, const double *d
     }
 }
 
+/* Exponent weights of one side over the tetrahedron index space Lidx = L + 2: the base shell's
+ * primitive exponent a enters as -|r-A|^2 on its Gaussian, the partner's b as
+ * -|r-B|^2 = -sum_x ((x-A_x)^2 + 2 AB_x (x-A_x) + AB_x^2):
+ *   Wp[e'] = -sum_x D[e'-2x],   Wq[e'] = -sum_x (D[e'-2x] + 2 AB_x D[e'-1x] + AB_x^2 D[e']) */
+__device__ __forceinline__ void cg_side_exp_weights(const double *D, int L, const double *AB, double *Wp,
+                                                    double *Wq, int lane)
+{
+    const int t2 = cg_ntet(L + 2);
+    for (int e = lane; e < t2; e += 32) {
+        int x[3];
+        cg_dec3(L + 2, e, x[0], x[1], x[2]);
+        const int s = x[0] + x[1] + x[2];
+        const double d0 = s <= L ? D[cg_idx3(L, x[0], x[1], x[2])] : 0.0;
+        double wp = 0.0, wq = 0.0;
+#pragma unroll
+        for (int ax = 0; ax < 3; ax++) {
+            int y[3] = {x[0], x[1], x[2]};
+            double d1 = 0.0, d2 = 0.0;
+            if (x[ax] >= 1 && s - 1 <= L) { y[ax] -= 1; d1 = D[cg_idx3(L, y[0], y[1], y[2])]; y[ax] += 1; }
+            if (x[ax] >= 2) { y[ax] -= 2; d2 = D[cg_idx3(L, y[0], y[1], y[2])]; }
+            wp -= d2;
+            wq -= fma(AB[ax], fma(AB[ax], d0, 2.0 * d1), d2);
+        }
+        Wp[e] = wp;
+        Wq[e] = wq;
+    }
+}
+
+/* Sum over the warp of two values per lane: x to lane 0, y to lane 16 (recursive halving) */
+__device__ __forceinline__ double cg_warp_sum2(double x, double y, int lane)
+{
+    double v = (lane & 16) ? y : x;
+    const double w = (lane & 16) ? x : y;
+    v += __shfl_xor_sync(FULL, w, 16);
+    for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+
+template <bool EXP>
 __global__ void __launch_bounds__(128, 2)
 rys_gradj_kernel(CGGradLaunch P)
 {
@@ -352,6 +397,7 @@ rys_gradj_kernel(CGGradLaunch P)
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     double *ws = smem + (size_t)warp * P.ws_doubles;
+    constexpr int LMODE = EXP ? CG_MODE_GRADAJ : CG_MODE_GRADJ;
 
     for (;;) {
         int tid = 0;
@@ -363,7 +409,7 @@ rys_gradj_kernel(CGGradLaunch P)
         const CGPair pkl = P.pairs[tk.pkl];
         const int li = pij.la, lj = pij.lb, lk = pkl.la, ll = pkl.lb;
         CGLayout L;
-        cg_class_layout(li, lj, lk, ll, CG_MODE_GRADJ, P.ws_doubles, &L);
+        cg_class_layout(li, lj, lk, ll, LMODE, P.ws_doubles, &L);
         if (L.T < 1) {
             if (lane == 0) atomicOr(P.status, 1);
             continue;
@@ -371,14 +417,18 @@ rys_gradj_kernel(CGGradLaunch P)
         const int T = L.T, n = L.nroots, gax = L.gax, gstride = L.gstride, bstride = L.scr;
         const int Le = li + lj, Lf = lk + ll, nmax = L.nmax, mmax = L.mmax;
         const int na = nmax + 1, nm = mmax + 1;
-        const int tE = cg_ntet(Le), tE1 = cg_ntet(Le + 1), tF = cg_ntet(Lf), tF1 = cg_ntet(Lf + 1);
+        const int tE0 = cg_ntet(Le), tF0 = cg_ntet(Lf), tE = cg_ntet(nmax), tF = cg_ntet(mmax);
         /* per task: transferred densities, then the sums over terms of Phi, 2a Phi, 2b Phi (bra,
-         * per e') and of Psi, 2c Psi (ket, per f'); the lane e' mod 32 owns entry e' */
-        double *De = ws, *dDe = De + tE, *Df = dDe + 3 * tE, *dDf = Df + tF;
-        double *S1 = dDf + 3 * tF, *Sa = S1 + tE1, *Sb = Sa + tE1, *S1k = Sb + tE1, *Sc = S1k + tF1;
+         * per e') and of Psi, 2c Psi (ket, per f'); the lane e' mod 32 owns entry e'.  With
+         * exponents: the four shells' exponent weights and per-primitive sums. */
+        double *De = ws, *dDe = De + tE0, *Df = dDe + 3 * tE0, *dDf = Df + tF0;
+        double *S1 = dDf + 3 * tF0, *Sa = S1 + tE, *Sb = Sa + tE, *S1k = Sb + tE, *Sc = S1k + tF;
+        double *WI = Sc + tF, *WJ = WI + tE, *WK = WJ + tE, *WL = WK + tF;
+        double *aacc = WL + tF;
         double *term = ws + L.off_w;
         double *greg = ws + L.off_g;
         double *buf = ws + L.off_scr;
+        const int bred = bstride - 64;          /* exponent partials: the last 64 of a term's buffer */
         const CGPrimPair *__restrict__ ppij = P.prims + pij.prim_off;
         const CGPrimPair *__restrict__ ppkl = P.prims + pkl.prim_off;
         const int *__restrict__ pql = P.pqlist + tk.pq_off;
@@ -389,8 +439,15 @@ rys_gradj_kernel(CGGradLaunch P)
                         * ((tk.sym & 4) ? 2.0 : 1.0);
         cg_pair_density(P.dm, P.nao, pij, wq, De, dDe, lane);
         cg_pair_density(P.dm, P.nao, pkl, 1.0, Df, dDf, lane);
-        for (int e = lane; e < 3 * tE1 + 2 * tF1; e += 32) S1[e] = 0.0;
+        for (int e = lane; e < 3 * tE + 2 * tF; e += 32) S1[e] = 0.0;
+        if (EXP)
+            for (int e = lane; e < 4 * CG_GRAD_MAXPRIM; e += 32) aacc[e] = 0.0;
         __syncwarp();
+        if (EXP) {
+            cg_side_exp_weights(De, Le, pij.AB, WI, WJ, lane);
+            cg_side_exp_weights(Df, Lf, pkl.AB, WK, WL, lane);
+            __syncwarp();
+        }
 
         const int nOm = cg_np2(Lf) * na, q2 = cg_np2(nmax);
         const int nOk = cg_np2(Le) * nm, q2k = cg_np2(mmax);
@@ -413,7 +470,16 @@ rys_gradj_kernel(CGGradLaunch P)
                 rec[12] = 2.0 * B.aA;
                 double mb = 0.0;
                 for (int m = 0; m <= mmax; m++) { rec[13 + m] = mb; mb += rec[2]; }
+                if (EXP) {
+                    int *ri = reinterpret_cast<int *>(rec + 13 + nm);
+                    ri[0] = ij % pij.npa;
+                    ri[1] = ij / pij.npa;
+                    ri[2] = kl % pkl.npa;
+                    ri[3] = kl / pkl.npa;
+                }
             }
+            if (EXP)
+                for (int e = lane; e < 64 * Tb; e += 32) buf[(size_t)(e >> 6) * bstride + bred + (e & 63)] = 0.0;
             __syncwarp();
             /* ---- stage 2: VRR, one lane per (term, axis) */
             for (int item = lane; item < 3 * Tb; item += 32) {
@@ -450,27 +516,49 @@ rys_gradj_kernel(CGGradLaunch P)
                 buf[(size_t)t * bstride + nOm + fx * q2 + q] = s;
             }
             __syncwarp();
-            for (int e = lane; e < tE1; e += 32) {
+            for (int e = lane; e < tE; e += 32) {
                 int x0, x1, x2;
                 cg_dec3(nmax, e, x0, x1, x2);
-                if (x0 + x1 + x2 < emin) continue;
+                const int es = x0 + x1 + x2;
+                if (es < emin) continue;
+                const bool crd = es <= Le + 1, xp = EXP && es >= li;
                 const int ixi = nOm + cg_idx2(nmax, x1, x2);
                 double s1 = S1[e], sa = Sa[e], sb = Sb[e];
+                const double wi = xp ? WI[e] : 0.0, wj = xp ? WJ[e] : 0.0;
                 for (int t = 0; t < Tb; t++) {
                     const double *gx = greg + (size_t)t * gstride + x0;
                     const double *xi = buf + (size_t)t * bstride + ixi;
                     double phi = 0.0;
                     for (int fx = 0; fx <= Lf; fx++) phi = fma(gx[na * fx], xi[fx * q2], phi);
                     const double *rec = term + t * L.termw;
-                    s1 += phi;
-                    sa = fma(rec[10], phi, sa);
-                    sb = fma(rec[11], phi, sb);
+                    if (crd) {
+                        s1 += phi;
+                        sa = fma(rec[10], phi, sa);
+                        sb = fma(rec[11], phi, sb);
+                    }
+                    if (xp) {
+                        double *red = buf + (size_t)t * bstride + bred + lane;
+                        red[0] = fma(phi, wi, red[0]);
+                        red[32] = fma(phi, wj, red[32]);
+                    }
                 }
                 S1[e] = s1;
                 Sa[e] = sa;
                 Sb[e] = sb;
             }
             __syncwarp();
+            if (EXP) {
+                /* the bra shells' exponent sums of each term, to its two primitives */
+                for (int t = 0; t < Tb; t++) {
+                    const double *red = buf + (size_t)t * bstride + bred + lane;
+                    const double v = cg_warp_sum2(red[0], red[32], lane);
+                    const int *ri = reinterpret_cast<const int *>(term + t * L.termw + 13 + nm);
+                    if (lane == 0) aacc[ri[0]] += v;
+                    if (lane == 16) aacc[CG_GRAD_MAXPRIM + ri[1]] += v;
+                }
+                for (int e = lane; e < 64 * Tb; e += 32) buf[(size_t)(e >> 6) * bstride + bred + (e & 63)] = 0.0;
+                __syncwarp();
+            }
             /* ---- ket side: the same with the pairs' roles exchanged, sums of Psi and 2c Psi */
             for (int it = lane; it < Tb * nOk; it += 32) {
                 const int t = it % Tb, r = it / Tb;
@@ -498,29 +586,49 @@ rys_gradj_kernel(CGGradLaunch P)
                 buf[(size_t)t * bstride + nOk + ex * q2k + q] = s;
             }
             __syncwarp();
-            for (int f = lane; f < tF1; f += 32) {
+            for (int f = lane; f < tF; f += 32) {
                 int y0, y1, y2;
                 cg_dec3(mmax, f, y0, y1, y2);
-                if (y0 + y1 + y2 < fmin) continue;
+                const int fs = y0 + y1 + y2;
+                if (fs < fmin) continue;
+                const bool crd = fs <= Lf + 1, xp = EXP && fs >= lk;
                 const int ixi = nOk + cg_idx2(mmax, y1, y2);
                 double s1 = S1k[f], sc = Sc[f];
+                const double wk = xp ? WK[f] : 0.0, wl = xp ? WL[f] : 0.0;
                 for (int t = 0; t < Tb; t++) {
                     const double *gx = greg + (size_t)t * gstride + na * y0;
                     const double *xi = buf + (size_t)t * bstride + ixi;
                     double psi = 0.0;
                     for (int ex = 0; ex <= Le; ex++) psi = fma(gx[ex], xi[ex * q2k], psi);
-                    s1 += psi;
-                    sc = fma(term[t * L.termw + 12], psi, sc);
+                    if (crd) {
+                        s1 += psi;
+                        sc = fma(term[t * L.termw + 12], psi, sc);
+                    }
+                    if (xp) {
+                        double *red = buf + (size_t)t * bstride + bred + lane;
+                        red[0] = fma(psi, wk, red[0]);
+                        red[32] = fma(psi, wl, red[32]);
+                    }
                 }
                 S1k[f] = s1;
                 Sc[f] = sc;
             }
             __syncwarp();
+            if (EXP) {
+                for (int t = 0; t < Tb; t++) {
+                    const double *red = buf + (size_t)t * bstride + bred + lane;
+                    const double v = cg_warp_sum2(red[0], red[32], lane);
+                    const int *ri = reinterpret_cast<const int *>(term + t * L.termw + 13 + nm);
+                    if (lane == 0) aacc[2 * CG_GRAD_MAXPRIM + ri[2]] += v;
+                    if (lane == 16) aacc[3 * CG_GRAD_MAXPRIM + ri[3]] += v;
+                }
+                __syncwarp();
+            }
         }
-        /* the derivative weights, once per task */
+        /* the coordinate weights, once per task */
         double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
-        cg_side_weights(De, dDe, Le, emin, pij.AB, S1, Sa, Sb, gA, gB, lane);
-        cg_side_weights(Df, dDf, Lf, fmin, pkl.AB, S1k, Sc, nullptr, gC, gC, lane);
+        cg_side_weights(De, dDe, Le, nmax, emin, pij.AB, S1, Sa, Sb, gA, gB, lane);
+        cg_side_weights(Df, dDf, Lf, mmax, fmin, pkl.AB, S1k, Sc, nullptr, gC, gC, lane);
         /* warp sums of the nine coordinate derivatives; D by translational invariance */
 #pragma unroll
         for (int a = 0; a < 3; a++) {
@@ -535,6 +643,15 @@ rys_gradj_kernel(CGGradLaunch P)
                 atomicAdd(P.grad + pij.atom_b * 3 + a, y);
                 atomicAdd(P.grad + pkl.atom_a * 3 + a, z);
                 atomicAdd(P.grad + pkl.atom_b * 3 + a, -(x + y + z));
+            }
+        }
+        if (EXP) {
+            __syncwarp();
+            const int np[4] = {pij.npa, pij.npb, pkl.npa, pkl.npb};
+            const int gp[4] = {pij.gp_a, pij.gp_b, pkl.gp_a, pkl.gp_b};
+            for (int e = lane; e < 4 * CG_GRAD_MAXPRIM; e += 32) {
+                int s = e / CG_GRAD_MAXPRIM, p = e - s * CG_GRAD_MAXPRIM;
+                if (p < np[s] && aacc[e] != 0.0) atomicAdd(P.galpha + gp[s] + p, aacc[e]);
             }
         }
         __syncwarp();
@@ -552,7 +669,10 @@ extern "C" int cg_grad_tu_init(const int *c2s_nnz, const int *c2s_idx, const dou
     e = cudaFuncSetAttribute((void *)rys_grad_kernel<CG_MODE_GRADA>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 8 * CG_WS_MAX);
     if (e != cudaSuccess) return (int)e;
-    e = cudaFuncSetAttribute((void *)rys_gradj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute((void *)rys_gradj_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             4 * 8 * CG_WS_MAX);
+    if (e != cudaSuccess) return (int)e;
+    e = cudaFuncSetAttribute((void *)rys_gradj_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              4 * 8 * CG_WS_MAX);
     return (int)e;
 }
@@ -562,7 +682,8 @@ extern "C" int cg_grad_blocks_per_sm(int mode, int ws_doubles)
     int nb = 0;
     size_t smem = (size_t)4 * ws_doubles * sizeof(double);
     void *fn = mode == CG_MODE_GRAD ? (void *)rys_grad_kernel<CG_MODE_GRAD>
-             : mode == CG_MODE_GRADJ ? (void *)rys_gradj_kernel : (void *)rys_grad_kernel<CG_MODE_GRADA>;
+             : mode == CG_MODE_GRADJ ? (void *)rys_gradj_kernel<false>
+             : mode == CG_MODE_GRADAJ ? (void *)rys_gradj_kernel<true> : (void *)rys_grad_kernel<CG_MODE_GRADA>;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem) != cudaSuccess) return 1;
     return nb > 0 ? nb : 1;
 }
@@ -571,7 +692,9 @@ extern "C" int cg_launch_grad(const CGGradLaunch *P, int mode, int nblocks, cuda
 {
     size_t smem = (size_t)4 * P->ws_doubles * sizeof(double);
     if (mode == CG_MODE_GRADJ)
-        rys_gradj_kernel<<<nblocks, 128, smem, stream>>>(*P);
+        rys_gradj_kernel<false><<<nblocks, 128, smem, stream>>>(*P);
+    else if (mode == CG_MODE_GRADAJ)
+        rys_gradj_kernel<true><<<nblocks, 128, smem, stream>>>(*P);
     else if (mode == CG_MODE_GRAD)
         rys_grad_kernel<CG_MODE_GRAD><<<nblocks, 128, smem, stream>>>(*P);
     else

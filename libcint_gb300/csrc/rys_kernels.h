@@ -18,6 +18,7 @@
 #define CG_MODE_GRADJ 7              /* adjoint, nuclear-coordinate gradient of the Coulomb energy,
                                         contraction first: the densities are carried through the
                                         transfers and the 2D integrals contracted axis by axis */
+#define CG_MODE_GRADAJ 8             /* the same with the primitive-exponent derivatives */
 #define CG_TERMW 12                  /* doubles per term record in shared memory */
 #define CG_TERMW_GRAD 20             /* term record of the adjoint kernel */
 #define CG_GRAD_MAXPRIM 16           /* primitives per shell supported by the exponent adjoint */

@@ -188,14 +188,15 @@ def test_j_high_l_per_primitive_classes(gpulib, oracle):
     assert abs(float(E) - Eref) <= 1e-10 * abs(Eref)
 
 
-def _grad_with(mol, dmt, adjoint, quartets=None):
+def _grad_with(mol, dmt, adjoint, quartets=None, exponents=False):
     import os
     from libcint_gb300.coulomb import CoulombPlans
     old = os.environ.get('CINTGPU_ADJOINT')
     os.environ['CINTGPU_ADJOINT'] = adjoint
     try:
         # the adjoint plan is built by the first grad call
-        return CoulombPlans(mol, quartets).grad(dmt)[0].cpu().numpy()
+        g, ga = CoulombPlans(mol, quartets, with_exponents=exponents).grad(dmt)
+        return (g.cpu().numpy(), ga.cpu().numpy()) if exponents else g.cpu().numpy()
     finally:
         if old is None:
             os.environ.pop('CINTGPU_ADJOINT')
@@ -242,3 +243,53 @@ def test_contraction_first_adjoint_matches_per_component(gpulib, case):
         ga = _grad_with(mol, dmt, 'contraction')
         gi = grad_via_ip1(mol, dmt).cpu().numpy()
         assert np.abs(ga - gi).max() <= 1e-10 * np.abs(gi).max(), np.abs(ga - gi).max() / np.abs(gi).max()
+
+
+def test_contraction_first_exponent_adjoint_matches_per_component(gpulib):
+    """Coordinate and primitive-exponent gradients from the contraction-first exponent adjoint
+    against the per-component kernel on a c3-type system and on s..f shells with up to 3
+    primitives: 1e-11 of each gradient's largest element."""
+    import torch
+    mol, dm = _system(natm=4, seed=5)
+    dmt = torch.as_tensor(dm, device='cuda')
+    g1, a1 = _grad_with(mol, dmt, 'contraction', exponents=True)
+    g2, a2 = _grad_with(mol, dmt, 'component', exponents=True)
+    assert np.abs(g1 - g2).max() <= 1e-11 * np.abs(g2).max()
+    assert np.abs(a1 - a2).max() <= 1e-11 * np.abs(a2).max()
+    b = M._Builder()
+    rng = np.random.RandomState(8)
+    for a in range(2):
+        at = b.atom(1 + a, tuple(rng.uniform(-1.0, 1.0, 3)))
+        for l, npr in ((0, 3), (1, 2), (2, 2), (3, 2)):
+            ex = sorted(rng.uniform(0.3, 4.0, npr), reverse=True)
+            b.shell(at, l, ex, [M.gto_norm(l, e) * rng.uniform(0.3, 1.0) for e in ex])
+    mol = b.mol('s..f')
+    nao = sum(mol.nsph(i) for i in range(mol.nbas))
+    d = rng.normal(0, 0.1, (nao, nao))
+    dmt = torch.as_tensor(0.5 * (d + d.T), device='cuda')
+    # the per-component exponent kernel cannot hold (ff|ff) and (ff|fd): compare without them
+    q = np.asarray(M.unique_quartets(mol.nbas))
+    part = q[(mol.bas[q, M.ANG_OF] == 3).sum(axis=1) < 3]
+    g1, a1 = _grad_with(mol, dmt, 'contraction', part, exponents=True)
+    g2, a2 = _grad_with(mol, dmt, 'component', part, exponents=True)
+    assert np.abs(g1 - g2).max() <= 1e-11 * np.abs(g2).max()
+    assert np.abs(a1 - a2).max() <= 1e-11 * np.abs(a2).max()
+    # every quartet: coordinates against the coordinate-only kernel, exponents of the f shells
+    # against central differences of the energy (relative step 1e-5)
+    from libcint_gb300.coulomb import CoulombPlans, exponents_of, with_geometry
+    g, ga = _grad_with(mol, dmt, 'contraction', exponents=True)
+    gc = _grad_with(mol, dmt, 'contraction')
+    assert np.abs(g - gc).max() <= 1e-11 * np.abs(gc).max()
+    ex = exponents_of(mol)
+    fprims = [p for p, (sh, _) in enumerate((i, k) for i in range(mol.nbas)
+                                            for k in range(mol.bas[i, M.NPRIM_OF]))
+              if mol.bas[sh, M.ANG_OF] == 3]
+    for p in fprims[:3]:
+        hp = 1e-5 * ex[p]
+        ep, em = ex.copy(), ex.copy()
+        ep[p] += hp
+        em[p] -= hp
+        Ep = float(CoulombPlans(with_geometry(mol, exps=ep)).energy(dmt)[0])
+        Em = float(CoulombPlans(with_geometry(mol, exps=em)).energy(dmt)[0])
+        fd = (Ep - Em) / (2 * hp)
+        assert abs(fd - ga[p]) <= 1e-7 * max(1.0, abs(ga[p])), (p, fd, ga[p])
