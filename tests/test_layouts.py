@@ -101,3 +101,45 @@ def test_adjoint_layouts_fit(mode):
             assert L.off_w - L.off_aacc >= 4 * GRAD_MAXPRIM
         if L.nf <= W_SMEM:
             assert L.off_g - L.off_w >= L.nf
+
+
+GRADJ, GRADAJ = 7, 8
+
+
+def _np2(L):
+    return 0 if L < 0 else (L + 1) * (L + 2) // 2
+
+
+def _ntet(L):
+    return 0 if L < 0 else (L + 1) * (L + 2) * (L + 3) // 6
+
+
+@pytest.mark.parametrize('mode', [GRADJ, GRADAJ])
+def test_contraction_first_adjoint_layouts_fit(mode):
+    """Every l <= 4 class of the contraction-first adjoint fits 48 KB per warp: per-task densities
+    (4 tetrahedra each side), the lane-owned sums (3 + 2 tetrahedra of the raised ranges; with
+    exponents the four exponent weights and 64 per-primitive sums), then per term the record, the
+    VRR arrays of both raised ranges and the larger side's contraction buffers (+ 64 exponent
+    partials); strides odd."""
+    ex = mode == GRADAJ
+    d = 2 if ex else 1
+    for l in classes(4):
+        if l[0] * 16 + l[1] < l[2] * 16 + l[3]:
+            continue                       # kernel order: the larger pair first
+        L = layout(l, mode, WS_MAX)
+        assert L.T >= 1, l
+        Le, Lf = l[0] + l[1], l[2] + l[3]
+        assert (L.nmax, L.mmax) == (Le + d, Lf + d)
+        assert L.nroots == (sum(l) + d) // 2 + 1
+        na, nm = L.nmax + 1, L.mmax + 1
+        assert L.gax % 2 == 1 and L.gax >= na * nm and L.gstride == 3 * L.gax
+        assert L.termw % 2 == 1 and L.termw >= 13 + nm + (2 if ex else 0)
+        bufb = _np2(Lf) * na + (Lf + 1) * _np2(L.nmax)
+        bufk = _np2(Le) * nm + (Le + 1) * _np2(L.mmax)
+        assert L.scr >= max(bufb, bufk) + (64 if ex else 0) and L.scr % 2 == 1
+        fixed = 4 * _ntet(Le) + 4 * _ntet(Lf) + 3 * _ntet(L.nmax) + 2 * _ntet(L.mmax)
+        if ex:
+            fixed += 2 * _ntet(L.nmax) + 2 * _ntet(L.mmax) + 4 * GRAD_MAXPRIM
+        assert L.off_w == fixed and L.off_g == fixed + L.T * L.termw
+        assert L.off_scr == L.off_g + L.T * L.gstride
+        assert L.off_scr + L.T * L.scr <= WS_MAX
