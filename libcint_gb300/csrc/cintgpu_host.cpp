@@ -1072,12 +1072,14 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     }
     P->ncomp = CG_IS_IP(P->mode) ? 3 : 1;
     /* env[PTR_RANGE_OMEGA] > 0: long-range Coulomb erf(omega r)/r (src/g2e.c:4477-4492), the same
-     * screening as 1/r; < 0 (short-range erfc, src/g2e.c:4447-4476) is not provided */
-    if (!(env[PTR_RANGE_OMEGA] >= 0.0) || !std::isfinite(env[PTR_RANGE_OMEGA])) {
-        set_error("short-range Coulomb (env[PTR_RANGE_OMEGA] = %g < 0) is not supported", env[PTR_RANGE_OMEGA]);
-        return CINTGPU_ERR_UNSUPPORTED;
+     * screening as 1/r; < 0: short-range erfc(|omega| r)/r (src/g2e.c:4447-4476), kept as
+     * -omega^2: the kernels evaluate 2n terms per primitive quartet (full minus long range) and
+     * drop primitive quartets whose attenuated integral libcint neglects */
+    if (!std::isfinite(env[PTR_RANGE_OMEGA])) {
+        set_error("env[PTR_RANGE_OMEGA] = %g is not finite", env[PTR_RANGE_OMEGA]);
+        return CINTGPU_ERR_ARG;
     }
-    P->omega2 = env[PTR_RANGE_OMEGA] * env[PTR_RANGE_OMEGA];
+    P->omega2 = (env[PTR_RANGE_OMEGA] < 0 ? -1.0 : 1.0) * env[PTR_RANGE_OMEGA] * env[PTR_RANGE_OMEGA];
     /* src/g2e.c:57-62 (+1), src/g3c2e.c:55-59 and src/g2c2e.c:44-48 (no +1) */
     if (env[PTR_EXPCUTOFF] == 0) P->expcutoff = 60;
     else P->expcutoff = std::max(40.0, env[PTR_EXPCUTOFF]) + (P->three ? 0 : 1);
@@ -1300,6 +1302,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         if (cls_cost[ck] < 0) {
             cls_cost[ck] = per_primitive(P, pe.l) ? flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3])
                          : flops_per_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3], class_mode(P, pe.l));
+            if (P->omega2 < 0) cls_cost[ck] *= 2;   /* short range: full and long-range terms */
             cls_ref[ck] = P->mode == CG_MODE_ERI ? flops_libcint_primq(pe.l[0], pe.l[1], pe.l[2], pe.l[3]) : 0.0;
         }
         const double cpq = cls_cost[ck];
@@ -1369,10 +1372,11 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         }
         /* at least one batch of terms per slice, at least 4 primitive quartets; slices hold whole
          * batches (terms a multiple of T) so only a quartet's last slice has a partial batch */
-        int64_t slice = std::max<int64_t>(std::max<int64_t>(4, (L.T + L.nroots - 1) / L.nroots),
+        const int nt = L.nroots * (P->omega2 < 0 ? 2 : 1);   /* terms per primitive quartet */
+        int64_t slice = std::max<int64_t>(std::max<int64_t>(4, (L.T + nt - 1) / nt),
                                           (int64_t)(target / w.cost_pq));
         {
-            int a = L.T, b = L.nroots;
+            int a = L.T, b = nt;
             while (b) { int t = a % b; a = b; b = t; }
             const int64_t m = L.T / a;
             slice = (slice + m - 1) / m * m;
@@ -1623,6 +1627,7 @@ static int launch_grad_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.rys_coef = g_ctx.rys_coef;
     L.common_base = M_PI * M_PI * M_PI * 2 / 1.7724538509055160272981674833411451;
     L.omega2 = P->omega2;
+    L.expcut = P->expcutoff;
     L.ws_doubles = G.ws;
     L.dm = P->cur_dm;
     L.nao = P->nao_cart;
@@ -1661,6 +1666,7 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     L.rys_coef = g_ctx.rys_coef;
     L.common_base = M_PI * M_PI * M_PI * 2 / 1.7724538509055160272981674833411451;
     L.omega2 = P->omega2;
+    L.expcut = P->expcutoff;
     L.three = P->three;
     L.two = P->two;
     L.ws_doubles = G.ws;

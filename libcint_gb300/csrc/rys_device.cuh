@@ -444,14 +444,14 @@ __device__ __forceinline__ double common_fac_sp(int l)   /* libcint src/g1e.c:56
     return l == 0 ? 0.282094791773878143 : (l == 1 ? 0.488602511902919921 : 1.0);
 }
 
-/* Stage 1 for one term (primitive quartet q = kl * nij + ij, root r): x, prefactor, Rys node and
- * weight, and the division-free recurrence coefficients (libcint CINTg0_2e, src/g2e.c:4425-4545,
+/* Stage 1 for one term (primitive quartet q = kl * nij + ij, root r; short-range plans: 2n terms
+ * per primitive quartet, see below): x, prefactor, Rys node and weight, and the division-free recurrence coefficients (libcint CINTg0_2e, src/g2e.c:4425-4545,
  * rewritten in s = t^2: b00 = s / 2(aij+akl), b10 = b00 + (1-s)/2aij, b01 = b00 + (1-s)/2akl,
  * c00 = PA - s akl/(aij+akl) PQ, c0p = QC + s aij/(aij+akl) PQ).  rec[9] = weight * prefactor. */
 __device__ __forceinline__ void cg_term(const CGPrimPair &A, const CGPrimPair &B, const CGPair &pij,
                                         const CGPair &pkl, int n, int r, double common,
                                         const double *__restrict__ coef, double *rec,
-                                        double omega2 = 0.0)
+                                        double omega2 = 0.0, double expcut = 0.0)
 {
     double aijkl = A.a + B.a;
     double rs = rsqrt(aijkl);
@@ -462,7 +462,24 @@ __device__ __forceinline__ void cg_term(const CGPrimPair &A, const CGPrimPair &B
     double x = rho * rr;
     double s, w;
     double fac1 = common * A.K * B.K * rs * A.inv_a * B.inv_a;
-    if (omega2 > 0.0) {
+    if (omega2 < 0.0) {
+        /* short-range Coulomb erfc(omega r)/r, omega^2 = -omega2: the full quadrature (terms
+         * r < n) minus the long-range one (terms n <= r < 2n: nodes theta s, weights
+         * -sqrt(theta) w at theta x), libcint's two-quadrature form of CINTg0_2e
+         * (src/g2e.c:4447-4476) used here for every order; a primitive quartet whose theta x
+         * exceeds its screening budget (expcutoff - cce_ij - cce_kl) or 40 is dropped, as libcint
+         * does */
+        const double theta = -omega2 / (rho - omega2);
+        const double tx = theta * x;
+        if (r < n) {
+            rys_node(n, x, r, coef, s, w);
+        } else {
+            rys_node(n, tx, r - n, coef, s, w);
+            s *= theta;
+            fac1 *= -sqrt(theta);
+        }
+        if (tx > fmin(expcut - A.cce - B.cce, 40.0)) fac1 = 0.0;
+    } else if (omega2 > 0.0) {
         /* long-range Coulomb erf(omega r)/r (libcint CINTg0_2e, src/g2e.c:4477-4492): the
          * quadrature of theta x, theta = omega^2 / (omega^2 + rho), weights times sqrt(theta),
          * nodes t^2 -> theta t^2 (in s = t^2 the coefficients below stay linear in s) */

@@ -87,18 +87,19 @@ rys_grad_kernel(CGGradLaunch P)
         double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
         const int sI = L.dJ * L.dK * L.dL, sJ = L.dK * L.dL, sK = L.dL;
 
-        const int nterm = tk.npq * n;
+        const int nt = P.omega2 < 0.0 ? 2 * n : n;   /* terms per primitive quartet */
+        const int nterm = tk.npq * nt;
         for (int t0 = 0; t0 < nterm; t0 += T) {
             const int Tb = min(T, nterm - t0);
             if (lane < Tb) {
                 int g = t0 + lane;
-                int p = g / n, r = g - p * n;
+                int p = g / nt, r = g - p * nt;
                 int q = __ldg(pql + p);
                 int kl = q / nij, ij = q - kl * nij;
                 const CGPrimPair A = ppij[ij];
                 const CGPrimPair B = ppkl[kl];
                 double *rec = term + lane * CG_TERMW_GRAD;
-                cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec, P.omega2);
+                cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec, P.omega2, P.expcut);
                 rec[10] = 2.0 * A.aA;
                 rec[11] = 2.0 * (A.a - A.aA);
                 rec[12] = 2.0 * B.aA;
@@ -452,19 +453,20 @@ rys_gradj_kernel(CGGradLaunch P)
         const int nOm = cg_np2(Lf) * na, q2 = cg_np2(nmax);
         const int nOk = cg_np2(Le) * nm, q2k = cg_np2(mmax);
         const int emin = li > 0 ? li - 1 : 0, fmin = lk > 0 ? lk - 1 : 0;
-        const int nterm = tk.npq * n;
+        const int nt = P.omega2 < 0.0 ? 2 * n : n;   /* terms per primitive quartet */
+        const int nterm = tk.npq * nt;
         for (int t0 = 0; t0 < nterm; t0 += T) {
             const int Tb = min(T, nterm - t0);
             /* ---- stage 1: one lane per term */
             if (lane < Tb) {
                 int g = t0 + lane;
-                int p = g / n, r = g - p * n;
+                int p = g / nt, r = g - p * nt;
                 int q = __ldg(pql + p);
                 int kl = q / nij, ij = q - kl * nij;
                 const CGPrimPair A = ppij[ij];
                 const CGPrimPair B = ppkl[kl];
                 double *rec = term + lane * L.termw;
-                cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec, P.omega2);
+                cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec, P.omega2, P.expcut);
                 rec[10] = 2.0 * A.aA;
                 rec[11] = 2.0 * (A.a - A.aA);
                 rec[12] = 2.0 * B.aA;

@@ -191,19 +191,20 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
         for (int c = lane; c < L.nf * L.ncomp; c += 32) acc[c] = 0.0;
     }
 
-    const int nterm = tk.npq * n;
+    const int nt = P.omega2 < 0.0 ? 2 * n : n;   /* terms per primitive quartet */
+    const int nterm = tk.npq * nt;
     for (int t0 = 0; t0 < nterm; t0 += T) {
         const int Tb = min(T, nterm - t0);
         /* ---- stage 1: one lane per term */
         if (lane < Tb) {
             int g = t0 + lane;
-            int p = g / n, r = g - p * n;
+            int p = g / nt, r = g - p * nt;
             int q = __ldg(pql + p);
             int kl = q / nij, ij = q - kl * nij;
             const CGPrimPair A = ppij[ij];
             const CGPrimPair B = ppkl[kl];
             double *rec = term + lane * CG_TERMW;
-            cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec, P.omega2);
+            cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec, P.omega2, P.expcut);
             rec[10] = -2.0 * (MODE == CG_MODE_IP2 ? B.aA : A.aA);   /* -2 a of the nabla shell */
         }
         __syncwarp();
@@ -515,17 +516,18 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
         __syncwarp();
     }
 
-    const int nterm = tk.npq * n;
+    const int nt = P.omega2 < 0.0 ? 2 * n : n;   /* terms per primitive quartet */
+    const int nterm = tk.npq * nt;
     for (int t0 = 0; t0 < nterm; t0 += T) {
         const int Tb = min(T, nterm - t0);
         /* ---- stage 1: one lane per term */
         if (lane < Tb) {
             int g = t0 + lane;
-            int p = g / n, rr = g - p * n;
+            int p = g / nt, rr = g - p * nt;
             int q = __ldg(pql + p);
             int kl = q / nij, ij = q - kl * nij;
             double *rec = term + lane * L.termw;
-            cg_term(ppij[ij], ppkl[kl], pij, pkl, n, rr, common, P.rys_coef, rec, P.omega2);
+            cg_term(ppij[ij], ppkl[kl], pij, pkl, n, rr, common, P.rys_coef, rec, P.omega2, P.expcut);
             double mb = 0.0;
             for (int m = 0; m <= L.mmax; m++) { rec[10 + m] = mb; mb += rec[2]; }   /* m b01 */
         }

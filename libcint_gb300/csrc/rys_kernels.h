@@ -51,7 +51,9 @@ typedef struct {
     int *status;
     const double *rys_coef;
     double common_base;       /* 2 pi^3 / sqrt(pi); times the s/p factors per task */
-    double omega2;            /* omega^2 of the long-range Coulomb erf(omega r)/r; 0: 1/r */
+    double omega2;            /* omega^2 of the long-range Coulomb erf(omega r)/r, minus omega^2 of
+                                 the short-range erfc(omega r)/r; 0: 1/r */
+    double expcut;            /* libcint's expcutoff (short-range screening of primitive quartets) */
     int three;                /* int3c2e, int2c2e: the fourth shell is the unit s partner */
     int two;                  /* int2c2e: the second shell is a unit s partner as well */
     int ws_doubles;
@@ -92,7 +94,8 @@ typedef struct {
     int *status;
     const double *rys_coef;
     double common_base;
-    double omega2;            /* omega^2 of the long-range Coulomb; 0: 1/r */
+    double omega2;            /* as CGLaunch::omega2 */
+    double expcut;
     int ws_doubles;
     const double *dm;         /* Cartesian density, nao x nao */
     int nao;

@@ -110,23 +110,27 @@ static int tridiag_ql(int n, double *d, double *e, double *z)
     return 0;
 }
 
-/* Rys quadrature for weight exp(-x t^2) on t in [0,1] with nodes in s = t^2.
- * Mirrors the contract of CINTrys_roots (src/rys_roots.c:57-122): u = s/(1-s), sum w = F_0(x). */
-int oracle_rys_roots(int nroots, double x, double *u, double *w)
+/* Rys quadrature for weight exp(-x t^2) on t in [lower, 1] with nodes in s = t^2: lower = 0 is
+ * the Coulomb operator (the contract of CINTrys_roots, src/rys_roots.c:57-122: u = s/(1-s),
+ * sum w = F_0(x)); lower = sqrt(theta) the short-range erfc(omega r)/r one (the contract of
+ * CINTsr_rys_roots, src/rys_roots.c:149-267, whose methods are not restated: the same discretised
+ * Stieltjes procedure as for lower = 0 on the shorter interval). */
+int oracle_rys_roots_range(int nroots, double x, double lower, double *u, double *w)
 {
     if (nroots < 1 || nroots > MAXROOTS) return 1;
-    /* integrand negligible beyond x t^2 = K (K grows with the polynomial degree 4n) */
+    /* integrand negligible beyond x (t^2 - lower^2) = K (K grows with the polynomial degree 4n) */
     double tmax = 1.0;
     double K = 80.0 + 8.0 * nroots;
-    if (x * 1.0 > K) tmax = sqrt(K / x);
+    if (x * (1.0 - lower * lower) > K) tmax = sqrt(lower * lower + K / x);
     double s[NGL], W[NGL], q[NGL], qp[NGL], r[NGL];
     static const int M = NGL;
     double Q[MAXROOTS + 1][NGL];
     double mu0 = 0;
+    const double span = tmax - lower;
     for (int j = 0; j < M; j++) {
-        double t = tmax * gl_t[j];
+        double t = lower + span * gl_t[j];
         s[j] = t * t;
-        W[j] = tmax * gl_w[j] * exp(-x * t * t);
+        W[j] = span * gl_w[j] * exp(-x * t * t);
         mu0 += W[j];
     }
     double alpha[MAXROOTS], beta[MAXROOTS + 1];
@@ -173,6 +177,11 @@ int oracle_rys_roots(int nroots, double x, double *u, double *w)
         w[i] = wt[i];
     }
     return 0;
+}
+
+int oracle_rys_roots(int nroots, double x, double *u, double *w)
+{
+    return oracle_rys_roots_range(nroots, x, 0.0, u, w);
 }
 
 /* ------------------------------------------------------------------ cart -> sph */
@@ -335,9 +344,11 @@ typedef struct {
     ((((((size_t)(c) * (G)->n + (r)) * (G)->di + (i)) * (G)->dj + (j)) * (G)->dk + (k)) * (G)->dl + (l))
 
 /* CINTg0_2e (src/g2e.c:4425-4545) + CINTg0_2e_2d (VRR, :272-421) + HRR (:428-693), written
- * with i and k as the recurrence bases.  P, Q: pair centres; aij, akl: pair exponents. */
+ * with i and k as the recurrence bases.  P, Q: pair centres; aij, akl: pair exponents; cutoff:
+ * the primitive quartet's remaining screening budget (expcutoff - cce_ij - cce_kl).  Returns 1
+ * when the short-range operator screens the primitive quartet out, -1 on failure. */
 static int g0_2e(const OEnv *E, GArr *G, const double *P, const double *Q,
-                 double aij, double akl, double fac)
+                 double aij, double akl, double fac, double cutoff)
 {
     const int n = E->nroots;
     double u[MAXROOTS], w[MAXROOTS];
@@ -347,8 +358,15 @@ static int g0_2e(const OEnv *E, GArr *G, const double *P, const double *Q,
     double a0 = a1 / (aij + akl);
     double fac1 = sqrt(a0 / (a1 * a1 * a1)) * fac;
     double x = a0 * rr;
-    double theta = 1;
-    if (E->omega > 0) {
+    double theta = 1, lower = 0;
+    if (E->omega < 0) {
+        /* short-range erfc(omega r)/r (src/g2e.c:4447-4476): the Rys weight restricted to
+         * t >= sqrt(theta), theta = omega^2/(omega^2 + a0); a primitive quartet whose theta x
+         * exceeds its screening budget (or 40) is dropped, as libcint does */
+        theta = E->omega * E->omega / (E->omega * E->omega + a0);
+        if (theta * x > cutoff || theta * x > 40.0) return 1;
+        lower = sqrt(theta);
+    } else if (E->omega > 0) {
         /* long-range Coulomb erf(omega r)/r (src/g2e.c:4477-4492): the Rys quadrature of
          * x' = theta x with theta = omega^2/(omega^2 + a0), weights times sqrt(theta), and every
          * node mapped to t^2 -> theta t^2, i.e. u -> theta u / (1 + u - theta u) */
@@ -356,7 +374,7 @@ static int g0_2e(const OEnv *E, GArr *G, const double *P, const double *Q,
         x *= theta;
         fac1 *= sqrt(theta);
     }
-    if (oracle_rys_roots(n, x, u, w)) return -1;
+    if (oracle_rys_roots_range(n, x, lower, u, w)) return -1;
     if (E->omega > 0)
         for (int r = 0; r < n; r++) u[r] = theta * u[r] / (1 + u[r] - theta * u[r]);
     const int nmax = E->lc[0] + E->lc[1];
@@ -584,7 +602,9 @@ static int contracted(const OEnv *E, double *gctr, int ncomp)
             if (pd->cce > eijcutoff) continue;
             double aij = E->ex[0][ip] + E->ex[1][jp];
             double fac = E->common * pd->e * ekl;
-            if (g0_2e(E, &G, pd->r, Q, aij, akl, fac)) { empty = 1; goto done; }
+            const int rc = g0_2e(E, &G, pd->r, Q, aij, akl, fac, eijcutoff - pd->cce);
+            if (rc < 0) { empty = 1; goto done; }
+            if (rc > 0) continue;
             gout(E, &G, E->dslot == 2 ? ak : E->ex[0][ip], gp, ncomp);
             empty = 0;
             /* prim -> contracted for every contraction pattern (src/g1e.c:530-559) */
@@ -679,7 +699,7 @@ static int driver(double *out, int *dims, int *shls, int *atm, int *bas, double 
 {
     OEnv E;
     init_env(&E, shls, atm, bas, env, three, dinc, dslot);
-    if (E.omega < 0) return -1;   /* short-range Coulomb is not restated */
+
     int ncomp = dinc ? 3 : 1;
     int nf = ncart(E.l[0]) * ncart(E.l[1]) * ncart(E.l[2]) * ncart(E.l[3]);
     int nc = E.nctr[0] * E.nctr[1] * E.nctr[2] * E.nctr[3];

@@ -22,6 +22,8 @@ extern "C" {
 /* u[i] = t_i^2/(1-t_i^2), w[i] = weights of int_0^1 f(t^2) exp(-x t^2) dt; mirrors
  * CINTrys_roots (libcint src/rys_roots.c:57-122). Returns 0 on success. */
 int oracle_rys_roots(int nroots, double x, double *u, double *w);
+/* the same for the weight restricted to t in [lower, 1] (short-range Coulomb: lower = sqrt(theta)) */
+int oracle_rys_roots_range(int nroots, double x, double lower, double *u, double *w);
 
 /* Same meaning and argument order as libcint's int2e_sph etc. opt and cache are ignored
  * (the restatement always takes the no-optimizer path, src/cint2e.c:57-269). */

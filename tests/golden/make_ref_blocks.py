@@ -28,6 +28,8 @@ Contents (all through libcint 6.1.1 built by oracle/Makefile, opt = NULL, cache 
   lr_c0_int2e_sph / lr_c0_int2e_ip1_sph / lr_c2_int3c2e_sph / lr_c2_int2c2e_sph
                                      long-range Coulomb erf(omega r)/r (env[PTR_RANGE_OMEGA] =
                                      0.3 for c0(3), 0.5 for the c2 molecule): 30 / 30 / 40 / 40 items
+  sr_c0_* / sr_c2_*                  the same items with short-range Coulomb erfc(omega r)/r
+                                     (env[PTR_RANGE_OMEGA] = -0.3, -0.5)
   cache_sizes                        the out == NULL cache-size answers for a few items
 Each block is stored flattened in libcint's (Fortran) order with its item list.
 """
@@ -175,6 +177,18 @@ def main():
                                                for t in tr[:40]])
     out['lr_c2_int2c2e_sph_items'] = pr[:40]
     out['lr_c2_int2c2e_sph'] = np.concatenate([o.ref.call('int2c2e_sph', m2, t)[1].ravel(order='F')
+                                               for t in pr[:40]])
+    # short-range Coulomb erfc(omega r)/r (env[PTR_RANGE_OMEGA] < 0): the same items
+    m0.env[8] = -0.3
+    for name in ('int2e_sph', 'int2e_ip1_sph'):
+        out['sr_c0_' + name + '_items'] = qs[:30]
+        out['sr_c0_' + name] = np.concatenate([o.ref.call(name, m0, q)[1].ravel(order='F') for q in qs[:30]])
+    m2.env[8] = -0.5
+    out['sr_c2_int3c2e_sph_items'] = tr[:40]
+    out['sr_c2_int3c2e_sph'] = np.concatenate([o.ref.call('int3c2e_sph', m2, t)[1].ravel(order='F')
+                                               for t in tr[:40]])
+    out['sr_c2_int2c2e_sph_items'] = pr[:40]
+    out['sr_c2_int2c2e_sph'] = np.concatenate([o.ref.call('int2c2e_sph', m2, t)[1].ravel(order='F')
                                                for t in pr[:40]])
     # libcint's own errors per item against the long-double restatement (the referee): largest
     # absolute error, and largest relative error on elements above 1e-10 and above c of the

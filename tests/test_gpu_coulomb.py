@@ -204,7 +204,7 @@ def _grad_with(mol, dmt, adjoint, quartets=None, exponents=False):
             os.environ['CINTGPU_ADJOINT'] = old
 
 
-@pytest.mark.parametrize('case', ['c3', 'g_shells', 'long_range'])
+@pytest.mark.parametrize('case', ['c3', 'g_shells', 'long_range', 'short_range'])
 def test_contraction_first_adjoint_matches_per_component(gpulib, case):
     """The two adjoint kernels: contraction first (densities carried through the transfers, the
     default) and per Cartesian component (CINTGPU_ADJOINT=component) on every unique quartet of a
@@ -231,6 +231,8 @@ def test_contraction_first_adjoint_matches_per_component(gpulib, case):
         mol, dm = _system(natm=5, seed=3)
         if case == 'long_range':
             mol.env[8] = 0.6           # env[PTR_RANGE_OMEGA]: long-range Coulomb
+        elif case == 'short_range':
+            mol.env[8] = -0.6
     dmt = torch.as_tensor(dm, device='cuda')
     g1 = _grad_with(mol, dmt, 'contraction', quartets)
     g2 = _grad_with(mol, dmt, 'component', quartets)

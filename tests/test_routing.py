@@ -101,7 +101,7 @@ def test_invalid_input_is_rejected_with_a_message():
         ('l = 7', _variant(mol, 'bas', (3, M.ANG_OF), 7), q, -3, 'angular momentum'),
         ('nprim = 65', _variant(mol, 'bas', (3, M.NPRIM_OF), 65), q, -1, 'nprim'),
         ('atom out of range', _variant(mol, 'bas', (3, M.ATOM_OF), 99), q, -1, 'atom'),
-        ('omega < 0', _variant(mol, 'env', 8, -0.3), q, -3, 'short-range'),
+        ('omega = NaN', _variant(mol, 'env', 8, float('nan')), q, -1, 'not finite'),
         ('NaN coordinate', _variant(mol, 'env', int(mol.atm[mol.bas[2, M.ATOM_OF], M.PTR_COORD]) + 1,
                                     float('nan')), q, -1, 'non-finite coordinate'),
         ('Inf exponent', _variant(mol, 'env', int(mol.bas[1, M.PTR_EXP]), float('inf')), q, -1,
@@ -112,6 +112,9 @@ def test_invalid_input_is_rejected_with_a_message():
     for what, m, items, code, text in cases:
         assert _build(cg.INT2E_SPH, m, items) == code, what
         assert text in cg.last_error(), (what, cg.last_error())
+    # short range (omega < 0) and long range (omega > 0) are both accepted
+    assert _build(cg.INT2E_SPH, _variant(mol, 'env', 8, -0.3), q) == 0
+    assert _build(cg.INT2E_SPH, _variant(mol, 'env', 8, 0.3), q) == 0
     # adjoint limits: l <= 4; exponent adjoint: nprim <= 16
     lg = _variant(mol, 'bas', (3, M.ANG_OF), 5)
     assert _build(8, lg, q) == -3 and 'adjoint' in cg.last_error()
