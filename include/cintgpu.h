@@ -85,6 +85,13 @@ CACHE_SIZE_T int2e_ip2_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT 
 CACHE_SIZE_T int2e_ip2_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
                             FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
 void int2e_ip2_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
+/* (nabla nabla i j|kl), 9 components (xx, xy, xz, yx, ..., zz); libcint
+ * src/autocode/hess.c:1175-1194 (ng = {2,0,0,0,...}) */
+CACHE_SIZE_T int2e_ipip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                             FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+CACHE_SIZE_T int2e_ipip1_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
+                              FINT *bas, FINT nbas, double *env, CINTOpt *opt, double *cache);
+void int2e_ipip1_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env);
 /* (nabla i j|k) and (ij|nabla k), 3 components each; libcint src/autocode/int3c2e.c:72-87 and
  * :153-168 */
 CACHE_SIZE_T int3c2e_ip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm,
@@ -133,6 +140,12 @@ FINT cint2e_ip2_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, F
                      double *env, CINTOpt *opt);
 void cint2e_ip2_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas,
                               double *env);
+FINT cint2e_ipip1_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                      double *env, CINTOpt *opt);
+FINT cint2e_ipip1_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                       double *env, CINTOpt *opt);
+void cint2e_ipip1_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas,
+                                double *env);
 FINT cint3c2e_ip1_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
                       double *env, CINTOpt *opt);
 FINT cint3c2e_ip1_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas,
@@ -179,6 +192,8 @@ void CINTshells_spheric_offset(FINT ao_loc[], const FINT *bas, const FINT nbas);
 #define CINTGPU_INT3C2E_IP1_CART 17
 #define CINTGPU_INT3C2E_IP2_SPH  18 /* (ij|nabla k), 3 components */
 #define CINTGPU_INT3C2E_IP2_CART 19
+#define CINTGPU_INT2E_IPIP1_SPH  20 /* (nabla nabla i j|kl), 9 components */
+#define CINTGPU_INT2E_IPIP1_CART 21
 
 #define CINTGPU_OK              0
 #define CINTGPU_ERR_ARG        -1   /* invalid argument (shell index, l, nprim, omega != 0) */

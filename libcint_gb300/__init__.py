@@ -16,7 +16,9 @@ INT2E_SPH, INT2E_CART, INT2E_IP1_SPH, INT2E_IP1_CART, INT3C2E_SPH, INT3C2E_CART 
 INT2C2E_SPH, INT2C2E_CART = 12, 13
 INT2E_IP2_SPH, INT2E_IP2_CART = 14, 15
 INT3C2E_IP1_SPH, INT3C2E_IP1_CART, INT3C2E_IP2_SPH, INT3C2E_IP2_CART = 16, 17, 18, 19
-_KIND_NSH = {1: 4, 2: 4, 3: 4, 4: 4, 5: 3, 6: 3, 12: 2, 13: 2, 14: 4, 15: 4, 16: 3, 17: 3, 18: 3, 19: 3}
+INT2E_IPIP1_SPH, INT2E_IPIP1_CART = 20, 21
+_KIND_NSH = {1: 4, 2: 4, 3: 4, 4: 4, 5: 3, 6: 3, 12: 2, 13: 2, 14: 4, 15: 4, 16: 3, 17: 3, 18: 3, 19: 3,
+             20: 4, 21: 4}
 
 _lib = None
 
@@ -38,19 +40,21 @@ def lib():
     vp, i32, i64, dbl = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
     for name in ('int2e_sph', 'int2e_cart', 'int2e_ip1_sph', 'int2e_ip1_cart', 'int3c2e_sph',
                  'int3c2e_cart', 'int2c2e_sph', 'int2c2e_cart', 'int2e_ip2_sph', 'int2e_ip2_cart',
-                 'int3c2e_ip1_sph', 'int3c2e_ip1_cart', 'int3c2e_ip2_sph', 'int3c2e_ip2_cart'):
+                 'int3c2e_ip1_sph', 'int3c2e_ip1_cart', 'int3c2e_ip2_sph', 'int3c2e_ip2_cart',
+                 'int2e_ipip1_sph', 'int2e_ipip1_cart'):
         f = getattr(L, name)
         f.restype = i32
         f.argtypes = [vp, vp, vp, vp, i32, vp, i32, vp, vp, vp]
     for name in ('cint2e_sph', 'cint2e_cart', 'cint2e_ip1_sph', 'cint2e_ip1_cart', 'cint3c2e_sph',
                  'cint3c2e_cart', 'cint2c2e_sph', 'cint2c2e_cart', 'cint2e_ip2_sph',
                  'cint2e_ip2_cart', 'cint3c2e_ip1_sph', 'cint3c2e_ip1_cart', 'cint3c2e_ip2_sph',
-                 'cint3c2e_ip2_cart'):
+                 'cint3c2e_ip2_cart', 'cint2e_ipip1_sph', 'cint2e_ipip1_cart'):
         f = getattr(L, name)
         f.restype = i32
         f.argtypes = [vp, vp, vp, i32, vp, i32, vp, vp]
     for name in ('int2e_optimizer', 'int2e_ip1_optimizer', 'int3c2e_optimizer', 'int2c2e_optimizer',
-                 'int2e_ip2_optimizer', 'int3c2e_ip1_optimizer', 'int3c2e_ip2_optimizer'):
+                 'int2e_ip2_optimizer', 'int3c2e_ip1_optimizer', 'int3c2e_ip2_optimizer',
+                 'int2e_ipip1_optimizer'):
         f = getattr(L, name)
         f.restype = None
         f.argtypes = [vp, vp, i32, vp, i32, vp]
@@ -220,7 +224,7 @@ def dropin(name, mol, shls, dims=None, nbas=None):
     nsh = 3 if 'int3c2e' in name else (2 if 'int2c2e' in name else 4)
     shls = np.ascontiguousarray(shls, dtype=np.int32)
     sph = name.endswith('_sph')
-    ncomp = 3 if ('_ip1' in name or '_ip2' in name) else 1
+    ncomp = 9 if '_ipip1' in name else (3 if ('_ip1' in name or '_ip2' in name) else 1)
     cnt = [(mol.nsph(s) if sph else mol.ncart(s)) for s in shls[:nsh]]
     n = int(np.prod(cnt)) * ncomp
     out = np.zeros(n if dims is None else int(np.prod(dims)) * ncomp)

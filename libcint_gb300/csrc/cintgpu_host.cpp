@@ -625,6 +625,8 @@ double flops_per_primq(int li, int lj, int lk, int ll, int mode)
     }
     double per_root = 20 + 3 * 5 * vrr + 3 * 2 * hrr;
     if (mode == CG_MODE_IP1) per_root += 3 * 3 * (double)L.G / L.dI * (L.dI - 1) + 9.0 * L.nf;
+    else if (mode == CG_MODE_IPIP1)
+        per_root += 3 * 3 * (double)L.G / L.dI * (2 * L.dI - 3) + 18.0 * L.nf;
     else if (mode == CG_MODE_IP2) per_root += 3 * 3 * (double)L.G / L.dK * (L.dK - 1) + 9.0 * L.nf;
     else if (mode == CG_MODE_GRAD || mode == CG_MODE_GRADA) {
         double nT = (double)(li + 1) * (lj + 1) * (lk + 1) * (ll + 1);
@@ -1023,7 +1025,7 @@ static int kind_shells(int kind)
 static bool kind_sph(int kind)
 {
     return kind == CINTGPU_INT2E_SPH || kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT3C2E_SPH
-        || kind == CINTGPU_INT2C2E_SPH || kind == CINTGPU_INT2E_IP2_SPH
+        || kind == CINTGPU_INT2C2E_SPH || kind == CINTGPU_INT2E_IP2_SPH || kind == CINTGPU_INT2E_IPIP1_SPH
         || kind == CINTGPU_INT3C2E_IP1_SPH || kind == CINTGPU_INT3C2E_IP2_SPH;
 }
 
@@ -1042,6 +1044,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     case CINTGPU_INT2E_IP1_CART: P->mode = CG_MODE_IP1; P->sph = 0; P->three = 0; break;
     case CINTGPU_INT2E_IP2_SPH: P->mode = CG_MODE_IP2; P->sph = 1; P->three = 0; break;
     case CINTGPU_INT2E_IP2_CART: P->mode = CG_MODE_IP2; P->sph = 0; P->three = 0; break;
+    case CINTGPU_INT2E_IPIP1_SPH: P->mode = CG_MODE_IPIP1; P->sph = 1; P->three = 0; break;
+    case CINTGPU_INT2E_IPIP1_CART: P->mode = CG_MODE_IPIP1; P->sph = 0; P->three = 0; break;
     case CINTGPU_INT3C2E_IP1_SPH: P->mode = CG_MODE_IP1; P->sph = 1; P->three = 1; break;
     case CINTGPU_INT3C2E_IP1_CART: P->mode = CG_MODE_IP1; P->sph = 0; P->three = 1; break;
     case CINTGPU_INT3C2E_IP2_SPH: P->mode = CG_MODE_IP2; P->sph = 1; P->three = 1; break;
@@ -1070,7 +1074,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         break;
     default: set_error("unknown integral kind %d", kind); return CINTGPU_ERR_ARG;
     }
-    P->ncomp = CG_IS_IP(P->mode) ? 3 : 1;
+    P->ncomp = CG_NCOMP(P->mode);
     /* env[PTR_RANGE_OMEGA] > 0: long-range Coulomb erf(omega r)/r (src/g2e.c:4477-4492), the same
      * screening as 1/r; < 0: short-range erfc(|omega| r)/r (src/g2e.c:4447-4476), kept as
      * -omega^2: the kernels evaluate 2n terms per primitive quartet (full minus long range) and
@@ -1105,7 +1109,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     }
     const int nsh = kind_shells(kind);
     /* the derivative raises the l ceiling entering libcint's log_rr of the differentiated pair */
-    const int dinc = P->mode == CG_MODE_IP1 ? 1 : 0, dinc_k = P->mode == CG_MODE_IP2 ? 1 : 0;
+    const int dinc = P->mode == CG_MODE_IP1 ? 1 : (P->mode == CG_MODE_IPIP1 ? 2 : 0);
+    const int dinc_k = P->mode == CG_MODE_IP2 ? 1 : 0;
 
     struct Pending { int pij, pkl, out; int64_t npq; int l[4]; int sym; };
     std::vector<Pending> pend;
@@ -1812,6 +1817,8 @@ CACHE_SIZE_T cache_size_query(int kind, const int *shls, const int *bas)
      * for ip2; one g-array shift and 3 components for both */
     int iinc = kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT2E_IP1_CART
             || kind == CINTGPU_INT3C2E_IP1_SPH || kind == CINTGPU_INT3C2E_IP1_CART;
+    const int ipip = kind == CINTGPU_INT2E_IPIP1_SPH || kind == CINTGPU_INT2E_IPIP1_CART;
+    if (ipip) iinc = 2;   /* hess.c ng = {2, 0, 0, 0, 2 (GSHIFT), 1, 1, 9} */
     int kinc = kind == CINTGPU_INT2E_IP2_SPH || kind == CINTGPU_INT2E_IP2_CART
             || kind == CINTGPU_INT3C2E_IP2_SPH || kind == CINTGPU_INT3C2E_IP2_CART;
     int ip1 = iinc || kinc;
@@ -1821,7 +1828,7 @@ CACHE_SIZE_T cache_size_query(int kind, const int *shls, const int *bas)
         const int *b = bas + BAS_SLOTS * shls[a];
         l[a] = b[ANG_OF]; np[a] = b[NPRIM_OF]; nc[a] = b[NCTR_OF];
     }
-    int ncomp = ip1 ? 3 : 1, gbits = ip1 ? 1 : 0;
+    int ncomp = ipip ? 9 : (ip1 ? 3 : 1), gbits = ipip ? 2 : (ip1 ? 1 : 0);
     int lic = l[0] + iinc, ljc = l[1], lkc = l[2] + kinc, llc = l[3];
     size_t nf = (size_t)ncart_l(l[0]) * ncart_l(l[1]) * ncart_l(l[2]) * (three ? 1 : ncart_l(l[3]));
     size_t ncx = nf * nc[0] * nc[1] * nc[2] * (three ? 1 : nc[3]);
@@ -1862,6 +1869,7 @@ CACHE_SIZE_T dropin(int kind, double *out, FINT *dims, FINT *shls, FINT *atm, FI
     const int nsh = kind_shells(kind);
     int ncomp = (kind == CINTGPU_INT2E_IP1_SPH || kind == CINTGPU_INT2E_IP1_CART
                  || (kind >= CINTGPU_INT2E_IP2_SPH && kind <= CINTGPU_INT3C2E_IP2_CART)) ? 3 : 1;
+    if (kind == CINTGPU_INT2E_IPIP1_SPH || kind == CINTGPU_INT2E_IPIP1_CART) ncomp = 9;
     int sph = kind_sph(kind);
     int counts[4] = {1, 1, 1, 1};
     for (int a = 0; a < nsh; a++) {
@@ -2698,6 +2706,12 @@ CACHE_SIZE_T int2e_ip2_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT 
 CACHE_SIZE_T int2e_ip2_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                             FINT nbas, double *env, CINTOpt *opt, double *cache)
 { (void)cache; return dropin(CINTGPU_INT2E_IP2_CART, out, dims, shls, atm, natm, bas, nbas, env, opt); }
+CACHE_SIZE_T int2e_ipip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                             FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)cache; return dropin(CINTGPU_INT2E_IPIP1_SPH, out, dims, shls, atm, natm, bas, nbas, env, opt); }
+CACHE_SIZE_T int2e_ipip1_cart(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
+                              FINT nbas, double *env, CINTOpt *opt, double *cache)
+{ (void)cache; return dropin(CINTGPU_INT2E_IPIP1_CART, out, dims, shls, atm, natm, bas, nbas, env, opt); }
 CACHE_SIZE_T int3c2e_ip1_sph(double *out, FINT *dims, FINT *shls, FINT *atm, FINT natm, FINT *bas,
                              FINT nbas, double *env, CINTOpt *opt, double *cache)
 { (void)cache; return dropin(CINTGPU_INT3C2E_IP1_SPH, out, dims, shls, atm, natm, bas, nbas, env, opt); }
@@ -2737,6 +2751,8 @@ void int2e_ip2_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nb
 { (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
 void int3c2e_ip1_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
 { (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
+void int2e_ipip1_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
 void int3c2e_ip2_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
 { (void)atm; (void)natm; (void)bas; (void)env; make_opt(opt, nbas); }
 void CINTdel_2e_optimizer(CINTOpt **opt)
@@ -2772,6 +2788,12 @@ FINT cint2e_ip2_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, F
 { return int2e_ip2_cart(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
 void cint2e_ip2_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
 { int2e_ip2_optimizer(opt, atm, natm, bas, nbas, env); }
+FINT cint2e_ipip1_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int2e_ipip1_sph(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+FINT cint2e_ipip1_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
+{ return int2e_ipip1_cart(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
+void cint2e_ipip1_sph_optimizer(CINTOpt **opt, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env)
+{ int2e_ipip1_optimizer(opt, atm, natm, bas, nbas, env); }
 FINT cint3c2e_ip1_sph(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)
 { return int3c2e_ip1_sph(out, NULL, shls, atm, natm, bas, nbas, env, opt, NULL); }
 FINT cint3c2e_ip1_cart(double *out, FINT *shls, FINT *atm, FINT natm, FINT *bas, FINT nbas, double *env, CINTOpt *opt)

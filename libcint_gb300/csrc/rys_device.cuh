@@ -64,6 +64,7 @@ __host__ __device__ inline void cg_mode_incs(int mode, int inc[4])
 {
     inc[0] = inc[1] = inc[2] = inc[3] = 0;
     if (mode == CG_MODE_IP1) inc[0] = 1;
+    else if (mode == CG_MODE_IPIP1) inc[0] = 2;   /* libcint hess.c ng = {2,0,0,0,...} */
     else if (mode == CG_MODE_IP2) inc[2] = 1;   /* libcint grad2.c ng = {0,0,1,0,...} */
     else if (mode == CG_MODE_GRAD) { inc[0] = 1; inc[1] = 1; inc[2] = 1; }
     else if (mode == CG_MODE_GRADA) { inc[0] = 2; inc[1] = 2; inc[2] = 2; inc[3] = 2; }
@@ -88,9 +89,9 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
     L->mmax = lkc + llc;
     L->dI = L->lic + 1; L->dJ = ljc + 1; L->dK = lkc + 1; L->dL = llc + 1;
     L->G = L->dI * L->dJ * L->dK * L->dL;
-    L->ng = CG_IS_IP(mode) ? 2 : 1;
+    L->ng = CG_NG(mode);
     L->nf = ncart(li) * ncart(lj) * ncart(lk) * ncart(ll);
-    L->ncomp = CG_IS_IP(mode) ? 3 : 1;
+    L->ncomp = CG_NCOMP(mode);
     /* per-lane scratch of g_axis; an odd stride keeps the 32 lanes' equal offsets in distinct
      * shared-memory banks */
     L->scr = (L->nmax + 1) * (L->mmax + 1) + (L->nmax + 1) + (L->mmax + 1);

@@ -159,7 +159,10 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
 
     /* per-lane component offsets into the g arrays (register path: packed 10 bits per axis, G < 1024) */
     int offs[NS > 0 ? NS : 1];
-    double ra[NS > 0 ? NS : 1][CG_IS_IP(MODE) ? 3 : 1];
+    /* accumulators per component: 1; 3 nabla components; 6 distinct second-nabla components
+     * (xx, yy, zz, xy, xz, yz) */
+    constexpr int NACC = MODE == CG_MODE_IPIP1 ? 6 : (CG_IS_IP(MODE) ? 3 : 1);
+    double ra[NS > 0 ? NS : 1][NACC];
     auto comp_offsets3 = [&](int c, int &ox, int &oy, int &oz) {
         int ic = c % nfi, rest = c / nfi;
         int kc = rest % nfk; rest /= nfk;
@@ -185,7 +188,7 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             int c = lane + 32 * s;
             offs[s] = c < L.nf ? comp_offsets(c) : 0;
 #pragma unroll
-            for (int q = 0; q < (CG_IS_IP(MODE) ? 3 : 1); q++) ra[s][q] = 0.0;
+            for (int q = 0; q < NACC; q++) ra[s][q] = 0.0;
         }
     } else {
         for (int c = lane; c < L.nf * L.ncomp; c += 32) acc[c] = 0.0;
@@ -216,16 +219,20 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
             double *gdst = greg + (size_t)(t * 3 + ax) * L.gax;
             g_axis(L, rec[0], rec[1], rec[2], rec[3 + ax], rec[6 + ax], g00,
                    pij.AB[ax], pkl.AB[ax], scr_base + lane * L.scr, gdst, (tk.sym >> 3) & 3);
-            if (MODE == CG_MODE_IP1) {
-                /* f(i) = i g(i-1) - 2 a_i g(i+1)   (CINTnabla1i_2e, src/g2e.c:4550-4591) */
+            if (MODE == CG_MODE_IP1 || MODE == CG_MODE_IPIP1) {
+                /* f(i) = i g(i-1) - 2 a_i g(i+1)   (CINTnabla1i_2e, src/g2e.c:4550-4591); with two
+                 * nablas the same once more on f: h(i) = i f(i-1) - 2 a_i f(i+1) */
                 const double ai2 = rec[10];
                 const int sI = L.dJ * L.dK * L.dL;
-                double *f = gdst + L.G;
-                for (int i = 0; i < L.dI - 1; i++) {
-                    for (int o = 0; o < sI; o++) {
-                        double v = ai2 * gdst[(i + 1) * sI + o];
-                        if (i > 0) v = fma((double)i, gdst[(i - 1) * sI + o], v);
-                        f[i * sI + o] = v;
+                for (int pass = 0; pass < (MODE == CG_MODE_IPIP1 ? 2 : 1); pass++) {
+                    const double *g = gdst + pass * L.G;
+                    double *f = gdst + (pass + 1) * L.G;
+                    for (int i = 0; i < L.dI - 1 - pass; i++) {
+                        for (int o = 0; o < sI; o++) {
+                            double v = ai2 * g[(i + 1) * sI + o];
+                            if (i > 0) v = fma((double)i, g[(i - 1) * sI + o], v);
+                            f[i * sI + o] = v;
+                        }
                     }
                 }
             } else if (MODE == CG_MODE_IP2) {
@@ -255,7 +262,24 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                 if (lane + 32 * s >= L.nf) continue;
                 const int ox = offs[s] & 1023, oy = (offs[s] >> 10) & 1023, oz = offs[s] >> 20;
                 const double *gb = greg;
-                if (CG_IS_IP(MODE)) {
+                if (MODE == CG_MODE_IPIP1) {
+                    double a[6];
+#pragma unroll
+                    for (int q = 0; q < 6; q++) a[q] = ra[s][q < NACC ? q : 0];
+                    for (int t = 0; t < Tb; t++, gb += stride_t) {
+                        const double gx = gb[ox], gy = gb[A + oy], gz = gb[2 * A + oz];
+                        const double fx = gb[G + ox], fy = gb[A + G + oy], fz = gb[2 * A + G + oz];
+                        const double hx = gb[2 * G + ox], hy = gb[A + 2 * G + oy], hz = gb[2 * A + 2 * G + oz];
+                        a[0] = fma(hx, gy * gz, a[0]);
+                        a[1] = fma(hy, gx * gz, a[1]);
+                        a[2] = fma(hz, gx * gy, a[2]);
+                        a[3] = fma(fx * fy, gz, a[3]);
+                        a[4] = fma(fx * fz, gy, a[4]);
+                        a[5] = fma(fy * fz, gx, a[5]);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 6; q++) ra[s][q < NACC ? q : 0] = a[q];
+                } else if (CG_IS_IP(MODE)) {
                     double sx = ra[s][0], sy = ra[s][CG_IS_IP(MODE) ? 1 : 0],
                            sz = ra[s][CG_IS_IP(MODE) ? 2 : 0];
                     for (int t = 0; t < Tb; t++, gb += stride_t) {
@@ -280,7 +304,25 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
                 int ox, oy, oz;
                 comp_offsets3(c, ox, oy, oz);
                 const double *gb = greg;
-                if (CG_IS_IP(MODE)) {
+                if (MODE == CG_MODE_IPIP1) {
+                    /* components 3a + b; xx, yy, zz, xy, xz, yz here, the mirrors at task end */
+                    const int nf = L.nf;
+                    double a0 = acc[c], a1 = acc[4 * nf + c], a2 = acc[8 * nf + c];
+                    double a3 = acc[nf + c], a4 = acc[2 * nf + c], a5 = acc[5 * nf + c];
+                    for (int t = 0; t < Tb; t++, gb += stride_t) {
+                        const double gx = gb[ox], gy = gb[A + oy], gz = gb[2 * A + oz];
+                        const double fx = gb[G + ox], fy = gb[A + G + oy], fz = gb[2 * A + G + oz];
+                        const double hx = gb[2 * G + ox], hy = gb[A + 2 * G + oy], hz = gb[2 * A + 2 * G + oz];
+                        a0 = fma(hx, gy * gz, a0);
+                        a1 = fma(hy, gx * gz, a1);
+                        a2 = fma(hz, gx * gy, a2);
+                        a3 = fma(fx * fy, gz, a3);
+                        a4 = fma(fx * fz, gy, a4);
+                        a5 = fma(fy * fz, gx, a5);
+                    }
+                    acc[c] = a0; acc[4 * nf + c] = a1; acc[8 * nf + c] = a2;
+                    acc[nf + c] = a3; acc[2 * nf + c] = a4; acc[5 * nf + c] = a5;
+                } else if (CG_IS_IP(MODE)) {
                     double sx = acc[c], sy = acc[L.nf + c], sz = acc[2 * L.nf + c];
                     for (int t = 0; t < Tb; t++, gb += stride_t) {
                         double gx = gb[ox], gy = gb[A + oy], gz = gb[2 * A + oz];
@@ -305,9 +347,22 @@ __device__ __forceinline__ void run_task(const CGLaunch &P, const CGTask &tk, co
         for (int s = 0; s < (NS > 0 ? NS : 1); s++) {
             int c = lane + 32 * s;
             if (c < L.nf) {
+                if (MODE == CG_MODE_IPIP1) {
+                    /* component 3a + b of the symmetric second nabla */
+                    const int from[9] = {0, 3, 4, 3, 1, 5, 4, 5, 2};
 #pragma unroll
-                for (int q = 0; q < (CG_IS_IP(MODE) ? 3 : 1); q++) acc[q * L.nf + c] = ra[s][q];
+                    for (int q = 0; q < 9; q++) acc[q * L.nf + c] = ra[s][from[q] < NACC ? from[q] : 0];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < NACC; q++) acc[q * L.nf + c] = ra[s][q];
+                }
             }
+        }
+    } else if (MODE == CG_MODE_IPIP1) {
+        for (int c = lane; c < L.nf; c += 32) {
+            acc[3 * L.nf + c] = acc[L.nf + c];
+            acc[6 * L.nf + c] = acc[2 * L.nf + c];
+            acc[7 * L.nf + c] = acc[5 * L.nf + c];
         }
     }
     if (MODE == CG_MODE_ERIP && P.jmode) {
@@ -671,13 +726,15 @@ __device__ __forceinline__ void rys_eri_body(const CGLaunch &P)
 __global__ void __launch_bounds__(128) rys_eri_kernel_e0f0(CGLaunch P) { rys_eri_body<CG_MODE_ERI>(P); }
 __global__ void __launch_bounds__(128, 2) rys_eri_kernel_ip1(CGLaunch P) { rys_eri_body<CG_MODE_IP1>(P); }
 __global__ void __launch_bounds__(128, 2) rys_eri_kernel_ip2(CGLaunch P) { rys_eri_body<CG_MODE_IP2>(P); }
+__global__ void __launch_bounds__(128, 2) rys_eri_kernel_ipip1(CGLaunch P) { rys_eri_body<CG_MODE_IPIP1>(P); }
 __global__ void __launch_bounds__(128, 2) rys_eri_kernel_prim(CGLaunch P) { rys_eri_body<CG_MODE_ERIP>(P); }
 
 static void *eri_kernel_of(int mode)
 {
     return mode == CG_MODE_ERI ? (void *)rys_eri_kernel_e0f0
          : mode == CG_MODE_IP1 ? (void *)rys_eri_kernel_ip1
-         : mode == CG_MODE_IP2 ? (void *)rys_eri_kernel_ip2 : (void *)rys_eri_kernel_prim;
+         : mode == CG_MODE_IP2 ? (void *)rys_eri_kernel_ip2
+         : mode == CG_MODE_IPIP1 ? (void *)rys_eri_kernel_ipip1 : (void *)rys_eri_kernel_prim;
 }
 
 /* ------------------------------------------------------------------ output kernel */
@@ -713,7 +770,7 @@ extern "C" int cg_kernels_init(const int *c2s_nnz, const int *c2s_idx, const dou
     double *d = nullptr;
     if ((e = cudaGetSymbolAddress((void **)&d, g_rys_coef)) != cudaSuccess) return (int)e;
     *rys_coef_dev = d;
-    for (int mode : {CG_MODE_ERI, CG_MODE_IP1, CG_MODE_IP2, CG_MODE_ERIP}) {
+    for (int mode : {CG_MODE_ERI, CG_MODE_IP1, CG_MODE_IP2, CG_MODE_IPIP1, CG_MODE_ERIP}) {
         e = cudaFuncSetAttribute(eri_kernel_of(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 8 * CG_WS_MAX);
         if (e != cudaSuccess) return (int)e;
     }
@@ -745,6 +802,8 @@ extern "C" int cg_launch_eri(const CGLaunch *P, int mode, int nblocks, cudaStrea
         rys_eri_kernel_ip1<<<nblocks, 128, smem, stream>>>(*P);
     else if (mode == CG_MODE_IP2)
         rys_eri_kernel_ip2<<<nblocks, 128, smem, stream>>>(*P);
+    else if (mode == CG_MODE_IPIP1)
+        rys_eri_kernel_ipip1<<<nblocks, 128, smem, stream>>>(*P);
     else
         rys_eri_kernel_prim<<<nblocks, 128, smem, stream>>>(*P);
     return (int)cudaGetLastError();

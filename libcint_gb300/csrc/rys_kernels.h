@@ -25,7 +25,11 @@
 #define CG_WS_SMALL (24 * 1024 / 8)  /* doubles of shared memory per warp, default */
 #define CG_WS_MAX (48 * 1024 / 8)    /* doubles of shared memory per warp, large classes */
 #define CG_C2S_MAXNNZ 16
-#define CG_IS_IP(m) ((m) == CG_MODE_IP1 || (m) == CG_MODE_IP2)
+#define CG_MODE_IPIP1 9              /* two nablas on kernel slot 0 (i): int2e_ipip1 */
+#define CG_IS_IP(m) ((m) == CG_MODE_IP1 || (m) == CG_MODE_IP2 || (m) == CG_MODE_IPIP1)
+/* output components and g arrays per axis (g, its nabla, the second nabla) of a mode */
+#define CG_NCOMP(m) ((m) == CG_MODE_IPIP1 ? 9 : (CG_IS_IP(m) ? 3 : 1))
+#define CG_NG(m) ((m) == CG_MODE_IPIP1 ? 3 : (CG_IS_IP(m) ? 2 : 1))
 
 typedef struct {
     int lic, nroots, nmax, mmax;

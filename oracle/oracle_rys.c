@@ -462,13 +462,40 @@ static void gout(const OEnv *E, const GArr *G, double ai, double *out, int ncomp
         const double *px = G->g + GIDX(G, 0, 0, ix, nx[1][j], nx[2][k], nx[3][l]);
         const double *py = G->g + GIDX(G, 1, 0, iy, ny[1][j], ny[2][k], ny[3][l]);
         const double *pz = G->g + GIDX(G, 2, 0, iz, nz[1][j], nz[2][k], nz[3][l]);
-        double s0 = 0, sx = 0, sy = 0, sz = 0;
+        double s0 = 0, sx = 0, sy = 0, sz = 0, h[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         for (int r = 0; r < n; r++) {
             double gx = px[r * rs];
             double gy = py[r * rs];
             double gz = pz[r * rs];
             if (ncomp == 1) {
                 s0 += gx * gy * gz;
+            } else if (ncomp == 9) {
+                /* two nablas on i (libcint int2e_ipip1, src/autocode/hess.c:1124-1170):
+                 * D g(i) = i g(i-1) - 2a g(i+1), D D g(i) = i(i-1) g(i-2) - 2a(2i+1) g(i)
+                 * + 4a^2 g(i+2); component 3p + q = D_p D_q (one D per axis, D D on one) */
+                const int ii[3] = {ix, iy, iz};
+                const int jj[3] = {nx[1][j], ny[1][j], nz[1][j]};
+                const int kk[3] = {nx[2][k], ny[2][k], nz[2][k]};
+                const int ll[3] = {nx[3][l], ny[3][l], nz[3][l]};
+                double g0[3], g1[3], g2[3];
+                for (int c = 0; c < 3; c++) {
+                    const int a = ii[c];
+                    double v = G->g[GIDX(G, c, r, a, jj[c], kk[c], ll[c])];
+                    double vp = G->g[GIDX(G, c, r, a + 1, jj[c], kk[c], ll[c])];
+                    double vpp = G->g[GIDX(G, c, r, a + 2, jj[c], kk[c], ll[c])];
+                    double vm = a >= 1 ? G->g[GIDX(G, c, r, a - 1, jj[c], kk[c], ll[c])] : 0;
+                    double vmm = a >= 2 ? G->g[GIDX(G, c, r, a - 2, jj[c], kk[c], ll[c])] : 0;
+                    g0[c] = v;
+                    g1[c] = a * vm - 2 * ai * vp;
+                    g2[c] = a * (a - 1) * vmm - 2 * ai * (2 * a + 1) * v + 4 * ai * ai * vpp;
+                }
+                for (int p = 0; p < 3; p++)
+                    for (int q = 0; q < 3; q++) {
+                        double t = 1;
+                        for (int c = 0; c < 3; c++)
+                            t *= (c == p && c == q) ? g2[c] : ((c == p || c == q) ? g1[c] : g0[c]);
+                        h[3 * p + q] += t;
+                    }
             } else if (E->dslot == 0) {
                 /* f(i) = i g(i-1) - 2 a_i g(i+1)   (CINTnabla1i_2e, src/g2e.c:4550-4591) */
                 double fx = -2 * ai * G->g[GIDX(G, 0, r, ix + 1, nx[1][j], nx[2][k], nx[3][l])];
@@ -495,6 +522,7 @@ static void gout(const OEnv *E, const GArr *G, double ai, double *out, int ncomp
             }
         }
         if (ncomp == 1) out[idx] = s0;
+        else if (ncomp == 9) for (int c = 0; c < 9; c++) out[idx * 9 + c] = h[c];
         else { out[idx * 3 + 0] = sx; out[idx * 3 + 1] = sy; out[idx * 3 + 2] = sz; }
     }
 }
@@ -700,7 +728,7 @@ static int driver(double *out, int *dims, int *shls, int *atm, int *bas, double 
     OEnv E;
     init_env(&E, shls, atm, bas, env, three, dinc, dslot);
 
-    int ncomp = dinc ? 3 : 1;
+    int ncomp = dinc == 2 ? 9 : (dinc ? 3 : 1);
     int nf = ncart(E.l[0]) * ncart(E.l[1]) * ncart(E.l[2]) * ncart(E.l[3]);
     int nc = E.nctr[0] * E.nctr[1] * E.nctr[2] * E.nctr[3];
     if (out == NULL) {
@@ -758,6 +786,13 @@ int oracle_int3c2e_ip2_cart(double *out, int *dims, int *shls, int *atm, int nat
                             int *bas, int nbas, double *env, void *opt, double *cache)
 { (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 1, 1, 0, 2); }
 
+int oracle_int2e_ipip1_sph(double *out, int *dims, int *shls, int *atm, int natm,
+                           int *bas, int nbas, double *env, void *opt, double *cache)
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 2, 1, 0); }
+int oracle_int2e_ipip1_cart(double *out, int *dims, int *shls, int *atm, int natm,
+                            int *bas, int nbas, double *env, void *opt, double *cache)
+{ (void)natm; (void)nbas; (void)opt; (void)cache; return driver(out, dims, shls, atm, bas, env, 0, 2, 0, 0); }
+
 double oracle_int2e_sph_list(const int *quartets, long nq, double *out, const long *offsets,
                              int *atm, int natm, int *bas, int nbas, double *env, int nthreads)
 {
@@ -794,21 +829,23 @@ double oracle_int2e_sph_list(const int *quartets, long nq, double *out, const lo
 }
 
 /* Evaluate n items of one kind (which: 0 int2e_sph, 1 int2e_cart, 2 int2e_ip1_sph, 3 int2e_ip1_cart,
- * 4 int3c2e_sph, 5 int3c2e_cart, 6 int2c2e_sph, 7 int2c2e_cart; 4, 3 or 2 shell indices per item)
+ * 4 int3c2e_sph, 5 int3c2e_cart, 6 int2c2e_sph, 7 int2c2e_cart, 8-9 int2e_ip2, 10-11 int3c2e_ip1,
+ * 12-13 int3c2e_ip2, 14-15 int2e_ipip1 (sph, cart); 4, 3 or 2 shell indices per item)
  * with OpenMP over items; item q writes its dense block (all components) at out + offsets[q].
  * Returns wall seconds, or -1 for an unknown kind. */
 double oracle_list(int which, const int *items, long n, double *out, const long *offsets,
                    int *atm, int natm, int *bas, int nbas, double *env, int nthreads)
 {
     typedef int (*fn_t)(double *, int *, int *, int *, int, int *, int, double *, void *, double *);
-    static const fn_t fns[14] = {oracle_int2e_sph, oracle_int2e_cart, oracle_int2e_ip1_sph,
+    static const fn_t fns[16] = {oracle_int2e_sph, oracle_int2e_cart, oracle_int2e_ip1_sph,
                                  oracle_int2e_ip1_cart, oracle_int3c2e_sph, oracle_int3c2e_cart,
                                  oracle_int2c2e_sph, oracle_int2c2e_cart, oracle_int2e_ip2_sph,
                                  oracle_int2e_ip2_cart, oracle_int3c2e_ip1_sph,
                                  oracle_int3c2e_ip1_cart, oracle_int3c2e_ip2_sph,
-                                 oracle_int3c2e_ip2_cart};
-    static const int nshs[14] = {4, 4, 4, 4, 3, 3, 2, 2, 4, 4, 3, 3, 3, 3};
-    if (which < 0 || which > 13) return -1;
+                                 oracle_int3c2e_ip2_cart, oracle_int2e_ipip1_sph,
+                                 oracle_int2e_ipip1_cart};
+    static const int nshs[16] = {4, 4, 4, 4, 3, 3, 2, 2, 4, 4, 3, 3, 3, 3, 4, 4};
+    if (which < 0 || which > 15) return -1;
     const int nsh = nshs[which];
     double t0 = 0, t1 = 0;
 #ifdef _OPENMP

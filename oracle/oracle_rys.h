@@ -53,6 +53,11 @@ int oracle_int3c2e_ip2_sph(double *out, int *dims, int *shls, int *atm, int natm
                            int *bas, int nbas, double *env, void *opt, double *cache);
 int oracle_int3c2e_ip2_cart(double *out, int *dims, int *shls, int *atm, int natm,
                             int *bas, int nbas, double *env, void *opt, double *cache);
+/* (nabla nabla i j|kl), 9 components 3p + q (libcint src/autocode/hess.c:1124-1194) */
+int oracle_int2e_ipip1_sph(double *out, int *dims, int *shls, int *atm, int natm,
+                           int *bas, int nbas, double *env, void *opt, double *cache);
+int oracle_int2e_ipip1_cart(double *out, int *dims, int *shls, int *atm, int natm,
+                            int *bas, int nbas, double *env, void *opt, double *cache);
 int oracle_int2c2e_sph(double *out, int *dims, int *shls, int *atm, int natm,
                        int *bas, int nbas, double *env, void *opt, double *cache);
 int oracle_int2c2e_cart(double *out, int *dims, int *shls, int *atm, int natm,
@@ -73,7 +78,7 @@ double oracle_int2e_sph_list(const int *quartets, long nq, double *out, const lo
 /* Any kind over a list of items (which: 0 int2e_sph, 1 int2e_cart, 2 int2e_ip1_sph,
  * 3 int2e_ip1_cart, 4 int3c2e_sph, 5 int3c2e_cart, 6 int2c2e_sph, 7 int2c2e_cart, 8 int2e_ip2_sph,
  * 9 int2e_ip2_cart, 10 int3c2e_ip1_sph, 11 int3c2e_ip1_cart, 12 int3c2e_ip2_sph,
- * 13 int3c2e_ip2_cart), OpenMP over
+ * 13 int3c2e_ip2_cart, 14 int2e_ipip1_sph, 15 int2e_ipip1_cart), OpenMP over
  * items, dense blocks (all components) at out + offsets[q].  Returns wall seconds. */
 double oracle_list(int which, const int *items, long n, double *out, const long *offsets,
                    int *atm, int natm, int *bas, int nbas, double *env, int nthreads);

@@ -17,7 +17,8 @@ REF_SO = os.path.join(ODIR, '_ref', 'libcint.so')
 
 _SIG = ('int2e_sph', 'int2e_cart', 'int2e_ip1_sph', 'int2e_ip1_cart', 'int3c2e_sph', 'int3c2e_cart',
         'int2c2e_sph', 'int2c2e_cart', 'int2e_ip2_sph', 'int2e_ip2_cart', 'int3c2e_ip1_sph',
-        'int3c2e_ip1_cart', 'int3c2e_ip2_sph', 'int3c2e_ip2_cart')
+        'int3c2e_ip1_cart', 'int3c2e_ip2_sph', 'int3c2e_ip2_cart', 'int2e_ipip1_sph',
+        'int2e_ipip1_cart')
 
 
 class _Lib:
@@ -35,7 +36,7 @@ class _Lib:
         nsh = 3 if 'int3c2e' in name else (2 if 'int2c2e' in name else 4)
         shls = np.ascontiguousarray(shls, dtype=np.int32)
         sph = name.endswith('_sph')
-        ncomp = 3 if ('_ip1' in name or '_ip2' in name) else 1
+        ncomp = 9 if '_ipip1' in name else (3 if ('_ip1' in name or '_ip2' in name) else 1)
         cnt = [(mol.nsph(s) if sph else mol.ncart(s)) for s in shls[:nsh]]
         n = int(np.prod(cnt)) * ncomp
         out = np.zeros(n if dims is None else int(np.prod(dims)) * ncomp)
@@ -73,7 +74,7 @@ class Oracles:
         nsh = 3 if 'int3c2e' in name else (2 if 'int2c2e' in name else 4)
         items = np.ascontiguousarray(items, dtype=np.int32).reshape(-1, nsh)
         sph = name.endswith('_sph')
-        ncomp = 3 if ('_ip1' in name or '_ip2' in name) else 1
+        ncomp = 9 if '_ipip1' in name else (3 if ('_ip1' in name or '_ip2' in name) else 1)
         l = mol.bas[:, 1].astype(np.int64)
         nctr = mol.bas[:, 3].astype(np.int64)
         per = ((2 * l + 1) if sph else (l + 1) * (l + 2) // 2) * nctr
@@ -101,7 +102,7 @@ class Oracles:
         nsh = 3 if 'int3c2e' in name else (2 if 'int2c2e' in name else 4)
         items = np.ascontiguousarray(items, dtype=np.int32).reshape(-1, nsh)
         sph = name.endswith('_sph')
-        ncomp = 3 if ('_ip1' in name or '_ip2' in name) else 1
+        ncomp = 9 if '_ipip1' in name else (3 if ('_ip1' in name or '_ip2' in name) else 1)
         l = mol.bas[:, 1].astype(np.int64)
         nctr = mol.bas[:, 3].astype(np.int64)
         per = ((2 * l + 1) if sph else (l + 1) * (l + 2) // 2) * nctr

@@ -24,6 +24,7 @@ Contents (all through libcint 6.1.1 built by oracle/Makefile, opt = NULL, cache 
                                      the restatement
   c3_int2e_sph / c3_int2e_ip1_sph    40 unique quartets of molecules.config3(seed=0)
   c0_int2e_ip2_sph / _cart           40 of the c0 quartets above, (ij|nabla k l)
+  c0_int2e_ipip1_sph / _cart         the same 40, (nabla nabla i j|k l), 9 components
   c2_int3c2e_ip1_sph / _cart, c2_int3c2e_ip2_sph / _cart    the 60 c2 triples above
   lr_c0_int2e_sph / lr_c0_int2e_ip1_sph / lr_c2_int3c2e_sph / lr_c2_int2c2e_sph
                                      long-range Coulomb erf(omega r)/r (env[PTR_RANGE_OMEGA] =
@@ -158,7 +159,7 @@ def main():
         out['c3_' + name + '_items'] = q3
         out['c3_' + name] = np.concatenate([o.ref.call(name, mol3, q)[1].ravel(order='F') for q in q3])
     # derivative family: (ij|nabla k l) on c0, (nabla i j|k) and (ij|nabla k) on the c2 molecule
-    for name in ('int2e_ip2_sph', 'int2e_ip2_cart'):
+    for name in ('int2e_ip2_sph', 'int2e_ip2_cart', 'int2e_ipip1_sph', 'int2e_ipip1_cart'):
         out['c0_' + name + '_items'] = qs[:40]
         out['c0_' + name] = np.concatenate([o.ref.call(name, mol0, q)[1].ravel(order='F') for q in qs[:40]])
     for name in ('int3c2e_ip1_sph', 'int3c2e_ip1_cart', 'int3c2e_ip2_sph', 'int3c2e_ip2_cart'):
@@ -196,6 +197,7 @@ def main():
     # itself against on ill-conditioned geometries
     for key, m in (('c4_int2e_sph', mol4), ('c4_int2e_cart', mol4), ('c4_int2e_ip1_sph', mol4),
                    ('c0_int2e_ip2_sph', mol0), ('c0_int2e_ip2_cart', mol0),
+                   ('c0_int2e_ipip1_sph', mol0), ('c0_int2e_ipip1_cart', mol0),
                    ('c2_int3c2e_ip1_sph', mol2), ('c2_int3c2e_ip1_cart', mol2),
                    ('c2_int3c2e_ip2_sph', mol2), ('c2_int3c2e_ip2_cart', mol2)):
         name = key.split('_', 1)[1]

@@ -36,7 +36,8 @@ def gpu_blocks(gpulib, name, mol, qs):
             'int3c2e_sph': gpulib.INT3C2E_SPH, 'int3c2e_cart': gpulib.INT3C2E_CART,
             'int2e_ip2_sph': gpulib.INT2E_IP2_SPH, 'int2e_ip2_cart': gpulib.INT2E_IP2_CART,
             'int3c2e_ip1_sph': gpulib.INT3C2E_IP1_SPH, 'int3c2e_ip1_cart': gpulib.INT3C2E_IP1_CART,
-            'int3c2e_ip2_sph': gpulib.INT3C2E_IP2_SPH, 'int3c2e_ip2_cart': gpulib.INT3C2E_IP2_CART}[name]
+            'int3c2e_ip2_sph': gpulib.INT3C2E_IP2_SPH, 'int3c2e_ip2_cart': gpulib.INT3C2E_IP2_CART,
+            'int2e_ipip1_sph': gpulib.INT2E_IPIP1_SPH, 'int2e_ipip1_cart': gpulib.INT2E_IPIP1_CART}[name]
     plan = gpulib.Plan(kind, mol, qs)
     out = torch.zeros(plan.output_size * plan.ncomp, dtype=torch.float64, device='cuda')
     plan.execute(out)

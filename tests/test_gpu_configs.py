@@ -31,7 +31,7 @@ def item_major(gpu, mol, items, name):
     """plan output (component-major: comp * output_size + block offset) -> per item, all
     components (libcint's per-call layout)"""
     sph = name.endswith('_sph')
-    ncomp = 3 if ('_ip1' in name or '_ip2' in name) else 1
+    ncomp = 9 if '_ipip1' in name else (3 if ('_ip1' in name or '_ip2' in name) else 1)
     nsh = 3 if 'int3c2e' in name else 4
     per = np.array([mol.nsph(s) if sph else mol.ncart(s) for s in range(mol.nbas)], dtype=np.int64)
     size = np.prod(per[np.asarray(items)[:, :nsh]], axis=1)

@@ -1,5 +1,5 @@
-"""The derivative family on the GPU: (ij|nabla k l) (int2e_ip2), (nabla i j|k) (int3c2e_ip1) and
-(ij|nabla k) (int3c2e_ip2), sph and cart, through batched plans and the drop-in, against libcint's
+"""The derivative family on the GPU: (ij|nabla k l) (int2e_ip2), (nabla i j|k) (int3c2e_ip1),
+(ij|nabla k) (int3c2e_ip2) and (nabla nabla i j|k l) (int2e_ipip1), sph and cart, through batched plans and the drop-in, against libcint's
 own blocks (tests/golden/ref_blocks.npz), the restatement and its long-double referee; plus the
 translational-invariance identity of the 3c2e derivatives:
 (nabla_i j|k) + (i nabla_j|k) + (ij|nabla_k) = 0, with (i nabla_j|k) from int3c2e_ip1 of (j, i, k)."""
@@ -25,7 +25,8 @@ def _mol(key):
 
 
 @pytest.mark.parametrize('key', ['c0_int2e_ip2_sph', 'c0_int2e_ip2_cart', 'c2_int3c2e_ip1_sph',
-                                 'c2_int3c2e_ip1_cart', 'c2_int3c2e_ip2_sph', 'c2_int3c2e_ip2_cart'])
+                                 'c2_int3c2e_ip1_cart', 'c2_int3c2e_ip2_sph', 'c2_int3c2e_ip2_cart',
+                                 'c0_int2e_ipip1_sph', 'c0_int2e_ipip1_cart'])
 def test_derivatives_match_libcint(gpulib, oracle, key):
     fx = np.load(os.path.join(GOLD, 'ref_blocks.npz'))
     items, ref = fx[key + '_items'], fx[key]
@@ -57,6 +58,20 @@ def test_int2e_ip2_c3_sample(gpulib, oracle):
     gpu = item_major(gpu_blocks(gpulib, 'int2e_ip2_sph', mol, qs), mol, qs, 'int2e_ip2_sph')
     ref, _ = oracle.blocks('int2e_ip2_sph', mol, qs)
     assert np.abs(gpu - ref).max() <= ABS_TOL
+
+
+def test_int2e_ipip1_c3_sample(gpulib, oracle):
+    """500 c3 quartets through one batched int2e_ipip1_sph plan (9 components), and the symmetry
+    of the second nabla (component xy = yx, xz = zx, yz = zy)."""
+    mol = M.config3(seed=0)
+    qs = M.unique_quartets(mol.nbas)
+    qs = qs[np.random.RandomState(6).choice(len(qs), 500, replace=False)]
+    raw = gpu_blocks(gpulib, 'int2e_ipip1_sph', mol, qs)
+    gpu = item_major(raw, mol, qs, 'int2e_ipip1_sph')
+    ref, _ = oracle.blocks('int2e_ipip1_sph', mol, qs)
+    assert np.abs(gpu - ref).max() <= ABS_TOL * max(1.0, np.abs(ref).max())
+    c = raw.reshape(9, -1)
+    assert np.array_equal(c[1], c[3]) and np.array_equal(c[2], c[6]) and np.array_equal(c[5], c[7])
 
 
 def test_int3c2e_translational_invariance(gpulib):

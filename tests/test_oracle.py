@@ -110,7 +110,8 @@ def _compare(got, ref, scale, atol=1e-12, rtol=1e-10):
                                          ('kat_int2c2e_sph', 'kat'), ('hl_int2e_sph', 'hl'),
                                          ('hl_int2e_cart', 'hl'), ('hl_int3c2e_sph', 'hl'),
                                          ('hl_int2e_ip1_sph', 'hl'), ('c0_int2e_ip2_sph', 'c0'),
-                                         ('c0_int2e_ip2_cart', 'c0'), ('c2_int3c2e_ip1_sph', 'c2'),
+                                         ('c0_int2e_ip2_cart', 'c0'), ('c0_int2e_ipip1_sph', 'c0'),
+                                         ('c0_int2e_ipip1_cart', 'c0'), ('c2_int3c2e_ip1_sph', 'c2'),
                                          ('c2_int3c2e_ip1_cart', 'c2'), ('c2_int3c2e_ip2_sph', 'c2'),
                                          ('c2_int3c2e_ip2_cart', 'c2')])
 def test_oracle_matches_libcint_blocks(oracle, key, molname):
