@@ -230,6 +230,13 @@ int cintgpu_plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n
 int cintgpu_plan_create_tuned(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
                               const int64_t *offsets, const int *atm, int natm, const int *bas,
                               int nbas, const double *env, int ws_kb, int separate_output);
+/* ... and per class: the nwide classes in `wide` (keys ((li*8 + lj)*8 + lk)*8 + ll in kernel order:
+ * li >= lj, lk >= ll, (li, lj) >= (lk, ll); int3c2e ll = 0) run in the 48 KB-per-warp task group
+ * (more terms per batch, fewer warps per SM) instead of the regular one. */
+int cintgpu_plan_create_classes(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
+                                const int64_t *offsets, const int *atm, int natm, const int *bas,
+                                int nbas, const double *env, int ws_kb, int separate_output,
+                                const int *wide, int nwide);
 /* doubles per component of the output (max offset + block), and the component count */
 int64_t cintgpu_plan_output_size(const CINTGPUPlan *plan);
 int cintgpu_plan_ncomp(const CINTGPUPlan *plan);

@@ -66,6 +66,8 @@ def lib():
     L.cintgpu_plan_create.restype = i32
     L.cintgpu_plan_create_tuned.argtypes = [vp, i32, vp, i64, vp, vp, i32, vp, i32, vp, i32, i32]
     L.cintgpu_plan_create_tuned.restype = i32
+    L.cintgpu_plan_create_classes.argtypes = [vp, i32, vp, i64, vp, vp, i32, vp, i32, vp, i32, i32, vp, i32]
+    L.cintgpu_plan_create_classes.restype = i32
     L.cintgpu_plan_output_size.argtypes = [vp]
     L.cintgpu_plan_output_size.restype = i64
     L.cintgpu_plan_ncomp.argtypes = [vp]
@@ -137,9 +139,10 @@ class Plan:
     device pointer) of ncomp * output_size elements; block q of component c starts at
     c * output_size + offsets[q] and is laid out like libcint's dense output (i fastest).
     ws_kb / separate_output: the launch parameters of cintgpu_plan_create_tuned (0 = defaults);
-    autotune.tuned_plan picks them."""
+    wide_classes: class keys ((li*8 + lj)*8 + lk)*8 + ll, kernel order) run with 48 KB of shared
+    memory per warp (cintgpu_plan_create_classes); autotune.tuned_plan picks all three."""
 
-    def __init__(self, kind, mol, shls, offsets=None, ws_kb=0, separate_output=0):
+    def __init__(self, kind, mol, shls, offsets=None, ws_kb=0, separate_output=0, wide_classes=()):
         L = lib()
         self.kind = kind
         self.mol = mol
@@ -149,12 +152,17 @@ class Plan:
         h = ctypes.c_void_p()
         args = (ctypes.byref(h), kind, _ptr(shls), self.n, _ptr(off), _ptr(mol.atm), mol.natm,
                 _ptr(mol.bas), mol.nbas, _ptr(mol.env))
-        if ws_kb or separate_output:
+        wide = np.ascontiguousarray(sorted(set(int(k) for k in wide_classes)), dtype=np.int32)
+        if len(wide):
+            rc = L.cintgpu_plan_create_classes(*args, int(ws_kb), int(separate_output), _ptr(wide),
+                                               len(wide))
+        elif ws_kb or separate_output:
             rc = L.cintgpu_plan_create_tuned(*args, int(ws_kb), int(separate_output))
         else:
             rc = L.cintgpu_plan_create(*args)
         _check(rc, 'cintgpu_plan_create')
         self.ws_kb, self.separate_output = int(ws_kb), int(separate_output)
+        self.wide_classes = tuple(int(k) for k in wide)
         self._h = h
         self.output_size = L.cintgpu_plan_output_size(h)
         self.ncomp = L.cintgpu_plan_ncomp(h)

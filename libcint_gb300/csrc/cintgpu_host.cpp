@@ -329,6 +329,7 @@ struct CINTGPUPlan {
     bool fuse_out = true;          /* the integral kernel stores finished quartets itself */
     int plan_threads = 1;          /* host threads for the planner's screening (plans created by
                                       cintgpu_plan_create*; chunk plans are built in parallel) */
+    std::vector<int> wide;         /* class keys forced into the 48 KB group (per-class tuning) */
     int ws_kb = 0;                 /* shared memory per warp of the regular group in KB (0: the
                                       CINTGPU_WS_KB override or the default 24) */
     int prim_l = 4;                /* int2e classes with ll >= prim_l (or lj >= prim_l when the
@@ -1362,7 +1363,9 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             if (per_primitive(P, pe.l)) {
                 cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], CG_MODE_ERIP, CG_WS_MAX, &Lc);
                 cls_group[ck] = 2;
-            } else if (Lc.T < 2) {
+            } else if (Lc.T < 2 || std::find(P->wide.begin(), P->wide.end(),
+                                             ((pe.l[0] * 8 + pe.l[1]) * 8 + pe.l[2]) * 8 + pe.l[3])
+                                       != P->wide.end()) {
                 cg_layout(pe.l[0], pe.l[1], pe.l[2], pe.l[3], lmode, CG_WS_MAX, &Lc);
                 cls_group[ck] = 1;
             }
@@ -1982,13 +1985,15 @@ int cintgpu_rys_roots_dev(int nroots, const double *xs_dev, int count, double *s
 
 static int plan_create(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
                        const int64_t *offsets, const int *atm, int natm, const int *bas,
-                       int nbas, const double *env, int ws_kb, int separate_output)
+                       int nbas, const double *env, int ws_kb, int separate_output,
+                       const int *wide = nullptr, int nwide = 0)
 {
     *plan = nullptr;
     int rc = ensure_init();
     if (rc) return rc;
     CINTGPUPlan *P = new CINTGPUPlan();
     P->ws_kb = ws_kb;
+    if (wide && nwide > 0) P->wide.assign(wide, wide + nwide);
     P->plan_threads = (int)std::thread::hardware_concurrency();
     /* CINTGPU_SEPARATE_OUTPUT=1: transform outputs in their own kernel (tuning) */
     if (const char *e = getenv("CINTGPU_SEPARATE_OUTPUT")) P->fuse_out = atoi(e) == 0;
@@ -2030,6 +2035,33 @@ int cintgpu_plan_create_tuned(CINTGPUPlan **plan, int kind, const int *shls, int
     }
     return plan_create(plan, kind, shls, n, offsets, atm, natm, bas, nbas, env, ws_kb,
                        separate_output);
+}
+
+int cintgpu_plan_create_classes(CINTGPUPlan **plan, int kind, const int *shls, int64_t n,
+                                const int64_t *offsets, const int *atm, int natm, const int *bas,
+                                int nbas, const double *env, int ws_kb, int separate_output,
+                                const int *wide, int nwide)
+{
+    if (plan) *plan = nullptr;
+    if (ws_kb != 0 && (ws_kb < 8 || ws_kb > 48)) {
+        set_error("ws_kb %d outside 8..48 (0 = default)", ws_kb);
+        return CINTGPU_ERR_ARG;
+    }
+    if (separate_output != 0 && separate_output != 1) {
+        set_error("separate_output must be 0 or 1");
+        return CINTGPU_ERR_ARG;
+    }
+    if (nwide < 0 || (nwide > 0 && !wide)) {
+        set_error("wide: %d class keys without an array", nwide);
+        return CINTGPU_ERR_ARG;
+    }
+    for (int i = 0; i < nwide; i++)
+        if (wide[i] < 0 || wide[i] >= 8 * 8 * 8 * 8) {
+            set_error("class key %d outside 0..4095", wide[i]);
+            return CINTGPU_ERR_ARG;
+        }
+    return plan_create(plan, kind, shls, n, offsets, atm, natm, bas, nbas, env, ws_kb,
+                       separate_output, wide, nwide);
 }
 
 int64_t cintgpu_plan_output_size(const CINTGPUPlan *plan) { return plan->out_size; }
@@ -2886,6 +2918,19 @@ extern "C" int cg_plan_groups(int kind, const int *shls, int64_t n, const int *a
     for (int g = 0; g < 3; g++) info[g] = P.groups[g].ntasks;
     info[3] = fused(&P) ? 1 : 0;
     info[4] = P.mode == CG_MODE_ERI ? bra_tasks(P) : 0;
+    return 0;
+}
+
+/* the groups with classes forced into the 48 KB group (per-class tuning) */
+extern "C" int cg_plan_groups_wide(int kind, const int *shls, int64_t n, const int *atm, int natm,
+                                   const int *bas, int nbas, const double *env, const int *wide,
+                                   int nwide, int64_t *info)
+{
+    CINTGPUPlan P;
+    if (nwide > 0) P.wide.assign(wide, wide + nwide);
+    int rc = build_plan(&P, kind, shls, n, nullptr, atm, natm, bas, nbas, env, 0);
+    if (rc) return rc;
+    for (int g = 0; g < 3; g++) info[g] = P.groups[g].ntasks;
     return 0;
 }
 

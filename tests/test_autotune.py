@@ -86,8 +86,8 @@ def test_choose_uses_the_cache_before_tuning(tmp_path):
         calls.append(kind)
         return (16, 1), {(16, 1): 1.0}
     dev = 'GB300 test|cuda 13.0'
-    assert at.choose(cg.INT2E_SPH, mol, qs, p, device=dev, tuner=tuner) == (16, 1)
-    assert at.choose(cg.INT2E_SPH, mol, qs, p, device=dev, tuner=tuner) == (16, 1)
+    assert at.choose(cg.INT2E_SPH, mol, qs, p, device=dev, tuner=tuner) == (16, 1, ())
+    assert at.choose(cg.INT2E_SPH, mol, qs, p, device=dev, tuner=tuner) == (16, 1, ())
     assert len(calls) == 1                                                  # second call: hit
     at.choose(cg.INT2E_SPH, mol, qs, p, device='other GPU|cuda 13.0', tuner=tuner)
     assert len(calls) == 2                                                  # keyed by device
@@ -131,3 +131,77 @@ def test_shared_memory_per_warp_reaches_the_planner():
     hl = high_l_basis()
     big = [(0, 0, 0, 0), (1, 1, 1, 1), (2, 2, 2, 2)]
     assert plan_info(hl, big, 24)[1] == 0 and plan_info(hl, big, 8)[1] > 0
+
+
+def test_tune_classes_marks_the_classes_the_wide_group_speeds_up():
+    """Per-class tuning with stand-in timings: a class goes to the 48 KB group when its own items
+    are faster there, and the set is dropped if the whole list is not faster with it; the choice
+    is cached with the launch parameters."""
+    mol, qs = _c0()
+    keys, w = at.kernel_classes(mol, qs)
+    uk = np.unique(keys)
+    assert len(uk) > 3 and w.min() > 0
+    fast = int(uk[np.argmax([w[keys == k].sum() for k in uk])])   # the heaviest class
+    made = []
+
+    class P:
+        def __init__(self, lst, wide):
+            self.n, self.wide = len(lst), tuple(wide)
+            made.append(self)
+
+        def close(self):
+            pass
+
+    def timer(p):
+        # the heaviest class runs 20 % faster in the wide group, every other class 10 % slower
+        base = float(p.n)
+        return base * (0.8 if fast in p.wide else (1.1 if p.wide else 1.0))
+    wide, times = at.tune_classes(cg.INT2E_SPH, mol, qs, make_plan=P, timer=timer)
+    assert wide == (fast,) and times[fast][1] < times[fast][0]
+    assert all(t1 > t0 for k, (t0, t1) in times.items() if k != fast)
+    # the whole list slower with the set: dropped
+    wide, _ = at.tune_classes(cg.INT2E_SPH, mol, qs, make_plan=P,
+                              timer=lambda p: float(p.n) * (0.8 if p.n < len(qs) and fast in p.wide
+                                                           else (1.1 if p.wide else 1.0)))
+    assert wide == ()
+    dev = 'GB300 test|cuda 13.0'
+    path = None
+
+    def ct(kind, mol_, items, ws, sep):
+        return (fast,), {fast: (2.0, 1.5)}
+    import tempfile, os
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, 'tuning.json')
+        got = at.choose(cg.INT2E_SPH, mol, qs, path, device=dev,
+                        tuner=lambda k, m, i: ((24, 0), {(24, 0): 1.0}), class_tuner=ct)
+        assert got == (24, 0, (fast,))
+        entry = list(at.load_cache(path).values())[0]
+        assert entry['wide'] == [fast] and entry['class_ms'][str(fast)] == [2.0, 1.5]
+
+
+def test_wide_classes_move_to_the_48kb_group():
+    """cintgpu_plan_create_classes's class list reaches the planner: the named class's tasks move
+    from the regular group to the 48 KB one; a bad key is rejected."""
+    mol, qs = _c0()
+    keys, _ = at.kernel_classes(mol, qs)
+    f = cg.lib().cg_plan_groups_wide
+    f.restype = ctypes.c_int
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    items = np.ascontiguousarray(qs[:400], dtype=np.int32)
+    k = int(keys[0])
+    n_k = int((keys[:400] == k).sum())
+
+    def info(wide):
+        wa = np.ascontiguousarray(wide, dtype=np.int32)
+        out = np.zeros(3, np.int64)
+        assert f(cg.INT2E_SPH, P(items), ctypes.c_int64(len(items)), P(mol.atm), mol.natm,
+                 P(mol.bas), mol.nbas, P(mol.env), P(wa), len(wa), P(out)) == 0, cg.last_error()
+        return out
+    a, b = info([]), info([k])
+    assert a[1] == 0 and b[1] > 0 and a[0] + a[1] == b[0] + b[1] and n_k > 0
+    h = ctypes.c_void_p()
+    bad = np.array([5000], dtype=np.int32)
+    rc = cg.lib().cintgpu_plan_create_classes(ctypes.byref(h), cg.INT2E_SPH, P(items), 4, None,
+                                              P(mol.atm), mol.natm, P(mol.bas), mol.nbas,
+                                              P(mol.env), 0, 0, P(bad), 1)
+    assert rc == -1 and 'class key' in cg.last_error() and not h.value
