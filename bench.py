@@ -74,7 +74,9 @@ def write_bench_input(path, mol, qs):
 def cpu_port_rate(mol, qs, threads, target_s=12.0):
     """Time the C restatement (oracle port) with OpenMP over a bounded prefix of qs."""
     subprocess.run(['make', '-s', '-C', os.path.join(ROOT, 'oracle'), 'oracle'], check=True)
-    exe = os.path.join(ROOT, 'oracle', '_build', 'oracle_bench')
+    # the restatement built with the GPU kernels' root tables (the tests' oracle keeps its own
+    # Stieltjes root finder): the faster of the two CPU implementations
+    exe = os.path.join(ROOT, 'oracle', '_build', 'oracle_bench_fast')
     with tempfile.TemporaryDirectory() as td:
         path = os.path.join(td, 'in.bin')
         n = min(len(qs), 2000)
@@ -148,11 +150,13 @@ def run_reference(args, rank, world):
         'config': {'workload': 'c1: 120 atoms, 14 A cube, 3s3p2d1f, 1-8 prims, Schwarz 1e-12',
                    'quartets_per_step': res['quartets']},
         'cpu_baseline': {'value': v, 'unit': 'integrals/s', 'cores': res['threads'], 'kind': 'port',
-                         'sample': '%d Schwarz-surviving c1 quartets, OpenMP dynamic' % res['quartets']},
+                         'sample': '%d Schwarz-surviving c1 quartets, OpenMP dynamic, table roots'
+                                   % res['quartets']},
         'e2e': {'value': v, 'unit': 'integrals/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
         'note': 'libcint itself is not buildable on the GPU host (its sources are not shipped); '
-                'the timed CPU implementation is the C restatement in oracle/ (same checksum as '
-                'libcint on a shared sample).',
+                'the timed CPU implementation is the C restatement in oracle/ with table roots '
+                '(same checksum as libcint on a shared sample; about 7x slower than libcint on '
+                'the same cores in the build container).',
     }
     print(json.dumps(line), flush=True)
 

@@ -179,10 +179,45 @@ int oracle_rys_roots_range(int nroots, double x, double lower, double *u, double
     return 0;
 }
 
+#ifdef ORACLE_TABLE_ROOTS
+/* CPU timing build only (oracle_bench_fast, the CPU baseline legs of bench.py): the Coulomb roots
+ * from the piecewise polynomial tables the GPU kernels use (rys_tables.inc: degree-10 pieces of
+ * width 1 in x, Gauss-Hermite asymptotics beyond), instead of the Stieltjes procedure above,
+ * which takes three quarters of the restatement's time.  The test oracle never defines this. */
+#include "rys_tables.inc"
+int oracle_rys_roots(int nroots, double x, double *u, double *w)
+{
+    if (nroots < 1 || nroots > RYS_NMAX) return oracle_rys_roots_range(nroots, x, 0.0, u, w);
+    for (int r = 0; r < nroots; r++) {
+        double s, wt;
+        if (x >= RYS_H * rys_nint_host[nroots]) {
+            const int o = nroots * (nroots - 1) / 2 + r;
+            const double rs = 1.0 / sqrt(x);
+            s = rys_large_r_host[o] * rs * rs;
+            wt = rys_large_w_host[o] * rs;
+        } else {
+            const int k = (int)x;
+            const double y = 2.0 * (x - k) - 1.0;
+            const double *c = rys_coef_host + rys_off_host[nroots] + (size_t)((k * nroots + r) * (RYS_DEG + 1)) * 2;
+            double a = c[2 * RYS_DEG], b = c[2 * RYS_DEG + 1];
+            for (int j = RYS_DEG - 1; j >= 0; j--) {
+                a = a * y + c[2 * j];
+                b = b * y + c[2 * j + 1];
+            }
+            s = a;
+            wt = b;
+        }
+        u[r] = s / (1.0 - s);
+        w[r] = wt;
+    }
+    return 0;
+}
+#else
 int oracle_rys_roots(int nroots, double x, double *u, double *w)
 {
     return oracle_rys_roots_range(nroots, x, 0.0, u, w);
 }
+#endif
 
 /* ------------------------------------------------------------------ cart -> sph */
 static double fact(int n) { double f = 1; for (int i = 2; i <= n; i++) f *= i; return f; }
@@ -374,7 +409,7 @@ static int g0_2e(const OEnv *E, GArr *G, const double *P, const double *Q,
         x *= theta;
         fac1 *= sqrt(theta);
     }
-    if (oracle_rys_roots_range(n, x, lower, u, w)) return -1;
+    if (lower > 0 ? oracle_rys_roots_range(n, x, lower, u, w) : oracle_rys_roots(n, x, u, w)) return -1;
     if (E->omega > 0)
         for (int r = 0; r < n; r++) u[r] = theta * u[r] / (1 + u[r] - theta * u[r]);
     const int nmax = E->lc[0] + E->lc[1];
