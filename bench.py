@@ -268,6 +268,78 @@ def extra_int3c2e(cg, seed=0, npairs=40):
                                'integrals_per_s': nint2 / dt2}}
 
 
+def extra_c2(cg, seed=0, thr=1e-12, chunk=4_000_000):
+    """c2 at full size: the whole Schwarz-screened (ij|P) tensor (Q_ij Q_P >= 1e-12 over every
+    orbital shell pair i >= j and every auxiliary shell), evaluated in streamed chunks of about
+    4M triples (each chunk planned on the host, then run into one reused device buffer; nothing is
+    kept).  Reports the triple and integral counts, the bounds' time, the planning and device
+    times, and integrals/s on the device and overall."""
+    import torch
+    from libcint_gb300 import molecules as M
+    from libcint_gb300.screening import pair_bounds
+    mol, norb = M.config2(seed=seed)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ii, jj = np.tril_indices(norb)
+    pairs = np.stack([ii, jj], 1)
+    qij = pair_bounds(mol, pairs)
+    # (P|P) of the auxiliary shells as (P s0|P s0) with the unit zero-exponent s shell
+    env = list(mol.env)
+    pe = len(env)
+    env += [0.0, 2.0 * np.sqrt(np.pi)]
+    bas = np.vstack([mol.bas, [[0, 0, 1, 1, 0, pe, pe + 1, 0]]]).astype(np.int32)
+    molf = M.Mol(mol.atm, bas, np.array(env), mol.name)
+    aux = np.arange(norb, mol.nbas, dtype=np.int64)
+    fit = np.full_like(aux, bas.shape[0] - 1)
+    qp = pair_bounds(molf, np.stack([aux, fit], 1))
+    torch.cuda.synchronize()
+    t_bounds = time.perf_counter() - t0
+    order = np.argsort(-qp, kind='stable')
+    qps = qp[order]
+    # per pair, the auxiliary shells with Q_ij Q_P >= thr are a prefix of the sorted list
+    with np.errstate(divide='ignore'):
+        need = np.where(qij > 0, thr / np.where(qij > 0, qij, 1.0), np.inf)
+    cnt = np.searchsorted(-qps, -need, side='right')
+    keep = cnt > 0
+    pairs, cnt = pairs[keep], cnt[keep]
+    total = int(cnt.sum())
+    L = mol.bas[:, M.ANG_OF]
+    ns = (2 * L + 1) * mol.bas[:, M.NCTR_OF]
+    nint_total = 0
+    buf, plan_s, dev_s, chunks = None, 0.0, 0.0, 0
+    cum = np.concatenate([[0], np.cumsum(cnt)])
+    a = 0
+    while a < len(pairs):
+        b = int(np.searchsorted(cum, cum[a] + chunk, side='right')) - 1
+        b = max(b, a + 1)
+        c = cnt[a:b]
+        tri = np.empty((int(c.sum()), 3), dtype=np.int32)
+        tri[:, :2] = np.repeat(pairs[a:b], c, axis=0)
+        starts = np.repeat(np.cumsum(c) - c, c)
+        tri[:, 2] = aux[order[np.arange(len(tri)) - starts]]
+        nint_total += int((ns[tri[:, 0]] * ns[tri[:, 1]] * ns[tri[:, 2]]).sum())
+        t1 = time.perf_counter()
+        p = cg.Plan(cg.INT3C2E_SPH, mol, tri)
+        plan_s += time.perf_counter() - t1
+        if buf is None or buf.numel() < p.output_size:
+            buf = torch.empty(int(p.output_size * 1.2), dtype=torch.float64, device='cuda')
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        p.execute(buf)
+        e1.record()
+        e1.synchronize()
+        dev_s += e0.elapsed_time(e1) / 1e3
+        p.close()
+        chunks += 1
+        a = b
+    return {'workload': 'c2: 200 atoms, 18 A; every orbital shell pair x every auxiliary shell '
+                        'with Q_ij Q_P >= 1e-12', 'orbital_pairs_kept': int(len(pairs)),
+            'triples': total, 'integrals': nint_total, 'bounds_s': t_bounds, 'chunks': chunks,
+            'plan_s': plan_s, 'device_s': dev_s, 'integrals_per_s_device': nint_total / dev_s,
+            'integrals_per_s_with_planning': nint_total / (dev_s + plan_s)}
+
+
 def extra_adjoint(cg, seed=0, natm=24):
     """c3: 24 atoms (fewer, in a box of the same density, for profiling), full unique quartet
     list; adjoint gradient vs int2e_ip1 formed and contracted on the same GPU; agreement between
@@ -619,7 +691,8 @@ def run_gpu(args, rank, world):
               'int3c2e': lambda: extra_int3c2e(cg),
               'fp64peak': extra_fp64peak,
               'screened': lambda: extra_screened(cg),
-              'c4': lambda: extra_c4(cg)}[args.only]
+              'c4': lambda: extra_c4(cg),
+              'c2': lambda: extra_c2(cg)}[args.only]
         if rank == 0:
             print(json.dumps({'extra': args.only, **fn()}), flush=True)
         return
@@ -761,7 +834,7 @@ def main():
                     help='default launch parameters instead of the autotuner\'s choice')
     ap.add_argument('--no-extras', action='store_true', help='skip the side workloads (drop-in, int3c2e, adjoint, J/K, screening, DF)')
     ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk', 'df', 'screening',
-                                                          'fp64peak', 'screened', 'c4'],
+                                                          'fp64peak', 'screened', 'c4', 'c2'],
                     help='run one side workload alone and print its line (profiling)')
     ap.add_argument('--c3-atoms', type=int, default=24, help='atoms of the adjoint workload')
     args = ap.parse_args()
