@@ -1165,8 +1165,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         auto amin = [](const ShellView &v) { return *std::min_element(v.ex, v.ex + v.nprim); };
         /* the contraction-first adjoint carries the density through the transfer about the first
          * shell of each pair for whole tasks, so there the tighter shell always comes first,
-         * whatever the l (with the larger l first, a distant tight-diffuse g pair of c4-type
-         * bases loses up to 2e-7 of the gradient; the cost is a longer range of e) */
+         * whatever the l: the product densities sit near it, and the transfer's binomial terms
+         * stay small (the cost is a longer range of e when the tighter shell has the lower l) */
         const bool tight_first = P->gradj && (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA);
         auto first = [&](int a, int b) {   /* shell a goes before shell b */
             if (tight_first) return amin(sv[a]) >= amin(sv[b]);

@@ -103,7 +103,8 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
          * exponents the term's four primitive indices), the VRR arrays g(e, f) for
          * e <= li+lj+d, f <= lk+ll+d (d = 1, 2 with exponents), and the buffers of one side's
          * axis-by-axis contraction (with exponents also the per-lane exponent partials, 64 per
-         * term); per task the transferred densities with their AB derivatives, the per-entry sums
+         * term); per task the transferred densities (bra: also its i-weighted and AB-derivative
+         * transfers; ket: its k-weighted transfer), the per-entry sums
          * over terms (three on the bra, two on the ket) and, with exponents, the exponent weights
          * of the four shells and their per-primitive sums */
         const bool ex = mode == CG_MODE_GRADAJ;
@@ -120,7 +121,7 @@ __host__ __device__ inline void cg_class_layout(int li, int lj, int lk, int ll, 
         const int bufk = cg_np2(Le) * nm + (Le + 1) * cg_np2(L->mmax);
         L->scr = ((bufb > bufk ? bufb : bufk) + (ex ? 64 : 0)) | 1;
         const int tE = cg_ntet(L->nmax), tF = cg_ntet(L->mmax);
-        const int fixed = 4 * cg_ntet(Le) + 4 * cg_ntet(Lf) + 3 * tE + 2 * tF
+        const int fixed = 7 * cg_ntet(Le) + 4 * cg_ntet(Lf) + 3 * tE + 2 * tF
                         + (ex ? 2 * tE + 2 * tF + 4 * CG_GRAD_MAXPRIM : 0);
         T = (ws_doubles - fixed) / (L->termw + L->gstride + L->scr);
         if (T > 32) T = 32;

@@ -244,12 +244,20 @@ rys_grad_kernel(CGGradLaunch P)
  * E = sum_{e,f} De Df (e0|f0) with the transferred densities De = sum_ij D_ij Tb[ij, e] and
  * Df = sum_kl D_kl Tk[kl, f], formed once per task.  Differentiating every factor that moves:
  *
- *   dE/dA_x = sum De Df [2a (e+1x 0|f0) - e_x (e-1x 0|f0)] + sum dDe/dAB_x Df (e0|f0)
- *   dE/dB_x = sum De Df 2b [(e+1x 0|f0) + AB_x (e0|f0)]    - sum dDe/dAB_x Df (e0|f0)
- *   dE/dC_x = sum De Df [2c (e0|f+1x 0) - f_x (e0|f-1x 0)] + sum De dDf/dCD_x (e0|f0)
+ * The nabla of libcint (src/g2e.c:4550-4591) acts on one shell's Gaussian: A moves only phi_i,
+ * (nabla_A i j| = 2a (i+1x j| - i_x (i-1x j|, and the transfer of (i+1x j| is the transfer of
+ * (ij| shifted by 1x, that of i_x (i-1x j| the transfer of the i_x-weighted density shifted back;
+ * B moves only phi_j, 2b (i j+1x| = 2b [(i+1x j| + AB_x (ij|] and j_x (i j-1x| is the transfer
+ * of the AB-derivative of Tb.  So with per-task densities De, iDe_x = sum_ij i_x D_ij Tb[ij, e]
+ * and dDe_x = d De / d AB_x (all sums of positive binomial terms, no cancellation):
  *
- * (a, b, c: the term's primitive exponents on I, J, K; the Gaussian derivatives of libcint's
- * nabla, src/g2e.c:4550-4591; D by translational invariance).  Per term the bra quantities need
+ *   dE/dA_x = sum_ef Df [2a De[e-1x] (e0|f0) - iDe_x[e+1x] (e0|f0)]
+ *   dE/dB_x = sum_ef Df [2b (De[e-1x] + AB_x De[e]) (e0|f0) - dDe_x[e] (e0|f0)]
+ *   dE/dC_x = sum_ef De [2c Df[f-1x] (e0|f0) - iDf_x[f+1x] (e0|f0)]
+ *
+ * (a, b, c: the term's primitive exponents on I, J, K; D by translational invariance).  Writing
+ * the A term instead as the derivative of (e0| plus that of De(AB) gives two large contributions
+ * that cancel for distant pairs (2e-7 of the gradient lost on c4-type bases).  Per term the bra quantities need
  * only Phi[e'] = sum_f Df (e'0|f0) for |e'| in [li-1, li+lj+1], contracted axis by axis (sum
  * factorisation: z, then y, then x), and the ket ones Psi[f'] = sum_e De (e0|f'0) likewise:
  *
@@ -260,7 +268,7 @@ rys_grad_kernel(CGGradLaunch P)
  * Sb = sum 2b Phi over the task's terms are kept (per e', by the lane owning e'), and the weights
  * are applied once per task:
  *
- *   dE/dA_x = sum_e' Sa[e'] De[e'-1x] + S1[e'] (dDe_x[e'] - (e'_x + 1) De[e'+1x])
+ *   dE/dA_x = sum_e' Sa[e'] De[e'-1x] - S1[e'] iDe_x[e'+1x]
  *   dE/dB_x = sum_e' Sb[e'] (De[e'-1x] + AB_x De[e']) - S1[e'] dDe_x[e']
  *
  * (C likewise from Psi).  Exponent derivatives (coefficients fixed): the base shell's exponent a
@@ -282,17 +290,19 @@ __device__ __forceinline__ double ipow_small(double x, int p)
 }
 
 /* Transferred density of one pair (shells la at A, lb at B = A - AB), tetrahedron layout over
- * |e| <= la + lb (zero below la): Dout[e] = sum_ij w D_ij Tb[ij, e] and its derivatives along AB
- * dDout[ax][e].  One lane per e. */
+ * |e| <= la + lb (zero below la): Dout[e] = sum_ij w D_ij Tb[ij, e], the transfers of the
+ * i_x-weighted density iDout[ax][e] = sum_ij i_ax w D_ij Tb[ij, e] and, when dDout is given, the
+ * derivatives along AB dDout[ax][e].  One lane per e. */
 __device__ __forceinline__ void cg_pair_density(const double *__restrict__ dm, int nao, const CGPair &pr,
-                                                double w, double *Dout, double *dDout, int lane)
+                                                double w, double *Dout, double *iDout, double *dDout,
+                                                int lane)
 {
     const int la = pr.la, lb = pr.lb, L = la + lb, t = cg_ntet(L);
     const int nfa = ncart(la), nfb = ncart(lb);
     for (int e = lane; e < t; e += 32) {
         int ex, ey, ez;
         cg_dec3(L, e, ex, ey, ez);
-        double v = 0.0, d0 = 0.0, d1 = 0.0, d2 = 0.0;
+        double v = 0.0, d0 = 0.0, d1 = 0.0, d2 = 0.0, i0 = 0.0, i1 = 0.0, i2 = 0.0;
         if (ex + ey + ez >= la) {
             for (int ci = 0; ci < nfa; ci++) {
                 int ix, iy, iz;
@@ -308,27 +318,39 @@ __device__ __forceinline__ void cg_pair_density(const double *__restrict__ dm, i
                     const double c = d * c_binom5[jx][kx] * c_binom5[jy][ky] * c_binom5[jz][kz];
                     const double qx = ipow_small(pr.AB[0], px), qy = ipow_small(pr.AB[1], py);
                     const double qz = ipow_small(pr.AB[2], pz);
-                    v = fma(c * qx, qy * qz, v);
-                    if (px) d0 = fma(c * (double)px * ipow_small(pr.AB[0], px - 1), qy * qz, d0);
-                    if (py) d1 = fma(c * (double)py * ipow_small(pr.AB[1], py - 1), qx * qz, d1);
-                    if (pz) d2 = fma(c * (double)pz * ipow_small(pr.AB[2], pz - 1), qx * qy, d2);
+                    const double t = c * qx * (qy * qz);
+                    v += t;
+                    i0 = fma((double)ix, t, i0);
+                    i1 = fma((double)iy, t, i1);
+                    i2 = fma((double)iz, t, i2);
+                    if (dDout) {
+                        if (px) d0 = fma(c * (double)px * ipow_small(pr.AB[0], px - 1), qy * qz, d0);
+                        if (py) d1 = fma(c * (double)py * ipow_small(pr.AB[1], py - 1), qx * qz, d1);
+                        if (pz) d2 = fma(c * (double)pz * ipow_small(pr.AB[2], pz - 1), qx * qy, d2);
+                    }
                 }
             }
         }
         Dout[e] = v;
-        dDout[e] = d0;
-        dDout[t + e] = d1;
-        dDout[2 * t + e] = d2;
+        iDout[e] = i0;
+        iDout[t + e] = i1;
+        iDout[2 * t + e] = i2;
+        if (dDout) {
+            dDout[e] = d0;
+            dDout[t + e] = d1;
+            dDout[2 * t + e] = d2;
+        }
     }
 }
 
 /* One side's coordinate weights applied to its sums (lane-owned entries e', tetrahedron index
  * space Lidx >= L + 1; entries with emin <= |e'| <= L + 1):
- * gP_x += sum Sp[e'] D[e'-1x] + S1[e'] (dD_x[e'] - (e'_x + 1) D[e'+1x]) for the base centre and,
- * with Sq given, gQ_x += sum Sq[e'] (D[e'-1x] + AB_x D[e']) - S1[e'] dD_x[e'] for the partner. */
-__device__ __forceinline__ void cg_side_weights(const double *D, const double *dD, int L, int Lidx, int emin,
-                                                const double *AB, const double *S1, const double *Sp,
-                                                const double *Sq, double gP[3], double gQ[3], int lane)
+ * gP_x += sum Sp[e'] D[e'-1x] - S1[e'] iD_x[e'+1x] for the base centre and, with Sq given,
+ * gQ_x += sum Sq[e'] (D[e'-1x] + AB_x D[e']) - S1[e'] dD_x[e'] for the partner. */
+__device__ __forceinline__ void cg_side_weights(const double *D, const double *iD, const double *dD, int L,
+                                                int Lidx, int emin, const double *AB, const double *S1,
+                                                const double *Sp, const double *Sq, double gP[3],
+                                                double gQ[3], int lane)
 {
     const int t = cg_ntet(L), t1 = cg_ntet(Lidx);
     for (int e = lane; e < t1; e += 32) {
@@ -342,12 +364,14 @@ __device__ __forceinline__ void cg_side_weights(const double *D, const double *d
 #pragma unroll
         for (int ax = 0; ax < 3; ax++) {
             int y[3] = {x[0], x[1], x[2]};
-            double dp = 0.0, dmn = 0.0;
-            if (s + 1 <= L) { y[ax]++; dp = D[cg_idx3(L, y[0], y[1], y[2])]; y[ax]--; }
+            double ip = 0.0, dmn = 0.0;
+            if (s + 1 <= L) { y[ax]++; ip = iD[ax * t + cg_idx3(L, y[0], y[1], y[2])]; y[ax]--; }
             if (x[ax] >= 1) { y[ax]--; dmn = D[cg_idx3(L, y[0], y[1], y[2])]; }
-            const double tt = me >= 0 ? dD[ax * t + me] : 0.0;
-            gP[ax] += fma(sp, dmn, s1 * fma(-(double)(x[ax] + 1), dp, tt));
-            if (Sq) gQ[ax] += fma(sq, fma(AB[ax], d0, dmn), -s1 * tt);
+            gP[ax] += fma(sp, dmn, -s1 * ip);
+            if (Sq) {
+                const double tt = me >= 0 ? dD[ax * t + me] : 0.0;
+                gQ[ax] += fma(sq, fma(AB[ax], d0, dmn), -s1 * tt);
+            }
         }
     }
 }
@@ -422,8 +446,8 @@ rys_gradj_kernel(CGGradLaunch P)
         /* per task: transferred densities, then the sums over terms of Phi, 2a Phi, 2b Phi (bra,
          * per e') and of Psi, 2c Psi (ket, per f'); the lane e' mod 32 owns entry e'.  With
          * exponents: the four shells' exponent weights and per-primitive sums. */
-        double *De = ws, *dDe = De + tE0, *Df = dDe + 3 * tE0, *dDf = Df + tF0;
-        double *S1 = dDf + 3 * tF0, *Sa = S1 + tE, *Sb = Sa + tE, *S1k = Sb + tE, *Sc = S1k + tF;
+        double *De = ws, *iDe = De + tE0, *dDe = iDe + 3 * tE0, *Df = dDe + 3 * tE0, *iDf = Df + tF0;
+        double *S1 = iDf + 3 * tF0, *Sa = S1 + tE, *Sb = Sa + tE, *S1k = Sb + tE, *Sc = S1k + tF;
         double *WI = Sc + tF, *WJ = WI + tE, *WK = WJ + tE, *WL = WK + tF;
         double *aacc = WL + tF;
         double *term = ws + L.off_w;
@@ -438,8 +462,8 @@ rys_gradj_kernel(CGGradLaunch P)
                             * common_fac_sp(lk) * common_fac_sp(ll);
         const double wq = 0.5 * ((tk.sym & 1) ? 2.0 : 1.0) * ((tk.sym & 2) ? 2.0 : 1.0)
                         * ((tk.sym & 4) ? 2.0 : 1.0);
-        cg_pair_density(P.dm, P.nao, pij, wq, De, dDe, lane);
-        cg_pair_density(P.dm, P.nao, pkl, 1.0, Df, dDf, lane);
+        cg_pair_density(P.dm, P.nao, pij, wq, De, iDe, dDe, lane);
+        cg_pair_density(P.dm, P.nao, pkl, 1.0, Df, iDf, nullptr, lane);
         for (int e = lane; e < 3 * tE + 2 * tF; e += 32) S1[e] = 0.0;
         if (EXP)
             for (int e = lane; e < 4 * CG_GRAD_MAXPRIM; e += 32) aacc[e] = 0.0;
@@ -629,8 +653,8 @@ rys_gradj_kernel(CGGradLaunch P)
         }
         /* the coordinate weights, once per task */
         double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
-        cg_side_weights(De, dDe, Le, nmax, emin, pij.AB, S1, Sa, Sb, gA, gB, lane);
-        cg_side_weights(Df, dDf, Lf, mmax, fmin, pkl.AB, S1k, Sc, nullptr, gC, gC, lane);
+        cg_side_weights(De, iDe, dDe, Le, nmax, emin, pij.AB, S1, Sa, Sb, gA, gB, lane);
+        cg_side_weights(Df, iDf, nullptr, Lf, mmax, fmin, pkl.AB, S1k, Sc, nullptr, gC, gC, lane);
         /* warp sums of the nine coordinate derivatives; D by translational invariance */
 #pragma unroll
         for (int a = 0; a < 3; a++) {

@@ -117,7 +117,7 @@ def _ntet(L):
 @pytest.mark.parametrize('mode', [GRADJ, GRADAJ])
 def test_contraction_first_adjoint_layouts_fit(mode):
     """Every l <= 4 class of the contraction-first adjoint fits 48 KB per warp: per-task densities
-    (4 tetrahedra each side), the lane-owned sums (3 + 2 tetrahedra of the raised ranges; with
+    (bra: the density, its i-weighted and AB-derivative transfers, 7 tetrahedra; ket: 4), the lane-owned sums (3 + 2 tetrahedra of the raised ranges; with
     exponents the four exponent weights and 64 per-primitive sums), then per term the record, the
     VRR arrays of both raised ranges and the larger side's contraction buffers (+ 64 exponent
     partials); strides odd."""
@@ -137,7 +137,7 @@ def test_contraction_first_adjoint_layouts_fit(mode):
         bufb = _np2(Lf) * na + (Lf + 1) * _np2(L.nmax)
         bufk = _np2(Le) * nm + (Le + 1) * _np2(L.mmax)
         assert L.scr >= max(bufb, bufk) + (64 if ex else 0) and L.scr % 2 == 1
-        fixed = 4 * _ntet(Le) + 4 * _ntet(Lf) + 3 * _ntet(L.nmax) + 2 * _ntet(L.mmax)
+        fixed = 7 * _ntet(Le) + 4 * _ntet(Lf) + 3 * _ntet(L.nmax) + 2 * _ntet(L.mmax)
         if ex:
             fixed += 2 * _ntet(L.nmax) + 2 * _ntet(L.mmax) + 4 * GRAD_MAXPRIM
         assert L.off_w == fixed and L.off_g == fixed + L.T * L.termw
