@@ -1163,13 +1163,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
          * about a distant centre (a distant, exponent-asymmetric f-f pair loses ~3e-7 of its
          * largest diagonal element with the base on the diffuse shell, libcint included). */
         auto amin = [](const ShellView &v) { return *std::min_element(v.ex, v.ex + v.nprim); };
-        /* the contraction-first adjoint carries the density through the transfer about the first
-         * shell of each pair for whole tasks, so there the tighter shell always comes first,
-         * whatever the l: the product densities sit near it, and the transfer's binomial terms
-         * stay small (the cost is a longer range of e when the tighter shell has the lower l) */
-        const bool tight_first = P->gradj && (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA);
         auto first = [&](int a, int b) {   /* shell a goes before shell b */
-            if (tight_first) return amin(sv[a]) >= amin(sv[b]);
             return sv[a].l > sv[b].l || (sv[a].l == sv[b].l && amin(sv[a]) >= amin(sv[b]));
         };
         int perm[4] = {0, 1, 2, 3};
@@ -1356,6 +1350,8 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
     };
     struct TaskCost { CGTask t; double cost; int group; };
     std::vector<TaskCost> tc;
+    std::vector<signed char> turn_of(P->gradj ? P->prims.size() : 0, -1);
+    std::vector<int> part_tmp;
     std::unordered_map<int, int> grad_cls, eri_cls;
     int64_t gpos = 0;
     for (const Work &w : work) {
@@ -1423,16 +1419,51 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
                 o.CD[c] = P->pairs[pe.pkl].AB[c];
             }
         }
-        for (int64_t a0 = 0; a0 < w.n; a0 += slice) {
+        /* the contraction-first adjoint expands a primitive pair's density about its first centre
+         * with binomial terms up to (1 + 2 b / a)^lb times the result (a, b: the primitives'
+         * exponents); where that exceeds 16 and the second centre would do better,
+         * (1 + 2 a / b)^la, the pair is seen from the second centre (bits 3/4): the quartet's
+         * primitive quartets are grouped by the two choices, each group sliced into its own
+         * tasks */
+        int64_t gbeg[5] = {0, w.n, w.n, w.n, w.n};
+        if (P->gradj) {
+            const CGPair &bp = P->pairs[pe.pij], &kp = P->pairs[pe.pkl];
+            const int nij = bp.npa * bp.npb;
+            auto turn = [&](const CGPair &pr, int i) {   /* cached per primitive pair */
+                signed char &t = turn_of[pr.prim_off + i];
+                if (t < 0) {
+                    const CGPrimPair &x = P->prims[pr.prim_off + i];
+                    const double a = x.aA, b = x.a - x.aA;
+                    const double k0 = pr.lb * std::log1p(2.0 * b / a), k1 = pr.la * std::log1p(2.0 * a / b);
+                    t = k0 > std::log(16.0) && k1 < k0 ? 1 : 0;
+                }
+                return t == 1;
+            };
+            auto grp = [&](int q) {
+                return (turn(bp, q % nij) ? 1 : 0) | (turn(kp, q / nij) ? 2 : 0);
+            };
+            int *beg = P->pqlist.data() + w.off;
+            part_tmp.assign(beg, beg + w.n);
+            const std::vector<int> &tmp = part_tmp;
+            int64_t cnt[4] = {0, 0, 0, 0};
+            for (int64_t i = 0; i < w.n; i++) cnt[grp(tmp[i])]++;
+            gbeg[0] = 0;
+            for (int g = 0; g < 4; g++) gbeg[g + 1] = gbeg[g] + cnt[g];
+            int64_t pos[4] = {gbeg[0], gbeg[1], gbeg[2], gbeg[3]};
+            for (int64_t i = 0; i < w.n; i++) beg[pos[grp(tmp[i])]++] = tmp[i];
+        }
+        for (int g = 0; g < 4; g++)
+        for (int64_t a0 = gbeg[g]; a0 < gbeg[g + 1]; a0 += slice) {
             TaskCost x;
             x.t.pij = pe.pij; x.t.pkl = pe.pkl;
             x.t.pq_off = (int)(w.off + a0);
-            x.t.npq = (int)std::min<int64_t>(slice, w.n - a0);
+            x.t.npq = (int)std::min<int64_t>(slice, gbeg[g + 1] - a0);
             x.t.cart_off = gpos;
             x.t.out = pe.out;
             x.t.sym = pe.sym;
             if (group == 2 || CG_IS_IP(P->mode))   /* per-primitive recurrences: base choice */
                 x.t.sym |= (pair_swap(pe.pij) ? 8 : 0) | (pair_swap(pe.pkl) ? 16 : 0);
+            if (P->gradj) x.t.sym |= g << 3;
             x.t.cls = cls;
             x.t.pad = 0;
             x.cost = x.t.npq * w.cost_pq;

@@ -257,7 +257,13 @@ rys_grad_kernel(CGGradLaunch P)
  *
  * (a, b, c: the term's primitive exponents on I, J, K; D by translational invariance).  Writing
  * the A term instead as the derivative of (e0| plus that of De(AB) gives two large contributions
- * that cancel for distant pairs (2e-7 of the gradient lost on c4-type bases).  Per term the bra quantities need
+ * that cancel.  Conditioning: for a primitive pair with product centre P, the transfer's binomial
+ * terms exceed the result by ((|PA| + |AB|) / |PB|)^lb = (1 + 2 b / a)^lb, harmless when the base
+ * primitive a is the tighter one and ruinous when it is a diffuse partner of a tight b (contracted
+ * shells mix both: 8e-8 of a c4 gradient).  So every primitive pair expands about its tighter
+ * primitive: the planner groups a quartet's primitive quartets by the two choices (bra, ket) into
+ * separate tasks, and a task with bit 3 (4) of sym set sees its bra (ket) pair from the second
+ * centre.  Per term the bra quantities need
  * only Phi[e'] = sum_f Df (e'0|f0) for |e'| in [li-1, li+lj+1], contracted axis by axis (sum
  * factorisation: z, then y, then x), and the ket ones Psi[f'] = sum_e De (e0|f'0) likewise:
  *
@@ -414,6 +420,22 @@ __device__ __forceinline__ double cg_warp_sum2(double x, double y, int lane)
     return v;
 }
 
+/* The same shell pair seen from its second centre: base and partner exchanged (AB -> -AB; the
+ * primitive pair records stay those of the original order) */
+__device__ __forceinline__ void cg_swap_pair(CGPair &p)
+{
+    for (int c = 0; c < 3; c++) {
+        p.A[c] -= p.AB[c];
+        p.AB[c] = -p.AB[c];
+    }
+    int t;
+    t = p.la; p.la = p.lb; p.lb = t;
+    t = p.ao_a; p.ao_a = p.ao_b; p.ao_b = t;
+    t = p.atom_a; p.atom_a = p.atom_b; p.atom_b = t;
+    t = p.gp_a; p.gp_a = p.gp_b; p.gp_b = t;
+    t = p.npa; p.npa = p.npb; p.npb = t;
+}
+
 template <bool EXP>
 __global__ void __launch_bounds__(128, 2)
 rys_gradj_kernel(CGGradLaunch P)
@@ -430,8 +452,14 @@ rys_gradj_kernel(CGGradLaunch P)
         tid = __shfl_sync(FULL, tid, 0);
         if (tid >= P.ntasks) break;
         const CGTask tk = P.tasks[tid];
-        const CGPair pij = P.pairs[tk.pij];
-        const CGPair pkl = P.pairs[tk.pkl];
+        /* the task's primitive pairs all expand about their tighter primitive: bit 3 (4) set, the
+         * bra (ket) pair's second centre */
+        CGPair pij = P.pairs[tk.pij];
+        CGPair pkl = P.pairs[tk.pkl];
+        const int npa0 = pij.npa, npc0 = pkl.npa;
+        const bool swb = (tk.sym >> 3) & 1, swk = (tk.sym >> 4) & 1;
+        if (swb) cg_swap_pair(pij);
+        if (swk) cg_swap_pair(pkl);
         const int li = pij.la, lj = pij.lb, lk = pkl.la, ll = pkl.lb;
         CGLayout L;
         cg_class_layout(li, lj, lk, ll, LMODE, P.ws_doubles, &L);
@@ -491,17 +519,20 @@ rys_gradj_kernel(CGGradLaunch P)
                 const CGPrimPair B = ppkl[kl];
                 double *rec = term + lane * L.termw;
                 cg_term(A, B, pij, pkl, n, r, common, P.rys_coef, rec, P.omega2, P.expcut);
-                rec[10] = 2.0 * A.aA;
-                rec[11] = 2.0 * (A.a - A.aA);
-                rec[12] = 2.0 * B.aA;
+                const double aa = A.aA, ab = A.a - A.aA, ac = B.aA, ad = B.a - B.aA;
+                rec[10] = 2.0 * (swb ? ab : aa);   /* the base exponents: 2a, 2b of the bra, 2c */
+                rec[11] = 2.0 * (swb ? aa : ab);
+                rec[12] = 2.0 * (swk ? ad : ac);
                 double mb = 0.0;
                 for (int m = 0; m <= mmax; m++) { rec[13 + m] = mb; mb += rec[2]; }
                 if (EXP) {
+                    /* primitive indices in the (possibly exchanged) base and partner shells */
                     int *ri = reinterpret_cast<int *>(rec + 13 + nm);
-                    ri[0] = ij % pij.npa;
-                    ri[1] = ij / pij.npa;
-                    ri[2] = kl % pkl.npa;
-                    ri[3] = kl / pkl.npa;
+                    const int ip = ij % npa0, jp = ij / npa0, kp = kl % npc0, lp = kl / npc0;
+                    ri[0] = swb ? jp : ip;
+                    ri[1] = swb ? ip : jp;
+                    ri[2] = swk ? lp : kp;
+                    ri[3] = swk ? kp : lp;
                 }
             }
             if (EXP)
