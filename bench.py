@@ -179,7 +179,9 @@ def extra_dropin(cg, mol, qs, batched_value, n=4000):
     """The plain drop-in on its own workload, configs[0]-style c0 (8 atoms, 6 A, s,s,p,p,d x 4
     primitives): one libcint-signature int2e_sph call per quartet from host buffers, without and
     with an int2e_optimizer (whose side table caches the shell pairs' primitive data), on the first
-    n of its 336,610 unique quartets; and the batched plan over the whole c0 list for the ratio."""
+    n of its 336,610 unique quartets, from one host thread and from 4, 16 and all host threads at
+    once (libcint's OpenMP caller pattern); and the batched plan over the whole c0 list for the
+    ratio."""
     import torch
     from libcint_gb300 import molecules as M
     m0 = M.config0(seed=0)
@@ -203,6 +205,27 @@ def extra_dropin(cg, mol, qs, batched_value, n=4000):
               P(m0.env), o, None)
         dt = time.perf_counter() - t0
         res[tag] = {'integrals_per_s': nint / dt, 'quartets_per_s': n / dt}
+    # libcint's caller pattern: host threads calling int2e_sph concurrently (each thread its own
+    # output buffer, one shared optimizer; the library keeps a stream per thread)
+    import threading
+    rows = [np.ascontiguousarray(q) for q in sub]
+    args = (P(m0.atm), m0.natm, P(m0.bas), m0.nbas, P(m0.env), opt, None)
+    res['threads'] = {}
+    for nth in sorted({4, 16, os.cpu_count() or 16}):
+        bufs = [np.zeros_like(buf) for _ in range(nth)]
+
+        def work(t):
+            b = P(bufs[t])
+            for i in range(t, len(rows), nth):
+                f(b, None, P(rows[i]), *args)
+        th = [threading.Thread(target=work, args=(t,)) for t in range(nth)]
+        t0 = time.perf_counter()
+        for x in th:
+            x.start()
+        for x in th:
+            x.join()
+        dt = time.perf_counter() - t0
+        res['threads'][str(nth)] = {'integrals_per_s': nint / dt, 'quartets_per_s': n / dt}
     L.CINTdel_optimizer(ctypes.byref(opt))
     p = cg.Plan(cg.INT2E_SPH, m0, allq)
     out = torch.empty(p.output_size, dtype=torch.float64, device='cuda')
@@ -710,7 +733,8 @@ def run_gpu(args, rank, world):
               'fp64peak': extra_fp64peak,
               'screened': lambda: extra_screened(cg),
               'c4': lambda: extra_c4(cg),
-              'c2': lambda: extra_c2(cg)}[args.only]
+              'c2': lambda: extra_c2(cg),
+              'dropin': lambda: extra_dropin(cg, None, None, None)}[args.only]
         if rank == 0:
             print(json.dumps({'extra': args.only, **fn()}), flush=True)
         return
@@ -852,7 +876,7 @@ def main():
                     help='default launch parameters instead of the autotuner\'s choice')
     ap.add_argument('--no-extras', action='store_true', help='skip the side workloads (drop-in, int3c2e, adjoint, J/K, screening, DF)')
     ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk', 'df', 'screening',
-                                                          'fp64peak', 'screened', 'c4', 'c2'],
+                                                          'fp64peak', 'screened', 'c4', 'c2', 'dropin'],
                     help='run one side workload alone and print its line (profiling)')
     ap.add_argument('--c3-atoms', type=int, default=24, help='atoms of the adjoint workload')
     args = ap.parse_args()

@@ -1952,24 +1952,23 @@ CACHE_SIZE_T dropin(int kind, double *out, FINT *dims, FINT *shls, FINT *atm, FI
     int rc = build_plan(&P, kind, shls, 1, NULL, atm, natm, bas, nbas, env,
                         (int64_t)g_ctx.sm_count * 8, os.get());
     if (rc) return failed();
+    /* libcint's return value: 0 when no primitive quartet survives the screening, which the
+     * planner decides on the host (a quartet without tasks); such a block is zero-filled here
+     * without a GPU round trip, and a block with tasks is non-empty */
+    if (P.empty_outs.size() == P.outs.size()) { zero_fill(); return 0; }
     size_t need = plan_device_bytes(&P);
     size_t up = plan_upload_bytes(&P);
     size_t outb = sizeof(double) * P.out_size * ncomp;
     if (grow_dev(&T.arena, &T.arena_size, need) || grow_dev((char **)&T.dout, &T.dout_size, outb)
-        || grow_host(&T.pinned, &T.pinned_size, up + sizeof(int) * P.outs.size())
+        || grow_host(&T.pinned, &T.pinned_size, up)
         || grow_host((char **)&T.hout, &T.hout_size, outb))
         return failed();
     rc = upload_plan(&P, T.arena, T.arena_size, T.stream, true, T.pinned);
     if (!rc) rc = execute_plan(&P, T.dout, T.stream);
-    int *ne_host = (int *)(T.pinned + up);
     if (!rc && cudaMemcpyAsync(T.hout, T.dout, outb, cudaMemcpyDeviceToHost, T.stream) != cudaSuccess) rc = -1;
-    if (!rc && cudaMemcpyAsync(ne_host, P.d_nonempty, sizeof(int) * P.outs.size(), cudaMemcpyDeviceToHost, T.stream) != cudaSuccess) rc = -1;
     if (!rc && cudaStreamSynchronize(T.stream) != cudaSuccess) { set_error("kernel execution failed: %s", cudaGetErrorString(cudaGetLastError())); rc = -1; }
     P.dbuf = nullptr;
     if (rc) return failed();
-    int nonempty = 0;
-    for (size_t o = 0; o < P.outs.size(); o++) nonempty |= ne_host[o];
-    if (!nonempty) { zero_fill(); return 0; }
     /* dense GPU block -> caller layout with dims */
     for (int comp = 0; comp < ncomp; comp++) {
         const double *src = T.hout + comp * P.out_size;

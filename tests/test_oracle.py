@@ -194,6 +194,35 @@ def test_oracle_matches_libcint_with_optimizer(oracle):
         L.CINTdel_optimizer(ctypes.byref(opt))
 
 
+def sparse_items(seed=5):
+    """A sparse system (config2's orbital basis, 4 atoms in a 14 A cube) where about 40 % of
+    random shell quartets and 15 % of (ij|P) triples have every primitive screened out, with the
+    int2e and int3c2e samples drawn from it"""
+    mol, norb = M.config2(seed=3, natm=4, box=14.0)
+    rng = np.random.RandomState(seed)
+    q4 = rng.randint(0, norb, (400, 4)).astype(np.int32)
+    q3 = np.c_[rng.randint(0, norb, (400, 2)), rng.randint(norb, mol.nbas, 400)].astype(np.int32)
+    return mol, q4, q3
+
+
+def test_oracle_flags_match_libcint_sparse(oracle):
+    """libcint's return value (0 when every primitive quartet is screened, src/cint2e.c:861-869;
+    the triple's cutoff without the +1, src/cint3c2e.c) on a sample where both values occur: the
+    oracle gives the same flag and block as libcint compiled from its sources"""
+    if oracle.ref is None:
+        pytest.skip('libcint not built from sources on this machine')
+    mol, q4, q3 = sparse_items()
+    seen = set()
+    for name, items in (('int2e_sph', q4), ('int2e_ip1_sph', q4[:150]), ('int3c2e_sph', q3)):
+        for it in items:
+            fa, a = oracle.port.call(name, mol, it)
+            fb, b = oracle.ref.call(name, mol, it)
+            assert fa == fb
+            seen.add(fa)
+            assert np.abs(a - b).max() <= 1e-12
+    assert seen == {0, 1}
+
+
 def test_oracle_matches_libcint_live_c1(oracle):
     if oracle.ref is None:
         pytest.skip('libcint not built from sources on this machine')
