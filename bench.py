@@ -452,10 +452,53 @@ def extra_jk(cg, seed=0, natm=24):
             'coulomb_energy': float(0.5 * (dm * J).sum()), 'exchange_energy': float(-0.25 * (dm * K).sum())}
 
 
+def hbm_peak_gbs():
+    """(GB/s, source): the driver's measured copy bandwidth when MEASURED_PEAKS.json is present,
+    else the fallback figure of an earlier GB300 measurement"""
+    path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    try:
+        with open(path) as f:
+            v = float(json.load(f)['hbm_gbs'])
+        return v, 'measured (MEASURED_PEAKS.json hbm_gbs)'
+    except Exception:
+        return 6800.0, 'fallback 6.8 TB/s (no MEASURED_PEAKS.json)'
+
+
+def _df_kernel_times(fit, dm, reps=5):
+    """best-of-reps CUDA-event times (ms) of the two DF kernels and of a whole J build"""
+    import torch
+    c = fit.coefficients(dm)
+    out = {}
+    for tag, fn in (('rho', lambda: fit.rho(dm)), ('j', lambda: fit.vj_from_coefficients(c)),
+                    ('vj', lambda: fit.vj(dm))):
+        fn()
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            best = e0.elapsed_time(e1) if best is None else min(best, e0.elapsed_time(e1))
+        out[tag + '_ms'] = best
+    # one FP64 FMA per 8-byte element: the FP64 pipe (measured DFMA peak) streams at most
+    # FP64_PEAK_TFLOPS / 2 G elements/s, below HBM, so it is the bound; HBM is reported beside it
+    peak, src = hbm_peak_gbs()
+    fma_gbs = FP64_PEAK_TFLOPS * 1e12 / 2 * 8 / 1e9
+    nbytes = 8.0 * fit.T.numel()
+    for tag in ('rho', 'j'):
+        gbs = nbytes / (out[tag + '_ms'] * 1e-3) / 1e9
+        out[tag + '_roofline'] = {'bound': 'fp64', 'achieved': gbs, 'peak': fma_gbs, 'unit': 'GB/s',
+                                  'frac': gbs / fma_gbs, 'algorithmic_bytes': nbytes,
+                                  'peak_source': 'one FMA per element at the measured DFMA peak',
+                                  'hbm_peak': peak, 'hbm_frac': gbs / peak, 'hbm_peak_source': src}
+    return out
+
+
 def extra_df(cg, seed=0, natm=20):
     """Density-fitted J on a c2-type system (orbital s,s,p,p,d with 1-6 primitives, auxiliary
-    l <= 4 x 2 per atom, same density of atoms as c2): set-up (both plans, metric Cholesky) and
-    one J build."""
+    l <= 4 x 2 per atom, same density of atoms as c2): set-up (the int3c2e buffer, the metric and
+    its Cholesky factor) and one J build, with the two DF kernels' own times against HBM."""
     import torch
     from libcint_gb300 import molecules as M
     from libcint_gb300.df import DFCoulomb
@@ -470,10 +513,52 @@ def extra_df(cg, seed=0, natm=20):
     d = rng.normal(0, 0.1, (fit.nao, fit.nao))
     dm = torch.as_tensor(0.5 * (d + d.T), device='cuda')
     t_j = _timed(lambda: fit.vj(dm))
-    return {'workload': 'c2-type: %d atoms, %.1f A, all %d orbital shell pairs x %d aux shells'
-                        % (natm, box, norb * (norb + 1) // 2, mol.nbas - norb),
-            'nao': fit.nao, 'naux': fit.naux, 'three_index_elements': int(fit.T.numel()),
-            'setup_s': t_setup, 'vj_ms': 1e3 * t_j}
+    res = {'workload': 'c2-type: %d atoms, %.1f A, all %d orbital shell pairs x %d aux shells'
+                       % (natm, box, norb * (norb + 1) // 2, mol.nbas - norb),
+           'nao': fit.nao, 'naux': fit.naux, 'three_index_elements': int(fit.T.numel()),
+           'setup_s': t_setup, 'vj_ms': 1e3 * t_j, 'kernels': _df_kernel_times(fit, dm)}
+    fit.close()
+    return res
+
+
+def extra_dfc2(cg, seed=0, thr=1e-12):
+    """Density-fitted J at c2's full size: 200 atoms, 1000 orbital shells (2600 AOs), 2000
+    auxiliary shells (10,000 functions); every orbital shell pair with Q_ij max_P Q_P >= 1e-12
+    (the pairs with any surviving triple) x every auxiliary shell, the three-index buffer resident
+    in HBM.  Reports the set-up and the J build's kernels against HBM."""
+    import torch
+    from libcint_gb300 import molecules as M
+    from libcint_gb300.df import DFCoulomb
+    from libcint_gb300.screening import pair_bounds
+    mol, norb = M.config2(seed=seed)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ii, jj = np.tril_indices(norb)
+    pairs = np.stack([ii, jj], 1)
+    qij = pair_bounds(mol, pairs)
+    env = list(mol.env)
+    pe = len(env)
+    env += [0.0, 2.0 * np.sqrt(np.pi)]
+    bas = np.vstack([mol.bas, [[0, 0, 1, 1, 0, pe, pe + 1, 0]]]).astype(np.int32)
+    molf = M.Mol(mol.atm, bas, np.array(env), mol.name)
+    aux = np.arange(norb, mol.nbas, dtype=np.int64)
+    qp = pair_bounds(molf, np.stack([aux, np.full_like(aux, bas.shape[0] - 1)], 1))
+    keep = qij * qp.max() >= thr
+    t_bounds = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    fit = DFCoulomb(mol, norb, pairs=pairs[keep])
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    rng = np.random.RandomState(seed)
+    d = torch.as_tensor(rng.normal(0, 0.1, (fit.nao, fit.nao)), device='cuda')
+    dm = 0.5 * (d + d.T)
+    res = {'workload': 'c2 full: 200 atoms, 18 A; %d of %d orbital shell pairs (Q_ij max Q_P >= 1e-12) '
+                       'x all %d auxiliary shells' % (int(keep.sum()), len(pairs), len(aux)),
+           'nao': fit.nao, 'naux': fit.naux, 'three_index_elements': int(fit.T.numel()),
+           'three_index_gb': 8e-9 * fit.T.numel(), 'bounds_s': t_bounds, 'setup_s': t_setup,
+           'kernels': _df_kernel_times(fit, dm, reps=3)}
+    fit.close()
+    return res
 
 
 def extra_screening(cg, seed=0, natm=24, threshold=1e-10):
@@ -734,7 +819,8 @@ def run_gpu(args, rank, world):
               'screened': lambda: extra_screened(cg),
               'c4': lambda: extra_c4(cg),
               'c2': lambda: extra_c2(cg),
-              'dropin': lambda: extra_dropin(cg, None, None, None)}[args.only]
+              'dropin': lambda: extra_dropin(cg, None, None, None),
+              'dfc2': lambda: extra_dfc2(cg)}[args.only]
         if rank == 0:
             print(json.dumps({'extra': args.only, **fn()}), flush=True)
         return
@@ -876,7 +962,7 @@ def main():
                     help='default launch parameters instead of the autotuner\'s choice')
     ap.add_argument('--no-extras', action='store_true', help='skip the side workloads (drop-in, int3c2e, adjoint, J/K, screening, DF)')
     ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk', 'df', 'screening',
-                                                          'fp64peak', 'screened', 'c4', 'c2', 'dropin'],
+                                                          'fp64peak', 'screened', 'c4', 'c2', 'dropin', 'dfc2'],
                     help='run one side workload alone and print its line (profiling)')
     ap.add_argument('--c3-atoms', type=int, default=24, help='atoms of the adjoint workload')
     args = ap.parse_args()

@@ -319,6 +319,26 @@ int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,
 int cintgpu_int2e_sph_noalloc(double *out_dev, const int *shls, int64_t n, const int *atm,
                               int natm, const int *bas, int nbas, const double *env, void *stream);
 
+/* Density-fitted Coulomb contractions (no libcint counterpart; the caller pattern of RI-J over
+ * int3c2e_sph, src/cint3c2e.c, with the metric from int2c2e_sph, src/cint2c2e.c).  The packed
+ * buffer T is what a CINTGPU_INT3C2E_SPH (or _CART) plan with offsets = NULL writes for the items
+ * "pair p = (i, j) with every auxiliary shell, auxiliary shells in order", pairs in the order
+ * given: pair p owns di*dj*naux doubles, element (a, b, Q) at a + di*(b + dj*Q).  pairs (host):
+ * npair x {oi, oj, di, dj}, the AO offsets and extents of shells i and j (oi == oj only for
+ * i == j; di*dj <= 256).  Device arrays: dm and vj nao x nao row-major, rho and c naux.
+ *   cintgpu_df_rho:  rho_Q = sum_p w_p sum_ab T_p[ab,Q] dm[oi+a, oj+b]   (w_p = 2 if i != j)
+ *   cintgpu_df_j:    vj = 0, then vj[oi+a, oj+b] = vj[oj+b, oi+a] = sum_Q T_p[ab,Q] c_Q
+ * Both are asynchronous on `stream` and read T once; calls on one handle are serialised by the
+ * caller (cintgpu_df_j keeps its work counter in the handle). */
+typedef struct CINTGPUDF CINTGPUDF;
+int cintgpu_df_create(CINTGPUDF **df, const int *pairs, int64_t npair, int nao, int naux);
+int64_t cintgpu_df_size(const CINTGPUDF *df);   /* doubles of T */
+int cintgpu_df_rho(CINTGPUDF *df, const double *T_dev, const double *dm_dev, double *rho_dev,
+                   void *stream);
+int cintgpu_df_j(CINTGPUDF *df, const double *T_dev, const double *c_dev, double *vj_dev,
+                 void *stream);
+void cintgpu_df_destroy(CINTGPUDF *df);
+
 /* Rys nodes s = t^2 and weights from the device tables, for testing: xs, s, w device arrays */
 int cintgpu_rys_roots_dev(int nroots, const double *xs_dev, int count, double *s_dev,
                           double *w_dev, void *stream);

@@ -114,6 +114,16 @@ def lib():
     L.cintgpu_dropin_failures.restype = i64
     L.cintgpu_dropin_failures.argtypes = []
     L.cintgpu_device_sm_count.restype = i32
+    L.cintgpu_df_create.argtypes = [vp, vp, i64, i32, i32]
+    L.cintgpu_df_create.restype = i32
+    L.cintgpu_df_size.argtypes = [vp]
+    L.cintgpu_df_size.restype = i64
+    L.cintgpu_df_rho.argtypes = [vp, vp, vp, vp, vp]
+    L.cintgpu_df_rho.restype = i32
+    L.cintgpu_df_j.argtypes = [vp, vp, vp, vp, vp]
+    L.cintgpu_df_j.restype = i32
+    L.cintgpu_df_destroy.argtypes = [vp]
+    L.cintgpu_df_destroy.restype = None
     _lib = L
     return L
 

@@ -18,7 +18,7 @@ LIB = os.path.join(BUILD, 'libcintgpu.so')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-std=c++17', '-O3', '-lineinfo', '-Xcompiler', '-fPIC',
               '-I' + os.path.join(ROOT, 'include'), '-I' + CSRC]
-SOURCES = ['rys_kernels.cu', 'rys_grad.cu', 'cintgpu_host.cpp', 'noalloc.cu']
+SOURCES = ['rys_kernels.cu', 'rys_grad.cu', 'cintgpu_host.cpp', 'noalloc.cu', 'df_kernels.cu']
 HEADERS = ['rys_kernels.h', 'rys_device.cuh', 'cintgpu_types.h', 'rys_tables.inc',
            'cintgpu_internal.h']
 

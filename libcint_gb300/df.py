@@ -7,12 +7,17 @@ batched int3c2e and int2c2e plans:
 The orbital and auxiliary shells live in one basis, as libcint's callers pass them to int3c2e_sph
 / int2c2e_sph (auxiliary shells after the orbital ones, src/cint3c2e.c:693-717,
 src/cint2c2e.c:351-358).  The three-centre integrals of every orbital shell pair i >= j with every
-auxiliary shell are computed once by one plan and stay in HBM in the plan's packed layout (blocks
-(di, dj, dP) back to back, i fastest); host-built index maps give each packed element its AO pair
-and auxiliary function, so a J build is two gathers and two scatter-adds over that buffer plus a
-triangular solve.  K uses the buffer scattered into a dense (naux, nao, nao) tensor whitened by
-the metric's Cholesky factor: K = sum_q B~_q D B~_q^T.  Densities, J and K are spherical
-(libcint's int2e_sph AO order).
+auxiliary shell are computed once (plans over chunks of pairs, planned on host threads while the
+GPU runs earlier chunks) and stay in HBM in the plans' packed layout (blocks (di, dj, dP) back to
+back, i fastest: pair p owns di dj naux doubles).  A J build is two passes of the library's DF
+kernels over that buffer (cintgpu_df_rho, cintgpu_df_j: per-pair descriptors only, no per-element
+index arrays, no atomics on J) around a triangular solve.  K uses the buffer scattered into a
+dense (naux, nao, nao) tensor whitened by the metric's Cholesky factor: K = sum_q B~_q D B~_q^T
+(small systems).  Densities, J and K are spherical (libcint's int2e_sph AO order).
+
+The per-element formulation (packed_index, fit_weights, contract_rho, contract_j: gathers and
+scatter-adds in torch) states the same contractions densely; the CPU tests check it against
+einsums over the oracle's full tensor and the GPU tests check the kernels against it.
 """
 import numpy as np
 
@@ -134,11 +139,15 @@ def contract_k(Bt, dm):
 
 class DFCoulomb:
     """RI-J for one geometry: orbital shells 0..norb-1, auxiliary shells norb..nbas-1 of mol.
-    pairs: orbital shell pairs (i >= j) to include (default: all)."""
+    pairs: orbital shell pairs (i >= j) to include (default: all).  chunk: (ij|P) triples per
+    int3c2e plan while the buffer is built."""
 
-    def __init__(self, mol, norb, pairs=None):
+    def __init__(self, mol, norb, pairs=None, chunk=4_000_000):
+        import ctypes
+        from concurrent.futures import ThreadPoolExecutor
+
         import torch
-        from . import INT2C2E_SPH, INT3C2E_SPH, Plan
+        from . import INT2C2E_SPH, INT3C2E_SPH, Plan, _check, _ptr, lib
         self.mol, self.norb = mol, norb
         nsph = _nsph(mol)
         loc = np.concatenate([[0], np.cumsum(nsph)])
@@ -146,42 +155,77 @@ class DFCoulomb:
         self.naux = int(loc[-1] - loc[norb])
         offs = loc[:-1].copy()
         offs[norb:] -= loc[norb]                          # auxiliary functions counted from 0
+        self._nsph, self._offs = nsph, offs
         if pairs is None:
             ii, jj = np.tril_indices(norb)
             pairs = np.stack([ii, jj], 1)
         pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
-        items3, items2 = df_items(norb, mol.nbas, pairs)
-        p3 = Plan(INT3C2E_SPH, mol, items3)
-        self.T = torch.empty(p3.output_size, dtype=torch.float64, device='cuda')
-        p3.execute(self.T)
-        pair_idx, aux_idx = df_index(pairs, nsph, offs, self.nao, self.naux)
-        if len(pair_idx) != self.T.numel() or (len(pair_idx) and (
-                pair_idx.max() >= self.nao * self.nao or aux_idx.max() >= self.naux)):
-            raise ValueError('index maps do not match the (ij|P) buffer')   # host-side check
-        dev = self.T.device
-        self.pair_idx = torch.as_tensor(pair_idx, device=dev)
-        self.aux_idx = torch.as_tensor(aux_idx, device=dev)
-        self.w = torch.as_tensor(fit_weights(items3, nsph), device=dev)
+        if len(pairs) and (pairs.min() < 0 or pairs.max() >= norb):
+            raise ValueError('pairs must index orbital shells 0..norb-1')
+        self.pairs = pairs
+        desc = np.ascontiguousarray(np.stack([offs[pairs[:, 0]], offs[pairs[:, 1]], nsph[pairs[:, 0]],
+                                              nsph[pairs[:, 1]]], 1), dtype=np.int32)
+        L = lib()
+        h = ctypes.c_void_p()
+        _check(L.cintgpu_df_create(ctypes.byref(h), _ptr(desc), len(pairs), self.nao, self.naux),
+               'cintgpu_df_create')
+        self._df = h
+        size = int(L.cintgpu_df_size(h))
+        self.T = torch.empty(max(size, 1), dtype=torch.float64, device='cuda')
+        # (ij|P) in chunks of whole pairs: chunk c's plan writes the segments of its pairs
+        seg = nsph[pairs[:, 0]] * nsph[pairs[:, 1]] * self.naux
+        start = np.concatenate([[0], np.cumsum(seg)])
+        naux_sh = mol.nbas - norb
+        per = max(1, chunk // max(naux_sh, 1))
+        bounds = [(a, min(a + per, len(pairs))) for a in range(0, len(pairs), per)]
+
+        def build(ab):
+            items3, _ = df_items(norb, mol.nbas, pairs[ab[0]:ab[1]])
+            return Plan(INT3C2E_SPH, mol, items3)
+        with ThreadPoolExecutor(min(6, max(1, len(bounds)))) as pool:
+            futs = [pool.submit(build, ab) for ab in bounds[:6]]
+            for c, (a, b) in enumerate(bounds):
+                p3 = futs[c].result()
+                if c + 6 < len(bounds):
+                    futs.append(pool.submit(build, bounds[c + 6]))
+                n = int(start[b] - start[a])
+                if p3.output_size != n:
+                    raise ValueError('int3c2e plan size %d != segments %d' % (p3.output_size, n))
+                p3.execute(self.T.narrow(0, int(start[a]), n))
+                torch.cuda.synchronize()
+                p3.close()
         # the metric over auxiliary pairs P >= Q, mirrored into a dense matrix
+        _, items2 = df_items(norb, mol.nbas, pairs[:0])
         p2 = Plan(INT2C2E_SPH, mol, items2)
         v = torch.empty(p2.output_size, dtype=torch.float64, device='cuda')
         p2.execute(v)
-        torch.cuda.synchronize()                          # both plans done before they are freed
-        p3.close()
+        torch.cuda.synchronize()
         p2.close()
         vi, _ = packed_index(items2, nsph, offs, self.naux)
         if len(vi) != v.numel() or (len(vi) and vi.max() >= self.naux * self.naux):
             raise ValueError('metric index map does not match the (P|Q) buffer')
-        self.V = mirror_metric(v, torch.as_tensor(vi, device=dev), self.naux)
+        self.V = mirror_metric(v, torch.as_tensor(vi, device=v.device), self.naux)
         self.L = torch.linalg.cholesky(self.V)
-        diag = np.zeros((self.nao, self.nao), dtype=bool)
-        for i in range(norb):
-            diag[loc[i]:loc[i + 1], loc[i]:loc[i + 1]] = True
-        self.diag = torch.as_tensor(diag, device=dev)
+
+    def _dev(self, x, shape, name):
+        import torch
+        if not (torch.is_tensor(x) and x.is_cuda and x.dtype == torch.float64 and tuple(x.shape) == shape):
+            raise ValueError('%s must be a CUDA float64 tensor of shape %s' % (name, shape))
+        return x.contiguous()
 
     def rho(self, dm):
-        """rho_Q = sum_cd (Q|cd) D_cd for the symmetric spherical density dm (torch, cuda)."""
-        return contract_rho(self.T, self.w, self.pair_idx, self.aux_idx, dm, self.naux)
+        """rho_Q = sum_cd (Q|cd) D_cd for the symmetric spherical density dm (CUDA tensor)."""
+        import ctypes
+
+        import torch
+        from . import _check, lib
+        dm = self._dev(dm, (self.nao, self.nao), 'dm')
+        r = torch.empty(self.naux, dtype=torch.float64, device=dm.device)
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _check(lib().cintgpu_df_rho(self._df, ctypes.c_void_p(self.T.data_ptr()),
+                                    ctypes.c_void_p(dm.data_ptr()), ctypes.c_void_p(r.data_ptr()), st),
+               'cintgpu_df_rho')
+        return r
 
     def coefficients(self, dm):
         import torch
@@ -189,13 +233,48 @@ class DFCoulomb:
         return torch.cholesky_solve(r[:, None], self.L)[:, 0]
 
     def vj(self, dm):
-        """Density-fitted J (spherical) for the symmetric density dm."""
-        return contract_j(self.T, self.pair_idx, self.aux_idx, self.coefficients(dm), self.nao,
-                          self.diag)
+        """Density-fitted J (spherical) for the symmetric density dm (CUDA tensor)."""
+        return self.vj_from_coefficients(self.coefficients(dm))
+
+    def vj_from_coefficients(self, c):
+        """J_ab = sum_P (ab|P) c_P for fitting coefficients c (CUDA tensor of naux)."""
+        import ctypes
+
+        import torch
+        from . import _check, lib
+        c = self._dev(c, (self.naux,), 'c')
+        J = torch.empty(self.nao, self.nao, dtype=torch.float64, device=c.device)
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _check(lib().cintgpu_df_j(self._df, ctypes.c_void_p(self.T.data_ptr()), ctypes.c_void_p(c.data_ptr()),
+                                  ctypes.c_void_p(J.data_ptr()), st), 'cintgpu_df_j')
+        return J
+
+    def index_maps(self):
+        """(pair_idx, aux_idx) device tensors of the packed buffer (per-element AO pair and
+        auxiliary function, df_index), built on first use: K and the dense formulation need
+        them, J does not."""
+        import torch
+        if getattr(self, '_maps', None) is None:
+            pi, ai = df_index(self.pairs, self._nsph, self._offs, self.nao, self.naux)
+            self._maps = (torch.as_tensor(pi, device=self.T.device), torch.as_tensor(ai, device=self.T.device))
+        return self._maps
 
     def vk(self, dm):
         """Density-fitted K (spherical) for the symmetric density dm; the whitened three-index
         tensor (naux * nao^2 doubles) is formed on first use and kept."""
         if getattr(self, 'Bt', None) is None:
-            self.Bt = dense_fitted(self.T, self.pair_idx, self.aux_idx, self.L, self.nao, self.naux)
+            pair_idx, aux_idx = self.index_maps()
+            self.Bt = dense_fitted(self.T, pair_idx, aux_idx, self.L, self.nao, self.naux)
         return contract_k(self.Bt, dm)
+
+    def close(self):
+        if getattr(self, '_df', None):
+            from . import lib
+            lib().cintgpu_df_destroy(self._df)
+            self._df = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -64,3 +64,65 @@ def test_df_k_matches_oracle_fit(gpulib, oracle):
     Kref = np.einsum('ijq,jl,klq->ik', W, dm, T3, optimize=True)
     assert np.abs(K - Kref).max() <= 1e-10 * np.abs(Kref).max()
     assert np.abs(K - K.T).max() <= 1e-12 * np.abs(Kref).max()
+
+
+def _high_l_df_system():
+    """two atoms; orbital shells s (2 primitives), p, d with two contracted functions, f
+    (2 primitives) and g on each atom, so AO-pair blocks reach 10 x 10 and 9 x 9 (above one warp's
+    32 lanes) as well as 1 x 1; auxiliary s, p, d, f, g with one primitive each"""
+    b = M._Builder()
+    atoms = [b.atom(1, (0.0, 0.0, 0.0)), b.atom(1, (0.3, -0.5, 1.4))]
+    for a in atoms:
+        b.shell(a, 0, [3.1, 0.7], [M.gto_norm(0, 3.1) * 0.4, M.gto_norm(0, 0.7) * 0.8])
+        b.shell(a, 1, [1.2], [M.gto_norm(1, 1.2)])
+        b.shell(a, 2, [2.0, 0.6], [[M.gto_norm(2, 2.0) * 0.7, M.gto_norm(2, 0.6) * 0.5],
+                                   [M.gto_norm(2, 2.0) * -0.3, M.gto_norm(2, 0.6) * 0.9]], nctr=2)
+        b.shell(a, 3, [1.5, 0.5], [M.gto_norm(3, 1.5) * 0.6, M.gto_norm(3, 0.5) * 0.6])
+        b.shell(a, 4, [0.9], [M.gto_norm(4, 0.9)])
+    norb = 10
+    for a in atoms:
+        for l, e in ((0, 1.7), (1, 1.1), (2, 0.9), (3, 0.8), (4, 0.7)):
+            b.shell(a, l, [e], [M.gto_norm(l, e)])
+    return b.mol('df high l'), norb
+
+
+@pytest.mark.parametrize('subset', [False, True])
+def test_df_kernels_match_dense_formulation(gpulib, oracle, subset):
+    """the DF kernels (cintgpu_df_rho / cintgpu_df_j) against the per-element torch formulation
+    (gathers and scatter-adds over the same packed buffer) on AO-pair blocks from 1 x 1 to
+    10 x 10 (both kernel paths), for all orbital pairs and for every other pair; with all pairs,
+    also rho and J against the oracle's dense fit"""
+    import torch
+    mol, norb = _high_l_df_system()
+    pairs = None
+    if subset:
+        ii, jj = np.tril_indices(norb)
+        pairs = np.stack([ii, jj], 1)[::2]
+    fit = df.DFCoulomb(mol, norb, pairs=pairs, chunk=7)      # several int3c2e chunks
+    n = fit.nao
+    d = np.random.RandomState(9).normal(0, 0.2, (n, n))
+    dm = torch.as_tensor(0.5 * (d + d.T), device='cuda')
+    pair_idx, aux_idx = fit.index_maps()
+    items3, _ = df.df_items(norb, mol.nbas, fit.pairs)
+    w = torch.as_tensor(df.fit_weights(items3, df._nsph(mol)), device='cuda')
+    rho = fit.rho(dm)
+    rho_ref = df.contract_rho(fit.T, w, pair_idx, aux_idx, dm, fit.naux)
+    assert torch.abs(rho - rho_ref).max().item() <= 1e-13 * torch.abs(rho_ref).max().item()
+    c = fit.coefficients(dm)
+    loc = np.concatenate([[0], np.cumsum(df._nsph(mol))])
+    diag = np.zeros((n, n), dtype=bool)
+    for i in range(norb):
+        diag[loc[i]:loc[i + 1], loc[i]:loc[i + 1]] = True
+    inpairs = np.zeros((n, n), dtype=bool)
+    for i, j in fit.pairs:
+        inpairs[loc[i]:loc[i + 1], loc[j]:loc[j + 1]] = inpairs[loc[j]:loc[j + 1], loc[i]:loc[i + 1]] = True
+    Jref = df.contract_j(fit.T, pair_idx, aux_idx, c, n, torch.as_tensor(diag, device='cuda'))
+    J = fit.vj(dm)
+    assert torch.abs(J - Jref).max().item() <= 1e-13 * torch.abs(Jref).max().item()
+    assert not J.cpu().numpy()[~inpairs].any()                 # blocks of absent pairs stay zero
+    assert torch.abs(J - J.T).max().item() <= 1e-14 * torch.abs(Jref).max().item()
+    if not subset:
+        _, _, rho_o, J_o = _dense_df(oracle, mol, norb, dm.cpu().numpy())
+        assert np.abs(rho.cpu().numpy() - rho_o).max() <= 1e-12 * np.abs(rho_o).max()
+        assert np.abs(J.cpu().numpy() - J_o).max() <= 1e-10 * np.abs(J_o).max()
+    fit.close()
