@@ -462,25 +462,30 @@ __device__ inline void cg_out_quartet(const CGOutTask &o, bool ne, bool peer_slo
             cur = cg_hrr(g0, eperm + ec.perm_off, eperm + ec.perm_off + ec.nE,
                          hprog + ec.hprog_off, o.l[0], o.l[1], o.l[2], o.l[3], o.AB, o.CD,
                          h1, h2, lane, ec.bra);
-        c2s_pass(cur, s1, o.l[1], sph, nfc[0] * nfc[2] * nfc[3], nfc[1], 1, lane);
-        __syncwarp();
+        /* a pass on an s or p shell (or any Cartesian one) maps every element to the same index,
+         * so it is skipped and the next pass reads its input where it is */
+        auto pass = [&](const double *src, int lsh, int inner, int nct, int outer) -> const double * {
+            if (!sph || lsh <= 1) return src;
+            double *d = src == s1 ? s2 : s1;
+            c2s_pass(src, d, lsh, sph, inner, nct, outer, lane);
+            __syncwarp();
+            return d;
+        };
+        cur = pass(cur, o.l[1], nfc[0] * nfc[2] * nfc[3], nfc[1], 1);
         /* pass l: (i,k | l | js) */
-        c2s_pass(s1, s2, o.l[3], sph, nfc[0] * nfc[2], nfc[3], nd[1], lane);
-        __syncwarp();
+        cur = pass(cur, o.l[3], nfc[0] * nfc[2], nfc[3], nd[1]);
         /* pass k: (i | k | ls, js) */
-        c2s_pass(s2, s1, o.l[2], sph, nfc[0], nfc[2], nd[3] * nd[1], lane);
-        __syncwarp();
+        cur = pass(cur, o.l[2], nfc[0], nfc[2], nd[3] * nd[1]);
         /* pass i: (1 | i | ks, ls, js) */
-        c2s_pass(s1, s2, o.l[0], sph, 1, nfc[0], nd[2] * nd[3] * nd[1], lane);
-        __syncwarp();
-        /* s2 layout: (is, ks, ls, js) */
+        cur = pass(cur, o.l[0], 1, nfc[0], nd[2] * nd[3] * nd[1]);
+        /* layout: (is, ks, ls, js) */
         int tot = nd[0] * nd[2] * nd[3] * nd[1];
         for (int e = lane; e < tot; e += 32) {
             int i = e % nd[0], r = e / nd[0];
             int k = r % nd[2]; r /= nd[2];
             int l = r % nd[3], j = r / nd[3];
             dst[(int64_t)i * o.st[0] + (int64_t)j * o.st[1] + (int64_t)k * o.st[2]
-                + (int64_t)l * o.st[3]] = s2[e];
+                + (int64_t)l * o.st[3]] = cur[e];
         }
         __syncwarp();
     }
