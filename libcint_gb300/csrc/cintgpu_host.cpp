@@ -2237,7 +2237,7 @@ namespace {
  * arena + output, pinned image + output), grown on demand and kept between calls. */
 #define CG_BATCH_SLOTS 4
 struct BatchCtx {
-    cudaStream_t s_exec[2] = {nullptr, nullptr}, s_copy = nullptr;
+    cudaStream_t s_exec[3] = {nullptr, nullptr, nullptr}, s_copy = nullptr;
     cudaEvent_t ev_h2d[CG_BATCH_SLOTS] = {}, ev_exec[CG_BATCH_SLOTS] = {}, ev_d2h[CG_BATCH_SLOTS] = {};
     char *arena[CG_BATCH_SLOTS] = {}, *dout[CG_BATCH_SLOTS] = {};
     char *pin_in[CG_BATCH_SLOTS] = {}, *pin_out[CG_BATCH_SLOTS] = {};
@@ -2255,7 +2255,7 @@ struct BatchCtx {
             if (ev_exec[s]) cudaEventDestroy(ev_exec[s]);
             if (ev_d2h[s]) cudaEventDestroy(ev_d2h[s]);
         }
-        for (int s = 0; s < 2; s++)
+        for (int s = 0; s < 3; s++)
             if (s_exec[s]) cudaStreamDestroy(s_exec[s]);
         if (s_copy) cudaStreamDestroy(s_copy);
     }
@@ -2264,6 +2264,7 @@ struct BatchCtx {
         if (s_copy) return 0;
         if (cudaStreamCreateWithFlags(&s_exec[0], cudaStreamNonBlocking) != cudaSuccess
             || cudaStreamCreateWithFlags(&s_exec[1], cudaStreamNonBlocking) != cudaSuccess
+            || cudaStreamCreateWithFlags(&s_exec[2], cudaStreamNonBlocking) != cudaSuccess
             || cudaStreamCreateWithFlags(&s_copy, cudaStreamNonBlocking) != cudaSuccess) {
             set_error("stream creation failed");
             return CINTGPU_ERR_CUDA;
@@ -2294,8 +2295,8 @@ int64_t item_block(int kind, const int *q, const int *bas)
 }  // namespace
 
 /* Host-buffer form over a packed output.  The item list is cut into chunks (512 items, growing
- * by a quarter per chunk up to 8192); chunk c uses slot c % CG_BATCH_SLOTS of a ring and
- * execution stream c % 2.
+ * by a quarter per chunk up to 12288); chunk c uses slot c % CG_BATCH_SLOTS of a ring and
+ * execution stream c % 3 (three streams overlap more of each chunk's launch tail than two).
  *   builder threads  build chunk plans and, once the slot's previous upload has completed, write
  *                    the plan's image into the slot's pinned buffer;
  *   the caller       uploads each image, executes the plan and queues the copy back, never
@@ -2327,11 +2328,11 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
         std::string err;
         bool image = false, h2d = false, d2h = false, scattered = false;
     };
-    /* chunk sizes 512, 640, 800, ... (x 1.25) up to 8192 items: the GPU starts after one small
+    /* chunk sizes 512, 640, 800, ... (x 1.25) up to 12288 items: the GPU starts after one small
      * plan, and each later chunk's plan (built by one thread) is ready before the GPU needs it */
     std::vector<Chunk> ch;
     int64_t total = 0;
-    int64_t first = 512, cap = 8192;
+    int64_t first = 512, cap = 12288;
     double growth = 1.25;
     if (const char *e = getenv("CINTGPU_CHUNK")) {   /* "first,growth,cap" (tuning) */
         long long f = 0, c = 0;
@@ -2444,7 +2445,7 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
     double t_image = 0, t_slot = 0, t_enqueue = 0;
     for (int c = 0; c < C; c++) {
         const int slot = c % R;
-        cudaStream_t st = X.s_exec[c & 1];
+        cudaStream_t st = X.s_exec[c % 3];
         CINTGPUPlan *P;
         {
             auto t0 = clk::now();
@@ -2500,6 +2501,7 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
     for (std::thread &t : pool) t.join();
     cudaStreamSynchronize(X.s_exec[0]);
     cudaStreamSynchronize(X.s_exec[1]);
+    cudaStreamSynchronize(X.s_exec[2]);
     cudaStreamSynchronize(X.s_copy);
     for (Chunk &x : ch) {
         delete x.P;

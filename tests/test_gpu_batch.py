@@ -1,5 +1,5 @@
 """The one-shot host-buffer entry cintgpu_batch_host, through the C-ABI.  Without offsets it cuts
-the item list into chunks (512 items, growing to 8192) planned on host threads while the GPU runs
+the item list into chunks (512 items, growing to 12288) planned on host threads while the GPU runs
 earlier chunks; its output must equal one device plan over the whole list (same layout:
 component-major, blocks back to back) to the tolerance of the other parity tests, and the oracle
 on a sample."""
