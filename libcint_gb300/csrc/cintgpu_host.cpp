@@ -2237,7 +2237,7 @@ namespace {
  * arena + output, pinned image + output), grown on demand and kept between calls. */
 #define CG_BATCH_SLOTS 4
 struct BatchCtx {
-    cudaStream_t s_exec[3] = {nullptr, nullptr, nullptr}, s_copy = nullptr;
+    cudaStream_t s_exec[CG_BATCH_SLOTS] = {}, s_copy = nullptr;   /* one per ring slot */
     cudaEvent_t ev_h2d[CG_BATCH_SLOTS] = {}, ev_exec[CG_BATCH_SLOTS] = {}, ev_d2h[CG_BATCH_SLOTS] = {};
     char *arena[CG_BATCH_SLOTS] = {}, *dout[CG_BATCH_SLOTS] = {};
     char *pin_in[CG_BATCH_SLOTS] = {}, *pin_out[CG_BATCH_SLOTS] = {};
@@ -2255,24 +2255,24 @@ struct BatchCtx {
             if (ev_exec[s]) cudaEventDestroy(ev_exec[s]);
             if (ev_d2h[s]) cudaEventDestroy(ev_d2h[s]);
         }
-        for (int s = 0; s < 3; s++)
+        for (int s = 0; s < CG_BATCH_SLOTS; s++)
             if (s_exec[s]) cudaStreamDestroy(s_exec[s]);
         if (s_copy) cudaStreamDestroy(s_copy);
     }
     int init()
     {
-        if (s_copy) return 0;
-        if (cudaStreamCreateWithFlags(&s_exec[0], cudaStreamNonBlocking) != cudaSuccess
-            || cudaStreamCreateWithFlags(&s_exec[1], cudaStreamNonBlocking) != cudaSuccess
-            || cudaStreamCreateWithFlags(&s_exec[2], cudaStreamNonBlocking) != cudaSuccess
-            || cudaStreamCreateWithFlags(&s_copy, cudaStreamNonBlocking) != cudaSuccess) {
+        if (s_copy && ev_d2h[CG_BATCH_SLOTS - 1]) return 0;   /* set up by an earlier call */
+        bool ok = s_copy || cudaStreamCreateWithFlags(&s_copy, cudaStreamNonBlocking) == cudaSuccess;
+        for (int s = 0; s < CG_BATCH_SLOTS && ok; s++)
+            ok = s_exec[s] || cudaStreamCreateWithFlags(&s_exec[s], cudaStreamNonBlocking) == cudaSuccess;
+        if (!ok) {
             set_error("stream creation failed");
             return CINTGPU_ERR_CUDA;
         }
         for (int s = 0; s < CG_BATCH_SLOTS; s++)
-            if (cudaEventCreateWithFlags(&ev_h2d[s], cudaEventDisableTiming) != cudaSuccess
-                || cudaEventCreateWithFlags(&ev_exec[s], cudaEventDisableTiming) != cudaSuccess
-                || cudaEventCreateWithFlags(&ev_d2h[s], cudaEventDisableTiming) != cudaSuccess) {
+            if ((!ev_h2d[s] && cudaEventCreateWithFlags(&ev_h2d[s], cudaEventDisableTiming) != cudaSuccess)
+                || (!ev_exec[s] && cudaEventCreateWithFlags(&ev_exec[s], cudaEventDisableTiming) != cudaSuccess)
+                || (!ev_d2h[s] && cudaEventCreateWithFlags(&ev_d2h[s], cudaEventDisableTiming) != cudaSuccess)) {
                 set_error("event creation failed");
                 return CINTGPU_ERR_CUDA;
             }
@@ -2295,8 +2295,8 @@ int64_t item_block(int kind, const int *q, const int *bas)
 }  // namespace
 
 /* Host-buffer form over a packed output.  The item list is cut into chunks (512 items, growing
- * by a quarter per chunk up to 12288); chunk c uses slot c % CG_BATCH_SLOTS of a ring and
- * execution stream c % 3 (three streams overlap more of each chunk's launch tail than two).
+ * by a quarter per chunk up to 12288); chunk c uses slot c % CG_BATCH_SLOTS of a ring and that
+ * slot's execution stream (four streams overlap more of the chunks' launch tails than two).
  *   builder threads  build chunk plans and, once the slot's previous upload has completed, write
  *                    the plan's image into the slot's pinned buffer;
  *   the caller       uploads each image, executes the plan and queues the copy back, never
@@ -2445,7 +2445,7 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
     double t_image = 0, t_slot = 0, t_enqueue = 0;
     for (int c = 0; c < C; c++) {
         const int slot = c % R;
-        cudaStream_t st = X.s_exec[c % 3];
+        cudaStream_t st = X.s_exec[slot];
         CINTGPUPlan *P;
         {
             auto t0 = clk::now();
@@ -2499,9 +2499,7 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
         t_enqueue += since(t0);
     }
     for (std::thread &t : pool) t.join();
-    cudaStreamSynchronize(X.s_exec[0]);
-    cudaStreamSynchronize(X.s_exec[1]);
-    cudaStreamSynchronize(X.s_exec[2]);
+    for (int s = 0; s < CG_BATCH_SLOTS; s++) cudaStreamSynchronize(X.s_exec[s]);
     cudaStreamSynchronize(X.s_copy);
     for (Chunk &x : ch) {
         delete x.P;
