@@ -835,7 +835,8 @@ def run_gpu(args, rank, world):
         wide, class_ms = autotune.tune_classes(cg.INT2E_SPH, mol, qs, *choice)
         tuning = {'choice': {'ws_kb': choice[0], 'separate_output': choice[1], 'wide_classes': list(wide)},
                   'candidate_ms': {'%d,%d' % c: round(t, 3) for c, t in times.items()},
-                  'class_ms_regular_wide': {str(k): [round(a, 3), round(b, 3)] for k, (a, b) in class_ms.items()}}
+                  'class_whole_list_ms_regular_wide': {str(k): [round(a, 3), round(b, 3)]
+                                                       for k, (a, b) in class_ms.items()}}
         plan = cg.Plan(cg.INT2E_SPH, mol, qs, ws_kb=choice[0], separate_output=choice[1],
                        wide_classes=wide)
     else:

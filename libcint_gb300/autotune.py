@@ -183,11 +183,13 @@ def tune(kind, mol, items, candidates=CANDIDATES, make_plan=None, timer=measure)
 def tune_classes(kind, mol, items, ws_kb=0, separate_output=0, min_share=0.02, max_classes=8,
                  make_plan=None, timer=measure, gain=0.98):
     """Per class carrying at least min_share of the list's work (largest first, at most
-    max_classes): time the class's own items in the regular group and in the 48 KB group; a class
-    is marked wide when that is faster by more than 1 - gain.  The whole list is then timed with
-    and without the marked set, which is kept only if the whole list is faster too (the groups
-    run side by side).  Returns (wide keys, {key: (ms regular, ms wide)}).  Lists of 2-shell items
-    are not tuned per class."""
+    max_classes): time the whole list with that class in the 48 KB group against the whole list
+    with none there (a class's items timed alone mostly measure the launch tail of a short
+    kernel, not the class's cost inside the full launch); a class is marked wide when the list
+    is faster by more than 1 - gain.  Several marked classes are kept together only if the list
+    is faster with all of them, else the single best one is kept.  Returns (wide keys,
+    {key: (ms with the class in the regular group, ms with it in the 48 KB group)}), both whole
+    list times.  Lists of 2-shell items are not tuned per class."""
     items = np.asarray(items)
     if items.ndim != 2 or items.shape[1] < 3 or len(items) == 0:
         return (), {}
@@ -202,22 +204,22 @@ def tune_classes(kind, mol, items, ws_kb=0, separate_output=0, min_share=0.02, m
     uk, inv = np.unique(keys, return_inverse=True)
     share = np.bincount(inv.ravel(), weights=w) / max(total, 1e-300)
     order = [int(uk[i]) for i in np.argsort(-share) if share[i] >= min_share][:max_classes]
-    times, wide = {}, []
 
-    def timed(lst, wset):
-        p = make_plan(lst, wset)
+    def timed(wset):
+        p = make_plan(items, wset)
         try:
             return timer(p)
         finally:
             p.close()
+    base = timed(())
+    times, wide = {}, []
     for k in order:
-        lst = items[keys == k]
-        t0, t1 = timed(lst, ()), timed(lst, (k,))
-        times[k] = (t0, t1)
-        if t1 < gain * t0:
+        t1 = timed((k,))
+        times[k] = (base, t1)
+        if t1 < gain * base:
             wide.append(k)
-    if wide and timed(items, tuple(wide)) >= gain * timed(items, ()):
-        wide = []
+    if len(wide) > 1 and timed(tuple(wide)) >= gain * base:
+        wide = [min(wide, key=lambda k: times[k][1])]
     return tuple(wide), times
 
 

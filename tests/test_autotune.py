@@ -134,9 +134,9 @@ def test_shared_memory_per_warp_reaches_the_planner():
 
 
 def test_tune_classes_marks_the_classes_the_wide_group_speeds_up():
-    """Per-class tuning with stand-in timings: a class goes to the 48 KB group when its own items
-    are faster there, and the set is dropped if the whole list is not faster with it; the choice
-    is cached with the launch parameters."""
+    """Per-class tuning with stand-in timings of the whole list: a class goes to the 48 KB group
+    when the list is faster with it there, not when it is slower; the choice is cached with the
+    launch parameters."""
     mol, qs = _c0()
     keys, w = at.kernel_classes(mol, qs)
     uk = np.unique(keys)
@@ -159,11 +159,20 @@ def test_tune_classes_marks_the_classes_the_wide_group_speeds_up():
     wide, times = at.tune_classes(cg.INT2E_SPH, mol, qs, make_plan=P, timer=timer)
     assert wide == (fast,) and times[fast][1] < times[fast][0]
     assert all(t1 > t0 for k, (t0, t1) in times.items() if k != fast)
-    # the whole list slower with the set: dropped
+    assert all(p.n == len(qs) for p in made)            # every timing is of the whole list
+    # no class helps: nothing marked
     wide, _ = at.tune_classes(cg.INT2E_SPH, mol, qs, make_plan=P,
-                              timer=lambda p: float(p.n) * (0.8 if p.n < len(qs) and fast in p.wide
-                                                           else (1.1 if p.wide else 1.0)))
+                              timer=lambda p: float(p.n) * (1.1 if p.wide else 1.0))
     assert wide == ()
+    # two classes help alone but not together: the better one is kept
+    second = int(uk[np.argsort([-w[keys == k].sum() for k in uk])[1]])
+
+    def timer2(p):
+        if len(p.wide) > 1:
+            return 2.0 * p.n
+        return float(p.n) * {fast: 0.8, second: 0.9}.get(p.wide[0] if p.wide else None, 1.0)
+    wide, _ = at.tune_classes(cg.INT2E_SPH, mol, qs, make_plan=P, timer=timer2, min_share=0.0)
+    assert wide == (fast,)
     dev = 'GB300 test|cuda 13.0'
     path = None
 
