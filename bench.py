@@ -793,7 +793,9 @@ def run_extras(cg, mol, qs, value, args):
                      ('adjoint', lambda: extra_adjoint(cg)),
                      ('jk', lambda: extra_jk(cg)),
                      ('screening', lambda: extra_screening(cg)),
-                     ('df', lambda: extra_df(cg))):
+                     ('df', lambda: extra_df(cg)),
+                     ('c2', lambda: extra_c2(cg)),
+                     ('dfc2', lambda: extra_dfc2(cg))):
         try:
             out[name] = fn()
         except Exception as e:  # an extra must not hide the headline line
@@ -961,7 +963,8 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-tune', dest='tune', action='store_false',
                     help='default launch parameters instead of the autotuner\'s choice')
-    ap.add_argument('--no-extras', action='store_true', help='skip the side workloads (drop-in, int3c2e, adjoint, J/K, screening, DF)')
+    ap.add_argument('--no-extras', action='store_true', help='skip the side workloads (drop-in, int3c2e, adjoint, J/K, screening, DF, '
+                                                             'c2 at full size)')
     ap.add_argument('--only', default='headline', choices=['headline', 'adjoint', 'int3c2e', 'jk', 'df', 'screening',
                                                           'fp64peak', 'screened', 'c4', 'c2', 'dropin', 'dfc2'],
                     help='run one side workload alone and print its line (profiling)')
