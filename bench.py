@@ -291,11 +291,17 @@ def extra_int3c2e(cg, seed=0, npairs=40):
                                'integrals_per_s': nint2 / dt2}}
 
 
+def planning_threads():
+    """host threads that plan chunks ahead of the GPU: all cores but two, at most 12 (each holds
+    one chunk plan, ~1 GB of host memory at 4M triples)"""
+    return max(1, min(12, (os.cpu_count() or 8) - 2))
+
+
 def extra_c2(cg, seed=0, thr=1e-12, chunk=4_000_000):
     """c2 at full size: the whole Schwarz-screened (ij|P) tensor (Q_ij Q_P >= 1e-12 over every
     orbital shell pair i >= j and every auxiliary shell), evaluated in streamed chunks of about
-    4M triples (planned on six host threads ahead of the GPU, each run into one reused device
-    buffer; nothing is kept).  Reports the triple and integral counts, the bounds' time, the
+    4M triples (planned on host threads ahead of the GPU, each run into one reused device buffer;
+    nothing is kept).  Reports the triple and integral counts, the bounds' time, the
     planning (summed over threads), device and wall times, and integrals/s on the device and
     overall."""
     import torch
@@ -356,12 +362,13 @@ def extra_c2(cg, seed=0, thr=1e-12, chunk=4_000_000):
     nint_total, buf, plan_s, dev_s = 0, None, 0.0, 0.0
     torch.cuda.synchronize()
     t_all = time.perf_counter()
-    with ThreadPoolExecutor(6) as pool:
-        futs = [pool.submit(build, ab) for ab in bounds[:6]]
+    nth = planning_threads()
+    with ThreadPoolExecutor(nth) as pool:
+        futs = [pool.submit(build, ab) for ab in bounds[:nth]]
         for i in range(len(bounds)):
             p, ps, ni = futs[i].result()
-            if i + 6 < len(bounds):
-                futs.append(pool.submit(build, bounds[i + 6]))
+            if i + nth < len(bounds):
+                futs.append(pool.submit(build, bounds[i + nth]))
             plan_s += ps
             nint_total += ni
             if buf is None or buf.numel() < p.output_size:

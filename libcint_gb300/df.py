@@ -19,6 +19,8 @@ The per-element formulation (packed_index, fit_weights, contract_rho, contract_j
 scatter-adds in torch) states the same contractions densely; the CPU tests check it against
 einsums over the oracle's full tensor and the GPU tests check the kernels against it.
 """
+import os
+
 import numpy as np
 
 from .molecules import shell_nsph as _nsph
@@ -182,12 +184,13 @@ class DFCoulomb:
         def build(ab):
             items3, _ = df_items(norb, mol.nbas, pairs[ab[0]:ab[1]])
             return Plan(INT3C2E_SPH, mol, items3)
-        with ThreadPoolExecutor(min(6, max(1, len(bounds)))) as pool:
-            futs = [pool.submit(build, ab) for ab in bounds[:6]]
+        nth = max(1, min(12, (os.cpu_count() or 8) - 2, len(bounds)))   # ~1 GB of host memory per chunk plan
+        with ThreadPoolExecutor(nth) as pool:
+            futs = [pool.submit(build, ab) for ab in bounds[:nth]]
             for c, (a, b) in enumerate(bounds):
                 p3 = futs[c].result()
-                if c + 6 < len(bounds):
-                    futs.append(pool.submit(build, bounds[c + 6]))
+                if c + nth < len(bounds):
+                    futs.append(pool.submit(build, bounds[c + nth]))
                 n = int(start[b] - start[a])
                 if p3.output_size != n:
                     raise ValueError('int3c2e plan size %d != segments %d' % (p3.output_size, n))
