@@ -335,8 +335,11 @@ struct CINTGPUPlan {
     int prim_l = 4;                /* int2e classes with ll >= prim_l (or lj >= prim_l when the
                                       bra route does not take them) transfer per primitive
                                       (CINTGPU_PER_PRIMITIVE_L overrides, 0 = every class) */
-    int bra_l = 2;                 /* classes with lj >= bra_l and ll < prim_l transfer the bra per
-                                      term (CINTGPU_BRA_TERM_L overrides, e.g. 99 = never) */
+    int bra_l = 2;                 /* classes with lj >= bra_l, li + lj >= bra_lsum and ll < prim_l
+                                      transfer the bra per term (CINTGPU_BRA_TERM_L overrides, e.g.
+                                      99 = never) */
+    int bra_lsum = 5;              /* (dd| stays contraction first: measured within 1e-11 of the
+                                      long-double referee on c1, where (fd| reaches 2e-10 */
     int hrr_max = 1;               /* doubles of one transfer buffer, largest class */
     int nef_max = 1;               /* (e0|f0) accumulators, largest class */
     std::vector<int> out_item;     /* item index of each CGOutTask */
@@ -971,11 +974,15 @@ static void free_plan_device(CINTGPUPlan *p)
  * (libcint: 1.1e-10 and 7e-15); with lj or ll >= 4 it even leaves the 1e-12 absolute bar
  * ((ih|ih): 1.2e-12).  So:
  *   ll >= prim_l (default 4)          both transfers per primitive (CG_MODE_ERIP);
- *   lj >= bra_l (default 2), ll < prim_l   the bra transfer per term, the ket transfer (ll <= 3:
+ *   lj >= bra_l (default 2), li + lj >= bra_lsum (default 5), ll < prim_l
+ *                                     the bra transfer per term, the ket transfer (ll <= 3:
  *                                     (ff|ff) keeps 8.8e-12 relative on uncancelled Cartesian
  *                                     elements, 5% faster than per primitive) after contraction
  *                                     (CG_MODE_ERIB);
- *   otherwise                         both transfers after contraction (contraction first).
+ *   otherwise                         both transfers after contraction (contraction first):
+ *                                     (dd| included, which stays within 1e-11 relative of the
+ *                                     long-double evaluation on 100 c1 quartets per class where
+ *                                     (fd| and (gd| reach 2e-10 and 4.5e-10 that way.
  * A class whose per-term arrays do not fit the largest per-warp shared memory falls back to the
  * next route that fits ((ii|ii)-type classes: contraction first). */
 static bool erip_fits(const int *l)
@@ -986,7 +993,8 @@ static bool erip_fits(const int *l)
 }
 static bool bra_term(const CINTGPUPlan *P, const int *l)
 {
-    if (P->mode != CG_MODE_ERI || l[1] < P->bra_l || l[3] >= P->prim_l) return false;
+    if (P->mode != CG_MODE_ERI || l[1] < P->bra_l || l[0] + l[1] < P->bra_lsum || l[3] >= P->prim_l)
+        return false;
     /* stage-3 rounds address groups with 16 bits */
     if (ncart_l(l[0]) * ncart_l(l[1]) * ncart_l(l[2] + l[3]) >= 65536) return false;
     CGLayout L;

@@ -1,7 +1,8 @@
 """Task routing of the planner, CPU only (host planning, no device): int2e classes whose horizontal
 transfer after contraction would lose precision go elsewhere: kernel-order ll >= 4 to the
-per-primitive group when its g arrays fit, lj >= 2 with ll <= 3 to the bra-per-term tables of the
-regular groups; CINTGPU_PER_PRIMITIVE_L and CINTGPU_BRA_TERM_L move the thresholds; plans
+per-primitive group when its g arrays fit, lj >= 2 with li + lj >= 5 and ll <= 3 to the
+bra-per-term tables of the regular groups ((dd| stays contraction first); CINTGPU_PER_PRIMITIVE_L
+and CINTGPU_BRA_TERM_L move the thresholds; plans
 transform their outputs inside the integral kernel."""
 import ctypes
 import os
