@@ -41,9 +41,9 @@ sys.path.insert(0, ROOT)
 
 FP64_PEAK_TFLOPS = 1.257      # measured DFMA peak of this GB300 pool (bench.py --only fp64peak;
                               # = 2 DFMA per SM per clock x 152 SMs x 2.07 GHz)
-# DRAM read + write of one integral-kernel launch per c1 quartet: 552.6 MB for the step's 100k
-# quartets (one ncu capture of that launch)
-ERI_DRAM_BYTES_PER_QUARTET = 552.6e6 / 100000
+# DRAM read + write of one integral-kernel launch per c1 quartet: 545.8 MB + 1115.7 MB for the
+# step's 100k quartets (one ncu capture of that launch)
+ERI_DRAM_BYTES_PER_QUARTET = (545.8e6 + 1115.7e6) / 100000
 SCHWARZ = 1e-12
 # one metric string for both arms, so the two lines are directly comparable
 METRIC = 'int2e_sph integrals/s (c1 Schwarz-screened quartets)'

@@ -340,6 +340,7 @@ struct CINTGPUPlan {
                                       99 = never) */
     int bra_lsum = 5;              /* (dd| stays contraction first: measured within 1e-11 of the
                                       long-double referee on c1, where (fd| reaches 2e-10 */
+    bool own_slots = false;        /* some tasks accumulate in per-warp slots (CGTask::own_slot) */
     int hrr_max = 1;               /* doubles of one transfer buffer, largest class */
     int nef_max = 1;               /* (e0|f0) accumulators, largest class */
     std::vector<int> out_item;     /* item index of each CGOutTask */
@@ -366,6 +367,7 @@ struct CINTGPUPlan {
     int *d_empty = nullptr;
     int *d_done = nullptr;         /* finished slices per output quartet (fused output) */
     double *d_oscr = nullptr;      /* per-warp transform scratch of the integral kernel */
+    double *d_wslot = nullptr;     /* per-warp slots of own-slot tasks */
     double *cur_out = nullptr;
     double *d_gctr = nullptr;
     int *d_counters = nullptr;     /* [0], [1], [3]: task counters of groups 0, 1, 2; [2]: status */
@@ -1038,6 +1040,8 @@ static bool kind_sph(int kind)
         || kind == CINTGPU_INT3C2E_IP1_SPH || kind == CINTGPU_INT3C2E_IP2_SPH;
 }
 
+static bool fused(const CINTGPUPlan *P);
+
 static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, const int64_t *offsets,
                       const int *atm, int natm, const int *bas, int nbas, const double *env,
                       int64_t split_target, OptState *opt = nullptr)
@@ -1460,25 +1464,30 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             int64_t pos[4] = {gbeg[0], gbeg[1], gbeg[2], gbeg[3]};
             for (int64_t i = 0; i < w.n; i++) beg[pos[grp(tmp[i])]++] = tmp[i];
         }
+        /* a quartet of one slice in a plan that transforms in the integral kernel accumulates
+         * in the running warp's own slot (reused, so it stays in L2), not in one of its own */
+        const bool own = P->fuse_out && P->mode == CG_MODE_ERI && !P->jmode && !P->gradj
+                      && group != 2 && w.n <= slice;
         for (int g = 0; g < 4; g++)
         for (int64_t a0 = gbeg[g]; a0 < gbeg[g + 1]; a0 += slice) {
             TaskCost x;
             x.t.pij = pe.pij; x.t.pkl = pe.pkl;
             x.t.pq_off = (int)(w.off + a0);
             x.t.npq = (int)std::min<int64_t>(slice, gbeg[g + 1] - a0);
-            x.t.cart_off = gpos;
+            x.t.cart_off = own ? 0 : gpos;
             x.t.out = pe.out;
             x.t.sym = pe.sym;
             if (group == 2 || CG_IS_IP(P->mode))   /* per-primitive recurrences: base choice */
                 x.t.sym |= (pair_swap(pe.pij) ? 8 : 0) | (pair_swap(pe.pkl) ? 16 : 0);
             if (P->gradj) x.t.sym |= g << 3;
             x.t.cls = cls;
-            x.t.pad = 0;
+            x.t.own_slot = own ? 1 : 0;
             x.cost = x.t.npq * w.cost_pq;
             x.group = group;
             tc.push_back(x);
             o.nparts++;
-            gpos += slot;
+            if (own) P->own_slots = true;
+            else gpos += slot;
         }
     }
     /* longest tasks first within each launch (LPT order for the dynamic work counter); a stable
@@ -1503,6 +1512,23 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
         P->groups[g].nblocks = std::min(std::max(1, g_ctx.sm_count) * P->groups[g].blocks_per_sm,
                                         std::max(1, (P->groups[g].ntasks + 3) / 4));
     }
+    /* own slots need the fused transform and one slot of the largest class per warp; where
+     * either is missing (or the slots would pass 256 MB), those tasks get slots of their own */
+    if (P->own_slots) {
+        const int64_t warps = 4 * (int64_t)(P->groups[0].nblocks + P->groups[1].nblocks + P->groups[2].nblocks);
+        if (!fused(P) || (double)warps * P->nef_max * 8.0 > 256.0 * (1 << 20)) {
+            for (CGTask &t : P->tasks)
+                if (t.own_slot) {
+                    /* the quartet's only slice: its output reads the same slot */
+                    const CGEriClass &ec = P->eclass[t.cls];
+                    t.own_slot = 0;
+                    t.cart_off = gpos;
+                    P->outs[t.out].cart_off = gpos;
+                    gpos += (int64_t)ec.nE * ec.nF;
+                }
+            P->own_slots = false;
+        }
+    }
     P->gctr_size = std::max<int64_t>(gpos, 1);
     P->empty_outs.clear();
     for (size_t q = 0; q < P->outs.size(); q++)
@@ -1512,7 +1538,7 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
 
 struct DevLayout {
     size_t pairs, prims, tasks, outs, pq, gcl, gch, gen, ecl, egr, epm, hpg, erd, emp, gctr, cnt, ne, scr, wscr;
-    size_t done, oscr;
+    size_t done, oscr, wslot;
     int oscr_warps;
     int64_t wstride;
     int wwarps;
@@ -1559,6 +1585,8 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     D.done = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
     D.oscr_warps = fo ? 4 * (P->groups[0].nblocks + P->groups[1].nblocks + P->groups[2].nblocks) : 0;
     D.oscr = fo ? al(sizeof(double) * (size_t)D.oscr_warps * D.spw) : 0;
+    D.wslot = P->own_slots ? al(sizeof(double) * (size_t)(4 * (P->groups[0].nblocks + P->groups[1].nblocks
+                                                              + P->groups[2].nblocks)) * P->nef_max) : 0;
     D.gctr = al(sizeof(double) * P->gctr_size);
     D.cnt = al(sizeof(int) * 4);
     D.ne = al(sizeof(int) * std::max<size_t>(P->outs.size(), 1));
@@ -1575,7 +1603,7 @@ static DevLayout dev_layout(const CINTGPUPlan *P)
     }
     if (P->jmode || grad) D.gctr = al(sizeof(double));   /* no per-task accumulators */
     D.upload = D.pairs + D.prims + D.tasks + D.outs + D.pq + D.gcl + D.gch + D.gen + D.ecl + D.egr + D.epm + D.hpg + D.erd + D.emp;
-    D.total = D.upload + D.gctr + D.cnt + D.ne + D.scr + D.wscr + D.done + D.oscr;
+    D.total = D.upload + D.gctr + D.cnt + D.ne + D.scr + D.wscr + D.done + D.oscr + D.wslot;
     return D;
 }
 
@@ -1608,6 +1636,7 @@ static void carve_plan(CINTGPUPlan *P, const DevLayout &D, char *p)
     P->d_wscratch = (double *)p; p += D.wscr;
     P->d_done = (int *)p; p += D.done;
     P->d_oscr = D.oscr ? (double *)p : nullptr; p += D.oscr;
+    P->d_wslot = D.wslot ? (double *)p : nullptr; p += D.wslot;
     P->wscratch_stride = D.wstride;
     P->wscratch_warps = D.wwarps;
 }
@@ -1745,6 +1774,11 @@ static int launch_group(CINTGPUPlan *P, int g, cudaStream_t stream)
     if (L.oscr && g >= 1)
         L.oscr += (size_t)4 * (P->groups[0].nblocks + (g == 2 ? P->groups[1].nblocks : 0)) * P->scratch_per_warp;
     L.oscr_stride = P->scratch_per_warp;
+    /* own slots: per warp of this launch, after those of the groups launched beside it */
+    L.wslot = P->d_wslot;
+    L.wslot_stride = P->nef_max;
+    if (L.wslot && g >= 1)
+        L.wslot += (size_t)4 * (P->groups[0].nblocks + (g == 2 ? P->groups[1].nblocks : 0)) * P->nef_max;
     L.nf_max = P->max_nf;
     L.out = P->cur_out;
     L.ncomp = P->ncomp;

@@ -51,7 +51,8 @@ typedef struct {
                             per-primitive kernels: bit3 (bit4) runs the bra (ket) recurrences
                             about the pair's second centre (see g_axis) */
     int cls;             /* class tables: CGGradClass (adjoint) or CGEriClass (int2e, int3c2e, J) */
-    int pad;
+    int own_slot;        /* 1: the quartet's only slice accumulates in the running warp's slot
+                            (CGLaunch::wslot), not at cart_off, and that warp transforms it */
 } CGTask;
 
 /* Adjoint iteration tables, one set per angular-momentum class, built on the host.

@@ -409,7 +409,7 @@ __device__ inline void cg_out_quartet(const CGOutTask &o, bool ne, bool peer_slo
                                       const CGEriClass *__restrict__ eclass,
                                       const int *__restrict__ eperm, const int *__restrict__ hprog,
                                       double *out, int ncomp, int64_t comp_stride, double *s1,
-                                      int64_t nf_max, int64_t spw, int lane)
+                                      int64_t nf_max, int64_t spw, int lane, double *own = nullptr)
 {
     double *s2 = s1 + nf_max;
     double *h1 = s2 + nf_max;
@@ -427,7 +427,8 @@ __device__ inline void cg_out_quartet(const CGOutTask &o, bool ne, bool peer_slo
     if (e0f0) ec = eclass[o.ecls];
     const int slot = e0f0 ? ec.nE * ec.nF : nf;   /* accumulators per part and component */
     for (int comp = 0; comp < ncomp; comp++) {
-        double *g0 = gctr + o.cart_off + (size_t)comp * slot;
+        /* own: the quartet's single slice sits in this warp's own slot */
+        double *g0 = (own ? own : gctr + o.cart_off) + (size_t)comp * slot;
         if (ne && o.nparts > 1) {
             for (int c = lane; c < slot; c += 32) {
                 double v = peer_slots ? __ldcg(g0 + c) : g0[c];
@@ -452,7 +453,7 @@ __device__ inline void cg_out_quartet(const CGOutTask &o, bool ne, bool peer_slo
             continue;
         }
         /* a single slice written by another warp: read it past L1 through the transfer's gather */
-        if (peer_slots && o.nparts == 1) {
+        if (peer_slots && o.nparts == 1 && !own) {
             for (int c = lane; c < slot; c += 32) g0[c] = __ldcg(g0 + c);
             __syncwarp();
         }
@@ -553,7 +554,9 @@ __device__ __forceinline__ void run_task_e0f0(const CGLaunch &P, const CGTask &t
     const int nF = ec.nF, nEF = ec.nE * ec.nF;
     double *wbase = P.jmode ? P.wscratch + (size_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * P.wscratch_stride
                             : nullptr;
-    double *acc = P.jmode ? wbase : P.gctr + tk.cart_off;
+    double *acc = P.jmode ? wbase
+                : tk.own_slot ? P.wslot + (size_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * P.wslot_stride
+                              : P.gctr + tk.cart_off;
     const int MA = ec.maxab & 0xff, MB = ec.maxab >> 8;
     const bool boxed = MA <= 4 && MB <= 4;
     const int mab = (MA - 1) + 4 * (MB - 1);
@@ -719,7 +722,8 @@ __device__ __forceinline__ void rys_eri_body(const CGLaunch &P)
                 const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
                 cg_out_quartet(P.outs[tk.out], true, true, P.gctr, P.eclass, P.eperm, P.hprog, P.out,
                                P.ncomp, P.comp_stride, P.oscr + (size_t)gw * P.oscr_stride, P.nf_max,
-                               P.oscr_stride, lane);
+                               P.oscr_stride, lane,
+                               tk.own_slot ? P.wslot + (size_t)gw * P.wslot_stride : nullptr);
             }
         }
     }

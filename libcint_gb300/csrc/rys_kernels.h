@@ -82,6 +82,8 @@ typedef struct {
     int *done;                /* finished slices per output quartet */
     double *oscr;             /* per-warp transform scratch */
     int64_t oscr_stride, nf_max;
+    double *wslot;            /* per-warp accumulator slot of own-slot tasks (CGTask::own_slot) */
+    int64_t wslot_stride;
     double *out;
     int ncomp;
     int64_t comp_stride;
