@@ -1490,21 +1490,32 @@ static int build_plan(CINTGPUPlan *P, int kind, const int *shls, int64_t n, cons
             else gpos += slot;
         }
     }
-    /* longest tasks first within each launch (LPT order for the dynamic work counter); a stable
-     * sort of indices, so equal costs keep their creation order */
-    struct Key { double cost; int64_t idx; int group; };
-    std::vector<Key> ord(tc.size());
-    for (size_t i = 0; i < ord.size(); i++) ord[i] = {tc[i].cost, (int64_t)i, tc[i].group};
-    std::stable_sort(ord.begin(), ord.end(), [](const Key &x, const Key &y) {
-        if (x.group != y.group) return x.group < y.group;
-        return x.cost > y.cost;
-    });
-    P->tasks.reserve(tc.size());
+    /* longest tasks first within each launch (LPT order for the dynamic work counter): a stable
+     * counting sort on the cost's logarithm (256 buckets per factor of two, so costs within 0.3 %
+     * share a bucket and keep their creation order), group by group */
+    constexpr int NB = 1 << 14;
+    double cmax = 0.0;
+    for (const TaskCost &x : tc) cmax = std::max(cmax, x.cost);
+    std::vector<int> bkt(tc.size());
+    std::vector<int64_t> cnt(3 * (size_t)NB + 1, 0);
+    for (size_t i = 0; i < tc.size(); i++) {
+        const double c = tc[i].cost;
+        int b = NB - 1;
+        if (c > 0 && cmax > 0) b = std::min(NB - 1, std::max(0, (int)(std::log2(cmax / c) * 256.0)));
+        bkt[i] = tc[i].group * NB + b;
+        cnt[bkt[i] + 1]++;
+    }
+    for (size_t k = 1; k < cnt.size(); k++) cnt[k] += cnt[k - 1];
+    const size_t tbase = P->tasks.size();
+    P->tasks.resize(tbase + tc.size());
+    for (size_t i = 0; i < tc.size(); i++) P->tasks[tbase + cnt[bkt[i]]++] = tc[i].t;
+    int64_t gstart = (int64_t)tbase;
     for (int g = 0; g < 3; g++) {
-        P->groups[g].task0 = (int)P->tasks.size();
-        for (const Key &k : ord)
-            if (k.group == g) P->tasks.push_back(tc[k.idx].t);
-        P->groups[g].ntasks = (int)P->tasks.size() - P->groups[g].task0;
+        int64_t ng = 0;
+        for (const TaskCost &x : tc) ng += x.group == g;
+        P->groups[g].task0 = (int)gstart;
+        gstart += ng;
+        P->groups[g].ntasks = (int)ng;
         P->groups[g].ws = g == 0 ? ws_small : CG_WS_MAX;
         P->groups[g].blocks_per_sm = (P->mode == CG_MODE_GRAD || P->mode == CG_MODE_GRADA)
                                          ? cg_grad_blocks_per_sm(grad_kernel_mode(P), P->groups[g].ws)
