@@ -301,6 +301,13 @@ int cintgpu_screened_run(int kind, const int *pairs, const double *q, int64_t np
                          double *vj_dev, double *vk_dev, double *grad_dev, double *galpha_dev,
                          int64_t *nquartets);
 
+/* the same pipeline with the blocks written straight into a device buffer (one-component kinds:
+ * int2e, int3c2e, int2c2e; out_dev holds the blocks back to back, sum of their sizes); chunk plans
+ * are built on host threads ahead of the GPU and run from a ring of reused device slots, so a long
+ * list costs no allocation per chunk.  Synchronous: returns when every chunk has run. */
+int cintgpu_batch_device(int kind, double *out_dev, const int *shls, int64_t n, const int *atm,
+                         int natm, const int *bas, int nbas, const double *env);
+
 /* one-shot host-buffer form: plan, H2D, execute, D2H into out_host (output_size*ncomp doubles) */
 int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,
                        const int64_t *offsets, const int *atm, int natm, const int *bas,

@@ -92,6 +92,8 @@ def lib():
     L.cintgpu_plan_destroy.restype = None
     L.cintgpu_batch_host.argtypes = [i32, vp, vp, i64, vp, vp, i32, vp, i32, vp]
     L.cintgpu_batch_host.restype = i32
+    L.cintgpu_batch_device.argtypes = [i32, vp, vp, i64, vp, i32, vp, i32, vp]
+    L.cintgpu_batch_device.restype = i32
     L.cintgpu_rys_roots_dev.argtypes = [i32, vp, i32, vp, vp, vp]
     L.cintgpu_rys_roots_dev.restype = i32
     L.cintgpu_rys_nmax.restype = i32
@@ -232,6 +234,16 @@ def batch_host(kind, mol, shls, offsets=None):
                                   _ptr(mol.atm), mol.natm, _ptr(mol.bas), mol.nbas, _ptr(mol.env))
     _check(rc, 'cintgpu_batch_host')
     return out.reshape(ncomp, size)
+
+
+def batch_device(kind, mol, shls, out):
+    """cintgpu_batch_device: the blocks of one-component kinds straight into the CUDA float64
+    tensor out (back to back, libcint's layout per block), chunks planned on host threads while
+    the GPU runs earlier ones; returns when done."""
+    shls = np.ascontiguousarray(shls, dtype=np.int32).reshape(-1, _KIND_NSH[kind])
+    _check(lib().cintgpu_batch_device(kind, ctypes.c_void_p(out.data_ptr()), _ptr(shls), shls.shape[0],
+                                      _ptr(mol.atm), mol.natm, _ptr(mol.bas), mol.nbas, _ptr(mol.env)),
+           'cintgpu_batch_device')
 
 
 def dropin(name, mol, shls, dims=None, nbas=None):

@@ -2359,8 +2359,9 @@ int64_t item_block(int kind, const int *q, const int *bas)
  * overlaps the next chunk on the other stream. */
 static int batch_host_pipelined(int kind, double *out_host, const int *shls, int64_t n,
                                 const int *atm, int natm, const int *bas, int nbas,
-                                const double *env)
+                                const double *env, double *out_dev = nullptr)
 {
+    /* out_dev: the blocks go straight into this device buffer (one component), no copy back */
     BatchCtx &X = tl_batch;
     int rc = X.init();
     if (rc) return rc;
@@ -2385,7 +2386,9 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
      * plan, and each later chunk's plan (built by one thread) is ready before the GPU needs it */
     std::vector<Chunk> ch;
     int64_t total = 0;
-    int64_t first = 512, cap = 12288;
+    /* two- and three-centre items are one to two orders of magnitude cheaper than quartets:
+     * their chunks may grow 20x larger before one chunk's plan outlasts the GPU's share */
+    int64_t first = 512, cap = kind_shells(kind) == 4 ? 12288 : 262144;
     double growth = 1.25;
     if (const char *e = getenv("CINTGPU_CHUNK")) {   /* "first,growth,cap" (tuning) */
         long long f = 0, c = 0;
@@ -2427,9 +2430,10 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
             if (c >= C) return;
             auto tb = clk::now();
             CINTGPUPlan *P = new CINTGPUPlan();
-            /* chunks are small: a separate output kernel on the chunk's stream beats transforms
-             * at the integral kernel's tail */
-            P->fuse_out = false;
+            /* host-buffer int2e chunks are small: a separate output kernel on the chunk's stream
+             * beats transforms at the integral kernel's tail; two- and three-centre chunks written
+             * to device memory transform inside the integral kernel */
+            P->fuse_out = out_dev && kind_shells(kind) < 4;
             int r = build_plan(P, kind, shls + nsh * ch[c].i0, ch[c].n, nullptr, atm, natm, bas, nbas, env, 0);
             us_build += (int64_t)(1e3 * since(tb));
             if (r) { fail(c, r, cintgpu_last_error()); delete P; return; }
@@ -2488,7 +2492,7 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
         }
     };
     const int nbuild = std::max(1, std::min<int>(C, std::min<int>(14, (int)std::thread::hardware_concurrency())));
-    const int nscatter = std::min(C, 2);
+    const int nscatter = out_dev ? 0 : std::min(C, 2);
     std::vector<std::thread> pool;
     for (int t = 0; t < nbuild; t++) pool.emplace_back(builder);
     for (int t = 0; t < nscatter; t++) pool.emplace_back(scatter);
@@ -2507,8 +2511,9 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
             t_image += since(t0);
             if (abort) break;
             t0 = clk::now();
-            /* slot reuse: chunk c - R copied back and scattered (so its kernels are done too) */
-            if (c >= R) cv.wait(lk, [&] { return abort || ch[c - R].scattered; });
+            /* slot reuse: chunk c - R copied back and scattered (so its kernels are done too); with
+             * device output the slot's stream orders the reuse after that chunk's kernels */
+            if (c >= R && !out_dev) cv.wait(lk, [&] { return abort || ch[c - R].scattered; });
             t_slot += since(t0);
             if (abort) break;
             P = ch[c].P;
@@ -2518,9 +2523,15 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
         const DevLayout &D = ch[c].D;
         const size_t outb = sizeof(double) * std::max<int64_t>(P->out_size * P->ncomp, 1);
         int r;
+        /* device output: the slot's previous chunk may still run from its arena; a growing
+         * arena waits for it first */
+        if (out_dev && D.total > X.arena_cap[slot] && cudaStreamSynchronize(st) != cudaSuccess) {
+            fail(c, CINTGPU_ERR_CUDA, "chunk stream failed");
+            break;
+        }
         if ((r = grow_dev(&X.arena[slot], &X.arena_cap[slot], D.total))
-            || (r = grow_dev(&X.dout[slot], &X.dout_cap[slot], outb))
-            || (r = grow_host(&X.pin_out[slot], &X.pin_out_cap[slot], outb))) {
+            || (!out_dev && (r = grow_dev(&X.dout[slot], &X.dout_cap[slot], outb)))
+            || (!out_dev && (r = grow_host(&X.pin_out[slot], &X.pin_out_cap[slot], outb)))) {
             fail(c, r, cintgpu_last_error());
             break;
         }
@@ -2533,11 +2544,13 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
             ch[c].h2d = true;
             cv.notify_all();
         }
-        if (ok && (r = execute_plan(P, (double *)X.dout[slot], st))) { fail(c, r, cintgpu_last_error()); break; }
-        ok = ok && cudaEventRecord(X.ev_exec[slot], st) == cudaSuccess
-             && cudaStreamWaitEvent(X.s_copy, X.ev_exec[slot], 0) == cudaSuccess
-             && cudaMemcpyAsync(X.pin_out[slot], X.dout[slot], outb, cudaMemcpyDeviceToHost, X.s_copy) == cudaSuccess
-             && cudaEventRecord(X.ev_d2h[slot], X.s_copy) == cudaSuccess;
+        double *dst = out_dev ? out_dev + ch[c].base : (double *)X.dout[slot];
+        if (ok && (r = execute_plan(P, dst, st))) { fail(c, r, cintgpu_last_error()); break; }
+        ok = ok && cudaEventRecord(X.ev_exec[slot], st) == cudaSuccess;
+        if (!out_dev)
+            ok = ok && cudaStreamWaitEvent(X.s_copy, X.ev_exec[slot], 0) == cudaSuccess
+                 && cudaMemcpyAsync(X.pin_out[slot], X.dout[slot], outb, cudaMemcpyDeviceToHost, X.s_copy) == cudaSuccess
+                 && cudaEventRecord(X.ev_d2h[slot], X.s_copy) == cudaSuccess;
         if (!ok) {
             fail(c, CINTGPU_ERR_CUDA, std::string("chunk enqueue failed: ") + cudaGetErrorString(cudaGetLastError()));
             break;
@@ -2771,6 +2784,28 @@ int cintgpu_screened_run(int kind, const int *pairs, const double *q, int64_t np
 {
     return screened_run(kind, pairs, q, npair, threshold, p_begin, p_end, atm, natm, bas, nbas, env,
                         dm_dev, vj_dev, vk_dev, grad_dev, galpha_dev, nquartets);
+}
+
+int cintgpu_batch_device(int kind, double *out_dev, const int *shls, int64_t n, const int *atm,
+                         int natm, const int *bas, int nbas, const double *env)
+{
+    if (kind == CINTGPU_J_BUILD || kind == CINTGPU_K_BUILD || kind == CINTGPU_JK_BUILD
+        || kind == CINTGPU_J_GRAD || kind == CINTGPU_J_GRAD_EXP) {
+        set_error("cintgpu_batch_device computes integral blocks; J, K and the gradient need a density");
+        return CINTGPU_ERR_ARG;
+    }
+    const int mode_comp = (kind == CINTGPU_INT2E_SPH || kind == CINTGPU_INT2E_CART || kind == CINTGPU_INT3C2E_SPH
+                           || kind == CINTGPU_INT3C2E_CART || kind == CINTGPU_INT2C2E_SPH
+                           || kind == CINTGPU_INT2C2E_CART) ? 1 : 0;
+    if (!mode_comp) {
+        set_error("cintgpu_batch_device takes the one-component kinds (int2e, int3c2e, int2c2e)");
+        return CINTGPU_ERR_ARG;
+    }
+    if (!out_dev && n > 0) { set_error("null output"); return CINTGPU_ERR_ARG; }
+    if (n <= 0) return 0;
+    int rc = ensure_init();
+    if (rc) return rc;
+    return batch_host_pipelined(kind, nullptr, shls, n, atm, natm, bas, nbas, env, out_dev);
 }
 
 int cintgpu_batch_host(int kind, double *out_host, const int *shls, int64_t n,

@@ -7,8 +7,8 @@ batched int3c2e and int2c2e plans:
 The orbital and auxiliary shells live in one basis, as libcint's callers pass them to int3c2e_sph
 / int2c2e_sph (auxiliary shells after the orbital ones, src/cint3c2e.c:693-717,
 src/cint2c2e.c:351-358).  The three-centre integrals of every orbital shell pair i >= j with every
-auxiliary shell are computed once (plans over chunks of pairs, planned on host threads while the
-GPU runs earlier chunks) and stay in HBM in the plans' packed layout (blocks (di, dj, dP) back to
+auxiliary shell are computed once (the library's pipelined batch entry: chunk plans built on host
+threads while the GPU runs earlier chunks) and stay in HBM in the plans' packed layout (blocks (di, dj, dP) back to
 back, i fastest: pair p owns di dj naux doubles).  A J build is two passes of the library's DF
 kernels over that buffer (cintgpu_df_rho, cintgpu_df_j: per-pair descriptors only, no per-element
 index arrays, no atomics on J) around a triangular solve.  K uses the buffer scattered into a
@@ -19,8 +19,6 @@ The per-element formulation (packed_index, fit_weights, contract_rho, contract_j
 scatter-adds in torch) states the same contractions densely; the CPU tests check it against
 einsums over the oracle's full tensor and the GPU tests check the kernels against it.
 """
-import os
-
 import numpy as np
 
 from .molecules import shell_nsph as _nsph
@@ -142,14 +140,13 @@ def contract_k(Bt, dm):
 class DFCoulomb:
     """RI-J for one geometry: orbital shells 0..norb-1, auxiliary shells norb..nbas-1 of mol.
     pairs: orbital shell pairs (i >= j) to include (default: all).  chunk: (ij|P) triples per
-    int3c2e plan while the buffer is built."""
+    call of the batch entry while the buffer is built."""
 
-    def __init__(self, mol, norb, pairs=None, chunk=4_000_000):
+    def __init__(self, mol, norb, pairs=None, chunk=40_000_000):
         import ctypes
-        from concurrent.futures import ThreadPoolExecutor
 
         import torch
-        from . import INT2C2E_SPH, INT3C2E_SPH, Plan, _check, _ptr, lib
+        from . import INT2C2E_SPH, INT3C2E_SPH, Plan, _check, _ptr, batch_device, lib
         self.mol, self.norb = mol, norb
         nsph = _nsph(mol)
         loc = np.concatenate([[0], np.cumsum(nsph)])
@@ -174,29 +171,17 @@ class DFCoulomb:
         self._df = h
         size = int(L.cintgpu_df_size(h))
         self.T = torch.empty(max(size, 1), dtype=torch.float64, device='cuda')
-        # (ij|P) in chunks of whole pairs: chunk c's plan writes the segments of its pairs
+        # (ij|P) through the library's pipelined batch entry (chunk plans built on host threads
+        # while the GPU runs earlier chunks, reused device slots), in calls of whole pairs so the
+        # item list on the host stays bounded
         seg = nsph[pairs[:, 0]] * nsph[pairs[:, 1]] * self.naux
         start = np.concatenate([[0], np.cumsum(seg)])
         naux_sh = mol.nbas - norb
         per = max(1, chunk // max(naux_sh, 1))
-        bounds = [(a, min(a + per, len(pairs))) for a in range(0, len(pairs), per)]
-
-        def build(ab):
-            items3, _ = df_items(norb, mol.nbas, pairs[ab[0]:ab[1]])
-            return Plan(INT3C2E_SPH, mol, items3)
-        nth = max(1, min(12, (os.cpu_count() or 8) - 2, len(bounds)))   # ~1 GB of host memory per chunk plan
-        with ThreadPoolExecutor(nth) as pool:
-            futs = [pool.submit(build, ab) for ab in bounds[:nth]]
-            for c, (a, b) in enumerate(bounds):
-                p3 = futs[c].result()
-                if c + nth < len(bounds):
-                    futs.append(pool.submit(build, bounds[c + nth]))
-                n = int(start[b] - start[a])
-                if p3.output_size != n:
-                    raise ValueError('int3c2e plan size %d != segments %d' % (p3.output_size, n))
-                p3.execute(self.T.narrow(0, int(start[a]), n))
-                torch.cuda.synchronize()
-                p3.close()
+        for a in range(0, len(pairs), per):
+            b = min(a + per, len(pairs))
+            items3, _ = df_items(norb, mol.nbas, pairs[a:b])
+            batch_device(INT3C2E_SPH, mol, items3, self.T.narrow(0, int(start[a]), int(start[b] - start[a])))
         # the metric over auxiliary pairs P >= Q, mirrored into a dense matrix
         _, items2 = df_items(norb, mol.nbas, pairs[:0])
         p2 = Plan(INT2C2E_SPH, mol, items2)

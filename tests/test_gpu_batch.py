@@ -69,3 +69,28 @@ def test_batch_host_offsets_and_rejects_j(gpulib):
     assert_block_close(got, want, 'batch_host offsets')
     with pytest.raises(cg.CintGpuError):
         cg.batch_host(7, mol, qs)
+
+
+@pytest.mark.parametrize('kind,n', [('INT2E_SPH', 6000), ('INT3C2E_SPH', 30000), ('INT2C2E_CART', 3000)])
+def test_batch_device_matches_plan(gpulib, kind, n):
+    """cintgpu_batch_device (the host-buffer pipeline writing into a device buffer) gives one
+    device plan's output; a two-component kind is refused"""
+    import torch
+    cg = gpulib
+    k = getattr(cg, kind)
+    mol = M.config0(seed=6)
+    rng = np.random.RandomState(n)
+    nsh = {'INT2E_SPH': 4, 'INT3C2E_SPH': 3, 'INT2C2E_CART': 2}[kind]
+    if nsh == 4:
+        qs = M.unique_quartets(mol.nbas)
+        items = np.ascontiguousarray(qs[rng.choice(len(qs), n, replace=False)])
+    else:
+        items = np.stack([rng.randint(0, mol.nbas, n) for _ in range(nsh)], 1).astype(np.int32)
+    want = _plan_out(cg, k, mol, items)[0]
+    out = torch.full((want.size + 7,), 7.0, dtype=torch.float64, device='cuda')
+    cg.batch_device(k, mol, items, out)
+    got = out.cpu().numpy()
+    assert (got[want.size:] == 7.0).all()                  # nothing written past the blocks
+    assert_block_close(got[:want.size], want, 'batch_device %s' % kind)
+    with pytest.raises(cg.CintGpuError):
+        cg.batch_device(cg.INT2E_IP1_SPH, mol, items[:10] if nsh == 4 else M.unique_quartets(mol.nbas)[:10], out)
