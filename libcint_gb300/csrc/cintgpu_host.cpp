@@ -2430,10 +2430,10 @@ static int batch_host_pipelined(int kind, double *out_host, const int *shls, int
             if (c >= C) return;
             auto tb = clk::now();
             CINTGPUPlan *P = new CINTGPUPlan();
-            /* host-buffer int2e chunks are small: a separate output kernel on the chunk's stream
-             * beats transforms at the integral kernel's tail; two- and three-centre chunks written
-             * to device memory transform inside the integral kernel */
-            P->fuse_out = out_dev && kind_shells(kind) < 4;
+            /* chunks are small: a separate output kernel on the chunk's stream beats transforms at
+             * the integral kernel's tail (measured for int2e to host memory and int3c2e to device
+             * memory alike) */
+            P->fuse_out = false;
             int r = build_plan(P, kind, shls + nsh * ch[c].i0, ch[c].n, nullptr, atm, natm, bas, nbas, env, 0);
             us_build += (int64_t)(1e3 * since(tb));
             if (r) { fail(c, r, cintgpu_last_error()); delete P; return; }
