@@ -176,7 +176,7 @@ def _timed(fn, reps=3):
 
 
 def extra_dropin(cg, mol, qs, batched_value, n=4000):
-    """The plain drop-in on its own workload, configs[0]-style c0 (8 atoms, 6 A, s,s,p,p,d x 4
+    """The plain drop-in on its own workload, c0 (8 atoms, 6 A, s,s,p,p,d x 4
     primitives): one libcint-signature int2e_sph call per quartet from host buffers, without and
     with an int2e_optimizer (whose side table caches the shell pairs' primitive data), on the first
     n of its 336,610 unique quartets, from one host thread and from 4, 16 and all host threads at
