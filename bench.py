@@ -460,8 +460,8 @@ def extra_jk(cg, seed=0, natm=24):
 
 
 def hbm_peak_gbs():
-    """(GB/s, source): the driver's measured copy bandwidth when MEASURED_PEAKS.json is present,
-    else the fallback figure of an earlier GB300 measurement"""
+    """(GB/s, source): the measured copy bandwidth in MEASURED_PEAKS.json when that file is
+    present, else the fallback figure of an earlier GB300 measurement"""
     path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
     try:
         with open(path) as f:
