@@ -247,8 +247,6 @@ int cintgpu_df_create(CINTGPUDF **out, const int *pairs, int64_t npair, int nao,
     *out = nullptr;
     if (npair < 0 || (npair > 0 && !pairs) || nao < 1 || naux < 1)
         return df_fail("df: need npair >= 0 (with its descriptors), nao >= 1, naux >= 1");
-    int rc = cg_init();
-    if (rc) return rc;
     std::vector<int64_t> seg((size_t)std::max<int64_t>(npair, 1));
     std::vector<int4> desc((size_t)std::max<int64_t>(npair, 1));
     int64_t pos = 0;
@@ -266,6 +264,8 @@ int cintgpu_df_create(CINTGPUDF **out, const int *pairs, int64_t npair, int nao,
         pos += (int64_t)di * dj * naux;
         max_ab = std::max(max_ab, di * dj);
     }
+    int rc = cg_init();
+    if (rc) return rc;
     CINTGPUDF *h = new CINTGPUDF();
     h->npair = npair;
     h->naux = naux;

@@ -129,3 +129,25 @@ def test_cache_size_query_matches_libcint_live(gpulib, oracle, name, nsh):
             want = getattr(oracle.ref.lib, name)(None, None, P(s), P(mol.atm), mol.natm,
                                                  P(mol.bas), nb, P(mol.env), None, None)
             assert got == want, (name, s[:nsh].tolist(), got, want)
+
+
+def test_new_entries_reject_bad_arguments_before_the_device(gpulib):
+    """argument checks of the device-output batch and the density-fitting handle run before any
+    device work, so they answer the same with or without a GPU: a two-component kind, a J kind,
+    pair descriptors outside the AO range or above the AO-pair limit"""
+    L = gpulib.lib()
+    mol = M.config0(seed=0)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    q = np.ascontiguousarray(M.unique_quartets(mol.nbas)[:4], dtype=np.int32)
+    out = ctypes.c_void_p(16)   # never dereferenced: the checks fail first
+    for kind in (gpulib.INT2E_IP1_SPH, 7):      # a two-component kind; J_BUILD
+        rc = L.cintgpu_batch_device(kind, out, P(q), len(q), P(mol.atm), mol.natm, P(mol.bas),
+                                    mol.nbas, P(mol.env))
+        assert rc == -1 and gpulib.last_error()
+    h = ctypes.c_void_p()
+    for desc, nao in (([0, 0, 3, 3], 2), ([-1, 0, 1, 1], 4), ([0, 0, 80, 80], 200)):
+        d = np.array(desc, np.int32)
+        assert L.cintgpu_df_create(ctypes.byref(h), P(d), 1, nao, 10) == -1
+        assert 'df: pair 0' in gpulib.last_error() and not h.value
+    assert L.cintgpu_df_create(ctypes.byref(h), None, 1, 4, 10) == -1
+    assert L.cintgpu_df_create(ctypes.byref(h), None, 0, 0, 10) == -1
